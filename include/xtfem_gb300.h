@@ -1,0 +1,166 @@
+/*
+ * xtfem_gb300.h -- C ABI of the GB300 space-time solve library
+ * (xtfem_gb300/libxtfem_gb300.so).
+ *
+ * Drop-in for the iterative solve path of the XTFEM extended space-time
+ * finite-element code: the Kronecker operator apply, the ILUT-preconditioned
+ * restarted GMRES built on it, the per-Gauss-point fatigue-damage update and
+ * the element-deletion test.  Every entry point takes plain pointers and
+ * sizes.  Arrays are host memory owned by the caller unless the name says
+ * "_device".
+ *
+ * Conventions of the Fortran entry points (trailing underscore, gfortran
+ * name mangling): scalars by reference, CSR/MSR index arrays 1-based, q x q
+ * temporal matrices column-major, a space-time vector of length p*q holds
+ * temporal block i at [(i-1)*p, i*p).  They return nothing, as the
+ * reference's subroutines do; the last error is available from
+ * xt_last_error() and the status-returning xt_* variants.
+ *
+ * Status codes: 0 success; the GMRES codes 1 (maxits) and -1 (zero initial
+ * residual) as in the reference; negative codes <= -10 for library errors.
+ */
+#ifndef XTFEM_GB300_H
+#define XTFEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XT_OK 0
+#define XT_ERR_ARG (-10)
+#define XT_ERR_CUDA (-11)
+#define XT_ERR_ALLOC (-12)
+#define XT_ERR_NONFINITE (-13)
+#define XT_ERR_SINGULAR (-14)
+#define XT_ERR_STATE (-15)
+#define XT_ERR_TIMEOUT (-16)
+#define XT_ERR_HOST (-17)
+
+/* ------------------------------------------------------------ lifetime */
+
+/* Replaces kokkos_init_ (src/kokkos_host.cpp:14-20): selects device 0 and
+ * creates the library's stream. */
+void kokkos_init_(void);
+/* Replaces kokkos_finish_ (src/kokkos_host.cpp:22-24): frees every cached
+ * device object. */
+void kokkos_finish_(void);
+
+int xt_init(int device);
+int xt_finalize(void);
+/* Message of the last error on the calling thread ("" when none). */
+const char *xt_last_error(void);
+void xt_clear_error(void);
+const char *xt_version(void);
+
+/* Operator and factor caching of the Fortran entry points.  With caching
+ * off (default) every call uploads K, M and the factor.  With caching on,
+ * device copies are kept and reused for calls with the same array addresses
+ * and sizes; the caller must call xt_invalidate_() after changing K, M or
+ * the factor in place (after element deletion, reassembly or refactoring).
+ */
+void xt_set_cache_(const int *on);
+void xt_invalidate_(void);
+
+/* ------------------------------------- Fortran solver entry points */
+
+/* src/kronecker.f90:19-85  kronspmv: y = (A (x) K + B (x) M) x. */
+void kronspmv_(const double *a, const double *b, const int *q, const int *ki,
+               const int *kj, const double *kv, const int *mi, const int *mj,
+               const double *mv, const int *p, const double *x, double *y);
+
+/* src/kronecker.f90:88-127  kronspgemv: y = alpha (A(x)K + B(x)M) x + beta y. */
+void kronspgemv_(const double *a, const double *b, const double *alpha,
+                 const double *beta, const int *q, const int *ki, const int *kj,
+                 const double *kv, const int *mi, const int *mj,
+                 const double *mv, const int *p, const double *x, double *y);
+
+/* src/kronecker.f90:130-178  kronlusol: y = (A^-1 (x) (LU)^-1) x with the
+ * SPARSKIT MSR factor alu/jlu/ju of src/ilut.f:152-495. */
+void kronlusol_(const double *a, const int *q, const double *alu,
+                const int *jlu, const int *ju, const int *p, const double *x,
+                double *y);
+
+/* src/kronecker.f90:181-365  kronpgmres: solve (A(x)K + B(x)M) sol = rhs by
+ * ILUT-right-preconditioned GMRES(im), FP64, with the reference's restart,
+ * convergence (|rs(i+1)| <= eps ||r0||) and ierr conventions (0, 1, -1;
+ * library errors <= -10).  rhs is used as scratch as in the reference
+ * (its content on return is unspecified). iout is accepted and ignored. */
+void kronpgmres_(const double *a, const double *b, const int *q,
+                 const int *ki, const int *kj, const double *kv,
+                 const int *mi, const int *mj, const double *mv, const int *p,
+                 const double *alu, const int *jlu, const int *ju, double *rhs,
+                 double *sol, const int *im, const double *eps,
+                 const int *maxits, const int *iout, int *ierr);
+
+/* src/delelement.f90:109-136  chkelesta on the device: element i fails when
+ * one of its ngpe Gauss points has D >= Dc; gpsta/elesta set to 0 for it
+ * and nefail gets the 1-based failed elements in ascending order. */
+void chkelesta_(const int *nn, const int *ne, const int *nnse, const int *ngpe,
+                const double *Dc, const double *D, int *elesta, int *gpsta,
+                int *nef, int *nefail);
+
+/* ------------------------------------------------ damage entry point */
+
+/* src/kokkos_host.cpp:37-41  kokkos_host_, same signature and array
+ * layouts (scalars by value, arrays flattened as in
+ * src/kokkos_damage.f90:51-84).  Runs the two-scale fatigue-damage update
+ * of every Gauss point over nip temporal points on the GPU. */
+void kokkos_host_(int rank, int ne, int nn, int ndofn, int nnse, int nnte,
+                  int ngpe, int ncmp, int nip, int *nodes, double *Nx,
+                  double *Ny, double *Nz, double *Nt, double *sol, double *ym,
+                  double *nu, double *eps_old, double *eps_pl,
+                  double *sig_eff, double *sig_back, double *p, double *D,
+                  double *ws, double *del_po, double *sig_d);
+
+/* Status-returning form of kokkos_host_ (no rank argument). */
+int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
+              int ncmp, int nip, const int *nodes, const double *Nx,
+              const double *Ny, const double *Nz, const double *Nt,
+              const double *sol, const double *ym, const double *nu,
+              double *eps_old, double *eps_pl, double *sig_eff,
+              double *sig_back, double *p, double *D, double *ws,
+              double *del_po, double *sig_d);
+
+/* --------------------------------------------- handle-based interface */
+
+/* A device-resident space-time system: K and M (1-based CSR, order p), the
+ * temporal size q, an optional ILUT factor and the current A, B.  This is
+ * the form the Fortran entry points use internally; it lets a caller keep
+ * the operator on the GPU across slabs. */
+typedef struct xt_system_s *xt_system;
+
+int xt_system_create(int p, int q, const int *ki, const int *kj,
+                     const double *kv, const int *mi, const int *mj,
+                     const double *mv, xt_system *out);
+int xt_system_destroy(xt_system s);
+/* Factor in SPARSKIT MSR form (src/ilut.f:152-240).  group = rows per node
+ * for the level schedule (3 for three DOFs per node; 1 = row levels). */
+int xt_system_set_ilu(xt_system s, const double *alu, const int *jlu,
+                      const int *ju, int group);
+/* Temporal matrices A (with the slab-start jump) and B, q x q column-major. */
+int xt_system_set_temporal(xt_system s, const double *a, const double *b);
+/* kronspgemv semantics with explicit temporal matrices (host vectors,
+ * block layout). */
+int xt_system_apply(xt_system s, const double *a, const double *b,
+                    double alpha, double beta, const double *x, double *y);
+/* kronlusol semantics with the system's factor and temporal matrix a. */
+int xt_system_lusol(xt_system s, const double *a, const double *x, double *y);
+/* kronpgmres semantics (host vectors, block layout).  rhs is preserved.
+ * its/ierr/est may be NULL; hist (may be NULL) receives up to hist_len
+ * residual estimates |rs(i+1)|/||r0||. */
+int xt_system_gmres(xt_system s, const double *rhs, double *sol, int im,
+                    double eps, int maxits, int *its, int *ierr, double *est,
+                    double *hist, int hist_len);
+/* Solve to a true relative residual <= tol with FP64 residuals and
+ * solution; precision 0 runs FP64 GMRES cycles, 1 runs FP32 operator,
+ * factor and Krylov basis (FP64 dot products and Hessenberg) inside FP64
+ * iterative refinement.  out_stats (may be NULL) gets 6 values: iterations,
+ * cycles, refinement passes, ierr, true relative residual, last estimate. */
+int xt_system_solve(xt_system s, const double *rhs, double *sol, int im,
+                    double tol, int maxits, int precision, double inner_tol,
+                    double *out_stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,132 @@
+/*
+ * xtfem_gb300_host.h -- host-side set-up and the slab driver of the GB300
+ * library (same shared object as xtfem_gb300.h).
+ *
+ * The reference's Fortran driver (src/main3d.f90) assembles K and M,
+ * applies boundary conditions, factors K with ILUT and marches the
+ * space-time slabs.  These entry points provide the same steps to a C, C++
+ * or Python caller: the set-up runs on the host in FP64 (as in the
+ * reference); the slab loop keeps every per-slab vector on the GPU.
+ */
+#ifndef XTFEM_GB300_HOST_H
+#define XTFEM_GB300_HOST_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* --------------------------------------------------- problem set-up */
+typedef struct xth_problem_s *xth_problem;
+
+/* Mesh from the reference's .inp format (src/main3d.f90:212-231), or a
+ * structured rod of nx x ny x nz C3D8 elements over [0,lx]x[0,ly]x[0,lz]
+ * numbered like inp/prismaticrod-*.inp; then K, M and the per-Gauss-point
+ * strain rows for a uniform isotropic material (src/mpisubs.f90:69-139). */
+int xth_problem_from_inp(const char *path, double E, double nu, double rho,
+                         xth_problem *out);
+int xth_problem_rod(int nx, int ny, int nz, double lx, double ly, double lz,
+                    double E, double nu, double rho, xth_problem *out);
+int xth_problem_destroy(xth_problem pr);
+/* Current sizes (K changes after deletion surgery). */
+int xth_problem_sizes(xth_problem pr, int *nn, int *ne, int *nnz_k,
+                      int *nnz_m);
+int xth_problem_mesh(xth_problem pr, double *xyz, int *conn);
+/* Copies of the current 1-based CSR K and M (ia: 3nn+1, ja/a: nnz). */
+int xth_problem_k(xth_problem pr, int *ia, int *ja, double *a);
+int xth_problem_m(xth_problem pr, int *ia, int *ja, double *a);
+/* Strain rows Nx, Ny, Nz, 8 per Gauss point, 8 Gauss points per element. */
+int xth_problem_strain_rows(xth_problem pr, double *nx, double *ny,
+                            double *nz);
+/* Constitutive matrix (6x6 column-major) of the uniform material. */
+int xth_problem_stiffness(xth_problem pr, double *d);
+/* src/spmtx.f90:268-307 csrapplybc on K and M with a mask over the 3nn
+ * spatial DOFs (nonzero = fixed). */
+int xth_problem_apply_bc(xth_problem pr, const int *bc);
+/* Element deletion surgery of src/main3d.f90:634-687 for the failed
+ * elements nefail[0..nef) (1-based): K -= sum of their element stiffness
+ * (delelement, src/delelement.f90:1-59), node-element counts decremented
+ * (chkcnsta), disconnected nodes found (chkndsta) and given unit diagonals
+ * (adddiagonal), their DOFs added to the mask bc (3nn entries, updated in
+ * place), then csrapplybc on M and K.  ndf_out gets the number of newly
+ * disconnected nodes. */
+int xth_problem_delete(xth_problem pr, int nef, const int *nefail, int *bc,
+                       int *ndf_out);
+
+/* src/ilut.f:152-495 ILUT(lfil, droptol) in FP64; alu/jlu hold iwk entries,
+ * ju n entries; returns SPARSKIT's ierr (0 = success). */
+int xth_ilut(int n, const int *ia, const int *ja, const double *a, int lfil,
+             double droptol, int iwk, double *alu, int *jlu, int *ju);
+
+/* src/stcoeff.f90:62-356 (mechanical, 6x6) and 1-60 (thermal, 3x3),
+ * column-major. */
+void xth_stcoeff_m(double t1, double dt, double w, double *k, double *m,
+                   double *ktn, double *mtn, double *ktn1, double *mtn1);
+void xth_stcoeff_t(double dt, double *k, double *m, double *ktn, double *mtn,
+                   double *ktn1, double *mtn1);
+/* src/getfextc.f90:22-58 */
+void xth_getfextc_m(double t1, double w, double dt, double *fextc,
+                    double *fint);
+/* src/kokkos_damage.f90:36-47 temporal shape table Nt[jj*6+k]. */
+void xth_nt_table(int nip, const double *tcoorde, double w, double *nt);
+
+/* ------------------------------------------------------ slab driver */
+/* Mechanical slab loop of src/main3d.f90:609-937 without the thermal part:
+ * deletion check, load and jump terms, GMRES solve, damage update, all on
+ * the GPU with the slab state resident. */
+typedef struct xt_slab_config {
+    int clamp_axis;      /* nodes with x[clamp_axis] == clamp_value fixed */
+    double clamp_value;
+    int load_axis;       /* traction face x[load_axis] == load_value */
+    double load_value;
+    int load_comp;       /* force component 0,1,2 */
+    double amplitude;    /* traction amplitude (MPa) */
+    double area;         /* loaded area (mm^2) */
+    double freq;         /* load frequency (Hz) */
+    double dt0;          /* step time per cycle unit (s) */
+    int n1, n2;          /* cycles per slab before / after first deletion */
+    int nipc;            /* temporal damage points per cycle */
+    int lfil;            /* ILUT fill */
+    double droptol;      /* ILUT drop tolerance */
+    int im;              /* GMRES restart length */
+    double tol;          /* true relative residual target */
+    int maxits;          /* Arnoldi steps per slab at most */
+    int precision;       /* 0 FP64 GMRES, 1 FP32 inner + FP64 refinement */
+    double inner_tol;    /* relative tolerance of an FP32 inner solve */
+    double Dc;           /* critical damage */
+    int damage;          /* 1 = run the damage update */
+    int group;           /* rows per node in the ILU level schedule */
+} xt_slab_config;
+
+typedef struct xt_slab_s *xt_slab;
+
+int xt_slab_create(xth_problem pr, const xt_slab_config *cfg, xt_slab *out);
+int xt_slab_destroy(xt_slab s);
+/* One slab.  stats (may be NULL) receives 12 values: slab index, GMRES
+ * iterations, restart cycles, refinement passes, ierr, true relative
+ * residual, max D, failed elements so far, elements deleted this slab,
+ * plastic steps, screened elastic steps, exact steps. */
+int xt_slab_step(xt_slab s, double *stats);
+/* The same slab through host buffers: fext (block layout, p*6) replaces the
+ * slab's external load vector, and the slab's displacement (block layout,
+ * p*6) and damage (8 per element) are copied back. */
+int xt_slab_step_host(xt_slab s, const double *fext, double *disp, double *D,
+                      double *stats);
+/* Copies of the current state. */
+int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
+/* Per-kernel CUDA-event timing on the library stream: enable, then read
+ * count and total milliseconds per kernel class (0 Kronecker FP64,
+ * 1 Kronecker FP32, 2 ILU FP64, 3 ILU FP32, 4 damage). */
+int xt_profile(int enable);
+int xt_profile_read(int cls, long long *count, double *ms);
+/* Kernel launches issued by the library since load. */
+long long xt_launch_count(void);
+/* CUDA events on the library stream: record slot 0..7, elapsed ms a -> b
+ * (waits for b), and a synchronize of the library stream. */
+int xt_mark(int slot);
+double xt_elapsed_ms(int a, int b);
+int xt_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,427 @@
+"""Python interface of the GB300 space-time solve path.
+
+Mirrors the reference's Fortran subroutines for this path (names, argument
+meaning, 1-based CSR/MSR index arrays, column-major q x q temporal matrices,
+block-major space-time vectors) on top of the C ABI of libxtfem_gb300.so:
+
+    kronspmv, kronspgemv, kronlusol, kronpgmres   src/kronecker.f90
+    kokkos_host (damage update)                   src/kokkos_host.cpp
+    chkelesta (element deletion test)             src/delelement.f90
+    ilut                                          src/ilut.f
+    stcoeff_m, stcoeff_t, getfextc_m, nt_table    src/stcoeff.f90, getfextc.f90,
+                                                  src/kokkos_damage.f90
+
+plus the handle-based forms (SpaceTimeSystem, Problem, SlabSolver) that keep
+the operator and the slab state on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+from ._lib import XtError, check, dptr, dref, iptr, iref, lib
+
+__all__ = [
+    "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "chkelesta", "kokkos_host",
+    "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "nt_table", "SpaceTimeSystem",
+    "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
+]
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+@dataclass
+class Csr:
+    """1-based CSR matrix (the reference's ia/ja/a arrays)."""
+
+    ia: np.ndarray
+    ja: np.ndarray
+    a: np.ndarray
+
+    def __post_init__(self):
+        self.ia, self.ja, self.a = _i32(self.ia), _i32(self.ja), _f64(self.a)
+
+    @property
+    def n(self) -> int:
+        return len(self.ia) - 1
+
+    @property
+    def nnz(self) -> int:
+        return int(self.ia[-1] - 1)
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+
+        return sp.csr_matrix((self.a, self.ja - 1, self.ia - 1), shape=(self.n, self.n))
+
+
+def set_cache(on: bool) -> None:
+    """Keep device copies of K, M and factors across Fortran-style calls."""
+    lib().xt_set_cache_(iref(1 if on else 0))
+
+
+def invalidate() -> None:
+    lib().xt_invalidate_()
+
+
+def kronspmv(a, b, K: Csr, M: Csr, x):
+    """y = (A (x) K + B (x) M) x   (src/kronecker.f90:19-85)."""
+    return kronspgemv(a, b, 1.0, 0.0, K, M, x, None)
+
+
+def _colmajor(m):
+    m = np.asarray(m, dtype=np.float64)
+    return np.ascontiguousarray(m.reshape(-1, order="F")) if m.ndim == 2 else _f64(m)
+
+
+def kronspgemv(a, b, alpha, beta, K: Csr, M: Csr, x, y=None):
+    """y = alpha (A (x) K + B (x) M) x + beta y   (src/kronecker.f90:88-127).
+
+    a, b: q x q arrays (2-D, or flat column-major); x, y: length p*q,
+    temporal block i at [i*p, (i+1)*p).  Returns y (a new array when y is
+    None)."""
+    A, B = _colmajor(a), _colmajor(b)
+    q = int(round(np.sqrt(A.size)))
+    p = K.n
+    x = _f64(x)
+    out = np.zeros(p * q) if y is None else _f64(y).copy()
+    if x.size != p * q or out.size != p * q:
+        raise ValueError("x and y must have p*q entries")
+    lib().xt_clear_error()
+    lib().kronspgemv_(dptr(A), dptr(B), dref(alpha), dref(beta), iref(q), iptr(K.ia), iptr(K.ja),
+                      dptr(K.a), iptr(M.ia), iptr(M.ja), dptr(M.a), iref(p), dptr(x), dptr(out))
+    _raise_if_error()
+    return out
+
+
+def kronlusol(a, alu, jlu, ju, x):
+    """y = (A^-1 (x) (LU)^-1) x with the SPARSKIT MSR factor
+    (src/kronecker.f90:130-178)."""
+    A = _colmajor(a)
+    q = int(round(np.sqrt(A.size)))
+    alu, jlu, ju, x = _f64(alu), _i32(jlu), _i32(ju), _f64(x)
+    p = len(ju)
+    y = np.zeros(p * q)
+    lib().xt_clear_error()
+    lib().kronlusol_(dptr(A), iref(q), dptr(alu), iptr(jlu), iptr(ju), iref(p), dptr(x), dptr(y))
+    _raise_if_error()
+    return y
+
+
+def kronpgmres(a, b, K: Csr, M: Csr, alu, jlu, ju, rhs, sol=None, im=30, eps=1e-8, maxits=1000):
+    """Solve (A (x) K + B (x) M) sol = rhs by ILUT-preconditioned GMRES(im)
+    (src/kronecker.f90:181-365).  Returns (sol, ierr); rhs is not modified
+    here (the C entry point may clobber its own copy, as the reference)."""
+    A, B = _colmajor(a), _colmajor(b)
+    q = int(round(np.sqrt(A.size)))
+    p = K.n
+    r = _f64(rhs).copy()
+    s = np.zeros(p * q) if sol is None else _f64(sol).copy()
+    ierr = C.c_int(0)
+    lib().xt_clear_error()
+    lib().kronpgmres_(dptr(A), dptr(B), iref(q), iptr(K.ia), iptr(K.ja), dptr(K.a), iptr(M.ia),
+                      iptr(M.ja), dptr(M.a), iref(p), dptr(_f64(alu)), iptr(_i32(jlu)),
+                      iptr(_i32(ju)), dptr(r), dptr(s), iref(im), dref(eps), iref(maxits),
+                      iref(-1), C.byref(ierr))
+    if ierr.value <= -10:
+        _raise_if_error(force=True)
+    return s, ierr.value
+
+
+def chkelesta(ne, ngpe, Dc, D, elesta, gpsta):
+    """Element status test (src/delelement.f90:109-136) on the GPU.  Returns
+    (nef, nefail[:nef] 1-based); elesta and gpsta are updated in place."""
+    D = _f64(D)
+    if elesta.dtype != np.int32 or gpsta.dtype != np.int32:
+        raise TypeError("elesta and gpsta must be int32 arrays")
+    nefail = np.zeros(ne, np.int32)
+    nef = C.c_int(0)
+    lib().xt_clear_error()
+    lib().chkelesta_(iref(0), iref(ne), iref(8), iref(ngpe), dref(Dc), dptr(D), iptr(elesta),
+                     iptr(gpsta), C.byref(nef), iptr(nefail))
+    _raise_if_error()
+    return nef.value, nefail[: nef.value]
+
+
+def damage(ne, nn, nip, nodes, Nx, Ny, Nz, Nt, sol, ym, nu, state: dict, ndofn=3, nnse=8, nnte=3,
+           ngpe=8, ncmp=6):
+    """Two-scale damage update (src/kokkos_kernel.h:45-344) through the
+    status-returning form of kokkos_host_.  state holds eps_old, eps_pl,
+    sig_eff, sig_back (ngp*6) and p, D, ws, del_po, sig_d (ngp), updated in
+    place (float64 arrays)."""
+    keys = ["eps_old", "eps_pl", "sig_eff", "sig_back", "p", "D", "ws", "del_po", "sig_d"]
+    for k in keys:
+        if state[k].dtype != np.float64 or not state[k].flags.c_contiguous:
+            raise TypeError(f"state[{k!r}] must be a contiguous float64 array")
+    args = [_i32(nodes), _f64(Nx), _f64(Ny), _f64(Nz), _f64(Nt), _f64(sol), _f64(ym), _f64(nu)]
+    check(lib().xt_damage(ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, iptr(args[0]),
+                          *[dptr(a) for a in args[1:]], *[dptr(state[k]) for k in keys]),
+          "damage")
+    return state
+
+
+def kokkos_host(rank, ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, nodes, Nx, Ny, Nz, Nt, sol, ym,
+                nu, eps_old, eps_pl, sig_eff, sig_back, p, D, ws, del_po, sig_d):
+    """The reference's kokkos_host_ signature (src/kokkos_host.cpp:37-41)."""
+    lib().kokkos_host_(rank, ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, iptr(nodes), dptr(Nx),
+                       dptr(Ny), dptr(Nz), dptr(Nt), dptr(sol), dptr(ym), dptr(nu), dptr(eps_old),
+                       dptr(eps_pl), dptr(sig_eff), dptr(sig_back), dptr(p), dptr(D), dptr(ws),
+                       dptr(del_po), dptr(sig_d))
+    _raise_if_error()
+
+
+def ilut(A: Csr, lfil=20, droptol=1e-4):
+    """SPARSKIT ILUT on the host in FP64 (src/ilut.f:152-495).  Returns
+    (alu, jlu, ju) in MSR form with 1-based indices, trimmed to size."""
+    n = A.n
+    iwk = n * (2 * lfil + 2) + n + 2
+    alu = np.zeros(iwk)
+    jlu = np.zeros(iwk, np.int32)
+    ju = np.zeros(n, np.int32)
+    ierr = lib().xth_ilut(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk, dptr(alu),
+                          iptr(jlu), iptr(ju))
+    if ierr != 0:
+        raise XtError(f"ilut failed with ierr = {ierr}")
+    end = int(jlu[n]) - 1
+    return alu[:end].copy(), jlu[:end].copy(), ju
+
+
+def stcoeff_m(t1, dt, w):
+    """Mechanical temporal matrices (src/stcoeff.f90:62-356), each 6x6."""
+    mats = [np.zeros(36) for _ in range(6)]
+    lib().xth_stcoeff_m(t1, dt, w, *[dptr(m) for m in mats])
+    return [m.reshape(6, 6, order="F") for m in mats]
+
+
+def stcoeff_t(dt):
+    """Thermal temporal matrices (src/stcoeff.f90:1-60), each 3x3."""
+    mats = [np.zeros(9) for _ in range(6)]
+    lib().xth_stcoeff_t(dt, *[dptr(m) for m in mats])
+    return [m.reshape(3, 3, order="F") for m in mats]
+
+
+def getfextc_m(t1, w, dt):
+    f, g = np.zeros(6), np.zeros(6)
+    lib().xth_getfextc_m(t1, w, dt, dptr(f), dptr(g))
+    return f, g
+
+
+def nt_table(nip, tcoorde, w):
+    out = np.zeros(nip * 6)
+    lib().xth_nt_table(nip, dptr(_f64(tcoorde)), w, dptr(out))
+    return out
+
+
+def _raise_if_error(force=False):
+    """Raise when the last void (Fortran-style) entry point set an error."""
+    msg = lib().xt_last_error().decode(errors="replace")
+    if msg or force:
+        lib().xt_clear_error()
+        raise XtError(msg or "library error")
+
+
+class SpaceTimeSystem:
+    """Device-resident operator A (x) K + B (x) M with an ILUT factor."""
+
+    def __init__(self, K: Csr, M: Csr, q: int = 6):
+        self.K, self.M, self.q, self.p = K, M, q, K.n
+        h = C.c_void_p()
+        check(lib().xt_system_create(self.p, q, iptr(K.ia), iptr(K.ja), dptr(K.a), iptr(M.ia),
+                                     iptr(M.ja), dptr(M.a), C.byref(h)), "xt_system_create")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().xt_system_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def set_ilu(self, alu, jlu, ju, group=3):
+        self._f = (_f64(alu), _i32(jlu), _i32(ju))
+        check(lib().xt_system_set_ilu(self._h, dptr(self._f[0]), iptr(self._f[1]),
+                                      iptr(self._f[2]), group), "set_ilu")
+
+    def set_temporal(self, a, b):
+        check(lib().xt_system_set_temporal(self._h, dptr(_colmajor(a)), dptr(_colmajor(b))),
+              "set_temporal")
+
+    def apply(self, a, b, x, alpha=1.0, beta=0.0, y=None):
+        out = np.zeros(self.p * self.q) if y is None else _f64(y).copy()
+        check(lib().xt_system_apply(self._h, dptr(_colmajor(a)), dptr(_colmajor(b)), alpha, beta,
+                                    dptr(_f64(x)), dptr(out)), "apply")
+        return out
+
+    def lusol(self, a, x):
+        y = np.zeros(self.p * self.q)
+        check(lib().xt_system_lusol(self._h, dptr(_colmajor(a)), dptr(_f64(x)), dptr(y)), "lusol")
+        return y
+
+    def gmres(self, rhs, sol=None, im=30, eps=1e-8, maxits=1000, hist_len=0):
+        s = np.zeros(self.p * self.q) if sol is None else _f64(sol).copy()
+        its, ierr, est = C.c_int(0), C.c_int(0), C.c_double(0)
+        hist = np.zeros(max(hist_len, 1))
+        check(lib().xt_system_gmres(self._h, dptr(_f64(rhs)), dptr(s), im, eps, maxits,
+                                    C.byref(its), C.byref(ierr), C.byref(est), dptr(hist),
+                                    hist_len), "gmres")
+        return s, {"its": its.value, "ierr": ierr.value, "est": est.value,
+                   "hist": hist[: min(hist_len, its.value)]}
+
+    def solve(self, rhs, sol=None, im=30, tol=1e-8, maxits=2000, precision=0, inner_tol=1e-5):
+        s = np.zeros(self.p * self.q) if sol is None else _f64(sol).copy()
+        st = np.zeros(6)
+        check(lib().xt_system_solve(self._h, dptr(_f64(rhs)), dptr(s), im, tol, maxits, precision,
+                                    inner_tol, dptr(st)), "solve")
+        keys = ["its", "cycles", "outer", "ierr", "relres", "est"]
+        return s, {k: (int(v) if k in ("its", "cycles", "outer", "ierr") else float(v))
+                   for k, v in zip(keys, st)}
+
+
+class Problem:
+    """Mesh, assembled K and M and strain rows (host, FP64)."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_inp(cls, path, E=2.0e5, nu=0.3, rho=7.8e-9):
+        h = C.c_void_p()
+        check(lib().xth_problem_from_inp(str(path).encode(), E, nu, rho, C.byref(h)), "from_inp")
+        return cls(h)
+
+    @classmethod
+    def rod(cls, nx, ny, nz, lx=3.0, ly=1.0, lz=1.0, E=2.0e5, nu=0.3, rho=7.8e-9):
+        h = C.c_void_p()
+        check(lib().xth_problem_rod(nx, ny, nz, lx, ly, lz, E, nu, rho, C.byref(h)), "rod")
+        return cls(h)
+
+    def close(self):
+        if self._h:
+            lib().xth_problem_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def sizes(self):
+        v = [C.c_int(0) for _ in range(4)]
+        check(lib().xth_problem_sizes(self._h, *[C.byref(x) for x in v]), "sizes")
+        return tuple(x.value for x in v)
+
+    def mesh(self):
+        nn, ne, _, _ = self.sizes()
+        xyz, conn = np.zeros(nn * 3), np.zeros(ne * 8, np.int32)
+        check(lib().xth_problem_mesh(self._h, dptr(xyz), iptr(conn)), "mesh")
+        return xyz.reshape(nn, 3), conn.reshape(ne, 8)
+
+    def _csr(self, fn, nnz):
+        nn = self.sizes()[0]
+        ia, ja, a = np.zeros(3 * nn + 1, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+        check(fn(self._h, iptr(ia), iptr(ja), dptr(a)), "csr")
+        return Csr(ia, ja, a)
+
+    def K(self) -> Csr:
+        return self._csr(lib().xth_problem_k, self.sizes()[2])
+
+    def M(self) -> Csr:
+        return self._csr(lib().xth_problem_m, self.sizes()[3])
+
+    def strain_rows(self):
+        ne = self.sizes()[1]
+        out = [np.zeros(ne * 64) for _ in range(3)]
+        check(lib().xth_problem_strain_rows(self._h, *[dptr(o) for o in out]), "strain_rows")
+        return out
+
+    def apply_bc(self, bc):
+        check(lib().xth_problem_apply_bc(self._h, iptr(_i32(bc))), "apply_bc")
+
+    def delete(self, nefail, bc):
+        """Element-deletion surgery; bc (int32, 3nn) is updated in place."""
+        if bc.dtype != np.int32:
+            raise TypeError("bc must be int32")
+        nef = _i32(nefail)
+        ndf = C.c_int(0)
+        check(lib().xth_problem_delete(self._h, len(nef), iptr(nef), iptr(bc), C.byref(ndf)),
+              "delete")
+        return ndf.value
+
+
+class SlabConfig(C.Structure):
+    """xt_slab_config of include/xtfem_gb300_host.h."""
+
+    _fields_ = [("clamp_axis", C.c_int), ("clamp_value", C.c_double), ("load_axis", C.c_int),
+                ("load_value", C.c_double), ("load_comp", C.c_int), ("amplitude", C.c_double),
+                ("area", C.c_double), ("freq", C.c_double), ("dt0", C.c_double), ("n1", C.c_int),
+                ("n2", C.c_int), ("nipc", C.c_int), ("lfil", C.c_int), ("droptol", C.c_double),
+                ("im", C.c_int), ("tol", C.c_double), ("maxits", C.c_int),
+                ("precision", C.c_int), ("inner_tol", C.c_double), ("Dc", C.c_double),
+                ("damage", C.c_int), ("group", C.c_int)]
+
+    @classmethod
+    def make(cls, **kw):
+        d = dict(clamp_axis=0, clamp_value=0.0, load_axis=0, load_value=3.0, load_comp=0,
+                 amplitude=100.0, area=1.0, freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256,
+                 lfil=20, droptol=1e-4, im=30, tol=1e-8, maxits=3000, precision=0,
+                 inner_tol=1e-5, Dc=0.99, damage=1, group=3)
+        d.update(kw)
+        return cls(**d)
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_}
+
+
+STAT_KEYS = ["slab", "its", "cycles", "outer", "ierr", "relres", "maxD", "nfailed", "deleted",
+             "plastic_steps", "screened_steps", "exact_steps"]
+
+
+class SlabSolver:
+    """The mechanical slab loop with its state on the GPU."""
+
+    def __init__(self, problem: Problem, cfg: SlabConfig):
+        self.problem, self.cfg = problem, cfg
+        h = C.c_void_p()
+        check(lib().xt_slab_create(problem._h, C.byref(cfg), C.byref(h)), "xt_slab_create")
+        self._h = h
+        nn, ne, _, _ = problem.sizes()
+        self.p, self.ne, self.ngp = 3 * nn, ne, 8 * ne
+
+    def close(self):
+        if self._h:
+            lib().xt_slab_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def step(self):
+        st = np.zeros(12)
+        check(lib().xt_slab_step(self._h, dptr(st)), "xt_slab_step")
+        return dict(zip(STAT_KEYS, st.tolist()))
+
+    def step_host(self, fext, disp_out, D_out):
+        st = np.zeros(12)
+        check(lib().xt_slab_step_host(self._h, dptr(fext), dptr(disp_out), dptr(D_out), dptr(st)),
+              "xt_slab_step_host")
+        return dict(zip(STAT_KEYS, st.tolist()))
+
+    def state(self):
+        disp, D, ws = np.zeros(self.p * 6), np.zeros(self.ngp), np.zeros(self.ngp)
+        el = np.zeros(self.ne, np.int32)
+        check(lib().xt_slab_get(self._h, dptr(disp), dptr(D), dptr(ws), iptr(el)), "xt_slab_get")
+        return {"disp": disp, "D": D, "ws": ws, "elesta": el}
+
+
+def profile(enable: bool) -> None:
+    check(lib().xt_profile(1 if enable else 0), "xt_profile")
+
+
+def profile_read(cls: int):
+    n, ms = C.c_longlong(0), C.c_double(0)
+    check(lib().xt_profile_read(cls, C.byref(n), C.byref(ms)), "xt_profile_read")
+    return n.value, ms.value

@@ -1,0 +1,451 @@
+// abi.cpp -- the C ABI of the library (include/xtfem_gb300.h).
+//
+// The Fortran entry points mirror the reference's subroutines
+// (src/kronecker.f90, src/delelement.f90, src/kokkos_host.cpp) argument for
+// argument; host arrays in the reference's block layout are converted to the
+// device's interleaved layout on the way in and back on the way out.
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <tuple>
+
+#include "../../include/xtfem_gb300.h"
+#include "solver.h"
+
+using namespace xt;
+
+struct xt_system_s {
+    System sys;
+    DBuf<double> blk;   // block-layout staging, p*q
+    DBuf<double> a_in, b_in;  // q x q staging
+};
+
+namespace {
+
+// ------------------------------------------------------------ caching
+bool g_cache = false;
+using OpKey = std::tuple<const void*, const void*, const void*, const void*, const void*,
+                         const void*, int, int, int, int>;
+using IluKey = std::tuple<const void*, const void*, const void*, int, int>;
+std::map<OpKey, std::unique_ptr<xt_system_s>> g_ops;
+std::map<IluKey, std::shared_ptr<DevIlu>> g_ilus;
+
+int to_status(int s) { return s; }
+
+int upload_blocks(xt_system_s& h, const double* host, double* dev_itl)
+{
+    System& S = h.sys;
+    cudaStream_t s = ctx().stream;
+    const size_t n = (size_t)S.p * S.q;
+    XT_TRY(h.blk.alloc(n));
+    XT_CUDA(cudaMemcpyAsync(h.blk.p, host, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    XT_TRY((to_interleaved<double, double>(h.blk.p, dev_itl, S.p, S.q, s)));
+    return XT_OK;
+}
+
+int download_blocks(xt_system_s& h, const double* dev_itl, double* host)
+{
+    System& S = h.sys;
+    cudaStream_t s = ctx().stream;
+    const size_t n = (size_t)S.p * S.q;
+    XT_TRY(h.blk.alloc(n));
+    XT_TRY((to_blocks<double, double>(dev_itl, h.blk.p, S.p, S.q, s)));
+    XT_CUDA(cudaMemcpyAsync(host, h.blk.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+int ensure_vec(DBuf<double>& d, size_t n) { return d.alloc(n); }
+
+// Fetch (or build) the system for a Fortran call.  With caching off the
+// returned object is owned by `tmp` and dies with the call.
+int get_system(const int* ki, const int* kj, const double* kv, const int* mi, const int* mj,
+               const double* mv, int p, int q, std::unique_ptr<xt_system_s>& tmp,
+               xt_system_s*& out)
+{
+    XT_TRY(ensure_init());
+    if (p <= 0 || q < 1 || q > 8 || !ki || !kj || !kv || !mi || !mj || !mv) {
+        set_error("invalid operator arguments (need p > 0, 1 <= q <= 8, non-null arrays)");
+        return XT_ERR_ARG;
+    }
+    const int nk = ki[p] - 1, nm = mi[p] - 1;
+    if (g_cache) {
+        OpKey key{ki, kj, kv, mi, mj, mv, p, q, nk, nm};
+        auto it = g_ops.find(key);
+        if (it != g_ops.end()) { out = it->second.get(); return XT_OK; }
+        auto h = std::make_unique<xt_system_s>();
+        XT_TRY(system_create(h->sys, p, q, ki, kj, kv, mi, mj, mv));
+        out = h.get();
+        g_ops[key] = std::move(h);
+        return XT_OK;
+    }
+    tmp = std::make_unique<xt_system_s>();
+    XT_TRY(system_create(tmp->sys, p, q, ki, kj, kv, mi, mj, mv));
+    out = tmp.get();
+    return XT_OK;
+}
+
+int get_ilu(const double* alu, const int* jlu, const int* ju, int p, std::shared_ptr<DevIlu>& out)
+{
+    if (!alu || !jlu || !ju || p <= 0) {
+        set_error("invalid factor arguments");
+        return XT_ERR_ARG;
+    }
+    const int nz = jlu[p] - 1;
+    const int group = (p % 3 == 0) ? 3 : 1;
+    if (g_cache) {
+        IluKey key{alu, jlu, ju, p, nz};
+        auto it = g_ilus.find(key);
+        if (it != g_ilus.end()) { out = it->second; return XT_OK; }
+    }
+    auto f = std::make_shared<DevIlu>();
+    XT_TRY(build_ilu(*f, p, alu, jlu, ju, group, ctx().stream));
+    if (g_cache) g_ilus[IluKey{alu, jlu, ju, p, nz}] = f;
+    out = f;
+    return XT_OK;
+}
+
+int do_spmv(const double* a, const double* b, double alpha, double beta, int q, const int* ki,
+            const int* kj, const double* kv, const int* mi, const int* mj, const double* mv,
+            int p, const double* x, double* y)
+{
+    std::unique_ptr<xt_system_s> tmp;
+    xt_system_s* h = nullptr;
+    XT_TRY(get_system(ki, kj, kv, mi, mj, mv, p, q, tmp, h));
+    return xt_system_apply(h, a, b, alpha, beta, x, y);
+}
+
+// A system without K and M for kronlusol_: only the factor and the
+// temporal inverse are needed.
+struct LuOnly {
+    System sys;
+    DBuf<double> blk;
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* xt_last_error(void) { return last_error(); }
+void xt_clear_error(void) { set_error(""); }
+const char* xt_version(void) { return "xtfem_gb300 0.1"; }
+
+int xt_init(int device) { return ensure_init(device); }
+
+int xt_finalize(void)
+{
+    g_ops.clear();
+    g_ilus.clear();
+    Context& c = ctx();
+    if (c.ready) {
+        cudaStreamSynchronize(c.stream);
+        cudaStreamDestroy(c.stream);
+        c.stream = nullptr;
+        c.ready = false;
+    }
+    return XT_OK;
+}
+
+void kokkos_init_(void) { (void)ensure_init(0); }
+void kokkos_finish_(void) { (void)xt_finalize(); }
+
+void xt_set_cache_(const int* on)
+{
+    g_cache = on && *on;
+    if (!g_cache) {
+        g_ops.clear();
+        g_ilus.clear();
+    }
+}
+
+void xt_invalidate_(void)
+{
+    g_ops.clear();
+    g_ilus.clear();
+}
+
+// ------------------------------------------------------- handle API
+int xt_system_create(int p, int q, const int* ki, const int* kj, const double* kv,
+                     const int* mi, const int* mj, const double* mv, xt_system* out)
+{
+    if (!out) { set_error("xt_system_create: null output"); return XT_ERR_ARG; }
+    *out = nullptr;
+    if (!ki || !kj || !kv || !mi || !mj || !mv) {
+        set_error("xt_system_create: null array");
+        return XT_ERR_ARG;
+    }
+    auto h = std::make_unique<xt_system_s>();
+    XT_TRY(system_create(h->sys, p, q, ki, kj, kv, mi, mj, mv));
+    *out = h.release();
+    return XT_OK;
+}
+
+int xt_system_destroy(xt_system s)
+{
+    delete s;
+    return XT_OK;
+}
+
+int xt_system_set_ilu(xt_system s, const double* alu, const int* jlu, const int* ju, int group)
+{
+    if (!s || !alu || !jlu || !ju) { set_error("xt_system_set_ilu: null argument"); return XT_ERR_ARG; }
+    return system_set_ilu(s->sys, alu, jlu, ju, group);
+}
+
+int xt_system_set_temporal(xt_system s, const double* a, const double* b)
+{
+    if (!s || !a || !b) { set_error("xt_system_set_temporal: null argument"); return XT_ERR_ARG; }
+    return system_set_temporal(s->sys, a, b);
+}
+
+int xt_system_apply(xt_system h, const double* a, const double* b, double alpha, double beta,
+                    const double* x, double* y)
+{
+    if (!h || !a || !b || !x || !y) { set_error("xt_system_apply: null argument"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    cudaStream_t s = ctx().stream;
+    const int q = S.q;
+    const size_t n = (size_t)S.p * q;
+    XT_TRY(h->a_in.alloc(64));
+    XT_TRY(h->b_in.alloc(64));
+    XT_CUDA(cudaMemcpyAsync(h->a_in.p, a, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaMemcpyAsync(h->b_in.p, b, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_TRY(ensure_vec(S.x64, n));
+    XT_TRY(ensure_vec(S.r64, n));
+    XT_TRY(upload_blocks(*h, x, S.x64.p));
+    if (beta != 0.0) XT_TRY(upload_blocks(*h, y, S.r64.p));
+    XT_TRY(system_apply_with(S, h->a_in.p, h->b_in.p, alpha, beta, S.x64.p, S.r64.p));
+    return download_blocks(*h, S.r64.p, y);
+}
+
+int xt_system_lusol(xt_system h, const double* a, const double* x, double* y)
+{
+    if (!h || !a || !x || !y) { set_error("xt_system_lusol: null argument"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    if (!S.ilu) { set_error("xt_system_lusol: no factor set"); return XT_ERR_STATE; }
+    const int q = S.q;
+    const size_t n = (size_t)S.p * q;
+    std::vector<double> ainv(q * q);
+    XT_TRY(invert_small(q, a, ainv.data()));
+    cudaStream_t s = ctx().stream;
+    XT_CUDA(cudaMemcpyAsync(S.Ainv.p, ainv.data(), sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_TRY(ensure_vec(S.x64, n));
+    XT_TRY(ensure_vec(S.r64, n));
+    XT_TRY(ensure_vec(S.w64, n));
+    XT_TRY(upload_blocks(*h, x, S.x64.p));
+    XT_TRY(ilu_apply<double>(*S.ilu, q, S.Ainv.p, S.x64.p, S.r64.p, S.w64.p, s));
+    XT_TRY(download_blocks(*h, S.r64.p, y));
+    if (!S.hAinv.empty())  // restore the solver's temporal inverse
+        XT_CUDA(cudaMemcpyAsync(S.Ainv.p, S.hAinv.data(), sizeof(double) * q * q,
+                                cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+int xt_system_gmres(xt_system h, const double* rhs, double* sol, int im, double eps, int maxits,
+                    int* its, int* ierr, double* est, double* hist, int hist_len)
+{
+    if (!h || !rhs || !sol) { set_error("xt_system_gmres: null argument"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    const size_t n = (size_t)S.p * S.q;
+    XT_TRY(ensure_vec(S.b64, n));
+    XT_TRY(ensure_vec(S.x64, n));
+    XT_TRY(upload_blocks(*h, rhs, S.b64.p));
+    XT_TRY(upload_blocks(*h, sol, S.x64.p));
+    GmresStats st;
+    std::vector<double> hv;
+    XT_TRY(gmres_fp64(S, S.b64.p, S.x64.p, im, eps, maxits, st, hist ? &hv : nullptr));
+    XT_TRY(download_blocks(*h, S.x64.p, sol));
+    if (its) *its = st.its;
+    if (ierr) *ierr = st.ierr;
+    if (est) *est = st.est;
+    if (hist)
+        for (int k = 0; k < hist_len && k < (int)hv.size(); ++k) hist[k] = hv[k];
+    return XT_OK;
+}
+
+int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double tol, int maxits,
+                    int precision, double inner_tol, double* out_stats)
+{
+    if (!h || !rhs || !sol) { set_error("xt_system_solve: null argument"); return XT_ERR_ARG; }
+    if (precision != 0 && precision != 1) { set_error("xt_system_solve: precision is 0 or 1"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    const size_t n = (size_t)S.p * S.q;
+    XT_TRY(ensure_vec(S.b64, n));
+    XT_TRY(ensure_vec(S.x64, n));
+    XT_TRY(upload_blocks(*h, rhs, S.b64.p));
+    XT_TRY(upload_blocks(*h, sol, S.x64.p));
+    GmresStats st;
+    XT_TRY(solve_refined(S, S.b64.p, S.x64.p, im, tol, maxits, precision, inner_tol, st));
+    XT_TRY(download_blocks(*h, S.x64.p, sol));
+    if (out_stats) {
+        out_stats[0] = st.its;
+        out_stats[1] = st.cycles;
+        out_stats[2] = st.outer;
+        out_stats[3] = st.ierr;
+        out_stats[4] = st.relres;
+        out_stats[5] = st.est;
+    }
+    return XT_OK;
+}
+
+// ------------------------------------------------- Fortran entry points
+void kronspmv_(const double* a, const double* b, const int* q, const int* ki, const int* kj,
+               const double* kv, const int* mi, const int* mj, const double* mv, const int* p,
+               const double* x, double* y)
+{
+    (void)do_spmv(a, b, 1.0, 0.0, *q, ki, kj, kv, mi, mj, mv, *p, x, y);
+}
+
+void kronspgemv_(const double* a, const double* b, const double* alpha, const double* beta,
+                 const int* q, const int* ki, const int* kj, const double* kv, const int* mi,
+                 const int* mj, const double* mv, const int* p, const double* x, double* y)
+{
+    (void)do_spmv(a, b, *alpha, *beta, *q, ki, kj, kv, mi, mj, mv, *p, x, y);
+}
+
+void kronlusol_(const double* a, const int* q, const double* alu, const int* jlu, const int* ju,
+                const int* p, const double* x, double* y)
+{
+    if (ensure_init() != XT_OK) return;
+    if (!q || !p || *q < 1 || *q > 8 || *p <= 0) { set_error("kronlusol_: bad sizes"); return; }
+    xt_system_s h;
+    h.sys.p = *p;
+    h.sys.q = *q;
+    if (h.sys.A.alloc(64) != XT_OK || h.sys.Ainv.alloc(64) != XT_OK) return;
+    if (get_ilu(alu, jlu, ju, *p, h.sys.ilu) != XT_OK) return;
+    (void)xt_system_lusol(&h, a, x, y);
+}
+
+void kronpgmres_(const double* a, const double* b, const int* q, const int* ki, const int* kj,
+                 const double* kv, const int* mi, const int* mj, const double* mv, const int* p,
+                 const double* alu, const int* jlu, const int* ju, double* rhs, double* sol,
+                 const int* im, const double* eps, const int* maxits, const int* iout, int* ierr)
+{
+    (void)iout;
+    if (!ierr) return;
+    *ierr = XT_ERR_ARG;
+    if (!q || !p || !im || !eps || !maxits) { set_error("kronpgmres_: null argument"); return; }
+    std::unique_ptr<xt_system_s> tmp;
+    xt_system_s* h = nullptr;
+    int st = get_system(ki, kj, kv, mi, mj, mv, *p, *q, tmp, h);
+    if (st != XT_OK) { *ierr = st; return; }
+    st = get_ilu(alu, jlu, ju, *p, h->sys.ilu);
+    if (st != XT_OK) { *ierr = st; return; }
+    st = system_set_temporal(h->sys, a, b);
+    if (st != XT_OK) { *ierr = st; return; }
+    int its = 0, e = 0;
+    st = xt_system_gmres(h, rhs, sol, *im, *eps, *maxits, &its, &e, nullptr, nullptr, 0);
+    *ierr = (st != XT_OK) ? st : e;
+}
+
+void chkelesta_(const int* nn, const int* ne, const int* nnse, const int* ngpe, const double* Dc,
+                const double* D, int* elesta, int* gpsta, int* nef, int* nefail)
+{
+    (void)nn;
+    (void)nnse;
+    if (!ne || !ngpe || !Dc || !D || !elesta || !gpsta || !nef || !nefail) return;
+    if (ensure_init() != XT_OK) return;
+    const int E = *ne, G = *ngpe;
+    if (E <= 0 || G <= 0) { *nef = 0; return; }
+    cudaStream_t s = ctx().stream;
+    DBuf<double> dD;
+    DBuf<int> de, dg, df, dn;
+    if (dD.upload(D, (size_t)E * G, s) || de.upload(elesta, E, s) || dg.upload(gpsta, (size_t)E * G, s) ||
+        df.alloc(E) || dn.alloc(1))
+        return;
+    if (chkelesta_device(E, G, *Dc, dD.p, de.p, dg.p, df.p, dn.p, s) != XT_OK) return;
+    cudaMemcpyAsync(elesta, de.p, sizeof(int) * E, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(gpsta, dg.p, sizeof(int) * (size_t)E * G, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(nefail, df.p, sizeof(int) * E, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(nef, dn.p, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+}
+
+int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, int ncmp, int nip,
+              const int* nodes, const double* Nx, const double* Ny, const double* Nz,
+              const double* Nt, const double* sol, const double* ym, const double* nu,
+              double* eps_old, double* eps_pl, double* sig_eff, double* sig_back, double* p,
+              double* D, double* ws, double* del_po, double* sig_d)
+{
+    XT_TRY(ensure_init());
+    if (ne <= 0 || nn <= 0 || ngpe <= 0 || nip < 0 || !nodes || !Nx || !Ny || !Nz || !Nt || !sol ||
+        !ym || !nu || !eps_old || !eps_pl || !sig_eff || !sig_back || !p || !D || !ws ||
+        !del_po || !sig_d) {
+        set_error("xt_damage: bad arguments");
+        return XT_ERR_ARG;
+    }
+    if (ndofn != 3 || nnte != 3 || ncmp != 6 || nnse < 1 || nnse > 8) {
+        set_error("xt_damage: the C3D8 update needs ndofn=3, nnte=3, ncmp=6, nnse<=8");
+        return XT_ERR_ARG;
+    }
+    const size_t ngp = (size_t)ngpe * ne;
+    for (size_t i = 0; i < ngp * nnse; ++i)
+        if (nodes[i] < 1 || nodes[i] > nn) {
+            set_error("xt_damage: node id out of range");
+            return XT_ERR_ARG;
+        }
+    cudaStream_t s = ctx().stream;
+    DBuf<int> dnodes;
+    DBuf<double> dNx, dNy, dNz, dNt, dsol, dym, dnu, deo, dep, dse, dsb, dp, dD, dws, ddp, dsd;
+    DBuf<float> dNt32, ntmax;
+    const size_t nsol = (size_t)2 * nnte * nn * ndofn, nnt = (size_t)2 * nnte * nip;
+    XT_TRY(dnodes.upload(nodes, ngp * nnse, s));
+    XT_TRY(dNx.upload(Nx, ngp * nnse, s));
+    XT_TRY(dNy.upload(Ny, ngp * nnse, s));
+    XT_TRY(dNz.upload(Nz, ngp * nnse, s));
+    XT_TRY(dNt.upload(Nt, nnt ? nnt : 1, s));
+    XT_TRY(dNt32.alloc(nnt ? nnt : 1));
+    XT_TRY(ntmax.alloc(8));
+    XT_TRY(to_f32(dNt.p, dNt32.p, nnt, s));
+    XT_TRY(dsol.upload(sol, nsol, s));
+    XT_TRY(dym.upload(ym, ngp, s));
+    XT_TRY(dnu.upload(nu, ngp, s));
+    XT_TRY(deo.upload(eps_old, ngp * ncmp, s));
+    XT_TRY(dep.upload(eps_pl, ngp * ncmp, s));
+    XT_TRY(dse.upload(sig_eff, ngp * ncmp, s));
+    XT_TRY(dsb.upload(sig_back, ngp * ncmp, s));
+    XT_TRY(dp.upload(p, ngp, s));
+    XT_TRY(dD.upload(D, ngp, s));
+    XT_TRY(dws.upload(ws, ngp, s));
+    XT_TRY(ddp.upload(del_po, ngp, s));
+    XT_TRY(dsd.upload(sig_d, ngp, s));
+    DamageArgs a{};
+    a.ngp = (int)ngp; a.nn = nn; a.ndofn = ndofn; a.nnse = nnse; a.nnte = nnte; a.ncmp = ncmp;
+    a.nip = nip;
+    a.nodes = dnodes.p; a.Nx = dNx.p; a.Ny = dNy.p; a.Nz = dNz.p; a.Nt = dNt.p; a.Nt32 = dNt32.p;
+    a.sol = dsol.p; a.ym = dym.p; a.nu = dnu.p;
+    a.eps_old = deo.p; a.eps_pl = dep.p; a.sig_eff = dse.p; a.sig_back = dsb.p;
+    a.p = dp.p; a.D = dD.p; a.ws = dws.p; a.del_po = ddp.p; a.sig_d = dsd.p;
+    a.gpsta = nullptr; a.counters = nullptr; a.ntmax = ntmax.p;
+    XT_TRY(damage_update(a, s));
+    auto back = [&](double* h, const DBuf<double>& d, size_t n) -> int {
+        XT_CUDA(cudaMemcpyAsync(h, d.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+        return XT_OK;
+    };
+    XT_TRY(back(eps_old, deo, ngp * ncmp));
+    XT_TRY(back(eps_pl, dep, ngp * ncmp));
+    XT_TRY(back(sig_eff, dse, ngp * ncmp));
+    XT_TRY(back(sig_back, dsb, ngp * ncmp));
+    XT_TRY(back(p, dp, ngp));
+    XT_TRY(back(D, dD, ngp));
+    XT_TRY(back(ws, dws, ngp));
+    XT_TRY(back(del_po, ddp, ngp));
+    XT_TRY(back(sig_d, dsd, ngp));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+void kokkos_host_(int rank, int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, int ncmp,
+                  int nip, int* nodes, double* Nx, double* Ny, double* Nz, double* Nt,
+                  double* sol, double* ym, double* nu, double* eps_old, double* eps_pl,
+                  double* sig_eff, double* sig_back, double* p, double* D, double* ws,
+                  double* del_po, double* sig_d)
+{
+    (void)rank;
+    (void)xt_damage(ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, nodes, Nx, Ny, Nz, Nt, sol, ym,
+                    nu, eps_old, eps_pl, sig_eff, sig_back, p, D, ws, del_po, sig_d);
+}
+
+}  // extern "C"

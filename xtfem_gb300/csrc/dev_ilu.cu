@@ -1,0 +1,311 @@
+// dev_ilu.cu -- the Kronecker ILUT preconditioner on the GPU.
+//
+// Applies z = (A^-1 (x) (LU)^-1) v, the operator of src/kronecker.f90:130-178
+// (kronlusol), whose spatial part is SPARSKIT lusol (src/ilut.f:2383-2432):
+// a forward sweep with the unit lower factor and a backward sweep with the
+// upper factor and inverted diagonal, for each of the q temporal blocks.
+//
+// The factor is computed on the host (ILUT, FP64) and arrives in MSR form.
+// Triangular solves are chains of dependent rows, so the work is organised
+// by level sets computed once per factor:
+//   * rows are grouped by node (g = 3 consecutive DOFs); a group's level is
+//     one more than the deepest other group it reads, and one warp solves
+//     the g rows of a group in sequence, which roughly halves the number of
+//     levels compared with single-row levels on C3D8 meshes;
+//   * all q right-hand sides of a row are solved together: lanes are split
+//     into q segments of S lanes, each segment walks the row's external
+//     nonzeros for one temporal block and reduces with shuffles;
+//   * the q x q mixing with A^-1 is applied to v on the fly while the
+//     forward sweep reads it (the mixing commutes with the spatial solve);
+//   * one thread block runs all levels of a sweep with a block barrier
+//     between levels; values solved earlier are read back from global
+//     memory (L2-resident) after the barrier.
+// The kernel is latency-bound (levels x barrier+gather latency), not
+// bandwidth-bound; batching independent systems fills the other SMs.
+#include <algorithm>
+#include <vector>
+
+#include "xt_device.h"
+
+namespace xt {
+
+namespace {
+
+constexpr int kMaxG = 3;
+
+struct TriHost {
+    int ngroups = 0, nlevels = 0, g = 1, maxw = 0;
+    std::vector<int> level_ptr, group_row0, ext_ptr, ext_col;
+    std::vector<double> ext_v, int_v, dinv;
+};
+
+// Level-schedule one triangle.  upper == false: rows' L parts
+// (jlu(i) .. ju(i)-1); upper == true: U parts (ju(i) .. jlu(i+1)-1).
+TriHost schedule(int n, const double* alu, const int* jlu, const int* ju, int g, bool upper)
+{
+    TriHost T;
+    T.g = g;
+    const int ng = n / g;
+    T.ngroups = ng;
+    std::vector<int> lev(ng, 0);
+    auto row_range = [&](int r, int& b, int& e) {  // 0-based positions into alu/jlu
+        if (!upper) { b = jlu[r] - 1; e = ju[r] - 1; }
+        else { b = ju[r] - 1; e = jlu[r + 1] - 1; }
+    };
+    int maxl = 0;
+    for (int s = 0; s < ng; ++s) {
+        const int G = upper ? ng - 1 - s : s;
+        int l = 0;
+        for (int ri = 0; ri < g; ++ri) {
+            int b, e;
+            row_range(G * g + ri, b, e);
+            for (int k = b; k < e; ++k) {
+                const int c = (jlu[k] - 1) / g;
+                if (c != G) l = std::max(l, lev[c] + 1);
+            }
+        }
+        lev[G] = l;
+        maxl = std::max(maxl, l);
+    }
+    T.nlevels = maxl + 1;
+    std::vector<int> cnt(T.nlevels + 1, 0);
+    for (int G = 0; G < ng; ++G) cnt[lev[G] + 1]++;
+    for (int l = 0; l < T.nlevels; ++l) {
+        cnt[l + 1] += cnt[l];
+        T.maxw = std::max(T.maxw, cnt[l + 1] - cnt[l]);
+    }
+    T.level_ptr = cnt;
+    std::vector<int> order(ng), pos(cnt.begin(), cnt.end() - 1);
+    for (int G = 0; G < ng; ++G) order[pos[lev[G]]++] = G;
+    T.group_row0.resize(ng);
+    T.ext_ptr.assign((size_t)ng * g + 1, 0);
+    T.int_v.assign((size_t)ng * g * g, 0.0);
+    if (upper) T.dinv.assign((size_t)ng * g, 0.0);
+    for (int i = 0; i < ng; ++i) {
+        const int G = order[i];
+        T.group_row0[i] = G * g;
+        for (int ri = 0; ri < g; ++ri) {
+            const int r = G * g + ri;
+            int b, e;
+            row_range(r, b, e);
+            for (int k = b; k < e; ++k) {
+                const int c = jlu[k] - 1;
+                if (c / g == G) {
+                    T.int_v[((size_t)i * g + ri) * g + (c - G * g)] += alu[k];
+                } else {
+                    T.ext_col.push_back(c);
+                    T.ext_v.push_back(alu[k]);
+                }
+            }
+            T.ext_ptr[(size_t)i * g + ri + 1] = (int)T.ext_col.size();
+            if (upper) T.dinv[(size_t)i * g + ri] = alu[r];
+        }
+    }
+    return T;
+}
+
+int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
+{
+    d.ngroups = h.ngroups;
+    d.nlevels = h.nlevels;
+    d.g = h.g;
+    d.max_level_groups = h.maxw;
+    XT_TRY(d.level_ptr.upload(h.level_ptr.data(), h.level_ptr.size(), s));
+    XT_TRY(d.group_row0.upload(h.group_row0.data(), h.group_row0.size(), s));
+    XT_TRY(d.ext_ptr.upload(h.ext_ptr.data(), h.ext_ptr.size(), s));
+    const size_t ne = h.ext_col.size();
+    if (ne) {
+        XT_TRY(d.ext_col.upload(h.ext_col.data(), ne, s));
+        XT_TRY(d.ext_v64.upload(h.ext_v.data(), ne, s));
+        std::vector<float> f(h.ext_v.begin(), h.ext_v.end());
+        XT_TRY(d.ext_v32.upload(f.data(), ne, s));
+        XT_CUDA(cudaStreamSynchronize(s));  // f goes out of scope
+    } else {
+        XT_TRY(d.ext_col.alloc(1));
+        XT_TRY(d.ext_v64.alloc(1));
+        XT_TRY(d.ext_v32.alloc(1));
+    }
+    XT_TRY(d.int_v64.upload(h.int_v.data(), h.int_v.size(), s));
+    {
+        std::vector<float> f(h.int_v.begin(), h.int_v.end());
+        XT_TRY(d.int_v32.upload(f.data(), f.size(), s));
+        XT_CUDA(cudaStreamSynchronize(s));
+    }
+    if (!h.dinv.empty()) {
+        XT_TRY(d.dinv64.upload(h.dinv.data(), h.dinv.size(), s));
+        std::vector<float> f(h.dinv.begin(), h.dinv.end());
+        XT_TRY(d.dinv32.upload(f.data(), f.size(), s));
+        XT_CUDA(cudaStreamSynchronize(s));
+    }
+    return XT_OK;
+}
+
+template <class T>
+struct TriView {
+    int nlevels, g;
+    const int *level_ptr, *group_row0, *ext_ptr, *ext_col;
+    const T *ext_v, *int_v, *dinv;
+};
+
+template <class T>
+TriView<T> view(const DevTri& d);
+template <>
+TriView<double> view<double>(const DevTri& d)
+{
+    return {d.nlevels, d.g, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+            d.ext_v64.p, d.int_v64.p, d.dinv64.p};
+}
+template <>
+TriView<float> view<float>(const DevTri& d)
+{
+    return {d.nlevels, d.g, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+            d.ext_v32.p, d.int_v32.p, d.dinv32.p};
+}
+
+// One sweep (forward when UPPER == false).  x is read and written by the
+// kernel itself, so it is accessed through plain (coherent) loads.  For the
+// forward sweep the right-hand side is v mixed with Ainv; for the backward
+// sweep it is x itself (the forward result) and the output goes to z.
+template <class T, int Q, int S, bool UPPER>
+__global__ void __launch_bounds__(1024, 1)
+k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v,
+            T* x, T* z)
+{
+    __shared__ T sAinv[Q * Q];
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sAinv[i] = (T)dAinv[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    const int nwarps = blockDim.x >> 5;
+    const int rhs = lane / S;
+    const int sub = lane % S;
+    const bool live = rhs < Q;
+    const int g = t.g;
+    for (int l = 0; l < t.nlevels; ++l) {
+        const int gb = t.level_ptr[l], ge = t.level_ptr[l + 1];
+        for (int gi = gb + warp; gi < ge; gi += nwarps) {
+            const int row0 = t.group_row0[gi];
+            T acc[kMaxG];
+#pragma unroll
+            for (int ri = 0; ri < kMaxG; ++ri) {
+                acc[ri] = T(0);
+                if (ri < g && live) {
+                    const int kb = t.ext_ptr[gi * g + ri], ke = t.ext_ptr[gi * g + ri + 1];
+                    for (int k = kb + sub; k < ke; k += S)
+                        acc[ri] = fma(t.ext_v[k], x[(size_t)t.ext_col[k] * Q + rhs], acc[ri]);
+                }
+            }
+#pragma unroll
+            for (int off = S / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int ri = 0; ri < kMaxG; ++ri)
+                    acc[ri] += __shfl_xor_sync(0xffffffffu, acc[ri], off);
+            if (live) {
+                T sol[kMaxG];
+                const T* iv = t.int_v + (size_t)gi * g * g;
+                for (int s = 0; s < g; ++s) {
+                    const int ri = UPPER ? g - 1 - s : s;
+                    const int r = row0 + ri;
+                    T b;
+                    if (!UPPER) {
+                        b = T(0);
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) b = fma(sAinv[j * Q + rhs], v[(size_t)r * Q + j], b);
+                    } else {
+                        b = x[(size_t)r * Q + rhs];
+                    }
+                    T val = b - acc[ri];
+                    if (!UPPER) {
+                        for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
+                    } else {
+                        for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
+                        val *= t.dinv[(size_t)gi * g + ri];
+                    }
+                    sol[ri] = val;
+                }
+                if (sub == 0)
+                    for (int ri = 0; ri < g; ++ri) {
+                        T* dst = UPPER ? z : x;
+                        dst[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                        if (UPPER && z != x) x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                    }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+template <class T, int Q>
+int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
+               cudaStream_t s)
+{
+    constexpr int S = (32 / Q) >= 32 ? 32 : ((32 / Q) >= 16 ? 16 : ((32 / Q) >= 8 ? 8 : ((32 / Q) >= 4 ? 4 : 2)));
+    k_tri_sweep<T, Q, S, false><<<1, 1024, 0, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    k_tri_sweep<T, Q, S, true><<<1, 1024, 0, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+}  // namespace
+
+int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju, int group,
+              cudaStream_t s)
+{
+    if (n <= 0 || !alu || !jlu || !ju) {
+        set_error("build_ilu: bad arguments");
+        return XT_ERR_ARG;
+    }
+    if (jlu[0] != n + 2) {
+        set_error("build_ilu: jlu(1) must be n+2 (SPARSKIT MSR layout)");
+        return XT_ERR_ARG;
+    }
+    const int nnz_end = jlu[n] - 1;
+    for (int i = 0; i < n; ++i) {
+        if (ju[i] < jlu[i] || ju[i] > jlu[i + 1] || jlu[i + 1] < jlu[i]) {
+            set_error("build_ilu: inconsistent MSR row pointers");
+            return XT_ERR_ARG;
+        }
+    }
+    for (int k = n + 1; k < nnz_end; ++k)
+        if (jlu[k] < 1 || jlu[k] > n) {
+            set_error("build_ilu: MSR column index out of range");
+            return XT_ERR_ARG;
+        }
+    int g = (group > 1 && n % group == 0 && group <= kMaxG) ? group : 1;
+    d.n = n;
+    TriHost L = schedule(n, alu, jlu, ju, g, false);
+    TriHost U = schedule(n, alu, jlu, ju, g, true);
+    XT_TRY(upload_tri(d.L, L, s));
+    XT_TRY(upload_tri(d.U, U, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+template <class T>
+int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* work,
+              cudaStream_t s)
+{
+    switch (q) {
+    case 1: return launch_tri<T, 1>(F, dAinv, v, z, work, s);
+    case 2: return launch_tri<T, 2>(F, dAinv, v, z, work, s);
+    case 3: return launch_tri<T, 3>(F, dAinv, v, z, work, s);
+    case 4: return launch_tri<T, 4>(F, dAinv, v, z, work, s);
+    case 5: return launch_tri<T, 5>(F, dAinv, v, z, work, s);
+    case 6: return launch_tri<T, 6>(F, dAinv, v, z, work, s);
+    case 7: return launch_tri<T, 7>(F, dAinv, v, z, work, s);
+    case 8: return launch_tri<T, 8>(F, dAinv, v, z, work, s);
+    default:
+        set_error("ilu_apply: 1 <= q <= 8");
+        return XT_ERR_ARG;
+    }
+}
+
+template int ilu_apply<double>(const DevIlu&, int, const double*, const double*, double*,
+                               double*, cudaStream_t);
+template int ilu_apply<float>(const DevIlu&, int, const double*, const float*, float*, float*,
+                              cudaStream_t);
+
+}  // namespace xt

@@ -1,0 +1,370 @@
+// dev_krylov.cu -- vector kernels of the restarted GMRES on the GPU.
+//
+// The reference orthogonalises each new Krylov vector with modified
+// Gram-Schmidt, one ddot + daxpy pair per basis vector (src/kronecker.f90:
+// 277-285), i.e. 2j dependent passes over n values at step j.  Here the
+// projection is classical Gram-Schmidt applied twice (CGS2), which is as
+// stable as MGS in exact terms and needs only four passes over the basis
+// per step with no dependency between the basis vectors inside a pass:
+//   h1 = V^T w ; w -= V h1 ; h2 = V^T w ; w -= V h2 ; ||w||.
+// Every dot product accumulates in FP64 whatever the storage type of the
+// basis, and reductions are two-stage with a fixed order so results are
+// bitwise repeatable run to run.
+#include "xt_device.h"
+
+namespace xt {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRowBlocks = 296;  // 2 per SM on a 148-152 SM part
+constexpr int kChunk = 8;        // basis vectors per block in a dot pass
+
+__device__ __forceinline__ double block_sum(double v, double* sh)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += sh[w];
+    return r;  // valid in thread 0
+}
+
+// partial[j * nb + b] = sum over block b's rows of V_j[r] * w[r]
+template <class TV>
+__global__ void k_multi_dot(const TV* __restrict__ V, size_t ld, int k, const TV* __restrict__ w,
+                            size_t n, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    const int j0 = blockIdx.y * kChunk;
+    const int nb = gridDim.x;
+    const size_t per = (n + nb - 1) / nb;
+    const size_t r0 = per * blockIdx.x, r1 = min(n, r0 + per);
+    double acc[kChunk];
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) acc[c] = 0.0;
+    for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const double wr = (double)w[r];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c)
+            if (j0 + c < k) acc[c] = fma((double)V[(size_t)(j0 + c) * ld + r], wr, acc[c]);
+    }
+    for (int c = 0; c < kChunk && j0 + c < k; ++c) {
+        const double s = block_sum(acc[c], sh);
+        if (threadIdx.x == 0) partial[(size_t)(j0 + c) * nb + blockIdx.x] = s;
+    }
+}
+
+// out[j] = sum_b partial[j * nb + b], one block per j, fixed order
+__global__ void k_finish(const double* __restrict__ partial, int nb, double* __restrict__ out,
+                         int accumulate)
+{
+    __shared__ double sh[32];
+    const int j = blockIdx.x;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += partial[(size_t)j * nb + b];
+    const double s = block_sum(v, sh);
+    if (threadIdx.x == 0) out[j] = accumulate ? out[j] + s : s;
+}
+
+// w[r] -= sum_j h[j] V_j[r]; optionally partial ||w||^2 per block
+template <class TV, bool NORM>
+__global__ void k_update(const TV* __restrict__ V, size_t ld, int k, const double* __restrict__ h,
+                         TV* __restrict__ w, size_t n, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    __shared__ double hs[512];
+    for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) hs[j] = h[j];
+    __syncthreads();
+    double nrm = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        double acc = (double)w[r];
+        for (int j = 0; j < k; ++j) {
+            const double hj = j < 512 ? hs[j] : h[j];
+            acc = fma(-hj, (double)V[(size_t)j * ld + r], acc);
+        }
+        const TV out = (TV)acc;
+        w[r] = out;
+        if (NORM) nrm = fma((double)out, (double)out, nrm);
+    }
+    if (NORM) {
+        const double s = block_sum(nrm, sh);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
+template <class TV, class TY>
+__global__ void k_lincomb(const TV* __restrict__ V, size_t ld, int k, const double* __restrict__ c,
+                          TY* __restrict__ y, size_t n)
+{
+    __shared__ double cs[512];
+    for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) cs[j] = c[j];
+    __syncthreads();
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        double acc = 0.0;
+        for (int j = 0; j < k; ++j) acc = fma(j < 512 ? cs[j] : c[j], (double)V[(size_t)j * ld + r], acc);
+        y[r] = (TY)acc;
+    }
+}
+
+template <class TX, class TY>
+__global__ void k_axpby(size_t n, double a, const TX* __restrict__ x, double b, TY* __restrict__ y)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+        y[r] = (TY)(b == 0.0 ? a * (double)x[r] : fma(a, (double)x[r], b * (double)y[r]));
+}
+
+template <class T>
+__global__ void k_norm2(const T* __restrict__ x, size_t n, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double v = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const double xr = (double)x[r];
+        v = fma(xr, xr, v);
+    }
+    const double s = block_sum(v, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+template <class T>
+__global__ void k_mask_rows(T* x, const int* __restrict__ mask, int p, int q)
+{
+    const size_t n = (size_t)p * q;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        if (mask[i / q]) x[i] = T(0);
+}
+
+template <class TI, class TO>
+__global__ void k_to_itl(const TI* __restrict__ blk, TO* __restrict__ itl, int p, int q)
+{
+    const size_t n = (size_t)p * q;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const size_t r = i / q, k = i % q;
+        itl[i] = (TO)blk[k * (size_t)p + r];
+    }
+}
+
+template <class TI, class TO>
+__global__ void k_to_blk(const TI* __restrict__ itl, TO* __restrict__ blk, int p, int q)
+{
+    const size_t n = (size_t)p * q;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const size_t k = i / p, r = i % p;
+        blk[i] = (TO)itl[r * q + k];
+    }
+}
+
+struct Coef8 {
+    double c[8];
+};
+
+__global__ void k_fill_load(const double* __restrict__ rext, Coef8 c, double* __restrict__ out,
+                            int p, int q)
+{
+    const size_t n = (size_t)p * q;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        out[i] = c.c[i % q] * rext[i / q];
+}
+
+__global__ void k_max(const double* __restrict__ x, size_t n, double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    double v = -1.0e300;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride)
+        v = fmax(v, x[r]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) sh[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = sh[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) r = fmax(r, sh[w]);
+        partial[blockIdx.x] = r;
+    }
+}
+
+__global__ void k_max_finish(const double* __restrict__ partial, int nb, double* out)
+{
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        double r = -1.0e300;
+        for (int b = 0; b < nb; ++b) r = fmax(r, partial[b]);
+        out[0] = r;
+    }
+}
+
+int grid_for(size_t n)
+{
+    size_t b = (n + kThreads - 1) / kThreads;
+    if (b > 4096) b = 4096;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace
+
+int reduce_init(Reduce& r, int kmax)
+{
+    if (kmax < 1) kmax = 1;
+    r.nblocks = kRowBlocks;
+    r.kmax = kmax;
+    XT_TRY(r.partial.alloc((size_t)kmax * kRowBlocks + kRowBlocks));
+    XT_TRY(r.out.alloc((size_t)kmax + 1));
+    return XT_OK;
+}
+
+template <class TV>
+int multi_dot(const TV* V, size_t ld, int k, const TV* w, size_t n, Reduce& r, cudaStream_t s)
+{
+    if (k > r.kmax) { set_error("multi_dot: k exceeds reduction capacity"); return XT_ERR_ARG; }
+    if (k <= 0) return XT_OK;
+    dim3 grid(r.nblocks, (k + kChunk - 1) / kChunk);
+    k_multi_dot<TV><<<grid, kThreads, 0, s>>>(V, ld, k, w, n, r.partial.p);
+    k_finish<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p, 0);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class TV>
+int update_and_dot(const TV* V, size_t ld, int k, const double* h, TV* w, size_t n, Reduce& r,
+                   cudaStream_t s)
+{
+    if (k <= 0) return XT_OK;
+    k_update<TV, false><<<grid_for(n), kThreads, 0, s>>>(V, ld, k, h, w, n, nullptr);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return multi_dot<TV>(V, ld, k, w, n, r, s);
+}
+
+template <class TV>
+int update_and_norm(const TV* V, size_t ld, int k, const double* h, TV* w, size_t n, Reduce& r,
+                    cudaStream_t s)
+{
+    const int nb = r.nblocks;
+    if (k > 0) {
+        k_update<TV, true><<<nb, kThreads, 0, s>>>(V, ld, k, h, w, n, r.partial.p);
+    } else {
+        k_norm2<TV><<<nb, kThreads, 0, s>>>(w, n, r.partial.p);
+    }
+    k_finish<<<1, kThreads, 0, s>>>(r.partial.p, nb, r.out.p, 0);
+    note_launches(3);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class TV, class TY>
+int lincomb(const TV* V, size_t ld, int k, const double* c, TY* y, size_t n, cudaStream_t s)
+{
+    k_lincomb<TV, TY><<<grid_for(n), kThreads, 0, s>>>(V, ld, k, c, y, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class TX, class TY>
+int axpby(size_t n, double a, const TX* x, double b, TY* y, cudaStream_t s)
+{
+    k_axpby<TX, TY><<<grid_for(n), kThreads, 0, s>>>(n, a, x, b, y);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class T>
+int norm2(const T* x, size_t n, Reduce& r, cudaStream_t s)
+{
+    k_norm2<T><<<r.nblocks, kThreads, 0, s>>>(x, n, r.partial.p);
+    k_finish<<<1, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p, 0);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class T>
+int mask_rows(T* x, const int* mask, int p, int q, cudaStream_t s)
+{
+    k_mask_rows<T><<<grid_for((size_t)p * q), kThreads, 0, s>>>(x, mask, p, q);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class TI, class TO>
+int to_interleaved(const TI* blk, TO* itl, int p, int q, cudaStream_t s)
+{
+    k_to_itl<TI, TO><<<grid_for((size_t)p * q), kThreads, 0, s>>>(blk, itl, p, q);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class TI, class TO>
+int to_blocks(const TI* itl, TO* blk, int p, int q, cudaStream_t s)
+{
+    k_to_blk<TI, TO><<<grid_for((size_t)p * q), kThreads, 0, s>>>(itl, blk, p, q);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int fill_load(const double* rext, const double* c, double* out, int p, int q, cudaStream_t s)
+{
+    Coef8 cc{};
+    for (int j = 0; j < q && j < 8; ++j) cc.c[j] = c[j];
+    k_fill_load<<<grid_for((size_t)p * q), kThreads, 0, s>>>(rext, cc, out, p, q);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int max_value(const double* x, size_t n, Reduce& r, cudaStream_t s)
+{
+    k_max<<<r.nblocks, kThreads, 0, s>>>(x, n, r.partial.p);
+    k_max_finish<<<1, 32, 0, s>>>(r.partial.p, r.nblocks, r.out.p);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+#define XT_INST_V(TV)                                                                       \
+    template int multi_dot<TV>(const TV*, size_t, int, const TV*, size_t, Reduce&,          \
+                               cudaStream_t);                                               \
+    template int update_and_dot<TV>(const TV*, size_t, int, const double*, TV*, size_t,     \
+                                    Reduce&, cudaStream_t);                                 \
+    template int update_and_norm<TV>(const TV*, size_t, int, const double*, TV*, size_t,    \
+                                     Reduce&, cudaStream_t);                                \
+    template int norm2<TV>(const TV*, size_t, Reduce&, cudaStream_t);                       \
+    template int mask_rows<TV>(TV*, const int*, int, int, cudaStream_t);
+XT_INST_V(double)
+XT_INST_V(float)
+#undef XT_INST_V
+
+template int lincomb<double, double>(const double*, size_t, int, const double*, double*, size_t,
+                                     cudaStream_t);
+template int lincomb<float, double>(const float*, size_t, int, const double*, double*, size_t,
+                                    cudaStream_t);
+template int lincomb<float, float>(const float*, size_t, int, const double*, float*, size_t,
+                                   cudaStream_t);
+template int axpby<double, double>(size_t, double, const double*, double, double*, cudaStream_t);
+template int axpby<float, double>(size_t, double, const float*, double, double*, cudaStream_t);
+template int axpby<double, float>(size_t, double, const double*, double, float*, cudaStream_t);
+template int axpby<float, float>(size_t, double, const float*, double, float*, cudaStream_t);
+template int to_interleaved<double, double>(const double*, double*, int, int, cudaStream_t);
+template int to_blocks<double, double>(const double*, double*, int, int, cudaStream_t);
+
+}  // namespace xt

@@ -1,0 +1,267 @@
+// host_abi.cpp -- C ABI of the host-side set-up (include/xtfem_gb300_host.h)
+// and the element-deletion surgery of src/main3d.f90:634-687.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+
+#include "../../include/xtfem_gb300_host.h"
+#include "host_problem.h"
+#include "xt_device.h"
+
+using namespace xt;
+
+namespace xt {
+
+int Problem::delete_elements(int nef, const int* nefail, int* bc, int* ndf_out)
+{
+    if (ndf_out) *ndf_out = 0;
+    if (nef <= 0) return XT_OK;
+    const int ndof = 3 * mesh.nn;
+    for (int k = 0; k < nef; ++k)
+        if (nefail[k] < 1 || nefail[k] > mesh.ne) {
+            set_error("delete: element number out of range");
+            return XT_ERR_ARG;
+        }
+    // delelement: the reference passes the per-Gauss-point stiffness array
+    // where one 6x6 matrix is expected (src/delelement.f90:46-47 into
+    // src/elesubs.f90:217), so every failed element's ke uses the first
+    // Gauss point's constitutive matrix; with a uniform material this is
+    // the material's matrix.
+    Triplets t;
+    t.i.reserve((size_t)nef * 576);
+    t.j.reserve((size_t)nef * 576);
+    t.v.reserve((size_t)nef * 576);
+    double ke[576];
+    for (int k = 0; k < nef; ++k) {
+        const int e = nefail[k] - 1;
+        element_stiffness(mesh, e, sys.stiff.data(), ke);
+        int dofs[24];
+        for (int i = 0; i < 8; ++i)
+            for (int c = 0; c < 3; ++c) dofs[3 * i + c] = 3 * (mesh.conn[(size_t)e * 8 + i] - 1) + c + 1;
+        for (int r = 0; r < 24; ++r)
+            for (int c = 0; c < 24; ++c) {
+                t.i.push_back(dofs[r]);
+                t.j.push_back(dofs[c]);
+                t.v.push_back(ke[r * 24 + c]);
+            }
+    }
+    cs_add(sys.K, tricsr(t, ndof), 1.0, -1.0);
+    // chkcnsta, then chkndsta (src/delelement.f90:139-201)
+    for (int k = 0; k < nef; ++k) {
+        const int e = nefail[k] - 1;
+        for (int i = 0; i < 8; ++i) necnt[mesh.conn[(size_t)e * 8 + i] - 1] -= 1;
+    }
+    std::vector<int> ndfail;
+    std::vector<char> seen(mesh.nn, 0);
+    for (int k = 0; k < nef; ++k) {
+        const int e = nefail[k] - 1;
+        for (int i = 0; i < 8; ++i) {
+            const int nd = mesh.conn[(size_t)e * 8 + i] - 1;
+            if (necnt[nd] == 0 && !seen[nd]) {
+                seen[nd] = 1;
+                ndfail.push_back(nd + 1);
+            }
+        }
+    }
+    // adddiagonal (src/delelement.f90:204-247)
+    if (!ndfail.empty()) {
+        Triplets d;
+        for (int nd : ndfail)
+            for (int c = 1; c <= 3; ++c) {
+                d.i.push_back((nd - 1) * 3 + c);
+                d.j.push_back((nd - 1) * 3 + c);
+                d.v.push_back(1.0);
+            }
+        cs_add(sys.K, tricsr(d, ndof), 1.0, 1.0);
+        for (int nd : ndfail)
+            for (int c = 0; c < 3; ++c) bc[(nd - 1) * 3 + c] = 1;
+    }
+    csrapplybc(sys.M, bc);
+    csrapplybc(sys.K, bc);
+    if (ndf_out) *ndf_out = (int)ndfail.size();
+    return XT_OK;
+}
+
+}  // namespace xt
+
+namespace {
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return XT_ERR_HOST;
+    }
+}
+
+int finish_problem(std::unique_ptr<Problem>& pr, double E, double nu, double rho,
+                   xth_problem* out)
+{
+    pr->sys = assemble_mech(pr->mesh, E, nu, rho);
+    pr->E = E;
+    pr->nu = nu;
+    pr->rho = rho;
+    pr->necnt.assign(pr->mesh.nn, 0);
+    for (size_t k = 0; k < pr->mesh.conn.size(); ++k) pr->necnt[pr->mesh.conn[k] - 1] += 1;
+    *out = reinterpret_cast<xth_problem>(pr.release());
+    return XT_OK;
+}
+
+Problem* P(xth_problem h) { return reinterpret_cast<Problem*>(h); }
+
+}  // namespace
+
+extern "C" {
+
+int xth_problem_from_inp(const char* path, double E, double nu, double rho, xth_problem* out)
+{
+    if (!path || !out) { set_error("xth_problem_from_inp: null argument"); return XT_ERR_ARG; }
+    return guarded([&] {
+        auto pr = std::make_unique<Problem>();
+        pr->mesh = read_inp(path);
+        return finish_problem(pr, E, nu, rho, out);
+    });
+}
+
+int xth_problem_rod(int nx, int ny, int nz, double lx, double ly, double lz, double E, double nu,
+                    double rho, xth_problem* out)
+{
+    if (!out) { set_error("xth_problem_rod: null argument"); return XT_ERR_ARG; }
+    return guarded([&] {
+        auto pr = std::make_unique<Problem>();
+        pr->mesh = make_rod(nx, ny, nz, lx, ly, lz);
+        return finish_problem(pr, E, nu, rho, out);
+    });
+}
+
+int xth_problem_destroy(xth_problem pr)
+{
+    delete P(pr);
+    return XT_OK;
+}
+
+int xth_problem_sizes(xth_problem h, int* nn, int* ne, int* nnz_k, int* nnz_m)
+{
+    if (!h) { set_error("null problem"); return XT_ERR_ARG; }
+    Problem* pr = P(h);
+    if (nn) *nn = pr->mesh.nn;
+    if (ne) *ne = pr->mesh.ne;
+    if (nnz_k) *nnz_k = pr->sys.K.nnz();
+    if (nnz_m) *nnz_m = pr->sys.M.nnz();
+    return XT_OK;
+}
+
+int xth_problem_mesh(xth_problem h, double* xyz, int* conn)
+{
+    if (!h) { set_error("null problem"); return XT_ERR_ARG; }
+    Problem* pr = P(h);
+    if (xyz) std::memcpy(xyz, pr->mesh.xyz.data(), pr->mesh.xyz.size() * sizeof(double));
+    if (conn) std::memcpy(conn, pr->mesh.conn.data(), pr->mesh.conn.size() * sizeof(int));
+    return XT_OK;
+}
+
+static int copy_csr(const Csr& m, int* ia, int* ja, double* a)
+{
+    if (ia) std::memcpy(ia, m.ia.data(), m.ia.size() * sizeof(int));
+    if (ja) std::memcpy(ja, m.ja.data(), m.ja.size() * sizeof(int));
+    if (a) std::memcpy(a, m.a.data(), m.a.size() * sizeof(double));
+    return XT_OK;
+}
+
+int xth_problem_k(xth_problem h, int* ia, int* ja, double* a)
+{
+    if (!h) { set_error("null problem"); return XT_ERR_ARG; }
+    return copy_csr(P(h)->sys.K, ia, ja, a);
+}
+
+int xth_problem_m(xth_problem h, int* ia, int* ja, double* a)
+{
+    if (!h) { set_error("null problem"); return XT_ERR_ARG; }
+    return copy_csr(P(h)->sys.M, ia, ja, a);
+}
+
+int xth_problem_strain_rows(xth_problem h, double* nx, double* ny, double* nz)
+{
+    if (!h) { set_error("null problem"); return XT_ERR_ARG; }
+    Problem* pr = P(h);
+    const size_t n = pr->sys.Nx.size();
+    if (nx) std::memcpy(nx, pr->sys.Nx.data(), n * sizeof(double));
+    if (ny) std::memcpy(ny, pr->sys.Ny.data(), n * sizeof(double));
+    if (nz) std::memcpy(nz, pr->sys.Nz.data(), n * sizeof(double));
+    return XT_OK;
+}
+
+int xth_problem_stiffness(xth_problem h, double* d)
+{
+    if (!h || !d) { set_error("null argument"); return XT_ERR_ARG; }
+    std::memcpy(d, P(h)->sys.stiff.data(), 36 * sizeof(double));
+    return XT_OK;
+}
+
+int xth_problem_apply_bc(xth_problem h, const int* bc)
+{
+    if (!h || !bc) { set_error("null argument"); return XT_ERR_ARG; }
+    return guarded([&] {
+        csrapplybc(P(h)->sys.K, bc);
+        csrapplybc(P(h)->sys.M, bc);
+        return XT_OK;
+    });
+}
+
+int xth_problem_delete(xth_problem h, int nef, const int* nefail, int* bc, int* ndf_out)
+{
+    if (!h || (nef > 0 && (!nefail || !bc))) { set_error("null argument"); return XT_ERR_ARG; }
+    return guarded([&] { return P(h)->delete_elements(nef, nefail, bc, ndf_out); });
+}
+
+int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, double droptol,
+             int iwk, double* alu, int* jlu, int* ju)
+{
+    if (n <= 0 || !ia || !ja || !a || !alu || !jlu || !ju) {
+        set_error("xth_ilut: bad arguments");
+        return XT_ERR_ARG;
+    }
+    return guarded([&] {
+        Csr m;
+        m.n = n;
+        m.ia.assign(ia, ia + n + 1);
+        m.ja.assign(ja, ja + (ia[n] - 1));
+        m.a.assign(a, a + (ia[n] - 1));
+        Msr f;
+        int ierr = ilut(m, lfil, droptol, f);
+        if (ierr != 0) return ierr;
+        if ((long long)f.alu.size() > iwk) return -2;
+        std::memcpy(alu, f.alu.data(), f.alu.size() * sizeof(double));
+        std::memcpy(jlu, f.jlu.data(), f.jlu.size() * sizeof(int));
+        std::memcpy(ju, f.ju.data(), f.ju.size() * sizeof(int));
+        return 0;
+    });
+}
+
+void xth_stcoeff_m(double t1, double dt, double w, double* k, double* m, double* ktn, double* mtn,
+                   double* ktn1, double* mtn1)
+{
+    stcoeff_m(t1, dt, w, k, m, ktn, mtn, ktn1, mtn1);
+}
+
+void xth_stcoeff_t(double dt, double* k, double* m, double* ktn, double* mtn, double* ktn1,
+                   double* mtn1)
+{
+    stcoeff_t(dt, k, m, ktn, mtn, ktn1, mtn1);
+}
+
+void xth_getfextc_m(double t1, double w, double dt, double* fextc, double* fint)
+{
+    getfextc_m(t1, w, dt, fextc, fint);
+}
+
+void xth_nt_table(int nip, const double* tcoorde, double w, double* nt)
+{
+    nt_table(nip, tcoorde, w, nt);
+}
+
+}  // extern "C"

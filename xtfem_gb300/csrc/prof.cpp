@@ -1,0 +1,136 @@
+// prof.cpp -- CUDA-event timing of kernel classes on the launching stream.
+//
+// When enabled, every launch of a timed class is bracketed by two events
+// recorded on the stream the kernel runs on; the elapsed times are summed
+// when read (after a synchronize).  Used by bench.py to report the average
+// duration of the dominant kernel inside the timed region.
+#include "prof.h"
+
+#include <vector>
+
+#include "../../include/xtfem_gb300_host.h"
+#include "solver.h"
+#include "xt_device.h"
+
+namespace xt {
+
+namespace {
+struct Rec {
+    int cls;
+    cudaEvent_t a, b;
+};
+bool g_on = false;
+std::vector<Rec> g_open;
+std::vector<cudaEvent_t> g_pool;
+long long g_count[PROF_NCLASS] = {0};
+double g_ms[PROF_NCLASS] = {0};
+
+cudaEvent_t take()
+{
+    if (!g_pool.empty()) {
+        cudaEvent_t e = g_pool.back();
+        g_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void settle()
+{
+    for (Rec& r : g_open) {
+        cudaEventSynchronize(r.b);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+            g_count[r.cls] += 1;
+            g_ms[r.cls] += ms;
+        }
+        g_pool.push_back(r.a);
+        g_pool.push_back(r.b);
+    }
+    g_open.clear();
+}
+}  // namespace
+
+int prof_begin(int cls, cudaStream_t s)
+{
+    if (!g_on) return -1;
+    if (g_open.size() > 4096) settle();
+    Rec r{cls, take(), take()};
+    cudaEventRecord(r.a, s);
+    g_open.push_back(r);
+    return (int)g_open.size() - 1;
+}
+
+void prof_end(int token, cudaStream_t s)
+{
+    if (token < 0 || token >= (int)g_open.size()) return;
+    cudaEventRecord(g_open[token].b, s);
+}
+
+}  // namespace xt
+
+extern "C" {
+
+int xt_profile(int enable)
+{
+    xt::settle();
+    xt::g_on = enable != 0;
+    for (int c = 0; c < xt::PROF_NCLASS; ++c) {
+        xt::g_count[c] = 0;
+        xt::g_ms[c] = 0.0;
+    }
+    return XT_OK;
+}
+
+int xt_profile_read(int cls, long long* count, double* ms)
+{
+    if (cls < 0 || cls >= xt::PROF_NCLASS) return XT_ERR_ARG;
+    xt::settle();
+    if (count) *count = xt::g_count[cls];
+    if (ms) *ms = xt::g_ms[cls];
+    return XT_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------ launch count and timers
+namespace xt {
+namespace {
+long long g_launches = 0;
+cudaEvent_t g_marks[8] = {nullptr};
+}  // namespace
+
+void note_launches(int n) { g_launches += n; }
+
+}  // namespace xt
+
+extern "C" {
+
+long long xt_launch_count(void) { return xt::g_launches; }
+
+int xt_mark(int slot)
+{
+    if (slot < 0 || slot >= 8) return XT_ERR_ARG;
+    if (xt::ensure_init() != XT_OK) return XT_ERR_CUDA;
+    if (!xt::g_marks[slot] && cudaEventCreate(&xt::g_marks[slot]) != cudaSuccess) return XT_ERR_CUDA;
+    return cudaEventRecord(xt::g_marks[slot], xt::ctx().stream) == cudaSuccess ? XT_OK : XT_ERR_CUDA;
+}
+
+double xt_elapsed_ms(int a, int b)
+{
+    if (a < 0 || a >= 8 || b < 0 || b >= 8 || !xt::g_marks[a] || !xt::g_marks[b]) return -1.0;
+    if (cudaEventSynchronize(xt::g_marks[b]) != cudaSuccess) return -1.0;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, xt::g_marks[a], xt::g_marks[b]) != cudaSuccess) return -1.0;
+    return ms;
+}
+
+int xt_sync(void)
+{
+    if (!xt::ctx().ready) return XT_OK;
+    return cudaStreamSynchronize(xt::ctx().stream) == cudaSuccess ? XT_OK : XT_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,15 @@
+// prof.h -- optional per-kernel-class CUDA-event timing on the library stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace xt {
+
+enum ProfClass { PROF_KRON64 = 0, PROF_KRON32 = 1, PROF_ILU64 = 2, PROF_ILU32 = 3, PROF_DAMAGE = 4,
+                 PROF_NCLASS = 5 };
+
+// Returns a token for prof_end, or -1 when profiling is off.
+int prof_begin(int cls, cudaStream_t s);
+void prof_end(int token, cudaStream_t s);
+
+}  // namespace xt

@@ -1,0 +1,368 @@
+// slab.cpp -- the mechanical space-time slab loop with its state on the GPU.
+//
+// Restates src/main3d.f90:609-937 for the mechanical-only run (no thermal
+// solve, no per-slab reassembly; the element-deletion subtraction then
+// persists, src/main3d.f90:752-783 is not executed):
+//   1. slab node times from the previous slab's end (:611-614);
+//   2. deletion check: any D >= Dc -> chkelesta, delelement, chkcnsta,
+//      chkndsta, adddiagonal, extra fixed DOFs, csrapplybc, refactor, and
+//      the slab length and damage resolution switch from n1 to n2 cycles
+//      (:625-691);
+//   3. load blocks fextc(j) * rext, stcoeff_m, jump term
+//      (ktn1 (x) K + mtn1 (x) M) u_prev, fixed rows zeroed (:804-823);
+//   4. GMRES solve from a zero start, fixed DOFs of the solution zeroed
+//      (:824-845);
+//   5. damage update with the failed-point clean-up (:880-883).
+// The reference passes the INTEGER slab index as stcoeff_m's REAL t1
+// argument (:816, implicit interface); the intended slab start time
+// tcoorde(1) is used here.  Every per-slab vector stays on the device; the
+// host sees a handful of scalars per slab.
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "../../include/xtfem_gb300_host.h"
+#include "host_problem.h"
+#include "prof.h"
+#include "solver.h"
+
+using namespace xt;
+
+struct xt_slab_s {
+    Problem* pr = nullptr;
+    xt_slab_config cfg{};
+    System S;
+    int p = 0, q = 6, nn = 0, ne = 0, ngp = 0;
+    std::vector<int> bc;
+    std::vector<double> rext;
+    DBuf<double> drext, fext, disp, dblk;
+    // damage state (device)
+    DBuf<int> nodes, gpsta, elesta, nefail, nef, flag;
+    DBuf<double> Nx, Ny, Nz, ym, nu, eo, ep, se, sb, pp, D, ws, dpo, sd, Nt64;
+    DBuf<float> Nt32, ntmax;
+    DBuf<unsigned long long> counters;
+    double tc[3] = {0, 0, 0};
+    double dt = 0, w = 0;
+    int nip = 0, slab = 0, nfailed = 0;
+    bool switched = false;
+};
+
+namespace {
+
+int refactor(xt_slab_s& s)
+{
+    const Csr& K = s.pr->sys.K;
+    Msr f;
+    const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f);
+    if (ierr != 0) {
+        set_error("ILUT failed with ierr = " + std::to_string(ierr));
+        return XT_ERR_HOST;
+    }
+    return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group);
+}
+
+int upload_operator(xt_slab_s& s)
+{
+    const Csr &K = s.pr->sys.K, &M = s.pr->sys.M;
+    cudaStream_t st = ctx().stream;
+    XT_TRY(upload_csr(s.S.K, K.n, K.ia.data(), K.ja.data(), K.a.data(), st));
+    XT_TRY(upload_csr(s.S.M, M.n, M.ia.data(), M.ja.data(), M.a.data(), st));
+    XT_TRY(s.S.bcmask.upload(s.bc.data(), s.bc.size(), st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    return XT_OK;
+}
+
+int deletion_check(xt_slab_s& s, int& deleted)
+{
+    deleted = 0;
+    cudaStream_t st = ctx().stream;
+    XT_TRY(any_ge_device(s.D.p, s.ngp, s.cfg.Dc, s.flag.p, st));
+    int f = 0;
+    XT_CUDA(cudaMemcpyAsync(&f, s.flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    if (!f) return XT_OK;
+    XT_TRY(chkelesta_device(s.ne, 8, s.cfg.Dc, s.D.p, s.elesta.p, s.gpsta.p, s.nefail.p, s.nef.p, st));
+    int nef = 0;
+    XT_CUDA(cudaMemcpyAsync(&nef, s.nef.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> list(nef > 0 ? nef : 1);
+    if (nef > 0) {
+        XT_CUDA(cudaMemcpyAsync(list.data(), s.nefail.p, sizeof(int) * nef, cudaMemcpyDeviceToHost, st));
+        XT_CUDA(cudaStreamSynchronize(st));
+    }
+    int ndf = 0;
+    XT_TRY(s.pr->delete_elements(nef, list.data(), s.bc.data(), &ndf));
+    XT_TRY(upload_operator(s));
+    XT_TRY(refactor(s));
+    s.dt = s.cfg.dt0 * s.cfg.n2;
+    s.nip = s.cfg.nipc * s.cfg.n2;
+    s.switched = true;
+    s.nfailed += nef;
+    deleted = nef;
+    return XT_OK;
+}
+
+// Steps 1-4 of a slab; the load blocks come from fext_host (block layout)
+// when given, else from fextc(j) * rext.
+int solve_slab(xt_slab_s& s, const double* fext_host, double* stats)
+{
+    cudaStream_t st = ctx().stream;
+    const size_t n = (size_t)s.p * s.q;
+    s.slab += 1;
+    const double t3 = s.tc[2];
+    for (int j = 0; j < 3; ++j) s.tc[j] = t3 + j * s.dt / 2.0;
+    int deleted = 0;
+    if (s.cfg.damage && s.slab > 1) XT_TRY(deletion_check(s, deleted));
+    // temporal matrices of this slab
+    double ck[36], cm[36], ckt[36], cmt[36], ck1[36], cm1[36], A[36], B[36];
+    stcoeff_m(s.tc[0], s.dt, s.w, ck, cm, ckt, cmt, ck1, cm1);
+    for (int k = 0; k < 36; ++k) {
+        A[k] = ck[k] + ckt[k];
+        B[k] = cm[k] + cmt[k];
+    }
+    XT_TRY(system_set_temporal(s.S, A, B));
+    XT_CUDA(cudaMemcpyAsync(s.S.Cj.p, ck1, sizeof(ck1), cudaMemcpyHostToDevice, st));
+    XT_CUDA(cudaMemcpyAsync(s.S.Mj.p, cm1, sizeof(cm1), cudaMemcpyHostToDevice, st));
+    // load blocks and jump term
+    if (fext_host) {
+        XT_TRY(s.dblk.alloc(n));
+        XT_CUDA(cudaMemcpyAsync(s.dblk.p, fext_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        XT_TRY((to_interleaved<double, double>(s.dblk.p, s.fext.p, s.p, s.q, st)));
+    } else {
+        double fextc[6], fint[6];
+        getfextc_m(s.tc[0], s.w, s.dt, fextc, fint);
+        XT_TRY(fill_load(s.drext.p, fextc, s.fext.p, s.p, s.q, st));
+    }
+    XT_TRY(system_apply_with(s.S, s.S.Cj.p, s.S.Mj.p, 1.0, 1.0, s.disp.p, s.fext.p));
+    XT_TRY(mask_rows<double>(s.fext.p, s.S.bcmask.p, s.p, s.q, st));
+    // solve from zero
+    XT_CUDA(cudaMemsetAsync(s.disp.p, 0, n * sizeof(double), st));
+    GmresStats gs;
+    XT_TRY(solve_refined(s.S, s.fext.p, s.disp.p, s.cfg.im, s.cfg.tol, s.cfg.maxits, s.cfg.precision,
+                         s.cfg.inner_tol, gs));
+    XT_TRY(mask_rows<double>(s.disp.p, s.S.bcmask.p, s.p, s.q, st));
+    if (stats) {
+        stats[0] = s.slab;
+        stats[1] = gs.its;
+        stats[2] = gs.cycles;
+        stats[3] = gs.outer;
+        stats[4] = gs.ierr;
+        stats[5] = gs.relres;
+        stats[8] = deleted;
+    }
+    if (gs.ierr != 0 && gs.ierr != -1) {
+        set_error("slab solve did not converge");
+        return gs.ierr;
+    }
+    return XT_OK;
+}
+
+int damage_slab(xt_slab_s& s, double* stats)
+{
+    cudaStream_t st = ctx().stream;
+    const size_t n = (size_t)s.p * s.q;
+    if (s.cfg.damage) {
+        XT_TRY(s.dblk.alloc(n));
+        XT_TRY((to_blocks<double, double>(s.disp.p, s.dblk.p, s.p, s.q, st)));
+        XT_TRY(s.Nt64.alloc((size_t)s.nip * 6));
+        XT_TRY(s.Nt32.alloc((size_t)s.nip * 6));
+        XT_TRY(nt_table_device(s.nip, s.tc[0], s.tc[1], s.tc[2], s.w, s.Nt64.p, s.Nt32.p, st));
+        XT_CUDA(cudaMemsetAsync(s.counters.p, 0, 3 * sizeof(unsigned long long), st));
+        DamageArgs a{};
+        a.ngp = s.ngp; a.nn = s.nn; a.ndofn = 3; a.nnse = 8; a.nnte = 3; a.ncmp = 6; a.nip = s.nip;
+        a.nodes = s.nodes.p; a.Nx = s.Nx.p; a.Ny = s.Ny.p; a.Nz = s.Nz.p;
+        a.Nt = s.Nt64.p; a.Nt32 = s.Nt32.p; a.sol = s.dblk.p; a.ym = s.ym.p; a.nu = s.nu.p;
+        a.eps_old = s.eo.p; a.eps_pl = s.ep.p; a.sig_eff = s.se.p; a.sig_back = s.sb.p;
+        a.p = s.pp.p; a.D = s.D.p; a.ws = s.ws.p; a.del_po = s.dpo.p; a.sig_d = s.sd.p;
+        a.gpsta = s.gpsta.p; a.counters = s.counters.p; a.ntmax = s.ntmax.p;
+        const int tok = prof_begin(PROF_DAMAGE, st);
+        XT_TRY(damage_update(a, st));
+        prof_end(tok, st);
+    }
+    if (stats) {
+        double mx = 0.0;
+        unsigned long long cnt[3] = {0, 0, 0};
+        if (s.cfg.damage) {
+            XT_TRY(max_value(s.D.p, (size_t)s.ngp, s.S.red, st));
+            XT_CUDA(cudaMemcpyAsync(&mx, s.S.red.out.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+            XT_CUDA(cudaMemcpyAsync(cnt, s.counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+        }
+        XT_CUDA(cudaStreamSynchronize(st));
+        stats[6] = mx;
+        stats[7] = s.nfailed;
+        stats[9] = (double)cnt[0];
+        stats[10] = (double)cnt[1];
+        stats[11] = (double)cnt[2];
+    } else {
+        XT_CUDA(cudaStreamSynchronize(st));
+    }
+    return XT_OK;
+}
+
+template <class F>
+int guarded(F&& f)
+{
+    try {
+        return f();
+    } catch (const std::exception& e) {
+        set_error(e.what());
+        return XT_ERR_HOST;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
+{
+    if (!h || !cfg || !out) { set_error("xt_slab_create: null argument"); return XT_ERR_ARG; }
+    *out = nullptr;
+    XT_TRY(ensure_init());
+    return guarded([&]() -> int {
+        auto s = std::make_unique<xt_slab_s>();
+        s->pr = reinterpret_cast<Problem*>(h);
+        s->cfg = *cfg;
+        Problem& pr = *s->pr;
+        const Mesh& m = pr.mesh;
+        if (cfg->clamp_axis < 0 || cfg->clamp_axis > 2 || cfg->load_axis < 0 || cfg->load_axis > 2 ||
+            cfg->load_comp < 0 || cfg->load_comp > 2 || cfg->im < 1 || cfg->dt0 <= 0 || cfg->n1 < 1 ||
+            cfg->n2 < 1 || cfg->nipc < 0 || cfg->lfil < 0) {
+            set_error("xt_slab_create: invalid configuration");
+            return XT_ERR_ARG;
+        }
+        s->nn = m.nn;
+        s->ne = m.ne;
+        s->ngp = 8 * m.ne;
+        s->p = 3 * m.nn;
+        // boundary conditions: all 3 DOFs of nodes on the clamped face
+        // (src/main3d.f90:482-497 with an axis-aware face selector)
+        s->bc.assign(s->p, 0);
+        for (int i = 0; i < m.nn; ++i)
+            if (m.xyz[(size_t)i * 3 + cfg->clamp_axis] == cfg->clamp_value)
+                for (int c = 0; c < 3; ++c) s->bc[(size_t)i * 3 + c] = 1;
+        csrapplybc(pr.sys.K, s->bc.data());
+        csrapplybc(pr.sys.M, s->bc.data());
+        // traction: the total force amplitude * area shared over the face's
+        // element-node incidences (src/main3d.f90:501-530)
+        std::vector<double> share(m.nn, 0.0);
+        for (size_t k = 0; k < m.conn.size(); ++k) share[m.conn[k] - 1] += 1.0;
+        double ntele = 0.0;
+        for (int i = 0; i < m.nn; ++i)
+            if (m.xyz[(size_t)i * 3 + cfg->load_axis] == cfg->load_value) ntele += share[i];
+        if (ntele == 0.0) {
+            set_error("xt_slab_create: no node on the loaded face");
+            return XT_ERR_ARG;
+        }
+        const double fnode = cfg->amplitude * cfg->area / ntele;
+        s->rext.assign(s->p, 0.0);
+        for (size_t k = 0; k < m.conn.size(); ++k) {
+            const int nd = m.conn[k] - 1;
+            if (m.xyz[(size_t)nd * 3 + cfg->load_axis] == cfg->load_value)
+                s->rext[(size_t)nd * 3 + cfg->load_comp] += fnode;
+        }
+        System& S = s->S;
+        S.p = s->p;
+        S.q = 6;
+        XT_TRY(S.A.alloc(64)); XT_TRY(S.B.alloc(64)); XT_TRY(S.Ainv.alloc(64));
+        XT_TRY(S.Cj.alloc(64)); XT_TRY(S.Mj.alloc(64));
+        XT_TRY(upload_operator(*s));
+        XT_TRY(refactor(*s));
+        cudaStream_t st = ctx().stream;
+        const size_t n = (size_t)s->p * 6, ngp = s->ngp;
+        XT_TRY(s->drext.upload(s->rext.data(), s->p, st));
+        XT_TRY(s->fext.alloc(n));
+        XT_TRY(s->disp.alloc(n));
+        XT_CUDA(cudaMemsetAsync(s->disp.p, 0, n * sizeof(double), st));
+        if (S.red.kmax < cfg->im + 1) XT_TRY(reduce_init(S.red, cfg->im + 1));
+        // damage state, zero initial state (src/main3d.f90:583-600)
+        std::vector<int> nodes(ngp * 8);
+        for (size_t gp = 0; gp < ngp; ++gp)
+            for (int i = 0; i < 8; ++i) nodes[gp * 8 + i] = m.conn[(gp / 8) * 8 + i];
+        XT_TRY(s->nodes.upload(nodes.data(), nodes.size(), st));
+        XT_TRY(s->Nx.upload(pr.sys.Nx.data(), pr.sys.Nx.size(), st));
+        XT_TRY(s->Ny.upload(pr.sys.Ny.data(), pr.sys.Ny.size(), st));
+        XT_TRY(s->Nz.upload(pr.sys.Nz.data(), pr.sys.Nz.size(), st));
+        std::vector<double> ymv(ngp, pr.E), nuv(ngp, pr.nu);
+        XT_TRY(s->ym.upload(ymv.data(), ngp, st));
+        XT_TRY(s->nu.upload(nuv.data(), ngp, st));
+        for (DBuf<double>* b : {&s->eo, &s->ep, &s->se, &s->sb}) {
+            XT_TRY(b->alloc(ngp * 6));
+            XT_CUDA(cudaMemsetAsync(b->p, 0, ngp * 6 * sizeof(double), st));
+        }
+        for (DBuf<double>* b : {&s->pp, &s->D, &s->ws, &s->dpo, &s->sd}) {
+            XT_TRY(b->alloc(ngp));
+            XT_CUDA(cudaMemsetAsync(b->p, 0, ngp * sizeof(double), st));
+        }
+        std::vector<int> ones(ngp, 1);
+        XT_TRY(s->gpsta.upload(ones.data(), ngp, st));
+        XT_TRY(s->elesta.upload(ones.data(), s->ne, st));
+        XT_TRY(s->nefail.alloc(s->ne));
+        XT_TRY(s->nef.alloc(1));
+        XT_TRY(s->flag.alloc(1));
+        XT_TRY(s->counters.alloc(3));
+        XT_TRY(s->ntmax.alloc(8));
+        XT_CUDA(cudaStreamSynchronize(st));
+        s->w = 2.0 * M_PI * cfg->freq;
+        s->dt = cfg->dt0 * cfg->n1;
+        s->nip = cfg->nipc * cfg->n1;
+        *out = s.release();
+        return XT_OK;
+    });
+}
+
+int xt_slab_destroy(xt_slab s)
+{
+    delete s;
+    return XT_OK;
+}
+
+int xt_slab_step(xt_slab s, double* stats)
+{
+    if (!s) { set_error("null slab"); return XT_ERR_ARG; }
+    double local[12] = {0};
+    double* st = stats ? stats : local;
+    return guarded([&]() -> int {
+        XT_TRY(solve_slab(*s, nullptr, st));
+        return damage_slab(*s, st);
+    });
+}
+
+int xt_slab_step_host(xt_slab s, const double* fext, double* disp, double* D, double* stats)
+{
+    if (!s || !fext) { set_error("xt_slab_step_host: null argument"); return XT_ERR_ARG; }
+    double local[12] = {0};
+    double* st = stats ? stats : local;
+    return guarded([&]() -> int {
+        XT_TRY(solve_slab(*s, fext, st));
+        XT_TRY(damage_slab(*s, st));
+        cudaStream_t cs = ctx().stream;
+        const size_t n = (size_t)s->p * s->q;
+        if (disp) {
+            XT_TRY((to_blocks<double, double>(s->disp.p, s->dblk.p, s->p, s->q, cs)));
+            XT_CUDA(cudaMemcpyAsync(disp, s->dblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        }
+        if (D) XT_CUDA(cudaMemcpyAsync(D, s->D.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        XT_CUDA(cudaStreamSynchronize(cs));
+        return XT_OK;
+    });
+}
+
+int xt_slab_get(xt_slab s, double* disp, double* D, double* ws, int* elesta)
+{
+    if (!s) { set_error("null slab"); return XT_ERR_ARG; }
+    cudaStream_t cs = ctx().stream;
+    const size_t n = (size_t)s->p * s->q;
+    if (disp) {
+        XT_TRY(s->dblk.alloc(n));
+        XT_TRY((to_blocks<double, double>(s->disp.p, s->dblk.p, s->p, s->q, cs)));
+        XT_CUDA(cudaMemcpyAsync(disp, s->dblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    }
+    if (D) XT_CUDA(cudaMemcpyAsync(D, s->D.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    if (ws) XT_CUDA(cudaMemcpyAsync(ws, s->ws.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
+    if (elesta) XT_CUDA(cudaMemcpyAsync(elesta, s->elesta.p, (size_t)s->ne * sizeof(int), cudaMemcpyDeviceToHost, cs));
+    XT_CUDA(cudaStreamSynchronize(cs));
+    return XT_OK;
+}
+
+}  // extern "C"

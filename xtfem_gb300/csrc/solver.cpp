@@ -1,0 +1,428 @@
+// solver.cpp -- the space-time system on the device and its restarted GMRES.
+//
+// gmres_core follows the control flow of the reference's kronpgmres
+// (src/kronecker.f90:181-365): right preconditioning with
+// (A^-1 (x) (LU)^-1), Arnoldi with Givens rotations, the correction of a
+// cycle applied before a restart, the restart residual rebuilt from the
+// Givens data, convergence when |rs(i+1)| <= eps * ||r0||, maxits tested at
+// the end of a cycle, ierr in {0, 1, -1}.  The vectors live on the device in
+// the interleaved layout; the (im+1) x im Hessenberg matrix, the rotations
+// and the small triangular solve stay on the host in FP64, fed by one
+// device-to-host copy per Arnoldi step.  The projection is CGS2 (see
+// dev_krylov.cu) instead of the reference's MGS.
+#include "solver.h"
+
+#include "prof.h"
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+namespace xt {
+
+namespace {
+thread_local std::string g_err;
+}
+
+void set_error(const std::string& msg) { g_err = msg; }
+const char* last_error() { return g_err.c_str(); }
+
+Context& ctx()
+{
+    static Context c;
+    return c;
+}
+
+int ensure_init(int device)
+{
+    Context& c = ctx();
+    if (c.ready && (device < 0 || device == c.device)) return XT_OK;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        set_error(std::string("no CUDA device available: ") + cudaGetErrorString(e));
+        return XT_ERR_CUDA;
+    }
+    if (device < 0) device = 0;
+    if (device >= count) {
+        set_error("device index out of range");
+        return XT_ERR_ARG;
+    }
+    XT_CUDA(cudaSetDevice(device));
+    if (c.stream) cudaStreamDestroy(c.stream);
+    XT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    c.device = device;
+    c.ready = true;
+    return XT_OK;
+}
+
+int invert_small(int n, const double* A, double* Ainv)
+{
+    std::vector<double> lu(A, A + (size_t)n * n);
+    std::vector<int> piv(n);
+    auto LU = [&](int i, int j) -> double& { return lu[(size_t)j * n + i]; };
+    for (int c = 0; c < n; ++c) {
+        int pr = c;
+        double best = std::fabs(LU(c, c));
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(LU(r, c)) > best) { best = std::fabs(LU(r, c)); pr = r; }
+        piv[c] = pr;
+        if (best == 0.0) {
+            set_error("temporal matrix is singular");
+            return XT_ERR_SINGULAR;
+        }
+        if (pr != c)
+            for (int j = 0; j < n; ++j) std::swap(LU(c, j), LU(pr, j));
+        for (int r = c + 1; r < n; ++r) {
+            LU(r, c) /= LU(c, c);
+            for (int j = c + 1; j < n; ++j) LU(r, j) -= LU(r, c) * LU(c, j);
+        }
+    }
+    for (int col = 0; col < n; ++col) {
+        double* e = Ainv + (size_t)col * n;
+        for (int r = 0; r < n; ++r) e[r] = (r == col) ? 1.0 : 0.0;
+        for (int c = 0; c < n; ++c)
+            if (piv[c] != c) std::swap(e[c], e[piv[c]]);
+        for (int r = 1; r < n; ++r)
+            for (int c = 0; c < r; ++c) e[r] -= LU(r, c) * e[c];
+        for (int r = n - 1; r >= 0; --r) {
+            for (int c = r + 1; c < n; ++c) e[r] -= LU(r, c) * e[c];
+            e[r] /= LU(r, r);
+        }
+    }
+    return XT_OK;
+}
+
+int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
+                  const int* mi, const int* mj, const double* mv)
+{
+    XT_TRY(ensure_init());
+    if (p <= 0 || q < 1 || q > 8) {
+        set_error("system_create: need p > 0 and 1 <= q <= 8");
+        return XT_ERR_ARG;
+    }
+    cudaStream_t s = ctx().stream;
+    S.p = p;
+    S.q = q;
+    XT_TRY(upload_csr(S.K, p, ki, kj, kv, s));
+    XT_TRY(upload_csr(S.M, p, mi, mj, mv, s));
+    XT_TRY(S.A.alloc(64));
+    XT_TRY(S.B.alloc(64));
+    XT_TRY(S.Ainv.alloc(64));
+    XT_TRY(S.Cj.alloc(64));
+    XT_TRY(S.Mj.alloc(64));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group)
+{
+    auto f = std::make_shared<DevIlu>();
+    XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, ctx().stream));
+    S.ilu = f;
+    return XT_OK;
+}
+
+int system_set_temporal(System& S, const double* A, const double* B)
+{
+    const int q = S.q;
+    S.hA.assign(A, A + q * q);
+    S.hB.assign(B, B + q * q);
+    S.hAinv.assign(q * q, 0.0);
+    XT_TRY(invert_small(q, A, S.hAinv.data()));
+    cudaStream_t s = ctx().stream;
+    XT_CUDA(cudaMemcpyAsync(S.A.p, A, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaMemcpyAsync(S.B.p, B, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaMemcpyAsync(S.Ainv.p, S.hAinv.data(), sizeof(double) * q * q,
+                            cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+int system_apply_with(System& S, const double* dA, const double* dB, double alpha, double beta,
+                      const double* x, double* y)
+{
+    const int tok = prof_begin(PROF_KRON64, ctx().stream);
+    const int st = kron_spmm<double>(S.K, S.M, S.q, dA, dB, alpha, beta, x, y, ctx().stream);
+    prof_end(tok, ctx().stream);
+    return st;
+}
+
+int system_apply(System& S, double alpha, double beta, const double* x, double* y)
+{
+    return system_apply_with(S, S.A.p, S.B.p, alpha, beta, x, y);
+}
+
+namespace {
+
+int ensure_workspace(System& S, int im, bool fp32)
+{
+    const size_t n = (size_t)S.p * S.q;
+    if (im > S.im_cap || S.red.kmax < im + 1) {
+        XT_TRY(reduce_init(S.red, im + 1));
+        XT_TRY(S.hsave.alloc((size_t)2 * (im + 1) + 2));
+        S.im_cap = im;
+        S.V64.release();
+        S.V32.release();
+    }
+    if (!fp32) {
+        if (S.V64.n < n * (im + 1)) XT_TRY(S.V64.alloc(n * (size_t)(im + 1)));
+        XT_TRY(S.z64.alloc(n));
+        XT_TRY(S.w64.alloc(n));
+        XT_TRY(S.u64.alloc(n));
+    } else {
+        if (S.V32.n < n * (im + 1)) XT_TRY(S.V32.alloc(n * (size_t)(im + 1)));
+        XT_TRY(S.z32.alloc(n));
+        XT_TRY(S.w32.alloc(n));
+        XT_TRY(S.u32.alloc(n));
+        XT_TRY(S.d32.alloc(n));
+        XT_TRY(S.r32.alloc(n));
+    }
+    XT_TRY(S.x64.alloc(n));
+    XT_TRY(S.r64.alloc(n));
+    XT_TRY(S.t64.alloc(n));
+    return XT_OK;
+}
+
+template <class T>
+struct Ws;
+template <>
+struct Ws<double> {
+    static double* V(System& S) { return S.V64.p; }
+    static double* z(System& S) { return S.z64.p; }
+    static double* w(System& S) { return S.w64.p; }
+    static double* u(System& S) { return S.u64.p; }
+};
+template <>
+struct Ws<float> {
+    static float* V(System& S) { return S.V32.p; }
+    static float* z(System& S) { return S.z32.p; }
+    static float* w(System& S) { return S.w32.p; }
+    static float* u(System& S) { return S.u32.p; }
+};
+
+template <class T>
+int apply_op(System& S, const T* x, T* y)
+{
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, ctx().stream);
+    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, 1.0, 0.0, x, y, ctx().stream);
+    prof_end(tok, ctx().stream);
+    return st;
+}
+
+template <class T>
+int apply_prec(System& S, const T* v, T* z)
+{
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_ILU64 : PROF_ILU32, ctx().stream);
+    const int st = ilu_apply<T>(*S.ilu, S.q, S.Ainv.p, v, z, Ws<T>::w(S), ctx().stream);
+    prof_end(tok, ctx().stream);
+    return st;
+}
+
+int fetch(double* h, const double* d, size_t count)
+{
+    cudaStream_t s = ctx().stream;
+    XT_CUDA(cudaMemcpyAsync(h, d, count * sizeof(double), cudaMemcpyDeviceToHost, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+// GMRES in the reference's control flow on vectors of type T; rhs and sol
+// are device vectors of type T (sol in/out).  rhs is preserved.
+template <class T>
+int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, GmresStats& st,
+               std::vector<double>* hist)
+{
+    cudaStream_t s = ctx().stream;
+    const size_t n = (size_t)S.p * S.q;
+    T* V = Ws<T>::V(S);
+    T* z = Ws<T>::z(S);
+    auto col = [&](int j) { return V + (size_t)j * n; };
+    std::vector<double> hh((size_t)(im + 1) * im, 0.0), c(im, 0.0), sn(im, 0.0), rs(im + 1, 0.0);
+    std::vector<double> hbuf(2 * (im + 1) + 2);
+    auto HH = [&](int r, int k) -> double& { return hh[(size_t)k * (im + 1) + r]; };
+    const double epsmac = 1.0e-16;
+    int its = 0, i = 0, ierr = 0;
+    double ro = 0.0, eps1 = 0.0, t;
+
+    XT_TRY(norm2<T>(rhs, n, S.red, s));
+    XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+    const double ro0 = std::sqrt(hbuf[0]);
+    // v1 = rhs - A sol
+    XT_CUDA(cudaMemcpyAsync(col(0), rhs, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    XT_TRY((kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, -1.0, 1.0, sol, col(0), s)));
+    for (;;) {  // label 20
+        XT_TRY(norm2<T>(col(0), n, S.red, s));
+        XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+        ro = std::sqrt(hbuf[0]);
+        if (!std::isfinite(ro)) {
+            set_error("gmres: non-finite residual");
+            return XT_ERR_NONFINITE;
+        }
+        if (ro == 0.0) { ierr = -1; break; }
+        XT_TRY((axpby<T, T>(n, 1.0 / ro, col(0), 0.0, col(0), s)));
+        if (its == 0) eps1 = eps * ro;
+        rs[0] = ro;
+        i = 0;
+        ++st.cycles;
+        for (;;) {  // label 4
+            ++i;
+            ++its;
+            const int i1 = i + 1;
+            XT_TRY(apply_prec<T>(S, col(i - 1), z));
+            XT_TRY(apply_op<T>(S, z, col(i1 - 1)));
+            // CGS2 projection against the i previous vectors
+            XT_TRY(multi_dot<T>(V, n, i, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(update_and_dot<T>(V, n, i, S.hsave.p, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(update_and_norm<T>(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(fetch(hbuf.data(), S.hsave.p, 2 * i + 1));
+            for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
+            t = std::sqrt(hbuf[2 * i]);
+            if (!std::isfinite(t)) {
+                set_error("gmres: non-finite Krylov vector");
+                return XT_ERR_NONFINITE;
+            }
+            HH(i1 - 1, i - 1) = t;
+            if (t != 0.0) XT_TRY((axpby<T, T>(n, 1.0 / t, col(i1 - 1), 0.0, col(i1 - 1), s)));
+            for (int k = 2; k <= i; ++k) {  // previous rotations
+                const int k1 = k - 1;
+                t = HH(k1 - 1, i - 1);
+                HH(k1 - 1, i - 1) = c[k1 - 1] * t + sn[k1 - 1] * HH(k - 1, i - 1);
+                HH(k - 1, i - 1) = -sn[k1 - 1] * t + c[k1 - 1] * HH(k - 1, i - 1);
+            }
+            double gam = std::sqrt(HH(i - 1, i - 1) * HH(i - 1, i - 1) +
+                                   HH(i1 - 1, i - 1) * HH(i1 - 1, i - 1));
+            if (gam == 0.0) gam = epsmac;
+            c[i - 1] = HH(i - 1, i - 1) / gam;
+            sn[i - 1] = HH(i1 - 1, i - 1) / gam;
+            rs[i1 - 1] = -sn[i - 1] * rs[i - 1];
+            rs[i - 1] = c[i - 1] * rs[i - 1];
+            HH(i - 1, i - 1) = c[i - 1] * HH(i - 1, i - 1) + sn[i - 1] * HH(i1 - 1, i - 1);
+            ro = std::fabs(rs[i1 - 1]);
+            if (hist) hist->push_back(ro / ro0);
+            if (i < im && ro > eps1) continue;
+            break;
+        }
+        // upper triangular solve, combination, preconditioner, update
+        std::vector<double> y(rs.begin(), rs.begin() + i);
+        y[i - 1] = y[i - 1] / HH(i - 1, i - 1);
+        for (int ii = 2; ii <= i; ++ii) {
+            const int k = i - ii + 1;
+            t = y[k - 1];
+            for (int j = k + 1; j <= i; ++j) t -= HH(k - 1, j - 1) * y[j - 1];
+            y[k - 1] = t / HH(k - 1, k - 1);
+        }
+        XT_CUDA(cudaMemcpyAsync(S.hsave.p, y.data(), i * sizeof(double), cudaMemcpyHostToDevice, s));
+        T* u = Ws<T>::u(S);
+        XT_TRY((lincomb<T, T>(V, n, i, S.hsave.p, u, n, s)));
+        XT_TRY(apply_prec<T>(S, u, z));
+        XT_TRY((axpby<T, T>(n, 1.0, z, 1.0, sol, s)));
+        XT_CUDA(cudaStreamSynchronize(s));
+        if (ro <= eps1) { ierr = 0; break; }
+        if (its >= maxits) { ierr = 1; break; }
+        // restart residual from the Givens data: v1 = sum_j rs'(j) v_j
+        {
+            const int i1 = i + 1;
+            std::vector<double> r2(rs);
+            for (int j = 1; j <= i; ++j) {
+                const int jj = i1 - j + 1;
+                r2[jj - 2] = -sn[jj - 2] * r2[jj - 1];
+                r2[jj - 1] = c[jj - 2] * r2[jj - 1];
+            }
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p, r2.data(), i1 * sizeof(double),
+                                    cudaMemcpyHostToDevice, s));
+            T* u = Ws<T>::u(S);
+            XT_TRY((lincomb<T, T>(V, n, i1, S.hsave.p, u, n, s)));
+            XT_CUDA(cudaMemcpyAsync(col(0), u, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+            XT_CUDA(cudaStreamSynchronize(s));
+        }
+    }
+    st.its += its;
+    st.ierr = ierr;
+    st.est = ro0 > 0 ? ro / ro0 : 0.0;
+    return XT_OK;
+}
+
+}  // namespace
+
+int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int maxits,
+               GmresStats& st, std::vector<double>* hist)
+{
+    if (!S.ilu) {
+        set_error("gmres: no preconditioner set");
+        return XT_ERR_STATE;
+    }
+    if (im < 1) {
+        set_error("gmres: restart length must be >= 1");
+        return XT_ERR_ARG;
+    }
+    XT_TRY(ensure_workspace(S, im, false));
+    return gmres_core<double>(S, b, x, im, eps, maxits, st, hist);
+}
+
+int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
+                  int inner, double inner_tol, GmresStats& st)
+{
+    if (!S.ilu) {
+        set_error("solve: no preconditioner set");
+        return XT_ERR_STATE;
+    }
+    cudaStream_t s = ctx().stream;
+    const size_t n = (size_t)S.p * S.q;
+    XT_TRY(ensure_workspace(S, im, inner == 1));
+    double hb[2];
+    XT_TRY(norm2<double>(b, n, S.red, s));
+    XT_TRY(fetch(hb, S.red.out.p, 1));
+    const double bn = std::sqrt(hb[0]);
+    st = GmresStats();
+    if (bn == 0.0) {
+        XT_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        XT_CUDA(cudaStreamSynchronize(s));
+        st.ierr = -1;
+        return XT_OK;
+    }
+    for (;;) {
+        // true residual in FP64
+        XT_CUDA(cudaMemcpyAsync(S.r64.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        XT_TRY(system_apply(S, -1.0, 1.0, x, S.r64.p));
+        XT_TRY(norm2<double>(S.r64.p, n, S.red, s));
+        XT_TRY(fetch(hb, S.red.out.p, 1));
+        const double rn = std::sqrt(hb[0]);
+        st.relres = rn / bn;
+        if (!std::isfinite(rn)) {
+            set_error("solve: non-finite residual");
+            return XT_ERR_NONFINITE;
+        }
+        if (st.relres <= tol) { st.ierr = 0; break; }
+        if (st.its >= maxits) { st.ierr = 1; break; }
+        ++st.outer;
+        const int left = maxits - st.its;
+        const double want = std::max(tol * bn / rn, inner == 1 ? inner_tol : 0.0);
+        GmresStats in;
+        if (inner == 1) {
+            // FP32 inner solve of A d = r / ||r||, then x += ||r|| d in FP64
+            XT_TRY((axpby<double, float>(n, 1.0 / rn, S.r64.p, 0.0, S.r32.p, s)));
+            XT_CUDA(cudaMemsetAsync(S.d32.p, 0, n * sizeof(float), s));
+            XT_TRY(gmres_core<float>(S, S.r32.p, S.d32.p, im, want, left, in, nullptr));
+            XT_TRY((axpby<float, double>(n, rn, S.d32.p, 1.0, x, s)));
+        } else {
+            XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
+            XT_TRY(gmres_core<double>(S, S.r64.p, S.t64.p, im, want, left, in, nullptr));
+            XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
+        }
+        XT_CUDA(cudaStreamSynchronize(s));
+        st.its += in.its;
+        st.cycles += in.cycles;
+        st.est = in.est;
+        if (in.its == 0) { st.ierr = 1; break; }
+    }
+    return XT_OK;
+}
+
+}  // namespace xt

@@ -1,0 +1,77 @@
+// solver.h -- device-resident space-time system and its GMRES solvers.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "xt_device.h"
+
+namespace xt {
+
+// Process-wide device context: the device, one stream, scratch.
+struct Context {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    bool ready = false;
+};
+Context& ctx();
+int ensure_init(int device = -1);
+
+// The operator (A (x) K + B (x) M) with its ILUT preconditioner, resident
+// on the device.  K, M and the factor are uploaded once; the temporal
+// matrices A, B may change every slab.
+struct System {
+    int p = 0, q = 0;
+    DevCsr K, M;
+    std::shared_ptr<DevIlu> ilu;  // may be shared with a factor cache
+    DBuf<double> A, B, Ainv, Cj, Mj;  // q x q each, column-major
+    std::vector<double> hA, hB, hAinv;
+    DBuf<int> bcmask;                 // p entries (0/1), optional
+    // GMRES workspace
+    int im_cap = 0;
+    DBuf<double> V64, z64, w64, u64;
+    DBuf<float> V32, z32, w32, u32, d32, r32;
+    DBuf<double> x64, r64, b64, t64;
+    DBuf<double> hsave;
+    Reduce red;
+};
+
+// Status-returning building blocks
+int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
+                  const int* mi, const int* mj, const double* mv);
+int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group);
+int system_set_temporal(System& S, const double* A, const double* B);
+
+// q x q inverse by LU with partial pivoting (host); returns XT_ERR_SINGULAR.
+int invert_small(int n, const double* A, double* Ainv);
+
+struct GmresStats {
+    int its = 0;         // Arnoldi steps in total
+    int cycles = 0;      // restart cycles
+    int outer = 0;       // refinement passes
+    int ierr = 0;        // 0 converged, 1 maxits, -1 zero residual
+    double relres = 0;   // final true relative residual ||b - A x|| / ||b||
+    double est = 0;      // last Givens estimate relative to the first residual
+};
+
+// kronpgmres semantics (src/kronecker.f90:181-365) on device vectors in the
+// interleaved layout, all in FP64: b and x are device arrays of p*q; x is
+// the initial guess and receives the solution.  b is not modified.
+int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int maxits,
+               GmresStats& st, std::vector<double>* hist);
+
+// Solve to a true relative residual <= tol: FP64 residuals and solution,
+// inner GMRES in precision `inner` (0 = FP64 operator/basis, 1 = FP32
+// operator, factor and basis with FP64 dots and Hessenberg), restarted with
+// the true residual until converged or maxits Arnoldi steps in total.
+int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
+                  int inner, double inner_tol, GmresStats& st);
+
+// y := alpha (A (x) K + B (x) M) x + beta y with the system's current A, B
+// (FP64, interleaved).
+int system_apply(System& S, double alpha, double beta, const double* x, double* y);
+// Same with explicit temporal matrices (device, q x q).
+int system_apply_with(System& S, const double* dA, const double* dB, double alpha, double beta,
+                      const double* x, double* y);
+
+}  // namespace xt

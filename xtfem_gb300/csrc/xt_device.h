@@ -1,0 +1,218 @@
+// xt_device.h -- device-side data structures and kernel launchers of the
+// GB300 space-time solve path (internal to the library).
+//
+// Layout in HBM.  A space-time vector of p spatial DOFs and q temporal
+// blocks is stored node-major ("interleaved"): element (row r, block k) at
+// r*q + k, so the q values a CSR column gathers are contiguous (48 B in
+// FP64, 24 B in FP32 for q = 6).  The reference's block-major layout (block
+// k at k*p + r, src/kronecker.f90:64) is converted at the C-ABI boundary.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "../../include/xtfem_gb300.h"
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace xt {
+
+// ---------------------------------------------------------------- errors
+// Status codes are the public ones of include/xtfem_gb300.h (XT_OK, ...).
+
+void set_error(const std::string& msg);
+const char* last_error();
+// Running count of kernel launches issued by the library.
+void note_launches(int n);
+
+#define XT_CUDA(call)                                                         \
+    do {                                                                      \
+        cudaError_t e_ = (call);                                              \
+        if (e_ != cudaSuccess) {                                              \
+            ::xt::set_error(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+            return XT_ERR_CUDA;                                               \
+        }                                                                     \
+    } while (0)
+
+#define XT_TRY(expr)                        \
+    do {                                    \
+        int s_ = (expr);                    \
+        if (s_ != XT_OK) return s_;         \
+    } while (0)
+
+// Owning device buffer (cudaMalloc / cudaFree).
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    ~DBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    int alloc(size_t count) {
+        if (count == n && p) return XT_OK;
+        release();
+        if (count == 0) return XT_OK;
+        cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            set_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+            return XT_ERR_ALLOC;
+        }
+        n = count;
+        return XT_OK;
+    }
+    int upload(const T* h, size_t count, cudaStream_t s) {
+        XT_TRY(alloc(count));
+        if (count) XT_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        return XT_OK;
+    }
+};
+
+// ------------------------------------------------------ sparse operators
+// 0-based CSR on the device with FP64 values and an FP32 copy.
+struct DevCsr {
+    int n = 0, nnz = 0;
+    DBuf<int> rowptr, col;
+    DBuf<double> v64;
+    DBuf<float> v32;
+};
+
+// FP64 -> FP32 copy on the device.
+int to_f32(const double* a, float* b, size_t n, cudaStream_t s);
+
+// Upload a 1-based host CSR (ia, ja, a) as 0-based device CSR.
+int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
+               cudaStream_t s);
+
+// Y := alpha * (K X A^T + M X B^T) + beta * Y on interleaved p x q blocks.
+// A, B are q x q column-major on the device (FP64).  T is the value/vector
+// type (double or float); accumulation is in T.
+template <class T>
+int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
+              const double* dB, double alpha, double beta, const T* x, T* y,
+              cudaStream_t s);
+
+// -------------------------------------------------- ILU triangular solves
+// Level-scheduled form of a SPARSKIT MSR factor.  Rows are handled in groups
+// of g consecutive rows (g = 3 for three DOFs per node, else 1); a group's
+// level is one more than the deepest group it depends on outside itself, and
+// the rows inside a group are solved in sequence by one warp.
+struct DevTri {
+    int ngroups = 0, nlevels = 0, g = 1;
+    DBuf<int> level_ptr;   // nlevels+1, into the level-ordered group list
+    DBuf<int> group_row0;  // first row of each group, level order
+    DBuf<int> ext_ptr;     // per (group, row-in-group): g*ngroups+1
+    DBuf<int> ext_col;     // external (outside the group) columns
+    DBuf<double> ext_v64;
+    DBuf<float> ext_v32;
+    DBuf<double> int_v64;  // per group g*g internal coefficients
+    DBuf<float> int_v32;
+    DBuf<double> dinv64;   // per group g inverted diagonals (upper only)
+    DBuf<float> dinv32;
+    int max_level_groups = 0;
+};
+
+struct DevIlu {
+    int n = 0;
+    DevTri L, U;
+};
+
+// Build the level schedule from the 1-based MSR arrays and upload it.
+int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju,
+              int group, cudaStream_t s);
+
+// z := (Ainv (x) (LU)^-1) v on interleaved blocks: the q x q mixing with the
+// inverse temporal matrix is applied to v first (it commutes with the
+// spatial solve), then the forward and backward sweeps.  dAinv is q x q
+// column-major FP64 on the device.  work has n*q entries.
+template <class T>
+int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* work,
+              cudaStream_t s);
+
+// ----------------------------------------------------- Krylov vector ops
+// Reduction scratch sized for the largest restart length in use.
+struct Reduce {
+    DBuf<double> partial;  // nblocks * kmax
+    DBuf<double> out;      // kmax
+    int nblocks = 0, kmax = 0;
+};
+int reduce_init(Reduce& r, int kmax);
+
+// h[j] = <V_j, w> for j < k (V column-major, column stride ld), FP64
+// accumulation; result in r.out (device).
+template <class TV>
+int multi_dot(const TV* V, size_t ld, int k, const TV* w, size_t n, Reduce& r,
+              cudaStream_t s);
+// w := w - V h (h on device, FP64), then h2 = V^T w (fused second pass of
+// classical Gram-Schmidt with re-orthogonalisation); result in r.out.
+template <class TV>
+int update_and_dot(const TV* V, size_t ld, int k, const double* h, TV* w, size_t n,
+                   Reduce& r, cudaStream_t s);
+// w := w - V h, then ||w||^2 into r.out[0].
+template <class TV>
+int update_and_norm(const TV* V, size_t ld, int k, const double* h, TV* w, size_t n,
+                    Reduce& r, cudaStream_t s);
+// y := sum_j c[j] V_j (c on device, FP64 accumulation), y of type TY.
+template <class TV, class TY>
+int lincomb(const TV* V, size_t ld, int k, const double* c, TY* y, size_t n,
+            cudaStream_t s);
+// y := a*x (+ y when accumulate); x, y may differ in type.
+template <class TX, class TY>
+int axpby(size_t n, double a, const TX* x, double b, TY* y, cudaStream_t s);
+// ||x||^2 (FP64) into r.out[0].
+template <class T>
+int norm2(const T* x, size_t n, Reduce& r, cudaStream_t s);
+// x[i] = 0 where mask[i / q] is set (BC rows of an interleaved vector, mask
+// over the spatial DOFs).
+template <class T>
+int mask_rows(T* x, const int* mask, int p, int q, cudaStream_t s);
+
+// out[r*q + j] = c[j] * rext[r] (c: q host values) -- the load blocks
+// fextc(j) * rext of src/main3d.f90:807-814 in the interleaved layout.
+int fill_load(const double* rext, const double* c, double* out, int p, int q, cudaStream_t s);
+// max_i x[i] into r.out[0].
+int max_value(const double* x, size_t n, Reduce& r, cudaStream_t s);
+
+// Interleaved <-> block-major conversion (reference layout at the boundary).
+template <class TI, class TO>
+int to_interleaved(const TI* blk, TO* itl, int p, int q, cudaStream_t s);
+template <class TI, class TO>
+int to_blocks(const TI* itl, TO* blk, int p, int q, cudaStream_t s);
+
+// ----------------------------------------------------------------- damage
+struct DamageArgs {
+    int ngp, nn, ndofn, nnse, nnte, ncmp, nip;
+    const int* nodes;            // ngp*nnse, 1-based node ids
+    const double *Nx, *Ny, *Nz;  // ngp*nnse
+    const double* Nt;            // nip*2*nnte (FP64)
+    const float* Nt32;           // nip*2*nnte (FP32 copy for the yield screen)
+    const double* sol;           // block-major space-time solution, 2*nnte*nn*ndofn
+    const double *ym, *nu;       // ngp
+    double *eps_old, *eps_pl, *sig_eff, *sig_back;  // ngp*ncmp
+    double *p, *D, *ws, *del_po, *sig_d;            // ngp
+    const int* gpsta;            // optional: zero D, ws where gpsta == 0
+    unsigned long long* counters;  // optional [3]: plastic, screened, exact steps
+    float* ntmax;                // device scratch, 6 floats (per-slab |Nt_k| bounds)
+};
+int damage_update(const DamageArgs& a, cudaStream_t s);
+
+// Temporal shape table on the device (FP64 and FP32 copies).
+int nt_table_device(int nip, double t0, double t1, double t2, double w, double* Nt64,
+                    float* Nt32, cudaStream_t s);
+
+// chkelesta: flags, ascending failed-element list, count.  D, elesta,
+// gpsta, nefail, nef on device.
+int chkelesta_device(int ne, int ngpe, double Dc, const double* D, int* elesta, int* gpsta,
+                     int* nefail, int* nef, cudaStream_t s);
+
+// any(D >= Dc) over ngp points, result (0/1) into *flag (device).
+int any_ge_device(const double* D, int ngp, double Dc, int* flag, cudaStream_t s);
+
+}  // namespace xt
