@@ -165,6 +165,16 @@ int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
         set_error("upload_csr: row pointers must be 1-based and non-decreasing");
         return XT_ERR_ARG;
     }
+    for (int r = 0; r < n; ++r)
+        if (ia[r + 1] < ia[r]) {
+            set_error("upload_csr: row pointers decrease");
+            return XT_ERR_ARG;
+        }
+    for (int k = 0; k < nnz; ++k)
+        if (ja[k] < 1 || ja[k] > n) {
+            set_error("upload_csr: column index out of range");
+            return XT_ERR_ARG;
+        }
     d.n = n;
     d.nnz = nnz;
     XT_TRY(d.rowptr.upload(ia, (size_t)n + 1, s));
