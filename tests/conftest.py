@@ -30,8 +30,9 @@ def orc():
     return oracle
 
 
-def rod_problem(xt, nx=4, ny=4, nz=12):
-    """The 4x4x12 rod of the C1 mesh (generated; equal to the shipped mesh)."""
+def rod_problem(xt, nx=12, ny=4, nz=4):
+    """The 4x4x12-element rod of the C1 mesh: 12 elements along x over [0, 3],
+    4 x 4 over the unit cross-section (generated; equal to the shipped mesh)."""
     return xt.Problem.rod(nx, ny, nz, 3.0, 1.0, 1.0, 2.0e5, 0.3, 7.8e-9)
 
 

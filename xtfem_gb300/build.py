@@ -56,16 +56,17 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         objs.append(obj)
         if _needs(obj, [src, *headers]):
             cmds.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xcompiler", "-ffp-contract=off",
                          "--expt-relaxed-constexpr", *EXTRA.get(src.name, []),
                          "-c", str(src), "-o", str(obj)])
     for src in cpp:
         obj = OUT / (src.name + ".o")
         objs.append(obj)
         if _needs(obj, [src, *headers]):
-            cmds.append([nvcc, "-x", "cu", *ARCH, "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
-                         "-c", str(src), "-o", str(obj)] if False else
-                        [nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-c", str(src),
-                         "-o", str(obj)])
+            # host code: no FMA contraction, so x86 and Arm hosts assemble
+            # bit-identical K and M
+            cmds.append([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
+                         "-ffp-contract=off", "-c", str(src), "-o", str(obj)])
     jobs = jobs or max(1, min(len(cmds), os.cpu_count() or 4))
 
     def run(cmd):

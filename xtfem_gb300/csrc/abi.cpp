@@ -211,12 +211,17 @@ int xt_system_apply(xt_system h, const double* a, const double* b, double alpha,
     XT_TRY(h->b_in.alloc(64));
     XT_CUDA(cudaMemcpyAsync(h->a_in.p, a, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
     XT_CUDA(cudaMemcpyAsync(h->b_in.p, b, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    trace("apply: temporal matrices staged");
     XT_TRY(ensure_vec(S.x64, n));
     XT_TRY(ensure_vec(S.r64, n));
     XT_TRY(upload_blocks(*h, x, S.x64.p));
+    trace("apply: x uploaded");
     if (beta != 0.0) XT_TRY(upload_blocks(*h, y, S.r64.p));
     XT_TRY(system_apply_with(S, h->a_in.p, h->b_in.p, alpha, beta, S.x64.p, S.r64.p));
-    return download_blocks(*h, S.r64.p, y);
+    trace("apply: operator applied");
+    const int st = download_blocks(*h, S.r64.p, y);
+    trace("apply: y downloaded");
+    return st;
 }
 
 int xt_system_lusol(xt_system h, const double* a, const double* x, double* y)

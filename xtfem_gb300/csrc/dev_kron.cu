@@ -58,12 +58,13 @@ __device__ __forceinline__ void load_row<double, 6>(const double* __restrict__ p
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
 }
 
+// value array of the requested precision (host-side selection)
 template <class T>
-__device__ __forceinline__ const T* vals(const double* v64, const float* v32);
+const T* vals(const double* v64, const float* v32);
 template <>
-__device__ __forceinline__ const double* vals<double>(const double* v64, const float*) { return v64; }
+const double* vals<double>(const double* v64, const float*) { return v64; }
 template <>
-__device__ __forceinline__ const float* vals<float>(const double*, const float* v32) { return v32; }
+const float* vals<float>(const double*, const float* v32) { return v32; }
 
 template <class T, int Q, int LANES>
 __global__ void __launch_bounds__(256)

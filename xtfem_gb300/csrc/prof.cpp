@@ -6,6 +6,8 @@
 // duration of the dominant kernel inside the timed region.
 #include "prof.h"
 
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "../../include/xtfem_gb300_host.h"
@@ -103,6 +105,16 @@ cudaEvent_t g_marks[8] = {nullptr};
 }  // namespace
 
 void note_launches(int n) { g_launches += n; }
+
+void trace(const char* what)
+{
+    static int on = -1;
+    if (on < 0) on = std::getenv("XTFEM_TRACE") ? 1 : 0;
+    if (!on) return;
+    cudaError_t e = cudaDeviceSynchronize();
+    std::fprintf(stderr, "[xtfem] %s: %s\n", what, cudaGetErrorString(e));
+    std::fflush(stderr);
+}
 
 }  // namespace xt
 

@@ -25,6 +25,9 @@ void set_error(const std::string& msg);
 const char* last_error();
 // Running count of kernel launches issued by the library.
 void note_launches(int n);
+// Diagnostics: when the environment variable XTFEM_TRACE is set, trace()
+// prints the step and synchronizes the device to surface errors early.
+void trace(const char* what);
 
 #define XT_CUDA(call)                                                         \
     do {                                                                      \
