@@ -415,7 +415,13 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--inner-tol", type=float, default=None)
+    ap.add_argument("--im", type=int, default=None)
     args = ap.parse_args()
+    if args.inner_tol is not None:
+        WORKLOAD["inner_tol"] = args.inner_tol
+    if args.im is not None:
+        WORKLOAD["im"] = args.im
     rank, world = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, rank, world)

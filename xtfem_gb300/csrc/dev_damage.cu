@@ -209,13 +209,74 @@ __device__ void screen_setup(const Mat& m, const State& st, const double E[6][6]
     err2 = (float)(e2 + 16.0 * 5.9604644775390625e-8 * tot) * 1.0001f + 1e-30f;
 }
 
-__global__ void __launch_bounds__(128)
+// Everything the rare exact FP64 path needs lives in one per-thread record
+// that only no-inline functions touch, so the FP32 screening loop keeps just
+// its 43 coefficients in registers (occupancy, no spills in the hot loop).
+struct Slow {
+    Mat m;
+    State st;
+    double E[6][6];
+};
+struct Screen {
+    float G[6][6];
+    float C0[6];
+    float err2;
+};
+
+__device__ __noinline__ void slow_screen(const Slow* s, const float* __restrict__ ntmax, Screen* sc)
+{
+    screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+}
+
+__device__ __forceinline__ void strain_at(const Slow* s, const double* __restrict__ Nt, int jj,
+                                          double eps[6])
+{
+    const double* ntr = Nt + (size_t)jj * 6;
+    double w[6];
+    for (int k = 0; k < 6; ++k) w[k] = ntr[k];
+    for (int c = 0; c < 6; ++c) {
+        double acc = 0.0;
+        for (int k = 0; k < 6; ++k) acc = fma(w[k], s->E[k][c], acc);
+        eps[c] = acc;
+    }
+}
+
+// outputs of an elastic step (sig_eff, eps_old, sig_d), reference order
+__device__ __noinline__ void slow_materialize(Slow* s, const double* __restrict__ Nt, int jj)
+{
+    double eps[6], tse[6];
+    strain_at(s, Nt, jj, eps);
+    const double teq = predictor(s->m, s->st.d, eps, s->st.epl, s->st.sbk, tse);
+    for (int i = 0; i < 6; ++i) { s->st.sef[i] = tse[i]; s->st.epo[i] = eps[i]; }
+    s->st.sigd = teq;
+}
+
+// exact FP64 step jj.  Returns 1 when the step was plastic (internal
+// variables changed and the screen was rebuilt), else 0.
+__device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, int jj, int last_el,
+                                      const float* __restrict__ ntmax, Screen* sc)
+{
+    double eps[6], tse[6];
+    strain_at(s, Nt, jj, eps);
+    const double teq = predictor(s->m, s->st.d, eps, s->st.epl, s->st.sbk, tse);
+    if (teq <= SIGF) {
+        for (int i = 0; i < 6; ++i) { s->st.sef[i] = tse[i]; s->st.epo[i] = eps[i]; }
+        s->st.sigd = teq;
+        return 0;
+    }
+    if (last_el >= 0) slow_materialize(s, Nt, last_el);
+    corrector(s->m, eps, s->st);
+    screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+    return 1;
+}
+
+__global__ void __launch_bounds__(256, 4)
 k_damage(DamageArgs a, const float* __restrict__ ntmax)
 {
     const int gp = blockIdx.x * blockDim.x + threadIdx.x;
     if (gp >= a.ngp) return;
-    const int nt = 2 * a.nnte;  // == 6 (checked on the host)
-    Mat m;
+    Slow s;
+    Mat& m = s.m;
     m.nu = a.nu[gp];
     m.E = a.ym[gp];
     m.ca = (1.0 + m.nu) / (3.0 * (1.0 - m.nu));
@@ -224,27 +285,26 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     m.Kb = m.E / (3.0 * (1.0 - 2.0 * m.nu));
     m.coef = m.E / ((1.0 + m.nu) * (1.0 - 2.0 * m.nu));
 
-    // strain basis E_k = B u_k
-    double E[6][6];
+    // strain basis E_k = B u_k (6 temporal blocks, checked on the host)
     for (int k = 0; k < 6; ++k)
-        for (int c = 0; c < 6; ++c) E[k][c] = 0.0;
+        for (int c = 0; c < 6; ++c) s.E[k][c] = 0.0;
     for (int i = 0; i < a.nnse; ++i) {
         const int nd = a.nodes[(size_t)gp * a.nnse + i] - 1;
         const double nx = a.Nx[(size_t)gp * a.nnse + i];
         const double ny = a.Ny[(size_t)gp * a.nnse + i];
         const double nz = a.Nz[(size_t)gp * a.nnse + i];
-        for (int k = 0; k < nt; ++k) {
+        for (int k = 0; k < 6; ++k) {
             const double* u = a.sol + (size_t)k * a.nn * a.ndofn + (size_t)nd * a.ndofn;
             const double u0 = u[0], u1 = u[1], u2 = u[2];
-            E[k][0] += nx * u0;
-            E[k][1] += ny * u1;
-            E[k][2] += nz * u2;
-            E[k][3] += ny * u0 + nx * u1;
-            E[k][4] += nz * u1 + ny * u2;
-            E[k][5] += nz * u0 + nx * u2;
+            s.E[k][0] += nx * u0;
+            s.E[k][1] += ny * u1;
+            s.E[k][2] += nz * u2;
+            s.E[k][3] += ny * u0 + nx * u1;
+            s.E[k][4] += nz * u1 + ny * u2;
+            s.E[k][5] += nz * u0 + nx * u2;
         }
     }
-    State st;
+    State& st = s.st;
     const size_t b6 = (size_t)gp * a.ncmp;
     for (int i = 0; i < 6; ++i) {
         st.epo[i] = a.eps_old[b6 + i];
@@ -258,63 +318,51 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     st.dpo = a.del_po[gp];
     st.sigd = a.sig_d[gp];
 
+    Screen sc;
+    slow_screen(&s, ntmax, &sc);
     float G[6][6], C0[6], err2;
-    screen_setup(m, st, E, ntmax, G, C0, err2);
-    const float sigf2 = (float)(SIGF * SIGF);
-    int last_el = -1;       // last step known elastic whose outputs are pending
-    unsigned long long n_exact = 0, n_plastic = 0;
-
-    auto strain_at = [&](int jj, double eps[6]) {
-        const double* ntr = a.Nt + (size_t)jj * nt;
-        double w[6];
-        for (int k = 0; k < 6; ++k) w[k] = ntr[k];
-        for (int c = 0; c < 6; ++c) {
-            double s = 0.0;
-            for (int k = 0; k < 6; ++k) s = fma(w[k], E[k][c], s);
-            eps[c] = s;
-        }
-    };
-    auto materialize = [&](int jj) {  // outputs of an elastic step
-        double eps[6], tse[6];
-        strain_at(jj, eps);
-        const double teq = predictor(m, st.d, eps, st.epl, st.sbk, tse);
-        for (int i = 0; i < 6; ++i) { st.sef[i] = tse[i]; st.epo[i] = eps[i]; }
-        st.sigd = teq;
-    };
-
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) G[k][i] = sc.G[k][i];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) C0[i] = sc.C0[i];
+    err2 = sc.err2;
+    // proven elastic when q + err2 < sig_f^2 (margin covers the float add)
+    const float thr = (float)(SIGF * SIGF) * 0.99999976f;
+    int last_el = -1;  // last step known elastic whose outputs are pending
+    unsigned n_exact = 0, n_plastic = 0;
+    const float2* nt2 = reinterpret_cast<const float2*>(a.Nt32);
     for (int jj = 0; jj < a.nip; ++jj) {
-        const float2* n2 = reinterpret_cast<const float2*>(a.Nt32 + (size_t)jj * 6);
-        const float2 t0 = __ldg(n2), t1 = __ldg(n2 + 1), t2 = __ldg(n2 + 2);
+        const float2 t0 = __ldg(nt2 + 3 * jj), t1 = __ldg(nt2 + 3 * jj + 1),
+                     t2 = __ldg(nt2 + 3 * jj + 2);
         const float w[6] = {t0.x, t0.y, t1.x, t1.y, t2.x, t2.y};
         float q = 0.0f;
 #pragma unroll
         for (int i = 0; i < 6; ++i) {
-            float s = C0[i];
+            float acc = C0[i];
 #pragma unroll
-            for (int k = 0; k < 6; ++k) s = fmaf(w[k], G[k][i], s);
-            q = fmaf(i < 3 ? 1.5f : 3.0f, s * s, q);
+            for (int k = 0; k < 6; ++k) acc = fmaf(w[k], G[k][i], acc);
+            q = fmaf(i < 3 ? 1.5f : 3.0f, acc * acc, q);
         }
-        if (q + err2 < sigf2 * 0.99999976f) {  // proven elastic (margin covers the float add)
+        if (q + err2 < thr) {
             last_el = jj;
             continue;
         }
-        // undecided or plastic: exact FP64 step
         ++n_exact;
-        double eps[6], tse[6];
-        strain_at(jj, eps);
-        const double teq = predictor(m, st.d, eps, st.epl, st.sbk, tse);
-        if (teq <= SIGF) {
-            for (int i = 0; i < 6; ++i) { st.sef[i] = tse[i]; st.epo[i] = eps[i]; }
-            st.sigd = teq;
-            last_el = -1;
-            continue;
+        if (slow_step(&s, a.Nt, jj, last_el, ntmax, &sc)) {
+            ++n_plastic;
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int i = 0; i < 6; ++i) G[k][i] = sc.G[k][i];
+#pragma unroll
+            for (int i = 0; i < 6; ++i) C0[i] = sc.C0[i];
+            err2 = sc.err2;
         }
-        if (last_el >= 0) { materialize(last_el); last_el = -1; }
-        ++n_plastic;
-        corrector(m, eps, st);
-        screen_setup(m, st, E, ntmax, G, C0, err2);
+        last_el = -1;
     }
-    if (last_el >= 0) materialize(last_el);
+    if (last_el >= 0) slow_materialize(&s, a.Nt, last_el);
 
     if (a.gpsta && a.gpsta[gp] == 0) {  // src/kokkos_damage.f90:102-107
         st.d = 0.0;
@@ -332,9 +380,9 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     a.del_po[gp] = st.dpo;
     a.sig_d[gp] = st.sigd;
     if (a.counters) {
-        atomicAdd(&a.counters[0], n_plastic);
+        atomicAdd(&a.counters[0], (unsigned long long)n_plastic);
         atomicAdd(&a.counters[1], (unsigned long long)a.nip - n_exact);
-        atomicAdd(&a.counters[2], n_exact);
+        atomicAdd(&a.counters[2], (unsigned long long)n_exact);
     }
 }
 
@@ -454,7 +502,7 @@ int damage_update(const DamageArgs& a, cudaStream_t s)
         return XT_ERR_ARG;
     }
     k_ntmax<<<1, 1024, 0, s>>>(a.Nt32, a.nip, a.ntmax);
-    k_damage<<<(a.ngp + 127) / 128, 128, 0, s>>>(a, a.ntmax);
+    k_damage<<<(a.ngp + 255) / 256, 256, 0, s>>>(a, a.ntmax);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

@@ -22,6 +22,8 @@
 //     memory (L2-resident) after the barrier.
 // The kernel is latency-bound (levels x barrier+gather latency), not
 // bandwidth-bound; batching independent systems fills the other SMs.
+#include <cuda_pipeline.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -35,7 +37,7 @@ constexpr int kMaxG = 3;
 
 struct TriHost {
     int ngroups = 0, nlevels = 0, g = 1, maxw = 0;
-    std::vector<int> level_ptr, group_row0, ext_ptr, ext_col;
+    std::vector<int> level_ptr, level_e, group_row0, ext_ptr, ext_col;
     std::vector<double> ext_v, int_v, dinv;
 };
 
@@ -101,6 +103,8 @@ TriHost schedule(int n, const double* alu, const int* jlu, const int* ju, int g,
             if (upper) T.dinv[(size_t)i * g + ri] = alu[r];
         }
     }
+    T.level_e.resize(T.nlevels + 1);
+    for (int l = 0; l <= T.nlevels; ++l) T.level_e[l] = T.ext_ptr[(size_t)T.level_ptr[l] * g];
     return T;
 }
 
@@ -111,6 +115,7 @@ int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
     d.g = h.g;
     d.max_level_groups = h.maxw;
     XT_TRY(d.level_ptr.upload(h.level_ptr.data(), h.level_ptr.size(), s));
+    XT_TRY(d.level_e.upload(h.level_e.data(), h.level_e.size(), s));
     XT_TRY(d.group_row0.upload(h.group_row0.data(), h.group_row0.size(), s));
     XT_TRY(d.ext_ptr.upload(h.ext_ptr.data(), h.ext_ptr.size(), s));
     const size_t ne = h.ext_col.size();
@@ -236,8 +241,196 @@ k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict_
 }
 
 template <class T, int Q>
+int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
+                      cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// Staged sweep.  The factor data of a level does not depend on the solution,
+// so it is copied into a three-deep shared-memory ring with asynchronous
+// copies issued two levels ahead; a level then costs one block barrier plus
+// the gathers of previously solved values, instead of a chain of dependent
+// global loads.  Each (group, temporal block) task is handled by kSub
+// threads that split the group's external nonzeros and reduce with shuffles.
+// Levels larger than the ring (more than kMaxGroups groups or kMaxEnt
+// nonzeros, e.g. the clamped face's identity rows) are read from global
+// memory directly.
+constexpr int kMaxGroups = 64;
+constexpr int kMaxEnt = 4096;
+constexpr int kRing = 3;
+constexpr int kSub = 4;
+constexpr int kLpCap = 2048;
+
+template <class T>
+struct Ring {
+    // byte offsets inside one ring slot
+    static constexpr size_t v_off = 0;                                    // kMaxEnt T
+    static constexpr size_t i_off = v_off + sizeof(T) * kMaxEnt;           // 9*kMaxGroups T
+    static constexpr size_t d_off = i_off + sizeof(T) * 9 * kMaxGroups;    // 3*kMaxGroups T
+    static constexpr size_t c_off = d_off + sizeof(T) * 3 * kMaxGroups;    // kMaxEnt int
+    static constexpr size_t e_off = c_off + sizeof(int) * kMaxEnt;         // 3*kMaxGroups+1 int
+    static constexpr size_t r_off = e_off + sizeof(int) * (3 * kMaxGroups + 4);
+    static constexpr size_t slot = ((r_off + sizeof(int) * kMaxGroups) + 127) / 128 * 128;
+    static constexpr size_t lp_off = kRing * slot;                        // 2*(kLpCap+1) int
+    static constexpr size_t bytes = lp_off + sizeof(int) * 2 * (kLpCap + 1);
+};
+
+template <class T, int Q, bool UPPER>
+__global__ void __launch_bounds__(1024, 1)
+k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __restrict__ dAinv,
+             const T* __restrict__ v, T* x, T* z)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    using R = Ring<T>;
+    __shared__ T sAinv[Q * Q];
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int g = t.g;
+    const int nl = t.nlevels;
+    const bool lp_in_smem = nl + 1 <= kLpCap + 1;
+    int* s_lp = reinterpret_cast<int*>(smem + R::lp_off);
+    int* s_le = s_lp + (kLpCap + 1);
+    for (int i = tid; i < Q * Q; i += nth) sAinv[i] = (T)dAinv[i];
+    if (lp_in_smem)
+        for (int i = tid; i <= nl; i += nth) {
+            s_lp[i] = t.level_ptr[i];
+            s_le[i] = level_e[i];
+        }
+    __syncthreads();
+    const int* lp = lp_in_smem ? s_lp : t.level_ptr;
+    const int* le = lp_in_smem ? s_le : level_e;
+
+    auto staged = [&](int L) {
+        return lp[L + 1] - lp[L] <= kMaxGroups && le[L + 1] - le[L] <= kMaxEnt;
+    };
+    auto prefetch = [&](int L) {
+        if (L < nl && staged(L)) {
+            unsigned char* slot = smem + (size_t)(L % kRing) * R::slot;
+            T* sv = reinterpret_cast<T*>(slot + R::v_off);
+            T* si = reinterpret_cast<T*>(slot + R::i_off);
+            T* sd = reinterpret_cast<T*>(slot + R::d_off);
+            int* sc = reinterpret_cast<int*>(slot + R::c_off);
+            int* se = reinterpret_cast<int*>(slot + R::e_off);
+            int* sr = reinterpret_cast<int*>(slot + R::r_off);
+            const int gb = lp[L], ng = lp[L + 1] - gb;
+            const int e0 = le[L], ne = le[L + 1] - e0;
+            for (int i = tid; i < ne; i += nth) {
+                __pipeline_memcpy_async(sc + i, t.ext_col + e0 + i, sizeof(int));
+                __pipeline_memcpy_async(sv + i, t.ext_v + e0 + i, sizeof(T));
+            }
+            for (int i = tid; i <= ng * g; i += nth)
+                __pipeline_memcpy_async(se + i, t.ext_ptr + (size_t)gb * g + i, sizeof(int));
+            for (int i = tid; i < ng; i += nth)
+                __pipeline_memcpy_async(sr + i, t.group_row0 + gb + i, sizeof(int));
+            for (int i = tid; i < ng * g * g; i += nth)
+                __pipeline_memcpy_async(si + i, t.int_v + (size_t)gb * g * g + i, sizeof(T));
+            if (UPPER)
+                for (int i = tid; i < ng * g; i += nth)
+                    __pipeline_memcpy_async(sd + i, t.dinv + (size_t)gb * g + i, sizeof(T));
+        }
+        __pipeline_commit();
+    };
+
+    prefetch(0);
+    prefetch(1);
+    __pipeline_wait_prior(1);
+    __syncthreads();
+    const int sub = tid % kSub;
+    const int tasks_per_pass = nth / kSub;
+    for (int l = 0; l < nl; ++l) {
+        prefetch(l + 2);
+        const int gb = lp[l], ng = lp[l + 1] - gb;
+        const int e0 = le[l];
+        const bool st = staged(l);
+        const unsigned char* slot = smem + (size_t)(l % kRing) * R::slot;
+        const T* sv = st ? reinterpret_cast<const T*>(slot + R::v_off) : t.ext_v + e0;
+        const int* sc = st ? reinterpret_cast<const int*>(slot + R::c_off) : t.ext_col + e0;
+        const int* se = st ? reinterpret_cast<const int*>(slot + R::e_off) : t.ext_ptr + (size_t)gb * g;
+        const int* sr = st ? reinterpret_cast<const int*>(slot + R::r_off) : t.group_row0 + gb;
+        const T* si = st ? reinterpret_cast<const T*>(slot + R::i_off) : t.int_v + (size_t)gb * g * g;
+        const T* sd = st ? reinterpret_cast<const T*>(slot + R::d_off) : (UPPER ? t.dinv + (size_t)gb * g : nullptr);
+        const int ntask = ng * Q;
+        for (int base = 0; base < ntask; base += tasks_per_pass) {
+            const int task = base + tid / kSub;
+            const bool act = task < ntask;
+            const int gi = act ? task / Q : 0, rhs = act ? task % Q : 0;
+            T acc[kMaxG] = {T(0), T(0), T(0)};
+            if (act) {
+                for (int ri = 0; ri < g; ++ri) {
+                    const int kb = se[gi * g + ri] - e0, ke = se[gi * g + ri + 1] - e0;
+                    T a = T(0);
+                    for (int k = kb + sub; k < ke; k += kSub)
+                        a = fma(sv[k], x[(size_t)sc[k] * Q + rhs], a);
+                    acc[ri] = a;
+                }
+            }
+#pragma unroll
+            for (int off = kSub / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int ri = 0; ri < kMaxG; ++ri)
+                    acc[ri] += __shfl_xor_sync(0xffffffffu, acc[ri], off, kSub);
+            if (act) {
+                const int row0 = sr[gi];
+                const T* iv = si + (size_t)gi * g * g;
+                T sol[kMaxG];
+                for (int s2 = 0; s2 < g; ++s2) {
+                    const int ri = UPPER ? g - 1 - s2 : s2;
+                    const int r = row0 + ri;
+                    T b;
+                    if (!UPPER) {
+                        b = T(0);
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) b = fma(sAinv[j * Q + rhs], __ldg(v + (size_t)r * Q + j), b);
+                    } else {
+                        b = x[(size_t)r * Q + rhs];
+                    }
+                    T val = b - acc[ri];
+                    if (!UPPER) {
+                        for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
+                    } else {
+                        for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
+                        val *= sd[gi * g + ri];
+                    }
+                    sol[ri] = val;
+                }
+                if (sub == 0)
+                    for (int ri = 0; ri < g; ++ri) {
+                        x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                        if (UPPER && z != x) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                    }
+            }
+        }
+        __pipeline_wait_prior(1);
+        __syncthreads();
+    }
+}
+
+template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
                cudaStream_t s)
+{
+    if (F.L.g <= kMaxG && F.U.g <= kMaxG && F.L.level_e.p && F.U.level_e.p) {
+        const size_t bytes = Ring<T>::bytes;
+        static bool attr_set[2] = {false, false};
+        if (!attr_set[0]) {
+            XT_CUDA(cudaFuncSetAttribute(k_tri_staged<T, Q, false>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+            XT_CUDA(cudaFuncSetAttribute(k_tri_staged<T, Q, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+            attr_set[0] = true;
+        }
+        k_tri_staged<T, Q, false><<<1, 1024, bytes, s>>>(view<T>(F.L), F.L.level_e.p, dAinv, v,
+                                                         work, nullptr);
+        k_tri_staged<T, Q, true><<<1, 1024, bytes, s>>>(view<T>(F.U), F.U.level_e.p, dAinv,
+                                                        nullptr, work, z);
+        note_launches(2);
+        XT_CUDA(cudaGetLastError());
+        return XT_OK;
+    }
+    return launch_tri_simple<T, Q>(F, dAinv, v, z, work, s);
+}
+
+template <class T, int Q>
+int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
+                      cudaStream_t s)
 {
     constexpr int S = (32 / Q) >= 32 ? 32 : ((32 / Q) >= 16 ? 16 : ((32 / Q) >= 8 ? 8 : ((32 / Q) >= 4 ? 4 : 2)));
     k_tri_sweep<T, Q, S, false><<<1, 1024, 0, s>>>(view<T>(F.L), dAinv, v, work, nullptr);

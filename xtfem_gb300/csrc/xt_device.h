@@ -110,6 +110,7 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 struct DevTri {
     int ngroups = 0, nlevels = 0, g = 1;
     DBuf<int> level_ptr;   // nlevels+1, into the level-ordered group list
+    DBuf<int> level_e;     // nlevels+1, first external nonzero of each level
     DBuf<int> group_row0;  // first row of each group, level order
     DBuf<int> ext_ptr;     // per (group, row-in-group): g*ngroups+1
     DBuf<int> ext_col;     // external (outside the group) columns
