@@ -22,6 +22,7 @@
 //     memory (L2-resident) after the barrier.
 // The kernel is latency-bound (levels x barrier+gather latency), not
 // bandwidth-bound; batching independent systems fills the other SMs.
+#include <cooperative_groups.h>
 #include <cuda_pipeline.h>
 
 #include <algorithm>
@@ -147,7 +148,7 @@ int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
 
 template <class T>
 struct TriView {
-    int nlevels, g;
+    int nlevels, g, ngroups;
     const int *level_ptr, *group_row0, *ext_ptr, *ext_col;
     const T *ext_v, *int_v, *dinv;
 };
@@ -157,13 +158,13 @@ TriView<T> view(const DevTri& d);
 template <>
 TriView<double> view<double>(const DevTri& d)
 {
-    return {d.nlevels, d.g, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
             d.ext_v64.p, d.int_v64.p, d.dinv64.p};
 }
 template <>
 TriView<float> view<float>(const DevTri& d)
 {
-    return {d.nlevels, d.g, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
             d.ext_v32.p, d.int_v32.p, d.dinv32.p};
 }
 
@@ -403,10 +404,229 @@ k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __rest
     }
 }
 
+// ---------------------------------------------------------------------------
+// Cluster sweep.  One thread-block cluster of C CTAs per temporal block c
+// (Q clusters run side by side).  The cluster keeps column c of the solution
+// in distributed shared memory: group G (g rows) lives in CTA G % C at slot
+// (G / C) * g, so every gather of a solved value is a shared-memory or
+// DSMEM load instead of an L2 round trip, and levels are separated by the
+// cluster barrier.  A warp solves one owned group of the level: its lanes
+// split the group's external nonzeros, reduce the g partial sums with
+// shuffles and lane 0 finishes the g x g internal solve.  Factor data is
+// double-buffered in shared memory with asynchronous copies one level ahead.
+constexpr int kCEnt = 3072;
+constexpr int kCGrp = 64;
+
+template <class T>
+struct CRing {
+    static constexpr size_t v_off = 0;
+    static constexpr size_t i_off = v_off + sizeof(T) * kCEnt;
+    static constexpr size_t d_off = i_off + sizeof(T) * 9 * kCGrp;
+    static constexpr size_t c_off = d_off + sizeof(T) * 3 * kCGrp;
+    static constexpr size_t e_off = c_off + sizeof(int) * kCEnt;
+    static constexpr size_t r_off = e_off + sizeof(int) * (3 * kCGrp + 4);
+    static constexpr size_t slot = ((r_off + sizeof(int) * kCGrp) + 127) / 128 * 128;
+    static constexpr size_t rings = 2 * slot;
+};
+
+template <class T, int Q, bool UPPER>
+__global__ void __launch_bounds__(1024, 1)
+k_tri_cluster(TriView<T> t, const int* __restrict__ level_e, const double* __restrict__ dAinv,
+              const T* __restrict__ v, T* x_io, T* z, int C, int xcap)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ __align__(128) unsigned char smem[];
+    using R = CRing<T>;
+    T* xs = reinterpret_cast<T*>(smem + R::rings);
+    __shared__ T sAinv[Q * Q];
+    const int rank = (int)cluster.block_rank();
+    const int col_c = blockIdx.x / C;  // temporal block handled by this cluster
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarps = nth >> 5;
+    const int g = t.g, nl = t.nlevels;
+    const int* lp = t.level_ptr;
+    const int* le = level_e;
+    for (int i = tid; i < Q * Q; i += nth) sAinv[i] = (T)dAinv[i];
+    // owned slice of the solution: rows of groups G = rank, rank + C, ...
+    const int ngroups = t.ngroups;
+    if (UPPER)
+        for (int i = tid; i < xcap; i += nth) {
+            const int G = (i / g) * C + rank, ri = i % g;
+            xs[i] = (G < ngroups) ? x_io[(size_t)(G * g + ri) * Q + col_c] : T(0);
+        }
+    T* xr[8];
+    for (int r = 0; r < C; ++r) xr[r] = cluster.map_shared_rank(xs, r);
+
+    auto staged = [&](int L) {
+        return lp[L + 1] - lp[L] <= kCGrp && le[L + 1] - le[L] <= kCEnt;
+    };
+    auto prefetch = [&](int L) {
+        if (L < nl && staged(L)) {
+            unsigned char* slot = smem + (size_t)(L & 1) * R::slot;
+            T* sv = reinterpret_cast<T*>(slot + R::v_off);
+            T* si = reinterpret_cast<T*>(slot + R::i_off);
+            T* sd = reinterpret_cast<T*>(slot + R::d_off);
+            int* sc = reinterpret_cast<int*>(slot + R::c_off);
+            int* se = reinterpret_cast<int*>(slot + R::e_off);
+            int* sr = reinterpret_cast<int*>(slot + R::r_off);
+            const int gb = lp[L], ng = lp[L + 1] - gb;
+            const int e0 = le[L], ne = le[L + 1] - e0;
+            for (int i = tid; i < ne; i += nth) {
+                __pipeline_memcpy_async(sc + i, t.ext_col + e0 + i, sizeof(int));
+                __pipeline_memcpy_async(sv + i, t.ext_v + e0 + i, sizeof(T));
+            }
+            for (int i = tid; i <= ng * g; i += nth)
+                __pipeline_memcpy_async(se + i, t.ext_ptr + (size_t)gb * g + i, sizeof(int));
+            for (int i = tid; i < ng; i += nth)
+                __pipeline_memcpy_async(sr + i, t.group_row0 + gb + i, sizeof(int));
+            for (int i = tid; i < ng * g * g; i += nth)
+                __pipeline_memcpy_async(si + i, t.int_v + (size_t)gb * g * g + i, sizeof(T));
+            if (UPPER)
+                for (int i = tid; i < ng * g; i += nth)
+                    __pipeline_memcpy_async(sd + i, t.dinv + (size_t)gb * g + i, sizeof(T));
+        }
+        __pipeline_commit();
+    };
+    auto xval = [&](int col) -> T {
+        const int G = col / g;
+        return xr[G % C][(G / C) * g + (col - G * g)];
+    };
+
+    prefetch(0);
+    __pipeline_wait_prior(0);
+    cluster.sync();
+    for (int l = 0; l < nl; ++l) {
+        prefetch(l + 1);
+        const int gb = lp[l], ng = lp[l + 1] - gb;
+        const int e0 = le[l];
+        const bool st = staged(l);
+        const unsigned char* slot = smem + (size_t)(l & 1) * R::slot;
+        const T* sv = st ? reinterpret_cast<const T*>(slot + R::v_off) : t.ext_v + e0;
+        const int* sc = st ? reinterpret_cast<const int*>(slot + R::c_off) : t.ext_col + e0;
+        const int* se = st ? reinterpret_cast<const int*>(slot + R::e_off) : t.ext_ptr + (size_t)gb * g;
+        const int* sr = st ? reinterpret_cast<const int*>(slot + R::r_off) : t.group_row0 + gb;
+        const T* si = st ? reinterpret_cast<const T*>(slot + R::i_off) : t.int_v + (size_t)gb * g * g;
+        const T* sd = st ? reinterpret_cast<const T*>(slot + R::d_off)
+                         : (UPPER ? t.dinv + (size_t)gb * g : nullptr);
+        for (int gl = warp; gl < ng; gl += nwarps) {  // warp-uniform
+            const int row0 = sr[gl];
+            const int G = row0 / g;
+            if (G % C != rank) continue;
+            // right-hand side values of the group's rows, loaded early
+            T vv = T(0);
+            if (!UPPER && lane < g * Q) vv = __ldg(v + (size_t)(row0 + lane / Q) * Q + lane % Q);
+            const int kb = se[gl * g] - e0, ke = se[gl * g + g] - e0;
+            const int b1 = g > 1 ? se[gl * g + 1] - e0 : ke, b2 = g > 2 ? se[gl * g + 2] - e0 : ke;
+            T a0 = T(0), a1 = T(0), a2 = T(0);
+            for (int k = kb + lane; k < ke; k += 32) {
+                const T prod = sv[k] * xval(sc[k]);
+                if (k < b1) a0 += prod;
+                else if (k < b2) a1 += prod;
+                else a2 += prod;
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, off);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
+                a2 += __shfl_xor_sync(0xffffffffu, a2, off);
+            }
+            T bq[kMaxG];
+#pragma unroll
+            for (int ri = 0; ri < kMaxG; ++ri) {
+                T b = T(0);
+                if (!UPPER) {
+#pragma unroll
+                    for (int j = 0; j < Q; ++j)
+                        b = fma(sAinv[j * Q + col_c], __shfl_sync(0xffffffffu, vv, ri * Q + j), b);
+                }
+                bq[ri] = b;
+            }
+            if (lane == 0) {
+                const T acc[kMaxG] = {a0, a1, a2};
+                const T* iv = si + (size_t)gl * g * g;
+                T* mine = xs + (G / C) * g;
+                T sol[kMaxG];
+                for (int s2 = 0; s2 < g; ++s2) {
+                    const int ri = UPPER ? g - 1 - s2 : s2;
+                    T val = (UPPER ? mine[ri] : bq[ri]) - acc[ri];
+                    if (!UPPER) {
+                        for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
+                    } else {
+                        for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
+                        val *= sd[gl * g + ri];
+                    }
+                    sol[ri] = val;
+                }
+                for (int ri = 0; ri < g; ++ri) mine[ri] = sol[ri];
+            }
+        }
+        __pipeline_wait_prior(0);
+        cluster.sync();
+    }
+    // owned rows out: forward result to x_io, backward result to z
+    T* out = UPPER ? z : x_io;
+    for (int i = tid; i < xcap; i += nth) {
+        const int G = (i / g) * C + rank, ri = i % g;
+        if (G < ngroups) out[(size_t)(G * g + ri) * Q + col_c] = xs[i];
+    }
+}
+
+template <class T, int Q>
+int launch_tri_cluster(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
+                       cudaStream_t s, bool& launched)
+{
+    launched = false;
+    const int g = F.L.g;
+    const size_t limit = 227 * 1024 - 1024;
+    int C = 0;
+    for (int c = 1; c <= 8; c *= 2) {
+        const size_t xcap = (size_t)((F.L.ngroups + c - 1) / c) * g;
+        if (CRing<T>::rings + xcap * sizeof(T) <= limit) { C = c; break; }
+    }
+    if (C == 0) return XT_OK;
+    const int xcap = ((F.L.ngroups + C - 1) / C) * g;
+    const size_t bytes = CRing<T>::rings + (size_t)xcap * sizeof(T);
+    static bool attr = false;
+    if (!attr) {
+        XT_CUDA(cudaFuncSetAttribute(k_tri_cluster<T, Q, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+        XT_CUDA(cudaFuncSetAttribute(k_tri_cluster<T, Q, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+        attr = true;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(Q * C, 1, 1);
+    cfg.blockDim = dim3(1024, 1, 1);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    XT_CUDA(cudaLaunchKernelEx(&cfg, k_tri_cluster<T, Q, false>, view<T>(F.L),
+                               (const int*)F.L.level_e.p, dAinv, v, work, (T*)nullptr, C, xcap));
+    XT_CUDA(cudaLaunchKernelEx(&cfg, k_tri_cluster<T, Q, true>, view<T>(F.U),
+                               (const int*)F.U.level_e.p, dAinv, (const T*)nullptr, work, z, C,
+                               xcap));
+    note_launches(2);
+    launched = true;
+    return XT_OK;
+}
+
 template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
                cudaStream_t s)
 {
+    if (F.L.g <= kMaxG && F.U.g == F.L.g && F.L.level_e.p && F.U.level_e.p &&
+        F.L.ngroups == F.U.ngroups) {
+        bool launched = false;
+        XT_TRY((launch_tri_cluster<T, Q>(F, dAinv, v, z, work, s, launched)));
+        if (launched) return XT_OK;
+    }
     if (F.L.g <= kMaxG && F.U.g <= kMaxG && F.L.level_e.p && F.U.level_e.p) {
         const size_t bytes = Ring<T>::bytes;
         static bool attr_set[2] = {false, false};
