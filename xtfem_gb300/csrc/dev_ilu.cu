@@ -259,6 +259,7 @@ constexpr int kMaxGroups = 64;
 constexpr int kMaxEnt = 4096;
 constexpr int kRing = 3;
 constexpr int kSub = 4;
+constexpr int kBatch = 8;  // gathers in flight per lane and batch
 constexpr int kLpCap = 2048;
 
 template <class T>
@@ -353,37 +354,67 @@ k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __rest
             const int task = base + tid / kSub;
             const bool act = task < ntask;
             const int gi = act ? task / Q : 0, rhs = act ? task % Q : 0;
-            T acc[kMaxG] = {T(0), T(0), T(0)};
+            const int row0 = act ? sr[gi] : 0;
+            // right-hand side of row (row0 + sub), issued before the gathers so
+            // its latency overlaps them: forward = Ainv-mixed v, backward = the
+            // forward result
+            T bmine = T(0);
+            if (act && sub < g) {
+                const int r = row0 + sub;
+                if (!UPPER) {
+#pragma unroll
+                    for (int j = 0; j < Q; ++j)
+                        bmine = fma(sAinv[j * Q + rhs], __ldg(v + (size_t)r * Q + j), bmine);
+                } else {
+                    bmine = x[(size_t)r * Q + rhs];
+                }
+            }
+            // the group's external nonzeros are contiguous over its g rows;
+            // each of the kSub lanes takes every kSub-th one, all gathers of a
+            // batch are issued before any is consumed
+            T a0 = T(0), a1 = T(0), a2 = T(0);
             if (act) {
-                for (int ri = 0; ri < g; ++ri) {
-                    const int kb = se[gi * g + ri] - e0, ke = se[gi * g + ri + 1] - e0;
-                    T a = T(0);
-                    for (int k = kb + sub; k < ke; k += kSub)
-                        a = fma(sv[k], x[(size_t)sc[k] * Q + rhs], a);
-                    acc[ri] = a;
+                const int kb = se[gi * g] - e0, ke = se[gi * g + g] - e0;
+                const int b1 = g > 1 ? se[gi * g + 1] - e0 : ke;
+                const int b2 = g > 2 ? se[gi * g + 2] - e0 : ke;
+                for (int k0 = kb + sub; k0 < ke; k0 += kBatch * kSub) {
+                    int cix[kBatch];
+                    T cv[kBatch], xv[kBatch];
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int k = k0 + u * kSub;
+                        const bool ok = k < ke;
+                        cix[u] = ok ? sc[k] : 0;
+                        cv[u] = ok ? sv[k] : T(0);
+                    }
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) xv[u] = x[(size_t)cix[u] * Q + rhs];
+#pragma unroll
+                    for (int u = 0; u < kBatch; ++u) {
+                        const int k = k0 + u * kSub;
+                        const T pr = cv[u] * xv[u];
+                        if (k < b1) a0 += pr;
+                        else if (k < b2) a1 += pr;
+                        else a2 += pr;
+                    }
                 }
             }
 #pragma unroll
-            for (int off = kSub / 2; off > 0; off >>= 1)
+            for (int off = kSub / 2; off > 0; off >>= 1) {
+                a0 += __shfl_xor_sync(0xffffffffu, a0, off, kSub);
+                a1 += __shfl_xor_sync(0xffffffffu, a1, off, kSub);
+                a2 += __shfl_xor_sync(0xffffffffu, a2, off, kSub);
+            }
+            T bq[kMaxG];
 #pragma unroll
-                for (int ri = 0; ri < kMaxG; ++ri)
-                    acc[ri] += __shfl_xor_sync(0xffffffffu, acc[ri], off, kSub);
+            for (int ri = 0; ri < kMaxG; ++ri) bq[ri] = __shfl_sync(0xffffffffu, bmine, ri, kSub);
             if (act) {
-                const int row0 = sr[gi];
+                const T acc[kMaxG] = {a0, a1, a2};
                 const T* iv = si + (size_t)gi * g * g;
                 T sol[kMaxG];
                 for (int s2 = 0; s2 < g; ++s2) {
                     const int ri = UPPER ? g - 1 - s2 : s2;
-                    const int r = row0 + ri;
-                    T b;
-                    if (!UPPER) {
-                        b = T(0);
-#pragma unroll
-                        for (int j = 0; j < Q; ++j) b = fma(sAinv[j * Q + rhs], __ldg(v + (size_t)r * Q + j), b);
-                    } else {
-                        b = x[(size_t)r * Q + rhs];
-                    }
-                    T val = b - acc[ri];
+                    T val = bq[ri] - acc[ri];
                     if (!UPPER) {
                         for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
                     } else {
@@ -621,12 +652,6 @@ template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
                cudaStream_t s)
 {
-    if (F.L.g <= kMaxG && F.U.g == F.L.g && F.L.level_e.p && F.U.level_e.p &&
-        F.L.ngroups == F.U.ngroups) {
-        bool launched = false;
-        XT_TRY((launch_tri_cluster<T, Q>(F, dAinv, v, z, work, s, launched)));
-        if (launched) return XT_OK;
-    }
     if (F.L.g <= kMaxG && F.U.g <= kMaxG && F.L.level_e.p && F.U.level_e.p) {
         const size_t bytes = Ring<T>::bytes;
         static bool attr_set[2] = {false, false};
