@@ -36,6 +36,7 @@ namespace {
 constexpr double CY = 1740.0, HH = 0.2, SD = 0.5, SEXP = 0.5, SIGF = 180.0, SIGU = 577.0,
                  EPSD = 0.08;
 constexpr double WD = (SIGU - SIGF) * EPSD;
+constexpr int kNtChunk = 1024;  // temporal points per shared-memory chunk
 
 struct Mat {
     double nu, E, ca, cb, G, Kb, coef;
@@ -270,11 +271,13 @@ __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, in
     return 1;
 }
 
-__global__ void __launch_bounds__(256, 4)
+__global__ void __launch_bounds__(256)
 k_damage(DamageArgs a, const float* __restrict__ ntmax)
 {
-    const int gp = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gp >= a.ngp) return;
+    // threads past the last point run a copy of it (they must reach the
+    // block barriers of the chunk loop) and store nothing
+    const bool live = (int)(blockIdx.x * blockDim.x + threadIdx.x) < a.ngp;
+    const int gp = live ? (int)(blockIdx.x * blockDim.x + threadIdx.x) : a.ngp - 1;
     Slow s;
     Mat& m = s.m;
     m.nu = a.nu[gp];
@@ -332,10 +335,19 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     const float thr = (float)(SIGF * SIGF) * 0.99999976f;
     int last_el = -1;  // last step known elastic whose outputs are pending
     unsigned n_exact = 0, n_plastic = 0;
+    // The FP32 shape table is shared by every point: the block streams it
+    // through shared memory in chunks, so each step's six values are a
+    // broadcast shared-memory read instead of an L2 round trip.
+    __shared__ float2 sNt[3 * kNtChunk];
     const float2* nt2 = reinterpret_cast<const float2*>(a.Nt32);
-    for (int jj = 0; jj < a.nip; ++jj) {
-        const float2 t0 = __ldg(nt2 + 3 * jj), t1 = __ldg(nt2 + 3 * jj + 1),
-                     t2 = __ldg(nt2 + 3 * jj + 2);
+    for (int j0 = 0; j0 < a.nip; j0 += kNtChunk) {
+    const int jn = min(kNtChunk, a.nip - j0);
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * jn; i += blockDim.x) sNt[i] = __ldg(nt2 + 3 * (size_t)j0 + i);
+    __syncthreads();
+    for (int jq = 0; jq < jn; ++jq) {
+        const int jj = j0 + jq;
+        const float2 t0 = sNt[3 * jq], t1 = sNt[3 * jq + 1], t2 = sNt[3 * jq + 2];
         const float w[6] = {t0.x, t0.y, t1.x, t1.y, t2.x, t2.y};
         float q = 0.0f;
 #pragma unroll
@@ -362,7 +374,9 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
         }
         last_el = -1;
     }
+    }
     if (last_el >= 0) slow_materialize(&s, a.Nt, last_el);
+    if (!live) return;
 
     if (a.gpsta && a.gpsta[gp] == 0) {  // src/kokkos_damage.f90:102-107
         st.d = 0.0;

@@ -6,26 +6,30 @@
 // upper factor and inverted diagonal, for each of the q temporal blocks.
 //
 // The factor is computed on the host (ILUT, FP64) and arrives in MSR form.
-// Triangular solves are chains of dependent rows, so the work is organised
-// by level sets computed once per factor:
+// A triangular solve is a chain of dependent rows, so it is organised by
+// level sets computed once per factor:
 //   * rows are grouped by node (g = 3 consecutive DOFs); a group's level is
-//     one more than the deepest other group it reads, and one warp solves
-//     the g rows of a group in sequence, which roughly halves the number of
-//     levels compared with single-row levels on C3D8 meshes;
-//   * all q right-hand sides of a row are solved together: lanes are split
-//     into q segments of S lanes, each segment walks the row's external
-//     nonzeros for one temporal block and reduces with shuffles;
-//   * the q x q mixing with A^-1 is applied to v on the fly while the
-//     forward sweep reads it (the mixing commutes with the spatial solve);
-//   * one thread block runs all levels of a sweep with a block barrier
-//     between levels; values solved earlier are read back from global
-//     memory (L2-resident) after the barrier.
-// The kernel is latency-bound (levels x barrier+gather latency), not
-// bandwidth-bound; batching independent systems fills the other SMs.
-#include <cooperative_groups.h>
+//     one more than the deepest other group it reads, and the g rows of a
+//     group are solved in sequence by the same threads, which halves the
+//     level count of C3D8 stiffness factors compared with row levels;
+//   * everything a level needs -- the external nonzeros (column, value), the
+//     group rows, the row pointers, the g x g in-group coefficients and the
+//     inverted diagonal -- is packed into one 16-byte-aligned blob per level,
+//     so a level is fetched with a handful of 16-byte asynchronous copies
+//     into a three-deep shared-memory ring, two levels ahead of use;
+//   * one (group, temporal block) task is handled by two lanes that split
+//     each row's nonzeros; all q temporal blocks of a level run at once;
+//   * the q x q mixing with A^-1 is applied to v while the forward sweep
+//     reads it (the mixing commutes with the spatial solve);
+//   * one thread block runs all levels of a sweep with one block barrier per
+//     level; values solved in earlier levels are read back through L1/L2.
+// A single SM runs the sweep: the kernel is bound by the level count times
+// the per-level latency (barrier, gathers) and by instruction issue, not by
+// HBM bandwidth.  Independent systems (batches) fill the other SMs.
 #include <cuda_pipeline.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "xt_device.h"
@@ -38,7 +42,7 @@ constexpr int kMaxG = 3;
 
 struct TriHost {
     int ngroups = 0, nlevels = 0, g = 1, maxw = 0;
-    std::vector<int> level_ptr, level_e, group_row0, ext_ptr, ext_col;
+    std::vector<int> level_ptr, group_row0, ext_ptr, ext_col;
     std::vector<double> ext_v, int_v, dinv;
 };
 
@@ -104,9 +108,70 @@ TriHost schedule(int n, const double* alu, const int* jlu, const int* ju, int g,
             if (upper) T.dinv[(size_t)i * g + ri] = alu[r];
         }
     }
-    T.level_e.resize(T.nlevels + 1);
-    for (int l = 0; l <= T.nlevels; ++l) T.level_e[l] = T.ext_ptr[(size_t)T.level_ptr[l] * g];
     return T;
+}
+
+// Per-level blob layout (all sections 16-byte aligned, offsets in bytes):
+//   cols  ne ints | vals ne T | row0 ng ints | eptr ng*g+1 ints (relative
+//   to the level's first nonzero) | intv ng*g*g T | dinv ng*g T (upper)
+struct BlobDesc {
+    int off16;  // blob start in 16-byte units
+    int len16;  // blob length in 16-byte units
+    int ng;     // groups in the level
+    int ne;     // external nonzeros in the level
+};
+
+template <class T>
+struct BlobLayout {
+    size_t cols, vals, row0, eptr, intv, dinv, bytes;
+    __host__ __device__ BlobLayout(int ne, int ng, int g)
+    {
+        cols = 0;
+        vals = up16(cols + sizeof(int) * (size_t)ne);
+        row0 = up16(vals + sizeof(T) * (size_t)ne);
+        eptr = up16(row0 + sizeof(int) * (size_t)ng);
+        intv = up16(eptr + sizeof(int) * ((size_t)ng * g + 1));
+        dinv = up16(intv + sizeof(T) * (size_t)ng * g * g);
+        bytes = up16(dinv + sizeof(T) * (size_t)ng * g);
+    }
+    __host__ __device__ static size_t up16(size_t b) { return (b + 15) / 16 * 16; }
+};
+
+template <class T>
+void build_blobs(const TriHost& h, std::vector<unsigned char>& blob, std::vector<BlobDesc>& desc)
+{
+    const int g = h.g;
+    desc.resize(h.nlevels);
+    size_t total = 0;
+    for (int l = 0; l < h.nlevels; ++l) {
+        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
+        const int e0 = h.ext_ptr[(size_t)gb * g], ne = h.ext_ptr[(size_t)(gb + ng) * g] - e0;
+        BlobLayout<T> L(ne, ng, g);
+        desc[l] = {(int)(total / 16), (int)(L.bytes / 16), ng, ne};
+        total += L.bytes;
+    }
+    blob.assign(total, 0);
+    for (int l = 0; l < h.nlevels; ++l) {
+        const int gb = h.level_ptr[l], ng = desc[l].ng, ne = desc[l].ne;
+        const int e0 = h.ext_ptr[(size_t)gb * g];
+        BlobLayout<T> L(ne, ng, g);
+        unsigned char* b = blob.data() + (size_t)desc[l].off16 * 16;
+        int* cols = reinterpret_cast<int*>(b + L.cols);
+        T* vals = reinterpret_cast<T*>(b + L.vals);
+        int* row0 = reinterpret_cast<int*>(b + L.row0);
+        int* eptr = reinterpret_cast<int*>(b + L.eptr);
+        T* intv = reinterpret_cast<T*>(b + L.intv);
+        T* dinv = reinterpret_cast<T*>(b + L.dinv);
+        for (int k = 0; k < ne; ++k) {
+            cols[k] = h.ext_col[(size_t)e0 + k];
+            vals[k] = (T)h.ext_v[(size_t)e0 + k];
+        }
+        for (int i = 0; i < ng; ++i) row0[i] = h.group_row0[(size_t)gb + i];
+        for (int i = 0; i <= ng * g; ++i) eptr[i] = h.ext_ptr[(size_t)gb * g + i] - e0;
+        for (int i = 0; i < ng * g * g; ++i) intv[i] = (T)h.int_v[(size_t)gb * g * g + i];
+        if (!h.dinv.empty())
+            for (int i = 0; i < ng * g; ++i) dinv[i] = (T)h.dinv[(size_t)gb * g + i];
+    }
 }
 
 int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
@@ -116,33 +181,30 @@ int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
     d.g = h.g;
     d.max_level_groups = h.maxw;
     XT_TRY(d.level_ptr.upload(h.level_ptr.data(), h.level_ptr.size(), s));
-    XT_TRY(d.level_e.upload(h.level_e.data(), h.level_e.size(), s));
     XT_TRY(d.group_row0.upload(h.group_row0.data(), h.group_row0.size(), s));
     XT_TRY(d.ext_ptr.upload(h.ext_ptr.data(), h.ext_ptr.size(), s));
     const size_t ne = h.ext_col.size();
-    if (ne) {
-        XT_TRY(d.ext_col.upload(h.ext_col.data(), ne, s));
-        XT_TRY(d.ext_v64.upload(h.ext_v.data(), ne, s));
-        std::vector<float> f(h.ext_v.begin(), h.ext_v.end());
-        XT_TRY(d.ext_v32.upload(f.data(), ne, s));
-        XT_CUDA(cudaStreamSynchronize(s));  // f goes out of scope
-    } else {
-        XT_TRY(d.ext_col.alloc(1));
-        XT_TRY(d.ext_v64.alloc(1));
-        XT_TRY(d.ext_v32.alloc(1));
-    }
+    std::vector<float> f32(h.ext_v.begin(), h.ext_v.end());
+    std::vector<float> i32(h.int_v.begin(), h.int_v.end());
+    std::vector<float> d32(h.dinv.begin(), h.dinv.end());
+    XT_TRY(d.ext_col.upload(ne ? h.ext_col.data() : nullptr, ne ? ne : 0, s));
+    XT_TRY(d.ext_v64.upload(h.ext_v.data(), ne, s));
+    XT_TRY(d.ext_v32.upload(f32.data(), ne, s));
     XT_TRY(d.int_v64.upload(h.int_v.data(), h.int_v.size(), s));
-    {
-        std::vector<float> f(h.int_v.begin(), h.int_v.end());
-        XT_TRY(d.int_v32.upload(f.data(), f.size(), s));
-        XT_CUDA(cudaStreamSynchronize(s));
-    }
+    XT_TRY(d.int_v32.upload(i32.data(), i32.size(), s));
     if (!h.dinv.empty()) {
         XT_TRY(d.dinv64.upload(h.dinv.data(), h.dinv.size(), s));
-        std::vector<float> f(h.dinv.begin(), h.dinv.end());
-        XT_TRY(d.dinv32.upload(f.data(), f.size(), s));
-        XT_CUDA(cudaStreamSynchronize(s));
+        XT_TRY(d.dinv32.upload(d32.data(), d32.size(), s));
     }
+    std::vector<unsigned char> b64, b32;
+    std::vector<BlobDesc> e64, e32;
+    build_blobs<double>(h, b64, e64);
+    build_blobs<float>(h, b32, e32);
+    XT_TRY(d.blob64.upload(b64.data(), b64.size(), s));
+    XT_TRY(d.blob32.upload(b32.data(), b32.size(), s));
+    XT_TRY(d.desc64.upload(reinterpret_cast<const int*>(e64.data()), e64.size() * 4, s));
+    XT_TRY(d.desc32.upload(reinterpret_cast<const int*>(e32.data()), e32.size() * 4, s));
+    XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     return XT_OK;
 }
 
@@ -151,6 +213,8 @@ struct TriView {
     int nlevels, g, ngroups;
     const int *level_ptr, *group_row0, *ext_ptr, *ext_col;
     const T *ext_v, *int_v, *dinv;
+    const unsigned char* blob;
+    const BlobDesc* desc;
 };
 
 template <class T>
@@ -159,19 +223,20 @@ template <>
 TriView<double> view<double>(const DevTri& d)
 {
     return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
-            d.ext_v64.p, d.int_v64.p, d.dinv64.p};
+            d.ext_v64.p, d.int_v64.p, d.dinv64.p, d.blob64.p,
+            reinterpret_cast<const BlobDesc*>(d.desc64.p)};
 }
 template <>
 TriView<float> view<float>(const DevTri& d)
 {
     return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
-            d.ext_v32.p, d.int_v32.p, d.dinv32.p};
+            d.ext_v32.p, d.int_v32.p, d.dinv32.p, d.blob32.p,
+            reinterpret_cast<const BlobDesc*>(d.desc32.p)};
 }
 
-// One sweep (forward when UPPER == false).  x is read and written by the
-// kernel itself, so it is accessed through plain (coherent) loads.  For the
-// forward sweep the right-hand side is v mixed with Ainv; for the backward
-// sweep it is x itself (the forward result) and the output goes to z.
+// ---------------------------------------------------------------------------
+// Reference-shaped sweep: one warp per group, factor data read from global
+// memory.  Used when the staged sweep cannot be configured.
 template <class T, int Q, int S, bool UPPER>
 __global__ void __launch_bounds__(1024, 1)
 k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v,
@@ -231,9 +296,8 @@ k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict_
                 }
                 if (sub == 0)
                     for (int ri = 0; ri < g; ++ri) {
-                        T* dst = UPPER ? z : x;
-                        dst[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
-                        if (UPPER && z != x) x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                        x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                        if (UPPER && z != x) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
                     }
             }
         }
@@ -241,92 +305,42 @@ k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict_
     }
 }
 
-template <class T, int Q>
-int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
-                      cudaStream_t s);
-
 // ---------------------------------------------------------------------------
-// Staged sweep.  The factor data of a level does not depend on the solution,
-// so it is copied into a three-deep shared-memory ring with asynchronous
-// copies issued two levels ahead; a level then costs one block barrier plus
-// the gathers of previously solved values, instead of a chain of dependent
-// global loads.  Each (group, temporal block) task is handled by kSub
-// threads that split the group's external nonzeros and reduce with shuffles.
-// Levels larger than the ring (more than kMaxGroups groups or kMaxEnt
-// nonzeros, e.g. the clamped face's identity rows) are read from global
-// memory directly.
-constexpr int kMaxGroups = 64;
-constexpr int kMaxEnt = 4096;
+// Staged sweep over per-level blobs (see the file comment).
 constexpr int kRing = 3;
-constexpr int kSub = 4;
-constexpr int kBatch = 8;  // gathers in flight per lane and batch
-constexpr int kLpCap = 2048;
+constexpr int kDescCap = 2048;  // levels whose descriptors are kept in shared memory
 
 template <class T>
-struct Ring {
-    // byte offsets inside one ring slot
-    static constexpr size_t v_off = 0;                                    // kMaxEnt T
-    static constexpr size_t i_off = v_off + sizeof(T) * kMaxEnt;           // 9*kMaxGroups T
-    static constexpr size_t d_off = i_off + sizeof(T) * 9 * kMaxGroups;    // 3*kMaxGroups T
-    static constexpr size_t c_off = d_off + sizeof(T) * 3 * kMaxGroups;    // kMaxEnt int
-    static constexpr size_t e_off = c_off + sizeof(int) * kMaxEnt;         // 3*kMaxGroups+1 int
-    static constexpr size_t r_off = e_off + sizeof(int) * (3 * kMaxGroups + 4);
-    static constexpr size_t slot = ((r_off + sizeof(int) * kMaxGroups) + 127) / 128 * 128;
-    static constexpr size_t lp_off = kRing * slot;                        // 2*(kLpCap+1) int
-    static constexpr size_t bytes = lp_off + sizeof(int) * 2 * (kLpCap + 1);
-};
+constexpr size_t slot_bytes() { return sizeof(T) == 8 ? 49152 : 40960; }
+template <class T>
+constexpr size_t staged_smem() { return kRing * slot_bytes<T>() + sizeof(BlobDesc) * kDescCap; }
 
 template <class T, int Q, bool UPPER>
 __global__ void __launch_bounds__(1024, 1)
-k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __restrict__ dAinv,
-             const T* __restrict__ v, T* x, T* z)
+k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v, T* x, T* z)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    using R = Ring<T>;
     __shared__ T sAinv[Q * Q];
     const int tid = threadIdx.x, nth = blockDim.x;
-    const int g = t.g;
-    const int nl = t.nlevels;
-    const bool lp_in_smem = nl + 1 <= kLpCap + 1;
-    int* s_lp = reinterpret_cast<int*>(smem + R::lp_off);
-    int* s_le = s_lp + (kLpCap + 1);
+    const int g = t.g, nl = t.nlevels;
+    constexpr size_t SLOT = slot_bytes<T>();
+    BlobDesc* sdesc = reinterpret_cast<BlobDesc*>(smem + kRing * SLOT);
+    const bool desc_in_smem = nl <= kDescCap;
     for (int i = tid; i < Q * Q; i += nth) sAinv[i] = (T)dAinv[i];
-    if (lp_in_smem)
-        for (int i = tid; i <= nl; i += nth) {
-            s_lp[i] = t.level_ptr[i];
-            s_le[i] = level_e[i];
-        }
+    if (desc_in_smem)
+        for (int i = tid; i < nl; i += nth) sdesc[i] = t.desc[i];
     __syncthreads();
-    const int* lp = lp_in_smem ? s_lp : t.level_ptr;
-    const int* le = lp_in_smem ? s_le : level_e;
+    const BlobDesc* desc = desc_in_smem ? sdesc : t.desc;
+    const int4* gblob = reinterpret_cast<const int4*>(t.blob);
 
-    auto staged = [&](int L) {
-        return lp[L + 1] - lp[L] <= kMaxGroups && le[L + 1] - le[L] <= kMaxEnt;
-    };
     auto prefetch = [&](int L) {
-        if (L < nl && staged(L)) {
-            unsigned char* slot = smem + (size_t)(L % kRing) * R::slot;
-            T* sv = reinterpret_cast<T*>(slot + R::v_off);
-            T* si = reinterpret_cast<T*>(slot + R::i_off);
-            T* sd = reinterpret_cast<T*>(slot + R::d_off);
-            int* sc = reinterpret_cast<int*>(slot + R::c_off);
-            int* se = reinterpret_cast<int*>(slot + R::e_off);
-            int* sr = reinterpret_cast<int*>(slot + R::r_off);
-            const int gb = lp[L], ng = lp[L + 1] - gb;
-            const int e0 = le[L], ne = le[L + 1] - e0;
-            for (int i = tid; i < ne; i += nth) {
-                __pipeline_memcpy_async(sc + i, t.ext_col + e0 + i, sizeof(int));
-                __pipeline_memcpy_async(sv + i, t.ext_v + e0 + i, sizeof(T));
+        if (L < nl) {
+            const BlobDesc d = desc[L];
+            if ((size_t)d.len16 * 16 <= SLOT) {
+                int4* dst = reinterpret_cast<int4*>(smem + (size_t)(L % kRing) * SLOT);
+                const int4* src = gblob + d.off16;
+                for (int i = tid; i < d.len16; i += nth) __pipeline_memcpy_async(dst + i, src + i, 16);
             }
-            for (int i = tid; i <= ng * g; i += nth)
-                __pipeline_memcpy_async(se + i, t.ext_ptr + (size_t)gb * g + i, sizeof(int));
-            for (int i = tid; i < ng; i += nth)
-                __pipeline_memcpy_async(sr + i, t.group_row0 + gb + i, sizeof(int));
-            for (int i = tid; i < ng * g * g; i += nth)
-                __pipeline_memcpy_async(si + i, t.int_v + (size_t)gb * g * g + i, sizeof(T));
-            if (UPPER)
-                for (int i = tid; i < ng * g; i += nth)
-                    __pipeline_memcpy_async(sd + i, t.dinv + (size_t)gb * g + i, sizeof(T));
         }
         __pipeline_commit();
     };
@@ -335,98 +349,88 @@ k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __rest
     prefetch(1);
     __pipeline_wait_prior(1);
     __syncthreads();
-    const int sub = tid % kSub;
-    const int tasks_per_pass = nth / kSub;
+    const int sub = tid & 1;
+    const int tasks_per_pass = nth >> 1;
     for (int l = 0; l < nl; ++l) {
         prefetch(l + 2);
-        const int gb = lp[l], ng = lp[l + 1] - gb;
-        const int e0 = le[l];
-        const bool st = staged(l);
-        const unsigned char* slot = smem + (size_t)(l % kRing) * R::slot;
-        const T* sv = st ? reinterpret_cast<const T*>(slot + R::v_off) : t.ext_v + e0;
-        const int* sc = st ? reinterpret_cast<const int*>(slot + R::c_off) : t.ext_col + e0;
-        const int* se = st ? reinterpret_cast<const int*>(slot + R::e_off) : t.ext_ptr + (size_t)gb * g;
-        const int* sr = st ? reinterpret_cast<const int*>(slot + R::r_off) : t.group_row0 + gb;
-        const T* si = st ? reinterpret_cast<const T*>(slot + R::i_off) : t.int_v + (size_t)gb * g * g;
-        const T* sd = st ? reinterpret_cast<const T*>(slot + R::d_off) : (UPPER ? t.dinv + (size_t)gb * g : nullptr);
-        const int ntask = ng * Q;
-        for (int base = 0; base < ntask; base += tasks_per_pass) {
-            const int task = base + tid / kSub;
+        const BlobDesc d = desc[l];
+        const unsigned char* base = ((size_t)d.len16 * 16 <= SLOT)
+                                        ? smem + (size_t)(l % kRing) * SLOT
+                                        : t.blob + (size_t)d.off16 * 16;
+        const BlobLayout<T> Lo(d.ne, d.ng, g);
+        const int* cols = reinterpret_cast<const int*>(base + Lo.cols);
+        const T* vals = reinterpret_cast<const T*>(base + Lo.vals);
+        const int* row0s = reinterpret_cast<const int*>(base + Lo.row0);
+        const int* eptr = reinterpret_cast<const int*>(base + Lo.eptr);
+        const T* intv = reinterpret_cast<const T*>(base + Lo.intv);
+        const T* dinv = reinterpret_cast<const T*>(base + Lo.dinv);
+        const int ntask = d.ng * Q;
+        for (int pass = 0; pass < ntask; pass += tasks_per_pass) {
+            const int task = pass + (tid >> 1);
             const bool act = task < ntask;
-            const int gi = act ? task / Q : 0, rhs = act ? task % Q : 0;
-            const int row0 = act ? sr[gi] : 0;
-            // right-hand side of row (row0 + sub), issued before the gathers so
-            // its latency overlaps them: forward = Ainv-mixed v, backward = the
-            // forward result
-            T bmine = T(0);
+            const int gi = act ? task / Q : 0, rhs = act ? task - gi * Q : 0;
+            const int row0 = act ? row0s[gi] : 0;
+            // right-hand sides of rows sub and sub+2 of the group, issued first
+            T bA = T(0), bB = T(0);
             if (act && sub < g) {
-                const int r = row0 + sub;
                 if (!UPPER) {
+                    const T* va = v + (size_t)(row0 + sub) * Q;
 #pragma unroll
-                    for (int j = 0; j < Q; ++j)
-                        bmine = fma(sAinv[j * Q + rhs], __ldg(v + (size_t)r * Q + j), bmine);
+                    for (int j = 0; j < Q; ++j) bA = fma(sAinv[j * Q + rhs], __ldg(va + j), bA);
+                    if (sub + 2 < g) {
+                        const T* vb = v + (size_t)(row0 + sub + 2) * Q;
+#pragma unroll
+                        for (int j = 0; j < Q; ++j) bB = fma(sAinv[j * Q + rhs], __ldg(vb + j), bB);
+                    }
                 } else {
-                    bmine = x[(size_t)r * Q + rhs];
+                    bA = x[(size_t)(row0 + sub) * Q + rhs];
+                    if (sub + 2 < g) bB = x[(size_t)(row0 + sub + 2) * Q + rhs];
                 }
             }
-            // the group's external nonzeros are contiguous over its g rows;
-            // each of the kSub lanes takes every kSub-th one, all gathers of a
-            // batch are issued before any is consumed
-            T a0 = T(0), a1 = T(0), a2 = T(0);
+            T acc[kMaxG] = {T(0), T(0), T(0)};
             if (act) {
-                const int kb = se[gi * g] - e0, ke = se[gi * g + g] - e0;
-                const int b1 = g > 1 ? se[gi * g + 1] - e0 : ke;
-                const int b2 = g > 2 ? se[gi * g + 2] - e0 : ke;
-                for (int k0 = kb + sub; k0 < ke; k0 += kBatch * kSub) {
-                    int cix[kBatch];
-                    T cv[kBatch], xv[kBatch];
 #pragma unroll
-                    for (int u = 0; u < kBatch; ++u) {
-                        const int k = k0 + u * kSub;
-                        const bool ok = k < ke;
-                        cix[u] = ok ? sc[k] : 0;
-                        cv[u] = ok ? sv[k] : T(0);
-                    }
-#pragma unroll
-                    for (int u = 0; u < kBatch; ++u) xv[u] = x[(size_t)cix[u] * Q + rhs];
-#pragma unroll
-                    for (int u = 0; u < kBatch; ++u) {
-                        const int k = k0 + u * kSub;
-                        const T pr = cv[u] * xv[u];
-                        if (k < b1) a0 += pr;
-                        else if (k < b2) a1 += pr;
-                        else a2 += pr;
+                for (int ri = 0; ri < kMaxG; ++ri) {
+                    if (ri < g) {
+                        const int kb = eptr[gi * g + ri], ke = eptr[gi * g + ri + 1];
+                        T a = T(0);
+#pragma unroll 4
+                        for (int k = kb + sub; k < ke; k += 2)
+                            a = fma(vals[k], x[(size_t)cols[k] * Q + rhs], a);
+                        acc[ri] = a;
                     }
                 }
             }
 #pragma unroll
-            for (int off = kSub / 2; off > 0; off >>= 1) {
-                a0 += __shfl_xor_sync(0xffffffffu, a0, off, kSub);
-                a1 += __shfl_xor_sync(0xffffffffu, a1, off, kSub);
-                a2 += __shfl_xor_sync(0xffffffffu, a2, off, kSub);
-            }
-            T bq[kMaxG];
-#pragma unroll
-            for (int ri = 0; ri < kMaxG; ++ri) bq[ri] = __shfl_sync(0xffffffffu, bmine, ri, kSub);
+            for (int ri = 0; ri < kMaxG; ++ri) acc[ri] += __shfl_xor_sync(0xffffffffu, acc[ri], 1);
+            // b of row 0, 1, 2 lives in (lane 0: bA), (lane 1: bA), (lane 0: bB)
+            const T oA = __shfl_xor_sync(0xffffffffu, bA, 1);
+            const T b0 = sub == 0 ? bA : oA, b1 = sub == 0 ? oA : bA;
+            const T b2 = __shfl_sync(0xffffffffu, bB, (threadIdx.x & 31) & ~1);
             if (act) {
-                const T acc[kMaxG] = {a0, a1, a2};
-                const T* iv = si + (size_t)gi * g * g;
+                const T bq[kMaxG] = {b0, b1, b2};
+                const T* iv = intv + (size_t)gi * g * g;
                 T sol[kMaxG];
-                for (int s2 = 0; s2 < g; ++s2) {
-                    const int ri = UPPER ? g - 1 - s2 : s2;
-                    T val = bq[ri] - acc[ri];
-                    if (!UPPER) {
-                        for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
-                    } else {
-                        for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
-                        val *= sd[gi * g + ri];
+#pragma unroll
+                for (int s2 = 0; s2 < kMaxG; ++s2) {
+                    if (s2 < g) {
+                        const int ri = UPPER ? g - 1 - s2 : s2;
+                        T val = bq[ri] - acc[ri];
+                        if (!UPPER) {
+                            for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
+                        } else {
+                            for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
+                            val *= dinv[gi * g + ri];
+                        }
+                        sol[ri] = val;
                     }
-                    sol[ri] = val;
                 }
-                if (sub == 0)
-                    for (int ri = 0; ri < g; ++ri) {
+                // lane 0 stores rows 0 and 2, lane 1 row 1
+#pragma unroll
+                for (int ri = 0; ri < kMaxG; ++ri)
+                    if (ri < g && (ri & 1) == sub) {
                         x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
-                        if (UPPER && z != x) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
+                        if (UPPER) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
                     }
             }
         }
@@ -435,254 +439,35 @@ k_tri_staged(TriView<T> t, const int* __restrict__ level_e, const double* __rest
     }
 }
 
-// ---------------------------------------------------------------------------
-// Cluster sweep.  One thread-block cluster of C CTAs per temporal block c
-// (Q clusters run side by side).  The cluster keeps column c of the solution
-// in distributed shared memory: group G (g rows) lives in CTA G % C at slot
-// (G / C) * g, so every gather of a solved value is a shared-memory or
-// DSMEM load instead of an L2 round trip, and levels are separated by the
-// cluster barrier.  A warp solves one owned group of the level: its lanes
-// split the group's external nonzeros, reduce the g partial sums with
-// shuffles and lane 0 finishes the g x g internal solve.  Factor data is
-// double-buffered in shared memory with asynchronous copies one level ahead.
-constexpr int kCEnt = 3072;
-constexpr int kCGrp = 64;
-
-template <class T>
-struct CRing {
-    static constexpr size_t v_off = 0;
-    static constexpr size_t i_off = v_off + sizeof(T) * kCEnt;
-    static constexpr size_t d_off = i_off + sizeof(T) * 9 * kCGrp;
-    static constexpr size_t c_off = d_off + sizeof(T) * 3 * kCGrp;
-    static constexpr size_t e_off = c_off + sizeof(int) * kCEnt;
-    static constexpr size_t r_off = e_off + sizeof(int) * (3 * kCGrp + 4);
-    static constexpr size_t slot = ((r_off + sizeof(int) * kCGrp) + 127) / 128 * 128;
-    static constexpr size_t rings = 2 * slot;
-};
-
-template <class T, int Q, bool UPPER>
-__global__ void __launch_bounds__(1024, 1)
-k_tri_cluster(TriView<T> t, const int* __restrict__ level_e, const double* __restrict__ dAinv,
-              const T* __restrict__ v, T* x_io, T* z, int C, int xcap)
-{
-    namespace cg = cooperative_groups;
-    cg::cluster_group cluster = cg::this_cluster();
-    extern __shared__ __align__(128) unsigned char smem[];
-    using R = CRing<T>;
-    T* xs = reinterpret_cast<T*>(smem + R::rings);
-    __shared__ T sAinv[Q * Q];
-    const int rank = (int)cluster.block_rank();
-    const int col_c = blockIdx.x / C;  // temporal block handled by this cluster
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nwarps = nth >> 5;
-    const int g = t.g, nl = t.nlevels;
-    const int* lp = t.level_ptr;
-    const int* le = level_e;
-    for (int i = tid; i < Q * Q; i += nth) sAinv[i] = (T)dAinv[i];
-    // owned slice of the solution: rows of groups G = rank, rank + C, ...
-    const int ngroups = t.ngroups;
-    if (UPPER)
-        for (int i = tid; i < xcap; i += nth) {
-            const int G = (i / g) * C + rank, ri = i % g;
-            xs[i] = (G < ngroups) ? x_io[(size_t)(G * g + ri) * Q + col_c] : T(0);
-        }
-    T* xr[8];
-    for (int r = 0; r < C; ++r) xr[r] = cluster.map_shared_rank(xs, r);
-
-    auto staged = [&](int L) {
-        return lp[L + 1] - lp[L] <= kCGrp && le[L + 1] - le[L] <= kCEnt;
-    };
-    auto prefetch = [&](int L) {
-        if (L < nl && staged(L)) {
-            unsigned char* slot = smem + (size_t)(L & 1) * R::slot;
-            T* sv = reinterpret_cast<T*>(slot + R::v_off);
-            T* si = reinterpret_cast<T*>(slot + R::i_off);
-            T* sd = reinterpret_cast<T*>(slot + R::d_off);
-            int* sc = reinterpret_cast<int*>(slot + R::c_off);
-            int* se = reinterpret_cast<int*>(slot + R::e_off);
-            int* sr = reinterpret_cast<int*>(slot + R::r_off);
-            const int gb = lp[L], ng = lp[L + 1] - gb;
-            const int e0 = le[L], ne = le[L + 1] - e0;
-            for (int i = tid; i < ne; i += nth) {
-                __pipeline_memcpy_async(sc + i, t.ext_col + e0 + i, sizeof(int));
-                __pipeline_memcpy_async(sv + i, t.ext_v + e0 + i, sizeof(T));
-            }
-            for (int i = tid; i <= ng * g; i += nth)
-                __pipeline_memcpy_async(se + i, t.ext_ptr + (size_t)gb * g + i, sizeof(int));
-            for (int i = tid; i < ng; i += nth)
-                __pipeline_memcpy_async(sr + i, t.group_row0 + gb + i, sizeof(int));
-            for (int i = tid; i < ng * g * g; i += nth)
-                __pipeline_memcpy_async(si + i, t.int_v + (size_t)gb * g * g + i, sizeof(T));
-            if (UPPER)
-                for (int i = tid; i < ng * g; i += nth)
-                    __pipeline_memcpy_async(sd + i, t.dinv + (size_t)gb * g + i, sizeof(T));
-        }
-        __pipeline_commit();
-    };
-    auto xval = [&](int col) -> T {
-        const int G = col / g;
-        return xr[G % C][(G / C) * g + (col - G * g)];
-    };
-
-    prefetch(0);
-    __pipeline_wait_prior(0);
-    cluster.sync();
-    for (int l = 0; l < nl; ++l) {
-        prefetch(l + 1);
-        const int gb = lp[l], ng = lp[l + 1] - gb;
-        const int e0 = le[l];
-        const bool st = staged(l);
-        const unsigned char* slot = smem + (size_t)(l & 1) * R::slot;
-        const T* sv = st ? reinterpret_cast<const T*>(slot + R::v_off) : t.ext_v + e0;
-        const int* sc = st ? reinterpret_cast<const int*>(slot + R::c_off) : t.ext_col + e0;
-        const int* se = st ? reinterpret_cast<const int*>(slot + R::e_off) : t.ext_ptr + (size_t)gb * g;
-        const int* sr = st ? reinterpret_cast<const int*>(slot + R::r_off) : t.group_row0 + gb;
-        const T* si = st ? reinterpret_cast<const T*>(slot + R::i_off) : t.int_v + (size_t)gb * g * g;
-        const T* sd = st ? reinterpret_cast<const T*>(slot + R::d_off)
-                         : (UPPER ? t.dinv + (size_t)gb * g : nullptr);
-        for (int gl = warp; gl < ng; gl += nwarps) {  // warp-uniform
-            const int row0 = sr[gl];
-            const int G = row0 / g;
-            if (G % C != rank) continue;
-            // right-hand side values of the group's rows, loaded early
-            T vv = T(0);
-            if (!UPPER && lane < g * Q) vv = __ldg(v + (size_t)(row0 + lane / Q) * Q + lane % Q);
-            const int kb = se[gl * g] - e0, ke = se[gl * g + g] - e0;
-            const int b1 = g > 1 ? se[gl * g + 1] - e0 : ke, b2 = g > 2 ? se[gl * g + 2] - e0 : ke;
-            T a0 = T(0), a1 = T(0), a2 = T(0);
-            for (int k = kb + lane; k < ke; k += 32) {
-                const T prod = sv[k] * xval(sc[k]);
-                if (k < b1) a0 += prod;
-                else if (k < b2) a1 += prod;
-                else a2 += prod;
-            }
-#pragma unroll
-            for (int off = 16; off > 0; off >>= 1) {
-                a0 += __shfl_xor_sync(0xffffffffu, a0, off);
-                a1 += __shfl_xor_sync(0xffffffffu, a1, off);
-                a2 += __shfl_xor_sync(0xffffffffu, a2, off);
-            }
-            T bq[kMaxG];
-#pragma unroll
-            for (int ri = 0; ri < kMaxG; ++ri) {
-                T b = T(0);
-                if (!UPPER) {
-#pragma unroll
-                    for (int j = 0; j < Q; ++j)
-                        b = fma(sAinv[j * Q + col_c], __shfl_sync(0xffffffffu, vv, ri * Q + j), b);
-                }
-                bq[ri] = b;
-            }
-            if (lane == 0) {
-                const T acc[kMaxG] = {a0, a1, a2};
-                const T* iv = si + (size_t)gl * g * g;
-                T* mine = xs + (G / C) * g;
-                T sol[kMaxG];
-                for (int s2 = 0; s2 < g; ++s2) {
-                    const int ri = UPPER ? g - 1 - s2 : s2;
-                    T val = (UPPER ? mine[ri] : bq[ri]) - acc[ri];
-                    if (!UPPER) {
-                        for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
-                    } else {
-                        for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
-                        val *= sd[gl * g + ri];
-                    }
-                    sol[ri] = val;
-                }
-                for (int ri = 0; ri < g; ++ri) mine[ri] = sol[ri];
-            }
-        }
-        __pipeline_wait_prior(0);
-        cluster.sync();
-    }
-    // owned rows out: forward result to x_io, backward result to z
-    T* out = UPPER ? z : x_io;
-    for (int i = tid; i < xcap; i += nth) {
-        const int G = (i / g) * C + rank, ri = i % g;
-        if (G < ngroups) out[(size_t)(G * g + ri) * Q + col_c] = xs[i];
-    }
-}
-
-template <class T, int Q>
-int launch_tri_cluster(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
-                       cudaStream_t s, bool& launched)
-{
-    launched = false;
-    const int g = F.L.g;
-    const size_t limit = 227 * 1024 - 1024;
-    int C = 0;
-    for (int c = 1; c <= 8; c *= 2) {
-        const size_t xcap = (size_t)((F.L.ngroups + c - 1) / c) * g;
-        if (CRing<T>::rings + xcap * sizeof(T) <= limit) { C = c; break; }
-    }
-    if (C == 0) return XT_OK;
-    const int xcap = ((F.L.ngroups + C - 1) / C) * g;
-    const size_t bytes = CRing<T>::rings + (size_t)xcap * sizeof(T);
-    static bool attr = false;
-    if (!attr) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_cluster<T, Q, false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_cluster<T, Q, true>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
-        attr = true;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(Q * C, 1, 1);
-    cfg.blockDim = dim3(1024, 1, 1);
-    cfg.dynamicSmemBytes = bytes;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = C;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    XT_CUDA(cudaLaunchKernelEx(&cfg, k_tri_cluster<T, Q, false>, view<T>(F.L),
-                               (const int*)F.L.level_e.p, dAinv, v, work, (T*)nullptr, C, xcap));
-    XT_CUDA(cudaLaunchKernelEx(&cfg, k_tri_cluster<T, Q, true>, view<T>(F.U),
-                               (const int*)F.U.level_e.p, dAinv, (const T*)nullptr, work, z, C,
-                               xcap));
-    note_launches(2);
-    launched = true;
-    return XT_OK;
-}
-
-template <class T, int Q>
-int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
-               cudaStream_t s)
-{
-    if (F.L.g <= kMaxG && F.U.g <= kMaxG && F.L.level_e.p && F.U.level_e.p) {
-        const size_t bytes = Ring<T>::bytes;
-        static bool attr_set[2] = {false, false};
-        if (!attr_set[0]) {
-            XT_CUDA(cudaFuncSetAttribute(k_tri_staged<T, Q, false>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-            XT_CUDA(cudaFuncSetAttribute(k_tri_staged<T, Q, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-            attr_set[0] = true;
-        }
-        k_tri_staged<T, Q, false><<<1, 1024, bytes, s>>>(view<T>(F.L), F.L.level_e.p, dAinv, v,
-                                                         work, nullptr);
-        k_tri_staged<T, Q, true><<<1, 1024, bytes, s>>>(view<T>(F.U), F.U.level_e.p, dAinv,
-                                                        nullptr, work, z);
-        note_launches(2);
-        XT_CUDA(cudaGetLastError());
-        return XT_OK;
-    }
-    return launch_tri_simple<T, Q>(F, dAinv, v, z, work, s);
-}
-
 template <class T, int Q>
 int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
                       cudaStream_t s)
 {
     constexpr int S = (32 / Q) >= 32 ? 32 : ((32 / Q) >= 16 ? 16 : ((32 / Q) >= 8 ? 8 : ((32 / Q) >= 4 ? 4 : 2)));
     k_tri_sweep<T, Q, S, false><<<1, 1024, 0, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
-    note_launches(1);
-    XT_CUDA(cudaGetLastError());
     k_tri_sweep<T, Q, S, true><<<1, 1024, 0, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
-    note_launches(1);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class T, int Q>
+int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
+{
+    const bool blob = F.L.g <= kMaxG && F.U.g <= kMaxG && (sizeof(T) == 8 ? F.L.blob64.p : F.L.blob32.p);
+    if (!blob) return launch_tri_simple<T, Q>(F, dAinv, v, z, work, s);
+    const size_t bytes = staged_smem<T>();
+    static bool attr = false;
+    if (!attr) {
+        XT_CUDA(cudaFuncSetAttribute(k_tri_blob<T, Q, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        XT_CUDA(cudaFuncSetAttribute(k_tri_blob<T, Q, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        attr = true;
+    }
+    k_tri_blob<T, Q, false><<<1, 1024, bytes, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
+    k_tri_blob<T, Q, true><<<1, 1024, bytes, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
+    note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
 }
@@ -712,13 +497,12 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
             set_error("build_ilu: MSR column index out of range");
             return XT_ERR_ARG;
         }
-    int g = (group > 1 && n % group == 0 && group <= kMaxG) ? group : 1;
+    const int g = (group > 1 && n % group == 0 && group <= kMaxG) ? group : 1;
     d.n = n;
     TriHost L = schedule(n, alu, jlu, ju, g, false);
     TriHost U = schedule(n, alu, jlu, ju, g, true);
     XT_TRY(upload_tri(d.L, L, s));
     XT_TRY(upload_tri(d.U, U, s));
-    XT_CUDA(cudaStreamSynchronize(s));
     return XT_OK;
 }
 

@@ -110,7 +110,6 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 struct DevTri {
     int ngroups = 0, nlevels = 0, g = 1;
     DBuf<int> level_ptr;   // nlevels+1, into the level-ordered group list
-    DBuf<int> level_e;     // nlevels+1, first external nonzero of each level
     DBuf<int> group_row0;  // first row of each group, level order
     DBuf<int> ext_ptr;     // per (group, row-in-group): g*ngroups+1
     DBuf<int> ext_col;     // external (outside the group) columns
@@ -121,6 +120,10 @@ struct DevTri {
     DBuf<double> dinv64;   // per group g inverted diagonals (upper only)
     DBuf<float> dinv32;
     int max_level_groups = 0;
+    // per-level packed blobs (FP64 and FP32 values) and their descriptors
+    // (offset, length in 16-byte units, groups, nonzeros)
+    DBuf<unsigned char> blob64, blob32;
+    DBuf<int> desc64, desc32;
 };
 
 struct DevIlu {
