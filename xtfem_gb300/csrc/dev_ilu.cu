@@ -315,8 +315,18 @@ constexpr size_t slot_bytes() { return sizeof(T) == 8 ? 49152 : 40960; }
 template <class T>
 constexpr size_t staged_smem() { return kRing * slot_bytes<T>() + sizeof(BlobDesc) * kDescCap; }
 
+// block size, lanes per group and nonzeros in flight per lane: FP32 keeps a
+// whole level in one pass of 1024 threads; FP64 halves the threads to give
+// each lane the registers for its double accumulators
+template <class T>
+struct BlobCfg {
+    static constexpr int threads = sizeof(T) == 8 ? 512 : 1024;
+    static constexpr int lanes = sizeof(T) == 8 ? 8 : 16;
+    static constexpr int per = sizeof(T) == 8 ? 2 : 4;
+};
+
 template <class T, int Q, bool UPPER>
-__global__ void __launch_bounds__(1024, 1)
+__global__ void __launch_bounds__(BlobCfg<T>::threads, 1)
 k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v, T* x, T* z)
 {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -349,8 +359,14 @@ k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__
     prefetch(1);
     __pipeline_wait_prior(1);
     __syncthreads();
-    const int sub = tid & 1;
-    const int tasks_per_pass = nth >> 1;
+    // a group is handled by kLanes lanes: lane `sub` takes every kLanes-th
+    // external nonzero of the group (all g rows together), gathers the Q
+    // solved values of its column in one go and accumulates all g x Q
+    // partial sums; shuffles reduce them, then lane r < Q finishes block r
+    constexpr int kLanes = BlobCfg<T>::lanes;
+    constexpr int kPer = BlobCfg<T>::per;  // nonzeros per lane in flight (one batch)
+    const int sub = tid % kLanes;
+    const int groups_per_pass = nth / kLanes;
     for (int l = 0; l < nl; ++l) {
         prefetch(l + 2);
         const BlobDesc d = desc[l];
@@ -364,58 +380,91 @@ k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__
         const int* eptr = reinterpret_cast<const int*>(base + Lo.eptr);
         const T* intv = reinterpret_cast<const T*>(base + Lo.intv);
         const T* dinv = reinterpret_cast<const T*>(base + Lo.dinv);
-        const int ntask = d.ng * Q;
-        for (int pass = 0; pass < ntask; pass += tasks_per_pass) {
-            const int task = pass + (tid >> 1);
-            const bool act = task < ntask;
-            const int gi = act ? task / Q : 0, rhs = act ? task - gi * Q : 0;
+        for (int pass = 0; pass < d.ng; pass += groups_per_pass) {
+            const int gi = pass + tid / kLanes;
+            const bool act = gi < d.ng;
             const int row0 = act ? row0s[gi] : 0;
-            // right-hand sides of rows sub and sub+2 of the group, issued first
-            T bA = T(0), bB = T(0);
-            if (act && sub < g) {
-                if (!UPPER) {
-                    const T* va = v + (size_t)(row0 + sub) * Q;
-#pragma unroll
-                    for (int j = 0; j < Q; ++j) bA = fma(sAinv[j * Q + rhs], __ldg(va + j), bA);
-                    if (sub + 2 < g) {
-                        const T* vb = v + (size_t)(row0 + sub + 2) * Q;
-#pragma unroll
-                        for (int j = 0; j < Q; ++j) bB = fma(sAinv[j * Q + rhs], __ldg(vb + j), bB);
-                    }
-                } else {
-                    bA = x[(size_t)(row0 + sub) * Q + rhs];
-                    if (sub + 2 < g) bB = x[(size_t)(row0 + sub + 2) * Q + rhs];
-                }
-            }
-            T acc[kMaxG] = {T(0), T(0), T(0)};
-            if (act) {
+            const int rhs = sub;  // temporal block finished by this lane (if < Q)
+            // right-hand sides of the group's rows for block `rhs`, issued
+            // before the gathers so their latency overlaps them
+            T bq[kMaxG] = {T(0), T(0), T(0)};
+            if (act && rhs < Q) {
 #pragma unroll
                 for (int ri = 0; ri < kMaxG; ++ri) {
                     if (ri < g) {
-                        const int kb = eptr[gi * g + ri], ke = eptr[gi * g + ri + 1];
-                        T a = T(0);
-#pragma unroll 4
-                        for (int k = kb + sub; k < ke; k += 2)
-                            a = fma(vals[k], x[(size_t)cols[k] * Q + rhs], a);
-                        acc[ri] = a;
+                        if (!UPPER) {
+                            const T* vr = v + (size_t)(row0 + ri) * Q;
+                            T b = T(0);
+#pragma unroll
+                            for (int j = 0; j < Q; ++j) b = fma(sAinv[j * Q + rhs], __ldg(vr + j), b);
+                            bq[ri] = b;
+                        } else {
+                            bq[ri] = x[(size_t)(row0 + ri) * Q + rhs];
+                        }
+                    }
+                }
+            }
+            T acc[kMaxG][Q];
+#pragma unroll
+            for (int ri = 0; ri < kMaxG; ++ri)
+#pragma unroll
+                for (int b = 0; b < Q; ++b) acc[ri][b] = T(0);
+            if (act) {
+                const int kb = eptr[gi * g], ke = eptr[gi * g + g];
+                const int b1 = g > 1 ? eptr[gi * g + 1] : ke, b2 = g > 2 ? eptr[gi * g + 2] : ke;
+                for (int k0 = kb + sub; k0 < ke; k0 += kPer * kLanes) {
+                    int cc[kPer];
+                    T cv[kPer];
+#pragma unroll
+                    for (int u = 0; u < kPer; ++u) {
+                        const int k = k0 + u * kLanes;
+                        cc[u] = k < ke ? cols[k] : -1;
+                        cv[u] = k < ke ? vals[k] : T(0);
+                    }
+                    T xv[kPer][Q];
+#pragma unroll
+                    for (int u = 0; u < kPer; ++u) {
+                        const T* xr = x + (size_t)(cc[u] < 0 ? 0 : cc[u]) * Q;
+#pragma unroll
+                        for (int b = 0; b < Q; ++b) xv[u][b] = cc[u] < 0 ? T(0) : xr[b];
+                    }
+#pragma unroll
+                    for (int u = 0; u < kPer; ++u) {
+                        const int k = k0 + u * kLanes;
+                        const int ri = (k >= b1) + (k >= b2);
+#pragma unroll
+                        for (int b = 0; b < Q; ++b) {
+                            const T pr = cv[u] * xv[u][b];
+                            acc[0][b] += ri == 0 ? pr : T(0);
+                            acc[1][b] += ri == 1 ? pr : T(0);
+                            acc[2][b] += ri == 2 ? pr : T(0);
+                        }
                     }
                 }
             }
 #pragma unroll
-            for (int ri = 0; ri < kMaxG; ++ri) acc[ri] += __shfl_xor_sync(0xffffffffu, acc[ri], 1);
-            // b of row 0, 1, 2 lives in (lane 0: bA), (lane 1: bA), (lane 0: bB)
-            const T oA = __shfl_xor_sync(0xffffffffu, bA, 1);
-            const T b0 = sub == 0 ? bA : oA, b1 = sub == 0 ? oA : bA;
-            const T b2 = __shfl_sync(0xffffffffu, bB, (threadIdx.x & 31) & ~1);
-            if (act) {
-                const T bq[kMaxG] = {b0, b1, b2};
+            for (int off = kLanes / 2; off > 0; off >>= 1)
+#pragma unroll
+                for (int ri = 0; ri < kMaxG; ++ri)
+#pragma unroll
+                    for (int b = 0; b < Q; ++b)
+                        acc[ri][b] += __shfl_xor_sync(0xffffffffu, acc[ri][b], off, kLanes);
+            if (act && rhs < Q) {
+                T accr[kMaxG];
+#pragma unroll
+                for (int ri = 0; ri < kMaxG; ++ri) {
+                    T a = acc[ri][0];
+#pragma unroll
+                    for (int b = 1; b < Q; ++b) a = (rhs == b) ? acc[ri][b] : a;
+                    accr[ri] = a;
+                }
                 const T* iv = intv + (size_t)gi * g * g;
                 T sol[kMaxG];
 #pragma unroll
                 for (int s2 = 0; s2 < kMaxG; ++s2) {
                     if (s2 < g) {
                         const int ri = UPPER ? g - 1 - s2 : s2;
-                        T val = bq[ri] - acc[ri];
+                        T val = bq[ri] - accr[ri];
                         if (!UPPER) {
                             for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
                         } else {
@@ -425,10 +474,9 @@ k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__
                         sol[ri] = val;
                     }
                 }
-                // lane 0 stores rows 0 and 2, lane 1 row 1
 #pragma unroll
                 for (int ri = 0; ri < kMaxG; ++ri)
-                    if (ri < g && (ri & 1) == sub) {
+                    if (ri < g) {
                         x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
                         if (UPPER) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
                     }
@@ -465,8 +513,9 @@ int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, 
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         attr = true;
     }
-    k_tri_blob<T, Q, false><<<1, 1024, bytes, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
-    k_tri_blob<T, Q, true><<<1, 1024, bytes, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
+    constexpr int nt = BlobCfg<T>::threads;
+    k_tri_blob<T, Q, false><<<1, nt, bytes, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
+    k_tri_blob<T, Q, true><<<1, nt, bytes, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
