@@ -145,6 +145,11 @@ int xt_system_apply(xt_system s, const double *a, const double *b,
                     double alpha, double beta, const double *x, double *y);
 /* kronlusol semantics with the system's factor and temporal matrix a. */
 int xt_system_lusol(xt_system s, const double *a, const double *x, double *y);
+/* The same apply with the factor, the vectors and the arithmetic in FP32
+ * (the preconditioner of the mixed-precision inner solve); x and y stay
+ * FP64 at the boundary.  No counterpart in the reference, whose lusol is
+ * FP64 only. */
+int xt_system_lusol_f32(xt_system s, const double *a, const double *x, double *y);
 /* kronpgmres semantics (host vectors, block layout).  rhs is preserved.
  * its/ierr/est may be NULL; hist (may be NULL) receives up to hist_len
  * residual estimates |rs(i+1)|/||r0||. */

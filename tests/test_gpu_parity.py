@@ -64,6 +64,64 @@ def test_kronlusol_row_levels_equal_node_levels(xt, orc, rod_system):
     sysm.close()
 
 
+@pytest.fixture(scope="module")
+def rod8_system(xt):
+    """An 8x8x24-element rod (2,025 nodes): several hundred levels, so the
+    staged sweeps' shared-memory ring wraps many times."""
+    pr = rod_problem(xt, 24, 8, 8)
+    xyz, conn = pr.mesh()
+    pr.apply_bc(clamp_mask(xyz))
+    K, M = pr.K(), pr.M()
+    alu, jlu, ju = xt.ilut(K, 20, 1e-4)
+    A, B, C1, M1 = temporal(xt)
+    sysm = xt.SpaceTimeSystem(K, M)
+    sysm.set_ilu(alu, jlu, ju, group=3)
+    yield dict(K=K, M=M, alu=alu, jlu=jlu, ju=ju, A=A, B=B, sys=sysm)
+    sysm.close()
+
+
+ILU_VARIANTS = [
+    {},                                  # defaults: node blocks (FP32), rows S=2 (FP64)
+    {"XTFEM_ILU_SHARES": "1"},
+    {"XTFEM_ILU_SHARES": "4"},
+    {"XTFEM_ILU_FMT": "0"},              # row format for FP32 too
+    {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "1"},
+    {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "4"},
+    {"XTFEM_ILU_WARPS": "1"},            # one compute warp: many passes per level
+    {"XTFEM_ILU_SIMPLE": "1"},           # one-warp-per-group fallback
+]
+
+
+@pytest.mark.parametrize("env", ILU_VARIANTS, ids=lambda e: ",".join(f"{k[10:]}={v}" for k, v in e.items()) or "default")
+def test_kronlusol_sweep_variants_fp64(xt, orc, rod8_system, monkeypatch, env):
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    s = rod8_system
+    x = np.random.default_rng(5).standard_normal(s["K"].n * 6)
+    y_ref = orc.kronlusol(s["A"], s["alu"], s["jlu"], s["ju"], x)
+    for _ in range(2):  # second call reuses the cached staged data
+        assert rel(s["sys"].lusol(s["A"], x), y_ref) <= 1e-10
+
+
+@pytest.mark.parametrize("env", ILU_VARIANTS, ids=lambda e: ",".join(f"{k[10:]}={v}" for k, v in e.items()) or "default")
+def test_kronlusol_sweep_variants_fp32(xt, orc, rod8_system, monkeypatch, env):
+    """FP32 factor and arithmetic: within 1e-4 of the FP64 oracle (the
+    factor itself is rounded to FP32), and within 1e-5 of the fallback
+    sweep, which uses the same FP32 factor in another summation order."""
+    s = rod8_system
+    x = np.random.default_rng(6).standard_normal(s["K"].n * 6)
+    y_ref = orc.kronlusol(s["A"], s["alu"], s["jlu"], s["ju"], x)
+    monkeypatch.setenv("XTFEM_ILU_SIMPLE", "1")
+    y_simple = s["sys"].lusol(s["A"], x, fp32=True)
+    monkeypatch.delenv("XTFEM_ILU_SIMPLE")
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    for _ in range(2):
+        y = s["sys"].lusol(s["A"], x, fp32=True)
+        assert rel(y, y_ref) <= 1e-4
+        assert rel(y, y_simple) <= 1e-5
+
+
 def c1_rhs(xt, s, amplitude=100.0):
     """RHS of the first C1 slab: fextc_j * rext with clamped rows zeroed."""
     xyz, conn, bc = s["xyz"], s["conn"], s["bc"]

@@ -43,6 +43,7 @@ SIGNATURES = {
     "xt_system_set_temporal": (C.c_int, [_vp, _dp, _dp]),
     "xt_system_apply": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_double, _dp, _dp]),
     "xt_system_lusol": (C.c_int, [_vp, _dp, _dp, _dp]),
+    "xt_system_lusol_f32": (C.c_int, [_vp, _dp, _dp, _dp]),
     "xt_system_gmres": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_double, C.c_int, _ip, _ip, _dp,
                                   _dp, C.c_int]),
     "xt_system_solve": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int,

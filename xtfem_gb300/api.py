@@ -260,9 +260,10 @@ class SpaceTimeSystem:
                                     dptr(_f64(x)), dptr(out)), "apply")
         return out
 
-    def lusol(self, a, x):
+    def lusol(self, a, x, fp32=False):
         y = np.zeros(self.p * self.q)
-        check(lib().xt_system_lusol(self._h, dptr(_colmajor(a)), dptr(_f64(x)), dptr(y)), "lusol")
+        fn = lib().xt_system_lusol_f32 if fp32 else lib().xt_system_lusol
+        check(fn(self._h, dptr(_colmajor(a)), dptr(_f64(x)), dptr(y)), "lusol")
         return y
 
     def gmres(self, rhs, sol=None, im=30, eps=1e-8, maxits=1000, hist_len=0):

@@ -245,7 +245,36 @@ int xt_system_lusol(xt_system h, const double* a, const double* x, double* y)
         XT_CUDA(cudaMemcpyAsync(S.Ainv.p, S.hAinv.data(), sizeof(double) * q * q,
                                 cudaMemcpyHostToDevice, s));
     XT_CUDA(cudaStreamSynchronize(s));
-    return XT_OK;
+    return ilu_check(s);
+}
+
+int xt_system_lusol_f32(xt_system h, const double* a, const double* x, double* y)
+{
+    if (!h || !a || !x || !y) { set_error("xt_system_lusol_f32: null argument"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    if (!S.ilu) { set_error("xt_system_lusol_f32: no factor set"); return XT_ERR_STATE; }
+    const int q = S.q;
+    const size_t n = (size_t)S.p * q;
+    std::vector<double> ainv(q * q);
+    XT_TRY(invert_small(q, a, ainv.data()));
+    cudaStream_t s = ctx().stream;
+    XT_CUDA(cudaMemcpyAsync(S.Ainv.p, ainv.data(), sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
+    XT_TRY(ensure_vec(S.x64, n));
+    XT_TRY(ensure_vec(S.r64, n));
+    DBuf<float> x32, y32, w32;
+    XT_TRY(x32.alloc(n));
+    XT_TRY(y32.alloc(n));
+    XT_TRY(w32.alloc(n));
+    XT_TRY(upload_blocks(*h, x, S.x64.p));
+    XT_TRY((axpby<double, float>(n, 1.0, S.x64.p, 0.0, x32.p, s)));
+    XT_TRY(ilu_apply<float>(*S.ilu, q, S.Ainv.p, x32.p, y32.p, w32.p, s));
+    XT_TRY((axpby<float, double>(n, 1.0, y32.p, 0.0, S.r64.p, s)));
+    XT_TRY(download_blocks(*h, S.r64.p, y));
+    if (!S.hAinv.empty())  // restore the solver's temporal inverse
+        XT_CUDA(cudaMemcpyAsync(S.Ainv.p, S.hAinv.data(), sizeof(double) * q * q,
+                                cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return ilu_check(s);
 }
 
 int xt_system_gmres(xt_system h, const double* rhs, double* sol, int im, double eps, int maxits,

@@ -7,28 +7,44 @@
 //
 // The factor is computed on the host (ILUT, FP64) and arrives in MSR form.
 // A triangular solve is a chain of dependent rows, so it is organised by
-// level sets computed once per factor:
-//   * rows are grouped by node (g = 3 consecutive DOFs); a group's level is
-//     one more than the deepest other group it reads, and the g rows of a
-//     group are solved in sequence by the same threads, which halves the
-//     level count of C3D8 stiffness factors compared with row levels;
-//   * everything a level needs -- the external nonzeros (column, value), the
-//     group rows, the row pointers, the g x g in-group coefficients and the
-//     inverted diagonal -- is packed into one 16-byte-aligned blob per level,
-//     so a level is fetched with a handful of 16-byte asynchronous copies
-//     into a three-deep shared-memory ring, two levels ahead of use;
-//   * one (group, temporal block) task is handled by two lanes that split
-//     each row's nonzeros; all q temporal blocks of a level run at once;
-//   * the q x q mixing with A^-1 is applied to v while the forward sweep
-//     reads it (the mixing commutes with the spatial solve);
-//   * one thread block runs all levels of a sweep with one block barrier per
-//     level; values solved in earlier levels are read back through L1/L2.
-// A single SM runs the sweep: the kernel is bound by the level count times
-// the per-level latency (barrier, gathers) and by instruction issue, not by
-// HBM bandwidth.  Independent systems (batches) fill the other SMs.
+// level sets computed once per factor.  Rows are grouped by node (g = 3
+// consecutive DOFs); a group's level is one more than the deepest other
+// group it reads.  The staged sweep runs a whole triangle in one thread
+// block and keeps every load on a level's critical path in shared memory:
+//
+//   * Solution window.  A solved group is read only by groups a few levels
+//     later, so its values live in a shared-memory slot from its own level
+//     to the last level that reads it.  Slots are assigned on the host by
+//     interval colouring of these live ranges; the factor's column indices
+//     are rewritten as window offsets.  (C3D8 rod, 80,703 DOFs: at most 697
+//     groups are live at once, 50 KB in FP32 for six temporal blocks.)
+//   * Level stream.  Each level's factor data (window offsets, values, row
+//     pointers, the inverted g x g diagonal block of every group) is one
+//     16-byte-aligned blob.  A producer warp copies blob and right-hand
+//     sides into a variable-size shared-memory ring with bulk asynchronous
+//     copies (TMA, completion counted on an mbarrier per level), several
+//     levels ahead of the compute warps; the host places every level in the
+//     ring and fixes the level at whose start its copy may be issued.
+//   * Compute.  S lanes share a row; each lane gathers its share of the
+//     row's nonzeros for all q temporal blocks at once (the q values of a
+//     window row are contiguous), the S partial sums are combined with
+//     shuffles, and the g rows of a group are finished with the group's
+//     inverted diagonal block, also through shuffles.  One named barrier
+//     per level separates the levels.
+//   * The q x q mixing with A^-1 is applied when the right-hand side is
+//     permuted into forward-sweep level order (a parallel pre-pass); the
+//     forward sweep writes its result in backward-sweep level order, so both
+//     sweeps read their right-hand sides as contiguous per-level chunks.
+//
+// Waits are bounded: a wait that gives up sets a device error word (read by
+// ilu_check) and the block leaves the sweep at the next level boundary.
+// A factor whose window does not fit in shared memory uses a plain
+// one-warp-per-group sweep that reads everything from global memory.
 #include <cuda_pipeline.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -36,14 +52,25 @@
 
 namespace xt {
 
+__device__ int g_ilu_error;  // 0 = clear; 1 = ring wait gave up; 2 = producer wait gave up
+
 namespace {
 
 constexpr int kMaxG = 3;
+constexpr int kNB = 16;          // mbarriers per direction: levels in flight < kNB
+constexpr int kHdrBytes = 2 * kNB * 8 + 16;
+constexpr long long kSpinLimit = 1ll << 20;
+constexpr int kStageThreads = 512;  // compute warps + the producer warp, at most
 
 struct TriHost {
     int ngroups = 0, nlevels = 0, g = 1, maxw = 0;
     std::vector<int> level_ptr, group_row0, ext_ptr, ext_col;
     std::vector<double> ext_v, int_v, dinv;
+    std::vector<int> order;  // level order -> group id
+    std::vector<int> pos;    // group id -> level-order position
+    std::vector<int> slot;   // group id -> window slot
+    int nslots = 0;
+    std::vector<double> minv;  // level order, g*g: inverse of the group's diagonal block
 };
 
 // Level-schedule one triangle.  upper == false: rows' L parts
@@ -82,14 +109,19 @@ TriHost schedule(int n, const double* alu, const int* jlu, const int* ju, int g,
         T.maxw = std::max(T.maxw, cnt[l + 1] - cnt[l]);
     }
     T.level_ptr = cnt;
-    std::vector<int> order(ng), pos(cnt.begin(), cnt.end() - 1);
-    for (int G = 0; G < ng; ++G) order[pos[lev[G]]++] = G;
+    T.order.resize(ng);
+    T.pos.resize(ng);
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (int G = 0; G < ng; ++G) {
+        T.pos[G] = fill[lev[G]]++;
+        T.order[T.pos[G]] = G;
+    }
     T.group_row0.resize(ng);
     T.ext_ptr.assign((size_t)ng * g + 1, 0);
     T.int_v.assign((size_t)ng * g * g, 0.0);
     if (upper) T.dinv.assign((size_t)ng * g, 0.0);
     for (int i = 0; i < ng; ++i) {
-        const int G = order[i];
+        const int G = T.order[i];
         T.group_row0[i] = G * g;
         for (int ri = 0; ri < g; ++ri) {
             const int r = G * g + ri;
@@ -108,135 +140,391 @@ TriHost schedule(int n, const double* alu, const int* jlu, const int* ju, int g,
             if (upper) T.dinv[(size_t)i * g + ri] = alu[r];
         }
     }
+
+    // Inverse of each group's diagonal block, column by column, with the
+    // lusol recurrences applied to unit vectors: forward
+    // x_r = e_r - sum_{c<r} l_rc x_c, backward x_r = d_r (e_r - sum_{c>r} u_rc x_c).
+    T.minv.assign((size_t)ng * g * g, 0.0);
+    for (int i = 0; i < ng; ++i) {
+        const double* iv = &T.int_v[(size_t)i * g * g];
+        double* mi = &T.minv[(size_t)i * g * g];
+        for (int col = 0; col < g; ++col) {
+            double x[kMaxG] = {0, 0, 0};
+            for (int s2 = 0; s2 < g; ++s2) {
+                const int r = upper ? g - 1 - s2 : s2;
+                double v = (r == col) ? 1.0 : 0.0;
+                if (!upper) {
+                    for (int c = 0; c < r; ++c) v -= iv[r * g + c] * x[c];
+                } else {
+                    for (int c = r + 1; c < g; ++c) v -= iv[r * g + c] * x[c];
+                    v *= T.dinv[(size_t)i * g + r];
+                }
+                x[r] = v;
+            }
+            for (int r = 0; r < g; ++r) mi[r * g + col] = x[r];
+        }
+    }
+
+    // Window slots: group G is live from its level to the last level that
+    // reads it; a slot freed after level e is reused from level e+1 on.
+    std::vector<int> last(ng);
+    for (int G = 0; G < ng; ++G) last[G] = lev[G];
+    for (int i = 0; i < ng; ++i) {
+        const int G = T.order[i];
+        for (int k = T.ext_ptr[(size_t)i * g]; k < T.ext_ptr[(size_t)(i + 1) * g]; ++k) {
+            const int Gc = T.ext_col[k] / g;
+            last[Gc] = std::max(last[Gc], lev[G]);
+        }
+    }
+    std::vector<std::vector<int>> release(T.nlevels + 1);
+    std::vector<int> free_slots;
+    T.slot.assign(ng, -1);
+    for (int l = 0; l < T.nlevels; ++l) {
+        for (int sl : release[l]) free_slots.push_back(sl);
+        for (int i = T.level_ptr[l]; i < T.level_ptr[l + 1]; ++i) {
+            const int G = T.order[i];
+            int sl;
+            if (!free_slots.empty()) { sl = free_slots.back(); free_slots.pop_back(); }
+            else sl = T.nslots++;
+            T.slot[G] = sl;
+            release[last[G] + 1].push_back(sl);
+        }
+    }
     return T;
 }
 
-// Per-level blob layout (all sections 16-byte aligned, offsets in bytes):
-//   cols  ne ints | vals ne T | row0 ng ints | eptr ng*g+1 ints (relative
-//   to the level's first nonzero) | intv ng*g*g T | dinv ng*g T (upper)
-struct BlobDesc {
-    int off16;  // blob start in 16-byte units
-    int len16;  // blob length in 16-byte units
-    int ng;     // groups in the level
-    int ne;     // external nonzeros in the level
+}  // namespace
+
+// Both schedules, kept on the host to build staged sweeps on first use.
+struct IluSched {
+    TriHost L, U;
 };
 
+namespace {
+
+// Per-level blob layout (sections 16-byte aligned, offsets in bytes):
+//   header {ng, ne, 0, 0} | eptr ng*g+1 ints (relative to the level's first
+//   nonzero) | gslot ng ints (window element offset of the group's rows) |
+//   gdst ng ints (destination record or first row) | minv ng*g*g T |
+//   offs ne ints (window element offset of each external column) | vals ne T
 template <class T>
-struct BlobLayout {
-    size_t cols, vals, row0, eptr, intv, dinv, bytes;
-    __host__ __device__ BlobLayout(int ne, int ng, int g)
+struct Layout {
+    unsigned eptr, gslot, gdst, minv, offs, vals, bytes;
+    __host__ __device__ static unsigned up16(unsigned b) { return (b + 15u) & ~15u; }
+    __host__ __device__ Layout(int ng, int ne, int g)
     {
-        cols = 0;
-        vals = up16(cols + sizeof(int) * (size_t)ne);
-        row0 = up16(vals + sizeof(T) * (size_t)ne);
-        eptr = up16(row0 + sizeof(int) * (size_t)ng);
-        intv = up16(eptr + sizeof(int) * ((size_t)ng * g + 1));
-        dinv = up16(intv + sizeof(T) * (size_t)ng * g * g);
-        bytes = up16(dinv + sizeof(T) * (size_t)ng * g);
+        eptr = 16;
+        gslot = up16(eptr + 4u * (unsigned)(ng * g + 1));
+        gdst = up16(gslot + 4u * (unsigned)ng);
+        minv = up16(gdst + 4u * (unsigned)ng);
+        offs = up16(minv + (unsigned)sizeof(T) * (unsigned)(ng * g * g));
+        vals = up16(offs + 4u * (unsigned)ne);
+        bytes = up16(vals + (unsigned)sizeof(T) * (unsigned)ne);
     }
-    __host__ __device__ static size_t up16(size_t b) { return (b + 15) / 16 * 16; }
 };
 
-template <class T>
-void build_blobs(const TriHost& h, std::vector<unsigned char>& blob, std::vector<BlobDesc>& desc)
+// Staged-sweep data of one triangle for one (q, precision).
+struct StageTri {
+    bool ok = false;
+    int nlevels = 0, g = 1, ring_bytes = 0, window_bytes = 0, p90 = 1;
+    DBuf<unsigned char> blob;
+    DBuf<int> table;  // per level {off16, pos16, grp0, iss, len16, rhs16, ng, ne or nb}
+};
+
+int max_dyn_smem()
 {
-    const int g = h.g;
-    desc.resize(h.nlevels);
-    size_t total = 0;
-    for (int l = 0; l < h.nlevels; ++l) {
-        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
-        const int e0 = h.ext_ptr[(size_t)gb * g], ne = h.ext_ptr[(size_t)(gb + ng) * g] - e0;
-        BlobLayout<T> L(ne, ng, g);
-        desc[l] = {(int)(total / 16), (int)(L.bytes / 16), ng, ne};
-        total += L.bytes;
+    static int v = -1;
+    if (v < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            v = 48 * 1024;
     }
-    blob.assign(total, 0);
-    for (int l = 0; l < h.nlevels; ++l) {
-        const int gb = h.level_ptr[l], ng = desc[l].ng, ne = desc[l].ne;
-        const int e0 = h.ext_ptr[(size_t)gb * g];
-        BlobLayout<T> L(ne, ng, g);
-        unsigned char* b = blob.data() + (size_t)desc[l].off16 * 16;
-        int* cols = reinterpret_cast<int*>(b + L.cols);
-        T* vals = reinterpret_cast<T*>(b + L.vals);
-        int* row0 = reinterpret_cast<int*>(b + L.row0);
-        int* eptr = reinterpret_cast<int*>(b + L.eptr);
-        T* intv = reinterpret_cast<T*>(b + L.intv);
-        T* dinv = reinterpret_cast<T*>(b + L.dinv);
-        for (int k = 0; k < ne; ++k) {
-            cols[k] = h.ext_col[(size_t)e0 + k];
-            vals[k] = (T)h.ext_v[(size_t)e0 + k];
-        }
-        for (int i = 0; i < ng; ++i) row0[i] = h.group_row0[(size_t)gb + i];
-        for (int i = 0; i <= ng * g; ++i) eptr[i] = h.ext_ptr[(size_t)gb * g + i] - e0;
-        for (int i = 0; i < ng * g * g; ++i) intv[i] = (T)h.int_v[(size_t)gb * g * g + i];
-        if (!h.dinv.empty())
-            for (int i = 0; i < ng * g; ++i) dinv[i] = (T)h.dinv[(size_t)gb * g + i];
-    }
+    return v;
 }
 
-int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
+bool trace_on() { return std::getenv("XTFEM_TRACE") != nullptr; }
+
+// Node-block format (FP32, g = 3), per level:
+//   header {ng, nb, 0, 0} | ng group records of 64 B {bstart, bcount, gslot,
+//   gdst, minv[9] row-major, pad} | nb blocks of 48 B {woff, v[9] row-major
+//   3 x 3 (rows of the group x DOFs of the neighbour node), pad}
+// woff is the window element offset of the neighbour node's first row.  A
+// block holds every factor entry between the group and one neighbour node,
+// zeros where ILUT dropped the entry.
+constexpr unsigned kGrec = 64, kBrec = 48;
+
+// Window and ring sizes of a triangle; false when they do not fit.
+bool stage_sizes(const TriHost& h, int Q, size_t tsize, long long& win_elems,
+                 long long& window_bytes, long long& ring)
 {
-    d.ngroups = h.ngroups;
-    d.nlevels = h.nlevels;
-    d.g = h.g;
-    d.max_level_groups = h.maxw;
-    XT_TRY(d.level_ptr.upload(h.level_ptr.data(), h.level_ptr.size(), s));
-    XT_TRY(d.group_row0.upload(h.group_row0.data(), h.group_row0.size(), s));
-    XT_TRY(d.ext_ptr.upload(h.ext_ptr.data(), h.ext_ptr.size(), s));
-    const size_t ne = h.ext_col.size();
-    std::vector<float> f32(h.ext_v.begin(), h.ext_v.end());
-    std::vector<float> i32(h.int_v.begin(), h.int_v.end());
-    std::vector<float> d32(h.dinv.begin(), h.dinv.end());
-    XT_TRY(d.ext_col.upload(ne ? h.ext_col.data() : nullptr, ne ? ne : 0, s));
-    XT_TRY(d.ext_v64.upload(h.ext_v.data(), ne, s));
-    XT_TRY(d.ext_v32.upload(f32.data(), ne, s));
-    XT_TRY(d.int_v64.upload(h.int_v.data(), h.int_v.size(), s));
-    XT_TRY(d.int_v32.upload(i32.data(), i32.size(), s));
-    if (!h.dinv.empty()) {
-        XT_TRY(d.dinv64.upload(h.dinv.data(), h.dinv.size(), s));
-        XT_TRY(d.dinv32.upload(d32.data(), d32.size(), s));
+    win_elems = (long long)h.nslots * h.g * Q;
+    window_bytes = (win_elems * (long long)tsize + 15) / 16 * 16;
+    const long long budget = (long long)max_dyn_smem() - kHdrBytes - window_bytes;
+    ring = std::min<long long>(budget, 192 * 1024) / 16 * 16;
+    if (ring < 16 * 1024 || win_elems >= (1ll << 31)) {
+        if (trace_on())
+            std::fprintf(stderr, "[xtfem] staged sweep off: window %lld B, ring %lld B\n",
+                         window_bytes, ring);
+        return false;
     }
-    std::vector<unsigned char> b64, b32;
-    std::vector<BlobDesc> e64, e32;
-    build_blobs<double>(h, b64, e64);
-    build_blobs<float>(h, b32, e32);
-    XT_TRY(d.blob64.upload(b64.data(), b64.size(), s));
-    XT_TRY(d.blob32.upload(b32.data(), b32.size(), s));
-    XT_TRY(d.desc64.upload(reinterpret_cast<const int*>(e64.data()), e64.size() * 4, s));
-    XT_TRY(d.desc32.upload(reinterpret_cast<const int*>(e32.data()), e32.size() * 4, s));
+    return true;
+}
+
+// Ring placement.  Each level's region (blob, then right-hand sides) goes
+// after the previous one, wrapping to the start when it does not fit; a
+// level larger than half the ring is read from global memory (pos16 = -1).
+// The issue level is the first level at whose start every earlier occupant
+// of the region has been consumed, with fewer than kNB levels in flight.
+// Fills tab[l*8+1] (pos16) and tab[l*8+3] (issue level) and checks the
+// result.
+bool place_ring(const std::vector<unsigned>& region, long long ring, std::vector<int>& tab)
+{
+    const int nl = (int)region.size();
+    std::vector<long long> posb(nl, -1);
+    long long cur = 0;
+    int prev_iss = 0;
+    auto overlap = [&](int a, int b) {
+        return posb[a] >= 0 && posb[b] >= 0 && posb[a] < posb[b] + region[b] &&
+               posb[b] < posb[a] + region[a];
+    };
+    for (int l = 0; l < nl; ++l) {
+        int* t = &tab[(size_t)l * 8];
+        int iss = std::max(prev_iss, l - kNB + 1);
+        if ((long long)region[l] * 2 > ring) {
+            t[1] = -1;
+        } else {
+            long long p = cur;
+            if (p + region[l] > ring) p = 0;
+            cur = p + region[l];
+            posb[l] = p;
+            t[1] = (int)(p / 16);
+            for (int l2 = l - 1; l2 >= iss; --l2)
+                if (overlap(l, l2)) { iss = l2 + 1; break; }
+        }
+        iss = std::min(iss, l);
+        t[3] = iss;
+        prev_iss = iss;
+    }
+    for (int l = 0; l < nl; ++l) {
+        const int iss = tab[(size_t)l * 8 + 3];
+        if (iss > l || l - iss >= kNB) return false;
+        if (posb[l] < 0) continue;
+        if (posb[l] % 16 || posb[l] + (long long)region[l] > ring) return false;
+        for (int l2 = iss; l2 < l; ++l2)
+            if (overlap(l, l2)) return false;
+    }
+    return true;
+}
+
+int finish_stage(StageTri& out, const TriHost& h, long long ring, long long window_bytes,
+                 const std::vector<unsigned char>& blob, const std::vector<int>& tab,
+                 cudaStream_t s)
+{
+    std::vector<int> wsz;
+    for (int l = 0; l < h.nlevels; ++l) wsz.push_back(h.level_ptr[l + 1] - h.level_ptr[l]);
+    std::sort(wsz.begin(), wsz.end());
+    out.p90 = std::max(1, wsz[(size_t)(0.9 * (wsz.size() - 1))]);
+    out.nlevels = h.nlevels;
+    out.g = h.g;
+    out.ring_bytes = (int)ring;
+    out.window_bytes = (int)window_bytes;
+    XT_TRY(out.blob.upload(blob.data(), blob.size(), s));
+    XT_TRY(out.table.upload(tab.data(), tab.size(), s));
     XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    out.ok = true;
     return XT_OK;
 }
 
+// Row format: blob, ring placement and issue levels of one triangle; leaves
+// out.ok false when the window or ring does not fit.
+template <class T>
+int build_row_tri(const TriHost& h, int Q, const std::vector<int>& gdst, StageTri& out,
+                  cudaStream_t s)
+{
+    out.ok = false;
+    const int g = h.g, nl = h.nlevels;
+    long long win_elems, window_bytes, ring;
+    if (!stage_sizes(h, Q, sizeof(T), win_elems, window_bytes, ring)) return XT_OK;
+    const unsigned rs = Layout<T>::up16((unsigned)(g * Q * sizeof(T)));
+    std::vector<int> tab((size_t)nl * 8, 0);
+    std::vector<unsigned> region(nl);
+    size_t total = 0;
+    for (int l = 0; l < nl; ++l) {
+        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
+        const int ne = h.ext_ptr[(size_t)(gb + ng) * g] - h.ext_ptr[(size_t)gb * g];
+        Layout<T> Lo(ng, ne, g);
+        region[l] = Lo.bytes + (unsigned)ng * rs;
+        int* t = &tab[(size_t)l * 8];
+        t[0] = (int)(total / 16);
+        t[2] = gb;
+        t[4] = (int)(Lo.bytes / 16);
+        t[5] = (int)((unsigned)ng * rs / 16);
+        t[6] = ng;
+        t[7] = ne;
+        total += Lo.bytes;
+    }
+    bool valid = place_ring(region, ring, tab);
+    std::vector<unsigned char> blob(total, 0);
+    for (int l = 0; l < nl && valid; ++l) {
+        const int* t = &tab[(size_t)l * 8];
+        const int gb = t[2], ng = t[6], ne = t[7];
+        const int e0 = h.ext_ptr[(size_t)gb * g];
+        Layout<T> Lo(ng, ne, g);
+        unsigned char* b = blob.data() + (size_t)t[0] * 16;
+        reinterpret_cast<int*>(b)[0] = ng;
+        reinterpret_cast<int*>(b)[1] = ne;
+        int* eptr = reinterpret_cast<int*>(b + Lo.eptr);
+        int* gslot = reinterpret_cast<int*>(b + Lo.gslot);
+        int* gd = reinterpret_cast<int*>(b + Lo.gdst);
+        T* minv = reinterpret_cast<T*>(b + Lo.minv);
+        int* offs = reinterpret_cast<int*>(b + Lo.offs);
+        T* vals = reinterpret_cast<T*>(b + Lo.vals);
+        for (int i = 0; i <= ng * g; ++i) eptr[i] = h.ext_ptr[(size_t)gb * g + i] - e0;
+        for (int j = 0; j < ng; ++j) {
+            const int G = h.order[(size_t)gb + j];
+            const long long so = (long long)h.slot[G] * g * Q;
+            valid = valid && so >= 0 && so + g * Q <= win_elems;
+            gslot[j] = (int)so;
+            gd[j] = gdst[G];
+            for (int e = 0; e < g * g; ++e)
+                minv[(size_t)j * g * g + e] = (T)h.minv[((size_t)gb + j) * g * g + e];
+        }
+        for (int k = 0; k < ne; ++k) {
+            const int c = h.ext_col[(size_t)e0 + k], Gc = c / g;
+            const long long o = ((long long)h.slot[Gc] * g + (c - Gc * g)) * Q;
+            valid = valid && o >= 0 && o + Q <= win_elems;
+            offs[k] = (int)o;
+            vals[k] = (T)h.ext_v[(size_t)e0 + k];
+        }
+    }
+    if (!valid) {
+        if (trace_on()) std::fprintf(stderr, "[xtfem] staged sweep off: schedule check failed\n");
+        return XT_OK;
+    }
+    return finish_stage(out, h, ring, window_bytes, blob, tab, s);
+}
+
+// Node-block format (see kGrec); FP32 values, g = 3, even Q.
+int build_block_tri(const TriHost& h, int Q, const std::vector<int>& gdst, StageTri& out,
+                    cudaStream_t s)
+{
+    out.ok = false;
+    if (h.g != 3 || Q % 2) return XT_OK;
+    const int g = 3, nl = h.nlevels;
+    long long win_elems, window_bytes, ring;
+    if (!stage_sizes(h, Q, sizeof(float), win_elems, window_bytes, ring)) return XT_OK;
+    const unsigned rs = Layout<float>::up16((unsigned)(g * Q * sizeof(float)));
+    std::vector<int> tab((size_t)nl * 8, 0);
+    std::vector<unsigned> region(nl);
+    std::vector<std::vector<unsigned char>> lv(nl);
+    bool valid = true;
+    size_t total = 0;
+    std::vector<int> bn;
+    std::vector<float> bv;
+    for (int l = 0; l < nl; ++l) {
+        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
+        std::vector<unsigned char> grp((size_t)ng * kGrec, 0), blk;
+        int nb = 0;
+        for (int j = 0; j < ng; ++j) {
+            const int i = gb + j, G = h.order[i];
+            bn.clear();
+            bv.clear();
+            for (int ri = 0; ri < g; ++ri)
+                for (int k = h.ext_ptr[(size_t)i * g + ri]; k < h.ext_ptr[(size_t)i * g + ri + 1]; ++k) {
+                    const int c = h.ext_col[k], Gc = c / g;
+                    int bi = (int)(std::find(bn.begin(), bn.end(), Gc) - bn.begin());
+                    if (bi == (int)bn.size()) {
+                        bn.push_back(Gc);
+                        bv.resize(bv.size() + 9, 0.0f);
+                    }
+                    bv[(size_t)bi * 9 + ri * 3 + (c - Gc * g)] = (float)h.ext_v[k];
+                }
+            int* gr = reinterpret_cast<int*>(grp.data() + (size_t)j * kGrec);
+            const long long so = (long long)h.slot[G] * g * Q;
+            valid = valid && so >= 0 && so + g * Q <= win_elems;
+            gr[0] = nb;
+            gr[1] = (int)bn.size();
+            gr[2] = (int)so;
+            gr[3] = gdst[G];
+            float* mv = reinterpret_cast<float*>(gr + 4);
+            for (int e = 0; e < 9; ++e) mv[e] = (float)h.minv[(size_t)i * 9 + e];
+            for (size_t bi = 0; bi < bn.size(); ++bi) {
+                unsigned char rec[kBrec] = {0};
+                const long long wo = (long long)h.slot[bn[bi]] * g * Q;
+                valid = valid && wo >= 0 && wo + g * Q <= win_elems;
+                const int woff = (int)wo;
+                std::memcpy(rec, &woff, 4);
+                std::memcpy(rec + 4, &bv[bi * 9], 36);
+                blk.insert(blk.end(), rec, rec + kBrec);
+            }
+            nb += (int)bn.size();
+        }
+        std::vector<unsigned char>& b = lv[l];
+        b.assign(16, 0);
+        reinterpret_cast<int*>(b.data())[0] = ng;
+        reinterpret_cast<int*>(b.data())[1] = nb;
+        b.insert(b.end(), grp.begin(), grp.end());
+        b.insert(b.end(), blk.begin(), blk.end());
+        region[l] = (unsigned)b.size() + (unsigned)ng * rs;
+        int* t = &tab[(size_t)l * 8];
+        t[0] = (int)(total / 16);
+        t[2] = gb;
+        t[4] = (int)(b.size() / 16);
+        t[5] = (int)((unsigned)ng * rs / 16);
+        t[6] = ng;
+        t[7] = nb;
+        total += b.size();
+    }
+    valid = valid && place_ring(region, ring, tab);
+    if (!valid) {
+        if (trace_on()) std::fprintf(stderr, "[xtfem] block sweep off: schedule check failed\n");
+        return XT_OK;
+    }
+    std::vector<unsigned char> blob;
+    blob.reserve(total);
+    for (auto& b : lv) blob.insert(blob.end(), b.begin(), b.end());
+    return finish_stage(out, h, ring, window_bytes, blob, tab, s);
+}
+
+}  // namespace
+
+struct IluStage {
+    int q = 0;
+    unsigned rs = 0;  // right-hand-side record stride in bytes
+    StageTri L, U;
+    DBuf<unsigned char> rhsL, rhsU;  // ngroups records each, level order
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Reference-shaped sweep: one warp per group, factor data read from global
+// memory.  Used when the staged sweep cannot be configured.
 template <class T>
 struct TriView {
     int nlevels, g, ngroups;
     const int *level_ptr, *group_row0, *ext_ptr, *ext_col;
     const T *ext_v, *int_v, *dinv;
-    const unsigned char* blob;
-    const BlobDesc* desc;
 };
 
+TriView<double> view64(const DevTri& d)
+{
+    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+            d.ext_v64.p, d.int_v64.p, d.dinv64.p};
+}
+TriView<float> view32(const DevTri& d)
+{
+    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
+            d.ext_v32.p, d.int_v32.p, d.dinv32.p};
+}
 template <class T>
 TriView<T> view(const DevTri& d);
 template <>
-TriView<double> view<double>(const DevTri& d)
-{
-    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
-            d.ext_v64.p, d.int_v64.p, d.dinv64.p, d.blob64.p,
-            reinterpret_cast<const BlobDesc*>(d.desc64.p)};
-}
+TriView<double> view<double>(const DevTri& d) { return view64(d); }
 template <>
-TriView<float> view<float>(const DevTri& d)
-{
-    return {d.nlevels, d.g, d.ngroups, d.level_ptr.p, d.group_row0.p, d.ext_ptr.p, d.ext_col.p,
-            d.ext_v32.p, d.int_v32.p, d.dinv32.p, d.blob32.p,
-            reinterpret_cast<const BlobDesc*>(d.desc32.p)};
-}
+TriView<float> view<float>(const DevTri& d) { return view32(d); }
 
-// ---------------------------------------------------------------------------
-// Reference-shaped sweep: one warp per group, factor data read from global
-// memory.  Used when the staged sweep cannot be configured.
 template <class T, int Q, int S, bool UPPER>
 __global__ void __launch_bounds__(1024, 1)
 k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v,
@@ -306,187 +594,429 @@ k_tri_sweep(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict_
 }
 
 // ---------------------------------------------------------------------------
-// Staged sweep over per-level blobs (see the file comment).
-constexpr int kRing = 3;
-constexpr int kDescCap = 2048;  // levels whose descriptors are kept in shared memory
-
-template <class T>
-constexpr size_t slot_bytes() { return sizeof(T) == 8 ? 49152 : 40960; }
-template <class T>
-constexpr size_t staged_smem() { return kRing * slot_bytes<T>() + sizeof(BlobDesc) * kDescCap; }
-
-// block size, lanes per group and nonzeros in flight per lane: FP32 keeps a
-// whole level in one pass of 1024 threads; FP64 halves the threads to give
-// each lane the registers for its double accumulators
-template <class T>
-struct BlobCfg {
-    static constexpr int threads = sizeof(T) == 8 ? 512 : 1024;
-    static constexpr int lanes = sizeof(T) == 8 ? 8 : 16;
-    static constexpr int per = sizeof(T) == 8 ? 2 : 4;
-};
-
-template <class T, int Q, bool UPPER>
-__global__ void __launch_bounds__(BlobCfg<T>::threads, 1)
-k_tri_blob(TriView<T> t, const double* __restrict__ dAinv, const T* __restrict__ v, T* x, T* z)
+// Staged sweep.
+__device__ __forceinline__ unsigned smem_addr(const void* p)
 {
-    extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ T sAinv[Q * Q];
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const int g = t.g, nl = t.nlevels;
-    constexpr size_t SLOT = slot_bytes<T>();
-    BlobDesc* sdesc = reinterpret_cast<BlobDesc*>(smem + kRing * SLOT);
-    const bool desc_in_smem = nl <= kDescCap;
-    for (int i = tid; i < Q * Q; i += nth) sAinv[i] = (T)dAinv[i];
-    if (desc_in_smem)
-        for (int i = tid; i < nl; i += nth) sdesc[i] = t.desc[i];
-    __syncthreads();
-    const BlobDesc* desc = desc_in_smem ? sdesc : t.desc;
-    const int4* gblob = reinterpret_cast<const int4*>(t.blob);
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_tx(unsigned long long* b, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for the phase of the given parity to complete.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity)
+{
+    for (long long i = 0; i < kSpinLimit; ++i)
+        if (mbar_try_wait(b, parity)) return true;
+    return false;
+}
+// Bulk asynchronous copy global -> shared, completion counted on bar.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+__device__ __forceinline__ void named_barrier(int id, int nthreads)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
 
-    auto prefetch = [&](int L) {
-        if (L < nl) {
-            const BlobDesc d = desc[L];
-            if ((size_t)d.len16 * 16 <= SLOT) {
-                int4* dst = reinterpret_cast<int4*>(smem + (size_t)(L % kRing) * SLOT);
-                const int4* src = gblob + d.off16;
-                for (int i = tid; i < d.len16; i += nth) __pipeline_memcpy_async(dst + i, src + i, 16);
-            }
-        }
-        __pipeline_commit();
-    };
+template <class T>
+struct Pair;
+template <>
+struct Pair<float> { using type = float2; };
+template <>
+struct Pair<double> { using type = double2; };
 
-    prefetch(0);
-    prefetch(1);
-    __pipeline_wait_prior(1);
-    __syncthreads();
-    // a group is handled by kLanes lanes: lane `sub` takes every kLanes-th
-    // external nonzero of the group (all g rows together), gathers the Q
-    // solved values of its column in one go and accumulates all g x Q
-    // partial sums; shuffles reduce them, then lane r < Q finishes block r
-    constexpr int kLanes = BlobCfg<T>::lanes;
-    constexpr int kPer = BlobCfg<T>::per;  // nonzeros per lane in flight (one batch)
-    const int sub = tid % kLanes;
-    const int groups_per_pass = nth / kLanes;
-    for (int l = 0; l < nl; ++l) {
-        prefetch(l + 2);
-        const BlobDesc d = desc[l];
-        const unsigned char* base = ((size_t)d.len16 * 16 <= SLOT)
-                                        ? smem + (size_t)(l % kRing) * SLOT
-                                        : t.blob + (size_t)d.off16 * 16;
-        const BlobLayout<T> Lo(d.ne, d.ng, g);
-        const int* cols = reinterpret_cast<const int*>(base + Lo.cols);
-        const T* vals = reinterpret_cast<const T*>(base + Lo.vals);
-        const int* row0s = reinterpret_cast<const int*>(base + Lo.row0);
-        const int* eptr = reinterpret_cast<const int*>(base + Lo.eptr);
-        const T* intv = reinterpret_cast<const T*>(base + Lo.intv);
-        const T* dinv = reinterpret_cast<const T*>(base + Lo.dinv);
-        for (int pass = 0; pass < d.ng; pass += groups_per_pass) {
-            const int gi = pass + tid / kLanes;
-            const bool act = gi < d.ng;
-            const int row0 = act ? row0s[gi] : 0;
-            const int rhs = sub;  // temporal block finished by this lane (if < Q)
-            // right-hand sides of the group's rows for block `rhs`, issued
-            // before the gathers so their latency overlaps them
-            T bq[kMaxG] = {T(0), T(0), T(0)};
-            if (act && rhs < Q) {
+// Q consecutive values from p (pairs when Q is even: p is then 2*sizeof(T)
+// aligned, as every row offset is a multiple of Q in an aligned buffer).
+template <class T, int Q>
+__device__ __forceinline__ void load_row(const T* p, T (&r)[Q])
+{
+    if constexpr (Q % 2 == 0) {
+        using P = typename Pair<T>::type;
 #pragma unroll
-                for (int ri = 0; ri < kMaxG; ++ri) {
-                    if (ri < g) {
-                        if (!UPPER) {
-                            const T* vr = v + (size_t)(row0 + ri) * Q;
-                            T b = T(0);
-#pragma unroll
-                            for (int j = 0; j < Q; ++j) b = fma(sAinv[j * Q + rhs], __ldg(vr + j), b);
-                            bq[ri] = b;
-                        } else {
-                            bq[ri] = x[(size_t)(row0 + ri) * Q + rhs];
-                        }
-                    }
-                }
-            }
-            T acc[kMaxG][Q];
-#pragma unroll
-            for (int ri = 0; ri < kMaxG; ++ri)
-#pragma unroll
-                for (int b = 0; b < Q; ++b) acc[ri][b] = T(0);
-            if (act) {
-                const int kb = eptr[gi * g], ke = eptr[gi * g + g];
-                const int b1 = g > 1 ? eptr[gi * g + 1] : ke, b2 = g > 2 ? eptr[gi * g + 2] : ke;
-                for (int k0 = kb + sub; k0 < ke; k0 += kPer * kLanes) {
-                    int cc[kPer];
-                    T cv[kPer];
-#pragma unroll
-                    for (int u = 0; u < kPer; ++u) {
-                        const int k = k0 + u * kLanes;
-                        cc[u] = k < ke ? cols[k] : -1;
-                        cv[u] = k < ke ? vals[k] : T(0);
-                    }
-                    T xv[kPer][Q];
-#pragma unroll
-                    for (int u = 0; u < kPer; ++u) {
-                        const T* xr = x + (size_t)(cc[u] < 0 ? 0 : cc[u]) * Q;
-#pragma unroll
-                        for (int b = 0; b < Q; ++b) xv[u][b] = cc[u] < 0 ? T(0) : xr[b];
-                    }
-#pragma unroll
-                    for (int u = 0; u < kPer; ++u) {
-                        const int k = k0 + u * kLanes;
-                        const int ri = (k >= b1) + (k >= b2);
-#pragma unroll
-                        for (int b = 0; b < Q; ++b) {
-                            const T pr = cv[u] * xv[u][b];
-                            acc[0][b] += ri == 0 ? pr : T(0);
-                            acc[1][b] += ri == 1 ? pr : T(0);
-                            acc[2][b] += ri == 2 ? pr : T(0);
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int off = kLanes / 2; off > 0; off >>= 1)
-#pragma unroll
-                for (int ri = 0; ri < kMaxG; ++ri)
-#pragma unroll
-                    for (int b = 0; b < Q; ++b)
-                        acc[ri][b] += __shfl_xor_sync(0xffffffffu, acc[ri][b], off, kLanes);
-            if (act && rhs < Q) {
-                T accr[kMaxG];
-#pragma unroll
-                for (int ri = 0; ri < kMaxG; ++ri) {
-                    T a = acc[ri][0];
-#pragma unroll
-                    for (int b = 1; b < Q; ++b) a = (rhs == b) ? acc[ri][b] : a;
-                    accr[ri] = a;
-                }
-                const T* iv = intv + (size_t)gi * g * g;
-                T sol[kMaxG];
-#pragma unroll
-                for (int s2 = 0; s2 < kMaxG; ++s2) {
-                    if (s2 < g) {
-                        const int ri = UPPER ? g - 1 - s2 : s2;
-                        T val = bq[ri] - accr[ri];
-                        if (!UPPER) {
-                            for (int c = 0; c < ri; ++c) val -= iv[ri * g + c] * sol[c];
-                        } else {
-                            for (int c = ri + 1; c < g; ++c) val -= iv[ri * g + c] * sol[c];
-                            val *= dinv[gi * g + ri];
-                        }
-                        sol[ri] = val;
-                    }
-                }
-#pragma unroll
-                for (int ri = 0; ri < kMaxG; ++ri)
-                    if (ri < g) {
-                        x[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
-                        if (UPPER) z[(size_t)(row0 + ri) * Q + rhs] = sol[ri];
-                    }
-            }
+        for (int i = 0; i < Q / 2; ++i) {
+            const P v = reinterpret_cast<const P*>(p)[i];
+            r[2 * i] = v.x;
+            r[2 * i + 1] = v.y;
         }
-        __pipeline_wait_prior(1);
-        __syncthreads();
+    } else {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) r[i] = p[i];
+    }
+}
+// Store the values of r owned by lane `sub` of S (pairs when Q is even).
+template <class T, int Q, int S>
+__device__ __forceinline__ void store_row(T* p, const T (&r)[Q], int sub)
+{
+    if constexpr (Q % 2 == 0) {
+        using P = typename Pair<T>::type;
+#pragma unroll
+        for (int i = 0; i < Q / 2; ++i)
+            if (i % S == sub) reinterpret_cast<P*>(p)[i] = P{r[2 * i], r[2 * i + 1]};
+    } else {
+#pragma unroll
+        for (int i = 0; i < Q; ++i)
+            if (i % S == sub) p[i] = r[i];
     }
 }
 
+// Forward-sweep right-hand sides in level order: record i (stride rsE
+// elements) holds the g rows of group i, each the q values
+// sum_j Ainv(q, j) v(row, j).
+template <class T, int Q>
+__global__ void k_rhs_perm(const int* __restrict__ row0, int ng, int g,
+                           const double* __restrict__ dAinv, const T* __restrict__ v,
+                           T* __restrict__ rec, unsigned rsE)
+{
+    __shared__ T sA[Q * Q];
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sA[i] = (T)dAinv[i];
+    __syncthreads();
+    const long long total = (long long)ng * g * Q;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int gq = g * Q;
+        const int i = (int)(t / gq), e = (int)(t - (long long)i * gq);
+        const int r = e / Q, q = e - r * Q;
+        const T* vr = v + (size_t)(row0[i] + r) * Q;
+        T b = T(0);
+#pragma unroll
+        for (int j = 0; j < Q; ++j) b = fma(sA[j * Q + q], vr[j], b);
+        rec[(size_t)i * rsE + e] = b;
+    }
+}
+
+template <class T>
+struct StageArgs {
+    const unsigned char* blob;
+    const int4* table;
+    const unsigned char* rhs;  // level-ordered right-hand-side records
+    T* out;                    // forward: backward-order records; backward: z
+    int nl, g, ncw, window_bytes;
+    unsigned rs;               // record stride in bytes
+};
+
+// Producer: one thread copies every level's blob and right-hand-side chunk
+// into its ring region once the levels that used that region are consumed.
+template <class T>
+__device__ void stage_producer(const StageArgs<T>& a, unsigned long long* full,
+                               unsigned long long* cons, unsigned char* ring)
+{
+    for (int L = 0; L < a.nl; ++L) {
+        const int4 t0 = a.table[2 * L], t1 = a.table[2 * L + 1];
+        const int iss = t0.w;
+        if (iss > 0) {
+            const int c = iss - 1;
+            if (!mbar_wait(cons + c % kNB, (unsigned)(c / kNB) & 1u)) {
+                atomicExch(&g_ilu_error, 2);
+                // let the copies already issued land before the block exits
+                for (int L2 = max(0, L - kNB); L2 < L; ++L2)
+                    (void)mbar_wait(full + L2 % kNB, (unsigned)(L2 / kNB) & 1u);
+                return;
+            }
+        }
+        unsigned long long* fb = full + L % kNB;
+        if (t0.y >= 0) {
+            const unsigned blen = (unsigned)t1.x * 16u, rlen = (unsigned)t1.y * 16u;
+            mbar_arrive_tx(fb, blen + rlen);
+            unsigned char* dst = ring + (size_t)t0.y * 16;
+            bulk_g2s(dst, a.blob + (size_t)t0.x * 16, blen, fb);
+            if (rlen) bulk_g2s(dst + blen, a.rhs + (size_t)t0.z * a.rs, rlen, fb);
+        } else {
+            mbar_arrive(fb);
+        }
+    }
+}
+
+// Block skeleton shared by both formats: barrier set-up, the producer warp
+// (the last one) and the compute warps' level loop.  Body::level<RING>
+// computes one level from the ring (RING: shared-memory addresses) or from
+// global memory (levels too large for the ring).
+template <class T, class Body>
+__device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, unsigned char* smem)
+{
+    unsigned long long* full = reinterpret_cast<unsigned long long*>(smem);
+    unsigned long long* cons = full + kNB;
+    volatile int* s_abort = reinterpret_cast<volatile int*>(cons + kNB);
+    T* win = reinterpret_cast<T*>(smem + kHdrBytes);
+    unsigned char* ring = smem + kHdrBytes + a.window_bytes;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        for (int i = 0; i < kNB; ++i) {
+            mbar_init(full + i, 1);
+            mbar_init(cons + i, 1);
+        }
+        *s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (warp == a.ncw) {
+        if (lane == 0) stage_producer(a, full, cons, ring);
+        return;
+    }
+    const int nct = a.ncw * 32;
+    int4 c0 = a.table[0], c1 = a.table[1];
+    for (int l = 0; l < a.nl; ++l) {
+        const int ln = min(l + 1, a.nl - 1);
+        const int4 n0 = a.table[2 * ln], n1 = a.table[2 * ln + 1];  // used next level
+        bool ok = mbar_wait(full + l % kNB, (unsigned)(l / kNB) & 1u);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) {
+            if (lane == 0) {
+                *s_abort = 1;
+                atomicExch(&g_ilu_error, 1);
+            }
+        } else if (c0.y >= 0) {
+            const unsigned char* base = ring + (size_t)c0.y * 16;
+            body.template level<true>(win, base, reinterpret_cast<const T*>(base + (size_t)c1.x * 16),
+                                      c1.z, c1.w);
+        } else {
+            body.template level<false>(win, a.blob + (size_t)c0.x * 16,
+                                       reinterpret_cast<const T*>(a.rhs + (size_t)c0.z * a.rs), c1.z,
+                                       c1.w);
+        }
+        named_barrier(1, nct);
+        if (*s_abort) break;
+        if (tid == 0) mbar_arrive(cons + l % kNB);
+        c0 = n0;
+        c1 = n1;
+    }
+}
+
+// Row format: S lanes per row, each lane all Q temporal blocks of its share
+// of the row's nonzeros; g rows of a group in consecutive lane sets.
+template <class T, int Q, int S, bool UPPER>
+struct RowBody {
+    int g, GS, GPW, gw, ri, sub, lane0, warp, ncw;
+    bool lane_ok;
+    unsigned rsE;
+    T* out;
+    __device__ RowBody(const StageArgs<T>& a)
+    {
+        const int lane = threadIdx.x & 31;
+        warp = threadIdx.x >> 5;
+        ncw = a.ncw;
+        g = a.g;
+        GS = g * S;
+        GPW = 32 / GS;
+        gw = lane / GS;
+        const int inl = lane - gw * GS;
+        ri = inl / S;
+        sub = inl - ri * S;
+        lane0 = gw * GS;
+        lane_ok = gw < GPW;
+        rsE = a.rs / (unsigned)sizeof(T);
+        out = a.out;
+    }
+    template <bool RING>
+    __device__ __forceinline__ void level(T* win, const unsigned char* base, const T* rh, int ng,
+                                          int ne)
+    {
+        const Layout<T> Lo(ng, ne, g);
+        const int* ep = reinterpret_cast<const int*>(base + Lo.eptr);
+        const int* gsl = reinterpret_cast<const int*>(base + Lo.gslot);
+        const int* gds = reinterpret_cast<const int*>(base + Lo.gdst);
+        const T* mv = reinterpret_cast<const T*>(base + Lo.minv);
+        const int* of = reinterpret_cast<const int*>(base + Lo.offs);
+        const T* va = reinterpret_cast<const T*>(base + Lo.vals);
+        for (int j0 = warp * GPW; j0 < ng; j0 += ncw * GPW) {
+            const int j = j0 + gw;
+            const bool act = lane_ok && j < ng;
+            T acc[Q], b[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) acc[q] = b[q] = T(0);
+            if (act) {
+                const int kb = ep[j * g + ri], ke = ep[j * g + ri + 1];
+                load_row<T, Q>(rh + (size_t)j * rsE + ri * Q, b);
+#pragma unroll 2
+                for (int k = kb + sub; k < ke; k += S) {
+                    const T w = va[k];
+                    T xr[Q];
+                    load_row<T, Q>(win + of[k], xr);
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) acc[q] = fma(w, xr[q], acc[q]);
+                }
+            }
+#pragma unroll
+            for (int m = 1; m < S; m <<= 1)
+#pragma unroll
+                for (int q = 0; q < Q; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], m);
+            T d[Q], sol[Q];
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                d[q] = b[q] - acc[q];
+                sol[q] = T(0);
+            }
+#pragma unroll
+            for (int c = 0; c < kMaxG; ++c) {
+                if (c < g) {
+                    const T m = act ? mv[(size_t)j * g * g + ri * g + c] : T(0);
+#pragma unroll
+                    for (int q = 0; q < Q; ++q)
+                        sol[q] = fma(m, __shfl_sync(0xffffffffu, d[q], lane0 + c * S), sol[q]);
+                }
+            }
+            if (act) {
+                store_row<T, Q, S>(win + gsl[j] + ri * Q, sol, sub);
+                const int dst = gds[j];
+                T* go = UPPER ? out + (size_t)(dst + ri) * Q : out + (size_t)dst * rsE + ri * Q;
+                store_row<T, Q, S>(go, sol, sub);
+            }
+        }
+    }
+};
+
+// Node-block format (FP32, g = 3, even Q): one lane per (group, pair of
+// temporal blocks, share h of the group's blocks); the H shares are summed
+// with shuffles and each lane finishes its pair for all three rows.
+template <int Q, int H, bool UPPER>
+struct BlockBody {
+    static constexpr int NP = Q / 2, GS = NP * H, GPW = 32 / GS;
+    int gw, p, h, lane0, warp, ncw;
+    bool lane_ok;
+    unsigned rsE;
+    float* out;
+    __device__ BlockBody(const StageArgs<float>& a)
+    {
+        const int lane = threadIdx.x & 31;
+        warp = threadIdx.x >> 5;
+        ncw = a.ncw;
+        gw = lane / GS;
+        const int inl = lane - gw * GS;
+        h = inl / NP;
+        p = inl - h * NP;
+        lane0 = gw * GS;
+        lane_ok = gw < GPW;
+        rsE = a.rs / (unsigned)sizeof(float);
+        out = a.out;
+    }
+    template <bool RING>
+    __device__ __forceinline__ void level(float* win, const unsigned char* base, const float* rh,
+                                          int ng, int nb)
+    {
+        (void)nb;
+        const unsigned char* grec = base + 16;
+        const unsigned char* brec = grec + (size_t)kGrec * ng;
+        for (int j0 = warp * GPW; j0 < ng; j0 += ncw * GPW) {
+            const int j = j0 + gw;
+            const bool act = lane_ok && j < ng;
+            float acc[3][2];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) acc[r][0] = acc[r][1] = 0.0f;
+            int4 gh = make_int4(0, 0, 0, 0);
+            if (act) {
+                gh = *reinterpret_cast<const int4*>(grec + (size_t)j * kGrec);
+                const unsigned char* bp = brec + (size_t)gh.x * kBrec;
+#pragma unroll 2
+                for (int bi = h; bi < gh.y; bi += H) {
+                    const unsigned char* rec = bp + (size_t)bi * kBrec;
+                    const float4 r0 = *reinterpret_cast<const float4*>(rec);
+                    const float4 r1 = *reinterpret_cast<const float4*>(rec + 16);
+                    const float2 r2 = *reinterpret_cast<const float2*>(rec + 32);
+                    const float* xp = win + __float_as_int(r0.x) + 2 * p;
+                    const float2 x0 = *reinterpret_cast<const float2*>(xp);
+                    const float2 x1 = *reinterpret_cast<const float2*>(xp + Q);
+                    const float2 x2 = *reinterpret_cast<const float2*>(xp + 2 * Q);
+                    const float v[9] = {r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        acc[r][0] = fmaf(v[r * 3 + 0], x0.x, acc[r][0]);
+                        acc[r][1] = fmaf(v[r * 3 + 0], x0.y, acc[r][1]);
+                        acc[r][0] = fmaf(v[r * 3 + 1], x1.x, acc[r][0]);
+                        acc[r][1] = fmaf(v[r * 3 + 1], x1.y, acc[r][1]);
+                        acc[r][0] = fmaf(v[r * 3 + 2], x2.x, acc[r][0]);
+                        acc[r][1] = fmaf(v[r * 3 + 2], x2.y, acc[r][1]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int m = 1; m < H; m <<= 1) {
+                const int src = lane0 + (h ^ m) * NP + p;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    acc[r][0] += __shfl_sync(0xffffffffu, acc[r][0], src);
+                    acc[r][1] += __shfl_sync(0xffffffffu, acc[r][1], src);
+                }
+            }
+            if (act) {
+                const float* rr = rh + (size_t)j * rsE + 2 * p;
+                float d[3][2];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float2 bb = *reinterpret_cast<const float2*>(rr + r * Q);
+                    d[r][0] = bb.x - acc[r][0];
+                    d[r][1] = bb.y - acc[r][1];
+                }
+                const unsigned char* gm = grec + (size_t)j * kGrec + 16;
+                const float4 m0 = *reinterpret_cast<const float4*>(gm);
+                const float4 m1 = *reinterpret_cast<const float4*>(gm + 16);
+                const float m8 = *reinterpret_cast<const float*>(gm + 32);
+                const float mv[9] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w, m8};
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    if (r % H != h) continue;  // row r is stored by share r mod H
+                    float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        s0 = fmaf(mv[r * 3 + c], d[c][0], s0);
+                        s1 = fmaf(mv[r * 3 + c], d[c][1], s1);
+                    }
+                    const float2 sv = make_float2(s0, s1);
+                    *reinterpret_cast<float2*>(win + gh.z + r * Q + 2 * p) = sv;
+                    float* go = UPPER ? out + (size_t)(gh.w + r) * Q + 2 * p
+                                      : out + (size_t)gh.w * rsE + r * Q + 2 * p;
+                    *reinterpret_cast<float2*>(go) = sv;
+                }
+            }
+        }
+    }
+};
+
+template <class T, int Q, int S, bool UPPER>
+__global__ void __launch_bounds__(kStageThreads, 1) k_tri_stage(StageArgs<T> a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    RowBody<T, Q, S, UPPER> body(a);
+    stage_main<T>(a, body, smem);
+}
+
+template <int Q, int H, bool UPPER>
+__global__ void __launch_bounds__(kStageThreads, 1) k_tri_block(StageArgs<float> a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    BlockBody<Q, H, UPPER> body(a);
+    stage_main<float>(a, body, smem);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers.
 template <class T, int Q>
 int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work,
                       cudaStream_t s)
@@ -499,25 +1029,160 @@ int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T*
     return XT_OK;
 }
 
+int env_int(const char* name, int dflt)
+{
+    const char* e = std::getenv(name);
+    return e ? std::atoi(e) : dflt;
+}
+
+// Staged-sweep data for (q, T, format), built on first use; nullptr when
+// the factor cannot use that staged sweep.  fmt 0: rows, 1: node blocks.
+template <class T>
+int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out)
+{
+    out = nullptr;
+    if (!F.sched || env_int("XTFEM_ILU_SIMPLE", 0)) return XT_OK;
+    const int key = 4 * q + 2 * fmt + (sizeof(T) == 4 ? 1 : 0);
+    auto it = F.stages.find(key);
+    if (it == F.stages.end()) {
+        auto st = std::make_shared<IluStage>();
+        st->q = q;
+        const TriHost& L = F.sched->L;
+        const TriHost& U = F.sched->U;
+        const int ng = L.ngroups, g = L.g;
+        std::vector<int> gdL(ng), gdU(ng);
+        for (int G = 0; G < ng; ++G) {
+            gdL[G] = U.pos[G];
+            gdU[G] = G * g;
+        }
+        if (fmt == 1) {
+            if (sizeof(T) == 4) {
+                XT_TRY(build_block_tri(L, q, gdL, st->L, s));
+                XT_TRY(build_block_tri(U, q, gdU, st->U, s));
+            }
+        } else {
+            XT_TRY(build_row_tri<T>(L, q, gdL, st->L, s));
+            XT_TRY(build_row_tri<T>(U, q, gdU, st->U, s));
+        }
+        if (st->L.ok && st->U.ok) {
+            st->rs = Layout<T>::up16((unsigned)(g * q * sizeof(T)));
+            XT_TRY(st->rhsL.alloc((size_t)ng * st->rs));
+            XT_TRY(st->rhsU.alloc((size_t)ng * st->rs));
+        }
+        it = F.stages.emplace(key, st).first;
+    }
+    if (it->second->L.ok && it->second->U.ok) out = it->second.get();
+    return XT_OK;
+}
+
+template <class T>
+StageArgs<T> stage_args(const StageTri& t, const unsigned char* rhs, T* out, int ncw, unsigned rs)
+{
+    return {t.blob.p, reinterpret_cast<const int4*>(t.table.p), rhs, out, t.nlevels, t.g, ncw,
+            t.window_bytes, rs};
+}
+
+// Pre-pass, forward sweep kl and backward sweep ku of a staged solve; GPW
+// groups per compute warp.
+template <class T, int Q>
+int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs<T>),
+              void (*ku)(StageArgs<T>), bool& attr, const double* dAinv, const T* v, T* z,
+              cudaStream_t s)
+{
+    if (!attr) {
+        XT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+        XT_CUDA(cudaFuncSetAttribute(ku, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+        attr = true;
+    }
+    const int g = F.L.g, ng = F.L.ngroups;
+    auto warps = [&](const StageTri& t) {
+        const int w = env_int("XTFEM_ILU_WARPS", (t.p90 + GPW - 1) / GPW);
+        return std::max(1, std::min(kStageThreads / 32 - 1, w));
+    };
+    const int wL = warps(st.L), wU = warps(st.U);
+    const long long total = (long long)ng * g * Q;
+    const int nblk = (int)std::max(1LL, std::min<long long>((total + 255) / 256, 152LL * 8));
+    T* recL = reinterpret_cast<T*>(st.rhsL.p);
+    T* recU = reinterpret_cast<T*>(st.rhsU.p);
+    k_rhs_perm<T, Q><<<nblk, 256, 0, s>>>(F.L.group_row0.p, ng, g, dAinv, v, recL,
+                                          st.rs / (unsigned)sizeof(T));
+    const size_t smL = kHdrBytes + (size_t)st.L.window_bytes + st.L.ring_bytes;
+    const size_t smU = kHdrBytes + (size_t)st.U.window_bytes + st.U.ring_bytes;
+    kl<<<1, (wL + 1) * 32, smL, s>>>(stage_args<T>(st.L, st.rhsL.p, recU, wL, st.rs));
+    ku<<<1, (wU + 1) * 32, smU, s>>>(stage_args<T>(st.U, st.rhsU.p, z, wU, st.rs));
+    note_launches(3);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <class T, int Q, int S>
+int launch_rows(const DevIlu& F, const IluStage& st, const double* dAinv, const T* v, T* z,
+                cudaStream_t s)
+{
+    static bool attr = false;
+    return run_stage<T, Q>(F, st, 32 / (F.L.g * S), k_tri_stage<T, Q, S, false>,
+                           k_tri_stage<T, Q, S, true>, attr, dAinv, v, z, s);
+}
+
+template <int Q, int H>
+int launch_blocks(const DevIlu& F, const IluStage& st, const double* dAinv, const float* v,
+                  float* z, cudaStream_t s)
+{
+    static bool attr = false;
+    return run_stage<float, Q>(F, st, BlockBody<Q, H, false>::GPW, k_tri_block<Q, H, false>,
+                               k_tri_block<Q, H, true>, attr, dAinv, v, z, s);
+}
+
 template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
 {
-    const bool blob = F.L.g <= kMaxG && F.U.g <= kMaxG && (sizeof(T) == 8 ? F.L.blob64.p : F.L.blob32.p);
-    if (!blob) return launch_tri_simple<T, Q>(F, dAinv, v, z, work, s);
-    const size_t bytes = staged_smem<T>();
-    static bool attr = false;
-    if (!attr) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_blob<T, Q, false>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_blob<T, Q, true>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-        attr = true;
+    IluStage* st = nullptr;
+    if constexpr (sizeof(T) == 4 && Q % 2 == 0) {
+        if (F.L.g == 3 && env_int("XTFEM_ILU_FMT", 1) == 1) {
+            XT_TRY(get_stage<T>(F, Q, 1, s, st));
+            if (st) {
+                const int H = env_int("XTFEM_ILU_SHARES", 2);
+                if constexpr (Q == 6) {
+                    if (H == 1) return launch_blocks<Q, 1>(F, *st, dAinv, v, z, s);
+                    if (H == 4) return launch_blocks<Q, 4>(F, *st, dAinv, v, z, s);
+                }
+                return launch_blocks<Q, 2>(F, *st, dAinv, v, z, s);
+            }
+        }
     }
-    constexpr int nt = BlobCfg<T>::threads;
-    k_tri_blob<T, Q, false><<<1, nt, bytes, s>>>(view<T>(F.L), dAinv, v, work, nullptr);
-    k_tri_blob<T, Q, true><<<1, nt, bytes, s>>>(view<T>(F.U), dAinv, nullptr, work, z);
-    note_launches(2);
-    XT_CUDA(cudaGetLastError());
+    if (F.L.g <= kMaxG) XT_TRY(get_stage<T>(F, Q, 0, s, st));
+    if (!st) return launch_tri_simple<T, Q>(F, dAinv, v, z, work, s);
+    if constexpr (Q == 6) {
+        const int S = env_int("XTFEM_ILU_LANES", 2);
+        if (S == 1) return launch_rows<T, Q, 1>(F, *st, dAinv, v, z, s);
+        if (S == 4) return launch_rows<T, Q, 4>(F, *st, dAinv, v, z, s);
+    }
+    return launch_rows<T, Q, 2>(F, *st, dAinv, v, z, s);
+}
+
+int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
+{
+    d.ngroups = h.ngroups;
+    d.nlevels = h.nlevels;
+    d.g = h.g;
+    d.max_level_groups = h.maxw;
+    XT_TRY(d.level_ptr.upload(h.level_ptr.data(), h.level_ptr.size(), s));
+    XT_TRY(d.group_row0.upload(h.group_row0.data(), h.group_row0.size(), s));
+    XT_TRY(d.ext_ptr.upload(h.ext_ptr.data(), h.ext_ptr.size(), s));
+    const size_t ne = h.ext_col.size();
+    std::vector<float> f32(h.ext_v.begin(), h.ext_v.end());
+    std::vector<float> i32(h.int_v.begin(), h.int_v.end());
+    std::vector<float> d32(h.dinv.begin(), h.dinv.end());
+    XT_TRY(d.ext_col.upload(ne ? h.ext_col.data() : nullptr, ne, s));
+    XT_TRY(d.ext_v64.upload(h.ext_v.data(), ne, s));
+    XT_TRY(d.ext_v32.upload(f32.data(), ne, s));
+    XT_TRY(d.int_v64.upload(h.int_v.data(), h.int_v.size(), s));
+    XT_TRY(d.int_v32.upload(i32.data(), i32.size(), s));
+    if (!h.dinv.empty()) {
+        XT_TRY(d.dinv64.upload(h.dinv.data(), h.dinv.size(), s));
+        XT_TRY(d.dinv32.upload(d32.data(), d32.size(), s));
+    }
+    XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     return XT_OK;
 }
 
@@ -548,10 +1213,13 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
         }
     const int g = (group > 1 && n % group == 0 && group <= kMaxG) ? group : 1;
     d.n = n;
-    TriHost L = schedule(n, alu, jlu, ju, g, false);
-    TriHost U = schedule(n, alu, jlu, ju, g, true);
-    XT_TRY(upload_tri(d.L, L, s));
-    XT_TRY(upload_tri(d.U, U, s));
+    auto sc = std::make_shared<IluSched>();
+    sc->L = schedule(n, alu, jlu, ju, g, false);
+    sc->U = schedule(n, alu, jlu, ju, g, true);
+    XT_TRY(upload_tri(d.L, sc->L, s));
+    XT_TRY(upload_tri(d.U, sc->U, s));
+    d.sched = sc;
+    d.stages.clear();
     return XT_OK;
 }
 
@@ -578,5 +1246,21 @@ template int ilu_apply<double>(const DevIlu&, int, const double*, const double*,
                                double*, cudaStream_t);
 template int ilu_apply<float>(const DevIlu&, int, const double*, const float*, float*, float*,
                               cudaStream_t);
+
+int ilu_check(cudaStream_t s)
+{
+    int h = 0;
+    XT_CUDA(cudaMemcpyFromSymbolAsync(&h, g_ilu_error, sizeof(int), 0, cudaMemcpyDeviceToHost, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    if (h != 0) {
+        const int zero = 0;
+        XT_CUDA(cudaMemcpyToSymbolAsync(g_ilu_error, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, s));
+        XT_CUDA(cudaStreamSynchronize(s));
+        set_error(h == 1 ? "ILU sweep: wait for a level's data gave up"
+                         : "ILU sweep: producer wait for a consumed level gave up");
+        return XT_ERR_CUDA;
+    }
+    return XT_OK;
+}
 
 }  // namespace xt

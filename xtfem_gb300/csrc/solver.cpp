@@ -363,7 +363,8 @@ int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int ma
         return XT_ERR_ARG;
     }
     XT_TRY(ensure_workspace(S, im, false));
-    return gmres_core<double>(S, b, x, im, eps, maxits, st, hist);
+    XT_TRY(gmres_core<double>(S, b, x, im, eps, maxits, st, hist));
+    return ilu_check(ctx().stream);
 }
 
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
@@ -417,6 +418,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
             XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
         }
         XT_CUDA(cudaStreamSynchronize(s));
+        XT_TRY(ilu_check(s));
         st.its += in.its;
         st.cycles += in.cycles;
         st.est = in.est;

@@ -13,6 +13,8 @@
 #include "../../include/xtfem_gb300.h"
 
 #include <cstdint>
+#include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -105,8 +107,7 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 // -------------------------------------------------- ILU triangular solves
 // Level-scheduled form of a SPARSKIT MSR factor.  Rows are handled in groups
 // of g consecutive rows (g = 3 for three DOFs per node, else 1); a group's
-// level is one more than the deepest group it depends on outside itself, and
-// the rows inside a group are solved in sequence by one warp.
+// level is one more than the deepest group it depends on outside itself.
 struct DevTri {
     int ngroups = 0, nlevels = 0, g = 1;
     DBuf<int> level_ptr;   // nlevels+1, into the level-ordered group list
@@ -120,15 +121,17 @@ struct DevTri {
     DBuf<double> dinv64;   // per group g inverted diagonals (upper only)
     DBuf<float> dinv32;
     int max_level_groups = 0;
-    // per-level packed blobs (FP64 and FP32 values) and their descriptors
-    // (offset, length in 16-byte units, groups, nonzeros)
-    DBuf<unsigned char> blob64, blob32;
-    DBuf<int> desc64, desc32;
 };
+
+struct IluSched;  // host copy of both level schedules (dev_ilu.cu)
+struct IluStage;  // staged-sweep data for one temporal width and precision
 
 struct DevIlu {
     int n = 0;
     DevTri L, U;
+    std::shared_ptr<IluSched> sched;
+    // built on first use for a (q, precision) pair; key 2*q + (FP32 ? 1 : 0)
+    mutable std::map<int, std::shared_ptr<IluStage>> stages;
 };
 
 // Build the level schedule from the 1-based MSR arrays and upload it.
@@ -142,6 +145,10 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
 template <class T>
 int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* work,
               cudaStream_t s);
+
+// Reads and clears the device-side error word of the staged sweeps (a
+// bounded wait that gave up); XT_OK when clear.
+int ilu_check(cudaStream_t s);
 
 // ----------------------------------------------------- Krylov vector ops
 // Reduction scratch sized for the largest restart length in use.
