@@ -134,11 +134,12 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6):
     ilu64 = ilu_nnz * (8 + 4) + 2 * (p + 1) * 4 + p * 8 + 2 * p * q * 8
     ngp = 8 * ne
     damage = ngp * (29 * 8 * 2 + 8 * 4 + 24 * 8 + 2 * 8) + p * q * 8
-    return {0: kron64, 1: kron32, 2: ilu64, 3: ilu32, 4: damage}
+    # a CGS2 step's bytes depend on the step index; its class reports time only
+    return {0: kron64, 1: kron32, 2: ilu64, 3: ilu32, 4: damage, 5: None, 6: None}
 
 
 CLASS_NAMES = {0: "kron_spmm_fp64", 1: "kron_spmm_fp32", 2: "ilu_apply_fp64",
-               3: "ilu_apply_fp32", 4: "damage_update"}
+               3: "ilu_apply_fp32", 4: "damage_update", 5: "cgs2_step_fp64", 6: "cgs2_step_fp32"}
 
 
 # -------------------------------------------------------------- GPU arm
@@ -176,7 +177,7 @@ def run_gpu(args, rank, world):
     # roofline of the dominant kernel class
     hbm, peak_kind = peaks()
     nbytes = algorithmic_bytes(prob, ilu_nnz, p)
-    dom = max(prof, key=lambda c: prof[c][1])
+    dom = max((c for c in prof if nbytes[c]), key=lambda c: prof[c][1])
     cnt, tot = prof[dom]
     avg_ms = tot / max(cnt, 1)
     achieved = nbytes[dom] / (avg_ms / 1e3) / 1e9 if cnt else 0.0
@@ -184,7 +185,7 @@ def run_gpu(args, rank, world):
                                 "avg_us": round(1e3 * prof[c][1] / max(prof[c][0], 1), 2),
                                 "bytes_per_launch": nbytes[c],
                                 "gbs": round(nbytes[c] / (prof[c][1] / max(prof[c][0], 1) / 1e3)
-                                             / 1e9, 1) if prof[c][0] else None}
+                                             / 1e9, 1) if prof[c][0] and nbytes[c] else None}
                for c in prof}
     its = [s["its"] for s in steps]
     res = [s["relres"] for s in steps]

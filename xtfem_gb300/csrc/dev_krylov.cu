@@ -59,6 +59,145 @@ __global__ void k_multi_dot(const TV* __restrict__ V, size_t ld, int k, const TV
     }
 }
 
+// Double-float helpers: a value held as hi + lo in two FP32 numbers.
+// Knuth's two-sum keeps the rounding error of every addition; explicit _rn
+// intrinsics keep the compiler from fusing or reordering the steps.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float x)
+{
+    const float s = __fadd_rn(hi, x);
+    const float bb = __fsub_rn(s, hi);
+    const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+    hi = s;
+    lo = __fadd_rn(lo, t);
+}
+__device__ __forceinline__ void df_add_df(float& hi, float& lo, float xh, float xl)
+{
+    df_add(hi, lo, xh);
+    lo = __fadd_rn(lo, xl);
+}
+
+// FP32 basis (n and ld even, pairs of rows): each pair of products is
+// formed in FP32 and accumulated in double-float, reduced across the block
+// in double-float; the block's (hi, lo) pair is stored in the FP64 partial
+// slot and k_finish_df adds the pairs in FP64.  The part's FP64 rate is
+// 1/64 of its FP32 rate, so no FP64 instruction is issued per element.
+__global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
+                                const float2* __restrict__ w, size_t n2,
+                                double* __restrict__ partial)
+{
+    __shared__ float2 sh[kChunk][32];
+    const int j0 = blockIdx.y * kChunk;
+    const int nb = gridDim.x;
+    const size_t per = (n2 + nb - 1) / nb;
+    const size_t r0 = per * blockIdx.x, r1 = min(n2, r0 + per);
+    float hi[kChunk], lo[kChunk];
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) hi[c] = lo[c] = 0.0f;
+    for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const float2 wr = w[r];
+        float2 v[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c)
+            v[c] = (j0 + c < k) ? V[(size_t)(j0 + c) * ld2 + r] : make_float2(0.0f, 0.0f);
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) df_add(hi[c], lo[c], fmaf(v[c].y, wr.y, v[c].x * wr.x));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi[c], off);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo[c], off);
+            df_add_df(hi[c], lo[c], oh, ol);
+        }
+        if (lane == 0) sh[c][warp] = make_float2(hi[c], lo[c]);
+    }
+    __syncthreads();
+    if (threadIdx.x < kChunk && j0 + (int)threadIdx.x < k) {
+        const int c = threadIdx.x;
+        float h = 0.0f, l = 0.0f;
+        for (int wi = 0; wi < nw; ++wi) df_add_df(h, l, sh[c][wi].x, sh[c][wi].y);
+        reinterpret_cast<float2*>(partial)[(size_t)(j0 + c) * nb + blockIdx.x] = make_float2(h, l);
+    }
+}
+
+// out[j] = sum_b (hi_b + lo_b) in FP64, one block per j, fixed order
+__global__ void k_finish_df(const double* __restrict__ partial, int nb, double* __restrict__ out)
+{
+    __shared__ double sh[32];
+    const int j = blockIdx.x;
+    const float2* p = reinterpret_cast<const float2*>(partial) + (size_t)j * nb;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += (double)p[b].x + (double)p[b].y;
+    const double s = block_sum(v, sh);
+    if (threadIdx.x == 0) out[j] = s;
+}
+
+// acc := acc - (a + b) v for acc = hi + lo held as two FP32 values: the
+// product a v is split exactly (fma), the subtraction is Knuth's two-sum,
+// and the low-order terms gather in lo (double-float arithmetic, about 48
+// significant bits; explicit _rn intrinsics keep the compiler from fusing
+// the error-free steps).
+__device__ __forceinline__ void df_sub_prod(float& hi, float& lo, float a, float b, float v)
+{
+    const float p = __fmul_rn(a, v);
+    const float e = fmaf(a, v, -p);
+    const float s = __fsub_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(-p, bb));
+    lo = fmaf(-b, v, __fsub_rn(__fadd_rn(lo, t), e));
+    hi = s;
+}
+
+// w -= V h for an FP32 basis with double-float accumulation (the update can
+// cancel most of w, so it is not summed in plain FP32); optional ||w||^2.
+template <bool NORM>
+__global__ void k_update_f32(const float2* __restrict__ V, size_t ld2, int k,
+                             const double* __restrict__ h, float2* __restrict__ w, size_t n2,
+                             double* __restrict__ partial)
+{
+    __shared__ double sh[32];
+    __shared__ float2 hs[512];
+    for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) {
+        const float a = (float)h[j];
+        hs[j] = make_float2(a, (float)(h[j] - (double)a));
+    }
+    __syncthreads();
+    double nrm = 0.0;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n2; r += stride) {
+        const float2 wv = w[r];
+        float hx = wv.x, lx = 0.0f, hy = wv.y, ly = 0.0f;
+        for (int jb = 0; jb < k; jb += 8) {
+            float2 v[8];  // eight independent loads in flight per thread
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                v[u] = (jb + u < k) ? V[(size_t)(jb + u) * ld2 + r] : make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int j = jb + u;
+                if (j >= k) break;
+                float2 hj;
+                if (j < 512) hj = hs[j];
+                else {
+                    const float a = (float)h[j];
+                    hj = make_float2(a, (float)(h[j] - (double)a));
+                }
+                df_sub_prod(hx, lx, hj.x, hj.y, v[u].x);
+                df_sub_prod(hy, ly, hj.x, hj.y, v[u].y);
+            }
+        }
+        const float2 out = make_float2(__fadd_rn(hx, lx), __fadd_rn(hy, ly));
+        w[r] = out;
+        if (NORM) nrm = fma((double)out.x, (double)out.x, fma((double)out.y, (double)out.y, nrm));
+    }
+    if (NORM) {
+        const double s = block_sum(nrm, sh);
+        if (threadIdx.x == 0) partial[blockIdx.x] = s;
+    }
+}
+
 // out[j] = sum_b partial[j * nb + b], one block per j, fixed order
 __global__ void k_finish(const double* __restrict__ partial, int nb, double* __restrict__ out,
                          int accumulate)
@@ -207,6 +346,15 @@ __global__ void k_max_finish(const double* __restrict__ partial, int nb, double*
     }
 }
 
+// FP32 basis stored as row pairs: n and ld even, 8-byte aligned vectors.
+template <class TV>
+bool pairs_ok(const TV* V, size_t ld, const TV* w, size_t n)
+{
+    if (sizeof(TV) != 4) return false;
+    return n % 2 == 0 && ld % 2 == 0 && reinterpret_cast<uintptr_t>(V) % 8 == 0 &&
+           reinterpret_cast<uintptr_t>(w) % 8 == 0;
+}
+
 int grid_for(size_t n)
 {
     size_t b = (n + kThreads - 1) / kThreads;
@@ -233,8 +381,15 @@ int multi_dot(const TV* V, size_t ld, int k, const TV* w, size_t n, Reduce& r, c
     if (k > r.kmax) { set_error("multi_dot: k exceeds reduction capacity"); return XT_ERR_ARG; }
     if (k <= 0) return XT_OK;
     dim3 grid(r.nblocks, (k + kChunk - 1) / kChunk);
-    k_multi_dot<TV><<<grid, kThreads, 0, s>>>(V, ld, k, w, n, r.partial.p);
-    k_finish<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p, 0);
+    if (pairs_ok<TV>(V, ld, w, n)) {
+        k_multi_dot_f32<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float2*>(V), ld / 2, k,
+                                                  reinterpret_cast<const float2*>(w), n / 2,
+                                                  r.partial.p);
+        k_finish_df<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p);
+    } else {
+        k_multi_dot<TV><<<grid, kThreads, 0, s>>>(V, ld, k, w, n, r.partial.p);
+        k_finish<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p, 0);
+    }
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -245,7 +400,12 @@ int update_and_dot(const TV* V, size_t ld, int k, const double* h, TV* w, size_t
                    cudaStream_t s)
 {
     if (k <= 0) return XT_OK;
-    k_update<TV, false><<<grid_for(n), kThreads, 0, s>>>(V, ld, k, h, w, n, nullptr);
+    if (pairs_ok<TV>(V, ld, w, n))
+        k_update_f32<false><<<grid_for(n / 2), kThreads, 0, s>>>(
+            reinterpret_cast<const float2*>(V), ld / 2, k, h, reinterpret_cast<float2*>(w), n / 2,
+            nullptr);
+    else
+        k_update<TV, false><<<grid_for(n), kThreads, 0, s>>>(V, ld, k, h, w, n, nullptr);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return multi_dot<TV>(V, ld, k, w, n, r, s);
@@ -256,7 +416,11 @@ int update_and_norm(const TV* V, size_t ld, int k, const double* h, TV* w, size_
                     cudaStream_t s)
 {
     const int nb = r.nblocks;
-    if (k > 0) {
+    if (k > 0 && pairs_ok<TV>(V, ld, w, n)) {
+        k_update_f32<true><<<nb, 2 * kThreads, 0, s>>>(reinterpret_cast<const float2*>(V), ld / 2,
+                                                       k, h, reinterpret_cast<float2*>(w), n / 2,
+                                                       r.partial.p);
+    } else if (k > 0) {
         k_update<TV, true><<<nb, kThreads, 0, s>>>(V, ld, k, h, w, n, r.partial.p);
     } else {
         k_norm2<TV><<<nb, kThreads, 0, s>>>(w, n, r.partial.p);

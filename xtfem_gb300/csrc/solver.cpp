@@ -272,6 +272,7 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
             XT_TRY(apply_prec<T>(S, col(i - 1), z));
             XT_TRY(apply_op<T>(S, z, col(i1 - 1)));
             // CGS2 projection against the i previous vectors
+            const int otok = prof_begin(sizeof(T) == 8 ? PROF_ORTH64 : PROF_ORTH32, s);
             XT_TRY(multi_dot<T>(V, n, i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
@@ -281,6 +282,7 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
             XT_TRY(update_and_norm<T>(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
+            prof_end(otok, s);
             XT_TRY(fetch(hbuf.data(), S.hsave.p, 2 * i + 1));
             for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
             t = std::sqrt(hbuf[2 * i]);
