@@ -36,9 +36,13 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = dict(nx=60, ny=20, nz=20, lx=3.0, ly=1.0, lz=1.0, E=2.0e5, nu=0.3, rho=7.8e-9,
                 freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256, lfil=20, droptol=1e-4, im=200,
-                tol=1e-8, inner_tol=1e-5, Dc=0.99, seed=0)
+                tol=1e-8, inner_tol=1e-5, Dc=0.99, seed=0, precision=2)
 METRIC = "time-slab solves/s to rel.res 1e-8, mixed-prec batched vs FP64 GMRES, 1 GB300"
 UNIT = "slab-solves/s"
+DTYPE_NAMES = {0: "fp64", 1: "fp32 operator/factor/basis, fp64 residual+refinement+damage",
+               2: "fp32 ilu factor and apply; fp64 operator, basis, residual, damage"}
+PRECISION_NAMES = {0: "fp64 gmres", 1: "fp32 gmres inside fp64 refinement",
+                   2: "flexible gmres: fp64 operator+basis, fp32 ilu, fp64 refinement"}
 
 
 def amplitude(seed):
@@ -148,7 +152,7 @@ def run_gpu(args, rank, world):
 
     xt.lib().xt_init(int(os.environ.get("LOCAL_RANK", "0")))
     prob = make_problem(xt)
-    cfg = make_config(xt, precision=1, seed=WORKLOAD["seed"] + rank)
+    cfg = make_config(xt, precision=WORKLOAD["precision"], seed=WORKLOAD["seed"] + rank)
     slab = xt.SlabSolver(prob, cfg)
     p = slab.p
     K = prob.K()
@@ -193,13 +197,14 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "fp32 operator/factor/basis, fp64 residual+refinement+damage",
+        "dtype": DTYPE_NAMES[WORKLOAD["precision"]],
         "data": "synthetic (generated rod mesh, seeded load amplitude)",
         "config": {"workload": "C2 prismatic rod 20x20x60 C3D8, 80,703 DOF x 6 temporal blocks",
                    "nip": WORKLOAD["nipc"] * WORKLOAD["n1"], "ilut": [WORKLOAD["droptol"],
                                                                       WORKLOAD["lfil"]],
                    "gmres_restart": WORKLOAD["im"], "tol": WORKLOAD["tol"],
-                   "precision": "fp32 inner + fp64 refinement", "amplitude_mpa": cfg.amplitude,
+                   "precision": PRECISION_NAMES[WORKLOAD["precision"]],
+                   "amplitude_mpa": cfg.amplitude,
                    "l2": "inputs larger than L2 (operator+factor+basis >> 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "iterations_per_slab": float(np.mean(its)), "relres_max": float(np.max(res)),
@@ -245,7 +250,7 @@ def run_e2e(xt, args, world):
     go host->device and the slab displacement and damage come back, every
     step, inside the timed region."""
     prob = make_problem(xt)
-    cfg = make_config(xt, precision=1, seed=WORKLOAD["seed"])
+    cfg = make_config(xt, precision=WORKLOAD["precision"], seed=WORKLOAD["seed"])
     slab = xt.SlabSolver(prob, cfg)
     p = slab.p
     xyz, conn = prob.mesh()
@@ -418,11 +423,16 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--im", type=int, default=None)
+    ap.add_argument("--precision", type=int, default=None,
+                    help="inner solve: 1 = FP32 GMRES in FP64 refinement, 2 = flexible GMRES "
+                         "(FP64 operator and basis, FP32 factor)")
     args = ap.parse_args()
     if args.inner_tol is not None:
         WORKLOAD["inner_tol"] = args.inner_tol
     if args.im is not None:
         WORKLOAD["im"] = args.im
+    if args.precision is not None:
+        WORKLOAD["precision"] = args.precision
     rank, world = dist_setup()
     if args.impl == "reference":
         out = run_reference(args, rank, world)

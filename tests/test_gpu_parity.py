@@ -173,7 +173,7 @@ def test_gmres_iteration_history_tracks_oracle(xt, orc, rod_system):
     sysm.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1, 2])
 def test_refined_solve_reaches_true_residual(xt, orc, rod_system, precision):
     s = rod_system
     rhs = c1_rhs(xt, s)

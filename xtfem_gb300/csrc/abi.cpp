@@ -303,7 +303,7 @@ int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double 
                     int precision, double inner_tol, double* out_stats)
 {
     if (!h || !rhs || !sol) { set_error("xt_system_solve: null argument"); return XT_ERR_ARG; }
-    if (precision != 0 && precision != 1) { set_error("xt_system_solve: precision is 0 or 1"); return XT_ERR_ARG; }
+    if (precision < 0 || precision > 2) { set_error("xt_system_solve: precision is 0, 1 or 2"); return XT_ERR_ARG; }
     System& S = h->sys;
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(ensure_vec(S.b64, n));

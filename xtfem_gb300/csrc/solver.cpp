@@ -155,7 +155,7 @@ int system_apply(System& S, double alpha, double beta, const double* x, double* 
 
 namespace {
 
-int ensure_workspace(System& S, int im, bool fp32)
+int ensure_workspace(System& S, int im, bool fp32, bool flex = false)
 {
     const size_t n = (size_t)S.p * S.q;
     if (im > S.im_cap || S.red.kmax < im + 1) {
@@ -177,6 +177,11 @@ int ensure_workspace(System& S, int im, bool fp32)
         XT_TRY(S.u32.alloc(n));
         XT_TRY(S.d32.alloc(n));
         XT_TRY(S.r32.alloc(n));
+    }
+    if (flex) {
+        if (S.Z32.n < n * (size_t)im) XT_TRY(S.Z32.alloc(n * (size_t)im));
+        XT_TRY(S.d32.alloc(n));
+        XT_TRY(S.w32.alloc(n));
     }
     XT_TRY(S.x64.alloc(n));
     XT_TRY(S.r64.alloc(n));
@@ -206,6 +211,15 @@ int apply_op(System& S, const T* x, T* y)
 {
     const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, ctx().stream);
     const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, 1.0, 0.0, x, y, ctx().stream);
+    prof_end(tok, ctx().stream);
+    return st;
+}
+
+template <class T>
+int apply_op_ab(System& S, double alpha, double beta, const T* x, T* y)
+{
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, ctx().stream);
+    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, ctx().stream);
     prof_end(tok, ctx().stream);
     return st;
 }
@@ -351,6 +365,117 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
     return XT_OK;
 }
 
+
+// Flexible GMRES (right preconditioning with the preconditioned vectors
+// kept): the control flow of kronpgmres (src/kronecker.f90:181-365) with
+// an FP64 operator and FP64 basis V, and the ILU applied in FP32; z_j =
+// M^-1 v_j is stored (FP32) and the solution update is x += Z y, so the
+// Arnoldi relation A Z = V H holds to FP64 accuracy however the FP32
+// preconditioner rounds.  A restart rebuilds the residual explicitly.
+int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
+               GmresStats& st)
+{
+    cudaStream_t s = ctx().stream;
+    const size_t n = (size_t)S.p * S.q;
+    double* V = S.V64.p;
+    float* Z = S.Z32.p;
+    auto col = [&](int j) { return V + (size_t)j * n; };
+    auto zc = [&](int j) { return Z + (size_t)j * n; };
+    std::vector<double> hh((size_t)(im + 1) * im, 0.0), c(im, 0.0), sn(im, 0.0), rs(im + 1, 0.0);
+    std::vector<double> hbuf(2 * (im + 1) + 2);
+    auto HH = [&](int r, int k) -> double& { return hh[(size_t)k * (im + 1) + r]; };
+    const double epsmac = 1.0e-16;
+    int its = 0, i = 0, ierr = 0;
+    double ro = 0.0, eps1 = 0.0, t;
+
+    XT_TRY(norm2<double>(rhs, n, S.red, s));
+    XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+    const double ro0 = std::sqrt(hbuf[0]);
+    for (;;) {
+        // v1 = rhs - A sol
+        XT_CUDA(cudaMemcpyAsync(col(0), rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, col(0)));
+        XT_TRY(norm2<double>(col(0), n, S.red, s));
+        XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+        ro = std::sqrt(hbuf[0]);
+        if (!std::isfinite(ro)) {
+            set_error("gmres: non-finite residual");
+            return XT_ERR_NONFINITE;
+        }
+        if (ro == 0.0) { ierr = -1; break; }
+        XT_TRY((axpby<double, double>(n, 1.0 / ro, col(0), 0.0, col(0), s)));
+        if (its == 0) eps1 = eps * ro;
+        rs.assign(im + 1, 0.0);
+        rs[0] = ro;
+        i = 0;
+        ++st.cycles;
+        for (;;) {
+            ++i;
+            ++its;
+            const int i1 = i + 1;
+            XT_TRY((axpby<double, float>(n, 1.0, col(i - 1), 0.0, S.d32.p, s)));
+            XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
+            XT_TRY((axpby<float, double>(n, 1.0, zc(i - 1), 0.0, S.u64.p, s)));
+            XT_TRY(apply_op<double>(S, S.u64.p, col(i1 - 1)));
+            const int otok = prof_begin(PROF_ORTH64, s);
+            XT_TRY(multi_dot<double>(V, n, i, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(update_and_dot<double>(V, n, i, S.hsave.p, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(update_and_norm<double>(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+            prof_end(otok, s);
+            XT_TRY(fetch(hbuf.data(), S.hsave.p, 2 * i + 1));
+            for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
+            t = std::sqrt(hbuf[2 * i]);
+            if (!std::isfinite(t)) {
+                set_error("gmres: non-finite Krylov vector");
+                return XT_ERR_NONFINITE;
+            }
+            HH(i1 - 1, i - 1) = t;
+            if (t != 0.0) XT_TRY((axpby<double, double>(n, 1.0 / t, col(i1 - 1), 0.0, col(i1 - 1), s)));
+            for (int k = 2; k <= i; ++k) {
+                const int k1 = k - 1;
+                t = HH(k1 - 1, i - 1);
+                HH(k1 - 1, i - 1) = c[k1 - 1] * t + sn[k1 - 1] * HH(k - 1, i - 1);
+                HH(k - 1, i - 1) = -sn[k1 - 1] * t + c[k1 - 1] * HH(k - 1, i - 1);
+            }
+            double gam = std::sqrt(HH(i - 1, i - 1) * HH(i - 1, i - 1) +
+                                   HH(i1 - 1, i - 1) * HH(i1 - 1, i - 1));
+            if (gam == 0.0) gam = epsmac;
+            c[i - 1] = HH(i - 1, i - 1) / gam;
+            sn[i - 1] = HH(i1 - 1, i - 1) / gam;
+            rs[i1 - 1] = -sn[i - 1] * rs[i - 1];
+            rs[i - 1] = c[i - 1] * rs[i - 1];
+            HH(i - 1, i - 1) = c[i - 1] * HH(i - 1, i - 1) + sn[i - 1] * HH(i1 - 1, i - 1);
+            ro = std::fabs(rs[i1 - 1]);
+            if (i < im && ro > eps1 && its < maxits) continue;
+            break;
+        }
+        std::vector<double> y(rs.begin(), rs.begin() + i);
+        y[i - 1] = y[i - 1] / HH(i - 1, i - 1);
+        for (int ii = 2; ii <= i; ++ii) {
+            const int k = i - ii + 1;
+            t = y[k - 1];
+            for (int j = k + 1; j <= i; ++j) t -= HH(k - 1, j - 1) * y[j - 1];
+            y[k - 1] = t / HH(k - 1, k - 1);
+        }
+        XT_CUDA(cudaMemcpyAsync(S.hsave.p, y.data(), i * sizeof(double), cudaMemcpyHostToDevice, s));
+        XT_TRY((lincomb<float, double>(Z, n, i, S.hsave.p, S.u64.p, n, s)));
+        XT_TRY((axpby<double, double>(n, 1.0, S.u64.p, 1.0, sol, s)));
+        XT_CUDA(cudaStreamSynchronize(s));
+        if (ro <= eps1) { ierr = 0; break; }
+        if (its >= maxits) { ierr = 1; break; }
+    }
+    st.its += its;
+    st.ierr = ierr;
+    st.est = ro0 > 0 ? ro / ro0 : 0.0;
+    return XT_OK;
+}
+
 }  // namespace
 
 int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int maxits,
@@ -378,7 +503,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
     }
     cudaStream_t s = ctx().stream;
     const size_t n = (size_t)S.p * S.q;
-    XT_TRY(ensure_workspace(S, im, inner == 1));
+    XT_TRY(ensure_workspace(S, im, inner == 1, inner == 2));
     double hb[2];
     XT_TRY(norm2<double>(b, n, S.red, s));
     XT_TRY(fetch(hb, S.red.out.p, 1));
@@ -414,6 +539,10 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
             XT_CUDA(cudaMemsetAsync(S.d32.p, 0, n * sizeof(float), s));
             XT_TRY(gmres_core<float>(S, S.r32.p, S.d32.p, im, want, left, in, nullptr));
             XT_TRY((axpby<float, double>(n, rn, S.d32.p, 1.0, x, s)));
+        } else if (inner == 2) {
+            XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
+            XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
+            XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
         } else {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
             XT_TRY(gmres_core<double>(S, S.r64.p, S.t64.p, im, want, left, in, nullptr));

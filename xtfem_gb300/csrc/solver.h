@@ -31,6 +31,7 @@ struct System {
     int im_cap = 0;
     DBuf<double> V64, z64, w64, u64;
     DBuf<float> V32, z32, w32, u32, d32, r32;
+    DBuf<float> Z32;  // flexible GMRES: preconditioned basis, im columns
     DBuf<double> x64, r64, b64, t64;
     DBuf<double> hsave;
     Reduce red;
@@ -61,9 +62,12 @@ int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int ma
                GmresStats& st, std::vector<double>* hist);
 
 // Solve to a true relative residual <= tol: FP64 residuals and solution,
-// inner GMRES in precision `inner` (0 = FP64 operator/basis, 1 = FP32
-// operator, factor and basis with FP64 dots and Hessenberg), restarted with
-// the true residual until converged or maxits Arnoldi steps in total.
+// inner GMRES in precision `inner`, restarted with the true residual until
+// converged or maxits Arnoldi steps in total:
+//   0 = FP64 operator, factor and basis;
+//   1 = FP32 operator, factor and basis (FP64-class dots, host Hessenberg);
+//   2 = flexible GMRES: FP64 operator and basis, FP32 factor, the
+//       preconditioned vectors kept (FP32) for the solution update.
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
                   int inner, double inner_tol, GmresStats& st);
 
