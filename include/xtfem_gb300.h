@@ -121,6 +121,35 @@ int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
               double *sig_back, double *p, double *D, double *ws,
               double *del_po, double *sig_d);
 
+/* Allocation-free form of xt_damage.  No counterpart in the reference: it
+ * serves callers that keep the damage state resident on the GPU and must
+ * not allocate inside their time loop (a slab loop captured into a CUDA
+ * graph, where cudaMalloc cannot be recorded; a driver that budgets all
+ * device memory up front; a loop whose streams must not be serialised by
+ * the implicit synchronisation of cudaMalloc/cudaFree).
+ *   - Every array argument is a DEVICE pointer with the layouts of
+ *     xt_damage; nothing is copied to or from the host except counts.
+ *   - The kernel's scratch (FP32 copy of Nt, shape-value bounds, step
+ *     counters) is a static 1.5 MB array in the library's device image, so
+ *     nip must be <= 65536 (XT_ERR_ARG with a message otherwise; use
+ *     xt_damage for longer slabs).
+ *   - The step counters are cleared at the start of every call (they
+ *     accumulate with atomics); counts (host, may be NULL) receives the
+ *     plastic, screened-elastic and exact step totals.
+ *   - The first call looks up the scratch address (cudaGetSymbolAddress,
+ *     once per device, with that device current) and may set up the
+ *     library context: make that first call, or xt_init, before any
+ *     stream capture.
+ *   - One scratch per process and device: calls that overlap in time (two
+ *     host threads) race on it.  Returns after the update has finished. */
+int xt_damage_device(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
+                     int ncmp, int nip, const int *nodes, const double *Nx,
+                     const double *Ny, const double *Nz, const double *Nt,
+                     const double *sol, const double *ym, const double *nu,
+                     double *eps_old, double *eps_pl, double *sig_eff,
+                     double *sig_back, double *p, double *D, double *ws,
+                     double *del_po, double *sig_d, unsigned long long *counts);
+
 /* --------------------------------------------- handle-based interface */
 
 /* A device-resident space-time system: K and M (1-based CSR, order p), the

@@ -37,6 +37,7 @@ SIGNATURES = {
     "chkelesta_": (None, [_ip, _ip, _ip, _ip, _dp, _dp, _ip, _ip, _ip, _ip]),
     "kokkos_host_": (None, [C.c_int] * 9 + [_ip] + [_dp] * 16),
     "xt_damage": (C.c_int, [C.c_int] * 8 + [_ip] + [_dp] * 16),
+    "xt_damage_device": (C.c_int, [C.c_int] * 8 + [_vp] * 17 + [C.POINTER(C.c_ulonglong)]),
     "xt_system_create": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp, C.POINTER(_vp)]),
     "xt_system_destroy": (C.c_int, [_vp]),
     "xt_system_set_ilu": (C.c_int, [_vp, _dp, _ip, _ip, C.c_int]),

@@ -471,6 +471,58 @@ int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, int ncmp,
     return XT_OK;
 }
 
+int xt_damage_device(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, int ncmp, int nip,
+                     const int* nodes, const double* Nx, const double* Ny, const double* Nz,
+                     const double* Nt, const double* sol, const double* ym, const double* nu,
+                     double* eps_old, double* eps_pl, double* sig_eff, double* sig_back,
+                     double* p, double* D, double* ws, double* del_po, double* sig_d,
+                     unsigned long long* counts)
+{
+    // Host-side checks first: they need no device and allocate nothing.
+    if (ne <= 0 || nn <= 0 || ngpe <= 0 || nip < 0 || !nodes || !Nx || !Ny || !Nz || !Nt || !sol ||
+        !ym || !nu || !eps_old || !eps_pl || !sig_eff || !sig_back || !p || !D || !ws ||
+        !del_po || !sig_d) {
+        set_error("xt_damage_device: bad arguments");
+        return XT_ERR_ARG;
+    }
+    if (ndofn != 3 || nnte != 3 || ncmp != 6 || nnse < 1 || nnse > 8) {
+        set_error("xt_damage_device: the C3D8 update needs ndofn=3, nnte=3, ncmp=6, nnse<=8");
+        return XT_ERR_ARG;
+    }
+    if (nip > kDamageStaticMaxNip) {
+        set_error("xt_damage_device: nip = " + std::to_string(nip) +
+                  " exceeds the static scratch of this entry point (at most " +
+                  std::to_string(kDamageStaticMaxNip) + " steps per call); use xt_damage");
+        return XT_ERR_ARG;
+    }
+    if ((long long)ngpe * ne > 2147483647LL) {
+        set_error("xt_damage_device: more than 2^31-1 Gauss points");
+        return XT_ERR_ARG;
+    }
+    XT_TRY(ensure_init());
+    cudaStream_t s = ctx().stream;
+    float *nt32 = nullptr, *ntmax = nullptr;
+    unsigned long long* counters = nullptr;
+    XT_TRY(damage_static_scratch(&nt32, &ntmax, &counters));
+    // the step counters accumulate with atomics: they must start at zero
+    XT_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), s));
+    if (nip > 0) XT_TRY(to_f32(Nt, nt32, (size_t)2 * nnte * nip, s));
+    DamageArgs a{};
+    a.ngp = ngpe * ne; a.nn = nn; a.ndofn = ndofn; a.nnse = nnse; a.nnte = nnte; a.ncmp = ncmp;
+    a.nip = nip;
+    a.nodes = nodes; a.Nx = Nx; a.Ny = Ny; a.Nz = Nz; a.Nt = Nt; a.Nt32 = nt32;
+    a.sol = sol; a.ym = ym; a.nu = nu;
+    a.eps_old = eps_old; a.eps_pl = eps_pl; a.sig_eff = sig_eff; a.sig_back = sig_back;
+    a.p = p; a.D = D; a.ws = ws; a.del_po = del_po; a.sig_d = sig_d;
+    a.gpsta = nullptr; a.counters = counters; a.ntmax = ntmax;
+    XT_TRY(damage_update(a, s));
+    if (counts)
+        XT_CUDA(cudaMemcpyAsync(counts, counters, 3 * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
 void kokkos_host_(int rank, int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, int ncmp,
                   int nip, int* nodes, double* Nx, double* Ny, double* Nz, double* Nt,
                   double* sol, double* ym, double* nu, double* eps_old, double* eps_pl,

@@ -492,7 +492,40 @@ __global__ void k_any_ge(const double* __restrict__ D, int n, double Dc, int* fl
     if (__any_sync(0xffffffffu, f) && (threadIdx.x & 31) == 0) atomicOr(flag, 1);
 }
 
+// Scratch of the allocation-free damage entry point (xt_damage_device):
+// the FP32 copy of the temporal shape table (6 values per step, up to
+// kDamageStaticMaxNip steps), the six shape-value bounds and the three step
+// counters.  1.5 MB in all, part of the library image; one set per process
+// and device, so concurrent calls share it.
+constexpr size_t kStaticNt = (size_t)kDamageStaticMaxNip * 6;
+constexpr size_t kStaticBytes = kStaticNt * sizeof(float) + 64 + 3 * sizeof(unsigned long long);
+static __device__ __align__(256) unsigned char g_damage_scratch[kStaticBytes];
+
 }  // namespace
+
+int damage_static_scratch(float** nt32, float** ntmax, unsigned long long** counters)
+{
+    // The address is looked up once per device (cudaGetSymbolAddress can load
+    // the module, so the first call must not sit inside a stream capture).
+    constexpr int kMaxDevices = 64;
+    static void* addr[kMaxDevices] = {nullptr};
+    int dev = -1;
+    XT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error("damage scratch: device index out of range");
+        return XT_ERR_ARG;
+    }
+    if (!addr[dev]) {
+        void* p = nullptr;
+        XT_CUDA(cudaGetSymbolAddress(&p, g_damage_scratch));
+        addr[dev] = p;
+    }
+    unsigned char* b = static_cast<unsigned char*>(addr[dev]);
+    *nt32 = reinterpret_cast<float*>(b);
+    *ntmax = reinterpret_cast<float*>(b + kStaticNt * sizeof(float));
+    *counters = reinterpret_cast<unsigned long long*>(b + kStaticNt * sizeof(float) + 64);
+    return XT_OK;
+}
 
 int nt_table_device(int nip, double t0, double t1, double t2, double w, double* Nt64,
                     float* Nt32, cudaStream_t s)

@@ -217,6 +217,13 @@ struct DamageArgs {
 };
 int damage_update(const DamageArgs& a, cudaStream_t s);
 
+// Static device scratch of the allocation-free damage entry point: FP32
+// shape table (6 * kDamageStaticMaxNip floats), 6 shape-value bounds and 3
+// step counters.  Address looked up once per device (the device must be
+// current).
+constexpr int kDamageStaticMaxNip = 65536;
+int damage_static_scratch(float** nt32, float** ntmax, unsigned long long** counters);
+
 // Temporal shape table on the device (FP64 and FP32 copies).
 int nt_table_device(int nip, double t0, double t1, double t2, double w, double* Nt64,
                     float* Nt32, cudaStream_t s);
