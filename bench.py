@@ -142,6 +142,13 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6):
     return {0: kron64, 1: kron32, 2: ilu64, 3: ilu32, 4: damage, 5: None, 6: None}
 
 
+# DRAM bytes per launch of the kernel classes, from one ncu capture each on
+# this workload (profiles/): dram__bytes_read.sum + dram__bytes_write.sum.
+# ilu_apply_fp32 = its forward and backward sweep kernels (the 6 us
+# right-hand-side pre-pass is not included).
+NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 20_210_176 + 20_057_856,
+               4: 98_174_464 + 33_518_848}
+
 CLASS_NAMES = {0: "kron_spmm_fp64", 1: "kron_spmm_fp32", 2: "ilu_apply_fp64",
                3: "ilu_apply_fp32", 4: "damage_update", 5: "cgs2_step_fp64", 6: "cgs2_step_fp32"}
 
@@ -211,7 +218,7 @@ def run_gpu(args, rank, world):
         "host_ms_per_step": round(t_host / args.steps, 3),
         "roofline": {"bound": "hbm", "kernel": CLASS_NAMES[dom], "achieved": round(achieved, 1),
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s",
-                     "frac": round(achieved / hbm, 4), "traffic": None},
+                     "frac": round(achieved / hbm, 4), "traffic": NCU_TRAFFIC.get(dom)},
         "kernels": kernels,
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
