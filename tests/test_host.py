@@ -1,0 +1,219 @@
+"""CPU tests: the oracle checked against mathematical identities and the
+reference's shipped meshes (golden fixtures), and the product's host-side
+routines (rod generator, assembly, ILUT, temporal coefficients) checked
+against the oracle.  No GPU is needed.
+
+The reference carries no test vectors for the solve path, so the oracle is
+pinned by identities instead: the Kronecker apply equals the explicit
+Kronecker product, ILUT without dropping is an exact LU, lusol inverts the
+factor, GMRES reaches the direct solution, and the rod generator reproduces
+the shipped inp/prismaticrod-*.inp files exactly.
+"""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as spla
+
+from conftest import clamp_mask, rod_problem, temporal
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+@pytest.fixture(scope="module")
+def c1(xt):
+    pr = rod_problem(xt)
+    xyz, conn = pr.mesh()
+    K0, M0 = pr.K(), pr.M()
+    bc = clamp_mask(xyz)
+    pr.apply_bc(bc)
+    K, M = pr.K(), pr.M()
+    A, B, C1, M1 = temporal(xt)
+    yield dict(pr=pr, xyz=xyz, conn=conn, K0=K0, M0=M0, K=K, M=M, bc=bc, A=A, B=B)
+    pr.close()
+
+
+def block_kron(a, b, K, M):
+    """The space-time operator in the reference's block-major layout."""
+    return (sp.kron(sp.csr_matrix(a), K.to_scipy()) + sp.kron(sp.csr_matrix(b), M.to_scipy())).tocsr()
+
+
+# ------------------------------------------------------------- golden meshes
+def test_rod_generator_reproduces_shipped_meshes(xt):
+    meta = json.loads((GOLDEN / "rod_meshes.json").read_text())
+    for name, m in meta.items():
+        nx, ny, nz, lx, ly, lz = m["generator"]
+        pr = xt.Problem.rod(nx, ny, nz, lx, ly, lz)
+        xyz, conn = pr.mesh()
+        pr.close()
+        assert (len(xyz), len(conn)) == (m["nn"], m["ne"]), name
+        assert hashlib.sha256(xyz.astype("<f8").tobytes()).hexdigest() == m["xyz_sha256"], name
+        assert hashlib.sha256(conn.astype("<i4").tobytes()).hexdigest() == m["conn_sha256"], name
+
+
+def test_c1_mesh_arrays_match_fixture(c1):
+    g = np.load(GOLDEN / "rod_c1_mesh.npz")
+    assert np.array_equal(c1["xyz"], g["xyz"])
+    assert np.array_equal(c1["conn"], g["conn"])
+
+
+# ------------------------------------------------------------- assembly
+def test_stiffness_symmetric_with_rigid_body_kernel(c1):
+    K = c1["K0"].to_scipy()
+    assert abs(K - K.T).max() <= 1e-9 * abs(K).max()
+    nn = len(c1["xyz"])
+    for d in range(3):  # rigid translations produce no force
+        u = np.zeros(3 * nn)
+        u[d::3] = 1.0
+        assert np.abs(K @ u).max() <= 1e-8 * abs(K).max()
+
+
+def test_mass_matrix_total_mass(c1):
+    M = c1["M0"].to_scipy()
+    nn = len(c1["xyz"])
+    u = np.zeros(3 * nn)
+    u[0::3] = 1.0
+    # consistent mass: u^T M u = rho * volume for a unit translation
+    assert u @ (M @ u) == pytest.approx(7.8e-9 * 3.0 * 1.0 * 1.0, rel=1e-12)
+
+
+# ------------------------------------------------------------- Kronecker apply
+def test_oracle_kronspmv_equals_explicit_kronecker(orc, c1):
+    x = np.random.default_rng(1).standard_normal(c1["K"].n * 6)
+    y = orc.kronspmv(c1["A"], c1["B"], c1["K"], c1["M"], x)
+    y_ref = block_kron(c1["A"], c1["B"], c1["K"], c1["M"]) @ x
+    assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+
+
+def test_oracle_kronspgemv_alpha_beta(orc, c1):
+    rng = np.random.default_rng(2)
+    x, y0 = rng.standard_normal((2, c1["K"].n * 6))
+    y = orc.kronspgemv(c1["A"], c1["B"], -0.5, 2.0, c1["K"], c1["M"], x, y0)
+    y_ref = -0.5 * (block_kron(c1["A"], c1["B"], c1["K"], c1["M"]) @ x) + 2.0 * y0
+    assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+
+
+# ------------------------------------------------------------- ILUT / lusol
+def msr_to_lu(alu, jlu, ju, n):
+    """L (unit lower) and U from SPARSKIT MSR (inverted diagonal in alu)."""
+    L, U = sp.lil_matrix((n, n)), sp.lil_matrix((n, n))
+    for i in range(n):
+        L[i, i] = 1.0
+        U[i, i] = 1.0 / alu[i]
+        for k in range(jlu[i] - 1, ju[i] - 1):
+            L[i, jlu[k] - 1] = alu[k]
+        for k in range(ju[i] - 1, jlu[i + 1] - 1):
+            U[i, jlu[k] - 1] = alu[k]
+    return L.tocsr(), U.tocsr()
+
+
+def test_oracle_ilut_without_dropping_is_exact_lu(orc, xt):
+    pr = rod_problem(xt, 4, 2, 2)
+    xyz, _ = pr.mesh()
+    pr.apply_bc(clamp_mask(xyz))
+    K = pr.K()
+    pr.close()
+    n = K.n
+    (alu, jlu, ju), ierr = orc.ilut(K, lfil=n, droptol=0.0)
+    assert ierr == 0
+    L, U = msr_to_lu(alu, jlu, ju, n)
+    A = K.to_scipy()
+    assert abs(L @ U - A).max() <= 1e-10 * abs(A).max()
+
+
+def test_oracle_lusol_inverts_its_factor(orc, c1):
+    (alu, jlu, ju), ierr = orc.ilut(c1["K"], 20, 1e-4)
+    assert ierr == 0
+    n = c1["K"].n
+    L, U = msr_to_lu(alu, jlu, ju, n)
+    x = np.random.default_rng(3).standard_normal(n)
+    y = orc.lusol(alu, jlu, ju, L @ (U @ x))
+    assert np.abs(y - x).max() <= 1e-9 * np.abs(x).max()
+
+
+def test_product_ilut_identical_to_oracle(xt, orc, c1):
+    alu, jlu, ju = xt.ilut(c1["K"], 20, 1e-4)
+    (oalu, ojlu, oju), ierr = orc.ilut(c1["K"], 20, 1e-4)
+    assert ierr == 0
+    assert np.array_equal(jlu, ojlu) and np.array_equal(ju, oju)
+    assert np.array_equal(alu, oalu)
+
+
+def test_qsplit_partial_order(orc):
+    rng = np.random.default_rng(4)
+    a = rng.standard_normal(50)
+    ind = np.arange(50, dtype=np.int32)
+    b, bi = orc.qsplit(a, ind, 10)
+    top = np.sort(np.abs(a))[::-1][:10]
+    assert np.allclose(np.sort(np.abs(b[:10]))[::-1], top)  # the 10 largest come first
+    assert np.array_equal(np.sort(bi), ind) and np.allclose(b, a[bi])
+
+
+# ------------------------------------------------------------- GMRES
+def test_oracle_gmres_reaches_direct_solution(orc, c1):
+    (alu, jlu, ju), _ = orc.ilut(c1["K"], 20, 1e-4)
+    rhs = np.random.default_rng(5).standard_normal(c1["K"].n * 6)
+    sol, ierr, its, _ = orc.kronpgmres(c1["A"], c1["B"], c1["K"], c1["M"], alu, jlu, ju, rhs,
+                                       im=30, eps=1e-12, maxits=3000)
+    assert ierr == 0
+    x_ref = spla.spsolve(block_kron(c1["A"], c1["B"], c1["K"], c1["M"]).tocsc(), rhs)
+    assert np.linalg.norm(sol - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
+
+
+# ------------------------------------------------------------- temporal basis
+def test_stcoeff_closed_forms_match_quadrature(xt, orc):
+    """The closed forms keep the reference's default-real (single-precision)
+    fraction literals of src/stcoeff.f90 (2./3. is 0.666666687...), so they
+    agree with the exact quadrature to single-precision rounding."""
+    for t1, dt in [(0.0, 0.5), (2.5, 0.5), (0.0, 0.01)]:
+        w = 2 * np.pi * 20
+        got = xt.stcoeff_m(t1, dt, w)
+        ref = orc.stcoeff_m_quad(t1, dt, w)
+        for g, r in zip(got, ref):
+            assert np.abs(g - r).max() <= 1e-7 * max(np.abs(r).max(), 1e-30)
+        f, _ = xt.getfextc_m(t1, w, dt)
+        fr = orc.getfextc_m_quad(t1, w, dt)
+        assert np.abs(f - fr).max() <= 1e-9 * np.abs(fr).max()
+
+
+# ------------------------------------------------------------- damage / deletion
+def test_oracle_damage_elastic_step_is_hookes_law(xt, orc, c1):
+    """Displacements far below yield: no plastic strain, no damage, and the
+    effective stress is the elastic law applied to the final strain."""
+    pr, conn = c1["pr"], c1["conn"]
+    nn, ne = len(c1["xyz"]), len(conn)
+    Nx, Ny, Nz = pr.strain_rows()
+    nodes = np.repeat(conn, 8, axis=0).ravel().astype(np.int32)
+    nip = 64
+    Nt = xt.nt_table(nip, np.array([0.0, 0.25, 0.5]), 2 * np.pi * 20)
+    sol = np.random.default_rng(6).standard_normal(6 * 3 * nn) * 1e-7
+    ngp = 8 * ne
+    st = {k: np.zeros(ngp * 6) for k in ["eps_old", "eps_pl", "sig_eff", "sig_back"]}
+    st.update({k: np.zeros(ngp) for k in ["p", "D", "ws", "del_po", "sig_d"]})
+    orc.damage(ne, nn, nip, nodes, Nx, Ny, Nz, Nt, sol, np.full(ngp, 2e5), np.full(ngp, 0.3), st)
+    assert np.all(st["D"] == 0) and np.all(st["p"] == 0) and np.all(st["eps_pl"] == 0)
+    E, nu = 2e5, 0.3
+    c = E / ((1 + nu) * (1 - 2 * nu))
+    Dm = np.zeros((6, 6))
+    Dm[:3, :3] = c * nu
+    np.fill_diagonal(Dm[:3, :3], c * (1 - nu))
+    Dm[3:, 3:] = np.eye(3) * c * (1 - 2 * nu) / 2
+    eps = st["eps_old"].reshape(ngp, 6)
+    sig = st["sig_eff"].reshape(ngp, 6)
+    assert np.abs(sig - eps @ Dm.T).max() <= 1e-9 * np.abs(sig).max()
+
+
+def test_oracle_chkelesta_lists_failed_elements_ascending(orc):
+    ne, ngpe = 10, 8
+    D = np.zeros(ne * ngpe)
+    D[3 * 8 + 5] = 0.995
+    D[7 * 8 + 0] = 0.99
+    D[1 * 8 + 2] = 0.98
+    elesta, gpsta = np.ones(ne, np.int32), np.ones(ne * ngpe, np.int32)
+    nef, failed = orc.chkelesta(ne, ngpe, 0.99, D, elesta, gpsta)
+    assert nef == 2 and list(failed) == [4, 8]  # 1-based element ids
+    assert elesta[3] == 0 and elesta[7] == 0 and elesta.sum() == ne - 2
+    assert gpsta[24:32].sum() == 0 and gpsta[56:64].sum() == 0 and gpsta.sum() == ne * ngpe - 16

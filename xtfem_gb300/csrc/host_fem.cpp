@@ -173,13 +173,20 @@ Mesh make_rod(int nx, int ny, int nz, double lx, double ly, double lz)
     m.ne = nx * ny * nz;
     m.xyz.resize((size_t)m.nn * 3);
     auto node = [&](int ix, int iy, int iz) { return ix * py * pz + iz * py + iy + 1; };
+    // The shipped meshes hold single-precision coordinates printed with nine
+    // significant digits and read back in double precision: reproduce that.
+    auto coord = [](double v) {
+        char buf[32];
+        std::snprintf(buf, sizeof buf, "%.9g", (double)(float)v);
+        return std::strtod(buf, nullptr);
+    };
     for (int ix = 0; ix < px; ++ix)
         for (int iz = 0; iz < pz; ++iz)
             for (int iy = 0; iy < py; ++iy) {
                 const int id = node(ix, iy, iz) - 1;
-                m.xyz[(size_t)id * 3 + 0] = (double)(float)(lx - lx * ix / nx);
-                m.xyz[(size_t)id * 3 + 1] = (double)(float)(ly - ly * iy / ny);
-                m.xyz[(size_t)id * 3 + 2] = (double)(float)(lz - lz * iz / nz);
+                m.xyz[(size_t)id * 3 + 0] = coord(lx - lx * ix / nx);
+                m.xyz[(size_t)id * 3 + 1] = coord(ly - ly * iy / ny);
+                m.xyz[(size_t)id * 3 + 2] = coord(lz - lz * iz / nz);
             }
     m.conn.resize((size_t)m.ne * 8);
     for (int ix = 0; ix < nx; ++ix)
