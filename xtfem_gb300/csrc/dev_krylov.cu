@@ -122,6 +122,181 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Double-float vectors: one float2 (hi, lo) per entry, value hi + lo with
+// |lo| <= ulp(hi)/2 (about 48 significant bits).  The flexible GMRES keeps
+// its FP64-accurate Krylov basis in this form: the same bytes as FP64, but
+// every operation runs on the FP32 pipe.
+
+// (hi, lo) += (ah + al)(bh + bl): the leading product exactly (fma), the
+// cross terms in FP32 (their rounding is below the format's precision).
+__device__ __forceinline__ void df_mul_acc(float& hi, float& lo, float ah, float al, float bh,
+                                           float bl)
+{
+    const float p = __fmul_rn(ah, bh);
+    const float e = fmaf(ah, bh, -p);
+    df_add(hi, lo, p);
+    lo = __fadd_rn(lo, __fadd_rn(e, fmaf(ah, bl, __fmul_rn(al, bh))));
+}
+
+// Renormalise (hi, lo) so that hi carries the rounded value.
+__device__ __forceinline__ float2 df_norm(float hi, float lo)
+{
+    const float s = __fadd_rn(hi, lo);
+    return make_float2(s, __fsub_rn(lo, __fsub_rn(s, hi)));
+}
+
+// partial[(j0+c) nb + b] = (hi, lo) of sum over block b's rows of V_j w
+__global__ void k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,
+                               const float4* __restrict__ w, size_t n2,
+                               double* __restrict__ partial)
+{
+    __shared__ float2 sh[kChunk][32];
+    const int j0 = blockIdx.y * kChunk;
+    const int nb = gridDim.x;
+    const size_t per = (n2 + nb - 1) / nb;
+    const size_t r0 = per * blockIdx.x, r1 = min(n2, r0 + per);
+    float hi[kChunk], lo[kChunk];
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) hi[c] = lo[c] = 0.0f;
+    for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const float4 wr = w[r];  // two entries: (hi, lo), (hi, lo)
+        float4 v[kChunk];
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c)
+            v[c] = (j0 + c < k) ? V[(size_t)(j0 + c) * ld2 + r] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int c = 0; c < kChunk; ++c) {
+            df_mul_acc(hi[c], lo[c], v[c].x, v[c].y, wr.x, wr.y);
+            df_mul_acc(hi[c], lo[c], v[c].z, v[c].w, wr.z, wr.w);
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int c = 0; c < kChunk; ++c) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, hi[c], off);
+            const float ol = __shfl_xor_sync(0xffffffffu, lo[c], off);
+            df_add_df(hi[c], lo[c], oh, ol);
+        }
+        if (lane == 0) sh[c][warp] = make_float2(hi[c], lo[c]);
+    }
+    __syncthreads();
+    if (threadIdx.x < kChunk && j0 + (int)threadIdx.x < k) {
+        const int c = threadIdx.x;
+        float h = 0.0f, l = 0.0f;
+        for (int wi = 0; wi < nw; ++wi) df_add_df(h, l, sh[c][wi].x, sh[c][wi].y);
+        reinterpret_cast<float2*>(partial)[(size_t)(j0 + c) * nb + blockIdx.x] = make_float2(h, l);
+    }
+}
+
+// (wh, wl) -= (hh + hl)(vh + vl)
+__device__ __forceinline__ void df_sub_mul(float& wh, float& wl, float hh, float hl, float vh,
+                                           float vl)
+{
+    const float p = __fmul_rn(hh, vh);
+    const float e = fmaf(hh, vh, -p);
+    df_add(wh, wl, -p);
+    wl = __fsub_rn(wl, __fadd_rn(e, fmaf(hh, vl, __fmul_rn(hl, vh))));
+}
+
+// w -= V h on double-float vectors (two entries per float4); optional
+// ||w||^2 as a (hi, lo) partial per block.
+template <bool NORM>
+__global__ void k_update_df(const float4* __restrict__ V, size_t ld2, int k,
+                            const double* __restrict__ h, float4* __restrict__ w, size_t n2,
+                            double* __restrict__ partial)
+{
+    __shared__ float2 hs[512];
+    __shared__ float2 sh[32];
+    for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) {
+        const float a = (float)h[j];
+        hs[j] = make_float2(a, (float)(h[j] - (double)a));
+    }
+    __syncthreads();
+    float nh = 0.0f, nl = 0.0f;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n2; r += stride) {
+        const float4 wv = w[r];
+        float ah = wv.x, al = wv.y, bh = wv.z, bl = wv.w;
+        for (int jb = 0; jb < k; jb += 8) {
+            float4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+                v[u] = (jb + u < k) ? V[(size_t)(jb + u) * ld2 + r] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int j = jb + u;
+                if (j >= k) break;
+                float2 hj;
+                if (j < 512) hj = hs[j];
+                else {
+                    const float a = (float)h[j];
+                    hj = make_float2(a, (float)(h[j] - (double)a));
+                }
+                df_sub_mul(ah, al, hj.x, hj.y, v[u].x, v[u].y);
+                df_sub_mul(bh, bl, hj.x, hj.y, v[u].z, v[u].w);
+            }
+        }
+        const float2 a2 = df_norm(ah, al), b2 = df_norm(bh, bl);
+        w[r] = make_float4(a2.x, a2.y, b2.x, b2.y);
+        if (NORM) {
+            df_mul_acc(nh, nl, a2.x, a2.y, a2.x, a2.y);
+            df_mul_acc(nh, nl, b2.x, b2.y, b2.x, b2.y);
+        }
+    }
+    if (NORM) {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, nh, off);
+            const float ol = __shfl_xor_sync(0xffffffffu, nl, off);
+            df_add_df(nh, nl, oh, ol);
+        }
+        if (lane == 0) sh[warp] = make_float2(nh, nl);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            float hh = 0.0f, ll = 0.0f;
+            for (int wi = 0; wi < nw; ++wi) df_add_df(hh, ll, sh[wi].x, sh[wi].y);
+            reinterpret_cast<float2*>(partial)[blockIdx.x] = make_float2(hh, ll);
+        }
+    }
+}
+
+// y = (hi, lo) split of x; y = hi part only; y = a * y (a FP64, split)
+__global__ void k_df_from_f64(const double* __restrict__ x, float2* __restrict__ y, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const double v = x[i];
+        const float h = __double2float_rn(v);
+        y[i] = make_float2(h, __double2float_rn(v - (double)h));
+    }
+}
+__global__ void k_df_hi(const float2* __restrict__ x, float* __restrict__ y, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        y[i] = x[i].x;
+}
+__global__ void k_df_to_f64(const float2* __restrict__ x, double* __restrict__ y, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        y[i] = (double)x[i].x + (double)x[i].y;
+}
+__global__ void k_df_scale(float2* __restrict__ y, float ah, float al, size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 v = y[i];
+        float h = 0.0f, l = 0.0f;
+        df_mul_acc(h, l, v.x, v.y, ah, al);
+        y[i] = df_norm(h, l);
+    }
+}
+
 // out[j] = sum_b (hi_b + lo_b) in FP64, one block per j, fixed order
 __global__ void k_finish_df(const double* __restrict__ partial, int nb, double* __restrict__ out)
 {
@@ -501,6 +676,82 @@ int max_value(const double* x, size_t n, Reduce& r, cudaStream_t s)
     k_max<<<r.nblocks, kThreads, 0, s>>>(x, n, r.partial.p);
     k_max_finish<<<1, 32, 0, s>>>(r.partial.p, r.nblocks, r.out.p);
     note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, Reduce& r,
+                 cudaStream_t s)
+{
+    if (k > r.kmax) { set_error("df_multi_dot: k exceeds reduction capacity"); return XT_ERR_ARG; }
+    if (k <= 0) return XT_OK;
+    if (n % 2 || ld % 2) { set_error("df_multi_dot: n and ld must be even"); return XT_ERR_ARG; }
+    dim3 grid(r.nblocks, (k + kChunk - 1) / kChunk);
+    k_multi_dot_df<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
+                                             reinterpret_cast<const float4*>(w), n / 2,
+                                             r.partial.p);
+    k_finish_df<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_update_and_dot(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
+                      Reduce& r, cudaStream_t s)
+{
+    if (k <= 0) return XT_OK;
+    if (n % 2 || ld % 2) { set_error("df_update: n and ld must be even"); return XT_ERR_ARG; }
+    k_update_df<false><<<grid_for(n / 2), kThreads, 0, s>>>(
+        reinterpret_cast<const float4*>(V), ld / 2, k, h, reinterpret_cast<float4*>(w), n / 2,
+        nullptr);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return df_multi_dot(V, ld, k, w, n, r, s);
+}
+
+int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
+                       Reduce& r, cudaStream_t s)
+{
+    if (n % 2 || ld % 2) { set_error("df_update: n and ld must be even"); return XT_ERR_ARG; }
+    const int nb = r.nblocks;
+    k_update_df<true><<<nb, 2 * kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
+                                                  h, reinterpret_cast<float4*>(w), n / 2,
+                                                  r.partial.p);
+    k_finish_df<<<1, kThreads, 0, s>>>(r.partial.p, nb, r.out.p);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_from_f64(const double* x, float2* y, size_t n, cudaStream_t s)
+{
+    k_df_from_f64<<<grid_for(n), kThreads, 0, s>>>(x, y, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_hi(const float2* x, float* y, size_t n, cudaStream_t s)
+{
+    k_df_hi<<<grid_for(n), kThreads, 0, s>>>(x, y, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_to_f64(const float2* x, double* y, size_t n, cudaStream_t s)
+{
+    k_df_to_f64<<<grid_for(n), kThreads, 0, s>>>(x, y, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_scale(float2* y, double a, size_t n, cudaStream_t s)
+{
+    const float ah = (float)a;
+    k_df_scale<<<grid_for(n), kThreads, 0, s>>>(y, ah, (float)(a - (double)ah), n);
+    note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
 }

@@ -368,16 +368,18 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
 
 // Flexible GMRES (right preconditioning with the preconditioned vectors
 // kept): the control flow of kronpgmres (src/kronecker.f90:181-365) with
-// an FP64 operator and FP64 basis V, and the ILU applied in FP32; z_j =
-// M^-1 v_j is stored (FP32) and the solution update is x += Z y, so the
-// Arnoldi relation A Z = V H holds to FP64 accuracy however the FP32
-// preconditioner rounds.  A restart rebuilds the residual explicitly.
+// an FP64 operator, the ILU applied in FP32, and the Krylov basis V held in
+// double-float (two FP32 numbers per entry: FP64's bytes, about 48
+// significant bits, FP32 arithmetic).  z_j = M^-1 v_j is stored in FP32 and
+// the update is x += Z y, so the Arnoldi relation A Z = V H holds to
+// double-float accuracy however the FP32 preconditioner rounds.  A restart
+// rebuilds the residual explicitly.
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
     cudaStream_t s = ctx().stream;
     const size_t n = (size_t)S.p * S.q;
-    double* V = S.V64.p;
+    float2* V = reinterpret_cast<float2*>(S.V64.p);  // double-float basis
     float* Z = S.Z32.p;
     auto col = [&](int j) { return V + (size_t)j * n; };
     auto zc = [&](int j) { return Z + (size_t)j * n; };
@@ -392,10 +394,10 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
     const double ro0 = std::sqrt(hbuf[0]);
     for (;;) {
-        // v1 = rhs - A sol
-        XT_CUDA(cudaMemcpyAsync(col(0), rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, col(0)));
-        XT_TRY(norm2<double>(col(0), n, S.red, s));
+        // v1 = (rhs - A sol) / ||rhs - A sol||, the residual formed in FP64
+        XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
+        XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
         XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
         ro = std::sqrt(hbuf[0]);
         if (!std::isfinite(ro)) {
@@ -403,7 +405,8 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             return XT_ERR_NONFINITE;
         }
         if (ro == 0.0) { ierr = -1; break; }
-        XT_TRY((axpby<double, double>(n, 1.0 / ro, col(0), 0.0, col(0), s)));
+        XT_TRY(df_from_f64(S.w64.p, col(0), n, s));
+        XT_TRY(df_scale(col(0), 1.0 / ro, n, s));
         if (its == 0) eps1 = eps * ro;
         rs.assign(im + 1, 0.0);
         rs[0] = ro;
@@ -413,18 +416,19 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             ++i;
             ++its;
             const int i1 = i + 1;
-            XT_TRY((axpby<double, float>(n, 1.0, col(i - 1), 0.0, S.d32.p, s)));
+            XT_TRY(df_hi(col(i - 1), S.d32.p, n, s));
             XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
             XT_TRY((axpby<float, double>(n, 1.0, zc(i - 1), 0.0, S.u64.p, s)));
-            XT_TRY(apply_op<double>(S, S.u64.p, col(i1 - 1)));
+            XT_TRY(apply_op<double>(S, S.u64.p, S.w64.p));
+            XT_TRY(df_from_f64(S.w64.p, col(i1 - 1), n, s));
             const int otok = prof_begin(PROF_ORTH64, s);
-            XT_TRY(multi_dot<double>(V, n, i, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_multi_dot(V, n, i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
-            XT_TRY(update_and_dot<double>(V, n, i, S.hsave.p, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_update_and_dot(V, n, i, S.hsave.p, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
-            XT_TRY(update_and_norm<double>(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_update_and_norm(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
             prof_end(otok, s);
@@ -436,7 +440,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
                 return XT_ERR_NONFINITE;
             }
             HH(i1 - 1, i - 1) = t;
-            if (t != 0.0) XT_TRY((axpby<double, double>(n, 1.0 / t, col(i1 - 1), 0.0, col(i1 - 1), s)));
+            if (t != 0.0) XT_TRY(df_scale(col(i1 - 1), 1.0 / t, n, s));
             for (int k = 2; k <= i; ++k) {
                 const int k1 = k - 1;
                 t = HH(k1 - 1, i - 1);

@@ -180,6 +180,19 @@ int lincomb(const TV* V, size_t ld, int k, const double* c, TY* y, size_t n,
 // y := a*x (+ y when accumulate); x, y may differ in type.
 template <class TX, class TY>
 int axpby(size_t n, double a, const TX* x, double b, TY* y, cudaStream_t s);
+// Double-float vectors (float2 (hi, lo) per entry, about 48 significant
+// bits, FP32 arithmetic only): the CGS2 passes of multi_dot /
+// update_and_dot / update_and_norm, conversions, and y *= a.  n, ld even.
+int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, Reduce& r,
+                 cudaStream_t s);
+int df_update_and_dot(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
+                      Reduce& r, cudaStream_t s);
+int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
+                       Reduce& r, cudaStream_t s);
+int df_from_f64(const double* x, float2* y, size_t n, cudaStream_t s);
+int df_hi(const float2* x, float* y, size_t n, cudaStream_t s);
+int df_to_f64(const float2* x, double* y, size_t n, cudaStream_t s);
+int df_scale(float2* y, double a, size_t n, cudaStream_t s);
 // ||x||^2 (FP64) into r.out[0].
 template <class T>
 int norm2(const T* x, size_t n, Reduce& r, cudaStream_t s);
