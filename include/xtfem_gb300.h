@@ -123,14 +123,15 @@ int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
 
 /* Allocation-free form of xt_damage.  No counterpart in the reference: it
  * serves callers that keep the damage state resident on the GPU and must
- * not allocate inside their time loop (a slab loop captured into a CUDA
- * graph, where cudaMalloc cannot be recorded; a driver that budgets all
- * device memory up front; a loop whose streams must not be serialised by
- * the implicit synchronisation of cudaMalloc/cudaFree).
+ * not allocate inside their time loop: a driver that hands all device
+ * memory to its own pool up front (a cudaMalloc there fails or steals from
+ * the pool), and a loop whose streams must keep running while it calls in
+ * (cudaMalloc and cudaFree can synchronise the device).
  *   - Every array argument is a DEVICE pointer with the layouts of
  *     xt_damage; nothing is copied to or from the host except counts.
  *   - The kernel's scratch (FP32 copy of Nt, shape-value bounds, step
- *     counters) is a static 1.5 MB array in the library's device image, so
+ *     counters) is a static 1.5 MB array in the library's device image,
+ *     held on every GPU that loads the library until the process exits, so
  *     nip must be <= 65536 (XT_ERR_ARG with a message otherwise; use
  *     xt_damage for longer slabs).
  *   - The step counters are cleared at the start of every call (they
@@ -140,8 +141,9 @@ int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
  *     once per device, with that device current) and may set up the
  *     library context: make that first call, or xt_init, before any
  *     stream capture.
- *   - One scratch per process and device: calls that overlap in time (two
- *     host threads) race on it.  Returns after the update has finished. */
+ *   - One scratch per process and device, keeping the last call's
+ *     contents: calls whose work overlaps on the GPU (two host threads)
+ *     race on it.  Returns after the update has finished. */
 int xt_damage_device(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
                      int ncmp, int nip, const int *nodes, const double *Nx,
                      const double *Ny, const double *Nz, const double *Nt,
