@@ -253,7 +253,10 @@ __device__ __noinline__ void slow_materialize(Slow* s, const double* __restrict_
 }
 
 // exact FP64 step jj.  Returns 1 when the step was plastic (internal
-// variables changed and the screen was rebuilt), else 0.
+// variables changed; the screen is marked stale with an infinite error
+// bound, so the following steps take this exact path too), else 0; an
+// elastic step on a stale screen rebuilds it.  A plastic phase therefore
+// rebuilds the screen once, at its end, not after every plastic step.
 __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, int jj, int last_el,
                                       const float* __restrict__ ntmax, Screen* sc)
 {
@@ -263,21 +266,30 @@ __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, in
     if (teq <= SIGF) {
         for (int i = 0; i < 6; ++i) { s->st.sef[i] = tse[i]; s->st.epo[i] = eps[i]; }
         s->st.sigd = teq;
+        if (isinf(sc->err2)) {
+            screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+            return 2;
+        }
         return 0;
     }
     if (last_el >= 0) slow_materialize(s, Nt, last_el);
     corrector(s->m, eps, s->st);
-    screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+    sc->err2 = __int_as_float(0x7f800000);  // +inf: screen stale
     return 1;
 }
 
 __global__ void __launch_bounds__(256)
 k_damage(DamageArgs a, const float* __restrict__ ntmax)
 {
-    // threads past the last point run a copy of it (they must reach the
-    // block barriers of the chunk loop) and store nothing
-    const bool live = (int)(blockIdx.x * blockDim.x + threadIdx.x) < a.ngp;
-    const int gp = live ? (int)(blockIdx.x * blockDim.x + threadIdx.x) : a.ngp - 1;
+    // Points are dealt to blocks round-robin (thread t of block b takes point
+    // t * gridDim + b): plastic points cluster in space, i.e. in consecutive
+    // point numbers, and their FP64 steps would otherwise pile up in a few
+    // blocks on a few SMs while the rest of the GPU idles.  Threads past the
+    // last point run a copy of it (they must reach the block barriers of the
+    // chunk loop) and store nothing.
+    const long long gidx = (long long)threadIdx.x * gridDim.x + blockIdx.x;
+    const bool live = gidx < a.ngp;
+    const int gp = live ? (int)gidx : a.ngp - 1;
     Slow s;
     Mat& m = s.m;
     m.nu = a.nu[gp];
@@ -362,8 +374,12 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
             continue;
         }
         ++n_exact;
-        if (slow_step(&s, a.Nt, jj, last_el, ntmax, &sc)) {
+        sc.err2 = err2;
+        const int r = slow_step(&s, a.Nt, jj, last_el, ntmax, &sc);
+        if (r == 1) {
             ++n_plastic;
+            err2 = sc.err2;  // stale: every step is exact until one is elastic
+        } else if (r == 2) {  // screen rebuilt after a plastic phase
 #pragma unroll
             for (int k = 0; k < 6; ++k)
 #pragma unroll
