@@ -95,6 +95,9 @@ typedef struct xt_slab_config {
     double Dc;           /* critical damage */
     int damage;          /* 1 = run the damage update */
     int group;           /* rows per node in the ILU level schedule */
+    int overlap;         /* 1 = run each slab's damage update on a second,
+                            lower-priority stream while the next slab is
+                            solved (see xt_slab_step) */
 } xt_slab_config;
 
 typedef struct xt_slab_s *xt_slab;
@@ -104,14 +107,30 @@ int xt_slab_destroy(xt_slab s);
 /* One slab.  stats (may be NULL) receives 12 values: slab index, GMRES
  * iterations, restart cycles, refinement passes, ierr, true relative
  * residual, max D, failed elements so far, elements deleted this slab,
- * plastic steps, screened elastic steps, exact steps. */
+ * plastic steps, screened elastic steps, exact steps.
+ * With cfg.overlap = 1 the slab's damage update is left running on a second
+ * stream when the call returns, and the next call solves its slab while it
+ * runs: the slab's operator changes only when the damage update deletes
+ * elements, so the next solve is started at once and, if the update did
+ * delete elements, discarded and repeated on the new operator.  The results
+ * are those of the sequential loop; the damage entries of stats (max D and
+ * the step counts) then describe the previous slab, and xt_slab_drain
+ * returns those of the last one. */
 int xt_slab_step(xt_slab s, double *stats);
 /* The same slab through host buffers: fext (block layout, p*6) replaces the
  * slab's external load vector, and the slab's displacement (block layout,
- * p*6) and damage (8 per element) are copied back. */
+ * p*6) and damage (8 per element) are copied back.  With cfg.overlap = 1,
+ * D is the damage after the previous slab (the current update is still
+ * running). */
 int xt_slab_step_host(xt_slab s, const double *fext, double *disp, double *D,
                       double *stats);
-/* Copies of the current state. */
+/* Waits for a damage update still running (cfg.overlap = 1) and writes its
+ * max D and step counts to stats[6], stats[9..11] (stats may be NULL). */
+int xt_slab_drain(xt_slab s, double *stats);
+/* Replaces the damage D and stored energy ws of every Gauss point (host
+ * arrays of 8 per element; either may be NULL), e.g. to resume a run. */
+int xt_slab_set_state(xt_slab s, const double *D, const double *ws);
+/* Copies of the current state (waits for a running damage update). */
 int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
 /* Per-kernel CUDA-event timing on the library stream: enable, then read
  * count and total milliseconds per kernel class (0 Kronecker FP64,

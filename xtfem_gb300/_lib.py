@@ -71,6 +71,8 @@ SIGNATURES = {
     "xt_slab_destroy": (C.c_int, [_vp]),
     "xt_slab_step": (C.c_int, [_vp, _dp]),
     "xt_slab_step_host": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
+    "xt_slab_drain": (C.c_int, [_vp, _dp]),
+    "xt_slab_set_state": (C.c_int, [_vp, _dp, _dp]),
     "xt_slab_get": (C.c_int, [_vp, _dp, _dp, _dp, _ip]),
     "xt_profile": (C.c_int, [C.c_int]),
     "xt_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_longlong), _dp]),

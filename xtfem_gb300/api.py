@@ -363,14 +363,14 @@ class SlabConfig(C.Structure):
                 ("n2", C.c_int), ("nipc", C.c_int), ("lfil", C.c_int), ("droptol", C.c_double),
                 ("im", C.c_int), ("tol", C.c_double), ("maxits", C.c_int),
                 ("precision", C.c_int), ("inner_tol", C.c_double), ("Dc", C.c_double),
-                ("damage", C.c_int), ("group", C.c_int)]
+                ("damage", C.c_int), ("group", C.c_int), ("overlap", C.c_int)]
 
     @classmethod
     def make(cls, **kw):
         d = dict(clamp_axis=0, clamp_value=0.0, load_axis=0, load_value=3.0, load_comp=0,
                  amplitude=100.0, area=1.0, freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256,
                  lfil=20, droptol=1e-4, im=30, tol=1e-8, maxits=3000, precision=0,
-                 inner_tol=1e-5, Dc=0.99, damage=1, group=3)
+                 inner_tol=1e-5, Dc=0.99, damage=1, group=3, overlap=0)
         d.update(kw)
         return cls(**d)
 
@@ -410,6 +410,20 @@ class SlabSolver:
         check(lib().xt_slab_step_host(self._h, dptr(fext), dptr(disp_out), dptr(D_out), dptr(st)),
               "xt_slab_step_host")
         return dict(zip(STAT_KEYS, st.tolist()))
+
+    def drain(self):
+        """Wait for a damage update still running (overlap mode); returns its
+        max D and step counts."""
+        st = np.zeros(12)
+        check(lib().xt_slab_drain(self._h, dptr(st)), "xt_slab_drain")
+        return dict(zip(STAT_KEYS, st.tolist()))
+
+    def set_state(self, D=None, ws=None):
+        """Replace the damage and stored energy of every Gauss point."""
+        a = None if D is None else _f64(D)
+        b = None if ws is None else _f64(ws)
+        check(lib().xt_slab_set_state(self._h, dptr(a) if a is not None else None,
+                                      dptr(b) if b is not None else None), "xt_slab_set_state")
 
     def state(self):
         disp, D, ws = np.zeros(self.p * 6), np.zeros(self.ngp), np.zeros(self.ngp)

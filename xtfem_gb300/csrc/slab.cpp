@@ -45,6 +45,26 @@ struct xt_slab_s {
     double dt = 0, w = 0;
     int nip = 0, slab = 0, nfailed = 0;
     bool switched = false;
+    // overlap mode: the damage update of the last slab runs on `ds`
+    cudaStream_t ds = nullptr;
+    cudaEvent_t ev_sol = nullptr, ev_dmg = nullptr;
+    bool pending = false;
+    DBuf<double> disp_prev, hblk;  // speculation restore point; host-output staging
+    Reduce red_dmg;
+    double* hbuf = nullptr;  // pinned: max D, 3 counters, deletion flag
+    // results of the last finished update, kept until the next slab uses them
+    int del_flag = 0;
+    double dmg_stats[4] = {0, 0, 0, 0};
+    ~xt_slab_s()
+    {
+        if (ds) {
+            cudaStreamSynchronize(ds);
+            cudaStreamDestroy(ds);
+        }
+        if (ev_sol) cudaEventDestroy(ev_sol);
+        if (ev_dmg) cudaEventDestroy(ev_dmg);
+        if (hbuf) cudaFreeHost(hbuf);
+    }
 };
 
 namespace {
@@ -103,8 +123,9 @@ int deletion_check(xt_slab_s& s, int& deleted)
 }
 
 // Steps 1-4 of a slab; the load blocks come from fext_host (block layout)
-// when given, else from fextc(j) * rext.
-int solve_slab(xt_slab_s& s, const double* fext_host, double* stats)
+// when given, else from fextc(j) * rext.  check = false skips the deletion
+// check (the overlapped loop makes it after a speculative solve).
+int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check = true)
 {
     cudaStream_t st = ctx().stream;
     const size_t n = (size_t)s.p * s.q;
@@ -112,7 +133,7 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats)
     const double t3 = s.tc[2];
     for (int j = 0; j < 3; ++j) s.tc[j] = t3 + j * s.dt / 2.0;
     int deleted = 0;
-    if (s.cfg.damage && s.slab > 1) XT_TRY(deletion_check(s, deleted));
+    if (check && s.cfg.damage && s.slab > 1) XT_TRY(deletion_check(s, deleted));
     // temporal matrices of this slab
     double ck[36], cm[36], ckt[36], cmt[36], ck1[36], cm1[36], A[36], B[36];
     stcoeff_m(s.tc[0], s.dt, s.w, ck, cm, ckt, cmt, ck1, cm1);
@@ -124,10 +145,10 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats)
     XT_CUDA(cudaMemcpyAsync(s.S.Cj.p, ck1, sizeof(ck1), cudaMemcpyHostToDevice, st));
     XT_CUDA(cudaMemcpyAsync(s.S.Mj.p, cm1, sizeof(cm1), cudaMemcpyHostToDevice, st));
     // load blocks and jump term
-    if (fext_host) {
-        XT_TRY(s.dblk.alloc(n));
-        XT_CUDA(cudaMemcpyAsync(s.dblk.p, fext_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
-        XT_TRY((to_interleaved<double, double>(s.dblk.p, s.fext.p, s.p, s.q, st)));
+    if (fext_host) {  // staged in hblk: dblk may still feed a running damage update
+        XT_TRY(s.hblk.alloc(n));
+        XT_CUDA(cudaMemcpyAsync(s.hblk.p, fext_host, n * sizeof(double), cudaMemcpyHostToDevice, st));
+        XT_TRY((to_interleaved<double, double>(s.hblk.p, s.fext.p, s.p, s.q, st)));
     } else {
         double fextc[6], fint[6];
         getfextc_m(s.tc[0], s.w, s.dt, fextc, fint);
@@ -196,6 +217,118 @@ int damage_slab(xt_slab_s& s, double* stats)
     } else {
         XT_CUDA(cudaStreamSynchronize(st));
     }
+    return XT_OK;
+}
+
+// ------------------------------------------------ overlapped damage update
+// The damage update of slab k reads only slab k's displacement and the
+// damage state; slab k+1's solve reads neither unless the update deletes
+// elements.  So the update runs on a second, lower-priority stream behind
+// an event on the displacement, the next slab is solved meanwhile, and the
+// deletion flag the update leaves decides afterwards whether that solve
+// stands (the usual case) or is repeated on the new operator.
+
+int overlap_init(xt_slab_s& s)
+{
+    if (s.ds) return XT_OK;
+    int least = 0, greatest = 0;
+    XT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    XT_CUDA(cudaStreamCreateWithPriority(&s.ds, cudaStreamNonBlocking, least));
+    XT_CUDA(cudaEventCreateWithFlags(&s.ev_sol, cudaEventDisableTiming));
+    XT_CUDA(cudaEventCreateWithFlags(&s.ev_dmg, cudaEventDisableTiming));
+    XT_CUDA(cudaMallocHost(&s.hbuf, 8 * sizeof(double)));
+    XT_TRY(reduce_init(s.red_dmg, 1));
+    XT_TRY(s.disp_prev.alloc((size_t)s.p * s.q));
+    return XT_OK;
+}
+
+// Launch the damage update of the slab just solved on s.ds.
+int damage_launch(xt_slab_s& s)
+{
+    cudaStream_t st = ctx().stream;
+    const size_t n = (size_t)s.p * s.q;
+    XT_TRY(s.dblk.alloc(n));
+    XT_TRY((to_blocks<double, double>(s.disp.p, s.dblk.p, s.p, s.q, st)));
+    XT_CUDA(cudaEventRecord(s.ev_sol, st));
+    cudaStream_t ds = s.ds;
+    XT_CUDA(cudaStreamWaitEvent(ds, s.ev_sol, 0));
+    XT_TRY(s.Nt64.alloc((size_t)s.nip * 6));
+    XT_TRY(s.Nt32.alloc((size_t)s.nip * 6));
+    XT_TRY(nt_table_device(s.nip, s.tc[0], s.tc[1], s.tc[2], s.w, s.Nt64.p, s.Nt32.p, ds));
+    XT_CUDA(cudaMemsetAsync(s.counters.p, 0, 3 * sizeof(unsigned long long), ds));
+    DamageArgs a{};
+    a.ngp = s.ngp; a.nn = s.nn; a.ndofn = 3; a.nnse = 8; a.nnte = 3; a.ncmp = 6; a.nip = s.nip;
+    a.nodes = s.nodes.p; a.Nx = s.Nx.p; a.Ny = s.Ny.p; a.Nz = s.Nz.p;
+    a.Nt = s.Nt64.p; a.Nt32 = s.Nt32.p; a.sol = s.dblk.p; a.ym = s.ym.p; a.nu = s.nu.p;
+    a.eps_old = s.eo.p; a.eps_pl = s.ep.p; a.sig_eff = s.se.p; a.sig_back = s.sb.p;
+    a.p = s.pp.p; a.D = s.D.p; a.ws = s.ws.p; a.del_po = s.dpo.p; a.sig_d = s.sd.p;
+    a.gpsta = s.gpsta.p; a.counters = s.counters.p; a.ntmax = s.ntmax.p;
+    const int tok = prof_begin(PROF_DAMAGE, ds);
+    XT_TRY(damage_update(a, ds));
+    prof_end(tok, ds);
+    XT_TRY(any_ge_device(s.D.p, s.ngp, s.cfg.Dc, s.flag.p, ds));
+    XT_TRY(max_value(s.D.p, (size_t)s.ngp, s.red_dmg, ds));
+    XT_CUDA(cudaMemcpyAsync(s.hbuf, s.red_dmg.out.p, sizeof(double), cudaMemcpyDeviceToHost, ds));
+    XT_CUDA(cudaMemcpyAsync(s.hbuf + 1, s.counters.p, 3 * sizeof(unsigned long long),
+                            cudaMemcpyDeviceToHost, ds));
+    XT_CUDA(cudaMemcpyAsync(s.hbuf + 4, s.flag.p, sizeof(int), cudaMemcpyDeviceToHost, ds));
+    XT_CUDA(cudaEventRecord(s.ev_dmg, ds));
+    s.pending = true;
+    return XT_OK;
+}
+
+// Wait for the running update (if any) and keep its deletion flag and
+// stats in the slab object; the stats of the last finished update go to
+// stats[6], [9..11] (stats may be NULL).
+int damage_wait(xt_slab_s& s, double* stats)
+{
+    if (s.pending) {
+        XT_CUDA(cudaEventSynchronize(s.ev_dmg));
+        s.pending = false;
+        unsigned long long cnt[3];
+        std::memcpy(cnt, s.hbuf + 1, sizeof(cnt));
+        int f = 0;
+        std::memcpy(&f, s.hbuf + 4, sizeof(int));
+        s.del_flag = f;
+        s.dmg_stats[0] = s.hbuf[0];
+        for (int k = 0; k < 3; ++k) s.dmg_stats[1 + k] = (double)cnt[k];
+    }
+    if (stats) {
+        stats[6] = s.dmg_stats[0];
+        stats[7] = s.nfailed;
+        stats[9] = s.dmg_stats[1];
+        stats[10] = s.dmg_stats[2];
+        stats[11] = s.dmg_stats[3];
+    }
+    return XT_OK;
+}
+
+// One slab in overlap mode.  D_host (may be NULL) receives the damage after
+// the previous slab, copied before this slab's update starts.
+int step_overlap(xt_slab_s& s, const double* fext_host, double* stats, double* D_host)
+{
+    XT_TRY(overlap_init(s));
+    cudaStream_t st = ctx().stream;
+    const size_t n = (size_t)s.p * s.q;
+    const int slab0 = s.slab;
+    const double tc0[3] = {s.tc[0], s.tc[1], s.tc[2]};
+    XT_CUDA(cudaMemcpyAsync(s.disp_prev.p, s.disp.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    // speculative solve, concurrent with the previous slab's damage update
+    XT_TRY(solve_slab(s, fext_host, stats, false));
+    XT_TRY(damage_wait(s, stats));
+    const int flag = s.del_flag;
+    s.del_flag = 0;
+    if (flag && s.cfg.damage) {
+        // the update deleted elements: repeat this slab exactly as the
+        // sequential loop does it (deletion check first, then the solve)
+        s.slab = slab0;
+        for (int j = 0; j < 3; ++j) s.tc[j] = tc0[j];
+        XT_CUDA(cudaMemcpyAsync(s.disp.p, s.disp_prev.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        XT_TRY(solve_slab(s, fext_host, stats, true));
+    }
+    if (D_host)
+        XT_CUDA(cudaMemcpyAsync(D_host, s.D.p, (size_t)s.ngp * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (s.cfg.damage) XT_TRY(damage_launch(s));
     return XT_OK;
 }
 
@@ -323,9 +456,20 @@ int xt_slab_step(xt_slab s, double* stats)
     double local[12] = {0};
     double* st = stats ? stats : local;
     return guarded([&]() -> int {
+        if (s->cfg.overlap) {
+            XT_TRY(step_overlap(*s, nullptr, st, nullptr));
+            XT_CUDA(cudaStreamSynchronize(ctx().stream));
+            return XT_OK;
+        }
         XT_TRY(solve_slab(*s, nullptr, st));
         return damage_slab(*s, st);
     });
+}
+
+int xt_slab_drain(xt_slab s, double* stats)
+{
+    if (!s) { set_error("null slab"); return XT_ERR_ARG; }
+    return guarded([&]() -> int { return damage_wait(*s, stats); });
 }
 
 int xt_slab_step_host(xt_slab s, const double* fext, double* disp, double* D, double* stats)
@@ -334,29 +478,47 @@ int xt_slab_step_host(xt_slab s, const double* fext, double* disp, double* D, do
     double local[12] = {0};
     double* st = stats ? stats : local;
     return guarded([&]() -> int {
-        XT_TRY(solve_slab(*s, fext, st));
-        XT_TRY(damage_slab(*s, st));
         cudaStream_t cs = ctx().stream;
         const size_t n = (size_t)s->p * s->q;
-        if (disp) {
-            XT_TRY((to_blocks<double, double>(s->disp.p, s->dblk.p, s->p, s->q, cs)));
-            XT_CUDA(cudaMemcpyAsync(disp, s->dblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        if (s->cfg.overlap) {
+            XT_TRY(step_overlap(*s, fext, st, D));
+        } else {
+            XT_TRY(solve_slab(*s, fext, st));
+            XT_TRY(damage_slab(*s, st));
+            if (D) XT_CUDA(cudaMemcpyAsync(D, s->D.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
         }
-        if (D) XT_CUDA(cudaMemcpyAsync(D, s->D.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        if (disp) {
+            XT_TRY(s->hblk.alloc(n));
+            XT_TRY((to_blocks<double, double>(s->disp.p, s->hblk.p, s->p, s->q, cs)));
+            XT_CUDA(cudaMemcpyAsync(disp, s->hblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        }
         XT_CUDA(cudaStreamSynchronize(cs));
         return XT_OK;
     });
 }
 
+int xt_slab_set_state(xt_slab s, const double* D, const double* ws)
+{
+    if (!s) { set_error("null slab"); return XT_ERR_ARG; }
+    XT_TRY(damage_wait(*s, nullptr));
+    cudaStream_t cs = ctx().stream;
+    const size_t b = (size_t)s->ngp * sizeof(double);
+    if (D) XT_CUDA(cudaMemcpyAsync(s->D.p, D, b, cudaMemcpyHostToDevice, cs));
+    if (ws) XT_CUDA(cudaMemcpyAsync(s->ws.p, ws, b, cudaMemcpyHostToDevice, cs));
+    XT_CUDA(cudaStreamSynchronize(cs));
+    return XT_OK;
+}
+
 int xt_slab_get(xt_slab s, double* disp, double* D, double* ws, int* elesta)
 {
     if (!s) { set_error("null slab"); return XT_ERR_ARG; }
+    XT_TRY(damage_wait(*s, nullptr));
     cudaStream_t cs = ctx().stream;
     const size_t n = (size_t)s->p * s->q;
     if (disp) {
-        XT_TRY(s->dblk.alloc(n));
-        XT_TRY((to_blocks<double, double>(s->disp.p, s->dblk.p, s->p, s->q, cs)));
-        XT_CUDA(cudaMemcpyAsync(disp, s->dblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+        XT_TRY(s->hblk.alloc(n));
+        XT_TRY((to_blocks<double, double>(s->disp.p, s->hblk.p, s->p, s->q, cs)));
+        XT_CUDA(cudaMemcpyAsync(disp, s->hblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
     }
     if (D) XT_CUDA(cudaMemcpyAsync(D, s->D.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));
     if (ws) XT_CUDA(cudaMemcpyAsync(ws, s->ws.p, (size_t)s->ngp * sizeof(double), cudaMemcpyDeviceToHost, cs));

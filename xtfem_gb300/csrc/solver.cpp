@@ -50,7 +50,11 @@ int ensure_init(int device)
     }
     XT_CUDA(cudaSetDevice(device));
     if (c.stream) cudaStreamDestroy(c.stream);
-    XT_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    // the solve stream runs at the highest priority, so work overlapped on
+    // lower-priority streams (the slab loop's damage update) yields to it
+    int least = 0, greatest = 0;
+    XT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    XT_CUDA(cudaStreamCreateWithPriority(&c.stream, cudaStreamNonBlocking, greatest));
     c.device = device;
     c.ready = true;
     return XT_OK;
