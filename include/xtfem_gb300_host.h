@@ -141,7 +141,7 @@ int xt_profile_read(int cls, long long *count, double *ms);
 /* Kernel launches issued by the library since load. */
 long long xt_launch_count(void);
 /* CUDA events on the library stream: record slot 0..7, elapsed ms a -> b
- * (waits for b), and a synchronize of the library stream. */
+ * (waits for b), and a synchronize of the device (every system's stream). */
 int xt_mark(int slot);
 double xt_elapsed_ms(int a, int b);
 int xt_sync(void);

@@ -36,7 +36,7 @@ int to_status(int s) { return s; }
 int upload_blocks(xt_system_s& h, const double* host, double* dev_itl)
 {
     System& S = h.sys;
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(h.blk.alloc(n));
     XT_CUDA(cudaMemcpyAsync(h.blk.p, host, n * sizeof(double), cudaMemcpyHostToDevice, s));
@@ -47,7 +47,7 @@ int upload_blocks(xt_system_s& h, const double* host, double* dev_itl)
 int download_blocks(xt_system_s& h, const double* dev_itl, double* host)
 {
     System& S = h.sys;
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(h.blk.alloc(n));
     XT_TRY((to_blocks<double, double>(dev_itl, h.blk.p, S.p, S.q, s)));
@@ -204,7 +204,8 @@ int xt_system_apply(xt_system h, const double* a, const double* b, double alpha,
 {
     if (!h || !a || !b || !x || !y) { set_error("xt_system_apply: null argument"); return XT_ERR_ARG; }
     System& S = h->sys;
-    cudaStream_t s = ctx().stream;
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
     const int q = S.q;
     const size_t n = (size_t)S.p * q;
     XT_TRY(h->a_in.alloc(64));
@@ -228,12 +229,13 @@ int xt_system_lusol(xt_system h, const double* a, const double* x, double* y)
 {
     if (!h || !a || !x || !y) { set_error("xt_system_lusol: null argument"); return XT_ERR_ARG; }
     System& S = h->sys;
+    XT_TRY(system_stream(S));
     if (!S.ilu) { set_error("xt_system_lusol: no factor set"); return XT_ERR_STATE; }
     const int q = S.q;
     const size_t n = (size_t)S.p * q;
     std::vector<double> ainv(q * q);
     XT_TRY(invert_small(q, a, ainv.data()));
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     XT_CUDA(cudaMemcpyAsync(S.Ainv.p, ainv.data(), sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
     XT_TRY(ensure_vec(S.x64, n));
     XT_TRY(ensure_vec(S.r64, n));
@@ -252,12 +254,13 @@ int xt_system_lusol_f32(xt_system h, const double* a, const double* x, double* y
 {
     if (!h || !a || !x || !y) { set_error("xt_system_lusol_f32: null argument"); return XT_ERR_ARG; }
     System& S = h->sys;
+    XT_TRY(system_stream(S));
     if (!S.ilu) { set_error("xt_system_lusol_f32: no factor set"); return XT_ERR_STATE; }
     const int q = S.q;
     const size_t n = (size_t)S.p * q;
     std::vector<double> ainv(q * q);
     XT_TRY(invert_small(q, a, ainv.data()));
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     XT_CUDA(cudaMemcpyAsync(S.Ainv.p, ainv.data(), sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
     XT_TRY(ensure_vec(S.x64, n));
     XT_TRY(ensure_vec(S.r64, n));
@@ -282,6 +285,7 @@ int xt_system_gmres(xt_system h, const double* rhs, double* sol, int im, double 
 {
     if (!h || !rhs || !sol) { set_error("xt_system_gmres: null argument"); return XT_ERR_ARG; }
     System& S = h->sys;
+    XT_TRY(system_stream(S));
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(ensure_vec(S.b64, n));
     XT_TRY(ensure_vec(S.x64, n));
@@ -305,6 +309,7 @@ int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double 
     if (!h || !rhs || !sol) { set_error("xt_system_solve: null argument"); return XT_ERR_ARG; }
     if (precision < 0 || precision > 2) { set_error("xt_system_solve: precision is 0, 1 or 2"); return XT_ERR_ARG; }
     System& S = h->sys;
+    XT_TRY(system_stream(S));
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(ensure_vec(S.b64, n));
     XT_TRY(ensure_vec(S.x64, n));

@@ -43,6 +43,7 @@
 #include <cuda_pipeline.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -233,13 +234,13 @@ struct StageTri {
 
 int max_dyn_smem()
 {
-    static int v = -1;
-    if (v < 0) {
-        int dev = 0;
+    static const int v = [] {
+        int dev = 0, r = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
-            v = 48 * 1024;
-    }
+        if (cudaDeviceGetAttribute(&r, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            r = 48 * 1024;
+        return r;
+    }();
     return v;
 }
 
@@ -1086,13 +1087,13 @@ StageArgs<T> stage_args(const StageTri& t, const unsigned char* rhs, T* out, int
 // groups per compute warp.
 template <class T, int Q>
 int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs<T>),
-              void (*ku)(StageArgs<T>), bool& attr, const double* dAinv, const T* v, T* z,
+              void (*ku)(StageArgs<T>), std::atomic<bool>& attr, const double* dAinv, const T* v, T* z,
               cudaStream_t s)
 {
-    if (!attr) {
+    if (!attr.load(std::memory_order_acquire)) {  // idempotent: concurrent first calls are harmless
         XT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         XT_CUDA(cudaFuncSetAttribute(ku, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     const int g = F.L.g, ng = F.L.ngroups;
     auto warps = [&](const StageTri& t) {
@@ -1119,7 +1120,7 @@ template <class T, int Q, int S>
 int launch_rows(const DevIlu& F, const IluStage& st, const double* dAinv, const T* v, T* z,
                 cudaStream_t s)
 {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     return run_stage<T, Q>(F, st, 32 / (F.L.g * S), k_tri_stage<T, Q, S, false>,
                            k_tri_stage<T, Q, S, true>, attr, dAinv, v, z, s);
 }
@@ -1128,7 +1129,7 @@ template <int Q, int H>
 int launch_blocks(const DevIlu& F, const IluStage& st, const double* dAinv, const float* v,
                   float* z, cudaStream_t s)
 {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};
     return run_stage<float, Q>(F, st, BlockBody<Q, H, false>::GPW, k_tri_block<Q, H, false>,
                                k_tri_block<Q, H, true>, attr, dAinv, v, z, s);
 }

@@ -8,6 +8,9 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <atomic>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "../../include/xtfem_gb300_host.h"
@@ -17,12 +20,17 @@
 namespace xt {
 
 namespace {
+// Records are keyed by token so that several host threads (independent
+// systems on their own streams) can time kernels at once.
 struct Rec {
     int cls;
     cudaEvent_t a, b;
+    bool ended;
 };
+std::mutex g_mu;
 bool g_on = false;
-std::vector<Rec> g_open;
+int g_next = 0;
+std::map<int, Rec> g_open;
 std::vector<cudaEvent_t> g_pool;
 long long g_count[PROF_NCLASS] = {0};
 double g_ms[PROF_NCLASS] = {0};
@@ -39,9 +47,12 @@ cudaEvent_t take()
     return e;
 }
 
-void settle()
+// Sum finished records (caller holds g_mu).
+void settle_locked()
 {
-    for (Rec& r : g_open) {
+    for (auto it = g_open.begin(); it != g_open.end();) {
+        Rec& r = it->second;
+        if (!r.ended) { ++it; continue; }
         cudaEventSynchronize(r.b);
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
@@ -50,25 +61,37 @@ void settle()
         }
         g_pool.push_back(r.a);
         g_pool.push_back(r.b);
+        it = g_open.erase(it);
     }
-    g_open.clear();
+}
+
+void settle()
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    settle_locked();
 }
 }  // namespace
 
 int prof_begin(int cls, cudaStream_t s)
 {
+    std::lock_guard<std::mutex> lk(g_mu);
     if (!g_on) return -1;
-    if (g_open.size() > 4096) settle();
-    Rec r{cls, take(), take()};
+    if (g_open.size() > 4096) settle_locked();
+    const int id = g_next++ & 0x3fffffff;
+    Rec r{cls, take(), take(), false};
     cudaEventRecord(r.a, s);
-    g_open.push_back(r);
-    return (int)g_open.size() - 1;
+    g_open[id] = r;
+    return id;
 }
 
 void prof_end(int token, cudaStream_t s)
 {
-    if (token < 0 || token >= (int)g_open.size()) return;
-    cudaEventRecord(g_open[token].b, s);
+    if (token < 0) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_open.find(token);
+    if (it == g_open.end()) return;
+    cudaEventRecord(it->second.b, s);
+    it->second.ended = true;
 }
 
 }  // namespace xt
@@ -78,6 +101,7 @@ extern "C" {
 int xt_profile(int enable)
 {
     xt::settle();
+    std::lock_guard<std::mutex> lk(xt::g_mu);
     xt::g_on = enable != 0;
     for (int c = 0; c < xt::PROF_NCLASS; ++c) {
         xt::g_count[c] = 0;
@@ -90,6 +114,7 @@ int xt_profile_read(int cls, long long* count, double* ms)
 {
     if (cls < 0 || cls >= xt::PROF_NCLASS) return XT_ERR_ARG;
     xt::settle();
+    std::lock_guard<std::mutex> lk(xt::g_mu);
     if (count) *count = xt::g_count[cls];
     if (ms) *ms = xt::g_ms[cls];
     return XT_OK;
@@ -100,7 +125,7 @@ int xt_profile_read(int cls, long long* count, double* ms)
 // ------------------------------------------------ launch count and timers
 namespace xt {
 namespace {
-long long g_launches = 0;
+std::atomic<long long> g_launches{0};
 cudaEvent_t g_marks[8] = {nullptr};
 }  // namespace
 
@@ -142,7 +167,7 @@ double xt_elapsed_ms(int a, int b)
 int xt_sync(void)
 {
     if (!xt::ctx().ready) return XT_OK;
-    return cudaStreamSynchronize(xt::ctx().stream) == cudaSuccess ? XT_OK : XT_ERR_CUDA;
+    return cudaDeviceSynchronize() == cudaSuccess ? XT_OK : XT_ERR_CUDA;
 }
 
 }  // extern "C"

@@ -84,7 +84,7 @@ int refactor(xt_slab_s& s)
 int upload_operator(xt_slab_s& s)
 {
     const Csr &K = s.pr->sys.K, &M = s.pr->sys.M;
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     XT_TRY(upload_csr(s.S.K, K.n, K.ia.data(), K.ja.data(), K.a.data(), st));
     XT_TRY(upload_csr(s.S.M, M.n, M.ia.data(), M.ja.data(), M.a.data(), st));
     XT_TRY(s.S.bcmask.upload(s.bc.data(), s.bc.size(), st));
@@ -95,7 +95,7 @@ int upload_operator(xt_slab_s& s)
 int deletion_check(xt_slab_s& s, int& deleted)
 {
     deleted = 0;
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     XT_TRY(any_ge_device(s.D.p, s.ngp, s.cfg.Dc, s.flag.p, st));
     int f = 0;
     XT_CUDA(cudaMemcpyAsync(&f, s.flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -127,7 +127,7 @@ int deletion_check(xt_slab_s& s, int& deleted)
 // check (the overlapped loop makes it after a speculative solve).
 int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check = true)
 {
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     const size_t n = (size_t)s.p * s.q;
     s.slab += 1;
     const double t3 = s.tc[2];
@@ -180,7 +180,7 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check 
 
 int damage_slab(xt_slab_s& s, double* stats)
 {
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     const size_t n = (size_t)s.p * s.q;
     if (s.cfg.damage) {
         XT_TRY(s.dblk.alloc(n));
@@ -245,7 +245,7 @@ int overlap_init(xt_slab_s& s)
 // Launch the damage update of the slab just solved on s.ds.
 int damage_launch(xt_slab_s& s)
 {
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     const size_t n = (size_t)s.p * s.q;
     XT_TRY(s.dblk.alloc(n));
     XT_TRY((to_blocks<double, double>(s.disp.p, s.dblk.p, s.p, s.q, st)));
@@ -308,7 +308,7 @@ int damage_wait(xt_slab_s& s, double* stats)
 int step_overlap(xt_slab_s& s, const double* fext_host, double* stats, double* D_host)
 {
     XT_TRY(overlap_init(s));
-    cudaStream_t st = ctx().stream;
+    cudaStream_t st = s.S.stream;
     const size_t n = (size_t)s.p * s.q;
     const int slab0 = s.slab;
     const double tc0[3] = {s.tc[0], s.tc[1], s.tc[2]};
@@ -399,9 +399,10 @@ int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
         S.q = 6;
         XT_TRY(S.A.alloc(64)); XT_TRY(S.B.alloc(64)); XT_TRY(S.Ainv.alloc(64));
         XT_TRY(S.Cj.alloc(64)); XT_TRY(S.Mj.alloc(64));
+        XT_TRY(system_stream(S));
         XT_TRY(upload_operator(*s));
         XT_TRY(refactor(*s));
-        cudaStream_t st = ctx().stream;
+        cudaStream_t st = s->S.stream;
         const size_t n = (size_t)s->p * 6, ngp = s->ngp;
         XT_TRY(s->drext.upload(s->rext.data(), s->p, st));
         XT_TRY(s->fext.alloc(n));
@@ -458,7 +459,7 @@ int xt_slab_step(xt_slab s, double* stats)
     return guarded([&]() -> int {
         if (s->cfg.overlap) {
             XT_TRY(step_overlap(*s, nullptr, st, nullptr));
-            XT_CUDA(cudaStreamSynchronize(ctx().stream));
+            XT_CUDA(cudaStreamSynchronize(s->S.stream));
             return XT_OK;
         }
         XT_TRY(solve_slab(*s, nullptr, st));
@@ -478,7 +479,7 @@ int xt_slab_step_host(xt_slab s, const double* fext, double* disp, double* D, do
     double local[12] = {0};
     double* st = stats ? stats : local;
     return guarded([&]() -> int {
-        cudaStream_t cs = ctx().stream;
+        cudaStream_t cs = s->S.stream;
         const size_t n = (size_t)s->p * s->q;
         if (s->cfg.overlap) {
             XT_TRY(step_overlap(*s, fext, st, D));
@@ -501,7 +502,7 @@ int xt_slab_set_state(xt_slab s, const double* D, const double* ws)
 {
     if (!s) { set_error("null slab"); return XT_ERR_ARG; }
     XT_TRY(damage_wait(*s, nullptr));
-    cudaStream_t cs = ctx().stream;
+    cudaStream_t cs = s->S.stream;
     const size_t b = (size_t)s->ngp * sizeof(double);
     if (D) XT_CUDA(cudaMemcpyAsync(s->D.p, D, b, cudaMemcpyHostToDevice, cs));
     if (ws) XT_CUDA(cudaMemcpyAsync(s->ws.p, ws, b, cudaMemcpyHostToDevice, cs));
@@ -513,7 +514,7 @@ int xt_slab_get(xt_slab s, double* disp, double* D, double* ws, int* elesta)
 {
     if (!s) { set_error("null slab"); return XT_ERR_ARG; }
     XT_TRY(damage_wait(*s, nullptr));
-    cudaStream_t cs = ctx().stream;
+    cudaStream_t cs = s->S.stream;
     const size_t n = (size_t)s->p * s->q;
     if (disp) {
         XT_TRY(s->hblk.alloc(n));

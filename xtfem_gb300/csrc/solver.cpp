@@ -97,6 +97,16 @@ int invert_small(int n, const double* A, double* Ainv)
     return XT_OK;
 }
 
+int system_stream(System& S)
+{
+    XT_TRY(ensure_init());
+    if (S.stream) return XT_OK;
+    int least = 0, greatest = 0;
+    XT_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    XT_CUDA(cudaStreamCreateWithPriority(&S.stream, cudaStreamNonBlocking, greatest));
+    return XT_OK;
+}
+
 int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
                   const int* mi, const int* mj, const double* mv)
 {
@@ -105,7 +115,8 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
         set_error("system_create: need p > 0 and 1 <= q <= 8");
         return XT_ERR_ARG;
     }
-    cudaStream_t s = ctx().stream;
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
     S.p = p;
     S.q = q;
     XT_TRY(upload_csr(S.K, p, ki, kj, kv, s));
@@ -122,7 +133,8 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
 int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group)
 {
     auto f = std::make_shared<DevIlu>();
-    XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, ctx().stream));
+    XT_TRY(system_stream(S));
+    XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, S.stream));
     S.ilu = f;
     return XT_OK;
 }
@@ -134,7 +146,8 @@ int system_set_temporal(System& S, const double* A, const double* B)
     S.hB.assign(B, B + q * q);
     S.hAinv.assign(q * q, 0.0);
     XT_TRY(invert_small(q, A, S.hAinv.data()));
-    cudaStream_t s = ctx().stream;
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
     XT_CUDA(cudaMemcpyAsync(S.A.p, A, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
     XT_CUDA(cudaMemcpyAsync(S.B.p, B, sizeof(double) * q * q, cudaMemcpyHostToDevice, s));
     XT_CUDA(cudaMemcpyAsync(S.Ainv.p, S.hAinv.data(), sizeof(double) * q * q,
@@ -146,9 +159,9 @@ int system_set_temporal(System& S, const double* A, const double* B)
 int system_apply_with(System& S, const double* dA, const double* dB, double alpha, double beta,
                       const double* x, double* y)
 {
-    const int tok = prof_begin(PROF_KRON64, ctx().stream);
-    const int st = kron_spmm<double>(S.K, S.M, S.q, dA, dB, alpha, beta, x, y, ctx().stream);
-    prof_end(tok, ctx().stream);
+    const int tok = prof_begin(PROF_KRON64, S.stream);
+    const int st = kron_spmm<double>(S.K, S.M, S.q, dA, dB, alpha, beta, x, y, S.stream);
+    prof_end(tok, S.stream);
     return st;
 }
 
@@ -213,33 +226,32 @@ struct Ws<float> {
 template <class T>
 int apply_op(System& S, const T* x, T* y)
 {
-    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, ctx().stream);
-    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, 1.0, 0.0, x, y, ctx().stream);
-    prof_end(tok, ctx().stream);
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, S.stream);
+    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, 1.0, 0.0, x, y, S.stream);
+    prof_end(tok, S.stream);
     return st;
 }
 
 template <class T>
 int apply_op_ab(System& S, double alpha, double beta, const T* x, T* y)
 {
-    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, ctx().stream);
-    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, ctx().stream);
-    prof_end(tok, ctx().stream);
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, S.stream);
+    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, S.stream);
+    prof_end(tok, S.stream);
     return st;
 }
 
 template <class T>
 int apply_prec(System& S, const T* v, T* z)
 {
-    const int tok = prof_begin(sizeof(T) == 8 ? PROF_ILU64 : PROF_ILU32, ctx().stream);
-    const int st = ilu_apply<T>(*S.ilu, S.q, S.Ainv.p, v, z, Ws<T>::w(S), ctx().stream);
-    prof_end(tok, ctx().stream);
+    const int tok = prof_begin(sizeof(T) == 8 ? PROF_ILU64 : PROF_ILU32, S.stream);
+    const int st = ilu_apply<T>(*S.ilu, S.q, S.Ainv.p, v, z, Ws<T>::w(S), S.stream);
+    prof_end(tok, S.stream);
     return st;
 }
 
-int fetch(double* h, const double* d, size_t count)
+int fetch(cudaStream_t s, double* h, const double* d, size_t count)
 {
-    cudaStream_t s = ctx().stream;
     XT_CUDA(cudaMemcpyAsync(h, d, count * sizeof(double), cudaMemcpyDeviceToHost, s));
     XT_CUDA(cudaStreamSynchronize(s));
     return XT_OK;
@@ -251,7 +263,7 @@ template <class T>
 int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, GmresStats& st,
                std::vector<double>* hist)
 {
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     T* V = Ws<T>::V(S);
     T* z = Ws<T>::z(S);
@@ -264,14 +276,14 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
     double ro = 0.0, eps1 = 0.0, t;
 
     XT_TRY(norm2<T>(rhs, n, S.red, s));
-    XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+    XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
     const double ro0 = std::sqrt(hbuf[0]);
     // v1 = rhs - A sol
     XT_CUDA(cudaMemcpyAsync(col(0), rhs, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
     XT_TRY((kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, -1.0, 1.0, sol, col(0), s)));
     for (;;) {  // label 20
         XT_TRY(norm2<T>(col(0), n, S.red, s));
-        XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+        XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
         ro = std::sqrt(hbuf[0]);
         if (!std::isfinite(ro)) {
             set_error("gmres: non-finite residual");
@@ -301,7 +313,7 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
             prof_end(otok, s);
-            XT_TRY(fetch(hbuf.data(), S.hsave.p, 2 * i + 1));
+            XT_TRY(fetch(s, hbuf.data(), S.hsave.p, 2 * i + 1));
             for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
             t = std::sqrt(hbuf[2 * i]);
             if (!std::isfinite(t)) {
@@ -381,7 +393,7 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
-    cudaStream_t s = ctx().stream;
+    cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     float2* V = reinterpret_cast<float2*>(S.V64.p);  // double-float basis
     float* Z = S.Z32.p;
@@ -395,14 +407,14 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     double ro = 0.0, eps1 = 0.0, t;
 
     XT_TRY(norm2<double>(rhs, n, S.red, s));
-    XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+    XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
     const double ro0 = std::sqrt(hbuf[0]);
     for (;;) {
         // v1 = (rhs - A sol) / ||rhs - A sol||, the residual formed in FP64
         XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
         XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
-        XT_TRY(fetch(hbuf.data(), S.red.out.p, 1));
+        XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
         ro = std::sqrt(hbuf[0]);
         if (!std::isfinite(ro)) {
             set_error("gmres: non-finite residual");
@@ -436,7 +448,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
             prof_end(otok, s);
-            XT_TRY(fetch(hbuf.data(), S.hsave.p, 2 * i + 1));
+            XT_TRY(fetch(s, hbuf.data(), S.hsave.p, 2 * i + 1));
             for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
             t = std::sqrt(hbuf[2 * i]);
             if (!std::isfinite(t)) {
@@ -497,9 +509,10 @@ int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int ma
         set_error("gmres: restart length must be >= 1");
         return XT_ERR_ARG;
     }
+    XT_TRY(system_stream(S));
     XT_TRY(ensure_workspace(S, im, false));
     XT_TRY(gmres_core<double>(S, b, x, im, eps, maxits, st, hist));
-    return ilu_check(ctx().stream);
+    return ilu_check(S.stream);
 }
 
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
@@ -509,12 +522,13 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
         set_error("solve: no preconditioner set");
         return XT_ERR_STATE;
     }
-    cudaStream_t s = ctx().stream;
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     XT_TRY(ensure_workspace(S, im, inner == 1, inner == 2));
     double hb[2];
     XT_TRY(norm2<double>(b, n, S.red, s));
-    XT_TRY(fetch(hb, S.red.out.p, 1));
+    XT_TRY(fetch(s, hb, S.red.out.p, 1));
     const double bn = std::sqrt(hb[0]);
     st = GmresStats();
     if (bn == 0.0) {
@@ -528,7 +542,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
         XT_CUDA(cudaMemcpyAsync(S.r64.p, b, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         XT_TRY(system_apply(S, -1.0, 1.0, x, S.r64.p));
         XT_TRY(norm2<double>(S.r64.p, n, S.red, s));
-        XT_TRY(fetch(hb, S.red.out.p, 1));
+        XT_TRY(fetch(s, hb, S.red.out.p, 1));
         const double rn = std::sqrt(hb[0]);
         st.relres = rn / bn;
         if (!std::isfinite(rn)) {

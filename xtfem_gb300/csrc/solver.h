@@ -21,6 +21,17 @@ int ensure_init(int device = -1);
 // on the device.  K, M and the factor are uploaded once; the temporal
 // matrices A, B may change every slab.
 struct System {
+    // Every operation on the system runs on its own stream (highest
+    // priority), so independent systems driven from different host threads
+    // run concurrently on the GPU.
+    cudaStream_t stream = nullptr;
+    System() = default;
+    System(const System&) = delete;
+    System& operator=(const System&) = delete;
+    ~System()
+    {
+        if (stream) cudaStreamDestroy(stream);
+    }
     int p = 0, q = 0;
     DevCsr K, M;
     std::shared_ptr<DevIlu> ilu;  // may be shared with a factor cache
@@ -36,6 +47,9 @@ struct System {
     DBuf<double> hsave;
     Reduce red;
 };
+
+// Creates the system's stream if it has none yet.
+int system_stream(System& S);
 
 // Status-returning building blocks
 int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
