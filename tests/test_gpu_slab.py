@@ -75,3 +75,35 @@ def test_overlapped_loop_without_draining(xt, sequential):
     assert [st["deleted"] for st in stats] == [st["deleted"] for st in seq_stats]
     for key in ["disp", "D", "ws", "elesta"]:
         assert np.array_equal(final[key], seq_final[key]), key
+
+
+def test_concurrent_specimens_match_separate_runs(xt):
+    """Two specimens stepped at once from two host threads (each slab loop
+    on its own streams) give the results of running them one after the
+    other."""
+    import threading
+
+    def one(amp, out, key):
+        pr = rod_problem(xt)
+        cfg = xt.SlabConfig.make(amplitude=amp, nipc=32, n1=10, n2=2, im=30, precision=2,
+                                 tol=1e-8, Dc=0.02, overlap=1)
+        s = xt.SlabSolver(pr, cfg)
+        s.set_state(ws=np.full(s.ngp, 31.7))
+        its = [s.step()["its"] for _ in range(4)]
+        out[key] = (its, s.state())
+        s.close()
+        pr.close()
+
+    alone = {}
+    one(900.0, alone, 0)
+    one(1100.0, alone, 1)
+    both = {}
+    ts = [threading.Thread(target=one, args=(a, both, k)) for k, a in enumerate([900.0, 1100.0])]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for k in (0, 1):
+        assert both[k][0] == alone[k][0]
+        for key in ["disp", "D", "ws", "elesta"]:
+            assert np.array_equal(both[k][1][key], alone[k][1][key]), (k, key)

@@ -48,7 +48,8 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
     nvcc = _nvcc()
     OUT.mkdir(exist_ok=True)
     cu, cpp = _sources()
-    headers = list(CSRC.glob("*.h")) + list((HERE.parent / "include").glob("*.h"))
+    headers = (list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) +
+               list((HERE.parent / "include").glob("*.h")))
     cmds = []
     objs = []
     for src in cu:

@@ -15,6 +15,7 @@
 // plus the row pointers, and touches X (gathered, L2-resident) and Y once.
 // In FP32 it is HBM-bound; in FP64 the GB300's FP64 pipe (about 1.2 TFLOP/s)
 // binds first because every nonzero carries q FMAs.
+#include "df.cuh"
 #include "xt_device.h"
 
 namespace xt {
@@ -135,6 +136,125 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
     }
 }
 
+__global__ void k_to_df(const double* __restrict__ a, float2* __restrict__ b, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) {
+        const float h = __double2float_rn(a[i]);
+        b[i] = make_float2(h, __double2float_rn(a[i] - (double)h));
+    }
+}
+
+// (hi, lo) += (vh + vl) x for an FP32 x: vh x exactly (fma), vl x in FP32
+__device__ __forceinline__ void df_axpy(float& hi, float& lo, float vh, float vl, float x)
+{
+    const float p = __fmul_rn(vh, x);
+    const float e = fmaf(vh, x, -p);
+    df_add(hi, lo, p);
+    lo = __fadd_rn(lo, fmaf(vl, x, e));
+}
+
+// The same row-team structure as k_kron_spmm, with double-float values and
+// accumulators, an FP32 X and a double-float Y (alpha = 1, beta = 0).
+template <int Q, int LANES>
+__global__ void __launch_bounds__(256)
+k_kron_df(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
+          const float2* __restrict__ kval, const int* __restrict__ mptr,
+          const int* __restrict__ mcol, const float2* __restrict__ mval,
+          const double* __restrict__ dA, const double* __restrict__ dB,
+          const float* __restrict__ x, float2* __restrict__ y)
+{
+    __shared__ float2 sA[Q * Q], sB[Q * Q];
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) {
+        const float ah = __double2float_rn(dA[i]), bh = __double2float_rn(dB[i]);
+        sA[i] = make_float2(ah, __double2float_rn(dA[i] - (double)ah));
+        sB[i] = make_float2(bh, __double2float_rn(dB[i] - (double)bh));
+    }
+    __syncthreads();
+    constexpr int TPW = 32 / LANES;
+    const int lane = threadIdx.x % LANES;
+    const int team = (threadIdx.x % 32) / LANES;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int nwarp = (gridDim.x * blockDim.x) / 32;
+    for (int rb = gwarp * TPW; rb < p; rb += nwarp * TPW) {
+        const int r = rb + team;
+        const bool act = r < p;
+        float kh[Q], kl[Q], mh[Q], ml[Q];
+#pragma unroll
+        for (int b = 0; b < Q; ++b) kh[b] = kl[b] = mh[b] = ml[b] = 0.0f;
+        const int k0 = act ? kptr[r] : 0, k1 = act ? kptr[r + 1] : 0;
+        for (int k = k0 + lane; k < k1; k += LANES) {
+            const float2 v = kval[k];
+            float xr[Q];
+            load_row<float, Q>(x + (size_t)kcol[k] * Q, xr);
+#pragma unroll
+            for (int b = 0; b < Q; ++b) df_axpy(kh[b], kl[b], v.x, v.y, xr[b]);
+        }
+        const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
+        for (int k = m0 + lane; k < m1; k += LANES) {
+            const float2 v = mval[k];
+            float xr[Q];
+            load_row<float, Q>(x + (size_t)mcol[k] * Q, xr);
+#pragma unroll
+            for (int b = 0; b < Q; ++b) df_axpy(mh[b], ml[b], v.x, v.y, xr[b]);
+        }
+#pragma unroll
+        for (int off = LANES / 2; off > 0; off >>= 1)
+#pragma unroll
+            for (int b = 0; b < Q; ++b) {
+                const float a1 = __shfl_xor_sync(0xffffffffu, kh[b], off, LANES);
+                const float a2 = __shfl_xor_sync(0xffffffffu, kl[b], off, LANES);
+                const float b1 = __shfl_xor_sync(0xffffffffu, mh[b], off, LANES);
+                const float b2 = __shfl_xor_sync(0xffffffffu, ml[b], off, LANES);
+                df_add_df(kh[b], kl[b], a1, a2);
+                df_add_df(mh[b], ml[b], b1, b2);
+            }
+        if (act) {
+#pragma unroll
+            for (int a = 0; a < Q; ++a) {
+                if (lane == a) {
+                    float h = 0.0f, l = 0.0f;
+#pragma unroll
+                    for (int b = 0; b < Q; ++b) {
+                        df_mul_acc(h, l, sA[b * Q + a].x, sA[b * Q + a].y, kh[b], kl[b]);
+                        df_mul_acc(h, l, sB[b * Q + a].x, sB[b * Q + a].y, mh[b], ml[b]);
+                    }
+                    y[(size_t)r * Q + a] = df_norm(h, l);
+                }
+            }
+        }
+    }
+}
+
+template <int Q>
+int launch_df(const DevCsr& K, const DevCsr& M, const double* dA, const double* dB,
+              const float* x, float2* y, cudaStream_t s)
+{
+    constexpr int LANES = 8;
+    const int threads = 256;
+    const int rows_per_block = threads / LANES;
+    int blocks = (K.n + rows_per_block - 1) / rows_per_block;
+    if (blocks < 1) blocks = 1;
+    k_kron_df<Q, LANES><<<blocks, threads, 0, s>>>(K.n, K.rowptr.p, K.col.p, K.vdf.p, M.rowptr.p,
+                                                   M.col.p, M.vdf.p, dA, dB, x, y);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int ensure_df(DevCsr& A, cudaStream_t s)
+{
+    if (A.vdf.p && A.vdf.n == (size_t)A.nnz) return XT_OK;
+    XT_TRY(A.vdf.alloc((size_t)A.nnz));
+    if (A.nnz) {
+        k_to_df<<<1024, 256, 0, s>>>(A.v64.p, A.vdf.p, (size_t)A.nnz);
+        note_launches(1);
+        XT_CUDA(cudaGetLastError());
+    }
+    return XT_OK;
+}
+
 template <class T, int Q>
 int launch_q(const DevCsr& K, const DevCsr& M, const double* dA, const double* dB,
              double alpha, double beta, const T* x, T* y, cudaStream_t s)
@@ -178,6 +298,7 @@ int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
         }
     d.n = n;
     d.nnz = nnz;
+    d.vdf.release();  // remade from the new values on first use
     XT_TRY(d.rowptr.upload(ia, (size_t)n + 1, s));
     XT_TRY(d.col.upload(ja, (size_t)(nnz > 0 ? nnz : 0), s));
     XT_TRY(d.v64.upload(a, (size_t)nnz, s));
@@ -222,6 +343,28 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
     case 6: return launch_q<T, 6>(K, M, dA, dB, alpha, beta, x, y, s);
     case 7: return launch_q<T, 7>(K, M, dA, dB, alpha, beta, x, y, s);
     default: return launch_q<T, 8>(K, M, dA, dB, alpha, beta, x, y, s);
+    }
+}
+
+int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,
+                 float2* y, cudaStream_t s)
+{
+    if (K.n != M.n || q < 1 || q > 8) {
+        set_error("kron_spmm_df: K and M must have the same order and 1 <= q <= 8");
+        return XT_ERR_ARG;
+    }
+    if (K.n == 0) return XT_OK;
+    XT_TRY(ensure_df(K, s));
+    XT_TRY(ensure_df(M, s));
+    switch (q) {
+    case 1: return launch_df<1>(K, M, dA, dB, x, y, s);
+    case 2: return launch_df<2>(K, M, dA, dB, x, y, s);
+    case 3: return launch_df<3>(K, M, dA, dB, x, y, s);
+    case 4: return launch_df<4>(K, M, dA, dB, x, y, s);
+    case 5: return launch_df<5>(K, M, dA, dB, x, y, s);
+    case 6: return launch_df<6>(K, M, dA, dB, x, y, s);
+    case 7: return launch_df<7>(K, M, dA, dB, x, y, s);
+    default: return launch_df<8>(K, M, dA, dB, x, y, s);
     }
 }
 

@@ -10,6 +10,7 @@
 // Every dot product accumulates in FP64 whatever the storage type of the
 // basis, and reductions are two-stage with a fixed order so results are
 // bitwise repeatable run to run.
+#include "df.cuh"
 #include "xt_device.h"
 
 namespace xt {
@@ -57,23 +58,6 @@ __global__ void k_multi_dot(const TV* __restrict__ V, size_t ld, int k, const TV
         const double s = block_sum(acc[c], sh);
         if (threadIdx.x == 0) partial[(size_t)(j0 + c) * nb + blockIdx.x] = s;
     }
-}
-
-// Double-float helpers: a value held as hi + lo in two FP32 numbers.
-// Knuth's two-sum keeps the rounding error of every addition; explicit _rn
-// intrinsics keep the compiler from fusing or reordering the steps.
-__device__ __forceinline__ void df_add(float& hi, float& lo, float x)
-{
-    const float s = __fadd_rn(hi, x);
-    const float bb = __fsub_rn(s, hi);
-    const float t = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(x, bb));
-    hi = s;
-    lo = __fadd_rn(lo, t);
-}
-__device__ __forceinline__ void df_add_df(float& hi, float& lo, float xh, float xl)
-{
-    df_add(hi, lo, xh);
-    lo = __fadd_rn(lo, xl);
 }
 
 // FP32 basis (n and ld even, pairs of rows): each pair of products is
@@ -127,24 +111,6 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
 // |lo| <= ulp(hi)/2 (about 48 significant bits).  The flexible GMRES keeps
 // its FP64-accurate Krylov basis in this form: the same bytes as FP64, but
 // every operation runs on the FP32 pipe.
-
-// (hi, lo) += (ah + al)(bh + bl): the leading product exactly (fma), the
-// cross terms in FP32 (their rounding is below the format's precision).
-__device__ __forceinline__ void df_mul_acc(float& hi, float& lo, float ah, float al, float bh,
-                                           float bl)
-{
-    const float p = __fmul_rn(ah, bh);
-    const float e = fmaf(ah, bh, -p);
-    df_add(hi, lo, p);
-    lo = __fadd_rn(lo, __fadd_rn(e, fmaf(ah, bl, __fmul_rn(al, bh))));
-}
-
-// Renormalise (hi, lo) so that hi carries the rounded value.
-__device__ __forceinline__ float2 df_norm(float hi, float lo)
-{
-    const float s = __fadd_rn(hi, lo);
-    return make_float2(s, __fsub_rn(lo, __fsub_rn(s, hi)));
-}
 
 // partial[(j0+c) nb + b] = (hi, lo) of sum over block b's rows of V_j w
 __global__ void k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,

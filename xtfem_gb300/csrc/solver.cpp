@@ -388,8 +388,9 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
 // double-float (two FP32 numbers per entry: FP64's bytes, about 48
 // significant bits, FP32 arithmetic).  z_j = M^-1 v_j is stored in FP32 and
 // the update is x += Z y, so the Arnoldi relation A Z = V H holds to
-// double-float accuracy however the FP32 preconditioner rounds.  A restart
-// rebuilds the residual explicitly.
+// double-float accuracy however the FP32 preconditioner rounds; the
+// operator is applied to z_j in double-float too (FP64-class result at FP32
+// throughput).  A restart rebuilds the residual explicitly (FP64).
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
@@ -434,9 +435,11 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             const int i1 = i + 1;
             XT_TRY(df_hi(col(i - 1), S.d32.p, n, s));
             XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
-            XT_TRY((axpby<float, double>(n, 1.0, zc(i - 1), 0.0, S.u64.p, s)));
-            XT_TRY(apply_op<double>(S, S.u64.p, S.w64.p));
-            XT_TRY(df_from_f64(S.w64.p, col(i1 - 1), n, s));
+            {  // w = A z in double-float, straight into the basis column
+                const int tok = prof_begin(PROF_KRON64, s);
+                XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, zc(i - 1), col(i1 - 1), s));
+                prof_end(tok, s);
+            }
             const int otok = prof_begin(PROF_ORTH64, s);
             XT_TRY(df_multi_dot(V, n, i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),

@@ -87,6 +87,7 @@ struct DevCsr {
     DBuf<int> rowptr, col;
     DBuf<double> v64;
     DBuf<float> v32;
+    DBuf<float2> vdf;  // double-float (hi, lo) copy, made on first use
 };
 
 // FP64 -> FP32 copy on the device.
@@ -103,6 +104,13 @@ template <class T>
 int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
               const double* dB, double alpha, double beta, const T* x, T* y,
               cudaStream_t s);
+
+// Y := K X A^T + M X B^T with X in FP32 (exact inputs, e.g. preconditioned
+// vectors) and Y in double-float (float2 (hi, lo) per entry): FP64-class
+// accuracy at FP32 throughput.  Makes the double-float copies of the CSR
+// values on first use.
+int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,
+                 float2* y, cudaStream_t s);
 
 // -------------------------------------------------- ILU triangular solves
 // Level-scheduled form of a SPARSKIT MSR factor.  Rows are handled in groups
