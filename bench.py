@@ -288,6 +288,8 @@ def run_batched(xt, args, specimens):
     except threading.BrokenBarrierError:
         pass
     xt.lib().xt_sync()
+    if args.batched_profile:
+        xt.profile(True)
     t0 = time.perf_counter()
     try:
         done.wait()
@@ -295,6 +297,11 @@ def run_batched(xt, args, specimens):
         pass
     xt.lib().xt_sync()
     sec = time.perf_counter() - t0
+    prof = {}
+    if args.batched_profile:
+        prof = {CLASS_NAMES[c]: dict(zip(("launches", "total_ms"), xt.profile_read(c)))
+                for c in CLASS_NAMES}
+        xt.profile(False)
     for t in threads:
         t.join()
     for sl in slabs:
@@ -307,7 +314,8 @@ def run_batched(xt, args, specimens):
             "ms_per_step_all": round(sec * 1e3 / args.steps, 1),
             "iterations_per_slab": float(np.mean(its)), "relres_max": float(np.max(res)),
             "timer": "host wall clock, device synchronised at both ends",
-            "workload": f"{B} independent C2 rods (load amplitudes of seeds 0..{B - 1})"}
+            "workload": f"{B} independent C2 rods (load amplitudes of seeds 0..{B - 1})",
+            **({"kernels": prof} if prof else {})}
 
 
 def run_fp64_reference_point(xt, args):
@@ -510,6 +518,8 @@ def main():
     ap.add_argument("--specimens", type=int, default=8,
                     help="also time this many independent specimens solved concurrently "
                          "(the batched line); 1 = off")
+    ap.add_argument("--batched-profile", action="store_true",
+                    help="per-class CUDA-event times inside the batched run")
     ap.add_argument("--overlap", type=int, default=None,
                     help="1 = each slab's damage update overlaps the next slab's solve")
     ap.add_argument("--precision", type=int, default=None,
