@@ -131,10 +131,14 @@ def peaks():
 
 
 # ------------------------------------------------------------ byte counts
-def algorithmic_bytes(problem, ilu_nnz, p, q=6):
+def algorithmic_bytes(problem, ilu_nnz, p, q=6, merged=True):
     nn, ne, nnz_k, nnz_m = problem.sizes()
-    kron32 = (nnz_k + nnz_m) * (4 + 4) + 2 * (p + 1) * 4 + 2 * p * q * 4
-    kron64 = (nnz_k + nnz_m) * (8 + 4) + 2 * (p + 1) * 4 + 2 * p * q * 8
+    if merged:  # K and M share one pattern: one index array, two value arrays
+        kron32 = nnz_k * (2 * 4 + 4) + (p + 1) * 4 + 2 * p * q * 4
+        kron64 = nnz_k * (2 * 8 + 4) + (p + 1) * 4 + 2 * p * q * 8
+    else:
+        kron32 = (nnz_k + nnz_m) * (4 + 4) + 2 * (p + 1) * 4 + 2 * p * q * 4
+        kron64 = (nnz_k + nnz_m) * (8 + 4) + 2 * (p + 1) * 4 + 2 * p * q * 8
     ilu32 = ilu_nnz * (4 + 4) + 2 * (p + 1) * 4 + p * 4 + 2 * p * q * 4
     ilu64 = ilu_nnz * (8 + 4) + 2 * (p + 1) * 4 + p * 8 + 2 * p * q * 8
     ngp = 8 * ne
@@ -164,6 +168,8 @@ def run_gpu(args, rank, world):
     slab = xt.SlabSolver(prob, cfg)
     p = slab.p
     K = prob.K()
+    Mh = prob.M()
+    merged = bool(np.array_equal(K.ia, Mh.ia) and np.array_equal(K.ja, Mh.ja))
     alu, jlu, ju = xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
     ilu_nnz = len(alu) - p - 1
     info = []
@@ -189,7 +195,7 @@ def run_gpu(args, rank, world):
 
     # roofline of the dominant kernel class
     hbm, peak_kind = peaks()
-    nbytes = algorithmic_bytes(prob, ilu_nnz, p)
+    nbytes = algorithmic_bytes(prob, ilu_nnz, p, merged=merged)
     dom = max((c for c in prof if nbytes[c]), key=lambda c: prof[c][1])
     cnt, tot = prof[dom]
     avg_ms = tot / max(cnt, 1)

@@ -15,6 +15,8 @@
 // plus the row pointers, and touches X (gathered, L2-resident) and Y once.
 // In FP32 it is HBM-bound; in FP64 the GB300's FP64 pipe (about 1.2 TFLOP/s)
 // binds first because every nonzero carries q FMAs.
+#include <cstring>
+
 #include "df.cuh"
 #include "xt_device.h"
 
@@ -67,7 +69,7 @@ const double* vals<double>(const double* v64, const float*) { return v64; }
 template <>
 const float* vals<float>(const double*, const float* v32) { return v32; }
 
-template <class T, int Q, int LANES>
+template <class T, int Q, int LANES, bool MERGED>
 __global__ void __launch_bounds__(256)
 k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
             const T* __restrict__ kval, const int* __restrict__ mptr,
@@ -95,20 +97,36 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
 #pragma unroll
         for (int b = 0; b < Q; ++b) { ak[b] = T(0); am[b] = T(0); }
         const int k0 = act ? kptr[r] : 0, k1 = act ? kptr[r + 1] : 0;
-        for (int k = k0 + lane; k < k1; k += LANES) {
-            const T v = kval[k];
-            T xr[Q];
-            load_row<T, Q>(x + (size_t)kcol[k] * Q, xr);
+        if constexpr (MERGED) {  // one pattern: one index and one X row for both
+#pragma unroll 4
+            for (int k = k0 + lane; k < k1; k += LANES) {
+                const T vk = kval[k], vm = mval[k];
+                T xr[Q];
+                load_row<T, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
-            for (int b = 0; b < Q; ++b) ak[b] = fma(v, xr[b], ak[b]);
-        }
-        const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
-        for (int k = m0 + lane; k < m1; k += LANES) {
-            const T v = mval[k];
-            T xr[Q];
-            load_row<T, Q>(x + (size_t)mcol[k] * Q, xr);
+                for (int b = 0; b < Q; ++b) {
+                    ak[b] = fma(vk, xr[b], ak[b]);
+                    am[b] = fma(vm, xr[b], am[b]);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int k = k0 + lane; k < k1; k += LANES) {
+                const T v = kval[k];
+                T xr[Q];
+                load_row<T, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
-            for (int b = 0; b < Q; ++b) am[b] = fma(v, xr[b], am[b]);
+                for (int b = 0; b < Q; ++b) ak[b] = fma(v, xr[b], ak[b]);
+            }
+            const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
+#pragma unroll 4
+            for (int k = m0 + lane; k < m1; k += LANES) {
+                const T v = mval[k];
+                T xr[Q];
+                load_row<T, Q>(x + (size_t)mcol[k] * Q, xr);
+#pragma unroll
+                for (int b = 0; b < Q; ++b) am[b] = fma(v, xr[b], am[b]);
+            }
         }
 #pragma unroll
         for (int off = LANES / 2; off > 0; off >>= 1)
@@ -157,7 +175,7 @@ __device__ __forceinline__ void df_axpy(float& hi, float& lo, float vh, float vl
 
 // The same row-team structure as k_kron_spmm, with double-float values and
 // accumulators, an FP32 X and a double-float Y (alpha = 1, beta = 0).
-template <int Q, int LANES>
+template <int Q, int LANES, bool MERGED>
 __global__ void __launch_bounds__(256)
 k_kron_df(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
           const float2* __restrict__ kval, const int* __restrict__ mptr,
@@ -184,20 +202,36 @@ k_kron_df(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
 #pragma unroll
         for (int b = 0; b < Q; ++b) kh[b] = kl[b] = mh[b] = ml[b] = 0.0f;
         const int k0 = act ? kptr[r] : 0, k1 = act ? kptr[r + 1] : 0;
-        for (int k = k0 + lane; k < k1; k += LANES) {
-            const float2 v = kval[k];
-            float xr[Q];
-            load_row<float, Q>(x + (size_t)kcol[k] * Q, xr);
+        if constexpr (MERGED) {
+#pragma unroll 4
+            for (int k = k0 + lane; k < k1; k += LANES) {
+                const float2 vk = kval[k], vm = mval[k];
+                float xr[Q];
+                load_row<float, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
-            for (int b = 0; b < Q; ++b) df_axpy(kh[b], kl[b], v.x, v.y, xr[b]);
-        }
-        const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
-        for (int k = m0 + lane; k < m1; k += LANES) {
-            const float2 v = mval[k];
-            float xr[Q];
-            load_row<float, Q>(x + (size_t)mcol[k] * Q, xr);
+                for (int b = 0; b < Q; ++b) {
+                    df_axpy(kh[b], kl[b], vk.x, vk.y, xr[b]);
+                    df_axpy(mh[b], ml[b], vm.x, vm.y, xr[b]);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int k = k0 + lane; k < k1; k += LANES) {
+                const float2 v = kval[k];
+                float xr[Q];
+                load_row<float, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
-            for (int b = 0; b < Q; ++b) df_axpy(mh[b], ml[b], v.x, v.y, xr[b]);
+                for (int b = 0; b < Q; ++b) df_axpy(kh[b], kl[b], v.x, v.y, xr[b]);
+            }
+            const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
+#pragma unroll 4
+            for (int k = m0 + lane; k < m1; k += LANES) {
+                const float2 v = mval[k];
+                float xr[Q];
+                load_row<float, Q>(x + (size_t)mcol[k] * Q, xr);
+#pragma unroll
+                for (int b = 0; b < Q; ++b) df_axpy(mh[b], ml[b], v.x, v.y, xr[b]);
+            }
         }
 #pragma unroll
         for (int off = LANES / 2; off > 0; off >>= 1)
@@ -236,8 +270,14 @@ int launch_df(const DevCsr& K, const DevCsr& M, const double* dA, const double* 
     const int rows_per_block = threads / LANES;
     int blocks = (K.n + rows_per_block - 1) / rows_per_block;
     if (blocks < 1) blocks = 1;
-    k_kron_df<Q, LANES><<<blocks, threads, 0, s>>>(K.n, K.rowptr.p, K.col.p, K.vdf.p, M.rowptr.p,
-                                                   M.col.p, M.vdf.p, dA, dB, x, y);
+    if (M.same_pattern && M.nnz == K.nnz)
+        k_kron_df<Q, LANES, true><<<blocks, threads, 0, s>>>(K.n, K.rowptr.p, K.col.p, K.vdf.p,
+                                                             M.rowptr.p, M.col.p, M.vdf.p, dA, dB,
+                                                             x, y);
+    else
+        k_kron_df<Q, LANES, false><<<blocks, threads, 0, s>>>(K.n, K.rowptr.p, K.col.p, K.vdf.p,
+                                                              M.rowptr.p, M.col.p, M.vdf.p, dA, dB,
+                                                              x, y);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -264,9 +304,14 @@ int launch_q(const DevCsr& K, const DevCsr& M, const double* dA, const double* d
     const int rows_per_block = threads / LANES;
     int blocks = (K.n + rows_per_block - 1) / rows_per_block;
     if (blocks < 1) blocks = 1;
-    k_kron_spmm<T, Q, LANES><<<blocks, threads, 0, s>>>(
-        K.n, K.rowptr.p, K.col.p, vals<T>(K.v64.p, K.v32.p), M.rowptr.p, M.col.p,
-        vals<T>(M.v64.p, M.v32.p), dA, dB, (T)alpha, (T)beta, x, y);
+    if (M.same_pattern && M.nnz == K.nnz)
+        k_kron_spmm<T, Q, LANES, true><<<blocks, threads, 0, s>>>(
+            K.n, K.rowptr.p, K.col.p, vals<T>(K.v64.p, K.v32.p), M.rowptr.p, M.col.p,
+            vals<T>(M.v64.p, M.v32.p), dA, dB, (T)alpha, (T)beta, x, y);
+    else
+        k_kron_spmm<T, Q, LANES, false><<<blocks, threads, 0, s>>>(
+            K.n, K.rowptr.p, K.col.p, vals<T>(K.v64.p, K.v32.p), M.rowptr.p, M.col.p,
+            vals<T>(M.v64.p, M.v32.p), dA, dB, (T)alpha, (T)beta, x, y);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -298,6 +343,7 @@ int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
         }
     d.n = n;
     d.nnz = nnz;
+    d.same_pattern = false;
     d.vdf.release();  // remade from the new values on first use
     XT_TRY(d.rowptr.upload(ia, (size_t)n + 1, s));
     XT_TRY(d.col.upload(ja, (size_t)(nnz > 0 ? nnz : 0), s));
@@ -311,6 +357,16 @@ int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
+}
+
+void csr_mark_shared_pattern(const DevCsr& K, DevCsr& M, const int* ki, const int* kj,
+                             const int* mi, const int* mj)
+{
+    M.same_pattern = false;
+    if (K.n != M.n || K.nnz != M.nnz) return;
+    if (std::memcmp(ki, mi, sizeof(int) * ((size_t)K.n + 1)) != 0) return;
+    if (std::memcmp(kj, mj, sizeof(int) * (size_t)K.nnz) != 0) return;
+    M.same_pattern = true;
 }
 
 int to_f32(const double* a, float* b, size_t n, cudaStream_t s)

@@ -87,6 +87,7 @@ int upload_operator(xt_slab_s& s)
     cudaStream_t st = s.S.stream;
     XT_TRY(upload_csr(s.S.K, K.n, K.ia.data(), K.ja.data(), K.a.data(), st));
     XT_TRY(upload_csr(s.S.M, M.n, M.ia.data(), M.ja.data(), M.a.data(), st));
+    csr_mark_shared_pattern(s.S.K, s.S.M, K.ia.data(), K.ja.data(), M.ia.data(), M.ja.data());
     XT_TRY(s.S.bcmask.upload(s.bc.data(), s.bc.size(), st));
     XT_CUDA(cudaStreamSynchronize(st));
     return XT_OK;

@@ -121,6 +121,7 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
     S.q = q;
     XT_TRY(upload_csr(S.K, p, ki, kj, kv, s));
     XT_TRY(upload_csr(S.M, p, mi, mj, mv, s));
+    csr_mark_shared_pattern(S.K, S.M, ki, kj, mi, mj);
     XT_TRY(S.A.alloc(64));
     XT_TRY(S.B.alloc(64));
     XT_TRY(S.Ainv.alloc(64));

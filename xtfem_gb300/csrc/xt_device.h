@@ -88,7 +88,15 @@ struct DevCsr {
     DBuf<double> v64;
     DBuf<float> v32;
     DBuf<float2> vdf;  // double-float (hi, lo) copy, made on first use
+    // set on M when its pattern equals K's (same mesh): the Kronecker
+    // kernels then read one column index and one X row per nonzero for both
+    bool same_pattern = false;
 };
+
+// Marks M as sharing K's sparsity pattern when the 1-based host arrays are
+// identical (both matrices of one mesh), after both were uploaded.
+void csr_mark_shared_pattern(const DevCsr& K, DevCsr& M, const int* ki, const int* kj,
+                             const int* mi, const int* mj);
 
 // FP64 -> FP32 copy on the device.
 int to_f32(const double* a, float* b, size_t n, cudaStream_t s);
