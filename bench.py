@@ -143,8 +143,13 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6, merged=True):
     ilu64 = ilu_nnz * (8 + 4) + 2 * (p + 1) * 4 + p * 8 + 2 * p * q * 8
     ngp = 8 * ne
     damage = ngp * (29 * 8 * 2 + 8 * 4 + 24 * 8 + 2 * 8) + p * q * 8
+    # double-float SpMM: hi/lo values (8 B), FP32 input, double-float output
+    if merged:
+        krondf = nnz_k * (2 * 8 + 4) + (p + 1) * 4 + p * q * (4 + 8)
+    else:
+        krondf = (nnz_k + nnz_m) * (8 + 4) + 2 * (p + 1) * 4 + p * q * (4 + 8)
     # a CGS2 step's bytes depend on the step index; its class reports time only
-    return {0: kron64, 1: kron32, 2: ilu64, 3: ilu32, 4: damage, 5: None, 6: None}
+    return {0: kron64, 1: kron32, 2: ilu64, 3: ilu32, 4: damage, 5: None, 6: None, 7: krondf}
 
 
 # DRAM bytes per launch of the kernel classes, from one ncu capture each on
@@ -155,7 +160,8 @@ NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 20_210_176 + 20_057_856,
                4: 98_174_464 + 33_518_848}
 
 CLASS_NAMES = {0: "kron_spmm_fp64", 1: "kron_spmm_fp32", 2: "ilu_apply_fp64",
-               3: "ilu_apply_fp32", 4: "damage_update", 5: "cgs2_step_fp64", 6: "cgs2_step_fp32"}
+               3: "ilu_apply_fp32", 4: "damage_update", 5: "cgs2_step_df", 6: "cgs2_step_fp32",
+               7: "kron_spmm_df"}
 
 
 # -------------------------------------------------------------- GPU arm

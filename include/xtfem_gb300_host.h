@@ -135,7 +135,8 @@ int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
 /* Per-kernel CUDA-event timing on the library stream: enable, then read
  * count and total milliseconds per kernel class (0 Kronecker FP64,
  * 1 Kronecker FP32, 2 ILU FP64, 3 ILU FP32, 4 damage, 5 Gram-Schmidt
- * projection of one Arnoldi step with an FP64 basis, 6 with an FP32 basis). */
+ * projection of one Arnoldi step with an FP64-class basis, 6 with an FP32
+ * basis, 7 Kronecker double-float on an FP32 vector). */
 int xt_profile(int enable);
 int xt_profile_read(int cls, long long *count, double *ms);
 /* Kernel launches issued by the library since load. */

@@ -896,10 +896,15 @@ struct RowBody {
 
 // Node-block format (FP32, g = 3, even Q): one lane per (group, pair of
 // temporal blocks, share h of the group's blocks); the H shares are summed
-// with shuffles and each lane finishes its pair for all three rows.
-template <int Q, int H, bool UPPER>
+// with shuffles and each lane finishes its pair for all three rows.  The
+// temporal blocks are independent in a triangular solve, so the Q/2 pairs
+// may be dealt to Q/(2 NPC) thread blocks on as many SMs, NPC pairs each:
+// every block streams the whole factor but gathers and updates only its
+// own pairs' window entries.
+template <int Q, int H, bool UPPER, int NPC = Q / 2>
 struct BlockBody {
-    static constexpr int NP = Q / 2, GS = NP * H, GPW = 32 / GS;
+    static_assert((Q / 2) % NPC == 0, "pairs must divide evenly among the blocks");
+    static constexpr int NP = NPC, GS = NP * H, GPW = 32 / GS;
     int gw, p, h, lane0, warp, ncw;
     bool lane_ok;
     unsigned rsE;
@@ -912,7 +917,7 @@ struct BlockBody {
         gw = lane / GS;
         const int inl = lane - gw * GS;
         h = inl / NP;
-        p = inl - h * NP;
+        p = inl - h * NP + (int)blockIdx.x * NPC;
         lane0 = gw * GS;
         lane_ok = gw < GPW;
         rsE = a.rs / (unsigned)sizeof(float);
@@ -928,9 +933,11 @@ struct BlockBody {
         for (int j0 = warp * GPW; j0 < ng; j0 += ncw * GPW) {
             const int j = j0 + gw;
             const bool act = lane_ok && j < ng;
-            float acc[3][2];
+            // each lane's two temporal blocks are one packed FP32 pair: one
+            // two-wide FMA (two independently rounded FMAs) per matrix entry
+            float2 acc[3];
 #pragma unroll
-            for (int r = 0; r < 3; ++r) acc[r][0] = acc[r][1] = 0.0f;
+            for (int r = 0; r < 3; ++r) acc[r] = make_float2(0.0f, 0.0f);
             int4 gh = make_int4(0, 0, 0, 0);
             if (act) {
                 gh = *reinterpret_cast<const int4*>(grec + (size_t)j * kGrec);
@@ -948,32 +955,28 @@ struct BlockBody {
                     const float v[9] = {r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w, r2.x, r2.y};
 #pragma unroll
                     for (int r = 0; r < 3; ++r) {
-                        acc[r][0] = fmaf(v[r * 3 + 0], x0.x, acc[r][0]);
-                        acc[r][1] = fmaf(v[r * 3 + 0], x0.y, acc[r][1]);
-                        acc[r][0] = fmaf(v[r * 3 + 1], x1.x, acc[r][0]);
-                        acc[r][1] = fmaf(v[r * 3 + 1], x1.y, acc[r][1]);
-                        acc[r][0] = fmaf(v[r * 3 + 2], x2.x, acc[r][0]);
-                        acc[r][1] = fmaf(v[r * 3 + 2], x2.y, acc[r][1]);
+                        acc[r] = __ffma2_rn(make_float2(v[r * 3 + 0], v[r * 3 + 0]), x0, acc[r]);
+                        acc[r] = __ffma2_rn(make_float2(v[r * 3 + 1], v[r * 3 + 1]), x1, acc[r]);
+                        acc[r] = __ffma2_rn(make_float2(v[r * 3 + 2], v[r * 3 + 2]), x2, acc[r]);
                     }
                 }
             }
 #pragma unroll
             for (int m = 1; m < H; m <<= 1) {
-                const int src = lane0 + (h ^ m) * NP + p;
+                const int src = lane0 + (h ^ m) * NP + (p - (int)blockIdx.x * NPC);
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
-                    acc[r][0] += __shfl_sync(0xffffffffu, acc[r][0], src);
-                    acc[r][1] += __shfl_sync(0xffffffffu, acc[r][1], src);
+                    acc[r].x += __shfl_sync(0xffffffffu, acc[r].x, src);
+                    acc[r].y += __shfl_sync(0xffffffffu, acc[r].y, src);
                 }
             }
             if (act) {
                 const float* rr = rh + (size_t)j * rsE + 2 * p;
-                float d[3][2];
+                float2 d[3];
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
                     const float2 bb = *reinterpret_cast<const float2*>(rr + r * Q);
-                    d[r][0] = bb.x - acc[r][0];
-                    d[r][1] = bb.y - acc[r][1];
+                    d[r] = make_float2(bb.x - acc[r].x, bb.y - acc[r].y);
                 }
                 const unsigned char* gm = grec + (size_t)j * kGrec + 16;
                 const float4 m0 = *reinterpret_cast<const float4*>(gm);
@@ -983,13 +986,10 @@ struct BlockBody {
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
                     if (r % H != h) continue;  // row r is stored by share r mod H
-                    float s0 = 0.0f, s1 = 0.0f;
+                    float2 sv = make_float2(0.0f, 0.0f);
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        s0 = fmaf(mv[r * 3 + c], d[c][0], s0);
-                        s1 = fmaf(mv[r * 3 + c], d[c][1], s1);
-                    }
-                    const float2 sv = make_float2(s0, s1);
+                    for (int c = 0; c < 3; ++c)
+                        sv = __ffma2_rn(make_float2(mv[r * 3 + c], mv[r * 3 + c]), d[c], sv);
                     *reinterpret_cast<float2*>(win + gh.z + r * Q + 2 * p) = sv;
                     float* go = UPPER ? out + (size_t)(gh.w + r) * Q + 2 * p
                                       : out + (size_t)gh.w * rsE + r * Q + 2 * p;
@@ -1008,11 +1008,11 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_tri_stage(StageArgs<T> a)
     stage_main<T>(a, body, smem);
 }
 
-template <int Q, int H, bool UPPER>
+template <int Q, int H, bool UPPER, int NPC>
 __global__ void __launch_bounds__(kStageThreads, 1) k_tri_block(StageArgs<float> a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    BlockBody<Q, H, UPPER> body(a);
+    BlockBody<Q, H, UPPER, NPC> body(a);
     stage_main<float>(a, body, smem);
 }
 
@@ -1084,11 +1084,12 @@ StageArgs<T> stage_args(const StageTri& t, const unsigned char* rhs, T* out, int
 }
 
 // Pre-pass, forward sweep kl and backward sweep ku of a staged solve; GPW
-// groups per compute warp.
+// groups per compute warp, each sweep on `grid` thread blocks (independent
+// shares of the temporal blocks).
 template <class T, int Q>
 int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs<T>),
               void (*ku)(StageArgs<T>), std::atomic<bool>& attr, const double* dAinv, const T* v, T* z,
-              cudaStream_t s)
+              cudaStream_t s, int grid = 1)
 {
     if (!attr.load(std::memory_order_acquire)) {  // idempotent: concurrent first calls are harmless
         XT_CUDA(cudaFuncSetAttribute(kl, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
@@ -1109,8 +1110,8 @@ int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs
                                           st.rs / (unsigned)sizeof(T));
     const size_t smL = kHdrBytes + (size_t)st.L.window_bytes + st.L.ring_bytes;
     const size_t smU = kHdrBytes + (size_t)st.U.window_bytes + st.U.ring_bytes;
-    kl<<<1, (wL + 1) * 32, smL, s>>>(stage_args<T>(st.L, st.rhsL.p, recU, wL, st.rs));
-    ku<<<1, (wU + 1) * 32, smU, s>>>(stage_args<T>(st.U, st.rhsU.p, z, wU, st.rs));
+    kl<<<grid, (wL + 1) * 32, smL, s>>>(stage_args<T>(st.L, st.rhsL.p, recU, wL, st.rs));
+    ku<<<grid, (wU + 1) * 32, smU, s>>>(stage_args<T>(st.U, st.rhsU.p, z, wU, st.rs));
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -1125,13 +1126,14 @@ int launch_rows(const DevIlu& F, const IluStage& st, const double* dAinv, const 
                            k_tri_stage<T, Q, S, true>, attr, dAinv, v, z, s);
 }
 
-template <int Q, int H>
+template <int Q, int H, int NPC = Q / 2>
 int launch_blocks(const DevIlu& F, const IluStage& st, const double* dAinv, const float* v,
                   float* z, cudaStream_t s)
 {
     static std::atomic<bool> attr{false};
-    return run_stage<float, Q>(F, st, BlockBody<Q, H, false>::GPW, k_tri_block<Q, H, false>,
-                               k_tri_block<Q, H, true>, attr, dAinv, v, z, s);
+    return run_stage<float, Q>(F, st, BlockBody<Q, H, false, NPC>::GPW,
+                               k_tri_block<Q, H, false, NPC>, k_tri_block<Q, H, true, NPC>, attr,
+                               dAinv, v, z, s, Q / 2 / NPC);
 }
 
 template <class T, int Q>
@@ -1144,6 +1146,14 @@ int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, 
             if (st) {
                 const int H = env_int("XTFEM_ILU_SHARES", 2);
                 if constexpr (Q == 6) {
+                    // thread blocks per sweep: 3 (default, one temporal-block
+                    // pair each) or 1 (all pairs in one block)
+                    if (env_int("XTFEM_ILU_SPLIT", 3) == 3) {
+                        if (H == 1) return launch_blocks<Q, 1, 1>(F, *st, dAinv, v, z, s);
+                        if (H == 4) return launch_blocks<Q, 4, 1>(F, *st, dAinv, v, z, s);
+                        if (H == 8) return launch_blocks<Q, 8, 1>(F, *st, dAinv, v, z, s);
+                        return launch_blocks<Q, 2, 1>(F, *st, dAinv, v, z, s);
+                    }
                     if (H == 1) return launch_blocks<Q, 1>(F, *st, dAinv, v, z, s);
                     if (H == 4) return launch_blocks<Q, 4>(F, *st, dAinv, v, z, s);
                 }

@@ -6,7 +6,7 @@
 namespace xt {
 
 enum ProfClass { PROF_KRON64 = 0, PROF_KRON32 = 1, PROF_ILU64 = 2, PROF_ILU32 = 3, PROF_DAMAGE = 4,
-                 PROF_ORTH64 = 5, PROF_ORTH32 = 6, PROF_NCLASS = 7 };
+                 PROF_ORTH64 = 5, PROF_ORTH32 = 6, PROF_KRONDF = 7, PROF_NCLASS = 8 };
 
 // Returns a token for prof_end, or -1 when profiling is off.
 int prof_begin(int cls, cudaStream_t s);

@@ -437,7 +437,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             XT_TRY(df_hi(col(i - 1), S.d32.p, n, s));
             XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
             {  // w = A z in double-float, straight into the basis column
-                const int tok = prof_begin(PROF_KRON64, s);
+                const int tok = prof_begin(PROF_KRONDF, s);
                 XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, zc(i - 1), col(i1 - 1), s));
                 prof_end(tok, s);
             }
