@@ -81,17 +81,20 @@ def rod8_system(xt):
 
 
 ILU_VARIANTS = [
-    {},                                  # defaults: node blocks, 3 blocks per sweep (FP32), rows S=2 (FP64)
-    {"XTFEM_ILU_SHARES": "1"},
-    {"XTFEM_ILU_SHARES": "4"},
-    {"XTFEM_ILU_SHARES": "8"},
-    {"XTFEM_ILU_SPLIT": "1"},            # all temporal-block pairs in one thread block
-    {"XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_SHARES": "4"},
+    {},                                  # defaults: column records, H=1 (FP32); rows S=2 (FP64)
+    {"XTFEM_ILU_SHARES": "2"},
+    {"XTFEM_ILU_WARPS": "1"},            # one compute warp: many passes per level
+    {"XTFEM_ILU_WARPS": "3"},
+    {"XTFEM_ILU_FMT": "1"},              # node blocks, 3 thread blocks per sweep
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SHARES": "1"},
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SHARES": "4"},
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SHARES": "8"},
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1"},  # all temporal-block pairs in one thread block
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_SHARES": "4"},
+    {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_WARPS": "1"},
     {"XTFEM_ILU_FMT": "0"},              # row format for FP32 too
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "1"},
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "4"},
-    {"XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_WARPS": "1"},
-    {"XTFEM_ILU_WARPS": "1"},            # one compute warp: many passes per level
     {"XTFEM_ILU_SIMPLE": "1"},           # one-warp-per-group fallback
 ]
 

@@ -59,9 +59,10 @@ namespace {
 
 constexpr int kMaxG = 3;
 constexpr int kNB = 16;          // mbarriers per direction: levels in flight < kNB
-constexpr int kHdrBytes = 2 * kNB * 8 + 16;
+constexpr int kTabLevels = 64;  // level table entries staged in shared memory
+constexpr int kHdrBytes = 2 * kNB * 8 + 16 + kTabLevels * 32;
 constexpr long long kSpinLimit = 1ll << 20;
-constexpr int kStageThreads = 512;  // compute warps + the producer warp, at most
+constexpr int kStageThreads = 512;  // compute warps + the producer and waiter warps, at most
 
 struct TriHost {
     int ngroups = 0, nlevels = 0, g = 1, maxw = 0;
@@ -228,8 +229,10 @@ struct Layout {
 struct StageTri {
     bool ok = false;
     int nlevels = 0, g = 1, ring_bytes = 0, window_bytes = 0, p90 = 1;
+    int ncw = 0;  // compute warps the blob was laid out for (column format), else 0
+    int aux = 0;  // column format: window offset of the all-zero padding slot
     DBuf<unsigned char> blob;
-    DBuf<int> table;  // per level {off16, pos16, grp0, iss, len16, rhs16, ng, ne or nb}
+    DBuf<int> table;  // per level {off16, pos16, grp0, iss, len16, rhs16, ng, ne, nb or passes}
 };
 
 int max_dyn_smem()
@@ -245,6 +248,12 @@ int max_dyn_smem()
 }
 
 bool trace_on() { return std::getenv("XTFEM_TRACE") != nullptr; }
+
+int env_int(const char* name, int dflt)
+{
+    const char* e = std::getenv(name);
+    return e ? std::atoi(e) : dflt;
+}
 
 // Node-block format (FP32, g = 3), per level:
 //   header {ng, nb, 0, 0} | ng group records of 64 B {bstart, bcount, gslot,
@@ -488,6 +497,145 @@ int build_block_tri(const TriHost& h, int Q, const std::vector<int>& gdst, Stage
     return finish_stage(out, h, ring, window_bytes, blob, tab, s);
 }
 
+// Column-record format (FP32, g = 3, even Q; one temporal-block pair per
+// thread block, so the window holds 3 rows x 2 values per slot).  A lane
+// owns (group, column c of the 3 x 3 blocks, share h of the group's
+// blocks); at every step it reads one 16-byte record {window offset of the
+// neighbour's row c, column c of the block} and one window pair, and adds
+// one two-wide FMA per row of the group.  The records of a chunk (GPW
+// groups, one warp) are stored step by step, 32 lanes side by side, so a
+// warp's record load is one contiguous 512-byte read with no bank
+// conflicts; lanes past a group's last block read a zero record pointing at
+// an all-zero window slot.  Groups of a level are sorted by block count so
+// that the groups sharing a chunk need about the same number of steps.
+// Per level:
+//   header {ng, passes, chunks, 0} | passes x ncw chunk entries {rec16, steps}
+//   (padded to 16 B) | ng group records of 48 B {gslot, gdst, rhs index,
+//   minv[9] row-major} in chunk order | the chunks' records.
+constexpr unsigned kCgrec = 48;
+
+int col_warps(const TriHost& h, int GPW)
+{
+    std::vector<int> wsz;
+    for (int l = 0; l < h.nlevels; ++l) wsz.push_back(h.level_ptr[l + 1] - h.level_ptr[l]);
+    std::sort(wsz.begin(), wsz.end());
+    const int p90 = std::max(1, wsz[(size_t)(0.9 * (wsz.size() - 1))]);
+    const int w = env_int("XTFEM_ILU_WARPS", (p90 + GPW - 1) / GPW);
+    return std::max(1, std::min(kStageThreads / 32 - 2, w));
+}
+
+int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, StageTri& out,
+                  cudaStream_t s)
+{
+    out.ok = false;
+    if (h.g != 3 || Q % 2 || (H != 1 && H != 2)) return XT_OK;
+    const int g = 3, nl = h.nlevels, GS = 3 * H, GPW = 32 / GS;
+    const int ncw = col_warps(h, GPW);
+    const long long win_elems = ((long long)h.nslots + 1) * 6;
+    const long long window_bytes = (win_elems * 4 + 15) / 16 * 16;
+    const long long ring =
+        std::min<long long>((long long)max_dyn_smem() - kHdrBytes - window_bytes, 192 * 1024) / 16 * 16;
+    if (ring < 16 * 1024 || win_elems >= (1ll << 31)) return XT_OK;
+    const int dummy = h.nslots * 6;
+    const unsigned rs = Layout<float>::up16((unsigned)(g * Q * sizeof(float)));
+    std::vector<int> tab((size_t)nl * 8, 0);
+    std::vector<unsigned> region(nl);
+    std::vector<std::vector<unsigned char>> lv(nl);
+    bool valid = true;
+    size_t total = 0;
+    std::vector<std::vector<int>> bn;     // per group: neighbour groups of its blocks
+    std::vector<std::vector<float>> bv;   // per group: 9 values per block, row-major
+    for (int l = 0; l < nl && valid; ++l) {
+        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
+        bn.assign(ng, {});
+        bv.assign(ng, {});
+        for (int j = 0; j < ng; ++j) {
+            const int i = gb + j;
+            for (int ri = 0; ri < g; ++ri)
+                for (int k = h.ext_ptr[(size_t)i * g + ri]; k < h.ext_ptr[(size_t)i * g + ri + 1]; ++k) {
+                    const int c = h.ext_col[k], Gc = c / g;
+                    int bi = (int)(std::find(bn[j].begin(), bn[j].end(), Gc) - bn[j].begin());
+                    if (bi == (int)bn[j].size()) {
+                        bn[j].push_back(Gc);
+                        bv[j].resize(bv[j].size() + 9, 0.0f);
+                    }
+                    bv[j][(size_t)bi * 9 + ri * 3 + (c - Gc * g)] = (float)h.ext_v[k];
+                }
+        }
+        std::vector<int> ord(ng);
+        for (int j = 0; j < ng; ++j) ord[j] = j;
+        std::stable_sort(ord.begin(), ord.end(),
+                         [&](int a, int b) { return bn[a].size() > bn[b].size(); });
+        const int nchunk = (ng + GPW - 1) / GPW, npass = (nchunk + ncw - 1) / ncw;
+        const size_t ctab = ((size_t)npass * ncw * 8 + 15) / 16 * 16;
+        std::vector<unsigned char>& b = lv[l];
+        b.assign(16 + ctab + (size_t)ng * kCgrec, 0);
+        int* hd = reinterpret_cast<int*>(b.data());
+        hd[0] = ng;
+        hd[1] = npass;
+        hd[2] = nchunk;
+        for (int jj = 0; jj < ng; ++jj) {
+            const int j = ord[jj], i = gb + j, G = h.order[i];
+            int* gr = reinterpret_cast<int*>(b.data() + 16 + ctab + (size_t)jj * kCgrec);
+            const long long so = (long long)h.slot[G] * 6;
+            valid = valid && so >= 0 && so + 6 <= dummy;
+            gr[0] = (int)so;
+            gr[1] = gdst[G];
+            gr[2] = j;
+            float* mv = reinterpret_cast<float*>(gr + 3);
+            for (int e = 0; e < 9; ++e) mv[e] = (float)h.minv[(size_t)i * 9 + e];
+        }
+        for (int c = 0; c < nchunk; ++c) {
+            int steps = 0;
+            for (int jj = c * GPW; jj < std::min(ng, (c + 1) * GPW); ++jj)
+                steps = std::max(steps, (int)((bn[ord[jj]].size() + H - 1) / H));
+            int* ce = reinterpret_cast<int*>(b.data() + 16 + (size_t)c * 8);
+            ce[0] = (int)(b.size() / 16);
+            ce[1] = steps;
+            for (int st = 0; st < steps; ++st)
+                for (int lane = 0; lane < 32; ++lane) {
+                    const int gw = lane / GS, inl = lane - gw * GS, col = inl / H, hh = inl - col * H;
+                    const int jj = c * GPW + gw, bi = hh + H * st;
+                    int off = dummy;
+                    float v[3] = {0.0f, 0.0f, 0.0f};
+                    if (gw < GPW && jj < ng && bi < (int)bn[ord[jj]].size()) {
+                        const int j = ord[jj];
+                        const long long wo = (long long)h.slot[bn[j][bi]] * 6 + 2 * col;
+                        valid = valid && wo >= 0 && wo + 2 <= dummy;
+                        off = (int)wo;
+                        for (int r = 0; r < 3; ++r) v[r] = bv[j][(size_t)bi * 9 + r * 3 + col];
+                    }
+                    unsigned char rec[16];
+                    std::memcpy(rec, &off, 4);
+                    std::memcpy(rec + 4, v, 12);
+                    b.insert(b.end(), rec, rec + 16);
+                }
+        }
+        region[l] = (unsigned)b.size() + (unsigned)ng * rs;
+        int* t = &tab[(size_t)l * 8];
+        t[0] = (int)(total / 16);
+        t[2] = gb;
+        t[4] = (int)(b.size() / 16);
+        t[5] = (int)((unsigned)ng * rs / 16);
+        t[6] = ng;
+        t[7] = npass;
+        total += b.size();
+        valid = valid && total / 16 < (size_t)INT32_MAX;
+    }
+    valid = valid && place_ring(region, ring, tab);
+    if (!valid) {
+        if (trace_on()) std::fprintf(stderr, "[xtfem] column sweep off: schedule check failed\n");
+        return XT_OK;
+    }
+    std::vector<unsigned char> blob;
+    blob.reserve(total);
+    for (auto& b : lv) blob.insert(blob.end(), b.begin(), b.end());
+    XT_TRY(finish_stage(out, h, ring, window_bytes, blob, tab, s));
+    out.ncw = ncw;
+    out.aux = dummy;
+    return XT_OK;
+}
+
 }  // namespace
 
 struct IluStage {
@@ -722,6 +870,7 @@ struct StageArgs {
     T* out;                    // forward: backward-order records; backward: z
     int nl, g, ncw, window_bytes;
     unsigned rs;               // record stride in bytes
+    int aux;                   // column format: offset of the all-zero window slot
 };
 
 // Producer: one thread copies every level's blob and right-hand-side chunk
@@ -756,8 +905,8 @@ __device__ void stage_producer(const StageArgs<T>& a, unsigned long long* full,
     }
 }
 
-// Block skeleton shared by both formats: barrier set-up, the producer warp
-// (the last one) and the compute warps' level loop.  Body::level<RING>
+// Block skeleton shared by both formats: barrier set-up, the producer and
+// waiter warps (the last two) and the compute warps' level loop.  Body::level<RING>
 // computes one level from the ring (RING: shared-memory addresses) or from
 // global memory (levels too large for the ring).
 template <class T, class Body>
@@ -768,6 +917,9 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
     volatile int* s_abort = reinterpret_cast<volatile int*>(cons + kNB);
     T* win = reinterpret_cast<T*>(smem + kHdrBytes);
     unsigned char* ring = smem + kHdrBytes + a.window_bytes;
+    // the level table: a ring of kTabLevels levels in shared memory, so no
+    // global load latency sits on a compute warp's level loop
+    int4* tabs = reinterpret_cast<int4*>(smem + 2 * kNB * 8 + 16);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int i = 0; i < kNB; ++i) {
@@ -777,24 +929,44 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
         *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    for (int i = tid; i < 2 * min(kTabLevels, a.nl); i += blockDim.x) tabs[i] = a.table[i];
     __syncthreads();
     if (warp == a.ncw) {
         if (lane == 0) stage_producer(a, full, cons, ring);
         return;
     }
-    const int nct = a.ncw * 32;
-    int4 c0 = a.table[0], c1 = a.table[1];
-    for (int l = 0; l < a.nl; ++l) {
-        const int ln = min(l + 1, a.nl - 1);
-        const int4 n0 = a.table[2 * ln], n1 = a.table[2 * ln + 1];  // used next level
-        bool ok = mbar_wait(full + l % kNB, (unsigned)(l / kNB) & 1u);
-        ok = __all_sync(0xffffffffu, ok);
-        if (!ok) {
-            if (lane == 0) {
+    // A waiter warp (after the producer) waits for each level's copies and
+    // then joins the level barrier that lets the compute warps start that
+    // level, so the mbarrier wait overlaps the previous level's work.  The
+    // barrier orders the completed copies before the compute warps' reads.
+    const int nbar = (a.ncw + 1) * 32;
+    if (warp == a.ncw + 1) {
+        for (int l = 0; l < a.nl; ++l) {
+            int ok = 1;
+            if (lane == 0) ok = mbar_wait(full + l % kNB, (unsigned)(l / kNB) & 1u) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok && lane == 0) {
                 *s_abort = 1;
                 atomicExch(&g_ilu_error, 1);
             }
-        } else if (c0.y >= 0) {
+            named_barrier(1, nbar);  // the compute warps start level l after it
+            if (*s_abort) return;
+            // levels l-32 .. l-1 are done: their table slots take levels
+            // l+32 .. l+63, read from level l+31 on
+            if (l % (kTabLevels / 2) == 0 && l > 0)
+                for (int i = lane; i < kTabLevels; i += 32) {
+                    const int e = 2 * (l + kTabLevels / 2) + i;
+                    if (e < 2 * a.nl) tabs[e % (2 * kTabLevels)] = a.table[e];
+                }
+        }
+        return;
+    }
+    named_barrier(1, nbar);
+    int4 c0 = tabs[0], c1 = tabs[1];
+    for (int l = 0; l < a.nl && !*s_abort; ++l) {
+        const int ln = min(l + 1, a.nl - 1) % kTabLevels;
+        const int4 n0 = tabs[2 * ln], n1 = tabs[2 * ln + 1];  // used next level
+        if (c0.y >= 0) {
             const unsigned char* base = ring + (size_t)c0.y * 16;
             body.template level<true>(win, base, reinterpret_cast<const T*>(base + (size_t)c1.x * 16),
                                       c1.z, c1.w);
@@ -803,8 +975,7 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
                                        reinterpret_cast<const T*>(a.rhs + (size_t)c0.z * a.rs), c1.z,
                                        c1.w);
         }
-        named_barrier(1, nct);
-        if (*s_abort) break;
+        if (l + 1 < a.nl) named_barrier(1, nbar);
         if (tid == 0) mbar_arrive(cons + l % kNB);
         c0 = n0;
         c1 = n1;
@@ -1016,6 +1187,105 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_tri_block(StageArgs<float>
     stage_main<float>(a, body, smem);
 }
 
+// Column-record format (see build_col_tri): thread block blockIdx.x solves
+// temporal-block pair blockIdx.x; lane = (group, column c, share h).  The
+// H shares are summed with shuffles, then the three columns; the lane of
+// column c (share 0) finishes row c of its group.
+template <int Q, int H, bool UPPER>
+struct ColBody {
+    static constexpr int GS = 3 * H, GPW = 32 / GS;
+    int lane, gw, col, hh, lane0, warp, ncw, pr;
+    bool lane_ok;
+    unsigned rsE;
+    float* out;
+    __device__ ColBody(const StageArgs<float>& a)
+    {
+        lane = threadIdx.x & 31;
+        warp = threadIdx.x >> 5;
+        ncw = a.ncw;
+        gw = lane / GS;
+        const int inl = lane - gw * GS;
+        col = inl / H;
+        hh = inl - col * H;
+        lane0 = gw * GS;
+        lane_ok = gw < GPW;
+        pr = blockIdx.x;
+        rsE = a.rs / (unsigned)sizeof(float);
+        out = a.out;
+    }
+    template <bool RING>
+    __device__ __forceinline__ void level(float* win, const unsigned char* base, const float* rh,
+                                          int ng, int npass)
+    {
+        const int nchunk = reinterpret_cast<const int*>(base)[2];
+        const int2* chunks = reinterpret_cast<const int2*>(base + 16);
+        const unsigned char* grec = base + 16 + (((size_t)npass * ncw * 8 + 15) & ~(size_t)15);
+        for (int k = 0; k < npass; ++k) {
+            const int c = k * ncw + warp;
+            if (c >= nchunk) break;  // warp-uniform
+            const int2 cd = chunks[c];
+            const float4* rp = reinterpret_cast<const float4*>(base + (size_t)cd.x * 16) + lane;
+            float2 acc[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) acc[r] = make_float2(0.0f, 0.0f);
+#pragma unroll 4
+            for (int st = 0; st < cd.y; ++st) {
+                const float4 rec = rp[(size_t)st * 32];
+                const float2 x = *reinterpret_cast<const float2*>(win + __float_as_int(rec.x));
+                acc[0] = __ffma2_rn(make_float2(rec.y, rec.y), x, acc[0]);
+                acc[1] = __ffma2_rn(make_float2(rec.z, rec.z), x, acc[1]);
+                acc[2] = __ffma2_rn(make_float2(rec.w, rec.w), x, acc[2]);
+            }
+#pragma unroll
+            for (int m = 1; m < H; m <<= 1)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    acc[r].x += __shfl_xor_sync(0xffffffffu, acc[r].x, m);
+                    acc[r].y += __shfl_xor_sync(0xffffffffu, acc[r].y, m);
+                }
+            float2 tot[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                const float2 t0 = make_float2(__shfl_sync(0xffffffffu, acc[r].x, lane0),
+                                              __shfl_sync(0xffffffffu, acc[r].y, lane0));
+                const float2 t1 = make_float2(__shfl_sync(0xffffffffu, acc[r].x, lane0 + H),
+                                              __shfl_sync(0xffffffffu, acc[r].y, lane0 + H));
+                const float2 t2 = make_float2(__shfl_sync(0xffffffffu, acc[r].x, lane0 + 2 * H),
+                                              __shfl_sync(0xffffffffu, acc[r].y, lane0 + 2 * H));
+                tot[r] = make_float2((t0.x + t1.x) + t2.x, (t0.y + t1.y) + t2.y);
+            }
+            const int jj = c * GPW + gw;
+            if (lane_ok && hh == 0 && jj < ng) {
+                const int* gr = reinterpret_cast<const int*>(grec + (size_t)jj * kCgrec);
+                const int gslot = gr[0], gdst = gr[1], ridx = gr[2];
+                const float* mv = reinterpret_cast<const float*>(gr + 3) + col * 3;
+                const float* rr = rh + (size_t)ridx * rsE + 2 * pr;
+                float2 sol = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float2 bb = *reinterpret_cast<const float2*>(rr + r * Q);
+                    const float2 d = make_float2(bb.x - tot[r].x, bb.y - tot[r].y);
+                    sol = __ffma2_rn(make_float2(mv[r], mv[r]), d, sol);
+                }
+                *reinterpret_cast<float2*>(win + gslot + 2 * col) = sol;
+                float* go = UPPER ? out + (size_t)(gdst + col) * Q + 2 * pr
+                                  : out + (size_t)gdst * rsE + col * Q + 2 * pr;
+                *reinterpret_cast<float2*>(go) = sol;
+            }
+        }
+    }
+};
+
+template <int Q, int H, bool UPPER>
+__global__ void __launch_bounds__(kStageThreads, 1) k_tri_col(StageArgs<float> a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    // the padding slot reads as zero (ordered by the set-up barrier)
+    if (threadIdx.x < 6) reinterpret_cast<float*>(smem + kHdrBytes)[a.aux + threadIdx.x] = 0.0f;
+    ColBody<Q, H, UPPER> body(a);
+    stage_main<float>(a, body, smem);
+}
+
 // ---------------------------------------------------------------------------
 // Launchers.
 template <class T, int Q>
@@ -1030,20 +1300,16 @@ int launch_tri_simple(const DevIlu& F, const double* dAinv, const T* v, T* z, T*
     return XT_OK;
 }
 
-int env_int(const char* name, int dflt)
-{
-    const char* e = std::getenv(name);
-    return e ? std::atoi(e) : dflt;
-}
-
 // Staged-sweep data for (q, T, format), built on first use; nullptr when
 // the factor cannot use that staged sweep.  fmt 0: rows, 1: node blocks.
 template <class T>
-int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out)
+int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, int H = 0)
 {
     out = nullptr;
     if (!F.sched || env_int("XTFEM_ILU_SIMPLE", 0)) return XT_OK;
-    const int key = 4 * q + 2 * fmt + (sizeof(T) == 4 ? 1 : 0);
+    // the column format's layout depends on the shares and the warp count
+    const int wenv = fmt == 2 ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
+    const int key = (((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (fmt == 2 ? H : 0)) * 64 + wenv;
     auto it = F.stages.find(key);
     if (it == F.stages.end()) {
         auto st = std::make_shared<IluStage>();
@@ -1056,7 +1322,12 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out)
             gdL[G] = U.pos[G];
             gdU[G] = G * g;
         }
-        if (fmt == 1) {
+        if (fmt == 2) {
+            if (sizeof(T) == 4) {
+                XT_TRY(build_col_tri(L, q, H, gdL, st->L, s));
+                XT_TRY(build_col_tri(U, q, H, gdU, st->U, s));
+            }
+        } else if (fmt == 1) {
             if (sizeof(T) == 4) {
                 XT_TRY(build_block_tri(L, q, gdL, st->L, s));
                 XT_TRY(build_block_tri(U, q, gdU, st->U, s));
@@ -1080,7 +1351,7 @@ template <class T>
 StageArgs<T> stage_args(const StageTri& t, const unsigned char* rhs, T* out, int ncw, unsigned rs)
 {
     return {t.blob.p, reinterpret_cast<const int4*>(t.table.p), rhs, out, t.nlevels, t.g, ncw,
-            t.window_bytes, rs};
+            t.window_bytes, rs, t.aux};
 }
 
 // Pre-pass, forward sweep kl and backward sweep ku of a staged solve; GPW
@@ -1098,8 +1369,9 @@ int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs
     }
     const int g = F.L.g, ng = F.L.ngroups;
     auto warps = [&](const StageTri& t) {
+        if (t.ncw > 0) return t.ncw;  // laid out for this warp count
         const int w = env_int("XTFEM_ILU_WARPS", (t.p90 + GPW - 1) / GPW);
-        return std::max(1, std::min(kStageThreads / 32 - 1, w));
+        return std::max(1, std::min(kStageThreads / 32 - 2, w));  // + producer + waiter
     };
     const int wL = warps(st.L), wU = warps(st.U);
     const long long total = (long long)ng * g * Q;
@@ -1110,8 +1382,8 @@ int run_stage(const DevIlu& F, const IluStage& st, int GPW, void (*kl)(StageArgs
                                           st.rs / (unsigned)sizeof(T));
     const size_t smL = kHdrBytes + (size_t)st.L.window_bytes + st.L.ring_bytes;
     const size_t smU = kHdrBytes + (size_t)st.U.window_bytes + st.U.ring_bytes;
-    kl<<<grid, (wL + 1) * 32, smL, s>>>(stage_args<T>(st.L, st.rhsL.p, recU, wL, st.rs));
-    ku<<<grid, (wU + 1) * 32, smU, s>>>(stage_args<T>(st.U, st.rhsU.p, z, wU, st.rs));
+    kl<<<grid, (wL + 2) * 32, smL, s>>>(stage_args<T>(st.L, st.rhsL.p, recU, wL, st.rs));
+    ku<<<grid, (wU + 2) * 32, smU, s>>>(stage_args<T>(st.U, st.rhsU.p, z, wU, st.rs));
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -1136,12 +1408,30 @@ int launch_blocks(const DevIlu& F, const IluStage& st, const double* dAinv, cons
                                dAinv, v, z, s, Q / 2 / NPC);
 }
 
+template <int Q, int H>
+int launch_cols(const DevIlu& F, const IluStage& st, const double* dAinv, const float* v, float* z,
+                cudaStream_t s)
+{
+    static std::atomic<bool> attr{false};
+    return run_stage<float, Q>(F, st, ColBody<Q, H, false>::GPW, k_tri_col<Q, H, false>,
+                               k_tri_col<Q, H, true>, attr, dAinv, v, z, s, Q / 2);
+}
+
 template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
 {
     IluStage* st = nullptr;
     if constexpr (sizeof(T) == 4 && Q % 2 == 0) {
-        if (F.L.g == 3 && env_int("XTFEM_ILU_FMT", 1) == 1) {
+        const int fmt = env_int("XTFEM_ILU_FMT", 2);
+        if (F.L.g == 3 && fmt == 2) {
+            const int H = env_int("XTFEM_ILU_SHARES", 1) == 2 ? 2 : 1;
+            XT_TRY(get_stage<T>(F, Q, 2, s, st, H));
+            if (st) {
+                if (H == 1) return launch_cols<Q, 1>(F, *st, dAinv, v, z, s);
+                return launch_cols<Q, 2>(F, *st, dAinv, v, z, s);
+            }
+        }
+        if (F.L.g == 3 && fmt >= 1) {
             XT_TRY(get_stage<T>(F, Q, 1, s, st));
             if (st) {
                 const int H = env_int("XTFEM_ILU_SHARES", 2);
