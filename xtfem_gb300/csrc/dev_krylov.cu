@@ -13,6 +13,8 @@
 #include "df.cuh"
 #include "xt_device.h"
 
+#include <algorithm>
+
 namespace xt {
 
 namespace {
@@ -652,11 +654,15 @@ int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, R
     if (k > r.kmax) { set_error("df_multi_dot: k exceeds reduction capacity"); return XT_ERR_ARG; }
     if (k <= 0) return XT_OK;
     if (n % 2 || ld % 2) { set_error("df_multi_dot: n and ld must be even"); return XT_ERR_ARG; }
-    dim3 grid(r.nblocks, (k + kChunk - 1) / kChunk);
+    // about eight resident blocks per SM over all chunks: row blocks shrink
+    // as k grows, so each block's rows outweigh its block reduction
+    const int nchunk = (k + kChunk - 1) / kChunk;
+    const int nb = std::max(38, std::min(r.nblocks, (8 * 152 + nchunk - 1) / nchunk));
+    dim3 grid(nb, nchunk);
     k_multi_dot_df<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                              reinterpret_cast<const float4*>(w), n / 2,
                                              r.partial.p);
-    k_finish_df<<<k, kThreads, 0, s>>>(r.partial.p, r.nblocks, r.out.p);
+    k_finish_df<<<k, kThreads, 0, s>>>(r.partial.p, nb, r.out.p);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
