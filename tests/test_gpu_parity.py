@@ -96,6 +96,15 @@ ILU_VARIANTS = [
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "1"},
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "4"},
     {"XTFEM_ILU_SIMPLE": "1"},           # one-warp-per-group fallback
+    # tight rings: a level's copy often needs the region of the level just
+    # before it, so that level must be released before the next can start
+    {"XTFEM_ILU_RING_KB": "10"},
+    {"XTFEM_ILU_RING_KB": "14"},
+    {"XTFEM_ILU_RING_KB": "20"},
+    {"XTFEM_ILU_RING_KB": "6", "XTFEM_ILU_FMT": "1"},
+    {"XTFEM_ILU_RING_KB": "10", "XTFEM_ILU_FMT": "1"},
+    {"XTFEM_ILU_RING_KB": "6", "XTFEM_ILU_FMT": "0"},
+    {"XTFEM_ILU_RING_KB": "10", "XTFEM_ILU_FMT": "0"},
 ]
 
 

@@ -255,6 +255,15 @@ int env_int(const char* name, int dflt)
     return e ? std::atoi(e) : dflt;
 }
 
+// Ring size cap; XTFEM_ILU_RING_KB shrinks it (tests use a tight ring to
+// make levels wait for the region of the level just before them).
+long long ring_cap()
+{
+    const int kb = env_int("XTFEM_ILU_RING_KB", 0);
+    return kb > 0 ? std::max(2, std::min(192, kb)) * 1024ll : 192 * 1024ll;
+}
+long long ring_min() { return env_int("XTFEM_ILU_RING_KB", 0) > 0 ? 2 * 1024 : 16 * 1024; }
+
 // Node-block format (FP32, g = 3), per level:
 //   header {ng, nb, 0, 0} | ng group records of 64 B {bstart, bcount, gslot,
 //   gdst, minv[9] row-major, pad} | nb blocks of 48 B {woff, v[9] row-major
@@ -271,8 +280,8 @@ bool stage_sizes(const TriHost& h, int Q, size_t tsize, long long& win_elems,
     win_elems = (long long)h.nslots * h.g * Q;
     window_bytes = (win_elems * (long long)tsize + 15) / 16 * 16;
     const long long budget = (long long)max_dyn_smem() - kHdrBytes - window_bytes;
-    ring = std::min<long long>(budget, 192 * 1024) / 16 * 16;
-    if (ring < 16 * 1024 || win_elems >= (1ll << 31)) {
+    ring = std::min<long long>(budget, ring_cap()) / 16 * 16;
+    if (ring < ring_min() || win_elems >= (1ll << 31)) {
         if (trace_on())
             std::fprintf(stderr, "[xtfem] staged sweep off: window %lld B, ring %lld B\n",
                          window_bytes, ring);
@@ -335,6 +344,15 @@ int finish_stage(StageTri& out, const TriHost& h, long long ring, long long wind
     for (int l = 0; l < h.nlevels; ++l) wsz.push_back(h.level_ptr[l + 1] - h.level_ptr[l]);
     std::sort(wsz.begin(), wsz.end());
     out.p90 = std::max(1, wsz[(size_t)(0.9 * (wsz.size() - 1))]);
+    if (trace_on()) {
+        int tight = 0, global = 0;
+        for (int l = 0; l < h.nlevels; ++l) {
+            tight += tab[(size_t)l * 8 + 3] == l;
+            global += tab[(size_t)l * 8 + 1] < 0;
+        }
+        std::fprintf(stderr, "[xtfem] staged sweep: %d levels, ring %lld B, %d issued at their own level, %d from global\n",
+                     h.nlevels, ring, tight, global);
+    }
     out.nlevels = h.nlevels;
     out.g = h.g;
     out.ring_bytes = (int)ring;
@@ -534,8 +552,8 @@ int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, 
     const long long win_elems = ((long long)h.nslots + 1) * 6;
     const long long window_bytes = (win_elems * 4 + 15) / 16 * 16;
     const long long ring =
-        std::min<long long>((long long)max_dyn_smem() - kHdrBytes - window_bytes, 192 * 1024) / 16 * 16;
-    if (ring < 16 * 1024 || win_elems >= (1ll << 31)) return XT_OK;
+        std::min<long long>((long long)max_dyn_smem() - kHdrBytes - window_bytes, ring_cap()) / 16 * 16;
+    if (ring < ring_min() || win_elems >= (1ll << 31)) return XT_OK;
     const int dummy = h.nslots * 6;
     const unsigned rs = Layout<float>::up16((unsigned)(g * Q * sizeof(float)));
     std::vector<int> tab((size_t)nl * 8, 0);
@@ -924,7 +942,7 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
     if (tid == 0) {
         for (int i = 0; i < kNB; ++i) {
             mbar_init(full + i, 1);
-            mbar_init(cons + i, 1);
+            mbar_init(cons + i, a.ncw);  // one arrival per compute warp
         }
         *s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -975,8 +993,12 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
                                        reinterpret_cast<const T*>(a.rhs + (size_t)c0.z * a.rs), c1.z,
                                        c1.w);
         }
+        // this warp is done with the level's ring region; the region is
+        // released by the last warp's arrival, before the level barrier
+        // (the next level's copy may need exactly this region)
+        __syncwarp();
+        if (lane == 0) mbar_arrive(cons + l % kNB);
         if (l + 1 < a.nl) named_barrier(1, nbar);
-        if (tid == 0) mbar_arrive(cons + l % kNB);
         c0 = n0;
         c1 = n1;
     }
@@ -1309,7 +1331,9 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
     if (!F.sched || env_int("XTFEM_ILU_SIMPLE", 0)) return XT_OK;
     // the column format's layout depends on the shares and the warp count
     const int wenv = fmt == 2 ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
-    const int key = (((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (fmt == 2 ? H : 0)) * 64 + wenv;
+    const int rkb = std::max(0, std::min(255, env_int("XTFEM_ILU_RING_KB", 0)));
+    const int key =
+        ((((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (fmt == 2 ? H : 0)) * 64 + wenv) * 256 + rkb;
     auto it = F.stages.find(key);
     if (it == F.stages.end()) {
         auto st = std::make_shared<IluStage>();
