@@ -262,6 +262,8 @@ def run_gpu(args, rank, world):
     }
     if rank == 0 and args.specimens > 1:
         out["batched"] = run_batched(xt, args, args.specimens)
+    if rank == 0 and args.rods > 0:
+        out["rod_batch"] = run_rod_batch(xt, args.rods, WORKLOAD["seed"])
     if rank == 0 and not args.skip_fp64:
         out["fp64_gpu"] = run_fp64_reference_point(xt, args)
     if rank == 0 and not args.skip_e2e:
@@ -272,6 +274,70 @@ def run_gpu(args, rank, world):
     slab.close()
     prob.close()
     return out
+
+
+def rod_system(xt, n, amp, dt=0.5, freq=20.0):
+    """Space-time system and first-slab load of the n x n x 3n rod (clamped
+    at x = 0, axial traction amp MPa on x = 3 shared by the face's nodes),
+    ILUT(1e-4, 20) factor attached."""
+    pr = xt.Problem.rod(3 * n, n, n, 3.0, 1.0, 1.0, WORKLOAD["E"], WORKLOAD["nu"], WORKLOAD["rho"])
+    xyz, _ = pr.mesh()
+    bc = np.repeat((xyz[:, 0] == 0.0).astype(np.int32), 3)
+    pr.apply_bc(bc)
+    K, M = pr.K(), pr.M()
+    alu, jlu, ju = xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
+    w = 2 * np.pi * freq
+    k, m, kt, mt, _, _ = xt.stcoeff_m(0.0, dt, w)
+    face = np.isclose(xyz[:, 0], 3.0)
+    rext = np.zeros(K.n)
+    rext[3 * np.flatnonzero(face)] = amp / face.sum()
+    fextc, _ = xt.getfextc_m(0.0, w, dt)
+    rhs = np.concatenate([f * rext for f in fextc])
+    rhs[np.tile(bc, 6) == 1] = 0.0
+    s = xt.SpaceTimeSystem(K, M)
+    s.set_ilu(alu, jlu, ju, group=3)
+    s.set_temporal(k + kt, m + mt)
+    pr.close()
+    return s, rhs
+
+
+def run_rod_batch(xt, count, seed):
+    """The many-rod workload: `count` rods of n x n x 3n elements, n drawn
+    uniformly from 4..10 and the load amplitude from U(50, 150) MPa with
+    numpy's default_rng(seed); one slab solve each (flexible GMRES(30),
+    FP32 ILU, true residual <= 1e-8) through xt_batch_solve, against the
+    same systems solved one after another.  Host wall clock with the device
+    synchronised at both ends; one untimed batch solve first."""
+    rng = np.random.default_rng(seed)
+    ns = rng.integers(4, 11, count)
+    amps = rng.uniform(50.0, 150.0, count)
+    cases = [rod_system(xt, int(n), float(a)) for n, a in zip(ns, amps)]
+    systems = [c[0] for c in cases]
+    rhs = [c[1] for c in cases]
+    batch = xt.SystemBatch(systems)
+    kw = dict(im=30, tol=WORKLOAD["tol"], precision=2)
+    batch.solve(rhs, **kw)
+    xt.lib().xt_sync()
+    t0 = time.perf_counter()
+    _, stats, _ = batch.solve(rhs, **kw)
+    xt.lib().xt_sync()
+    t_batch = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for s, r in zip(systems, rhs):
+        s.solve(r, **kw)
+    xt.lib().xt_sync()
+    t_seq = time.perf_counter() - t0
+    batch.close()
+    dofs = int(sum(s.p * s.q for s in systems))
+    for s in systems:
+        s.close()
+    return {"rods": count, "value": round(count / t_batch, 2), "unit": "rod-slab-solves/s",
+            "ms_all": round(t_batch * 1e3, 2), "one_after_another_ms": round(t_seq * 1e3, 2),
+            "iterations_mean": round(float(np.mean([st["its"] for st in stats])), 1),
+            "relres_max": float(max(st["relres"] for st in stats)),
+            "space_time_dofs": dofs, "n_values": ns.tolist(),
+            "timer": "host wall clock, device synchronised at both ends",
+            "workload": f"{count} rods n x n x 3n, n ~ U{{4..10}}, amplitude U(50,150) MPa, seed {seed}"}
 
 
 def run_batched(xt, args, specimens):
@@ -553,6 +619,8 @@ def main():
     ap.add_argument("--specimens", type=int, default=8,
                     help="also time this many independent specimens solved concurrently "
                          "(the batched line); 1 = off")
+    ap.add_argument("--rods", type=int, default=64,
+                    help="also time a batch of this many uneven rods (xt_batch_solve); 0 = off")
     ap.add_argument("--batched-profile", action="store_true",
                     help="per-class CUDA-event times inside the batched run")
     ap.add_argument("--overlap", type=int, default=None,

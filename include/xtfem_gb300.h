@@ -190,11 +190,39 @@ int xt_system_gmres(xt_system s, const double *rhs, double *sol, int im,
 /* Solve to a true relative residual <= tol with FP64 residuals and
  * solution; precision 0 runs FP64 GMRES cycles, 1 runs FP32 operator,
  * factor and Krylov basis (FP64 dot products and Hessenberg) inside FP64
- * iterative refinement.  out_stats (may be NULL) gets 6 values: iterations,
- * cycles, refinement passes, ierr, true relative residual, last estimate. */
+ * iterative refinement, 2 runs flexible GMRES with the FP32 factor and a
+ * double-float (FP32 pair) basis and operator on the preconditioned
+ * vectors.  out_stats (may be NULL) gets 6 values: iterations, cycles,
+ * refinement passes, ierr, true relative residual, last estimate. */
 int xt_system_solve(xt_system s, const double *rhs, double *sol, int im,
                     double tol, int maxits, int precision, double inner_tol,
                     double *out_stats);
+
+/* ------------------------------------------------ batches of systems */
+
+/* A batch of independent systems (load cases or specimens of uneven
+ * sizes) solved together.  No counterpart in the reference, which solves
+ * one system per process; these are the batched entries of the many-rod
+ * workload (64 rods of n x n x 3n elements).  Each system keeps its own
+ * stream; a pool of host worker threads drives them, largest first, so the
+ * level-scheduled triangular sweeps of different systems (each a
+ * dependent chain on three SMs) and their bandwidth-bound kernels run at
+ * the same time on different SMs.  The systems stay owned by the caller
+ * and must outlive the batch; a system must not be used elsewhere while a
+ * batch solve runs.  workers <= 0 picks min(count, 16). */
+typedef struct xt_batch_s *xt_batch;
+
+int xt_batch_create(int count, const xt_system *systems, int workers, xt_batch *out);
+int xt_batch_destroy(xt_batch b);
+/* xt_system_solve on every system of the batch: rhs[i] and sol[i] are
+ * system i's host vectors (block layout; sol[i] is the initial guess and
+ * receives the solution).  stats (may be NULL) gets 6 values per system as
+ * in xt_system_solve; status (may be NULL) gets each system's return code.
+ * Returns XT_OK when every system succeeded, else the first failing
+ * system's code (its message is the batch's last error). */
+int xt_batch_solve(xt_batch b, const double *const *rhs, double *const *sol, int im,
+                   double tol, int maxits, int precision, double inner_tol,
+                   double *stats, int *status);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,84 @@
+"""GPU batches of independent systems (xt_batch_*): rods of n x n x 3n
+elements with uneven n and their own load amplitudes, as in the many-rod
+workload, solved together; each result equals the same system solved
+alone, and the smallest rod (the 4 x 4 x 12 mesh) matches the oracle's
+FP64 GMRES."""
+import numpy as np
+import pytest
+
+from conftest import clamp_mask, temporal
+
+pytestmark = pytest.mark.gpu
+
+
+def rod_case(xt, n, amp, dt=0.5, freq=20.0):
+    """System and first-slab load of the n x n x 3n rod: clamped at x = 0,
+    axial traction of amplitude amp (MPa) on x = 3 shared equally by the
+    face's nodes, temporal load shape of the slab [0, dt]."""
+    pr = xt.Problem.rod(3 * n, n, n, 3.0, 1.0, 1.0, 2.0e5, 0.3, 7.8e-9)
+    xyz, _ = pr.mesh()
+    bc = clamp_mask(xyz)
+    pr.apply_bc(bc)
+    K, M = pr.K(), pr.M()
+    alu, jlu, ju = xt.ilut(K, 20, 1e-4)
+    A, B, _, _ = temporal(xt, dt=dt, freq=freq)
+    face = np.isclose(xyz[:, 0], 3.0)
+    rext = np.zeros(K.n)
+    rext[3 * np.flatnonzero(face)] = amp * 1.0 / face.sum()
+    fextc, _ = xt.getfextc_m(0.0, 2 * np.pi * freq, dt)
+    rhs = np.concatenate([f * rext for f in fextc])
+    rhs[np.tile(bc, 6) == 1] = 0.0
+    s = xt.SpaceTimeSystem(K, M)
+    s.set_ilu(alu, jlu, ju, group=3)
+    s.set_temporal(A, B)
+    pr.close()
+    return dict(sys=s, K=K, M=M, alu=alu, jlu=jlu, ju=ju, A=A, B=B, rhs=rhs, n=n)
+
+
+@pytest.fixture(scope="module")
+def cases(xt):
+    rng = np.random.default_rng(4)
+    ns = [4, 7, 5, 6, 4, 5]
+    out = [rod_case(xt, n, float(rng.uniform(50.0, 150.0))) for n in ns]
+    yield out
+    for c in out:
+        c["sys"].close()
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_batch_equals_separate_solves(xt, cases, precision):
+    alone = [c["sys"].solve(c["rhs"], im=30, tol=1e-8, precision=precision) for c in cases]
+    batch = xt.SystemBatch([c["sys"] for c in cases], workers=4)
+    sols, stats, status = batch.solve([c["rhs"] for c in cases], im=30, tol=1e-8,
+                                      precision=precision)
+    batch.close()
+    assert (status == 0).all()
+    for (x, st), y, bst in zip(alone, sols, stats):
+        assert np.array_equal(x, y)
+        assert bst["its"] == st["its"] and bst["relres"] <= 1e-8
+
+
+def test_batch_smallest_rod_matches_oracle(xt, orc, cases):
+    c = cases[0]
+    assert c["n"] == 4
+    batch = xt.SystemBatch([cc["sys"] for cc in cases])
+    sols, stats, _ = batch.solve([cc["rhs"] for cc in cases], im=30, tol=1e-8, precision=2)
+    batch.close()
+    ref, ierr, _, _ = orc.kronpgmres(c["A"], c["B"], c["K"], c["M"], c["alu"], c["jlu"], c["ju"],
+                                     c["rhs"], im=30, eps=1e-10, maxits=2000)
+    assert ierr == 0
+    assert np.linalg.norm(sols[0] - ref) <= 1e-6 * np.linalg.norm(ref)
+
+
+def test_batch_reports_the_failing_system(xt, cases):
+    """A system without a factor fails on its own; the others still solve
+    and the error names the failing system."""
+    c = cases[2]
+    bare = xt.SpaceTimeSystem(c["K"], c["M"])
+    bare.set_temporal(c["A"], c["B"])
+    systems = [cases[0]["sys"], bare, cases[3]["sys"]]
+    batch = xt.SystemBatch(systems, workers=2)
+    with pytest.raises(xt.XtError, match="system 1"):
+        batch.solve([cases[0]["rhs"], c["rhs"], cases[3]["rhs"]], im=30, tol=1e-8, precision=2)
+    batch.close()
+    bare.close()

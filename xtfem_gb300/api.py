@@ -21,11 +21,12 @@ from dataclasses import dataclass, fields
 
 import numpy as np
 
-from ._lib import XtError, check, dptr, dref, iptr, iref, lib
+from ._lib import XtError, _dp, check, dptr, dref, iptr, iref, lib
 
 __all__ = [
     "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "chkelesta", "kokkos_host",
     "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "nt_table", "SpaceTimeSystem",
+    "SystemBatch",
     "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
 ]
 
@@ -284,6 +285,43 @@ class SpaceTimeSystem:
         keys = ["its", "cycles", "outer", "ierr", "relres", "est"]
         return s, {k: (int(v) if k in ("its", "cycles", "outer", "ierr") else float(v))
                    for k, v in zip(keys, st)}
+
+
+class SystemBatch:
+    """Independent systems solved together (xt_batch_*): one host worker
+    thread per system at a time, each system on its own stream."""
+
+    def __init__(self, systems, workers=0):
+        self.systems = list(systems)
+        arr = (C.c_void_p * len(self.systems))(*[s._h.value for s in self.systems])
+        h = C.c_void_p()
+        check(lib().xt_batch_create(len(self.systems), arr, workers, C.byref(h)), "xt_batch_create")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().xt_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def solve(self, rhs, sols=None, im=30, tol=1e-8, maxits=2000, precision=0, inner_tol=1e-5):
+        """rhs: list of host vectors; returns (solutions, stats list, status
+        array).  Raises when any system failed."""
+        n = len(self.systems)
+        rhs = [_f64(r) for r in rhs]
+        out = [np.zeros(s.p * s.q) if sols is None else _f64(sols[i]).copy()
+               for i, s in enumerate(self.systems)]
+        rp = (_dp * n)(*[dptr(r) for r in rhs])
+        sp = (_dp * n)(*[dptr(o) for o in out])
+        st = np.zeros(6 * n)
+        status = np.zeros(n, np.int32)
+        check(lib().xt_batch_solve(self._h, rp, sp, im, tol, maxits, precision, inner_tol,
+                                   dptr(st), iptr(status)), "xt_batch_solve")
+        keys = ["its", "cycles", "outer", "ierr", "relres", "est"]
+        stats = [{k: (int(v) if k in ("its", "cycles", "outer", "ierr") else float(v))
+                  for k, v in zip(keys, st[6 * i:6 * i + 6])} for i in range(n)]
+        return out, stats, status
 
 
 class Problem:

@@ -4,11 +4,16 @@
 // (src/kronecker.f90, src/delelement.f90, src/kokkos_host.cpp) argument for
 // argument; host arrays in the reference's block layout are converted to the
 // device's interleaved layout on the way in and back on the way out.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
+#include <string>
+#include <thread>
 #include <tuple>
+#include <vector>
 
 #include "../../include/xtfem_gb300.h"
 #include "solver.h"
@@ -303,8 +308,9 @@ int xt_system_gmres(xt_system h, const double* rhs, double* sol, int im, double 
     return XT_OK;
 }
 
-int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double tol, int maxits,
-                    int precision, double inner_tol, double* out_stats)
+// xt_system_solve's body, shared with the batch workers.
+static int system_solve_host(xt_system h, const double* rhs, double* sol, int im, double tol,
+                             int maxits, int precision, double inner_tol, double* out_stats)
 {
     if (!h || !rhs || !sol) { set_error("xt_system_solve: null argument"); return XT_ERR_ARG; }
     if (precision < 0 || precision > 2) { set_error("xt_system_solve: precision is 0, 1 or 2"); return XT_ERR_ARG; }
@@ -328,6 +334,84 @@ int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double 
     }
     return XT_OK;
 }
+
+int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double tol, int maxits,
+                    int precision, double inner_tol, double* out_stats)
+{
+    return system_solve_host(h, rhs, sol, im, tol, maxits, precision, inner_tol, out_stats);
+}
+
+// ------------------------------------------------------------- batches
+struct xt_batch_s {
+    std::vector<xt_system> sys;
+    std::vector<int> order;  // largest system first
+    int workers = 1;
+};
+
+int xt_batch_create(int count, const xt_system* systems, int workers, xt_batch* out)
+{
+    if (!out || count <= 0 || !systems) { set_error("xt_batch_create: bad arguments"); return XT_ERR_ARG; }
+    *out = nullptr;
+    for (int i = 0; i < count; ++i)
+        if (!systems[i]) { set_error("xt_batch_create: null system"); return XT_ERR_ARG; }
+    XT_TRY(ensure_init());
+    auto b = std::make_unique<xt_batch_s>();
+    b->sys.assign(systems, systems + count);
+    b->order.resize(count);
+    for (int i = 0; i < count; ++i) b->order[i] = i;
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int x, int y) {
+        return (long long)b->sys[x]->sys.p * b->sys[x]->sys.q > (long long)b->sys[y]->sys.p * b->sys[y]->sys.q;
+    });
+    b->workers = std::max(1, std::min(count, workers > 0 ? workers : 16));
+    *out = b.release();
+    return XT_OK;
+}
+
+int xt_batch_destroy(xt_batch b)
+{
+    delete b;
+    return XT_OK;
+}
+
+int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
+                   int maxits, int precision, double inner_tol, double* stats, int* status)
+{
+    if (!b || !rhs || !sol) { set_error("xt_batch_solve: null argument"); return XT_ERR_ARG; }
+    const int count = (int)b->sys.size();
+    for (int i = 0; i < count; ++i)
+        if (!rhs[i] || !sol[i]) { set_error("xt_batch_solve: null vector"); return XT_ERR_ARG; }
+    std::vector<int> code(count, XT_OK);
+    std::vector<std::string> msg(count);
+    std::atomic<int> next{0};
+    const int device = ctx().device;
+    auto work = [&] {
+        if (cudaSetDevice(device) != cudaSuccess) return;
+        for (int k; (k = next.fetch_add(1)) < count;) {
+            const int i = b->order[k];
+            code[i] = system_solve_host(b->sys[i], rhs[i], sol[i], im, tol, maxits, precision,
+                                        inner_tol, stats ? stats + (size_t)6 * i : nullptr);
+            if (code[i] != XT_OK) msg[i] = last_error();
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < b->workers; ++w) pool.emplace_back(work);
+    work();
+    for (auto& t : pool) t.join();
+    if (next.load() < count) {  // a worker could not select the device
+        set_error("xt_batch_solve: worker thread could not select the device");
+        return XT_ERR_CUDA;
+    }
+    int rc = XT_OK;
+    for (int i = 0; i < count; ++i) {
+        if (status) status[i] = code[i];
+        if (code[i] != XT_OK && rc == XT_OK) {
+            rc = code[i];
+            set_error("xt_batch_solve: system " + std::to_string(i) + ": " + msg[i]);
+        }
+    }
+    return rc;
+}
+
 
 // ------------------------------------------------- Fortran entry points
 void kronspmv_(const double* a, const double* b, const int* q, const int* ki, const int* kj,
