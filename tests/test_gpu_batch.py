@@ -82,3 +82,20 @@ def test_batch_reports_the_failing_system(xt, cases):
         batch.solve([cases[0]["rhs"], c["rhs"], cases[3]["rhs"]], im=30, tol=1e-8, precision=2)
     batch.close()
     bare.close()
+
+
+def test_batch_restart_tuner(xt, cases):
+    """im=0 tunes the restart length once (one batch solve per candidate)
+    and later calls reuse it; the tuned solve reaches the tolerance."""
+    batch = xt.SystemBatch([c["sys"] for c in cases])
+    assert batch.restart == 0
+    sols, stats, _ = batch.solve([c["rhs"] for c in cases], im=0, tol=1e-8, precision=2)
+    im = batch.restart
+    assert im in (30, 60, 120, 200)
+    assert all(st["relres"] <= 1e-8 for st in stats)
+    again, _, _ = batch.solve([c["rhs"] for c in cases], im=0, tol=1e-8, precision=2)
+    assert batch.restart == im
+    fixed, _, _ = batch.solve([c["rhs"] for c in cases], im=im, tol=1e-8, precision=2)
+    batch.close()
+    for a, b, c in zip(sols, again, fixed):
+        assert np.array_equal(a, b) and np.array_equal(a, c)

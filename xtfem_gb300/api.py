@@ -305,9 +305,15 @@ class SystemBatch:
 
     __del__ = close
 
+    @property
+    def restart(self) -> int:
+        """The restart length picked by the tuner (0 before a solve with im=0)."""
+        return lib().xt_batch_restart(self._h)
+
     def solve(self, rhs, sols=None, im=30, tol=1e-8, maxits=2000, precision=0, inner_tol=1e-5):
         """rhs: list of host vectors; returns (solutions, stats list, status
-        array).  Raises when any system failed."""
+        array).  im=0 uses the tuned restart length (tuned on first use).
+        Raises when any system failed."""
         n = len(self.systems)
         rhs = [_f64(r) for r in rhs]
         out = [np.zeros(s.p * s.q) if sols is None else _f64(sols[i]).copy()

@@ -6,6 +6,7 @@
 // device's interleaved layout on the way in and back on the way out.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -346,6 +347,7 @@ struct xt_batch_s {
     std::vector<xt_system> sys;
     std::vector<int> order;  // largest system first
     int workers = 1;
+    int tuned_im = 0;        // restart length picked by the tuner, 0 before
 };
 
 int xt_batch_create(int count, const xt_system* systems, int workers, xt_batch* out)
@@ -373,6 +375,46 @@ int xt_batch_destroy(xt_batch b)
     return XT_OK;
 }
 
+namespace {
+int batch_run(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
+              int maxits, int precision, double inner_tol, double* stats, int* status);
+
+// Restart-length tuner: each candidate length solves the whole batch from
+// the caller's initial guesses; the fastest (host wall clock, device work
+// included: every solve ends with its download) is kept.
+int batch_tune(xt_batch b, const double* const* rhs, double* const* sol, double tol, int maxits,
+               int precision, double inner_tol)
+{
+    const int count = (int)b->sys.size();
+    long long nmax = 0;
+    for (xt_system h : b->sys) nmax = std::max(nmax, (long long)h->sys.p * h->sys.q);
+    std::vector<std::vector<double>> x0(count);
+    for (int i = 0; i < count; ++i) {
+        const size_t n = (size_t)b->sys[i]->sys.p * b->sys[i]->sys.q;
+        x0[i].assign(sol[i], sol[i] + n);
+    }
+    double best = 0.0;
+    int best_im = 0;
+    for (int cand : {30, 60, 120, 200}) {
+        const int im = (int)std::min<long long>(cand, nmax);
+        if (im == best_im) continue;
+        for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
+        const auto t0 = std::chrono::steady_clock::now();
+        XT_TRY(batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, nullptr, nullptr));
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (best_im == 0 || t < best) {
+            best = t;
+            best_im = im;
+        }
+    }
+    for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
+    b->tuned_im = best_im;
+    return XT_OK;
+}
+}  // namespace
+
+int xt_batch_restart(xt_batch b) { return b ? b->tuned_im : 0; }
+
 int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
                    int maxits, int precision, double inner_tol, double* stats, int* status)
 {
@@ -380,6 +422,18 @@ int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int
     const int count = (int)b->sys.size();
     for (int i = 0; i < count; ++i)
         if (!rhs[i] || !sol[i]) { set_error("xt_batch_solve: null vector"); return XT_ERR_ARG; }
+    if (im <= 0) {
+        if (b->tuned_im == 0) XT_TRY(batch_tune(b, rhs, sol, tol, maxits, precision, inner_tol));
+        im = b->tuned_im;
+    }
+    return batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, stats, status);
+}
+
+namespace {
+int batch_run(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
+              int maxits, int precision, double inner_tol, double* stats, int* status)
+{
+    const int count = (int)b->sys.size();
     std::vector<int> code(count, XT_OK);
     std::vector<std::string> msg(count);
     std::atomic<int> next{0};
@@ -411,6 +465,7 @@ int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int
     }
     return rc;
 }
+}  // namespace
 
 
 // ------------------------------------------------- Fortran entry points
