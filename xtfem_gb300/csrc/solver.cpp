@@ -184,7 +184,10 @@ int ensure_workspace(System& S, int im, bool fp32, bool flex = false)
         S.V32.release();
     }
     if (!fp32) {
-        if (S.V64.n < n * (im + 1)) XT_TRY(S.V64.alloc(n * (size_t)(im + 1)));
+        // columns of an even length: the double-float basis is read two
+        // entries at a time (an odd n gets one zero pad entry per column)
+        const size_t nl = n + (n & 1);
+        if (S.V64.n < nl * (im + 1)) XT_TRY(S.V64.alloc(nl * (size_t)(im + 1)));
         XT_TRY(S.z64.alloc(n));
         XT_TRY(S.w64.alloc(n));
         XT_TRY(S.u64.alloc(n));
@@ -397,9 +400,11 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
 {
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
+    const size_t nl = n + (n & 1);  // basis column stride: even, zero pad when n is odd
     float2* V = reinterpret_cast<float2*>(S.V64.p);  // double-float basis
     float* Z = S.Z32.p;
-    auto col = [&](int j) { return V + (size_t)j * n; };
+    auto col = [&](int j) { return V + (size_t)j * nl; };
+    if (nl != n) XT_CUDA(cudaMemsetAsync(V, 0, (size_t)(im + 1) * nl * sizeof(float2), s));
     auto zc = [&](int j) { return Z + (size_t)j * n; };
     std::vector<double> hh((size_t)(im + 1) * im, 0.0), c(im, 0.0), sn(im, 0.0), rs(im + 1, 0.0);
     std::vector<double> hbuf(2 * (im + 1) + 2);
@@ -442,13 +447,13 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
                 prof_end(tok, s);
             }
             const int otok = prof_begin(PROF_ORTH64, s);
-            XT_TRY(df_multi_dot(V, n, i, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_multi_dot(V, nl, i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
-            XT_TRY(df_update_and_dot(V, n, i, S.hsave.p, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_update_and_dot(V, nl, i, S.hsave.p, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
-            XT_TRY(df_update_and_norm(V, n, i, S.hsave.p + i, col(i1 - 1), n, S.red, s));
+            XT_TRY(df_update_and_norm(V, nl, i, S.hsave.p + i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
             prof_end(otok, s);
