@@ -15,7 +15,11 @@
 // plus the row pointers, and touches X (gathered, L2-resident) and Y once.
 // In FP32 it is HBM-bound; in FP64 the GB300's FP64 pipe (about 1.2 TFLOP/s)
 // binds first because every nonzero carries q FMAs.
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "df.cuh"
 #include "xt_device.h"
@@ -154,6 +158,13 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
     }
 }
 
+// XTFEM_KRON_NB=0 keeps the CSR kernel (tests compare the two).
+bool nb_enabled()
+{
+    const char* e = std::getenv("XTFEM_KRON_NB");
+    return !e || std::atoi(e) != 0;
+}
+
 __global__ void k_to_df(const double* __restrict__ a, float2* __restrict__ b, size_t n)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,6 +272,104 @@ k_kron_df(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
     }
 }
 
+// Node-block double-float apply, Y = K X A^T + M X B^T (even Q): a lane
+// owns (node row a, DOF c, temporal pair qp) and accumulates (KX)[3a+c][2qp..]
+// and (MX)[3a+c][2qp..] over the node row's blocks: per block one column
+// index, row c of K's block, M's scalar and the neighbour's three X pairs.
+// The Q/2 lanes of (a, c) then exchange their sums and each finishes its
+// two outputs with the q x q temporal mixing.  3 Q/2 lanes per node row,
+// 32 / (3 Q/2) node rows per warp.
+template <int Q>
+__global__ void __launch_bounds__(256)
+k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
+          const float2* __restrict__ kv, const float2* __restrict__ mv,
+          const double* __restrict__ dA, const double* __restrict__ dB,
+          const float* __restrict__ x, float2* __restrict__ y)
+{
+    static_assert(Q % 2 == 0 && Q <= 8, "pairs of temporal blocks");
+    constexpr int NP = Q / 2, LPR = 3 * NP, RPW = 32 / LPR;
+    __shared__ float2 sA[Q * Q], sB[Q * Q];
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) {
+        const float ah = __double2float_rn(dA[i]), bh = __double2float_rn(dB[i]);
+        sA[i] = make_float2(ah, __double2float_rn(dA[i] - (double)ah));
+        sB[i] = make_float2(bh, __double2float_rn(dB[i] - (double)bh));
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, slot = lane / LPR, inl = lane - slot * LPR;
+    const int c = inl / NP, qp = inl - c * NP;
+    const bool lane_ok = slot < RPW;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int nwarp = (gridDim.x * blockDim.x) / 32;
+    for (int a0 = gwarp * RPW; a0 < nodes; a0 += nwarp * RPW) {
+        const int a = a0 + slot;
+        const bool act = lane_ok && a < nodes;
+        // (hi, lo) of the lane's two temporal entries, packed: .x entry 2qp,
+        // .y entry 2qp+1
+        float2 kh = make_float2(0.f, 0.f), kl = kh, mh = kh, ml = kh;
+        const int b0 = act ? bptr[a] : 0, b1 = act ? bptr[a + 1] : 0;
+#pragma unroll 4
+        for (int b = b0; b < b1; ++b) {
+            const float* xb = x + (size_t)bcol[b] * (3 * Q) + 2 * qp;
+            const float2* kr = kv + (size_t)b * 9 + c * 3;
+            const float2 k0 = kr[0], k1 = kr[1], k2 = kr[2], m = mv[b];
+            const float2 x0 = *reinterpret_cast<const float2*>(xb);
+            const float2 x1 = *reinterpret_cast<const float2*>(xb + Q);
+            const float2 x2 = *reinterpret_cast<const float2*>(xb + 2 * Q);
+            df2_axpy(kh, kl, k0.x, k0.y, x0);
+            df2_axpy(kh, kl, k1.x, k1.y, x1);
+            df2_axpy(kh, kl, k2.x, k2.y, x2);
+            df2_axpy(mh, ml, m.x, m.y, c == 0 ? x0 : (c == 1 ? x1 : x2));
+        }
+        const float kh0 = kh.x, kl0 = kl.x, kh1 = kh.y, kl1 = kl.y;
+        const float mh0 = mh.x, ml0 = ml.x, mh1 = mh.y, ml1 = ml.y;
+        // all Q temporal entries of row 3a+c, from the NP lanes of (a, c)
+        float KH[Q], KL[Q], MH[Q], ML[Q];
+        const int base = slot * LPR + c * NP;
+#pragma unroll
+        for (int j = 0; j < NP; ++j) {
+            const int src = base + j;
+            KH[2 * j] = __shfl_sync(0xffffffffu, kh0, src);
+            KL[2 * j] = __shfl_sync(0xffffffffu, kl0, src);
+            KH[2 * j + 1] = __shfl_sync(0xffffffffu, kh1, src);
+            KL[2 * j + 1] = __shfl_sync(0xffffffffu, kl1, src);
+            MH[2 * j] = __shfl_sync(0xffffffffu, mh0, src);
+            ML[2 * j] = __shfl_sync(0xffffffffu, ml0, src);
+            MH[2 * j + 1] = __shfl_sync(0xffffffffu, mh1, src);
+            ML[2 * j + 1] = __shfl_sync(0xffffffffu, ml1, src);
+        }
+        if (act) {
+            float2 out[2];
+#pragma unroll
+            for (int t = 0; t < 2; ++t) {
+                const int i = 2 * qp + t;
+                float h = 0.0f, l = 0.0f;
+#pragma unroll
+                for (int j = 0; j < Q; ++j) {
+                    df_mul_acc(h, l, sA[j * Q + i].x, sA[j * Q + i].y, KH[j], KL[j]);
+                    df_mul_acc(h, l, sB[j * Q + i].x, sB[j * Q + i].y, MH[j], ML[j]);
+                }
+                out[t] = df_norm(h, l);
+            }
+            *reinterpret_cast<float4*>(y + (size_t)(3 * a + c) * Q + 2 * qp) =
+                make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
+        }
+    }
+}
+
+template <int Q>
+int launch_nb(const DevNodeBlocks& nb, const double* dA, const double* dB, const float* x,
+              float2* y, cudaStream_t s)
+{
+    constexpr int RPW = 32 / (3 * (Q / 2));
+    const int threads = 256, rows_per_block = (threads / 32) * RPW;
+    const int blocks = std::max(1, (nb.nodes + rows_per_block - 1) / rows_per_block);
+    k_kron_nb<Q><<<blocks, threads, 0, s>>>(nb.nodes, nb.ptr.p, nb.col.p, nb.kdf.p, nb.mdf.p, dA,
+                                            dB, x, y);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
 template <int Q>
 int launch_df(const DevCsr& K, const DevCsr& M, const double* dA, const double* dB,
               const float* x, float2* y, cudaStream_t s)
@@ -345,6 +454,7 @@ int upload_csr(DevCsr& d, int n, const int* ia, const int* ja, const double* a,
     d.nnz = nnz;
     d.same_pattern = false;
     d.vdf.release();  // remade from the new values on first use
+    d.nb.ok = false;  // rebuilt by csr_build_node_blocks
     XT_TRY(d.rowptr.upload(ia, (size_t)n + 1, s));
     XT_TRY(d.col.upload(ja, (size_t)(nnz > 0 ? nnz : 0), s));
     XT_TRY(d.v64.upload(a, (size_t)nnz, s));
@@ -367,6 +477,74 @@ void csr_mark_shared_pattern(const DevCsr& K, DevCsr& M, const int* ki, const in
     if (std::memcmp(ki, mi, sizeof(int) * ((size_t)K.n + 1)) != 0) return;
     if (std::memcmp(kj, mj, sizeof(int) * (size_t)K.nnz) != 0) return;
     M.same_pattern = true;
+}
+
+int csr_build_node_blocks(DevCsr& K, int n, const int* ki, const int* kj, const double* kv,
+                          const int* mi, const int* mj, const double* mv, cudaStream_t s)
+{
+    DevNodeBlocks& nb = K.nb;
+    nb.ok = false;
+    if (n <= 0 || n % 3 != 0 || K.n != n) return XT_OK;
+    const int nodes = n / 3;
+    std::vector<int> ptr(nodes + 1, 0), col;
+    std::vector<float2> kdf, mdf;
+    std::vector<int> pos(nodes, -1);  // block index of neighbour node b in the current row
+    auto split = [](double v) {
+        const float h = (float)v;
+        return make_float2(h, (float)(v - (double)h));
+    };
+    for (int a = 0; a < nodes; ++a) {
+        const int first = (int)col.size();
+        for (int c = 0; c < 3; ++c)
+            for (int k = ki[3 * a + c] - 1; k < ki[3 * a + c + 1] - 1; ++k) {
+                const int b = (kj[k] - 1) / 3;
+                if (pos[b] < 0) {
+                    pos[b] = (int)col.size();
+                    col.push_back(b);
+                    kdf.resize(kdf.size() + 9, make_float2(0.f, 0.f));
+                    mdf.push_back(make_float2(0.f, 0.f));
+                }
+            }
+        // neighbour nodes in ascending order (the CSR columns are sorted)
+        std::vector<int> order(col.begin() + first, col.end());
+        std::sort(order.begin(), order.end());
+        for (size_t t = 0; t < order.size(); ++t) pos[order[t]] = first + (int)t;
+        std::copy(order.begin(), order.end(), col.begin() + first);
+        for (int c = 0; c < 3; ++c)
+            for (int k = ki[3 * a + c] - 1; k < ki[3 * a + c + 1] - 1; ++k) {
+                const int j = kj[k] - 1, b = j / 3;
+                kdf[(size_t)pos[b] * 9 + c * 3 + (j - 3 * b)] = split(kv[k]);
+            }
+        // M: m_ab on the three diagonal entries of each block, nothing else
+        std::vector<double> mval(order.size(), 0.0);
+        std::vector<int> mcount(order.size(), 0);
+        bool fits = true;
+        for (int c = 0; c < 3 && fits; ++c)
+            for (int k = mi[3 * a + c] - 1; k < mi[3 * a + c + 1] - 1; ++k) {
+                const int j = mj[k] - 1, b = j / 3;
+                if (j - 3 * b != c || pos[b] < 0) { fits = false; break; }
+                const int t = pos[b] - first;
+                if (mcount[t] > 0 && mval[t] != mv[k]) { fits = false; break; }
+                mval[t] = mv[k];
+                ++mcount[t];
+            }
+        for (size_t t = 0; t < order.size() && fits; ++t) {
+            if (mcount[t] != 0 && mcount[t] != 3) fits = false;
+            mdf[first + t] = split(mval[t]);
+        }
+        for (int b : order) pos[b] = -1;
+        if (!fits) return XT_OK;  // no exact node-block form: the CSR kernel stays
+        ptr[a + 1] = (int)col.size();
+    }
+    nb.nodes = nodes;
+    nb.nblocks = (int)col.size();
+    XT_TRY(nb.ptr.upload(ptr.data(), ptr.size(), s));
+    XT_TRY(nb.col.upload(col.data(), col.size(), s));
+    XT_TRY(nb.kdf.upload(kdf.data(), kdf.size(), s));
+    XT_TRY(nb.mdf.upload(mdf.data(), mdf.size(), s));
+    XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    nb.ok = true;
+    return XT_OK;
 }
 
 int to_f32(const double* a, float* b, size_t n, cudaStream_t s)
@@ -410,6 +588,16 @@ int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB
         return XT_ERR_ARG;
     }
     if (K.n == 0) return XT_OK;
+    // node blocks: y must be 16-byte aligned (one float4 store per lane)
+    if (K.nb.ok && q % 2 == 0 && reinterpret_cast<uintptr_t>(y) % 16 == 0 &&
+        reinterpret_cast<uintptr_t>(x) % 8 == 0 && nb_enabled()) {
+        switch (q) {
+        case 2: return launch_nb<2>(K.nb, dA, dB, x, y, s);
+        case 4: return launch_nb<4>(K.nb, dA, dB, x, y, s);
+        case 6: return launch_nb<6>(K.nb, dA, dB, x, y, s);
+        default: return launch_nb<8>(K.nb, dA, dB, x, y, s);
+        }
+    }
     XT_TRY(ensure_df(K, s));
     XT_TRY(ensure_df(M, s));
     switch (q) {

@@ -39,6 +39,26 @@ __device__ __forceinline__ void df_mul_acc(float& hi, float& lo, float ah, float
     lo = __fadd_rn(lo, __fadd_rn(e, fmaf(ah, bl, __fmul_rn(al, bh))));
 }
 
+// Two double-float accumulators side by side, (h.x + l.x, h.y + l.y) +=
+// (vh + vl) (x.x, x.y) for FP32 x: the steps of an FP32-input axpy (leading
+// product exact by fma, two-sum of the sum, the low part's products in
+// FP32) on packed two-wide FP32 instructions, each element rounded exactly
+// as the scalar sequence would round it.
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+
+__device__ __forceinline__ void df2_axpy(float2& h, float2& l, float vh, float vl, float2 x)
+{
+    const float2 v = make_float2(vh, vh);
+    const float2 p = __fmul2_rn(v, x);
+    const float2 e = __ffma2_rn(v, x, neg2(p));
+    const float2 s = __fadd2_rn(h, p);
+    const float2 bb = __fadd2_rn(s, neg2(h));
+    const float2 t = __fadd2_rn(__fadd2_rn(h, neg2(__fadd2_rn(s, neg2(bb)))), __fadd2_rn(p, neg2(bb)));
+    h = s;
+    l = __fadd2_rn(l, t);
+    l = __fadd2_rn(l, __ffma2_rn(make_float2(vl, vl), x, e));
+}
+
 // Renormalise (hi, lo) so that hi carries the rounded value.
 __device__ __forceinline__ float2 df_norm(float hi, float lo)
 {

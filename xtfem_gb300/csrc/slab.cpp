@@ -88,6 +88,8 @@ int upload_operator(xt_slab_s& s)
     XT_TRY(upload_csr(s.S.K, K.n, K.ia.data(), K.ja.data(), K.a.data(), st));
     XT_TRY(upload_csr(s.S.M, M.n, M.ia.data(), M.ja.data(), M.a.data(), st));
     csr_mark_shared_pattern(s.S.K, s.S.M, K.ia.data(), K.ja.data(), M.ia.data(), M.ja.data());
+    XT_TRY(csr_build_node_blocks(s.S.K, K.n, K.ia.data(), K.ja.data(), K.a.data(), M.ia.data(),
+                                 M.ja.data(), M.a.data(), st));
     XT_TRY(s.S.bcmask.upload(s.bc.data(), s.bc.size(), st));
     XT_CUDA(cudaStreamSynchronize(st));
     return XT_OK;

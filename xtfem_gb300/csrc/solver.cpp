@@ -122,6 +122,7 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
     XT_TRY(upload_csr(S.K, p, ki, kj, kv, s));
     XT_TRY(upload_csr(S.M, p, mi, mj, mv, s));
     csr_mark_shared_pattern(S.K, S.M, ki, kj, mi, mj);
+    XT_TRY(csr_build_node_blocks(S.K, p, ki, kj, kv, mi, mj, mv, s));
     XT_TRY(S.A.alloc(64));
     XT_TRY(S.B.alloc(64));
     XT_TRY(S.Ainv.alloc(64));

@@ -82,6 +82,19 @@ struct DBuf {
 
 // ------------------------------------------------------ sparse operators
 // 0-based CSR on the device with FP64 values and an FP32 copy.
+// Node-block form of a three-DOF-per-node pair (K, M): for every node row
+// the neighbour nodes, K's 3 x 3 block (zeros where the CSR has no entry)
+// and M's one scalar per block when M = m_ab I3 blockwise (a consistent
+// mass matrix).  One column index and one contiguous gather of the
+// neighbour's 3 x q slice of X serve nine K values and one M value.
+struct DevNodeBlocks {
+    bool ok = false;
+    int nodes = 0, nblocks = 0;
+    DBuf<int> ptr, col;    // nodes + 1 block pointers, neighbour node per block
+    DBuf<float2> kdf;      // 9 per block, row-major, double-float
+    DBuf<float2> mdf;      // 1 per block, double-float
+};
+
 struct DevCsr {
     int n = 0, nnz = 0;
     DBuf<int> rowptr, col;
@@ -91,7 +104,14 @@ struct DevCsr {
     // set on M when its pattern equals K's (same mesh): the Kronecker
     // kernels then read one column index and one X row per nonzero for both
     bool same_pattern = false;
+    DevNodeBlocks nb;  // on K: node-block form of (K, M), when it exists
 };
+
+// Builds K.nb from the 1-based host CSR pairs after both were uploaded;
+// leaves K.nb.ok false when the pair has no exact node-block form (order
+// not a multiple of 3, M not m_ab I3 blockwise, or M outside K's blocks).
+int csr_build_node_blocks(DevCsr& K, int n, const int* ki, const int* kj, const double* kv,
+                          const int* mi, const int* mj, const double* mv, cudaStream_t s);
 
 // Marks M as sharing K's sparsity pattern when the 1-based host arrays are
 // identical (both matrices of one mesh), after both were uploaded.
