@@ -1247,6 +1247,25 @@ struct ColBody {
             if (c >= nchunk) break;  // warp-uniform
             const int2 cd = chunks[c];
             const float4* rp = reinterpret_cast<const float4*>(base + (size_t)cd.x * 16) + lane;
+            // the finishing lane's group record and right-hand side, loaded
+            // before the gathers so their latency overlaps them
+            const int jj = c * GPW + gw;
+            const bool fin = lane_ok && hh == 0 && jj < ng;
+            int gslot = 0, gdst = 0;
+            float mv[3] = {0.0f, 0.0f, 0.0f};
+            float2 bb[3] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};
+            if (fin) {
+                const int* gr = reinterpret_cast<const int*>(grec + (size_t)jj * kCgrec);
+                gslot = gr[0];
+                gdst = gr[1];
+                const float* m = reinterpret_cast<const float*>(gr + 3) + col * 3;
+                const float* rr = rh + (size_t)gr[2] * rsE + 2 * pr;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    mv[r] = m[r];
+                    bb[r] = *reinterpret_cast<const float2*>(rr + r * Q);
+                }
+            }
             float2 acc[3];
 #pragma unroll
             for (int r = 0; r < 3; ++r) acc[r] = make_float2(0.0f, 0.0f);
@@ -1276,17 +1295,11 @@ struct ColBody {
                                               __shfl_sync(0xffffffffu, acc[r].y, lane0 + 2 * H));
                 tot[r] = make_float2((t0.x + t1.x) + t2.x, (t0.y + t1.y) + t2.y);
             }
-            const int jj = c * GPW + gw;
-            if (lane_ok && hh == 0 && jj < ng) {
-                const int* gr = reinterpret_cast<const int*>(grec + (size_t)jj * kCgrec);
-                const int gslot = gr[0], gdst = gr[1], ridx = gr[2];
-                const float* mv = reinterpret_cast<const float*>(gr + 3) + col * 3;
-                const float* rr = rh + (size_t)ridx * rsE + 2 * pr;
+            if (fin) {
                 float2 sol = make_float2(0.0f, 0.0f);
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
-                    const float2 bb = *reinterpret_cast<const float2*>(rr + r * Q);
-                    const float2 d = make_float2(bb.x - tot[r].x, bb.y - tot[r].y);
+                    const float2 d = make_float2(bb[r].x - tot[r].x, bb[r].y - tot[r].y);
                     sol = __ffma2_rn(make_float2(mv[r], mv[r]), d, sol);
                 }
                 *reinterpret_cast<float2*>(win + gslot + 2 * col) = sol;
