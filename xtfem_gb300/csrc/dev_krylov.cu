@@ -115,7 +115,7 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
 // every operation runs on the FP32 pipe.
 
 // partial[(j0+c) nb + b] = (hi, lo) of sum over block b's rows of V_j w
-__global__ void k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,
+__global__ void __launch_bounds__(256, 6) k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,
                                const float4* __restrict__ w, size_t n2,
                                double* __restrict__ partial)
 {
