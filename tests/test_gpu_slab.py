@@ -107,3 +107,25 @@ def test_concurrent_specimens_match_separate_runs(xt):
         assert both[k][0] == alone[k][0]
         for key in ["disp", "D", "ws", "elesta"]:
             assert np.array_equal(both[k][1][key], alone[k][1][key]), (k, key)
+
+
+def test_mixed_precision_deletes_the_fp64_set(xt, sequential):
+    """The deleted-element set of the mixed-precision loop (FP32 ILU,
+    double-float basis) equals the plain FP64 loop's, slab by slab, and
+    the damage agrees to 1e-6."""
+    seq_stats, seq_states, _ = sequential
+    pr = rod_problem(xt)
+    cfg = xt.SlabConfig.make(amplitude=1000.0, nipc=32, n1=10, n2=2, im=30, precision=0,
+                             tol=1e-8, Dc=0.02, overlap=0)
+    s = xt.SlabSolver(pr, cfg)
+    s.set_state(ws=np.full(s.ngp, 31.7))
+    scale = max(np.max(np.abs(st["disp"])) for st in seq_states)  # loaded rod, before failure
+    for k in range(NSLAB):
+        st = s.step()
+        ref = s.state()
+        assert st["deleted"] == seq_stats[k]["deleted"], k
+        assert np.array_equal(ref["elesta"], seq_states[k]["elesta"]), k
+        assert np.max(np.abs(ref["D"] - seq_states[k]["D"])) <= 1e-6, k
+        assert np.max(np.abs(ref["disp"] - seq_states[k]["disp"])) <= 1e-6 * scale, k
+    s.close()
+    pr.close()
