@@ -198,6 +198,32 @@ int xt_system_solve(xt_system s, const double *rhs, double *sol, int im,
                     double tol, int maxits, int precision, double inner_tol,
                     double *out_stats);
 
+/* Device reassembly of the system's stiffness K from per-Gauss-point
+ * moduli: the element loop of mpiglbmtx_m (src/mpisubs.f90:69-139, with
+ * setsdstiff and elemtx_m per Gauss point), which a coupled run calls every
+ * slab after material_update (src/thermoelastic.f90:1-46), merged into the
+ * system's fixed CSR pattern instead of through tricsr
+ * (src/spmtx.f90:359-407).  No counterpart as an entry point in the
+ * reference, which assembles on the host.  xt_system_set_mesh gives the
+ * C3D8 mesh (xyz: nn x 3; conn: ne x 8, 1-based, the reference's node
+ * order) and the constrained DOFs (bc: 3 nn entries, 1 = constrained, with
+ * csrapplybc semantics: row and column zero, diagonal 1).  K then takes the
+ * mesh's full element pattern (every DOF pair of a shared element, explicit
+ * zeros kept, so that any moduli fit it) with its current values carried
+ * over; it fails when K has an entry outside that pattern.
+ * xt_system_assemble_k recomputes K's values from ym and nu (ne x 8; Gauss
+ * point l of element e at 8 e + l, the 2x2x2 rule's order with xi
+ * outermost) on the device.  The ILU factor is not touched: a caller that
+ * wants one for the new K downloads it (xt_system_get_k), refactors on the
+ * host and sets it. */
+int xt_system_set_mesh(xt_system s, int nn, int ne, const double *xyz, const int *conn,
+                       const int *bc);
+int xt_system_assemble_k(xt_system s, const double *ym, const double *nu);
+/* K's current number of entries, and K itself as 1-based CSR (ia: p + 1,
+ * ja and kv: nnz entries; any of the three may be NULL). */
+int xt_system_k_nnz(xt_system s);
+int xt_system_get_k(xt_system s, int *ia, int *ja, double *kv);
+
 /* ------------------------------------------------ batches of systems */
 
 /* A batch of independent systems (load cases or specimens of uneven

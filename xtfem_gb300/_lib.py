@@ -49,6 +49,10 @@ SIGNATURES = {
                                   _dp, C.c_int]),
     "xt_system_solve": (C.c_int, [_vp, _dp, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
                                   C.c_double, _dp]),
+    "xt_system_set_mesh": (C.c_int, [_vp, C.c_int, C.c_int, _dp, _ip, _ip]),
+    "xt_system_assemble_k": (C.c_int, [_vp, _dp, _dp]),
+    "xt_system_k_nnz": (C.c_int, [_vp]),
+    "xt_system_get_k": (C.c_int, [_vp, _ip, _ip, _dp]),
     "xt_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     "xt_batch_destroy": (C.c_int, [_vp]),
     "xt_batch_restart": (C.c_int, [_vp]),

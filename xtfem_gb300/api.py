@@ -261,6 +261,26 @@ class SpaceTimeSystem:
                                     dptr(_f64(x)), dptr(out)), "apply")
         return out
 
+    def set_mesh(self, xyz, conn, bc):
+        """C3D8 mesh (nn x 3, ne x 8 1-based) and constrained DOFs of K, for
+        device reassembly."""
+        self._mesh = (_f64(xyz).reshape(-1), _i32(conn).reshape(-1), _i32(bc))
+        nn, ne = self._mesh[0].size // 3, self._mesh[1].size // 8
+        check(lib().xt_system_set_mesh(self._h, nn, ne, dptr(self._mesh[0]), iptr(self._mesh[1]),
+                                       iptr(self._mesh[2])), "set_mesh")
+
+    def assemble_k(self, ym, nu):
+        """Recompute K on the device from Gauss-point moduli (ne x 8 each)."""
+        check(lib().xt_system_assemble_k(self._h, dptr(_f64(ym).reshape(-1)),
+                                         dptr(_f64(nu).reshape(-1))), "assemble_k")
+
+    def get_k(self) -> Csr:
+        """K as it is on the device now (1-based CSR)."""
+        nnz = lib().xt_system_k_nnz(self._h)
+        ia, ja, a = np.zeros(self.p + 1, np.int32), np.zeros(nnz, np.int32), np.zeros(nnz)
+        check(lib().xt_system_get_k(self._h, iptr(ia), iptr(ja), dptr(a)), "get_k")
+        return Csr(ia, ja, a)
+
     def lusol(self, a, x, fp32=False):
         y = np.zeros(self.p * self.q)
         fn = lib().xt_system_lusol_f32 if fp32 else lib().xt_system_lusol

@@ -11,6 +11,7 @@
 #include <cstring>
 #include <map>
 #include <memory>
+#include <new>
 #include <string>
 #include <thread>
 #include <tuple>
@@ -340,6 +341,43 @@ int xt_system_solve(xt_system h, const double* rhs, double* sol, int im, double 
                     int precision, double inner_tol, double* out_stats)
 {
     return system_solve_host(h, rhs, sol, im, tol, maxits, precision, inner_tol, out_stats);
+}
+
+int xt_system_set_mesh(xt_system h, int nn, int ne, const double* xyz, const int* conn,
+                       const int* bc)
+{
+    if (!h || !xyz || !conn || !bc) { set_error("xt_system_set_mesh: null argument"); return XT_ERR_ARG; }
+    XT_TRY(system_stream(h->sys));
+    try {
+        return system_set_mesh(h->sys, nn, ne, xyz, conn, bc);
+    } catch (const std::bad_alloc&) {
+        set_error("xt_system_set_mesh: out of host memory");
+        return XT_ERR_ALLOC;
+    }
+}
+
+int xt_system_assemble_k(xt_system h, const double* ym, const double* nu)
+{
+    if (!h || !ym || !nu) { set_error("xt_system_assemble_k: null argument"); return XT_ERR_ARG; }
+    return system_assemble_k(h->sys, ym, nu);
+}
+
+int xt_system_k_nnz(xt_system h) { return h ? h->sys.K.nnz : 0; }
+
+int xt_system_get_k(xt_system h, int* ia, int* ja, double* kv)
+{
+    if (!h) { set_error("xt_system_get_k: null argument"); return XT_ERR_ARG; }
+    System& S = h->sys;
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
+    const size_t nnz = (size_t)S.K.nnz;
+    if (ia) XT_CUDA(cudaMemcpyAsync(ia, S.K.rowptr.p, sizeof(int) * ((size_t)S.p + 1), cudaMemcpyDeviceToHost, s));
+    if (ja) XT_CUDA(cudaMemcpyAsync(ja, S.K.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost, s));
+    if (kv) XT_CUDA(cudaMemcpyAsync(kv, S.K.v64.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    if (ia) for (int r = 0; r <= S.p; ++r) ++ia[r];  // the device keeps 0-based indices
+    if (ja) for (size_t k = 0; k < nnz; ++k) ++ja[k];
+    return XT_OK;
 }
 
 // ------------------------------------------------------------- batches

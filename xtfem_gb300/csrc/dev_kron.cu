@@ -165,6 +165,17 @@ bool nb_enabled()
     return !e || std::atoi(e) != 0;
 }
 
+// b[at[i]] = double-float of a[i]
+__global__ void k_scatter_df(const double* __restrict__ a, const int* __restrict__ at,
+                             float2* __restrict__ b, size_t n)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const float h = __double2float_rn(a[i]);
+        b[at[i]] = make_float2(h, __double2float_rn(a[i] - (double)h));
+    }
+}
+
 __global__ void k_to_df(const double* __restrict__ a, float2* __restrict__ b, size_t n)
 {
     size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -489,6 +500,7 @@ int csr_build_node_blocks(DevCsr& K, int n, const int* ki, const int* kj, const 
     std::vector<int> ptr(nodes + 1, 0), col;
     std::vector<float2> kdf, mdf;
     std::vector<int> pos(nodes, -1);  // block index of neighbour node b in the current row
+    std::vector<int> from_csr((size_t)K.nnz, -1);
     auto split = [](double v) {
         const float h = (float)v;
         return make_float2(h, (float)(v - (double)h));
@@ -513,7 +525,9 @@ int csr_build_node_blocks(DevCsr& K, int n, const int* ki, const int* kj, const 
         for (int c = 0; c < 3; ++c)
             for (int k = ki[3 * a + c] - 1; k < ki[3 * a + c + 1] - 1; ++k) {
                 const int j = kj[k] - 1, b = j / 3;
-                kdf[(size_t)pos[b] * 9 + c * 3 + (j - 3 * b)] = split(kv[k]);
+                const size_t at = (size_t)pos[b] * 9 + c * 3 + (j - 3 * b);
+                kdf[at] = split(kv[k]);
+                from_csr[k] = (int)at;
             }
         // M: m_ab on the three diagonal entries of each block, nothing else
         std::vector<double> mval(order.size(), 0.0);
@@ -542,8 +556,19 @@ int csr_build_node_blocks(DevCsr& K, int n, const int* ki, const int* kj, const 
     XT_TRY(nb.col.upload(col.data(), col.size(), s));
     XT_TRY(nb.kdf.upload(kdf.data(), kdf.size(), s));
     XT_TRY(nb.mdf.upload(mdf.data(), mdf.size(), s));
+    XT_TRY(nb.from_csr.upload(from_csr.data(), from_csr.size(), s));
     XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     nb.ok = true;
+    return XT_OK;
+}
+
+int node_blocks_refresh(DevCsr& K, cudaStream_t s)
+{
+    if (!K.nb.ok || K.nnz == 0) return XT_OK;
+    k_scatter_df<<<std::max(1, std::min(4096, (K.nnz + 255) / 256)), 256, 0, s>>>(
+        K.v64.p, K.nb.from_csr.p, K.nb.kdf.p, (size_t)K.nnz);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
     return XT_OK;
 }
 

@@ -46,6 +46,7 @@ struct System {
     DBuf<double> x64, r64, b64, t64;
     DBuf<double> hsave;
     Reduce red;
+    DevAssembly asmb;  // device reassembly of K, when a mesh was set
 };
 
 // Creates the system's stream if it has none yet.
@@ -56,6 +57,10 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
                   const int* mi, const int* mj, const double* mv);
 int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group);
 int system_set_temporal(System& S, const double* A, const double* B);
+// Device reassembly of K from per-Gauss-point moduli (dev_assembly.cu):
+// the mesh and constrained DOFs once, then any number of reassemblies.
+int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* conn, const int* bc);
+int system_assemble_k(System& S, const double* ym, const double* nu);
 
 // q x q inverse by LU with partial pivoting (host); returns XT_ERR_SINGULAR.
 int invert_small(int n, const double* A, double* Ainv);

@@ -93,6 +93,20 @@ struct DevNodeBlocks {
     DBuf<int> ptr, col;    // nodes + 1 block pointers, neighbour node per block
     DBuf<float2> kdf;      // 9 per block, row-major, double-float
     DBuf<float2> mdf;      // 1 per block, double-float
+    DBuf<int> from_csr;    // K's nnz entries: position of each in kdf
+};
+
+
+// Mesh data and maps of the device reassembly of K (dev_assembly.cu).
+struct DevAssembly {
+    bool ok = false;
+    int nn = 0, ne = 0;
+    DBuf<double> xyz;            // nn x 3
+    DBuf<int> conn;              // ne x 8, 0-based nodes
+    DBuf<int> cptr, cidx;        // per K entry: its element-matrix entries
+    DBuf<unsigned char> bcdiag;  // per K entry: diagonal of a constrained DOF
+    DBuf<double> ke;             // ne x 576 element matrices
+    DBuf<double> ym, nu;         // ne x 8 Gauss-point moduli
 };
 
 struct DevCsr {
@@ -106,6 +120,10 @@ struct DevCsr {
     bool same_pattern = false;
     DevNodeBlocks nb;  // on K: node-block form of (K, M), when it exists
 };
+
+// Refreshes K.nb's K values from K's CSR values (after a reassembly on
+// the device); no-op when K has no node-block form.
+int node_blocks_refresh(DevCsr& K, cudaStream_t s);
 
 // Builds K.nb from the 1-based host CSR pairs after both were uploaded;
 // leaves K.nb.ok false when the pair has no exact node-block form (order
