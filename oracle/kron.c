@@ -46,7 +46,7 @@ void orc_kronspmv(const double *a, const double *b, int q,
                   int p, const double *x, double *y)
 {
     const size_t n = (size_t)p * q;
-    double *u = (double *)malloc(n * sizeof(double));
+    double *u = (double *)calloc(n, sizeof(double));
     memset(y, 0, n * sizeof(double));
     for (int i = 0; i < q; ++i)
         orc_amux(p, x + (size_t)i * p, u + (size_t)i * p, kv, kj, ki);
