@@ -132,6 +132,52 @@ int xt_slab_drain(xt_slab s, double *stats);
 int xt_slab_set_state(xt_slab s, const double *D, const double *ws);
 /* Copies of the current state (waits for a running damage update). */
 int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
+/* ------------------------------------------------ thermal slab loop */
+
+/* The temperature part of the reference's slab loop (src/main3d.f90:
+ * 429-476 set-up, 586-608 initial and boundary terms, 697-734 per slab)
+ * for a run without the mechanical coupling: q = 3 temporal nodes,
+ * conductivity and capacity of the mesh (elemtx_t, src/elesubs.f90:60-116),
+ * fixed temperature T0 on the faces x[fixed_axis] == fixed_value[0] or
+ * fixed_value[1], heat flux q0 on the faces x[flux_axis] == flux_value[0]
+ * or flux_value[1] (the total q0 * area shared by the element-node
+ * incidences of the first face, as the reference counts them), initial
+ * temperature Tref, GMRES with the ILUT factor of the conductivity (the
+ * reference's MPI route uses an exact MUMPS factor instead). */
+typedef struct xt_thermal_config {
+    int fixed_axis;
+    double fixed_value[2];
+    double T0;           /* fixed temperature */
+    double Tref;         /* initial temperature */
+    int flux_axis;
+    double flux_value[2];
+    double q0;           /* heat flux per unit area */
+    double area;         /* area the total flux is referred to */
+    double kappa;        /* conductivity */
+    double rho;          /* density */
+    double cp;           /* specific heat */
+    double dt0;          /* slab length dt0 * n1 */
+    int n1;
+    int lfil;            /* ILUT fill */
+    double droptol;      /* ILUT drop tolerance */
+    int im;              /* GMRES restart length */
+    double tol;          /* true relative residual target */
+    int maxits;
+    int precision;       /* as in xt_system_solve */
+    double inner_tol;
+} xt_thermal_config;
+
+typedef struct xt_thermal_s *xt_thermal;
+
+int xt_thermal_create(xth_problem pr, const xt_thermal_config *cfg, xt_thermal *out);
+int xt_thermal_destroy(xt_thermal t);
+/* One slab; stats (may be NULL) receives 6 values: slab index, GMRES
+ * iterations, restart cycles, refinement passes, ierr, true relative
+ * residual. */
+int xt_thermal_step(xt_thermal t, double *stats);
+/* The slab's nodal temperatures, block layout (3 temporal blocks of nn). */
+int xt_thermal_get(xt_thermal t, double *temp);
+
 /* Per-kernel CUDA-event timing on the library stream: enable, then read
  * count and total milliseconds per kernel class (0 Kronecker FP64,
  * 1 Kronecker FP32, 2 ILU FP64, 3 ILU FP32, 4 damage, 5 Gram-Schmidt

@@ -26,7 +26,7 @@ from ._lib import XtError, _dp, check, dptr, dref, iptr, iref, lib
 __all__ = [
     "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "chkelesta", "kokkos_host",
     "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "nt_table", "SpaceTimeSystem",
-    "SystemBatch",
+    "SystemBatch", "ThermalConfig", "ThermalSolver",
     "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
 ]
 
@@ -440,6 +440,57 @@ class SlabConfig(C.Structure):
 
     def as_dict(self):
         return {f[0]: getattr(self, f[0]) for f in self._fields_}
+
+
+class ThermalConfig(C.Structure):
+    """xt_thermal_config of include/xtfem_gb300_host.h."""
+
+    _fields_ = [("fixed_axis", C.c_int), ("fixed_value", C.c_double * 2), ("T0", C.c_double),
+                ("Tref", C.c_double), ("flux_axis", C.c_int), ("flux_value", C.c_double * 2),
+                ("q0", C.c_double), ("area", C.c_double), ("kappa", C.c_double),
+                ("rho", C.c_double), ("cp", C.c_double), ("dt0", C.c_double), ("n1", C.c_int),
+                ("lfil", C.c_int), ("droptol", C.c_double), ("im", C.c_int), ("tol", C.c_double),
+                ("maxits", C.c_int), ("precision", C.c_int), ("inner_tol", C.c_double)]
+
+    @classmethod
+    def make(cls, **kw):
+        d = dict(fixed_axis=0, fixed_value=(0.0, 3.0), T0=20.0, Tref=20.0, flux_axis=1,
+                 flux_value=(0.0, 1.0), q0=1.0, area=1.0, kappa=45.0, rho=7.8e-9, cp=4.6e8,
+                 dt0=0.5, n1=1, lfil=20, droptol=1e-4, im=30, tol=1e-8, maxits=3000,
+                 precision=0, inner_tol=1e-5)
+        d.update(kw)
+        d["fixed_value"] = (C.c_double * 2)(*d["fixed_value"])
+        d["flux_value"] = (C.c_double * 2)(*d["flux_value"])
+        return cls(**d)
+
+
+class ThermalSolver:
+    """The thermal slab loop (xt_thermal_*) of a problem's mesh."""
+
+    def __init__(self, problem: "Problem", cfg: ThermalConfig):
+        self.cfg = cfg
+        self.nn = problem.sizes()[0]
+        h = C.c_void_p()
+        check(lib().xt_thermal_create(problem._h, C.byref(cfg), C.byref(h)), "xt_thermal_create")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            lib().xt_thermal_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def step(self):
+        st = np.zeros(6)
+        check(lib().xt_thermal_step(self._h, dptr(st)), "xt_thermal_step")
+        keys = ["slab", "its", "cycles", "outer", "ierr", "relres"]
+        return {k: (float(v) if k == "relres" else int(v)) for k, v in zip(keys, st)}
+
+    def temperature(self):
+        out = np.zeros(3 * self.nn)
+        check(lib().xt_thermal_get(self._h, dptr(out)), "xt_thermal_get")
+        return out
 
 
 STAT_KEYS = ["slab", "its", "cycles", "outer", "ierr", "relres", "maxD", "nfailed", "deleted",

@@ -268,4 +268,38 @@ MechSystem assemble_mech(const Mesh& mesh, double E, double nu, double rho)
     return S;
 }
 
+ThermSystem assemble_therm(const Mesh& mesh, double kappa, double rho, double cp)
+{
+    ThermSystem S;
+    Triplets tk, tm;
+    const size_t per = 64;
+    tk.i.resize(per * mesh.ne); tk.j.resize(per * mesh.ne); tk.v.resize(per * mesh.ne);
+    tm.i.resize(per * mesh.ne); tm.j.resize(per * mesh.ne); tm.v.resize(per * mesh.ne);
+    for (int e = 0; e < mesh.ne; ++e) {
+        double xe[8][3], ke[64] = {0}, me[64] = {0};
+        element_coords(mesh, e, xe);
+        for (int l = 0; l < 8; ++l) {
+            const GaussGeom G = gauss_geom(xe, l);
+            for (int i = 0; i < 8; ++i)
+                for (int j = 0; j < 8; ++j) {
+                    me[i * 8 + j] += rho * cp * G.N[i] * G.N[j] * G.jacdet;
+                    for (int m = 0; m < 3; ++m)
+                        ke[i * 8 + j] += kappa * G.dNdx[i][m] * G.dNdx[j][m] * G.jacdet;
+                }
+        }
+        const size_t base = per * e;
+        for (int r = 0; r < 8; ++r)
+            for (int c = 0; c < 8; ++c) {
+                const size_t k = base + r * 8 + c;
+                tk.i[k] = tm.i[k] = mesh.conn[(size_t)e * 8 + r];
+                tk.j[k] = tm.j[k] = mesh.conn[(size_t)e * 8 + c];
+                tk.v[k] = ke[r * 8 + c];
+                tm.v[k] = me[r * 8 + c];
+            }
+    }
+    S.K = tricsr(tk, mesh.nn);
+    S.M = tricsr(tm, mesh.nn);
+    return S;
+}
+
 }  // namespace xt

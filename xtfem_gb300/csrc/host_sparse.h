@@ -73,6 +73,14 @@ struct MechSystem {
 };
 MechSystem assemble_mech(const Mesh& mesh, double E, double nu, double rho);
 
+// Thermal set-up (src/mpisubs.f90 mpiglbmtx_t with elemtx_t,
+// src/elesubs.f90:60-116): conductivity K (kappa grad N . grad N) and
+// capacity M (rho cp N N), one DOF per node, 2x2x2 Gauss rule.
+struct ThermSystem {
+    Csr K, M;
+};
+ThermSystem assemble_therm(const Mesh& mesh, double kappa, double rho, double cp);
+
 // Element stiffness (24x24, row-major) of src/elesubs.f90:207-251 for a
 // given constitutive matrix (36, column-major).
 void element_stiffness(const Mesh& mesh, int elem, const double* stiff,
@@ -96,6 +104,8 @@ void stcoeff_t(double dt, double* k, double* m, double* ktn, double* mtn,
                double* ktn1, double* mtn1);
 // src/getfextc.f90:22-58.
 void getfextc_m(double t1, double w, double dt, double* fextc, double* fint);
+// src/getfextc.f90:1-20 (3 temporal load weights, w = 2 3.14159 / 24).
+void getfextc_t(double t1, double dt, double* fextc);
 // src/kokkos_damage.f90:36-47 temporal shape table, Nt[jj*6+k].
 void nt_table(int nip, const double* tcoorde, double w, double* Nt);
 

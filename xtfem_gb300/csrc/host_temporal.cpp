@@ -202,6 +202,22 @@ void stcoeff_t(double dt, double* k, double* m, double* ktn, double* mtn, double
     mtn1[6] = 1.;  // (1,3), column-major
 }
 
+void getfextc_t(double t1, double dt, double* fextc)
+{
+    // src/getfextc.f90:9-18: the first three assignments are overwritten
+    // by the sinusoidal forms, with the reference's w = 2 * 3.14159 / 24
+    using std::cos;
+    using std::sin;
+    const double w = 2 * 3.14159 / 24;
+    const double d2w2 = dt * dt * w * w, dw = dt * w;
+    fextc[0] = -((3. * dw * cos(t1 * w) + dw * cos((dt + t1) * w) + 4. * sin(t1 * w) -
+                  4. * sin((dt + t1) * w)) / d2w2);
+    fextc[1] = (4. * (dw * cos(t1 * w) + dw * cos((dt + t1) * w) + 2. * sin(t1 * w) -
+                      2. * sin((dt + t1) * w))) / d2w2;
+    fextc[2] = -((dw * cos(t1 * w) + 3. * dw * cos((dt + t1) * w) + 4 * sin(t1 * w) -
+                  4. * sin((dt + t1) * w)) / d2w2);
+}
+
 void getfextc_m(double t1, double w, double dt, double* fextc, double* fint)
 {
     using std::cos;
