@@ -130,6 +130,15 @@ int xt_slab_drain(xt_slab s, double *stats);
 /* Replaces the damage D and stored energy ws of every Gauss point (host
  * arrays of 8 per element; either may be NULL), e.g. to resume a run. */
 int xt_slab_set_state(xt_slab s, const double *D, const double *ws);
+/* The reference's output step (src/postprocess.f90:106-378) for the last
+ * slab: nodal displacement and Gauss-point strain, stress, damage, stored
+ * energy and element status at the slab's output time, appended to
+ * <job>.time, <job>.disp and <job>_0.strain / .stress / .damage / .energy /
+ * .status (strain and stress as 6(E16.8,2X) records, list-directed values
+ * with 17 significant digits); truncate = 1 empties the files first, as the
+ * reference's initfile does (an empty <job>.temp is made too).  Waits for a
+ * running damage update. */
+int xt_slab_dump(xt_slab s, const char *job, int truncate);
 /* Copies of the current state (waits for a running damage update). */
 int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
 /* ------------------------------------------------ thermal slab loop */

@@ -540,6 +540,11 @@ class SlabSolver:
         check(lib().xt_slab_set_state(self._h, dptr(a) if a is not None else None,
                                       dptr(b) if b is not None else None), "xt_slab_set_state")
 
+    def dump(self, job, truncate=False):
+        """The reference's output step for the last slab, appended to
+        <job>.time, <job>.disp and <job>_0.{strain,stress,damage,energy,status}."""
+        check(lib().xt_slab_dump(self._h, str(job).encode(), 1 if truncate else 0), "xt_slab_dump")
+
     def state(self):
         disp, D, ws = np.zeros(self.p * 6), np.zeros(self.ngp), np.zeros(self.ngp)
         el = np.zeros(self.ne, np.int32)

@@ -18,8 +18,13 @@
 // tcoorde(1) is used here.  Every per-slab vector stays on the device; the
 // host sees a handful of scalars per slab.
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
 
 #include "../../include/xtfem_gb300_host.h"
 #include "host_problem.h"
@@ -348,6 +353,121 @@ int guarded(F&& f)
 
 }  // namespace
 
+// ------------------------------------------------------------ state dump
+// The output step of the reference (mpipostprocess and its writers,
+// src/postprocess.f90:106-378): at t = tc1 + (nout - 1) dt / nip with
+// nout = nip - (nipc / 4) 3 + 1, the nodal displacement (.disp), the
+// Gauss-point strain and stress (.strain, .stress, 6(E16.8,2X)), damage
+// (.damage), stored energy (.energy) and element status (.status); the
+// time goes to .time.  Files <job>.time and <job>.disp are the root rank's,
+// <job>_0.* the per-rank ones of a one-process run; records are appended,
+// after truncating every file when asked (initfile).  List-directed
+// records carry 17 significant digits, one value per field.
+namespace {
+
+void fortran_e16_8(double v, char* out)
+{
+    // Fortran E16.8: 0.dddddddd with an exponent of two digits
+    if (v == 0.0) {
+        std::snprintf(out, 17, "%16s", "0.00000000E+00");
+        return;
+    }
+    char buf[32];
+    std::snprintf(buf, sizeof buf, "%.7e", std::fabs(v));  // d.ddddddde+XX
+    const int ex = std::atoi(buf + 10) + 1;
+    char body[24];
+    std::snprintf(body, sizeof body, "%s0.%c%.7sE%c%02d", v < 0 ? "-" : "", buf[0], buf + 2,
+                  ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
+    std::snprintf(out, 17, "%16s", body);
+}
+
+FILE* open_dump(const std::string& path, bool truncate)
+{
+    FILE* f = std::fopen(path.c_str(), truncate ? "w" : "a");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    return f;
+}
+
+int slab_dump(xt_slab_s& s, const std::string& job, bool truncate)
+{
+    if (s.slab < 1) {
+        set_error("xt_slab_dump: no slab solved yet");
+        return XT_ERR_STATE;
+    }
+    cudaStream_t st = s.S.stream;
+    const int nn = s.nn, ngp = s.ngp;
+    const size_t n = (size_t)s.p * 6;
+    const int nip = s.nip, nipc = s.cfg.nipc;
+    const double dt = s.tc[2] - s.tc[0];
+    const int nout = nip - nipc / 4 * 3 + 1;
+    const double t = s.tc[0] + (nout - 1) * dt / nip;
+    double Nt[6];
+    Nt[0] = 2.0 * (s.tc[1] - t) * (s.tc[2] - t) / (dt * dt);
+    Nt[1] = -4.0 * (s.tc[0] - t) * (s.tc[2] - t) / (dt * dt);
+    Nt[2] = 2.0 * (s.tc[0] - t) * (s.tc[1] - t) / (dt * dt);
+    Nt[3] = Nt[0] * (std::sin(s.w * t) - std::sin(s.w * s.tc[0]));
+    Nt[4] = Nt[1] * (std::sin(s.w * t) - std::sin(s.w * s.tc[1]));
+    Nt[5] = Nt[2] * (std::sin(s.w * t) - std::sin(s.w * s.tc[2]));
+    XT_TRY(s.hblk.alloc(n));
+    XT_TRY((to_blocks<double, double>(s.disp.p, s.hblk.p, s.p, 6, st)));
+    DBuf<double> strain, stress;
+    XT_TRY(strain.alloc((size_t)ngp * 6));
+    XT_TRY(stress.alloc((size_t)ngp * 6));
+    XT_TRY(post_strain_stress(ngp, nn, s.nodes.p, s.Nx.p, s.Ny.p, s.Nz.p, s.ym.p, s.nu.p,
+                              s.gpsta.p, s.hblk.p, Nt, strain.p, stress.p, st));
+    std::vector<double> sol(n), hs((size_t)ngp * 6), hst((size_t)ngp * 6), D(ngp), ws(ngp);
+    std::vector<int> el(s.ne);
+    XT_CUDA(cudaMemcpyAsync(sol.data(), s.hblk.p, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(hs.data(), strain.p, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(hst.data(), stress.p, hst.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(D.data(), s.D.p, ngp * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(ws.data(), s.ws.p, ngp * sizeof(double), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(el.data(), s.elesta.p, s.ne * sizeof(int), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    const std::string rank = job + "_0";
+    if (truncate) {  // initfile: the root's .temp exists too (no thermal part here)
+        std::fclose(open_dump(job + ".temp", true));
+    }
+    FILE* f = open_dump(job + ".time", truncate);
+    std::fprintf(f, " %25.17E\n", t);
+    std::fclose(f);
+    f = open_dump(job + ".disp", truncate);
+    for (int j = 0; j < nn; ++j) {
+        for (int c = 0; c < 3; ++c) {
+            double v = 0.0;
+            for (int k = 0; k < 6; ++k) v += Nt[k] * sol[(size_t)k * nn * 3 + (size_t)j * 3 + c];
+            std::fprintf(f, " %25.17E", v);
+        }
+        std::fputc('\n', f);
+    }
+    std::fclose(f);
+    char field[20];
+    for (int pass = 0; pass < 2; ++pass) {
+        const std::vector<double>& a = pass == 0 ? hs : hst;
+        f = open_dump(rank + (pass == 0 ? ".strain" : ".stress"), truncate);
+        for (int g = 0; g < ngp; ++g) {
+            for (int c = 0; c < 6; ++c) {
+                fortran_e16_8(a[(size_t)g * 6 + c], field);
+                std::fprintf(f, "%s  ", field);
+            }
+            std::fputc('\n', f);
+        }
+        std::fclose(f);
+    }
+    f = open_dump(rank + ".damage", truncate);
+    for (double v : D) std::fprintf(f, " %25.17E\n", v);
+    std::fclose(f);
+    f = open_dump(rank + ".energy", truncate);
+    for (double v : ws) std::fprintf(f, " %25.17E\n", v);
+    std::fclose(f);
+    f = open_dump(rank + ".status", truncate);
+    for (int v : el) std::fprintf(f, " %11d\n", v);
+    std::fclose(f);
+    return XT_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
@@ -511,6 +631,18 @@ int xt_slab_set_state(xt_slab s, const double* D, const double* ws)
     if (ws) XT_CUDA(cudaMemcpyAsync(s->ws.p, ws, b, cudaMemcpyHostToDevice, cs));
     XT_CUDA(cudaStreamSynchronize(cs));
     return XT_OK;
+}
+
+int xt_slab_dump(xt_slab s, const char* job, int truncate)
+{
+    if (!s || !job) { set_error("xt_slab_dump: null argument"); return XT_ERR_ARG; }
+    XT_TRY(damage_wait(*s, nullptr));
+    try {
+        return slab_dump(*s, job, truncate != 0);
+    } catch (const std::exception& e) {
+        set_error(std::string("xt_slab_dump: ") + e.what());
+        return XT_ERR_HOST;
+    }
 }
 
 int xt_slab_get(xt_slab s, double* disp, double* D, double* ws, int* elesta)

@@ -267,6 +267,15 @@ int to_interleaved(const TI* blk, TO* itl, int p, int q, cudaStream_t s);
 template <class TI, class TO>
 int to_blocks(const TI* itl, TO* blk, int p, int q, cudaStream_t s);
 
+// Per-Gauss-point strain and stress of the reference's output step
+// (dev_post.cu): sol_blocks is the slab solution in block layout (6 temporal
+// blocks of 3 nn), Nt6 the six temporal shape values at the output time
+// (host); strain and stress are ngp x 6, zero at failed points.
+int post_strain_stress(int ngp, int nn, const int* nodes, const double* Nx, const double* Ny,
+                       const double* Nz, const double* ym, const double* nu, const int* gpsta,
+                       const double* sol_blocks, const double* Nt6, double* strain, double* stress,
+                       cudaStream_t s);
+
 // ----------------------------------------------------------------- damage
 struct DamageArgs {
     int ngp, nn, ndofn, nnse, nnte, ncmp, nip;
