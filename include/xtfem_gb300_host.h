@@ -145,7 +145,8 @@ int xt_slab_get(xt_slab s, double *disp, double *D, double *ws, int *elesta);
 
 /* The temperature part of the reference's slab loop (src/main3d.f90:
  * 429-476 set-up, 586-608 initial and boundary terms, 697-734 per slab)
- * for a run without the mechanical coupling: q = 3 temporal nodes,
+ * (on its own, or advanced by a coupled mechanical loop, xt_slab_couple):
+ * q = 3 temporal nodes,
  * conductivity and capacity of the mesh (elemtx_t, src/elesubs.f90:60-116),
  * fixed temperature T0 on the faces x[fixed_axis] == fixed_value[0] or
  * fixed_value[1], heat flux q0 on the faces x[flux_axis] == flux_value[0]
@@ -186,6 +187,31 @@ int xt_thermal_destroy(xt_thermal t);
 int xt_thermal_step(xt_thermal t, double *stats);
 /* The slab's nodal temperatures, block layout (3 temporal blocks of nn). */
 int xt_thermal_get(xt_thermal t, double *temp);
+
+/* ------------------------------------------------ thermo-mechanical coupling */
+
+/* Couples a thermal slab loop to the mechanical one, as the reference's
+ * coupled run does every slab (src/main3d.f90:697-813): each xt_slab_step
+ * then first advances the thermal loop one slab, then on the device takes
+ * the end-of-slab temperatures to every Gauss point, updates the moduli
+ * (material_update, src/thermoelastic.f90:1-46; the damage update uses them
+ * too), reassembles K with them (mpiglbmtx_m, src/mpisubs.f90:69-139) and
+ * forms the thermal stress load vv (calc_thermo_stress and elevec_m,
+ * src/thermoelastic.f90:48-78, src/elesubs.f90:119-167), and adds fint(j) vv
+ * to load block j (src/main3d.f90:813).  refactor_every = k recomputes the
+ * ILUT factor from the reassembled K on the host every k slabs and after
+ * every deletion (0: after deletions only; the reference refactors its MUMPS
+ * preconditioner every slab).  The thermal loop must have been created on
+ * the same problem and outlive the coupling; the slab must not use
+ * cfg.overlap. */
+typedef struct xt_coupling_config {
+    double alpha;        /* thermal expansion coefficient */
+    double Tref;         /* reference temperature */
+    double ym0, nu0;     /* moduli at Tref */
+    int refactor_every;
+} xt_coupling_config;
+
+int xt_slab_couple(xt_slab s, xt_thermal t, const xt_coupling_config *cc);
 
 /* Per-kernel CUDA-event timing on the library stream: enable, then read
  * count and total milliseconds per kernel class (0 Kronecker FP64,

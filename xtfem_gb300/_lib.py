@@ -83,6 +83,7 @@ SIGNATURES = {
     "xt_slab_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
     "xt_slab_destroy": (C.c_int, [_vp]),
     "xt_slab_dump": (C.c_int, [_vp, C.c_char_p, C.c_int]),
+    "xt_slab_couple": (C.c_int, [_vp, _vp, _vp]),
     "xt_slab_step": (C.c_int, [_vp, _dp]),
     "xt_slab_step_host": (C.c_int, [_vp, _dp, _dp, _dp, _dp]),
     "xt_slab_drain": (C.c_int, [_vp, _dp]),

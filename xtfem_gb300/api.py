@@ -464,6 +464,13 @@ class ThermalConfig(C.Structure):
         return cls(**d)
 
 
+class CouplingConfig(C.Structure):
+    """xt_coupling_config of include/xtfem_gb300_host.h."""
+
+    _fields_ = [("alpha", C.c_double), ("Tref", C.c_double), ("ym0", C.c_double),
+                ("nu0", C.c_double), ("refactor_every", C.c_int)]
+
+
 class ThermalSolver:
     """The thermal slab loop (xt_thermal_*) of a problem's mesh."""
 
@@ -539,6 +546,16 @@ class SlabSolver:
         b = None if ws is None else _f64(ws)
         check(lib().xt_slab_set_state(self._h, dptr(a) if a is not None else None,
                                       dptr(b) if b is not None else None), "xt_slab_set_state")
+
+    def couple(self, thermal: "ThermalSolver", ym0, nu0, alpha=1.2e-5, Tref=0.0,
+               refactor_every=1):
+        """Couple a thermal slab loop (xt_slab_couple): each step then
+        advances it one slab, updates the moduli from ym0, nu0 at Tref,
+        reassembles K on the device and adds the thermal stress load."""
+        cc = CouplingConfig(alpha=alpha, Tref=Tref, ym0=ym0, nu0=nu0,
+                            refactor_every=refactor_every)
+        self._thermal = thermal  # kept alive while coupled
+        check(lib().xt_slab_couple(self._h, thermal._h, C.byref(cc)), "xt_slab_couple")
 
     def dump(self, job, truncate=False):
         """The reference's output step for the last slab, appended to

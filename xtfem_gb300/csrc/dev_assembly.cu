@@ -46,8 +46,8 @@ __constant__ signed char c_sign[8][3] = {{-1, -1, +1}, {-1, -1, -1}, {-1, +1, -1
 
 __global__ void __launch_bounds__(576)
 k_element_k(int ne, const int* __restrict__ conn, const double* __restrict__ xyz,
-            const double* __restrict__ ym, const double* __restrict__ nu,
-            double* __restrict__ ke)
+            const int* __restrict__ gel, const double* __restrict__ ym,
+            const double* __restrict__ nu, double* __restrict__ ke)
 {
     __shared__ double dN[8][8][3];  // [gauss point][node][x, y, z]
     __shared__ double det[8], lam[8], mu[8];
@@ -94,7 +94,8 @@ k_element_k(int ne, const int* __restrict__ conn, const double* __restrict__ xyz
                 dN[l][i][m] = s;
             }
         det[l] = d;
-        const double E = ym[(size_t)e * 8 + l], v = nu[(size_t)e * 8 + l];
+        const size_t gi = (size_t)(gel ? gel[e] : e) * 8 + l;  // the moduli's element
+        const double E = ym[gi], v = nu[gi];
         const double c = E / ((1.0 + v) * (1.0 - 2.0 * v));
         lam[l] = c * v;
         mu[l] = c * (0.5 - v);
@@ -125,9 +126,101 @@ __global__ void k_gather_k(int nnz, const int* __restrict__ cptr, const int* __r
     }
 }
 
+// Thermal coupling of one element (all elements, one block of 32 threads
+// each; threads 0..7 own a Gauss point): the point's temperature from the
+// end-of-slab nodal temperatures (the third temporal block), the moduli of
+// material_update (src/thermoelastic.f90:21-44: E = E0 - 1.6 dT - 0.1 dT^2,
+// nu = nu0 + 5e-5 dT for T >= 0, else E0, nu0; dT = T - Tref), the thermal
+// stress of calc_thermo_stress (:66-76: the sum of the first three columns
+// of D(E, nu) times alpha dT, for the three normal components) and the
+// element vector of elevec_m (src/elesubs.f90:119-167):
+// ve(3 i + m) = sum_l dN_i/dx_m(l) sigma_m(l) detJ(l).
+__global__ void __launch_bounds__(32)
+k_thermal_couple(int ne, const int* __restrict__ conn, const double* __restrict__ xyz,
+                 const double* __restrict__ temp, double alpha, double Tref, double ym0,
+                 double nu0, double* __restrict__ ym, double* __restrict__ nu,
+                 double* __restrict__ ve)
+{
+    __shared__ double contrib[8][24];
+    const int e = blockIdx.x;
+    if (e >= ne) return;
+    const int l = threadIdx.x;
+    if (l < 8) {
+        const double g[2] = {-kGaussAbs, kGaussAbs};
+        const double xi = g[(l >> 2) & 1], eta = g[(l >> 1) & 1], zeta = g[l & 1];
+        double xe[8][3], dn[8][3], N[8];
+        double T = 0.0;
+        for (int i = 0; i < 8; ++i) {
+            const int nd = conn[(size_t)e * 8 + i];
+            for (int m = 0; m < 3; ++m) xe[i][m] = xyz[(size_t)nd * 3 + m];
+            const double sx = c_sign[i][0], sy = c_sign[i][1], sz = c_sign[i][2];
+            N[i] = 0.125 * (1.0 + sx * xi) * (1.0 + sy * eta) * (1.0 + sz * zeta);
+            dn[i][0] = 0.125 * sx * (1.0 + sy * eta) * (1.0 + sz * zeta);
+            dn[i][1] = 0.125 * sy * (1.0 + sx * xi) * (1.0 + sz * zeta);
+            dn[i][2] = 0.125 * sz * (1.0 + sx * xi) * (1.0 + sy * eta);
+            T += N[i] * temp[(size_t)nd * 3 + 2];
+        }
+        double J[3][3];
+        for (int a = 0; a < 3; ++a)
+            for (int m = 0; m < 3; ++m) {
+                double s = 0.0;
+                for (int i = 0; i < 8; ++i) s += dn[i][a] * xe[i][m];
+                J[a][m] = s;
+            }
+        const double d = J[0][0] * J[1][1] * J[2][2] + J[0][1] * J[1][2] * J[2][0] +
+                         J[0][2] * J[1][0] * J[2][1] - J[0][0] * J[1][2] * J[2][1] -
+                         J[0][1] * J[1][0] * J[2][2] - J[0][2] * J[1][1] * J[2][0];
+        double inv[3][3];
+        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / d;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / d;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / d;
+        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / d;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / d;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / d;
+        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / d;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / d;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / d;
+        const double dT = T - Tref;
+        double E = ym0, v = nu0;
+        if (T >= 0.0) {
+            E = ym0 - 1.6 * dT - 0.1 * dT * dT;
+            v = nu0 + 5.e-5 * dT;
+        }
+        ym[(size_t)e * 8 + l] = E;
+        nu[(size_t)e * 8 + l] = v;
+        const double c = E / ((1.0 + v) * (1.0 - 2.0 * v));
+        // D(m, 1) + D(m, 2) + D(m, 3) = c (1 - nu) + 2 c nu for m = 1..3
+        const double sig = (c * (1.0 - v) + 2.0 * c * v) * (alpha * dT);
+        for (int i = 0; i < 8; ++i)
+            for (int m = 0; m < 3; ++m) {
+                double dx = 0.0;
+                for (int a = 0; a < 3; ++a) dx += inv[m][a] * dn[i][a];
+                contrib[l][3 * i + m] = dx * sig * d;
+            }
+    }
+    __syncthreads();
+    if (l < 24) {
+        double s = 0.0;
+        for (int g = 0; g < 8; ++g) s += contrib[g][l];  // Gauss points in order
+        ve[(size_t)e * 24 + l] = s;
+    }
+}
+
+// y[k] = sum of x over the listed entries, in list order
+__global__ void k_gather_list(int n, const int* __restrict__ ptr, const int* __restrict__ idx,
+                              const double* __restrict__ x, double* __restrict__ y)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int t = ptr[k]; t < ptr[k + 1]; ++t) s += x[idx[t]];
+        y[k] = s;
+    }
+}
+
 }  // namespace
 
-int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* conn, const int* bc)
+int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* conn, const int* bc,
+                    const int* gel)
 {
     DevAssembly& A = S.asmb;
     A.ok = false;
@@ -239,6 +332,11 @@ int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* con
     XT_TRY(A.cptr.upload(cnt.data(), cnt.size(), s));
     XT_TRY(A.cidx.upload(idx.data(), idx.size(), s));
     XT_TRY(A.bcdiag.upload(bcd.data(), bcd.size(), s));
+    if (gel) {
+        XT_TRY(A.gel.upload(gel, (size_t)ne, s));
+    } else {
+        A.gel.release();
+    }
     XT_TRY(A.ke.alloc((size_t)ne * 576));
     XT_TRY(A.ym.alloc((size_t)ne * 8));
     XT_TRY(A.nu.alloc((size_t)ne * 8));
@@ -257,7 +355,21 @@ int system_assemble_k(System& S, const double* ym, const double* nu)
     cudaStream_t s = S.stream;
     XT_CUDA(cudaMemcpyAsync(A.ym.p, ym, sizeof(double) * A.ne * 8, cudaMemcpyHostToDevice, s));
     XT_CUDA(cudaMemcpyAsync(A.nu.p, nu, sizeof(double) * A.ne * 8, cudaMemcpyHostToDevice, s));
-    k_element_k<<<A.ne, 576, 0, s>>>(A.ne, A.conn.p, A.xyz.p, A.ym.p, A.nu.p, A.ke.p);
+    XT_TRY(system_assemble_k_device(S, A.ym.p, A.nu.p, false));
+    XT_CUDA(cudaStreamSynchronize(s));  // the host ym, nu may be reused at once
+    return XT_OK;
+}
+
+int system_assemble_k_device(System& S, const double* ym, const double* nu, bool by_gel)
+{
+    DevAssembly& A = S.asmb;
+    if (!A.ok) {
+        set_error("system_assemble_k: no mesh set");
+        return XT_ERR_STATE;
+    }
+    cudaStream_t s = S.stream;
+    k_element_k<<<A.ne, 576, 0, s>>>(A.ne, A.conn.p, A.xyz.p, by_gel ? A.gel.p : nullptr, ym, nu,
+                                     A.ke.p);
     const int nnz = S.K.nnz;
     const int blocks = std::max(1, std::min(4096, (nnz + 255) / 256));
     k_gather_k<<<blocks, 256, 0, s>>>(nnz, A.cptr.p, A.cidx.p, A.ke.p, A.bcdiag.p, S.K.v64.p);
@@ -266,7 +378,24 @@ int system_assemble_k(System& S, const double* ym, const double* nu)
     XT_TRY(to_f32(S.K.v64.p, S.K.v32.p, (size_t)nnz, s));
     S.K.vdf.release();  // remade from the new values on first use
     XT_TRY(node_blocks_refresh(S.K, s));
-    XT_CUDA(cudaStreamSynchronize(s));  // the host ym, nu may be reused at once
+    return XT_OK;
+}
+
+int thermal_couple_device(int ne, const int* conn0, const double* xyz, const double* temp,
+                          double alpha, double Tref, double ym0, double nu0, double* ym, double* nu,
+                          double* ve, cudaStream_t s)
+{
+    k_thermal_couple<<<ne, 32, 0, s>>>(ne, conn0, xyz, temp, alpha, Tref, ym0, nu0, ym, nu, ve);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int gather_list(int n, const int* ptr, const int* idx, const double* x, double* y, cudaStream_t s)
+{
+    k_gather_list<<<std::max(1, std::min(4096, (n + 255) / 256)), 256, 0, s>>>(n, ptr, idx, x, y);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
     return XT_OK;
 }
 

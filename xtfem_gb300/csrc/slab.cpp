@@ -30,6 +30,7 @@
 #include "host_problem.h"
 #include "prof.h"
 #include "solver.h"
+#include "thermal.h"
 
 using namespace xt;
 
@@ -60,6 +61,13 @@ struct xt_slab_s {
     // results of the last finished update, kept until the next slab uses them
     int del_flag = 0;
     double dmg_stats[4] = {0, 0, 0, 0};
+    // thermal coupling (xt_slab_couple)
+    xt_thermal_s* therm = nullptr;
+    xt_coupling_config cc{};
+    DBuf<int> conn0, vptr, vidx;
+    DBuf<double> xyzd, ymc, nuc, ve, vv, work;
+    int coupled_slabs = 0;
+    bool force_refactor = false;
     ~xt_slab_s()
     {
         if (ds) {
@@ -84,6 +92,87 @@ int refactor(xt_slab_s& s)
         return XT_ERR_HOST;
     }
     return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group);
+}
+
+// ILUT of the device K (after a reassembly on the device)
+int refactor_device(xt_slab_s& s)
+{
+    cudaStream_t st = s.S.stream;
+    const int n = s.p, nnz = s.S.K.nnz;
+    Csr K;
+    K.n = n;
+    K.ia.resize(n + 1);
+    K.ja.resize(nnz);
+    K.a.resize(nnz);
+    XT_CUDA(cudaMemcpyAsync(K.ia.data(), s.S.K.rowptr.p, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(K.ja.data(), s.S.K.col.p, sizeof(int) * nnz, cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaMemcpyAsync(K.a.data(), s.S.K.v64.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    for (int& v : K.ia) ++v;
+    for (int& v : K.ja) ++v;
+    Msr f;
+    const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f);
+    if (ierr != 0) {
+        set_error("ILUT of the reassembled K failed with ierr = " + std::to_string(ierr));
+        return XT_ERR_HOST;
+    }
+    return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group);
+}
+
+// Maps of the coupled loop for the live elements: K's element pattern and
+// its reassembly map, and per DOF the entries of the element thermal-stress
+// vectors that sum into it (ascending element order).
+int couple_maps(xt_slab_s& s)
+{
+    cudaStream_t st = s.S.stream;
+    const Mesh& m = s.pr->mesh;
+    std::vector<int> el(s.ne);
+    XT_CUDA(cudaMemcpyAsync(el.data(), s.elesta.p, sizeof(int) * s.ne, cudaMemcpyDeviceToHost, st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    std::vector<int> conn, gel;
+    for (int e = 0; e < s.ne; ++e)
+        if (el[e]) {
+            gel.push_back(e);
+            conn.insert(conn.end(), m.conn.begin() + (size_t)e * 8, m.conn.begin() + (size_t)e * 8 + 8);
+        }
+    XT_TRY(system_set_mesh(s.S, s.nn, (int)gel.size(), m.xyz.data(), conn.data(), s.bc.data(),
+                           gel.data()));
+    std::vector<int> cnt(s.p + 1, 0);
+    for (int e : gel)
+        for (int i = 0; i < 8; ++i)
+            for (int c = 0; c < 3; ++c) ++cnt[3 * (m.conn[(size_t)e * 8 + i] - 1) + c + 1];
+    for (int g = 0; g < s.p; ++g) cnt[g + 1] += cnt[g];
+    std::vector<int> idx(cnt[s.p]), fill(cnt.begin(), cnt.end() - 1);
+    for (int e : gel)
+        for (int i = 0; i < 8; ++i)
+            for (int c = 0; c < 3; ++c)
+                idx[fill[3 * (m.conn[(size_t)e * 8 + i] - 1) + c]++] = e * 24 + 3 * i + c;
+    XT_TRY(s.vptr.upload(cnt.data(), cnt.size(), st));
+    XT_TRY(s.vidx.upload(idx.data(), idx.size(), st));
+    XT_CUDA(cudaStreamSynchronize(st));
+    return XT_OK;
+}
+
+// One thermal slab, then the moduli, K and the thermal stress load vv
+int couple_update(xt_slab_s& s)
+{
+    XT_TRY(thermal_advance(*s.therm, nullptr));
+    cudaStream_t st = s.S.stream;
+    const size_t ngp = s.ngp;
+    XT_TRY(thermal_couple_device(s.ne, s.conn0.p, s.xyzd.p, thermal_temperature(*s.therm),
+                                 s.cc.alpha, s.cc.Tref, s.cc.ym0, s.cc.nu0, s.ymc.p, s.nuc.p,
+                                 s.ve.p, st));
+    XT_CUDA(cudaMemcpyAsync(s.ym.p, s.ymc.p, ngp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    XT_CUDA(cudaMemcpyAsync(s.nu.p, s.nuc.p, ngp * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    XT_TRY(system_assemble_k_device(s.S, s.ymc.p, s.nuc.p, true));
+    if (s.force_refactor ||
+        (s.cc.refactor_every > 0 && s.coupled_slabs % s.cc.refactor_every == 0)) {
+        XT_TRY(refactor_device(s));
+        s.force_refactor = false;
+    }
+    XT_TRY(gather_list(s.p, s.vptr.p, s.vidx.p, s.ve.p, s.vv.p, st));
+    ++s.coupled_slabs;
+    return XT_OK;
 }
 
 int upload_operator(xt_slab_s& s)
@@ -121,7 +210,12 @@ int deletion_check(xt_slab_s& s, int& deleted)
     int ndf = 0;
     XT_TRY(s.pr->delete_elements(nef, list.data(), s.bc.data(), &ndf));
     XT_TRY(upload_operator(s));
-    XT_TRY(refactor(s));
+    if (s.therm) {  // the coupled K is reassembled on the device from the live elements
+        XT_TRY(couple_maps(s));
+        s.force_refactor = true;
+    } else {
+        XT_TRY(refactor(s));
+    }
     s.dt = s.cfg.dt0 * s.cfg.n2;
     s.nip = s.cfg.nipc * s.cfg.n2;
     s.switched = true;
@@ -149,6 +243,7 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check 
         A[k] = ck[k] + ckt[k];
         B[k] = cm[k] + cmt[k];
     }
+    if (s.therm) XT_TRY(couple_update(s));  // before the jump term: it uses the new K
     XT_TRY(system_set_temporal(s.S, A, B));
     XT_CUDA(cudaMemcpyAsync(s.S.Cj.p, ck1, sizeof(ck1), cudaMemcpyHostToDevice, st));
     XT_CUDA(cudaMemcpyAsync(s.S.Mj.p, cm1, sizeof(cm1), cudaMemcpyHostToDevice, st));
@@ -161,6 +256,10 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check 
         double fextc[6], fint[6];
         getfextc_m(s.tc[0], s.w, s.dt, fextc, fint);
         XT_TRY(fill_load(s.drext.p, fextc, s.fext.p, s.p, s.q, st));
+        if (s.therm) {  // + fint(j) vv, the thermal stress load (src/main3d.f90:813)
+            XT_TRY(fill_load(s.vv.p, fint, s.work.p, s.p, s.q, st));
+            XT_TRY((axpby<double, double>(n, 1.0, s.work.p, 1.0, s.fext.p, st)));
+        }
     }
     XT_TRY(system_apply_with(s.S, s.S.Cj.p, s.S.Mj.p, 1.0, 1.0, s.disp.p, s.fext.p));
     XT_TRY(mask_rows<double>(s.fext.p, s.S.bcmask.p, s.p, s.q, st));
@@ -631,6 +730,37 @@ int xt_slab_set_state(xt_slab s, const double* D, const double* ws)
     if (ws) XT_CUDA(cudaMemcpyAsync(s->ws.p, ws, b, cudaMemcpyHostToDevice, cs));
     XT_CUDA(cudaStreamSynchronize(cs));
     return XT_OK;
+}
+
+int xt_slab_couple(xt_slab s, xt_thermal t, const xt_coupling_config* cc)
+{
+    if (!s || !t || !cc) { set_error("xt_slab_couple: null argument"); return XT_ERR_ARG; }
+    if (s->cfg.overlap) { set_error("xt_slab_couple: not with cfg.overlap"); return XT_ERR_ARG; }
+    if (thermal_nodes(*t) != s->nn) {
+        set_error("xt_slab_couple: the thermal loop has another mesh");
+        return XT_ERR_ARG;
+    }
+    if (s->slab > 0) { set_error("xt_slab_couple: couple before the first slab"); return XT_ERR_STATE; }
+    try {
+        s->therm = t;
+        s->cc = *cc;
+        const Mesh& m = s->pr->mesh;
+        cudaStream_t st = s->S.stream;
+        std::vector<int> c0(m.conn.begin(), m.conn.end());
+        for (int& v : c0) --v;
+        XT_TRY(s->conn0.upload(c0.data(), c0.size(), st));
+        XT_TRY(s->xyzd.upload(m.xyz.data(), m.xyz.size(), st));
+        for (DBuf<double>* b : {&s->ymc, &s->nuc}) XT_TRY(b->alloc((size_t)s->ngp));
+        XT_TRY(s->ve.alloc((size_t)s->ne * 24));
+        XT_TRY(s->vv.alloc((size_t)s->p));
+        XT_TRY(s->work.alloc((size_t)s->p * s->q));
+        XT_TRY(couple_maps(*s));
+        return XT_OK;
+    } catch (const std::exception& e) {
+        s->therm = nullptr;
+        set_error(std::string("xt_slab_couple: ") + e.what());
+        return XT_ERR_HOST;
+    }
 }
 
 int xt_slab_dump(xt_slab s, const char* job, int truncate)

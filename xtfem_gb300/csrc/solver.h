@@ -59,8 +59,21 @@ int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, 
 int system_set_temporal(System& S, const double* A, const double* B);
 // Device reassembly of K from per-Gauss-point moduli (dev_assembly.cu):
 // the mesh and constrained DOFs once, then any number of reassemblies.
-int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* conn, const int* bc);
+// gel (may be null): the full-mesh index of each listed element, for
+// moduli arrays that cover every element of the mesh.
+int system_set_mesh(System& S, int nn, int ne, const double* xyz, const int* conn, const int* bc,
+                    const int* gel = nullptr);
 int system_assemble_k(System& S, const double* ym, const double* nu);
+// The same from moduli already on the device (by_gel: indexed through gel).
+int system_assemble_k_device(System& S, const double* ym, const double* nu, bool by_gel);
+// Thermal coupling of every element (dev_assembly.cu): Gauss-point moduli
+// and element thermal-stress vectors (ne x 24) from the end-of-slab nodal
+// temperatures (temp: interleaved, nn x 3).
+int thermal_couple_device(int ne, const int* conn0, const double* xyz, const double* temp,
+                          double alpha, double Tref, double ym0, double nu0, double* ym, double* nu,
+                          double* ve, cudaStream_t s);
+// y[k] = sum over t in [ptr[k], ptr[k+1]) of x[idx[t]]
+int gather_list(int n, const int* ptr, const int* idx, const double* x, double* y, cudaStream_t s);
 
 // q x q inverse by LU with partial pivoting (host); returns XT_ERR_SINGULAR.
 int invert_small(int n, const double* A, double* Ainv);

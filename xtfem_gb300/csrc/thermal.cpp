@@ -1,8 +1,8 @@
 // thermal.cpp -- the thermal space-time slab loop (q = 3) with its state on
 // the GPU.
 //
-// Restates the temperature part of src/main3d.f90 for a run without the
-// mechanical coupling:
+// Restates the temperature part of src/main3d.f90 (alone, or driven by the
+// mechanical slab loop through thermal.h when the two are coupled):
 //   set-up   conductivity and capacity (mpiglbmtx_t / elemtx_t,
 //            src/elesubs.f90:60-116), the fixed-temperature faces
 //            (:429-441), K and M kept before the boundary conditions
@@ -27,6 +27,7 @@
 #include "../../include/xtfem_gb300_host.h"
 #include "host_problem.h"
 #include "solver.h"
+#include "thermal.h"
 
 using namespace xt;
 
@@ -195,6 +196,12 @@ int thermal_step(xt_thermal_s& t, double* stats)
 }
 
 }  // namespace
+
+namespace xt {
+int thermal_advance(xt_thermal_s& t, double* stats) { return thermal_step(t, stats); }
+const double* thermal_temperature(const xt_thermal_s& t) { return t.temp.p; }
+int thermal_nodes(const xt_thermal_s& t) { return t.nn; }
+}  // namespace xt
 
 extern "C" {
 

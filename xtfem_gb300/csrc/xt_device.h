@@ -107,6 +107,7 @@ struct DevAssembly {
     DBuf<unsigned char> bcdiag;  // per K entry: diagonal of a constrained DOF
     DBuf<double> ke;             // ne x 576 element matrices
     DBuf<double> ym, nu;         // ne x 8 Gauss-point moduli
+    DBuf<int> gel;               // optional: element e's index in full-mesh moduli arrays
 };
 
 struct DevCsr {
