@@ -24,6 +24,10 @@ typedef struct xth_problem_s *xth_problem;
  * strain rows for a uniform isotropic material (src/mpisubs.f90:69-139). */
 int xth_problem_from_inp(const char *path, double E, double nu, double rho,
                          xth_problem *out);
+/* A problem from a C3D8 mesh in memory: xyz (nn x 3), conn (ne x 8, 1-based,
+ * the node order of the reference's shape functions, src/procs.f90:1366-1389). */
+int xth_problem_from_mesh(int nn, int ne, const double *xyz, const int *conn, double E,
+                          double nu, double rho, xth_problem *out);
 int xth_problem_rod(int nx, int ny, int nz, double lx, double ly, double lz,
                     double E, double nu, double rho, xth_problem *out);
 int xth_problem_destroy(xth_problem pr);

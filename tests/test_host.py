@@ -217,3 +217,33 @@ def test_oracle_chkelesta_lists_failed_elements_ascending(orc):
     assert nef == 2 and list(failed) == [4, 8]  # 1-based element ids
     assert elesta[3] == 0 and elesta[7] == 0 and elesta.sum() == ne - 2
     assert gpsta[24:32].sum() == 0 and gpsta[56:64].sum() == 0 and gpsta.sum() == ne * ngpe - 16
+
+
+# ------------------------------------------------------------- generated meshes
+def test_sent_plate_generator(xt):
+    """The SENT plate: positive Jacobian at every element's centre, no
+    unattached node, the notch's elements missing, and the host assembly
+    of the mesh symmetric with the rigid-body modes in its kernel."""
+    from xtfem_gb300.meshes import sent_plate
+
+    nx, ny, nz = 12, 24, 2
+    xyz, conn = sent_plate(nx, ny, nz)
+    assert len(xyz) == (nx + 1) * (ny + 1) * (nz + 1)
+    assert len(conn) < nx * ny * nz and len(conn) >= nx * ny * nz - nx * nz
+    assert np.array_equal(np.unique(conn), np.arange(1, len(xyz) + 1))
+    sign = np.array([[-1, -1, 1], [-1, -1, -1], [-1, 1, -1], [-1, 1, 1],
+                     [1, -1, 1], [1, -1, -1], [1, 1, -1], [1, 1, 1]], float)
+    for e in range(len(conn)):
+        J = (sign / 8.0).T @ xyz[conn[e] - 1]
+        assert np.linalg.det(J) > 0
+    centres = xyz[conn - 1].mean(1)
+    mid = (np.abs(centres[:, 1] - 1.0) < 0.05) & (centres[:, 0] < 0.3)
+    assert not mid.any() or centres[mid, 1].min() > 1.0  # below mid-height, left of the tip: removed
+    pr = xt.Problem.from_mesh(xyz, conn)
+    K = pr.K().to_scipy()
+    assert abs(K - K.T).max() <= 1e-10 * abs(K).max()
+    rigid = np.zeros((K.shape[0], 3))
+    for c in range(3):
+        rigid[c::3, c] = 1.0
+    assert np.abs(K @ rigid).max() <= 1e-8 * abs(K).max()
+    pr.close()

@@ -60,6 +60,8 @@ SIGNATURES = {
                                  C.c_int, C.c_double, _dp, _ip]),
     "xth_problem_from_inp": (C.c_int, [C.c_char_p, C.c_double, C.c_double, C.c_double,
                                        C.POINTER(_vp)]),
+    "xth_problem_from_mesh": (C.c_int, [C.c_int, C.c_int, _dp, _ip, C.c_double, C.c_double,
+                                        C.c_double, C.POINTER(_vp)]),
     "xth_problem_rod": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                                   C.c_double, C.c_double, C.c_double, C.POINTER(_vp)]),
     "xth_problem_destroy": (C.c_int, [_vp]),

@@ -363,6 +363,16 @@ class Problem:
         return cls(h)
 
     @classmethod
+    def from_mesh(cls, xyz, conn, E=2.0e5, nu=0.3, rho=7.8e-9):
+        """A problem from a C3D8 mesh in memory (xyz: nn x 3; conn: ne x 8,
+        1-based, the reference's node order)."""
+        x, c = _f64(xyz).reshape(-1), _i32(conn).reshape(-1)
+        h = C.c_void_p()
+        check(lib().xth_problem_from_mesh(x.size // 3, c.size // 8, dptr(x), iptr(c), E, nu, rho,
+                                          C.byref(h)), "from_mesh")
+        return cls(h)
+
+    @classmethod
     def rod(cls, nx, ny, nz, lx=3.0, ly=1.0, lz=1.0, E=2.0e5, nu=0.3, rho=7.8e-9):
         h = C.c_void_p()
         check(lib().xth_problem_rod(nx, ny, nz, lx, ly, lz, E, nu, rho, C.byref(h)), "rod")

@@ -127,6 +127,28 @@ int xth_problem_from_inp(const char* path, double E, double nu, double rho, xth_
     });
 }
 
+int xth_problem_from_mesh(int nn, int ne, const double* xyz, const int* conn, double E, double nu,
+                          double rho, xth_problem* out)
+{
+    if (!xyz || !conn || !out || nn <= 0 || ne <= 0) {
+        set_error("xth_problem_from_mesh: bad arguments");
+        return XT_ERR_ARG;
+    }
+    return guarded([&] {
+        auto pr = std::make_unique<Problem>();
+        pr->mesh.nn = nn;
+        pr->mesh.ne = ne;
+        pr->mesh.xyz.assign(xyz, xyz + (size_t)nn * 3);
+        pr->mesh.conn.assign(conn, conn + (size_t)ne * 8);
+        for (int v : pr->mesh.conn)
+            if (v < 1 || v > nn) {
+                set_error("xth_problem_from_mesh: connectivity out of range");
+                return XT_ERR_ARG;
+            }
+        return finish_problem(pr, E, nu, rho, out);
+    });
+}
+
 int xth_problem_rod(int nx, int ny, int nz, double lx, double ly, double lz, double E, double nu,
                     double rho, xth_problem* out)
 {

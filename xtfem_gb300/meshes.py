@@ -1,0 +1,61 @@
+"""Generated C3D8 meshes of the reference's workloads whose mesh files are
+not shipped with it: the single-edge-notched tension (SENT) plate.
+
+The shipped rods come from the host generator (``Problem.rod``); these are
+built here and handed over with ``Problem.from_mesh``.  Connectivity uses the
+node order of the reference's C3D8 shape functions (src/procs.f90:1366-1389:
+local node n sits at the natural coordinates of its sign row, xi along x,
+eta along y, zeta along z), so every Jacobian is positive.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+# natural coordinates of the 8 local nodes (src/procs.f90:1366-1373)
+_SIGN = np.array([[-1, -1, 1], [-1, -1, -1], [-1, 1, -1], [-1, 1, 1],
+                  [1, -1, 1], [1, -1, -1], [1, 1, -1], [1, 1, 1]])
+
+
+def _graded(a, b, n, ratio, toward_b):
+    """n + 1 coordinates on [a, b], spacings in geometric progression of the
+    given ratio (>= 1), finest at b when toward_b, else at a."""
+    w = ratio ** np.arange(n, dtype=float)
+    w = w[::-1] if toward_b else w
+    x = a + (b - a) * np.concatenate([[0.0], np.cumsum(w) / w.sum()])
+    x[-1] = b
+    return x
+
+
+def sent_plate(nx=48, ny=96, nz=2, W=1.0, H=2.0, t=0.1, notch=0.3, ratio=1.05):
+    """Single-edge-notched tension plate W x H x t with an edge notch of
+    length notch*W at mid-height, made by removing one row of elements (the
+    row just below y = H/2, from x = 0 to the notch tip).  The grid is graded
+    toward the notch tip in x and toward the mid-height in y (spacing ratio
+    `ratio` between neighbours), nz elements through the thickness.  Returns
+    (xyz (nn x 3), conn (ne x 8, 1-based)) with no unattached node."""
+    a = notch * W
+    nxl = max(1, int(round(nx * notch)))
+    xs = np.concatenate([_graded(0.0, a, nxl, ratio, True),
+                         _graded(a, W, nx - nxl, ratio, False)[1:]])
+    nyh = ny // 2
+    ys = np.concatenate([_graded(0.0, H / 2, nyh, ratio, True),
+                         _graded(H / 2, H, ny - nyh, ratio, False)[1:]])
+    zs = np.linspace(0.0, t, nz + 1)
+    # nodes numbered with the long side (y) outermost, then x, then z: the
+    # matrix bandwidth is one x-z layer, as for the shipped rods, which the
+    # level-of-fill-limited ILUT needs
+    nxn, nzn = len(xs), len(zs)
+    Y, X, Z = np.meshgrid(ys, xs, zs, indexing="ij")
+    xyz = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+
+    def node(i, j, k):
+        return (j * nxn + i) * nzn + k + 1
+
+    conn = []
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                if j == nyh - 1 and xs[i + 1] <= a + 1e-12:
+                    continue  # the notch: one row of elements removed
+                conn.append([node(i + (sx > 0), j + (sy > 0), k + (sz > 0)) for sx, sy, sz in _SIGN])
+    return xyz, np.array(conn, np.int32)
