@@ -1,0 +1,47 @@
+"""The holed panel (the generated stand-in for the reference's missing
+thin-panel mesh) in a coupled thermo-mechanical run: the plain FP64 loop and
+the mixed-precision loop give the same temperatures (1e-6) and displacements
+(1e-5, the thin panel being badly conditioned), slab by slab, and the
+heating acts."""
+import numpy as np
+import pytest
+
+from xtfem_gb300.meshes import holed_panel
+
+pytestmark = pytest.mark.gpu
+
+NSLAB = 2
+
+
+def run(xt, precision):
+    xyz, conn = holed_panel(32, 6, 1, W=1.0, t=0.05, radius=0.1)
+    pr = xt.Problem.from_mesh(xyz, conn)
+    th = xt.ThermalSolver(pr, xt.ThermalConfig.make(
+        fixed_axis=0, fixed_value=(0.0, 1.0), T0=20.0, Tref=20.0, flux_axis=1,
+        flux_value=(1.0, 0.0), q0=2000.0, area=0.05, kappa=45.0, rho=7.8e-9, cp=4.6e8,
+        dt0=0.05, n1=1, im=60, tol=1e-10, precision=precision))
+    s = xt.SlabSolver(pr, xt.SlabConfig.make(
+        clamp_axis=1, clamp_value=0.0, load_axis=1, load_value=1.0, load_comp=1,
+        amplitude=100.0, area=0.05, freq=20.0, dt0=0.005, n1=10, nipc=32, im=200, tol=1e-9,
+        maxits=40000, precision=precision, damage=0, overlap=0))
+    s.couple(th, ym0=2.0e5, nu0=0.3, alpha=1.2e-5, Tref=20.0, refactor_every=1)
+    out = []
+    for _ in range(NSLAB):
+        st = s.step()
+        out.append((st, th.temperature(), s.state()["disp"]))
+    s.close()
+    th.close()
+    pr.close()
+    return out
+
+
+def test_coupled_panel_fp64_and_mixed_agree(xt):
+    ref = run(xt, 0)
+    mix = run(xt, 2)
+    for k in range(NSLAB):
+        assert ref[k][0]["relres"] <= 1e-9 and mix[k][0]["relres"] <= 1e-9
+        assert np.linalg.norm(mix[k][1] - ref[k][1]) <= 1e-6 * np.linalg.norm(ref[k][1]), k
+        # the thin panel's stiffness is far worse conditioned than the rod's:
+        # at a 1e-9 residual both solutions sit a few 1e-6 from the exact one
+        assert np.linalg.norm(mix[k][2] - ref[k][2]) <= 1e-5 * np.linalg.norm(ref[k][2]), k
+    assert ref[-1][1].max() > 21.0  # heated

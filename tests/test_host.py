@@ -247,3 +247,28 @@ def test_sent_plate_generator(xt):
         rigid[c::3, c] = 1.0
     assert np.abs(K @ rigid).max() <= 1e-8 * abs(K).max()
     pr.close()
+
+
+def test_holed_panel_generator(xt):
+    """The holed panel's O-grid: positive Jacobians, no unattached node,
+    the hole's area missing from the panel, and the square's edges exact."""
+    from xtfem_gb300.meshes import holed_panel
+
+    xyz, conn = holed_panel(32, 6, 1, W=1.0, t=0.05, radius=0.1)
+    sign = np.array([[-1, -1, 1], [-1, -1, -1], [-1, 1, -1], [-1, 1, 1],
+                     [1, -1, 1], [1, -1, -1], [1, 1, -1], [1, 1, 1]], float)
+    vol = 0.0
+    for e in range(len(conn)):
+        J = (sign / 8.0).T @ xyz[conn[e] - 1]
+        assert np.linalg.det(J) > 0
+        vol += 8 * np.linalg.det(J)
+    assert np.array_equal(np.unique(conn), np.arange(1, len(xyz) + 1))
+    # panel area minus the (polygonal) hole, times the thickness
+    assert abs(vol / 0.05 - (1.0 - np.pi * 0.01)) < 5e-3
+    for axis in (0, 1):
+        for v in (0.0, 1.0):
+            assert (xyz[:, axis] == v).sum() == 2 * 9
+    pr = xt.Problem.from_mesh(xyz, conn)
+    K = pr.K().to_scipy()
+    assert abs(K - K.T).max() <= 1e-10 * abs(K).max()
+    pr.close()

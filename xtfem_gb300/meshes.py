@@ -59,3 +59,43 @@ def sent_plate(nx=48, ny=96, nz=2, W=1.0, H=2.0, t=0.1, notch=0.3, ratio=1.05):
                     continue  # the notch: one row of elements removed
                 conn.append([node(i + (sx > 0), j + (sy > 0), k + (sz > 0)) for sx, sy, sz in _SIGN])
     return xyz, np.array(conn, np.int32)
+
+
+def holed_panel(ntheta=64, nr=12, nz=1, W=1.0, t=0.05, radius=0.1, ratio=1.1):
+    """Square panel W x W x t with a central circular hole of radius
+    radius*W, one O-grid: ntheta elements around the hole (a multiple of 4,
+    the square's corners at 45, 135, 225 and 315 degrees), nr elements from
+    the hole to the outer edge (graded toward the hole, spacing ratio
+    `ratio`), nz through the thickness.  Node (ring j, angle i) sits on the
+    segment from the hole point at angle theta_i to the point where that ray
+    meets the square.  Rings are numbered outermost (bandwidth one ring
+    layer).  Returns (xyz (nn x 3), conn (ne x 8, 1-based))."""
+    if ntheta % 4:
+        raise ValueError("ntheta must be a multiple of 4")
+    c = 0.5 * W
+    th = 2 * np.pi * np.arange(ntheta) / ntheta + np.pi / 4
+    cs, sn = np.cos(th), np.sin(th)
+    inner = np.stack([c + radius * W * cs, c + radius * W * sn], 1)
+    scale = 0.5 * W / np.maximum(np.abs(cs), np.abs(sn))
+    outer = np.stack([c + scale * cs, c + scale * sn], 1)
+    # the square's edges exactly (the ray meets x or y = 0 or W)
+    outer = np.where(np.abs(outer - 0.0) < 1e-12, 0.0, outer)
+    outer = np.where(np.abs(outer - W) < 1e-12, W, outer)
+    s = _graded(0.0, 1.0, nr, ratio, False)  # finest at the hole
+    zs = np.linspace(0.0, t, nz + 1)
+    nzn = nz + 1
+    xyz = np.zeros(((nr + 1) * ntheta * nzn, 3))
+    for j in range(nr + 1):
+        P = inner + s[j] * (outer - inner)
+        for i in range(ntheta):
+            for k in range(nzn):
+                xyz[(j * ntheta + i) * nzn + k] = (P[i, 0], P[i, 1], zs[k])
+
+    def node(j, i, k):
+        return (j * ntheta + (i % ntheta)) * nzn + k + 1
+
+    # local xi along the ray (outward), eta around the hole (counterclockwise),
+    # zeta through the thickness: a right-handed element
+    conn = [[node(j + (sx > 0), i + (sy > 0), k + (sz > 0)) for sx, sy, sz in _SIGN]
+            for k in range(nz) for j in range(nr) for i in range(ntheta)]
+    return xyz, np.array(conn, np.int32)
