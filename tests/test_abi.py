@@ -47,3 +47,35 @@ def test_host_entry_points_validate_arguments(xt):
     assert lib.xth_problem_sizes(None, None, None, None, None) == -10
     assert lib.xt_slab_step(None, None) == -10
     assert lib.xt_system_destroy(None) == 0
+
+
+def test_widened_entry_points_validate_arguments(xt):
+    """The batch, reassembly, thermal, coupling and dump entry points reject
+    null or empty arguments with XT_ERR_ARG before touching a device."""
+    lib = xt.lib()
+    out = ctypes.c_void_p()
+    assert lib.xt_batch_create(0, None, 0, ctypes.byref(out)) == -10
+    assert lib.xt_batch_solve(None, None, None, 30, 1e-8, 100, 0, 1e-5, None, None) == -10
+    assert lib.xt_batch_destroy(None) == 0
+    assert lib.xt_batch_restart(None) == 0
+    assert lib.xt_system_set_mesh(None, 1, 1, None, None, None) == -10
+    assert lib.xt_system_assemble_k(None, None, None) == -10
+    assert lib.xt_system_get_k(None, None, None, None) == -10
+    assert lib.xt_system_k_nnz(None) == 0
+    assert lib.xt_thermal_create(None, None, ctypes.byref(out)) == -10
+    assert lib.xt_thermal_step(None, None) == -10
+    assert lib.xt_thermal_get(None, None) == -10
+    assert lib.xt_thermal_destroy(None) == 0
+    assert lib.xt_slab_couple(None, None, None) == -10
+    assert lib.xt_slab_dump(None, b"job", 1) == -10
+    assert lib.xth_problem_from_mesh(0, 0, None, None, 2e5, 0.3, 7.8e-9, ctypes.byref(out)) == -10
+
+
+def test_problem_from_mesh_rejects_bad_connectivity(xt):
+    import numpy as np
+
+    xyz = np.zeros((8, 3))
+    conn = np.arange(1, 9, dtype=np.int32).reshape(1, 8)
+    conn[0, 3] = 9  # no node 9
+    with pytest.raises(xt.XtError, match="connectivity"):
+        xt.Problem.from_mesh(xyz, conn)
