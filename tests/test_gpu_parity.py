@@ -81,8 +81,12 @@ def rod8_system(xt):
 
 
 ILU_VARIANTS = [
-    {},                                  # defaults: column records, H=1 (FP32); rows S=2 (FP64)
-    {"XTFEM_ILU_SHARES": "2"},
+    {},                                  # defaults: column records, one temporal block per
+                                         # thread block, H=2 (FP32); rows S=2 (FP64)
+    {"XTFEM_ILU_SHARES": "1"},
+    {"XTFEM_ILU_FMT": "2"},              # column records, one pair per thread block
+    {"XTFEM_ILU_FMT": "2", "XTFEM_ILU_SHARES": "2"},
+    {"XTFEM_ILU_FMT": "2", "XTFEM_ILU_RING_KB": "10"},
     {"XTFEM_ILU_WARPS": "1"},            # one compute warp: many passes per level
     {"XTFEM_ILU_WARPS": "3"},
     {"XTFEM_ILU_FMT": "1"},              # node blocks, 3 thread blocks per sweep

@@ -543,18 +543,19 @@ int col_warps(const TriHost& h, int GPW)
 }
 
 int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, StageTri& out,
-                  cudaStream_t s)
+                  cudaStream_t s, int vps = 2)
 {
     out.ok = false;
-    if (h.g != 3 || Q % 2 || (H != 1 && H != 2)) return XT_OK;
+    if (h.g != 3 || (vps != 1 && vps != 2) || Q % vps || (H != 1 && H != 2)) return XT_OK;
     const int g = 3, nl = h.nlevels, GS = 3 * H, GPW = 32 / GS;
     const int ncw = col_warps(h, GPW);
-    const long long win_elems = ((long long)h.nslots + 1) * 6;
+    const int sw = 3 * vps;  // window values per slot: 3 rows x vps temporal blocks
+    const long long win_elems = ((long long)h.nslots + 1) * sw;
     const long long window_bytes = (win_elems * 4 + 15) / 16 * 16;
     const long long ring =
         std::min<long long>((long long)max_dyn_smem() - kHdrBytes - window_bytes, ring_cap()) / 16 * 16;
     if (ring < ring_min() || win_elems >= (1ll << 31)) return XT_OK;
-    const int dummy = h.nslots * 6;
+    const int dummy = h.nslots * sw;
     const unsigned rs = Layout<float>::up16((unsigned)(g * Q * sizeof(float)));
     std::vector<int> tab((size_t)nl * 8, 0);
     std::vector<unsigned> region(nl);
@@ -595,8 +596,8 @@ int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, 
         for (int jj = 0; jj < ng; ++jj) {
             const int j = ord[jj], i = gb + j, G = h.order[i];
             int* gr = reinterpret_cast<int*>(b.data() + 16 + ctab + (size_t)jj * kCgrec);
-            const long long so = (long long)h.slot[G] * 6;
-            valid = valid && so >= 0 && so + 6 <= dummy;
+            const long long so = (long long)h.slot[G] * sw;
+            valid = valid && so >= 0 && so + sw <= dummy;
             gr[0] = (int)so;
             gr[1] = gdst[G];
             gr[2] = j;
@@ -618,8 +619,8 @@ int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, 
                     float v[3] = {0.0f, 0.0f, 0.0f};
                     if (gw < GPW && jj < ng && bi < (int)bn[ord[jj]].size()) {
                         const int j = ord[jj];
-                        const long long wo = (long long)h.slot[bn[j][bi]] * 6 + 2 * col;
-                        valid = valid && wo >= 0 && wo + 2 <= dummy;
+                        const long long wo = (long long)h.slot[bn[j][bi]] * sw + vps * col;
+                        valid = valid && wo >= 0 && wo + vps <= dummy;
                         off = (int)wo;
                         for (int r = 0; r < 3; ++r) v[r] = bv[j][(size_t)bi * 9 + r * 3 + col];
                     }
@@ -1311,6 +1312,101 @@ struct ColBody {
     }
 };
 
+// The same with one temporal block per thread block (Q thread blocks per
+// sweep): the window keeps 3 rows x 1 value per slot, a lane gathers one
+// FP32 value per step and adds three scalar FMAs.
+template <int Q, int H, bool UPPER>
+struct ColBody1 {
+    static constexpr int GS = 3 * H, GPW = 32 / GS;
+    int lane, gw, col, hh, lane0, warp, ncw, tb;
+    bool lane_ok;
+    unsigned rsE;
+    float* out;
+    __device__ ColBody1(const StageArgs<float>& a)
+    {
+        lane = threadIdx.x & 31;
+        warp = threadIdx.x >> 5;
+        ncw = a.ncw;
+        gw = lane / GS;
+        const int inl = lane - gw * GS;
+        col = inl / H;
+        hh = inl - col * H;
+        lane0 = gw * GS;
+        lane_ok = gw < GPW;
+        tb = blockIdx.x;
+        rsE = a.rs / (unsigned)sizeof(float);
+        out = a.out;
+    }
+    template <bool RING>
+    __device__ __forceinline__ void level(float* win, const unsigned char* base, const float* rh,
+                                          int ng, int npass)
+    {
+        const int nchunk = reinterpret_cast<const int*>(base)[2];
+        const int2* chunks = reinterpret_cast<const int2*>(base + 16);
+        const unsigned char* grec = base + 16 + (((size_t)npass * ncw * 8 + 15) & ~(size_t)15);
+        for (int k = 0; k < npass; ++k) {
+            const int c = k * ncw + warp;
+            if (c >= nchunk) break;  // warp-uniform
+            const int2 cd = chunks[c];
+            const float4* rp = reinterpret_cast<const float4*>(base + (size_t)cd.x * 16) + lane;
+            const int jj = c * GPW + gw;
+            const bool fin = lane_ok && hh == 0 && jj < ng;
+            int gslot = 0, gdst = 0;
+            float mv[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
+            if (fin) {
+                const int* gr = reinterpret_cast<const int*>(grec + (size_t)jj * kCgrec);
+                gslot = gr[0];
+                gdst = gr[1];
+                const float* m = reinterpret_cast<const float*>(gr + 3) + col * 3;
+                const float* rr = rh + (size_t)gr[2] * rsE + tb;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    mv[r] = m[r];
+                    bb[r] = rr[r * Q];
+                }
+            }
+            float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll 4
+            for (int st = 0; st < cd.y; ++st) {
+                const float4 rec = rp[(size_t)st * 32];
+                const float x = win[__float_as_int(rec.x)];
+                acc[0] = fmaf(rec.y, x, acc[0]);
+                acc[1] = fmaf(rec.z, x, acc[1]);
+                acc[2] = fmaf(rec.w, x, acc[2]);
+            }
+#pragma unroll
+            for (int m = 1; m < H; m <<= 1)
+#pragma unroll
+                for (int r = 0; r < 3; ++r) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], m);
+            float tot[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                tot[r] = (__shfl_sync(0xffffffffu, acc[r], lane0) +
+                          __shfl_sync(0xffffffffu, acc[r], lane0 + H)) +
+                         __shfl_sync(0xffffffffu, acc[r], lane0 + 2 * H);
+            if (fin) {
+                float sol = 0.0f;
+#pragma unroll
+                for (int r = 0; r < 3; ++r) sol = fmaf(mv[r], bb[r] - tot[r], sol);
+                win[gslot + col] = sol;
+                float* go = UPPER ? out + (size_t)(gdst + col) * Q + tb
+                                  : out + (size_t)gdst * rsE + col * Q + tb;
+                *go = sol;
+            }
+        }
+    }
+};
+
+template <int Q, int H, bool UPPER>
+__global__ void __launch_bounds__(kStageThreads, 1) k_tri_col1(StageArgs<float> a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    // the padding slot reads as zero (ordered by the set-up barrier)
+    if (threadIdx.x < 3) reinterpret_cast<float*>(smem + kHdrBytes)[a.aux + threadIdx.x] = 0.0f;
+    ColBody1<Q, H, UPPER> body(a);
+    stage_main<float>(a, body, smem);
+}
+
 template <int Q, int H, bool UPPER>
 __global__ void __launch_bounds__(kStageThreads, 1) k_tri_col(StageArgs<float> a)
 {
@@ -1343,10 +1439,11 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
     out = nullptr;
     if (!F.sched || env_int("XTFEM_ILU_SIMPLE", 0)) return XT_OK;
     // the column format's layout depends on the shares and the warp count
-    const int wenv = fmt == 2 ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
+    const bool col = fmt == 2 || fmt == 3;
+    const int wenv = col ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
     const int rkb = std::max(0, std::min(255, env_int("XTFEM_ILU_RING_KB", 0)));
     const int key =
-        ((((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (fmt == 2 ? H : 0)) * 64 + wenv) * 256 + rkb;
+        ((((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (col ? H : 0)) * 64 + wenv) * 256 + rkb;
     auto it = F.stages.find(key);
     if (it == F.stages.end()) {
         auto st = std::make_shared<IluStage>();
@@ -1359,10 +1456,11 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
             gdL[G] = U.pos[G];
             gdU[G] = G * g;
         }
-        if (fmt == 2) {
+        if (fmt == 2 || fmt == 3) {
             if (sizeof(T) == 4) {
-                XT_TRY(build_col_tri(L, q, H, gdL, st->L, s));
-                XT_TRY(build_col_tri(U, q, H, gdU, st->U, s));
+                const int vps = fmt == 2 ? 2 : 1;
+                XT_TRY(build_col_tri(L, q, H, gdL, st->L, s, vps));
+                XT_TRY(build_col_tri(U, q, H, gdU, st->U, s, vps));
             }
         } else if (fmt == 1) {
             if (sizeof(T) == 4) {
@@ -1454,12 +1552,32 @@ int launch_cols(const DevIlu& F, const IluStage& st, const double* dAinv, const 
                                k_tri_col<Q, H, true>, attr, dAinv, v, z, s, Q / 2);
 }
 
+template <int Q, int H>
+int launch_cols1(const DevIlu& F, const IluStage& st, const double* dAinv, const float* v,
+                 float* z, cudaStream_t s)
+{
+    static std::atomic<bool> attr{false};
+    return run_stage<float, Q>(F, st, ColBody1<Q, H, false>::GPW, k_tri_col1<Q, H, false>,
+                               k_tri_col1<Q, H, true>, attr, dAinv, v, z, s, Q);
+}
+
 template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
 {
     IluStage* st = nullptr;
     if constexpr (sizeof(T) == 4 && Q % 2 == 0) {
-        const int fmt = env_int("XTFEM_ILU_FMT", 2);
+        // 3 (default): column records, one temporal block per thread block;
+        // 2: column records, one pair per thread block; 1: node blocks;
+        // 0: rows
+        const int fmt = env_int("XTFEM_ILU_FMT", 3);
+        if (F.L.g == 3 && fmt == 3) {
+            const int H = env_int("XTFEM_ILU_SHARES", 2) == 1 ? 1 : 2;
+            XT_TRY(get_stage<T>(F, Q, 3, s, st, H));
+            if (st) {
+                if (H == 1) return launch_cols1<Q, 1>(F, *st, dAinv, v, z, s);
+                return launch_cols1<Q, 2>(F, *st, dAinv, v, z, s);
+            }
+        }
         if (F.L.g == 3 && fmt == 2) {
             const int H = env_int("XTFEM_ILU_SHARES", 1) == 2 ? 2 : 1;
             XT_TRY(get_stage<T>(F, Q, 2, s, st, H));
