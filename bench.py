@@ -156,16 +156,16 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6, merged=True):
 # DRAM bytes per launch of the kernel classes, from one ncu capture each on
 # this workload (profiles/): dram__bytes_read.sum + dram__bytes_write.sum.
 # ilu_apply_fp32 = its forward and backward sweep kernels (the 6 us
-# right-hand-side pre-pass is not included; three thread blocks read each
-# sweep's blob, DRAM serves it once).  kron_spmm_df = the node-block
+# right-hand-side pre-pass is not included; the six thread blocks of a sweep
+# read its blob, DRAM serves it once).  kron_spmm_df = the node-block
 # kernel, which reads K as 3 x 3 blocks and M as one scalar per block (its
 # algorithmic bytes are counted for the CSR operands, as for the others).
-NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 23_705_600 + 22_351_104,
+NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 23_080_960 + 22_542_336,
                4: 99_808_256 + 41_192_960, 7: 57_748_992 + 28_160}
 
 ROOFLINE_NOTES = {
-    3: "level-scheduled triangular sweeps: 764 + 743 dependent levels, each sweep on one SM per "
-       "temporal-block pair; bound by per-level shared-memory latency and barriers, not by HBM "
+    3: "level-scheduled triangular sweeps: 764 + 743 dependent levels, each sweep on six SMs, one "
+       "per temporal block; bound by per-level shared-memory latency and barriers, not by HBM "
        "(DRAM at 0.5 % of peak under ncu); roofline_streaming gives the HBM-bound kernel",
 }
 
