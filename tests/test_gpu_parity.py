@@ -3,7 +3,7 @@
 Tolerances (relative to the oracle's FP64 result):
   * Kronecker apply (FP64):           1e-12 in the max norm
   * preconditioner apply (FP64):      1e-10
-  * GMRES solution, both to 1e-10:    1e-6 relative L2 (BASELINE parity bar)
+  * GMRES solution, both to 1e-10:    1e-6 relative L2 (the parity bar)
   * damage state over a slab:         1e-6 absolute on D, 1e-8 relative on
                                       the stress/strain state
 Integer outputs (failed-element lists, status flags) must be identical.
