@@ -235,7 +235,8 @@ int xt_system_get_k(xt_system s, int *ia, int *ja, double *kv);
  * dependent chain on three SMs) and their bandwidth-bound kernels run at
  * the same time on different SMs.  The systems stay owned by the caller
  * and must outlive the batch; a system must not be used elsewhere while a
- * batch solve runs.  workers <= 0 picks min(count, 16). */
+ * batch solve runs, nor be listed twice (XT_ERR_ARG).  workers <= 0 picks
+ * min(count, 16). */
 typedef struct xt_batch_s *xt_batch;
 
 int xt_batch_create(int count, const xt_system *systems, int workers, xt_batch *out);

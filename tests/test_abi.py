@@ -55,6 +55,9 @@ def test_widened_entry_points_validate_arguments(xt):
     lib = xt.lib()
     out = ctypes.c_void_p()
     assert lib.xt_batch_create(0, None, 0, ctypes.byref(out)) == -10
+    twice = (ctypes.c_void_p * 2)(0x1000, 0x1000)  # never dereferenced: rejected first
+    assert lib.xt_batch_create(2, twice, 0, ctypes.byref(out)) == -10
+    assert b"twice" in lib.xt_last_error()
     assert lib.xt_batch_solve(None, None, None, 30, 1e-8, 100, 0, 1e-5, None, None) == -10
     assert lib.xt_batch_destroy(None) == 0
     assert lib.xt_batch_restart(None) == 0

@@ -394,6 +394,14 @@ int xt_batch_create(int count, const xt_system* systems, int workers, xt_batch* 
     *out = nullptr;
     for (int i = 0; i < count; ++i)
         if (!systems[i]) { set_error("xt_batch_create: null system"); return XT_ERR_ARG; }
+    {  // one worker per system at a time: a system listed twice would race
+        std::vector<xt_system> sorted(systems, systems + count);
+        std::sort(sorted.begin(), sorted.end());
+        if (std::adjacent_find(sorted.begin(), sorted.end()) != sorted.end()) {
+            set_error("xt_batch_create: a system is listed twice");
+            return XT_ERR_ARG;
+        }
+    }
     XT_TRY(ensure_init());
     auto b = std::make_unique<xt_batch_s>();
     b->sys.assign(systems, systems + count);
