@@ -11,10 +11,25 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Host threads for the Kronecker apply, the preconditioner and the Krylov
+ * vector operations.  1 (the default) runs the reference's serial code
+ * order; above 1 the same arithmetic per entry runs under OpenMP (rows of
+ * each amux pass, the q independent lusol calls, rows of the block mixing
+ * and of every vector update), and only the dot products and norms change
+ * their summation order (per-thread partial sums).  This is the threaded
+ * CPU baseline; the reference itself has no threading on this path. */
+static int g_threads = 1;
+
+void orc_set_threads(int n) { g_threads = n > 1 ? n : 1; }
+
+int orc_get_threads(void) { return g_threads; }
+
 /* src/ilut.f:3-44.  Row-by-row CSR product, 1-based ia/ja. */
 void orc_amux(int n, const double *x, double *y, const double *a,
               const int *ja, const int *ia)
 {
+    const int nt = g_threads;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
     for (int r = 0; r < n; ++r) {
         double acc = 0.0;
         for (int k = ia[r] - 1; k < ia[r + 1] - 1; ++k)
@@ -28,6 +43,17 @@ void orc_amux(int n, const double *x, double *y, const double *a,
 static void block_mix_add(const double *c, int q, int p, const double *u,
                           double *y)
 {
+    const int nt = g_threads;
+    if (nt > 1) {
+        /* the same q*q updates of each entry, in the same order */
+#pragma omp parallel for schedule(static) num_threads(nt)
+        for (int r = 0; r < p; ++r)
+            for (int i = 0; i < q; ++i)
+                for (int j = 0; j < q; ++j)
+                    y[(size_t)i * p + r] = y[(size_t)i * p + r] +
+                                           c[j * q + i] * u[(size_t)j * p + r];
+        return;
+    }
     for (int i = 0; i < q; ++i)
         for (int j = 0; j < q; ++j) {
             const double cij = c[j * q + i];
@@ -66,7 +92,9 @@ void orc_kronspgemv(const double *a, const double *b, double alpha,
     const size_t n = (size_t)p * q;
     double *z = (double *)malloc(n * sizeof(double));
     orc_kronspmv(a, b, q, ki, kj, kv, mi, mj, mv, p, x, z);
-    for (size_t r = 0; r < n; ++r)
+    const int nt = g_threads;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (long long r = 0; r < (long long)n; ++r)
         y[r] = alpha * z[r] + beta * y[r];
     free(z);
 }
@@ -145,6 +173,8 @@ int orc_kronlusol(const double *a, int q, const double *alu, const int *jlu,
     double inva[64 * 64];
     if (q > 64 || orc_inverse(q, a, inva) != 0) return 1;
     double *w = (double *)calloc(n, sizeof(double));
+    const int nt = g_threads < q ? g_threads : q;
+#pragma omp parallel for schedule(static, 1) num_threads(nt) if (nt > 1)
     for (int i = 0; i < q; ++i)
         orc_lusol(p, x + (size_t)i * p, w + (size_t)i * p, alu, jlu, ju);
     memset(y, 0, n * sizeof(double));
@@ -153,20 +183,51 @@ int orc_kronlusol(const double *a, int q, const double *alu, const int *jlu,
     return 0;
 }
 
+static double ddot(size_t n, const double *x, const double *y)
+{
+    const int nt = g_threads;
+    double s = 0.0;
+    if (nt > 1) {
+        const long long nn = (long long)n;
+#pragma omp parallel for schedule(static) num_threads(nt) reduction(+ : s)
+        for (long long i = 0; i < nn; ++i) s += x[i] * y[i];
+        return s;
+    }
+    for (size_t i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+
 static double dnrm2(size_t n, const double *x)
 {
     /* Plain two-norm; BLAS dnrm2 scales to avoid overflow, which changes
      * nothing at the magnitudes of this path. */
-    double s = 0.0;
-    for (size_t i = 0; i < n; ++i) s += x[i] * x[i];
-    return sqrt(s);
+    return sqrt(ddot(n, x, x));
 }
 
-static double ddot(size_t n, const double *x, const double *y)
+/* The vector updates of kronpgmres, one expression per entry as in the
+ * reference; rows in parallel when threaded. */
+static void vscal(size_t n, double *y, double t)          /* y = y*t */
 {
-    double s = 0.0;
-    for (size_t i = 0; i < n; ++i) s += x[i] * y[i];
-    return s;
+    const int nt = g_threads;
+    const long long nn = (long long)n;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (long long i = 0; i < nn; ++i) y[i] *= t;
+}
+
+static void vaxpy(size_t n, double *y, double t, const double *x)  /* y += t*x */
+{
+    const int nt = g_threads;
+    const long long nn = (long long)n;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (long long i = 0; i < nn; ++i) y[i] += t * x[i];
+}
+
+static void vcopy_scaled(size_t n, double *y, const double *x, double t)  /* y = x*t */
+{
+    const int nt = g_threads;
+    const long long nn = (long long)n;
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+    for (long long i = 0; i < nn; ++i) y[i] = x[i] * t;
 }
 
 /* src/kronecker.f90:181-365.  The control flow (labels 20, 4, 58, 121,
@@ -194,13 +255,19 @@ int orc_kronpgmres(const double *a, const double *b, int q,
     const double ro0 = dnrm2(n, rhs);
 
     orc_kronspmv(a, b, q, ki, kj, kv, mi, mj, mv, p, sol, V(0));
-    for (size_t r = 0; r < n; ++r) V(0)[r] = rhs[r] - V(0)[r];
+    {
+        const int nt = g_threads;
+        const long long nn = (long long)n;
+        double *v0 = V(0);
+#pragma omp parallel for schedule(static) num_threads(nt) if (nt > 1)
+        for (long long r = 0; r < nn; ++r) v0[r] = rhs[r] - v0[r];
+    }
 
     for (;;) {                                   /* label 20 */
         ro = dnrm2(n, V(0));
         if (ro == 0.0) { ierr = -1; break; }
         t = 1.0 / ro;
-        for (size_t r = 0; r < n; ++r) V(0)[r] *= t;
+        vscal(n, V(0), t);
         if (its == 0) eps1 = eps * ro;
         rs[0] = ro;
         i = 0;
@@ -215,13 +282,13 @@ int orc_kronpgmres(const double *a, const double *b, int q,
             for (int j = 1; j <= i; ++j) {       /* modified Gram-Schmidt */
                 t = ddot(n, V(j - 1), V(i1 - 1));
                 HH(j - 1, i - 1) = t;
-                for (size_t r = 0; r < n; ++r) V(i1 - 1)[r] += -t * V(j - 1)[r];
+                vaxpy(n, V(i1 - 1), -t, V(j - 1));
             }
             t = dnrm2(n, V(i1 - 1));
             HH(i1 - 1, i - 1) = t;
             if (t != 0.0) {
                 t = 1.0 / t;
-                for (size_t r = 0; r < n; ++r) V(i1 - 1)[r] *= t;
+                vscal(n, V(i1 - 1), t);
             }
             for (int k = 2; k <= i; ++k) {       /* label 58 */
                 const int k1 = k - 1;
@@ -253,13 +320,13 @@ int orc_kronpgmres(const double *a, const double *b, int q,
         }
         /* linear combination of the basis, preconditioner, update */
         t = rs[0];
-        for (size_t r = 0; r < n; ++r) rhs[r] = V(0)[r] * t;
+        vcopy_scaled(n, rhs, V(0), t);
         for (int j = 2; j <= i; ++j) {
             t = rs[j - 1];
-            for (size_t r = 0; r < n; ++r) rhs[r] = rhs[r] + t * V(j - 1)[r];
+            vaxpy(n, rhs, t, V(j - 1));
         }
         if (orc_kronlusol(a, q, alu, jlu, ju, p, rhs, rhs)) { ierr = 2; break; }
-        for (size_t r = 0; r < n; ++r) sol[r] = sol[r] + rhs[r];
+        vaxpy(n, sol, 1.0, rhs);
         if (ro <= eps1) { ierr = 0; break; }
         if (its >= maxits) { ierr = 1; break; }
         /* residual of the restart from the Givens data */
@@ -273,7 +340,7 @@ int orc_kronpgmres(const double *a, const double *b, int q,
             for (int j = 1; j <= i1; ++j) {
                 t = rs[j - 1];
                 if (j == 1) t = t - 1.0;
-                for (size_t r = 0; r < n; ++r) V(0)[r] += t * V(j - 1)[r];
+                vaxpy(n, V(0), t, V(j - 1));
             }
         }
     }

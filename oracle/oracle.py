@@ -8,7 +8,7 @@ the product never imports it.
 Parity pinning: the reference ships no tests or golden vectors for this path
 and cannot be built here, so parity is unpinned by the reference's own
 tests; the oracle is validated by invariants and independent statements in
-tests/test_oracle.py.
+tests/test_host.py.
 """
 from __future__ import annotations
 
@@ -40,6 +40,8 @@ def lib():
             build()
         L = C.CDLL(str(LIB))
         sig = {
+            "orc_set_threads": (None, [C.c_int]),
+            "orc_get_threads": (C.c_int, []),
             "orc_amux": (None, [C.c_int, _dp, _dp, _dp, _ip, _ip]),
             "orc_kronspmv": (None, [_dp, _dp, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp, C.c_int,
                                     _dp, _dp]),
@@ -82,6 +84,16 @@ def _i(a):
 def _cm(m):
     m = np.asarray(m, dtype=np.float64)
     return np.ascontiguousarray(m.reshape(-1, order="F")) if m.ndim == 2 else m
+
+
+def set_threads(n):
+    """Host threads for amux, kronspmv, kronlusol and kronpgmres (1, the
+    default, is the reference's serial order bit for bit)."""
+    lib().orc_set_threads(int(n))
+
+
+def get_threads():
+    return lib().orc_get_threads()
 
 
 def amux(K, x):

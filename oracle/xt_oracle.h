@@ -25,6 +25,13 @@
 extern "C" {
 #endif
 
+/* Host threads for amux, kronspmv/kronspgemv, kronlusol and kronpgmres
+ * (default 1: the reference's serial order, bit for bit).  Above 1 the
+ * per-entry arithmetic is unchanged and only the dot products and norms of
+ * kronpgmres sum in another order; this is the threaded CPU baseline. */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
 /* src/ilut.f:3-44  amux: y = A x for CSR A (1-based). */
 void orc_amux(int n, const double *x, double *y, const double *a,
               const int *ja, const int *ia);

@@ -163,6 +163,34 @@ def test_oracle_gmres_reaches_direct_solution(orc, c1):
     assert np.linalg.norm(sol - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
 
 
+def test_oracle_threaded_path_matches_serial(orc, c1):
+    """The threaded CPU baseline does the serial oracle's work: the Kronecker
+    apply and the preconditioner are bit-identical (the same expression per
+    entry), and GMRES, whose dot products sum in another order, reaches the
+    same solution."""
+    (alu, jlu, ju), _ = orc.ilut(c1["K"], 20, 1e-4)
+    rng = np.random.default_rng(6)
+    x, y0, rhs = rng.standard_normal((3, c1["K"].n * 6))
+    args = (c1["A"], c1["B"], c1["K"], c1["M"])
+    assert orc.get_threads() == 1
+
+    def run():
+        return (orc.kronspgemv(*args[:2], -0.5, 2.0, *args[2:], x, y0),
+                orc.kronlusol(c1["A"], alu, jlu, ju, x),
+                orc.kronpgmres(*args, alu, jlu, ju, rhs, im=30, eps=1e-12, maxits=3000))
+
+    ser = run()
+    try:
+        orc.set_threads(4)
+        par = run()
+    finally:
+        orc.set_threads(1)
+    assert np.array_equal(par[0], ser[0]) and np.array_equal(par[1], ser[1])
+    (s0, e0, i0, _), (s1, e1, i1, _) = ser[2], par[2]
+    assert e0 == e1 == 0 and abs(i0 - i1) <= 2
+    assert np.linalg.norm(s1 - s0) <= 1e-9 * np.linalg.norm(s0)
+
+
 # ------------------------------------------------------------- temporal basis
 def test_stcoeff_closed_forms_match_quadrature(xt, orc):
     """The closed forms keep the reference's default-real (single-precision)
