@@ -191,6 +191,51 @@ def test_oracle_threaded_path_matches_serial(orc, c1):
     assert np.linalg.norm(s1 - s0) <= 1e-9 * np.linalg.norm(s0)
 
 
+# ------------------------------------------------------------- deletion surgery
+def test_deletion_surgery_equals_assembly_of_surviving_elements(xt):
+    """delelement / chkcnsta / chkndsta / adddiagonal (src/delelement.f90:
+    1-59, 139-247) on the host: after deleting a corner element (whose far
+    corner node then belongs to no element) and an interior one, K equals
+    the assembly of the surviving elements with the boundary conditions of
+    the clamped face plus the disconnected node, M equals the original mass
+    matrix under the new conditions, and the disconnected node's three DOFs
+    are now fixed.  Element integrals are restated in numpy."""
+    from test_gpu_assembly import element_k
+    from test_gpu_thermal import applybc
+
+    pr = rod_problem(xt, 6, 2, 2)
+    xyz, conn = pr.mesh()
+    nn, ne = len(xyz), len(conn)
+    M0 = pr.M().to_scipy()
+    bc = clamp_mask(xyz)
+    pr.apply_bc(bc)
+    far = np.flatnonzero(np.all(xyz == [3.0, 1.0, 1.0], axis=1))[0]
+    corner = next(e for e in range(ne) if far + 1 in conn[e])
+    nefail = np.array(sorted([corner + 1, ne // 2 + 1]), np.int32)
+    bc_new = bc.copy()
+    ndf = pr.delete(nefail, bc_new)
+    keep = np.setdiff1d(np.arange(ne), nefail - 1)
+    alive = np.zeros(nn, bool)
+    alive[conn[keep].ravel() - 1] = True
+    assert ndf == int((~alive).sum()) == 1 and not alive[far]
+    expect_bc = bc.copy()
+    expect_bc[np.repeat(~alive, 3)] = 1
+    assert np.array_equal(bc_new, expect_bc)
+    rows, cols, vals = [], [], []
+    for e in keep:
+        dofs = (3 * (conn[e] - 1)[:, None] + np.arange(3)).ravel()
+        rows += list(np.repeat(dofs, 24)); cols += list(np.tile(dofs, 24))
+        vals += list(element_k(xyz[conn[e] - 1], np.full(8, 2.0e5), np.full(8, 0.3)).ravel())
+    Ks = sp.csr_matrix((vals, (rows, cols)), shape=(3 * nn, 3 * nn))
+    K_exp, M_exp = applybc(Ks, expect_bc), applybc(M0, expect_bc)
+    K, M = pr.K().to_scipy(), pr.M().to_scipy()
+    assert abs(K - K_exp).max() <= 1e-10 * abs(K_exp).max()
+    assert abs(M - M_exp).max() <= 1e-14 * abs(M_exp).max()
+    with pytest.raises(RuntimeError):
+        pr.delete(np.array([ne + 1], np.int32), bc_new)
+    pr.close()
+
+
 # ------------------------------------------------------------- temporal basis
 def test_stcoeff_closed_forms_match_quadrature(xt, orc):
     """The closed forms keep the reference's default-real (single-precision)
