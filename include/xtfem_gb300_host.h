@@ -70,6 +70,9 @@ void xth_stcoeff_t(double dt, double *k, double *m, double *ktn, double *mtn,
 /* src/getfextc.f90:22-58 */
 void xth_getfextc_m(double t1, double w, double dt, double *fextc,
                     double *fint);
+/* src/getfextc.f90:1-20: the thermal load weights fextc[3] of the slab
+ * [t1, t1+dt] (load period 24, w = 2 * 3.14159 / 24 as in the reference). */
+void xth_getfextc_t(double t1, double dt, double *fextc);
 /* src/kokkos_damage.f90:36-47 temporal shape table Nt[jj*6+k]. */
 void xth_nt_table(int nip, const double *tcoorde, double w, double *nt);
 

@@ -62,6 +62,8 @@ def lib():
             "orc_chkelesta": (C.c_int, [C.c_int, C.c_int, C.c_double, _dp, _ip, _ip, _ip]),
             "orc_stcoeff_m_quad": (None, [C.c_double, C.c_double, C.c_double] + [_dp] * 6),
             "orc_getfextc_m_quad": (None, [C.c_double, C.c_double, C.c_double, _dp]),
+            "orc_stcoeff_t_quad": (None, [C.c_double] + [_dp] * 6),
+            "orc_fint_m_def": (None, [C.c_double, C.c_double, C.c_double, _dp]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -238,4 +240,16 @@ def stcoeff_m_quad(t1, dt, w):
 def getfextc_m_quad(t1, w, dt):
     f = np.zeros(6)
     lib().orc_getfextc_m_quad(t1, w, dt, f.ctypes.data_as(_dp))
+    return f
+
+
+def stcoeff_t_quad(dt):
+    mats = [np.zeros(9) for _ in range(6)]
+    lib().orc_stcoeff_t_quad(dt, *[m.ctypes.data_as(_dp) for m in mats])
+    return [m.reshape(3, 3, order="F") for m in mats]
+
+
+def fint_m_def(t1, w, dt):
+    f = np.zeros(6)
+    lib().orc_fint_m_def(t1, w, dt, f.ctypes.data_as(_dp))
     return f

@@ -20,6 +20,13 @@
  * functions at the end of the same slab, which is how the reference's closed
  * forms are written (its column terms carry sin/cos of (t1+dt) w).
  *
+ * The thermal slab (src/stcoeff.f90:1-60) uses the three quadratic
+ * Lagrange functions alone, first order in time:
+ *   k(i,j)    = int N_i(t) N_j(t) dt        (with the conductivity)
+ *   m(i,j)    = int N_i(t) N_j'(t) dt       (with the capacity)
+ *   mtn(i,j)  = N_i(t1) N_j(t1),  mtn1(i,j) = N_i(t1) N_j(t1+dt)
+ *   ktn = ktn1 = 0
+ *
  * TEST INFRASTRUCTURE ONLY (the checker); see xt_oracle.h.
  */
 #include "xt_oracle.h"
@@ -108,4 +115,38 @@ void orc_getfextc_m_quad(double t1, double w, double dt, double *fextc)
                 fextc[j] += wt * basis(j, t, t1, dt, w).d1 * sin(w * t);
         }
     }
+}
+
+void orc_stcoeff_t_quad(double dt, double *k, double *m, double *ktn,
+                        double *mtn, double *ktn1, double *mtn1)
+{
+    for (int e = 0; e < 9; ++e) k[e] = m[e] = ktn[e] = mtn[e] = ktn1[e] = mtn1[e] = 0.0;
+    const double h = dt / NSUB;
+    for (int s = 0; s < NSUB; ++s) {
+        const double c = (s + 0.5) * h;
+        for (int g = 0; g < 8; ++g) {
+            const double t = c + 0.5 * h * GX[g];
+            const double wt = 0.5 * h * GW[g];
+            jet B[3];
+            for (int a = 0; a < 3; ++a) B[a] = basis(a, t, 0.0, dt, 0.0);
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    k[j * 3 + i] += wt * B[i].v * B[j].v;
+                    m[j * 3 + i] += wt * B[i].v * B[j].d1;
+                }
+        }
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const jet Si = basis(i, 0.0, 0.0, dt, 0.0);
+            mtn[j * 3 + i] = Si.v * basis(j, 0.0, 0.0, dt, 0.0).v;
+            mtn1[j * 3 + i] = Si.v * basis(j, dt, 0.0, dt, 0.0).v;
+        }
+}
+
+void orc_fint_m_def(double t1, double w, double dt, double *fint)
+{
+    /* int N_j'(t) dt over the slab = N_j(t1+dt) - N_j(t1), exactly */
+    for (int j = 0; j < 6; ++j)
+        fint[j] = basis(j, t1 + dt, t1, dt, w).v - basis(j, t1, t1, dt, w).v;
 }

@@ -117,6 +117,16 @@ void orc_stcoeff_m_quad(double t1, double dt, double w, double *k, double *m,
  * dN_j/dt * sin(w t) over the slab. */
 void orc_getfextc_m_quad(double t1, double w, double dt, double *fextc);
 
+/* src/stcoeff.f90:1-60 by definition (quadrature of the quadratic Lagrange
+ * products): the thermal k, m, ktn, mtn, ktn1, mtn1 (3x3, column-major). */
+void orc_stcoeff_t_quad(double dt, double *k, double *m, double *ktn,
+                        double *mtn, double *ktn1, double *mtn1);
+
+/* By definition: fint[j] = integral of dN_j/dt over the slab for the six
+ * mechanical basis functions (the thermal-stress load weights whose closed
+ * forms are src/getfextc.f90:53-58). */
+void orc_fint_m_def(double t1, double w, double dt, double *fint);
+
 #ifdef __cplusplus
 }
 #endif

@@ -247,9 +247,31 @@ def test_stcoeff_closed_forms_match_quadrature(xt, orc):
         ref = orc.stcoeff_m_quad(t1, dt, w)
         for g, r in zip(got, ref):
             assert np.abs(g - r).max() <= 1e-7 * max(np.abs(r).max(), 1e-30)
-        f, _ = xt.getfextc_m(t1, w, dt)
+        f, fint = xt.getfextc_m(t1, w, dt)
         fr = orc.getfextc_m_quad(t1, w, dt)
         assert np.abs(f - fr).max() <= 1e-9 * np.abs(fr).max()
+        # the thermal-stress weights: int N_j' dt for the first five basis
+        # functions; the reference's sixth weight (src/getfextc.f90:58) is
+        # sin(w(t1+dt)) - sin(w t1), not the definition's 0, and is kept
+        fd = orc.fint_m_def(t1, w, dt)
+        assert np.abs(fint[:5] - fd[:5]).max() <= 1e-12 and abs(fd[5]) <= 1e-12
+        assert fint[5] == -np.sin(t1 * w) + np.sin(w * (t1 + dt))
+
+
+def test_thermal_stcoeff_and_load_match_quadrature(xt, orc):
+    """The thermal temporal matrices (src/stcoeff.f90:1-60) against the
+    quadrature of the quadratic Lagrange products (to single-precision
+    rounding: the reference's fractions are default-real literals), and the
+    thermal load weights (src/getfextc.f90:1-20) against the integral of
+    dN_j/dt sin(w t) with the reference's w = 2 * 3.14159 / 24."""
+    wt = 2 * 3.14159 / 24
+    for dt in (0.5, 0.05, 3.0):
+        got, ref = xt.stcoeff_t(dt), orc.stcoeff_t_quad(dt)
+        for g, r in zip(got, ref):
+            assert np.abs(g - r).max() <= 1e-7 * max(np.abs(r).max(), 1e-30)
+        for t1 in (0.0, 1.5, 7.0):
+            f, fr = xt.getfextc_t(t1, dt), orc.getfextc_m_quad(t1, wt, dt)[:3]
+            assert np.abs(f - fr).max() <= 1e-9 * np.abs(fr).max()
 
 
 # ------------------------------------------------------------- damage / deletion

@@ -25,7 +25,7 @@ from ._lib import XtError, _dp, check, dptr, dref, iptr, iref, lib
 
 __all__ = [
     "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "chkelesta", "kokkos_host",
-    "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "nt_table", "SpaceTimeSystem",
+    "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "getfextc_t", "nt_table", "SpaceTimeSystem",
     "SystemBatch", "ThermalConfig", "ThermalSolver",
     "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
 ]
@@ -213,6 +213,13 @@ def getfextc_m(t1, w, dt):
     f, g = np.zeros(6), np.zeros(6)
     lib().xth_getfextc_m(t1, w, dt, dptr(f), dptr(g))
     return f, g
+
+
+def getfextc_t(t1, dt):
+    """Thermal load weights of the slab [t1, t1+dt] (src/getfextc.f90:1-20)."""
+    f = np.zeros(3)
+    lib().xth_getfextc_t(t1, dt, dptr(f))
+    return f
 
 
 def nt_table(nip, tcoorde, w):

@@ -281,6 +281,11 @@ void xth_getfextc_m(double t1, double w, double dt, double* fextc, double* fint)
     getfextc_m(t1, w, dt, fextc, fint);
 }
 
+void xth_getfextc_t(double t1, double dt, double* fextc)
+{
+    getfextc_t(t1, dt, fextc);
+}
+
 void xth_nt_table(int nip, const double* tcoorde, double w, double* nt)
 {
     nt_table(nip, tcoorde, w, nt);
