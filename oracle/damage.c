@@ -1,7 +1,8 @@
 /*
  * damage.c -- oracle restatement of the two-scale fatigue-damage update
  * (src/kokkos_kernel.h:45-344 with constants src/damage.h:9-17), of the
- * temporal shape table built by src/kokkos_damage.f90:36-47, of the
+ * temporal shape table built by src/kokkos_damage.f90:36-47, a second
+ * statement of the same law after src/getdfinal.f:10-397, of the
  * failed-point clean-up src/kokkos_damage.f90:102-107 and of the element
  * status test chkelesta (src/delelement.f90:109-136).
  *
@@ -252,6 +253,117 @@ void orc_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
         damage_point(gp, nn, ndofn, nnse, nnte, ncmp, nip, nodes, Nx, Ny, Nz,
                      Nt, sol, ym, nu, eps_old, eps_pl, sig_eff, sig_back, p,
                      D, ws, del_po, sig_d);
+}
+
+/* src/getdfinal.f:10-397, the reference's second (stand-alone, F77)
+ * statement of the same two-scale law: one strain increment per call, from
+ * the previous global strain strain_tgo to strain_tg.  It is written here
+ * independently of damage_point above, following getdfinal's own steps:
+ * the elastic stiffness from the Lame constants (lambda + 2G, lambda, G),
+ * the localisation constants a, b, the bulk modulus in the plastic
+ * corrector, and the equivalent stress 1.5 (sum s_n^2 + 2 sum s_s^2).  The
+ * reference hard-codes E = 1.97e5 and nu = 0.3 and takes dmat from its
+ * caller; here E and nu are arguments (the per-point override), so both
+ * statements can be run on the same point. */
+static void getdfinal_step(const double eg[6], double ego[6], double epl[6],
+                           double *p, double *D, double *ws, double se[6],
+                           double bs[6], double *dpo, double *sd, double E,
+                           double nu)
+{
+    const double G = E / (2.0 * (1.0 + nu));
+    const double bulk = E / (3.0 * (1.0 - 2.0 * nu));
+    const double lam = bulk - 2.0 / 3.0 * G;
+    const double a = (1.0 + nu) / (3.0 * (1.0 - nu));
+    const double b = 2.0 * (4.0 - 5.0 * nu) / (15.0 * (1.0 - nu));
+    const double d = *D;
+    /* isotropic stiffness applied to a Voigt vector (engineering shear) */
+#define STIFF(in, out)                                                      \
+    do {                                                                    \
+        const double tr_ = (in)[0] + (in)[1] + (in)[2];                     \
+        for (int j = 0; j < 3; ++j) (out)[j] = lam * tr_ + 2.0 * G * (in)[j]; \
+        for (int j = 3; j < 6; ++j) (out)[j] = G * (in)[j];                 \
+    } while (0)
+    /* elastic predictor: local strain (eq. 40), elastic part (41), stress (42) */
+    const double k1 = 1.0 / (1.0 - b * d);
+    const double k2 = (a - b) * d / ((1.0 - b * d) * (1.0 - a * d));
+    const double k3 = b * (1.0 - d) / (1.0 - b * d);
+    double loc[6], el[6], trial[6];
+    const double vol = k2 * (eg[0] + eg[1] + eg[2]) / 3.0;
+    for (int j = 0; j < 6; ++j) loc[j] = k1 * eg[j] + k3 * epl[j] + (j < 3 ? vol : 0.0);
+    for (int j = 0; j < 6; ++j) el[j] = loc[j] - epl[j];
+    STIFF(el, trial);
+    const double mt = (trial[0] + trial[1] + trial[2]) / 3.0;
+    double rel[6];
+    for (int j = 0; j < 6; ++j) rel[j] = trial[j] - (j < 3 ? mt : 0.0) - bs[j];
+    const double teq = sqrt(1.5 * (rel[0] * rel[0] + rel[1] * rel[1] + rel[2] * rel[2] +
+                                   2.0 * (rel[3] * rel[3] + rel[4] * rel[4] + rel[5] * rel[5])));
+    if (teq <= DM_SIGF) {
+        for (int j = 0; j < 6; ++j) { se[j] = trial[j]; ego[j] = eg[j]; }
+        *sd = teq;
+        return;
+    }
+    /* plastic corrector (eqs. 162-175) */
+    double de[6], dsg[6], q[6];
+    for (int j = 0; j < 6; ++j) de[j] = eg[j] - ego[j];
+    STIFF(de, dsg);
+    for (int j = 0; j < 6; ++j) dsg[j] /= (1.0 - b * d);
+    const double k4 = bulk * (a - b) * d / ((1.0 - b * d) * (1.0 - a * d));
+    const double trde = de[0] + de[1] + de[2];
+    for (int j = 0; j < 3; ++j) dsg[j] += k4 * trde;
+    for (int j = 0; j < 6; ++j) q[j] = bs[j] - se[j] - dsg[j];
+    const double eta = DM_CY * (1.0 - d) + 3.0 * G * ((1.0 - b) / (1.0 - b * d));
+    const double mq = (q[0] + q[1] + q[2]) / 3.0;
+    double dq[6];
+    for (int j = 0; j < 6; ++j) dq[j] = q[j] - (j < 3 ? mq : 0.0);
+    const double qeq = sqrt(1.5 * (dq[0] * dq[0] + dq[1] * dq[1] + dq[2] * dq[2] +
+                                   2.0 * (dq[3] * dq[3] + dq[4] * dq[4] + dq[5] * dq[5])));
+    const double dp = (qeq - DM_SIGF) / eta;
+    *p += dp;
+    const double k5 = 1.0 + eta * dp / DM_SIGF;
+    double sdev[6], dpl[6];
+    for (int j = 0; j < 6; ++j) sdev[j] = -dq[j] / k5;
+    for (int j = 0; j < 6; ++j) {
+        dpl[j] = 3.0 * sdev[j] * dp / (2.0 * DM_SIGF);
+        epl[j] += dpl[j];
+    }
+    for (int j = 0; j < 6; ++j) bs[j] += 2.0 * DM_CY * (1.0 - d) * dpl[j] / 3.0;
+    for (int j = 0; j < 6; ++j) se[j] = sdev[j] + (j < 3 ? -mq : 0.0) + bs[j];
+    const double ms = (se[0] + se[1] + se[2]) / 3.0;
+    double sv[6];
+    for (int j = 0; j < 6; ++j) sv[j] = se[j] - (j < 3 ? ms : 0.0);
+    const double seq = sqrt(1.5 * (sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2] +
+                                   2.0 * (sv[3] * sv[3] + sv[4] * sv[4] + sv[5] * sv[5])));
+    /* stored energy (eq. 147) and damage (eqs. 177-178) */
+    *ws += (fabs(seq - DM_SIGF) * dp + fabs(*sd - DM_SIGF) * *dpo) / 2.0;
+    if (*ws >= DM_WD) {
+        const double x = (1.0 - d) / (1.0 - DM_H * d);
+        double pos = 0.0, neg = 0.0;
+        for (int j = 0; j < 3; ++j) {
+            if (se[j] < 0.0) neg += se[j] * se[j];
+            else pos += se[j] * se[j];
+        }
+        const double tr = se[0] + se[1] + se[2];
+        const double yp = (1.0 + nu) / (2.0 * E) * (pos + DM_H * x * x * neg);
+        const double yn = tr >= 0.0 ? nu / (2.0 * E) * tr * tr
+                                    : nu / (2.0 * E) * (DM_H * x * x * tr * tr);
+        *D = d + pow((yp - yn) / DM_S, DM_SEXP) * dp;
+    } else {
+        *D = 0.0;
+    }
+    for (int j = 0; j < 6; ++j) ego[j] = eg[j];
+    *sd = seq;
+    *dpo = dp;
+#undef STIFF
+}
+
+void orc_getdfinal_history(int nsteps, const double *eps, double *eps_old,
+                           double *eps_pl, double *sig_eff, double *sig_back,
+                           double *p, double *D, double *ws, double *del_po,
+                           double *sig_d, double E, double nu)
+{
+    for (int s = 0; s < nsteps; ++s)
+        getdfinal_step(eps + (size_t)s * 6, eps_old, eps_pl, p, D, ws, sig_eff,
+                       sig_back, del_po, sig_d, E, nu);
 }
 
 void orc_damage_cleanup(int ngp, const int *gpsta, double *D, double *ws)

@@ -59,6 +59,7 @@ def lib():
             "orc_nt_table": (None, [C.c_int, _dp, C.c_double, _dp]),
             "orc_damage": (None, [C.c_int] * 8 + [_ip] + [_dp] * 16 + [C.c_int]),
             "orc_damage_cleanup": (None, [C.c_int, _ip, _dp, _dp]),
+            "orc_getdfinal_history": (None, [C.c_int] + [_dp] * 10 + [C.c_double] * 2),
             "orc_chkelesta": (C.c_int, [C.c_int, C.c_int, C.c_double, _dp, _ip, _ip, _ip]),
             "orc_stcoeff_m_quad": (None, [C.c_double, C.c_double, C.c_double] + [_dp] * 6),
             "orc_getfextc_m_quad": (None, [C.c_double, C.c_double, C.c_double, _dp]),
@@ -215,6 +216,18 @@ def damage(ne, nn, nip, nodes, Nx, Ny, Nz, Nt, sol, ym, nu, state, nthreads=1):
         assert state[k].dtype == np.float64 and state[k].flags.c_contiguous
     lib().orc_damage(ne, nn, 3, 8, 3, 8, 6, nip, *[x[1] for x in ins],
                      *[state[k].ctypes.data_as(_dp) for k in STATE_KEYS], nthreads)
+    return state
+
+
+def getdfinal_history(eps, state, E, nu):
+    """src/getdfinal.f driven over the strain history eps (nsteps x 6) for
+    one point; state holds that point's nine state entries (six-vectors for
+    the tensors, length-1 arrays for the scalars), updated in place."""
+    eps = np.ascontiguousarray(eps, dtype=np.float64).reshape(-1, 6)
+    for k in STATE_KEYS:
+        assert state[k].dtype == np.float64 and state[k].flags.c_contiguous
+    lib().orc_getdfinal_history(len(eps), eps.ctypes.data_as(_dp),
+                                *[state[k].ctypes.data_as(_dp) for k in STATE_KEYS], E, nu)
     return state
 
 

@@ -97,6 +97,17 @@ void orc_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
                 double *sig_back, double *p, double *D, double *ws,
                 double *del_po, double *sig_d, int nthreads);
 
+/* src/getdfinal.f:10-397: the reference's stand-alone statement of the
+ * same two-scale law, driven over a prescribed global strain history eps
+ * (nsteps x 6, Voigt, engineering shear) for ONE point whose state (the six
+ * -component eps_old, eps_pl, sig_eff, sig_back and the scalars) is updated
+ * in place; E and nu replace the reference's hard-coded 1.97e5 and 0.3.
+ * Written independently of orc_damage, to cross-check it. */
+void orc_getdfinal_history(int nsteps, const double *eps, double *eps_old,
+                           double *eps_pl, double *sig_eff, double *sig_back,
+                           double *p, double *D, double *ws, double *del_po,
+                           double *sig_d, double E, double nu);
+
 /* Same as orc_damage but applies the failed-point clean-up of
  * src/kokkos_damage.f90:102-107 (D = ws = 0 where gpsta == 0). */
 void orc_damage_cleanup(int ngp, const int *gpsta, double *D, double *ws);

@@ -301,6 +301,56 @@ def test_oracle_damage_elastic_step_is_hookes_law(xt, orc, c1):
     assert np.abs(sig - eps @ Dm.T).max() <= 1e-9 * np.abs(sig).max()
 
 
+def gp_strains(Nt, sol, Nx, Ny, Nz, nn):
+    """Global strain history (steps x 6, engineering shear) of each point of
+    one element whose nodes are 1..8: displacement from the temporal shape
+    table, then the strain rows (src/kokkos_kernel.h:45-110)."""
+    u = np.einsum("tk,knj->tnj", Nt, sol.reshape(6, nn, 3))
+    return [np.stack([u[:, :, 0] @ nx, u[:, :, 1] @ ny, u[:, :, 2] @ nz,
+                      u[:, :, 0] @ ny + u[:, :, 1] @ nx, u[:, :, 1] @ nz + u[:, :, 2] @ ny,
+                      u[:, :, 0] @ nz + u[:, :, 2] @ nx], 1)
+            for nx, ny, nz in zip(Nx, Ny, Nz)]
+
+
+def test_oracle_damage_matches_getdfinal_statement(xt, orc):
+    """The damage oracle (after src/kokkos_kernel.h) against the oracle's
+    separate statement of the reference's stand-alone src/getdfinal.f, with
+    per-point E and nu, over hand-built histories on one element: a point
+    far below yield (D and p stay 0), cyclically plastic points whose stored
+    energy stays below w_d (D stays 0), and points seeded just below w_d that
+    cross it and accumulate damage; then a monotone ramp.  The two statements
+    agree to 1e-12 while D < 1; the comparison stops before D reaches 0.99,
+    as a run deletes the element there (beyond D = 1 the law is unstable and
+    rounding differences grow without bound)."""
+    rng = np.random.default_rng(11)
+    nn, nip = 8, 300
+    scale = np.array([1e-4, 1, 1, 2, 2, 3, 3, 4.0])
+    Nx, Ny, Nz = (rng.uniform(-1, 1, (8, 8)) * scale[:, None] for _ in range(3))
+    nodes = np.tile(np.arange(1, 9, dtype=np.int32), 8)
+    sol = rng.standard_normal(6 * 3 * nn) * 1.5e-3
+    ym, nu = 2e5 * (1 + 0.1 * rng.uniform(-1, 1, 8)), 0.3 + 0.02 * rng.uniform(-1, 1, 8)
+    cyclic = xt.nt_table(2000, np.array([0.0, 0.25, 0.5]), 2 * np.pi * 20).reshape(2000, 6)[:nip]
+    ramp = np.zeros((nip, 6))
+    ramp[:, 0] = np.linspace(0.0, 1.0, nip)
+    for Nt, ws0 in ((cyclic, 31.7), (ramp, 31.74)):
+        st = {k: np.zeros(48) for k in ["eps_old", "eps_pl", "sig_eff", "sig_back"]}
+        st.update({k: np.zeros(8) for k in ["p", "D", "ws", "del_po", "sig_d"]})
+        st["ws"][4:] = ws0
+        per_gp = [{k: (v[6 * g:6 * g + 6] if v.size == 48 else v[g:g + 1]).copy()
+                   for k, v in st.items()} for g in range(8)]
+        orc.damage(1, nn, nip, nodes, Nx.ravel(), Ny.ravel(), Nz.ravel(), Nt.ravel(), sol, ym,
+                   nu, st)
+        for g, eps in enumerate(gp_strains(Nt, sol, Nx, Ny, Nz, nn)):
+            orc.getdfinal_history(eps, per_gp[g], ym[g], nu[g])
+        for k in st:
+            other = np.concatenate([s[k] for s in per_gp])
+            assert np.abs(other - st[k]).max() <= 1e-12 * max(np.abs(st[k]).max(), 1e-300), k
+        assert st["p"][0] == 0 and st["D"][0] == 0          # elastic
+        assert np.all(st["p"][1:] > 0)                       # plastic
+        assert np.all(st["D"][1:4] == 0)                     # below w_d
+        assert np.all(st["D"][4:] > 0) and st["D"].max() < 0.99  # crossed w_d
+
+
 def test_oracle_chkelesta_lists_failed_elements_ascending(orc):
     ne, ngpe = 10, 8
     D = np.zeros(ne * ngpe)
