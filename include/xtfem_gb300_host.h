@@ -57,7 +57,11 @@ int xth_problem_delete(xth_problem pr, int nef, const int *nefail, int *bc,
                        int *ndf_out);
 
 /* src/ilut.f:152-495 ILUT(lfil, droptol) in FP64; alu/jlu hold iwk entries,
- * ju n entries; returns SPARSKIT's ierr (0 = success). */
+ * ju n entries; returns SPARSKIT's ierr: 0 success, -1 a row's L or U
+ * length exceeds n, -2 the L part overflows iwk, -3 the U part overflows
+ * iwk (tested as the reference tests it, row by row), -4 lfil < 0, -5 a
+ * zero row.  A zero pivot is replaced by (1e-4 + droptol) times the row
+ * norm, with 1e-4 rounded to single precision as in the reference. */
 int xth_ilut(int n, const int *ia, const int *ja, const double *a, int lfil,
              double droptol, int iwk, double *alu, int *jlu, int *ju);
 

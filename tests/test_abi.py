@@ -74,6 +74,41 @@ def test_widened_entry_points_validate_arguments(xt):
     assert lib.xth_problem_from_mesh(0, 0, None, None, 2e5, 0.3, 7.8e-9, ctypes.byref(out)) == -10
 
 
+def test_corrupt_csr_rejected_on_the_host(xt):
+    """A corrupt K or M (row pointers not starting at 1 or decreasing, a
+    column index out of range) and bad sizes are XT_ERR_ARG with a message,
+    found on the host before any device work: the same answer with or
+    without a GPU."""
+    import numpy as np
+
+    lib = xt.lib()
+    ip = ctypes.POINTER(ctypes.c_int)
+    dp = ctypes.POINTER(ctypes.c_double)
+    v = np.ones(2)
+    good = (np.array([1, 2, 3], np.int32), np.array([1, 2], np.int32))
+    bad = {"start at 1": (np.array([0, 1, 2], np.int32), good[1]),
+           "decrease": (np.array([1, 3, 2], np.int32), good[1]),
+           "out of range": (good[0], np.array([1, 3], np.int32)),
+           "out of range ": (good[0], np.array([0, 2], np.int32))}
+
+    def create(p, q, k, m):
+        out = ctypes.c_void_p()
+        st = lib.xt_system_create(p, q, k[0].ctypes.data_as(ip), k[1].ctypes.data_as(ip),
+                                  v.ctypes.data_as(dp), m[0].ctypes.data_as(ip),
+                                  m[1].ctypes.data_as(ip), v.ctypes.data_as(dp), ctypes.byref(out))
+        return st, out.value
+
+    for words, csr in bad.items():
+        for which, (k, m) in (("K", (csr, good)), ("M", (good, csr))):
+            lib.xt_clear_error()
+            st, h = create(2, 6, k, m)
+            msg = lib.xt_last_error().decode()
+            assert st == -10 and h is None, (words, which)
+            assert which in msg and words.strip() in msg, msg
+    for p, q in ((0, 6), (2, 0), (2, 9)):
+        assert create(p, q, good, good)[0] == -10
+
+
 def test_problem_from_mesh_rejects_bad_connectivity(xt):
     import numpy as np
 

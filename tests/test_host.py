@@ -142,6 +142,42 @@ def test_product_ilut_identical_to_oracle(xt, orc, c1):
     assert np.array_equal(alu, oalu)
 
 
+def test_ilut_error_codes_and_zero_pivot_match_oracle(xt, orc, c1):
+    """SPARSKIT ILUT's failure modes (src/ilut.f:199-208, 152-495), product
+    against oracle: the storage codes over a window of capacities below the
+    factor's size (-2 when an L part overflows, -3 when a U part does; both
+    occur), lfil < 0 (-4), a zero row (-5); and the zero-pivot fallback
+    (0.0001 + droptol) * row norm, with 0.0001 single precision (:455)."""
+    K = c1["K"]
+    (alu, _, _), _ = orc.ilut(K, 20, 1e-4)
+    need = len(alu) + 1  # the reference tests U with its diagonal slot
+
+    def product(A, lfil, droptol, iwk=None):
+        try:
+            return xt.ilut(A, lfil, droptol, iwk), 0
+        except xt.XtError as e:
+            return None, e.ierr
+
+    seen = set()
+    for iwk in range(need - 150, need + 2):
+        f, code = product(K, 20, 1e-4, iwk)
+        g, ocode = orc.ilut(K, 20, 1e-4, iwk)
+        assert code == ocode, iwk
+        seen.add(code)
+        if code == 0:
+            assert all(np.array_equal(a, b) for a, b in zip(f, g))
+    assert {0, -2, -3} <= seen, seen
+    assert product(K, -1, 1e-4)[1] == orc.ilut(K, -1, 1e-4)[1] == -4
+    z = xt.Csr(np.array([1, 3, 3, 4]), np.array([1, 2, 3]), np.array([2.0, 1.0, 1.0]))
+    assert product(z, 2, 0.0)[1] == orc.ilut(z, 2, 0.0)[1] == -5
+    # [[1, 1], [1, 1]]: the second pivot eliminates to 0
+    s = xt.Csr(np.array([1, 3, 5]), np.array([1, 2, 1, 2]), np.ones(4))
+    (palu, pjlu, pju), _ = product(s, 2, 1e-4)
+    (oalu, ojlu, oju), ierr = orc.ilut(s, 2, 1e-4)
+    assert ierr == 0 and np.array_equal(palu, oalu) and np.array_equal(pjlu, ojlu)
+    assert palu[1] == 1.0 / ((float(np.float32(1e-4)) + 1e-4) * 1.0)
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)

@@ -179,18 +179,22 @@ def kokkos_host(rank, ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, nodes, Nx, Ny,
     _raise_if_error()
 
 
-def ilut(A: Csr, lfil=20, droptol=1e-4):
+def ilut(A: Csr, lfil=20, droptol=1e-4, iwk=None):
     """SPARSKIT ILUT on the host in FP64 (src/ilut.f:152-495).  Returns
-    (alu, jlu, ju) in MSR form with 1-based indices, trimmed to size."""
+    (alu, jlu, ju) in MSR form with 1-based indices, trimmed to size.  iwk
+    is the capacity of alu/jlu (default: enough for any factor); an error
+    raises XtError carrying SPARSKIT's ierr (.ierr)."""
     n = A.n
-    iwk = n * (2 * lfil + 2) + n + 2
+    iwk = iwk or n * (2 * max(lfil, 0) + 2) + n + 2
     alu = np.zeros(iwk)
     jlu = np.zeros(iwk, np.int32)
     ju = np.zeros(n, np.int32)
     ierr = lib().xth_ilut(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk, dptr(alu),
                           iptr(jlu), iptr(ju))
     if ierr != 0:
-        raise XtError(f"ilut failed with ierr = {ierr}")
+        err = XtError(f"ilut failed with ierr = {ierr}")
+        err.ierr = ierr
+        raise err
     end = int(jlu[n]) - 1
     return alu[:end].copy(), jlu[:end].copy(), ju
 

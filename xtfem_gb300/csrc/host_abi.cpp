@@ -256,7 +256,21 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
         Msr f;
         int ierr = ilut(m, lfil, droptol, f);
         if (ierr != 0) return ierr;
-        if ((long long)f.alu.size() > iwk) return -2;
+        // The storage test of src/ilut.f:152-495, row by row on the finished
+        // factor: -2 when an L entry would be stored past iwk, -3 when the
+        // U part (counted with its diagonal, as the reference counts it)
+        // would end past iwk.  The first failing row decides, as in the
+        // reference, which stops there.
+        long long pos = (long long)n + 2;  // 1-based next free slot
+        for (int i = 0; i < n; ++i) {
+            const long long nl = f.ju[i] - f.jlu[i];
+            if (nl > 0 && pos + nl - 1 > iwk) return -2;
+            pos += nl;
+            const long long nu = f.jlu[i + 1] - f.ju[i];
+            if (nu + 1 + pos > iwk) return -3;
+            pos += nu;
+        }
+        if ((long long)f.alu.size() > iwk) return -3;
         std::memcpy(alu, f.alu.data(), f.alu.size() * sizeof(double));
         std::memcpy(jlu, f.jlu.data(), f.jlu.size() * sizeof(int));
         std::memcpy(ju, f.ju.data(), f.ju.size() * sizeof(int));

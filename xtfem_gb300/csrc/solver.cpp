@@ -15,6 +15,7 @@
 #include "prof.h"
 
 #include <cmath>
+#include <string>
 #include <cstring>
 #include <mutex>
 
@@ -107,14 +108,45 @@ int system_stream(System& S)
     return XT_OK;
 }
 
+// A caller's 1-based CSR, checked on the host before anything touches the
+// device: first row pointer 1, row pointers non-decreasing, column indices
+// in 1..n.  A corrupt matrix is XT_ERR_ARG with a message, never a fault.
+static int check_csr(const char* what, int n, const int* ia, const int* ja)
+{
+    if (!ia || !ja) {
+        set_error(std::string("system_create: null ") + what + " array");
+        return XT_ERR_ARG;
+    }
+    if (ia[0] != 1) {
+        set_error(std::string("system_create: ") + what + " row pointers must start at 1");
+        return XT_ERR_ARG;
+    }
+    for (int r = 0; r < n; ++r)
+        if (ia[r + 1] < ia[r]) {
+            set_error(std::string("system_create: ") + what + " row pointers decrease at row " +
+                      std::to_string(r + 1));
+            return XT_ERR_ARG;
+        }
+    const int nnz = ia[n] - 1;
+    for (int k = 0; k < nnz; ++k)
+        if (ja[k] < 1 || ja[k] > n) {
+            set_error(std::string("system_create: ") + what + " column index out of range at entry " +
+                      std::to_string(k + 1));
+            return XT_ERR_ARG;
+        }
+    return XT_OK;
+}
+
 int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
                   const int* mi, const int* mj, const double* mv)
 {
-    XT_TRY(ensure_init());
     if (p <= 0 || q < 1 || q > 8) {
         set_error("system_create: need p > 0 and 1 <= q <= 8");
         return XT_ERR_ARG;
     }
+    XT_TRY(check_csr("K", p, ki, kj));
+    XT_TRY(check_csr("M", p, mi, mj));
+    XT_TRY(ensure_init());
     XT_TRY(system_stream(S));
     cudaStream_t s = S.stream;
     S.p = p;
