@@ -13,13 +13,16 @@ tests/test_host.py.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import subprocess
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-LIB = HERE / "liboracle.so"
+# XTFEM_ORACLE_LIB selects another build of the same sources (the sanitizer
+# build of oracle/Makefile's `sanitize` target)
+LIB = Path(os.environ.get("XTFEM_ORACLE_LIB", HERE / "liboracle.so"))
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

@@ -12,7 +12,10 @@ from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "libxtfem_gb300.so"
+# XTFEM_LIB selects another build of the same sources (the sanitizer build,
+# xtfem_gb300/build.py --sanitize); by default the in-tree release build
+LIB_PATH = Path(os.environ.get("XTFEM_LIB") or
+                Path(__file__).resolve().parent / "libxtfem_gb300.so")
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

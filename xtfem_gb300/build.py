@@ -17,6 +17,11 @@ HERE = Path(__file__).resolve().parent
 CSRC = HERE / "csrc"
 OUT = HERE / "_build"
 LIB = HERE / "libxtfem_gb300.so"
+# debug build: host C++ under AddressSanitizer and UBSan, in its own folder
+# and file (load it with XTFEM_LIB and the sanitizer runtimes preloaded)
+OUT_SAN = HERE / "_build_san"
+LIB_SAN = HERE / "libxtfem_gb300_san.so"
+SAN = ["-fsanitize=address", "-fsanitize=undefined", "-fno-omit-frame-pointer"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # per-file extra flags: the damage kernel keeps the reference's operation
@@ -44,16 +49,18 @@ def _needs(obj: Path, deps) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> Path:
+def build(verbose: bool = False, jobs: int | None = None, sanitize: bool = False) -> Path:
     nvcc = _nvcc()
-    OUT.mkdir(exist_ok=True)
+    out_dir, lib = (OUT_SAN, LIB_SAN) if sanitize else (OUT, LIB)
+    host_san = [f for s in SAN for f in ("-Xcompiler", s)] if sanitize else []
+    out_dir.mkdir(exist_ok=True)
     cu, cpp = _sources()
     headers = (list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) +
                list((HERE.parent / "include").glob("*.h")))
     cmds = []
     objs = []
     for src in cu:
-        obj = OUT / (src.name + ".o")
+        obj = out_dir / (src.name + ".o")
         objs.append(obj)
         if _needs(obj, [src, *headers]):
             cmds.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
@@ -61,13 +68,14 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
                          "--expt-relaxed-constexpr", *EXTRA.get(src.name, []),
                          "-c", str(src), "-o", str(obj)])
     for src in cpp:
-        obj = OUT / (src.name + ".o")
+        obj = out_dir / (src.name + ".o")
         objs.append(obj)
         if _needs(obj, [src, *headers]):
             # host code: no FMA contraction, so x86 and Arm hosts assemble
             # bit-identical K and M
-            cmds.append([nvcc, "-O2", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
-                         "-ffp-contract=off", "-c", str(src), "-o", str(obj)])
+            cmds.append([nvcc, "-O1" if sanitize else "-O2", "-std=c++17", "-Xcompiler", "-fPIC",
+                         "-Xcompiler", "-ffp-contract=off", *host_san, "-c", str(src), "-o",
+                         str(obj)])
     jobs = jobs or max(1, min(len(cmds), os.cpu_count() or 4))
 
     def run(cmd):
@@ -83,13 +91,13 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
                 failed.append(cmd[-3])
     if failed:
         raise RuntimeError(f"compilation failed: {failed}")
-    if cmds or not LIB.exists():
-        link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
+    if cmds or not lib.exists():
+        link = [nvcc, *ARCH, "-shared", "-o", str(lib), *map(str, objs), "-lcudart", *host_san]
         p = subprocess.run(link, capture_output=True, text=True)
         if p.returncode:
             raise RuntimeError("link failed:\n" + p.stdout + p.stderr)
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(verbose="-v" in sys.argv))
+    print(build(verbose="-v" in sys.argv, sanitize="--sanitize" in sys.argv))
