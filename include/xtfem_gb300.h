@@ -84,13 +84,25 @@ void kronlusol_(const double *a, const int *q, const double *alu,
  * ILUT-right-preconditioned GMRES(im), FP64, with the reference's restart,
  * convergence (|rs(i+1)| <= eps ||r0||) and ierr conventions (0, 1, -1;
  * library errors <= -10).  rhs is used as scratch as in the reference
- * (its content on return is unspecified). iout is accepted and ignored. */
+ * (its content on return is unspecified).  The reference writes its
+ * residual history to Fortran unit iout (:257-259, :311; the driver opens
+ * it as gmres.log); a C library cannot write to a Fortran unit, so with
+ * iout >= 0 the history is kept for xt_gmres_log and the caller's shim
+ * writes the lines (iout < 0: nothing is kept). */
 void kronpgmres_(const double *a, const double *b, const int *q,
                  const int *ki, const int *kj, const double *kv,
                  const int *mi, const int *mj, const double *mv, const int *p,
                  const double *alu, const int *jlu, const int *ju, double *rhs,
                  double *sol, const int *im, const double *eps,
                  const int *maxits, const int *iout, int *ierr);
+
+/* The residual history of this thread's last kronpgmres_ call made with
+ * iout >= 0, as the reference writes it: entry 0 is ||r0||/||rhs|| at
+ * its = 0 (the line written when iout >= 0), entry k >= 1 the estimate
+ * |rs(i+1)|/||rhs|| after iteration k (written when iout > 0).  Copies up
+ * to cap entries to rel and returns the number of entries (0 before any
+ * such call). */
+int xt_gmres_log(double *rel, int cap);
 
 /* src/delelement.f90:109-136  chkelesta on the device: element i fails when
  * one of its ngpe Gauss points has D >= Dc; gpsta/elesta set to 0 for it

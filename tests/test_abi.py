@@ -117,3 +117,18 @@ def test_problem_from_mesh_rejects_bad_connectivity(xt):
     conn[0, 3] = 9  # no node 9
     with pytest.raises(xt.XtError, match="connectivity"):
         xt.Problem.from_mesh(xyz, conn)
+
+
+def test_gmres_log_empty_and_line_format(xt):
+    """Before any kronpgmres_ call with iout >= 0 the kept history is empty;
+    the lines written from a history follow the reference's FORMAT 199
+    (src/kronecker.f90:354), the its = 0 line for iout >= 0 and the others
+    only for iout > 0."""
+    assert xt.lib().xt_gmres_log(None, 0) == 0 and xt.gmres_log().size == 0
+    lines = xt.gmres_log_lines([1.0, 0.25, 3.5e-9], iout=40)
+    assert lines == ["   its =   0 rel. res. norm =        0.100000D+01",
+                     "   its =   1 rel. res. norm =        0.250000D+00",
+                     "   its =   2 rel. res. norm =        0.350000D-08"]
+    assert xt.gmres_log_lines([1.0, 0.25], iout=0) == lines[:1]
+    assert xt.gmres_log_lines([1.0, 0.25], iout=-1) == []
+    assert xt.api.fortran_d20_6(-123456.7) == "       -0.123457D+06"

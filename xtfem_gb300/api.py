@@ -24,7 +24,7 @@ import numpy as np
 from ._lib import XtError, _dp, check, dptr, dref, iptr, iref, lib
 
 __all__ = [
-    "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "chkelesta", "kokkos_host",
+    "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "gmres_log", "gmres_log_lines", "chkelesta", "kokkos_host",
     "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "getfextc_t", "nt_table", "SpaceTimeSystem",
     "SystemBatch", "ThermalConfig", "ThermalSolver",
     "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
@@ -117,10 +117,12 @@ def kronlusol(a, alu, jlu, ju, x):
     return y
 
 
-def kronpgmres(a, b, K: Csr, M: Csr, alu, jlu, ju, rhs, sol=None, im=30, eps=1e-8, maxits=1000):
+def kronpgmres(a, b, K: Csr, M: Csr, alu, jlu, ju, rhs, sol=None, im=30, eps=1e-8, maxits=1000,
+               iout=-1):
     """Solve (A (x) K + B (x) M) sol = rhs by ILUT-preconditioned GMRES(im)
     (src/kronecker.f90:181-365).  Returns (sol, ierr); rhs is not modified
-    here (the C entry point may clobber its own copy, as the reference)."""
+    here (the C entry point may clobber its own copy, as the reference).
+    iout >= 0 keeps the residual history for gmres_log()."""
     A, B = _colmajor(a), _colmajor(b)
     q = int(round(np.sqrt(A.size)))
     p = K.n
@@ -131,10 +133,45 @@ def kronpgmres(a, b, K: Csr, M: Csr, alu, jlu, ju, rhs, sol=None, im=30, eps=1e-
     lib().kronpgmres_(dptr(A), dptr(B), iref(q), iptr(K.ia), iptr(K.ja), dptr(K.a), iptr(M.ia),
                       iptr(M.ja), dptr(M.a), iref(p), dptr(_f64(alu)), iptr(_i32(jlu)),
                       iptr(_i32(ju)), dptr(r), dptr(s), iref(im), dref(eps), iref(maxits),
-                      iref(-1), C.byref(ierr))
+                      iref(iout), C.byref(ierr))
     if ierr.value <= -10:
         _raise_if_error(force=True)
     return s, ierr.value
+
+
+def gmres_log():
+    """Residual history of this thread's last kronpgmres call with iout >= 0:
+    entry 0 is ||r0||/||rhs||, entry k the estimate after iteration k."""
+    n = lib().xt_gmres_log(None, 0)
+    out = np.zeros(n)
+    if n:
+        lib().xt_gmres_log(dptr(out), n)
+    return out
+
+
+def gmres_log_lines(rel, iout=40):
+    """The lines the reference writes to unit iout for that history
+    (FORMAT 199 of src/kronecker.f90:354: its as i4, the ratio as d20.6);
+    the first only when iout >= 0, the others only when iout > 0."""
+    lines = []
+    for k, v in enumerate(rel):
+        if iout < 0 or (k > 0 and iout == 0):
+            break
+        lines.append("   its =" + f"{k:4d}"[-4:] + " rel. res. norm =" + fortran_d20_6(v))
+    return lines
+
+
+def fortran_d20_6(v):
+    """Fortran D20.6 edit: sign, 0.dddddd (six significant digits), then the
+    exponent as D+dd (or +ddd beyond 99), right-justified in 20 columns."""
+    if not np.isfinite(v):
+        return f"{'NaN' if np.isnan(v) else ('Infinity' if v > 0 else '-Infinity'):>20}"
+    if v == 0.0:
+        return f"{'0.000000D+00':>20}"
+    m, e = f"{abs(v):.5e}".split("e")
+    exp = int(e) + 1
+    ex = f"D{exp:+03d}" if abs(exp) < 100 else f"{exp:+04d}"
+    return f"{('-' if v < 0 else '') + '0.' + m.replace('.', '') + ex:>20}"
 
 
 def chkelesta(ne, ngpe, Dc, D, elesta, gpsta):

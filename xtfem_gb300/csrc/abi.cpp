@@ -542,12 +542,24 @@ void kronlusol_(const double* a, const int* q, const double* alu, const int* jlu
     (void)xt_system_lusol(&h, a, x, y);
 }
 
+// kronpgmres_'s residual history for the caller's Fortran shim (one per
+// host thread: each thread drives its own solves)
+static thread_local std::vector<double> t_gmres_log;
+
+int xt_gmres_log(double* rel, int cap)
+{
+    const int n = (int)t_gmres_log.size();
+    for (int k = 0; rel && k < cap && k < n; ++k) rel[k] = t_gmres_log[k];
+    return n;
+}
+
 void kronpgmres_(const double* a, const double* b, const int* q, const int* ki, const int* kj,
                  const double* kv, const int* mi, const int* mj, const double* mv, const int* p,
                  const double* alu, const int* jlu, const int* ju, double* rhs, double* sol,
                  const int* im, const double* eps, const int* maxits, const int* iout, int* ierr)
 {
-    (void)iout;
+    const bool keep_log = iout && *iout >= 0;
+    if (keep_log) t_gmres_log.clear();
     if (!ierr) return;
     *ierr = XT_ERR_ARG;
     if (!q || !p || !im || !eps || !maxits) { set_error("kronpgmres_: null argument"); return; }
@@ -560,8 +572,33 @@ void kronpgmres_(const double* a, const double* b, const int* q, const int* ki, 
     st = system_set_temporal(h->sys, a, b);
     if (st != XT_OK) { *ierr = st; return; }
     int its = 0, e = 0;
-    st = xt_system_gmres(h, rhs, sol, *im, *eps, *maxits, &its, &e, nullptr, nullptr, 0);
+    if (!keep_log) {
+        st = xt_system_gmres(h, rhs, sol, *im, *eps, *maxits, &its, &e, nullptr, nullptr, 0);
+        *ierr = (st != XT_OK) ? st : e;
+        return;
+    }
+    // the its = 0 line: ||rhs - A sol|| / ||rhs|| before the first cycle
+    const size_t n = (size_t)(*p) * (*q);
+    double ro0 = 0.0, ro = 0.0;
+    for (size_t k = 0; k < n; ++k) ro0 += rhs[k] * rhs[k];
+    bool zero_start = true;
+    for (size_t k = 0; k < n && zero_start; ++k) zero_start = sol[k] == 0.0;
+    if (zero_start) {
+        ro = ro0;
+    } else {
+        std::vector<double> r(rhs, rhs + n);
+        st = xt_system_apply(h, a, b, -1.0, 1.0, sol, r.data());
+        if (st != XT_OK) { *ierr = st; return; }
+        for (size_t k = 0; k < n; ++k) ro += r[k] * r[k];
+    }
+    std::vector<double> hist((size_t)std::max(*maxits, 0) + (size_t)std::max(*im, 0) + 1, 0.0);
+    st = xt_system_gmres(h, rhs, sol, *im, *eps, *maxits, &its, &e, nullptr, hist.data(),
+                         (int)hist.size());
     *ierr = (st != XT_OK) ? st : e;
+    if (st != XT_OK) return;
+    t_gmres_log.assign(1, std::sqrt(ro) / std::sqrt(ro0));
+    t_gmres_log.insert(t_gmres_log.end(), hist.begin(),
+                       hist.begin() + std::min((size_t)std::max(its, 0), hist.size()));
 }
 
 void chkelesta_(const int* nn, const int* ne, const int* nnse, const int* ngpe, const double* Dc,
