@@ -178,6 +178,23 @@ def test_ilut_error_codes_and_zero_pivot_match_oracle(xt, orc, c1):
     assert palu[1] == 1.0 / ((float(np.float32(1e-4)) + 1e-4) * 1.0)
 
 
+def test_product_ilut_identical_to_oracle_at_c2_size(xt, orc):
+    """The product's ILUT (candidate columns kept as a bit set read upward,
+    in place of the reference's linear scan for the smallest column) gives
+    the reference-order factor bit for bit on the full 20 x 20 x 60 rod
+    (80,703 rows, 3.17 M factor entries)."""
+    pr = rod_problem(xt, 60, 20, 20)
+    xyz, _ = pr.mesh()
+    pr.apply_bc(clamp_mask(xyz))
+    K = pr.K()
+    pr.close()
+    got = xt.ilut(K, 20, 1e-4)
+    (alu, jlu, ju), ierr = orc.ilut(K, 20, 1e-4)
+    assert ierr == 0 and len(alu) == 3_173_569
+    assert np.array_equal(got[1], jlu) and np.array_equal(got[2], ju)
+    assert np.array_equal(got[0], alu)
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)

@@ -65,6 +65,16 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
     // of column c in the current row, or -1.
     std::vector<double> w(n + 1);
     std::vector<int> col(n + 1), where(n, -1);
+    // L candidates waiting for elimination, as a bit set of columns read
+    // upward: the reference picks the smallest remaining column by a linear
+    // scan (and swaps it forward), which is the same order, and every fill-in
+    // lies above the column being eliminated, so one upward pass over the
+    // words below i visits them all.  The kept multipliers go to their own
+    // arrays in that order, where the reference compacts them to the front
+    // of the row.  Same factor, without the quadratic scan.
+    std::vector<unsigned long long> pending((size_t)n / 64 + 2, 0ull);
+    std::vector<double> wl(n + 1);
+    std::vector<int> cl(n + 1);
     F.jlu[1] = n + 2;
     F.alu.reserve((size_t)n * (2 * lfil + 2));
     F.jlu.reserve((size_t)n * (2 * lfil + 2));
@@ -78,10 +88,13 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
         col[i] = i;
         w[i] = 0.0;
         where[i] = i;
+        int lo = i;  // lowest candidate column
         for (int k = b; k < e; ++k) {
             const int c = A.ja[k] - 1;
             if (c < i) {
                 col[lenl] = c; w[lenl] = A.a[k]; where[c] = lenl; ++lenl;
+                pending[(size_t)c >> 6] |= 1ull << (c & 63);
+                if (c < lo) lo = c;
             } else if (c == i) {
                 w[i] = A.a[k];
             } else {
@@ -89,23 +102,17 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
                 col[s] = c; w[s] = A.a[k]; where[c] = s; ++lenu;
             }
         }
-        // eliminate with earlier rows in ascending column order; the kept
-        // multipliers are compacted to the front of the L slots
+        // eliminate with earlier rows in ascending column order
         int kept = 0;
-        for (int jj = 0; jj < lenl; ++jj) {
-            int pick = jj;
-            for (int s = jj + 1; s < lenl; ++s)
-                if (col[s] < col[pick]) pick = s;
-            const int r = col[pick];
-            if (pick != jj) {
-                const int cj = col[jj];
-                std::swap(col[jj], col[pick]);
-                where[r] = jj;
-                where[cj] = pick;
-                std::swap(w[jj], w[pick]);
-            }
+        size_t wd = (size_t)lo >> 6;
+        const size_t wend = ((size_t)i >> 6) + 1;
+        for (;;) {
+            while (wd < wend && pending[wd] == 0) ++wd;
+            if (wd >= wend) break;
+            const int r = (int)(wd << 6) + __builtin_ctzll(pending[wd]);
+            pending[wd] &= pending[wd] - 1;  // clear the lowest set bit
+            const double fact = w[where[r]] * F.alu[r + 1];
             where[r] = -1;
-            const double fact = w[jj] * F.alu[r + 1];
             if (std::fabs(fact) <= droptol) continue;
             // row r of U: MSR positions ju[r] .. jlu[r+1]-1 (1-based)
             for (int k = F.ju[r]; k <= F.jlu[r + 2] - 1; ++k) {
@@ -124,22 +131,23 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
                     if (slot < 0) {
                         if (lenl + 1 > n) return -1;
                         col[lenl] = c; where[c] = lenl; w[lenl] = -s; ++lenl;
+                        pending[(size_t)c >> 6] |= 1ull << (c & 63);
                     } else {
                         w[slot] -= s;
                     }
                 }
             }
-            w[kept] = fact;
-            col[kept] = r;
+            wl[kept] = fact;
+            cl[kept] = r;
             ++kept;
         }
         for (int k = 0; k < lenu; ++k) where[col[i + k]] = -1;
         // L row: the lfil largest multipliers
         const int nl = kept < lfil ? kept : lfil;
-        split_largest(w.data(), col.data(), kept, nl);
+        split_largest(wl.data(), cl.data(), kept, nl);
         for (int k = 0; k < nl; ++k) {
-            F.alu.push_back(w[k]);
-            F.jlu.push_back(col[k] + 1);
+            F.alu.push_back(wl[k]);
+            F.jlu.push_back(cl[k] + 1);
         }
         F.ju[i] = (int)F.jlu.size();  // 1-based start of U row i
         // U row: threshold, then the lfil-1 largest off-diagonals
