@@ -273,9 +273,50 @@ def run_gpu(args, rank, world):
     if rank == 0 and not args.skip_cpu:
         out["cpu_baseline"] = cpu_baseline(its=float(np.mean(its)), sample_its=args.cpu_its,
                                            threads=os.cpu_count() or 1, for_arm=False)
+    if rank == 0:
+        out["refactor_host"] = refactor_host(xt)
     slab.close()
     prob.close()
     return out
+
+
+def refactor_host(xt, nfail=24):
+    """Host side of a deletion event on the C2 rod (host code only, after
+    the GPU measurements): the deletion surgery of nfail seeded elements
+    (K -= their element matrices, disconnected nodes fixed, boundary
+    conditions re-applied) and the ILUT refactor of the new K, which the
+    library pipelines over the host threads (serial-order ILUT timed beside
+    it).  Wall clock; the factor's re-upload to the device is not included."""
+    try:
+        pr = make_problem(xt)
+        xyz, conn = pr.mesh()
+        bc = np.repeat((xyz[:, 0] == 0.0).astype(np.int32), 3)
+        pr.apply_bc(bc)
+        nef = np.sort(np.random.default_rng(WORKLOAD["seed"]).choice(len(conn), nfail,
+                                                                      replace=False) + 1)
+        t0 = time.perf_counter()
+        pr.delete(nef.astype(np.int32), bc)
+        t1 = time.perf_counter()
+        K = pr.K()
+        t2 = time.perf_counter()
+        xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
+        t3 = time.perf_counter()
+        os.environ["XTFEM_ILUT_THREADS"] = "1"
+        try:
+            t4 = time.perf_counter()
+            xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
+            t5 = time.perf_counter()
+        finally:
+            del os.environ["XTFEM_ILUT_THREADS"]
+        pr.close()
+        return {"deleted_elements": nfail, "surgery_ms": round((t1 - t0) * 1e3, 1),
+                "ilut_ms": round((t3 - t2) * 1e3, 1),
+                "ilut_ms_one_thread": round((t5 - t4) * 1e3, 1),
+                "host_threads": os.cpu_count() or 1,
+                "timer": "host wall clock", "scope": "deletion surgery + ILUT(1e-4, 20) of "
+                "the C2 K; the device re-upload of the factor is not included"}
+    except Exception as e:  # a failure here must not cost the measurements above
+        return {"error": f"{type(e).__name__}: {e}"}
 
 
 def rod_system(xt, n, amp, dt=0.5, freq=20.0):

@@ -195,6 +195,36 @@ def test_product_ilut_identical_to_oracle_at_c2_size(xt, orc):
     assert np.array_equal(got[0], alu)
 
 
+def test_ilut_row_pipeline_same_factor_and_first_failure_for_any_thread_count(
+        xt, orc, monkeypatch):
+    """The product pipelines ILUT rows over host threads
+    (XTFEM_ILUT_THREADS): the factor is the oracle's bit for bit at 1, 3 and
+    8 threads; a zero row gives -5 at every thread count; and a capacity that
+    runs out in an early row gives that row's storage code, not the later
+    zero row's, as in the reference, which stops at its first failing row."""
+    pr = rod_problem(xt, 24, 8, 8)
+    xyz, _ = pr.mesh()
+    pr.apply_bc(clamp_mask(xyz))
+    K = pr.K()
+    pr.close()
+    (alu, jlu, ju), _ = orc.ilut(K, 20, 1e-4)
+    bad = xt.Csr(K.ia, K.ja, K.a.copy())
+    z = 4000
+    bad.a[K.ia[z] - 1:K.ia[z + 1] - 1] = 0.0
+    small = K.n + 2 + 300
+    assert orc.ilut(bad, 20, 1e-4)[1] == -5
+    early = orc.ilut(bad, 20, 1e-4, iwk=small)[1]
+    assert early in (-2, -3)
+    for t in (1, 3, 8):
+        monkeypatch.setenv("XTFEM_ILUT_THREADS", str(t))
+        got = xt.ilut(K, 20, 1e-4)
+        assert all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju))), t
+        for iwk, code in ((None, -5), (small, early)):
+            with pytest.raises(xt.XtError) as e:
+                xt.ilut(bad, 20, 1e-4, iwk)
+            assert e.value.ierr == code, (t, iwk)
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)

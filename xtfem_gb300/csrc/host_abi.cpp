@@ -254,15 +254,16 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
         m.ja.assign(ja, ja + (ia[n] - 1));
         m.a.assign(a, a + (ia[n] - 1));
         Msr f;
-        int ierr = ilut(m, lfil, droptol, f);
-        if (ierr != 0) return ierr;
-        // The storage test of src/ilut.f:152-495, row by row on the finished
-        // factor: -2 when an L entry would be stored past iwk, -3 when the
-        // U part (counted with its diagonal, as the reference counts it)
-        // would end past iwk.  The first failing row decides, as in the
-        // reference, which stops there.
+        const int ierr = ilut(m, lfil, droptol, f);
+        // The storage test of src/ilut.f:152-495, row by row over the rows
+        // the factorisation finished: -2 when an L entry would be stored
+        // past iwk, -3 when the U part (counted with its diagonal, as the
+        // reference counts it) would end past iwk.  The first failing row
+        // decides, as in the reference, which stops there: a storage failure
+        // before the row that failed otherwise wins.
         long long pos = (long long)n + 2;  // 1-based next free slot
-        for (int i = 0; i < n; ++i) {
+        const int rows = (int)f.ju.size();
+        for (int i = 0; i < rows; ++i) {
             const long long nl = f.ju[i] - f.jlu[i];
             if (nl > 0 && pos + nl - 1 > iwk) return -2;
             pos += nl;
@@ -270,6 +271,7 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
             if (nu + 1 + pos > iwk) return -3;
             pos += nu;
         }
+        if (ierr != 0) return ierr;
         if ((long long)f.alu.size() > iwk) return -3;
         std::memcpy(alu, f.alu.data(), f.alu.size() * sizeof(double));
         std::memcpy(jlu, f.jlu.data(), f.jlu.size() * sizeof(int));

@@ -14,7 +14,22 @@
 //   * L keeps at most lfil entries, U at most lfil-1 off-diagonal entries;
 //   * a zero pivot is replaced by (1e-4 + droptol) * tnorm where 1e-4 is the
 //     reference's single-precision literal.
+//
+// Rows are pipelined over host threads.  Row i eliminates with earlier rows
+// in ascending column order, so it needs its nearest predecessors last: a
+// thread works on row i while rows i-1, i-2, ... are still being finished
+// by other threads, and waits on a row's done flag only when it reaches
+// that row.  Every row does the same arithmetic in the same order whatever
+// the thread count, so the factor is bit-for-bit the serial one; a failing
+// row stops the rows after it, and the lowest failing row's code is the
+// result, as in the reference, which stops at its first failing row.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <functional>
+#include <cstdlib>
+#include <memory>
+#include <thread>
 #include <vector>
 
 #include "host_sparse.h"
@@ -49,20 +64,74 @@ void split_largest(double* v, int* idx, int n, int cut)
 
 }  // namespace
 
-int ilut(const Csr& A, int lfil, double droptol, Msr& F)
+namespace {
+
+// Append-only storage of finished rows for one thread: blocks never move,
+// so other threads can read a finished row while more rows are appended.
+struct RowStore {
+    std::vector<std::unique_ptr<double[]>> vals;
+    std::vector<std::unique_ptr<int[]>> cols;
+    size_t used = 0, cap = 0, block;
+    explicit RowStore(size_t b) : block(b) {}
+    void take(size_t len, double*& v, int*& c)
+    {
+        if (used + len > cap) {
+            vals.emplace_back(new double[block]);
+            cols.emplace_back(new int[block]);
+            used = 0;
+            cap = block;
+        }
+        v = vals.back().get() + used;
+        c = cols.back().get() + used;
+        used += len;
+    }
+};
+
+// One finished row: L multipliers and U off-diagonals (0-based columns) in
+// the order they are stored, and the inverted pivot.
+struct RowOut {
+    const double* lv = nullptr;
+    const int* lc = nullptr;
+    const double* uv = nullptr;
+    const int* uc = nullptr;
+    int nl = 0, nu = 0;
+    double dinv = 0.0;
+};
+
+struct Shared {
+    const Csr& A;
+    int n, lfil;
+    double droptol;
+    std::vector<RowOut> rows;
+    std::unique_ptr<std::atomic<int>[]> done;
+    std::atomic<int> first_fail;
+    std::vector<int> code;  // error code of a failing row
+    Shared(const Csr& a, int lf, double dt)
+        : A(a), n(a.n), lfil(lf), droptol(dt), rows(a.n), done(new std::atomic<int>[a.n]),
+          first_fail(a.n), code(a.n, 0)
+    {
+        for (int i = 0; i < n; ++i) done[i].store(0, std::memory_order_relaxed);
+    }
+    void fail(int i, int c)
+    {
+        code[i] = c;
+        int cur = first_fail.load();
+        while (i < cur && !first_fail.compare_exchange_weak(cur, i)) {}
+    }
+};
+
+// Rows first, first + stride, ... of the factor, stored in `store` (which
+// outlives the call: the rows are read again when the factor is assembled).
+// Returns when its rows are done or a row at or below one of its rows has
+// failed.
+void factor_rows(Shared& S, RowStore& store, int first, int stride)
 {
-    const int n = A.n;
-    if (lfil < 0) return -4;
-    F.n = n;
-    // Built in SPARSKIT's 1-based position space (vector index == position,
-    // index 0 a pad dropped at the end): alu[1..n] inverted diagonal,
-    // jlu[1..n+1] row starts, off-diagonal entries from position n+2.
-    F.ju.assign(n, 0);
-    F.jlu.assign(n + 2, 0);
-    F.alu.assign(n + 2, 0.0);
-    // Row workspace.  Slots [0, lenl) hold the L part (column, value), slot
-    // i the diagonal and slots (i, i+lenu) the U part; where[c] is the slot
-    // of column c in the current row, or -1.
+    const int n = S.n, lfil = S.lfil;
+    const double droptol = S.droptol;
+    const Csr& A = S.A;
+    // Row workspace.  Slots [0, lenl) hold the L candidates (column, value),
+    // slot i the diagonal and slots (i, i+lenu) the U part; where[c] is the
+    // slot of column c in the current row, or -1.
     std::vector<double> w(n + 1);
     std::vector<int> col(n + 1), where(n, -1);
     // L candidates waiting for elimination, as a bit set of columns read
@@ -75,14 +144,12 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
     std::vector<unsigned long long> pending((size_t)n / 64 + 2, 0ull);
     std::vector<double> wl(n + 1);
     std::vector<int> cl(n + 1);
-    F.jlu[1] = n + 2;
-    F.alu.reserve((size_t)n * (2 * lfil + 2));
-    F.jlu.reserve((size_t)n * (2 * lfil + 2));
-    for (int i = 0; i < n; ++i) {
+    for (int i = first; i < n; i += stride) {
+        if (S.first_fail.load(std::memory_order_relaxed) < i) return;
         const int b = A.ia[i] - 1, e = A.ia[i + 1] - 1;
         double tnorm = 0.0;
         for (int k = b; k < e; ++k) tnorm += std::fabs(A.a[k]);
-        if (tnorm == 0.0) return -5;
+        if (tnorm == 0.0) { S.fail(i, -5); return; }
         tnorm /= (double)(float)(e - b);
         int lenl = 0, lenu = 1;
         col[i] = i;
@@ -98,8 +165,8 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
             } else if (c == i) {
                 w[i] = A.a[k];
             } else {
-                const int s = i + lenu;
-                col[s] = c; w[s] = A.a[k]; where[c] = s; ++lenu;
+                const int sl = i + lenu;
+                col[sl] = c; w[sl] = A.a[k]; where[c] = sl; ++lenu;
             }
         }
         // eliminate with earlier rows in ascending column order
@@ -111,29 +178,34 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
             if (wd >= wend) break;
             const int r = (int)(wd << 6) + __builtin_ctzll(pending[wd]);
             pending[wd] &= pending[wd] - 1;  // clear the lowest set bit
-            const double fact = w[where[r]] * F.alu[r + 1];
+            // row r finished (by this thread or another)?
+            for (int spins = 0; S.done[r].load(std::memory_order_acquire) == 0; ++spins) {
+                if (S.first_fail.load(std::memory_order_relaxed) < i) return;
+                if (spins > 64) std::this_thread::yield();
+            }
+            const RowOut& R = S.rows[r];
+            const double fact = w[where[r]] * R.dinv;
             where[r] = -1;
             if (std::fabs(fact) <= droptol) continue;
-            // row r of U: MSR positions ju[r] .. jlu[r+1]-1 (1-based)
-            for (int k = F.ju[r]; k <= F.jlu[r + 2] - 1; ++k) {
-                const double s = fact * F.alu[k];
-                const int c = F.jlu[k] - 1;
+            for (int k = 0; k < R.nu; ++k) {
+                const double sv = fact * R.uv[k];
+                const int c = R.uc[k];
                 const int slot = where[c];
                 if (c >= i) {
                     if (slot < 0) {
-                        if (lenu + 1 > n) return -1;
+                        if (lenu + 1 > n) { S.fail(i, -1); return; }
                         const int ns = i + lenu;
-                        col[ns] = c; where[c] = ns; w[ns] = -s; ++lenu;
+                        col[ns] = c; where[c] = ns; w[ns] = -sv; ++lenu;
                     } else {
-                        w[slot] -= s;
+                        w[slot] -= sv;
                     }
                 } else {
                     if (slot < 0) {
-                        if (lenl + 1 > n) return -1;
-                        col[lenl] = c; where[c] = lenl; w[lenl] = -s; ++lenl;
+                        if (lenl + 1 > n) { S.fail(i, -1); return; }
+                        col[lenl] = c; where[c] = lenl; w[lenl] = -sv; ++lenl;
                         pending[(size_t)c >> 6] |= 1ull << (c & 63);
                     } else {
-                        w[slot] -= s;
+                        w[slot] -= sv;
                     }
                 }
             }
@@ -142,14 +214,10 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
             ++kept;
         }
         for (int k = 0; k < lenu; ++k) where[col[i + k]] = -1;
+        RowOut& O = S.rows[i];
         // L row: the lfil largest multipliers
         const int nl = kept < lfil ? kept : lfil;
         split_largest(wl.data(), cl.data(), kept, nl);
-        for (int k = 0; k < nl; ++k) {
-            F.alu.push_back(wl[k]);
-            F.jlu.push_back(cl[k] + 1);
-        }
-        F.ju[i] = (int)F.jlu.size();  // 1-based start of U row i
         // U row: threshold, then the lfil-1 largest off-diagonals
         int nu = 0;
         for (int k = 1; k < lenu; ++k)
@@ -161,17 +229,76 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
         const int lenu2 = nu + 1;
         const int keep = lenu2 < lfil ? lenu2 : lfil;
         split_largest(w.data() + i + 1, col.data() + i + 1, lenu2 - 1, keep);
-        for (int k = 1; k <= keep - 1; ++k) {
-            F.alu.push_back(w[i + k]);
-            F.jlu.push_back(col[i + k] + 1);
-        }
+        double* v;
+        int* c;
+        store.take((size_t)nl + (keep > 1 ? keep - 1 : 0), v, c);
+        for (int k = 0; k < nl; ++k) { v[k] = wl[k]; c[k] = cl[k]; }
+        O.lv = v; O.lc = c; O.nl = nl;
+        for (int k = 1; k <= keep - 1; ++k) { v[nl + k - 1] = w[i + k]; c[nl + k - 1] = col[i + k]; }
+        O.uv = v + nl; O.uc = c + nl; O.nu = keep > 1 ? keep - 1 : 0;
         if (w[i] == 0.0) w[i] = ((double)0.0001f + droptol) * tnorm;
-        F.alu[i + 1] = 1.0 / w[i];
-        F.jlu[i + 2] = (int)F.jlu.size();
+        O.dinv = 1.0 / w[i];
+        S.done[i].store(1, std::memory_order_release);
     }
-    F.alu.erase(F.alu.begin());
-    F.jlu.erase(F.jlu.begin());
-    return 0;
+}
+
+int ilut_threads(int n)
+{
+    if (const char* e = std::getenv("XTFEM_ILUT_THREADS")) {
+        const int t = std::atoi(e);
+        if (t >= 1) return t < 64 ? t : 64;
+    }
+    if (n < 16384) return 1;
+    const unsigned hw = std::thread::hardware_concurrency();
+    return hw == 0 ? 1 : (int)(hw < 16 ? hw : 16);
+}
+
+}  // namespace
+
+int ilut(const Csr& A, int lfil, double droptol, Msr& F)
+{
+    const int n = A.n;
+    if (lfil < 0) return -4;
+    Shared S(A, lfil, droptol);
+    const int T = n > 0 ? std::min(ilut_threads(n), n) : 1;
+    // one row store per thread; blocks hold at least one row's L and U
+    const size_t row_max = (size_t)(lfil < n ? lfil : n) * 2 + 2;
+    std::vector<RowStore> stores;
+    stores.reserve(T);
+    for (int t = 0; t < T; ++t) stores.emplace_back(row_max > 65536 ? row_max : 65536);
+    if (T <= 1) {
+        factor_rows(S, stores[0], 0, 1);
+    } else {
+        std::vector<std::thread> pool;
+        pool.reserve(T - 1);
+        for (int t = 1; t < T; ++t)
+            pool.emplace_back(factor_rows, std::ref(S), std::ref(stores[t]), t, T);
+        factor_rows(S, stores[0], 0, T);
+        for (auto& th : pool) th.join();
+    }
+    // SPARSKIT MSR, 1-based: alu(1..n) inverted pivots, alu(n+1) unused,
+    // rows' L then U entries from position n+2; jlu(1..n+1) row starts,
+    // jlu(k >= n+2) columns; ju(i) the start of row i's U entries.  After a
+    // failure only the rows before the failing one are filled in (ju has
+    // that many entries), for a caller that checks storage row by row.
+    const int f = S.first_fail.load();
+    size_t tot = 0;
+    for (int i = 0; i < f; ++i) tot += (size_t)S.rows[i].nl + S.rows[i].nu;
+    F.n = n;
+    F.alu.assign((size_t)n + 1 + tot, 0.0);
+    F.jlu.assign((size_t)n + 1 + tot, 0);
+    F.ju.assign(f, 0);
+    size_t pos = (size_t)n + 2;
+    for (int i = 0; i < f; ++i) {
+        const RowOut& R = S.rows[i];
+        F.jlu[i] = (int)pos;
+        for (int k = 0; k < R.nl; ++k, ++pos) { F.alu[pos - 1] = R.lv[k]; F.jlu[pos - 1] = R.lc[k] + 1; }
+        F.ju[i] = (int)pos;
+        for (int k = 0; k < R.nu; ++k, ++pos) { F.alu[pos - 1] = R.uv[k]; F.jlu[pos - 1] = R.uc[k] + 1; }
+        F.alu[i] = R.dinv;
+    }
+    F.jlu[f] = (int)pos;
+    return f < n ? S.code[f] : 0;
 }
 
 }  // namespace xt
