@@ -273,6 +273,8 @@ def run_gpu(args, rank, world):
     if rank == 0 and not args.skip_cpu:
         out["cpu_baseline"] = cpu_baseline(its=float(np.mean(its)), sample_its=args.cpu_its,
                                            threads=os.cpu_count() or 1, for_arm=False)
+    if rank == 0 and not args.skip_variants:
+        out["variants"] = run_variants(xt, args)
     if rank == 0:
         out["refactor_host"] = refactor_host(xt)
     slab.close()
@@ -483,6 +485,41 @@ def run_fp64_reference_point(xt, args):
             "iterations_per_slab": float(np.mean([s["its"] for s in st]))}
 
 
+def run_variants(xt, args):
+    """The C2 slab two more ways, timed like fp64_gpu (CUDA events around
+    n slabs after one untimed slab): without the damage update (the solve,
+    load and jump terms only; sequential loop), and with the damage update
+    at a reduced temporal resolution (16 points per load cycle, 1,600 per
+    slab instead of 25,600; overlapped loop as the headline)."""
+    out = {}
+    variants = (("no_damage", {"damage": 0, "overlap": 0}),
+                ("reduced_nip", {"nipc": 16}))
+    for name, change in variants:
+        try:
+            prob = make_problem(xt)
+            cfg = make_config(xt, precision=WORKLOAD["precision"], seed=WORKLOAD["seed"])
+            for k, v in change.items():
+                setattr(cfg, k, v)
+            slab = xt.SlabSolver(prob, cfg)
+            slab.step()
+            xt.lib().xt_sync()
+            n = max(1, min(args.steps, 3))
+            xt.lib().xt_mark(4)
+            st = [slab.step() for _ in range(n)]
+            slab.drain()
+            xt.lib().xt_mark(5)
+            ms = xt.lib().xt_elapsed_ms(4, 5)
+            slab.close()
+            prob.close()
+            out[name] = {"value": round(n / (ms / 1e3), 4), "unit": UNIT, "steps": n,
+                         "nip": cfg.nipc * cfg.n1, "damage": int(cfg.damage),
+                         "iterations_per_slab": float(np.mean([s["its"] for s in st])),
+                         "relres_max": float(max(s["relres"] for s in st))}
+        except Exception as e:  # a failure here must not cost the headline line
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
 def run_e2e(xt, args, world):
     """Same slabs through the public API with host buffers: the load blocks
     go host->device and the slab displacement and damage come back, every
@@ -677,6 +714,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-variants", action="store_true",
+                    help="skip the no-damage and reduced-nip slab lines")
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--im", type=int, default=None)
     ap.add_argument("--specimens", type=int, default=8,

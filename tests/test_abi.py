@@ -132,3 +132,11 @@ def test_gmres_log_empty_and_line_format(xt):
     assert xt.gmres_log_lines([1.0, 0.25], iout=0) == lines[:1]
     assert xt.gmres_log_lines([1.0, 0.25], iout=-1) == []
     assert xt.api.fortran_d20_6(-123456.7) == "       -0.123457D+06"
+
+
+def test_failed_construction_leaves_nothing_to_close(xt):
+    """A handle class whose constructor raised closes quietly (its __del__
+    runs on a half-built object)."""
+    for cls in (xt.SpaceTimeSystem, xt.SystemBatch, xt.Problem, xt.ThermalSolver, xt.SlabSolver):
+        obj = cls.__new__(cls)
+        obj.close()

@@ -288,7 +288,8 @@ class SpaceTimeSystem:
         self._h = h
 
     def close(self):
-        if self._h:
+        # also called by __del__ of an object whose constructor raised
+        if getattr(self, "_h", None):
             lib().xt_system_destroy(self._h)
             self._h = None
 
@@ -367,7 +368,8 @@ class SystemBatch:
         self._h = h
 
     def close(self):
-        if self._h:
+        # also called by __del__ of an object whose constructor raised
+        if getattr(self, "_h", None):
             lib().xt_batch_destroy(self._h)
             self._h = None
 
@@ -427,7 +429,8 @@ class Problem:
         return cls(h)
 
     def close(self):
-        if self._h:
+        # also called by __del__ of an object whose constructor raised
+        if getattr(self, "_h", None):
             lib().xth_problem_destroy(self._h)
             self._h = None
 
@@ -540,7 +543,8 @@ class ThermalSolver:
         self._h = h
 
     def close(self):
-        if self._h:
+        # also called by __del__ of an object whose constructor raised
+        if getattr(self, "_h", None):
             lib().xt_thermal_destroy(self._h)
             self._h = None
 
@@ -574,7 +578,8 @@ class SlabSolver:
         self.p, self.ne, self.ngp = 3 * nn, ne, 8 * ne
 
     def close(self):
-        if self._h:
+        # also called by __del__ of an object whose constructor raised
+        if getattr(self, "_h", None):
             lib().xt_slab_destroy(self._h)
             self._h = None
 
