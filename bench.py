@@ -303,13 +303,17 @@ def refactor_host(xt, nfail=24):
         t2 = time.perf_counter()
         xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
         t3 = time.perf_counter()
+        prev = os.environ.get("XTFEM_ILUT_THREADS")
         os.environ["XTFEM_ILUT_THREADS"] = "1"
         try:
             t4 = time.perf_counter()
             xt.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
             t5 = time.perf_counter()
         finally:
-            del os.environ["XTFEM_ILUT_THREADS"]
+            if prev is None:
+                del os.environ["XTFEM_ILUT_THREADS"]
+            else:
+                os.environ["XTFEM_ILUT_THREADS"] = prev
         pr.close()
         return {"deleted_elements": nfail, "surgery_ms": round((t1 - t0) * 1e3, 1),
                 "ilut_ms": round((t3 - t2) * 1e3, 1),
