@@ -85,7 +85,7 @@ void kronlusol_(const double *a, const int *q, const double *alu,
  * convergence (|rs(i+1)| <= eps ||r0||) and ierr conventions (0, 1, -1;
  * library errors <= -10).  rhs is used as scratch as in the reference
  * (its content on return is unspecified).  The reference writes its
- * residual history to Fortran unit iout (:257-259, :311; the driver opens
+ * residual history to Fortran unit iout (:257-259, :311; src/main3d.f90 opens
  * it as gmres.log); a C library cannot write to a Fortran unit, so with
  * iout >= 0 the history is kept for xt_gmres_log and the caller's shim
  * writes the lines (iout < 0: nothing is kept). */
