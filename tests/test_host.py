@@ -225,6 +225,30 @@ def test_ilut_row_pipeline_same_factor_and_first_failure_for_any_thread_count(
             assert e.value.ierr == code, (t, iwk)
 
 
+def test_ilut_rows_without_off_diagonals(xt, orc, monkeypatch):
+    """Rows with no off-diagonal entries (a clamped DOF's identity row, here
+    the first row of the notched plate, whose clamped edge is numbered
+    first; and a diagonal matrix) factor like the oracle at 1 and 4
+    threads."""
+    from xtfem_gb300.meshes import sent_plate
+
+    xyz, conn = sent_plate(12, 24, 2)
+    pr = xt.Problem.from_mesh(xyz, conn)
+    bc = np.repeat((xyz[:, 1] == 0.0).astype(np.int32), 3)
+    assert bc[0] == 1
+    pr.apply_bc(bc)
+    K = pr.K()
+    pr.close()
+    D = xt.Csr(np.arange(1, 6), np.arange(1, 5), np.array([1.0, 2.0, 3.0, 4.0]))
+    for A in (K, D):
+        (alu, jlu, ju), ierr = orc.ilut(A, 20, 1e-4)
+        assert ierr == 0
+        for t in (1, 4):
+            monkeypatch.setenv("XTFEM_ILUT_THREADS", str(t))
+            got = xt.ilut(A, 20, 1e-4)
+            assert all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju))), (A.n, t)
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)

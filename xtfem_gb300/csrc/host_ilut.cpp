@@ -75,7 +75,8 @@ struct RowStore {
     explicit RowStore(size_t b) : block(b) {}
     void take(size_t len, double*& v, int*& c)
     {
-        if (used + len > cap) {
+        // a block exists before the first row is stored, even an empty row
+        if (vals.empty() || used + len > cap) {
             vals.emplace_back(new double[block]);
             cols.emplace_back(new int[block]);
             used = 0;
