@@ -524,3 +524,15 @@ def test_holed_panel_generator(xt):
     K = pr.K().to_scipy()
     assert abs(K - K.T).max() <= 1e-10 * abs(K).max()
     pr.close()
+    # the ray-first numbering: the same nodes and elements, renumbered, and
+    # a bandwidth of one ray instead of one ring
+    xr, cr = holed_panel(32, 6, 1, W=1.0, t=0.05, radius=0.1, order="rays")
+    assert sorted(map(tuple, xr)) == sorted(map(tuple, xyz))
+    assert sorted(tuple(sorted(map(tuple, xr[c - 1]))) for c in cr) == \
+        sorted(tuple(sorted(map(tuple, xyz[c - 1]))) for c in conn)
+    for e in range(len(cr)):
+        assert np.linalg.det((sign / 8.0).T @ xr[cr[e] - 1]) > 0
+    # node-number spread of the elements, leaving out the few that close the
+    # O-grid (3 % of them here)
+    spread = lambda c: np.percentile(np.ptp(c, axis=1), 95)
+    assert spread(cr) < spread(conn) / 3
