@@ -249,6 +249,31 @@ def test_ilut_rows_without_off_diagonals(xt, orc, monkeypatch):
             assert all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju))), (A.n, t)
 
 
+def test_ilut_of_the_thermal_matrix_matches_oracle(xt, orc):
+    """The thermal slab's factor (one scalar DOF per node, both rod ends at
+    a fixed temperature, so the first rows are identity rows): product and
+    oracle ILUT agree bit for bit on a conductivity matrix integrated in
+    numpy."""
+    import scipy.sparse as sp
+    from test_gpu_thermal import applybc, thermal_element, to_csr
+
+    pr = rod_problem(xt)
+    xyz, conn = pr.mesh()
+    pr.close()
+    nn = len(xyz)
+    rows, cols, kv = [], [], []
+    for e in range(len(conn)):
+        ke, _ = thermal_element(xyz[conn[e] - 1])
+        idx = conn[e] - 1
+        rows += list(np.repeat(idx, 8)); cols += list(np.tile(idx, 8)); kv += list(ke.ravel())
+    bc = np.isin(xyz[:, 0], [0.0, 3.0]).astype(int)
+    assert bc[0] == 1
+    Kt = to_csr(xt, applybc(sp.csr_matrix((kv, (rows, cols)), shape=(nn, nn)), bc))
+    (alu, jlu, ju), ierr = orc.ilut(Kt, 20, 1e-4)
+    got = xt.ilut(Kt, 20, 1e-4)
+    assert ierr == 0 and all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju)))
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)
@@ -299,7 +324,7 @@ def test_oracle_threaded_path_matches_serial(orc, c1):
 
 
 # ------------------------------------------------------------- deletion surgery
-def test_deletion_surgery_equals_assembly_of_surviving_elements(xt):
+def test_deletion_surgery_equals_assembly_of_surviving_elements(xt, orc):
     """delelement / chkcnsta / chkndsta / adddiagonal (src/delelement.f90:
     1-59, 139-247) on the host: after deleting a corner element (whose far
     corner node then belongs to no element) and an interior one, K equals
@@ -338,6 +363,10 @@ def test_deletion_surgery_equals_assembly_of_surviving_elements(xt):
     K, M = pr.K().to_scipy(), pr.M().to_scipy()
     assert abs(K - K_exp).max() <= 1e-10 * abs(K_exp).max()
     assert abs(M - M_exp).max() <= 1e-14 * abs(M_exp).max()
+    # the refactor after the surgery (identity rows of the disconnected node)
+    (alu, jlu, ju), ierr = orc.ilut(pr.K(), 20, 1e-4)
+    got = xt.ilut(pr.K(), 20, 1e-4)
+    assert ierr == 0 and all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju)))
     with pytest.raises(RuntimeError):
         pr.delete(np.array([ne + 1], np.int32), bc_new)
     pr.close()
