@@ -10,6 +10,9 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 /* Host threads for the Kronecker apply, the preconditioner and the Krylov
  * vector operations.  1 (the default) runs the reference's serial code
@@ -185,12 +188,28 @@ int orc_kronlusol(const double *a, int q, const double *alu, const int *jlu,
 
 static double ddot(size_t n, const double *x, const double *y)
 {
-    const int nt = g_threads;
+    const int nt = g_threads < 64 ? g_threads : 64;
     double s = 0.0;
     if (nt > 1) {
-        const long long nn = (long long)n;
-#pragma omp parallel for schedule(static) num_threads(nt) reduction(+ : s)
-        for (long long i = 0; i < nn; ++i) s += x[i] * y[i];
+        /* each thread sums its contiguous share; the shares are added in
+         * thread order, so a given thread count repeats bit for bit (an
+         * OpenMP reduction may combine them in any order) */
+        double part[64];
+        int used = 1;
+#pragma omp parallel num_threads(nt)
+        {
+#ifdef _OPENMP
+            const int t = omp_get_thread_num(), T = omp_get_num_threads();
+#else
+            const int t = 0, T = 1;
+#endif
+            const size_t b = n * (size_t)t / (size_t)T, e = n * (size_t)(t + 1) / (size_t)T;
+            double acc = 0.0;
+            for (size_t i = b; i < e; ++i) acc += x[i] * y[i];
+            part[t] = acc;
+            if (t == 0) used = T;
+        }
+        for (int t = 0; t < used; ++t) s += part[t];
         return s;
     }
     for (size_t i = 0; i < n; ++i) s += x[i] * y[i];

@@ -319,8 +319,16 @@ def test_oracle_threaded_path_matches_serial(orc, c1):
         orc.set_threads(1)
     assert np.array_equal(par[0], ser[0]) and np.array_equal(par[1], ser[1])
     (s0, e0, i0, _), (s1, e1, i1, _) = ser[2], par[2]
-    assert e0 == e1 == 0 and abs(i0 - i1) <= 2
+    # ~770 restarted iterations to 1e-12: the other summation order moves the
+    # count by a few; the threaded run repeats bit for bit
+    assert e0 == e1 == 0 and abs(i0 - i1) <= max(2, 0.02 * i0)
     assert np.linalg.norm(s1 - s0) <= 1e-9 * np.linalg.norm(s0)
+    try:
+        orc.set_threads(4)
+        again = run()
+    finally:
+        orc.set_threads(1)
+    assert again[2][2] == i1 and np.array_equal(again[2][0], s1)
 
 
 # ------------------------------------------------------------- deletion surgery
