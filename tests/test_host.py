@@ -61,6 +61,33 @@ def test_c1_mesh_arrays_match_fixture(c1):
 
 
 # ------------------------------------------------------------- assembly
+def test_mesh_file_reader(xt, c1, tmp_path):
+    """Problem.from_inp reads the reference's mesh-file layout (node count,
+    id x y z lines, element count, id n1..n8 lines): the C1 fixture's arrays
+    written that way come back exactly and give the generated rod's K; a
+    truncated or missing file is an error, not a crash."""
+    g = np.load(GOLDEN / "rod_c1_mesh.npz")
+    xyz, conn = g["xyz"], g["conn"]
+    lines = [str(len(xyz))]
+    lines += [f"{i + 1} {x:.17g} {y:.17g} {z:.17g}" for i, (x, y, z) in enumerate(xyz)]
+    lines += [str(len(conn))]
+    lines += [" ".join(map(str, [e + 1, *c])) for e, c in enumerate(conn)]
+    path = tmp_path / "rod.inp"
+    path.write_text("\n".join(lines) + "\n")
+    pr = xt.Problem.from_inp(path)
+    x2, c2 = pr.mesh()
+    assert np.array_equal(x2, xyz) and np.array_equal(c2, conn)
+    K = pr.K()
+    assert np.array_equal(K.ia, c1["K0"].ia) and np.array_equal(K.ja, c1["K0"].ja)
+    assert np.array_equal(K.a, c1["K0"].a)
+    pr.close()
+    bad = tmp_path / "bad.inp"
+    bad.write_text("\n".join(lines[: len(xyz) + 3]) + "\n")
+    for p in (bad, tmp_path / "missing.inp"):
+        with pytest.raises(xt.XtError):
+            xt.Problem.from_inp(p)
+
+
 def test_stiffness_symmetric_with_rigid_body_kernel(c1):
     K = c1["K0"].to_scipy()
     assert abs(K - K.T).max() <= 1e-9 * abs(K).max()
