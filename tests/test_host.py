@@ -88,6 +88,30 @@ def test_mesh_file_reader(xt, c1, tmp_path):
             xt.Problem.from_inp(p)
 
 
+def test_strain_rows_reproduce_affine_fields(xt, c1):
+    """The strain rows (the per-Gauss-point shape-function derivatives that
+    the damage update gathers strains with, src/kokkos_kernel.h:45-110): an
+    affine displacement u = G x gives the constant strain of G at every
+    point (engineering shear), on the rod and on the distorted O-grid
+    elements of the holed panel."""
+    from xtfem_gb300.meshes import holed_panel
+
+    G = np.array([[1.0, 0.3, -0.2], [0.5, -2.0, 0.7], [0.1, 0.4, 1.5]]) * 1e-3
+    want = np.array([G[0, 0], G[1, 1], G[2, 2], G[0, 1] + G[1, 0], G[1, 2] + G[2, 1],
+                     G[0, 2] + G[2, 0]])
+    panel = xt.Problem.from_mesh(*holed_panel(32, 6, 1))
+    for pr in (c1["pr"], panel):
+        xyz, conn = pr.mesh()
+        Nx, Ny, Nz = (r.reshape(len(conn), 8, 8) for r in pr.strain_rows())
+        u = xyz @ G.T
+        ue = u[conn - 1]  # (ne, 8 nodes, 3)
+        gx, gy, gz = (np.einsum("egi,eic->egc", N, ue) for N in (Nx, Ny, Nz))
+        eps = np.stack([gx[..., 0], gy[..., 1], gz[..., 2], gy[..., 0] + gx[..., 1],
+                        gz[..., 1] + gy[..., 2], gz[..., 0] + gx[..., 2]], -1)
+        assert np.abs(eps - want).max() <= 1e-12
+    panel.close()
+
+
 def test_stiffness_symmetric_with_rigid_body_kernel(c1):
     K = c1["K0"].to_scipy()
     assert abs(K - K.T).max() <= 1e-9 * abs(K).max()
