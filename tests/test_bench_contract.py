@@ -37,3 +37,22 @@ def test_gpu_arm_flags_parse():
     for flag in ("--gpus", "--steps", "--warmup", "--impl", "--skip-variants", "--rods",
                  "--specimens"):
         assert flag in p.stdout, flag
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Launched as for N > 1 (torchrun, two ranks, gloo on CPU): rank 0 runs
+    and prints the one line, the other rank exits 0 without work."""
+    import socket
+
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    p = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                        "--nproc-per-node", "2", "--master-addr", "127.0.0.1", "--master-port",
+                        str(port), "bench.py", "--impl", "reference", "--gpus", "2", "--steps",
+                        "1", "--warmup", "0", "--cpu-its", "4"], cwd=ROOT, capture_output=True,
+                       text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1 and json.loads(lines[0])["n_gpus"] == 2
