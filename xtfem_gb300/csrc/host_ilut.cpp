@@ -26,9 +26,12 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
-#include <functional>
 #include <cstdlib>
+#include <exception>
+#include <functional>
 #include <memory>
+#include <mutex>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -107,6 +110,8 @@ struct Shared {
     std::unique_ptr<std::atomic<int>[]> done;
     std::atomic<int> first_fail;
     std::vector<int> code;  // error code of a failing row
+    std::mutex error_m;     // an exception of a thread (allocation), for the caller
+    std::exception_ptr error;
     Shared(const Csr& a, int lf, double dt)
         : A(a), n(a.n), lfil(lf), droptol(dt), rows(a.n), done(new std::atomic<int>[a.n]),
           first_fail(a.n), code(a.n, 0)
@@ -243,6 +248,22 @@ void factor_rows(Shared& S, RowStore& store, int first, int stride)
     }
 }
 
+// factor_rows for a thread: an exception (an allocation that failed) is
+// kept for the calling thread, which rethrows it after the join, and stops
+// the other threads; it must not leave a thread function.
+void factor_rows_kept(Shared& S, RowStore& store, int first, int stride)
+{
+    try {
+        factor_rows(S, store, first, stride);
+    } catch (...) {
+        {
+            std::lock_guard<std::mutex> g(S.error_m);
+            if (!S.error) S.error = std::current_exception();
+        }
+        S.first_fail.store(-1);
+    }
+}
+
 int ilut_threads(int n)
 {
     if (const char* e = std::getenv("XTFEM_ILUT_THREADS")) {
@@ -256,32 +277,16 @@ int ilut_threads(int n)
 
 }  // namespace
 
-int ilut(const Csr& A, int lfil, double droptol, Msr& F)
+namespace {
+
+// SPARSKIT MSR, 1-based: alu(1..n) inverted pivots, alu(n+1) unused, rows'
+// L then U entries from position n+2; jlu(1..n+1) row starts, jlu(k >= n+2)
+// columns; ju(i) the start of row i's U entries.  After a failure only the
+// rows before the failing one are filled in (ju has that many entries), for
+// a caller that checks storage row by row.
+void assemble(const Shared& S, Msr& F)
 {
-    const int n = A.n;
-    if (lfil < 0) return -4;
-    Shared S(A, lfil, droptol);
-    const int T = n > 0 ? std::min(ilut_threads(n), n) : 1;
-    // one row store per thread; blocks hold at least one row's L and U
-    const size_t row_max = (size_t)(lfil < n ? lfil : n) * 2 + 2;
-    std::vector<RowStore> stores;
-    stores.reserve(T);
-    for (int t = 0; t < T; ++t) stores.emplace_back(row_max > 65536 ? row_max : 65536);
-    if (T <= 1) {
-        factor_rows(S, stores[0], 0, 1);
-    } else {
-        std::vector<std::thread> pool;
-        pool.reserve(T - 1);
-        for (int t = 1; t < T; ++t)
-            pool.emplace_back(factor_rows, std::ref(S), std::ref(stores[t]), t, T);
-        factor_rows(S, stores[0], 0, T);
-        for (auto& th : pool) th.join();
-    }
-    // SPARSKIT MSR, 1-based: alu(1..n) inverted pivots, alu(n+1) unused,
-    // rows' L then U entries from position n+2; jlu(1..n+1) row starts,
-    // jlu(k >= n+2) columns; ju(i) the start of row i's U entries.  After a
-    // failure only the rows before the failing one are filled in (ju has
-    // that many entries), for a caller that checks storage row by row.
+    const int n = S.n;
     const int f = S.first_fail.load();
     size_t tot = 0;
     for (int i = 0; i < f; ++i) tot += (size_t)S.rows[i].nl + S.rows[i].nu;
@@ -299,7 +304,54 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F)
         F.alu[i] = R.dinv;
     }
     F.jlu[f] = (int)pos;
-    return f < n ? S.code[f] : 0;
+}
+
+// The factor on T threads, assembled into F with its code in ierr; false
+// when a thread could not be started (the threads already running are
+// stopped and joined first, and F is left alone).
+bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr)
+{
+    const int n = A.n;
+    Shared S(A, lfil, droptol);
+    // one row store per thread; blocks hold at least one row's L and U
+    const size_t row_max = (size_t)(lfil < n ? lfil : n) * 2 + 2;
+    std::vector<RowStore> stores;
+    stores.reserve(T);
+    for (int t = 0; t < T; ++t) stores.emplace_back(row_max > 65536 ? row_max : 65536);
+    if (T <= 1) {
+        factor_rows_kept(S, stores[0], 0, 1);
+    } else {
+        std::vector<std::thread> pool;
+        pool.reserve(T - 1);
+        bool all = true;
+        try {
+            for (int t = 1; t < T; ++t)
+                pool.emplace_back(factor_rows_kept, std::ref(S), std::ref(stores[t]), t, T);
+        } catch (const std::system_error&) {
+            all = false;
+            S.first_fail.store(-1);  // every row is "after" it: the started threads stop
+        }
+        if (all) factor_rows_kept(S, stores[0], 0, T);
+        for (auto& th : pool) th.join();
+        if (S.error) std::rethrow_exception(S.error);
+        if (!all) return false;
+    }
+    if (S.error) std::rethrow_exception(S.error);
+    assemble(S, F);
+    const int f = S.first_fail.load();
+    ierr = f < n ? S.code[f] : 0;
+    return true;
+}
+
+}  // namespace
+
+int ilut(const Csr& A, int lfil, double droptol, Msr& F)
+{
+    if (lfil < 0) return -4;
+    const int T = A.n > 0 ? std::min(ilut_threads(A.n), A.n) : 1;
+    int ierr = 0;
+    if (!ilut_on(A, lfil, droptol, T, F, ierr)) ilut_on(A, lfil, droptol, 1, F, ierr);
+    return ierr;
 }
 
 }  // namespace xt
