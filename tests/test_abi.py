@@ -140,3 +140,16 @@ def test_failed_construction_leaves_nothing_to_close(xt):
     for cls in (xt.SpaceTimeSystem, xt.SystemBatch, xt.Problem, xt.ThermalSolver, xt.SlabSolver):
         obj = cls.__new__(cls)
         obj.close()
+
+
+def test_slab_log_line(xt):
+    """The per-slab JSON line: the step's statistics with integer counts, and
+    the host wall time."""
+    import json
+
+    stats = dict(zip(xt.api.STAT_KEYS, [3.0, 191.0, 1.0, 2.0, 0.0, 9.3e-9, 0.25, 4.0, 2.0,
+                                        10.0, 20.0, 30.0]))
+    rec = json.loads(xt.slab_log_line(stats, 0.3141))
+    assert rec["slab"] == 3 and rec["its"] == 191 and rec["deleted"] == 2
+    assert isinstance(rec["its"], int) and rec["relres"] == 9.3e-9 and rec["maxD"] == 0.25
+    assert rec["seconds"] == 0.3141 and len(rec) == len(stats) + 1

@@ -17,6 +17,7 @@ the operator and the slab state on the GPU.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, fields
 
 import numpy as np
@@ -24,10 +25,11 @@ import numpy as np
 from ._lib import XtError, _dp, check, dptr, dref, iptr, iref, lib
 
 __all__ = [
-    "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "gmres_log", "gmres_log_lines", "chkelesta", "kokkos_host",
-    "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m", "getfextc_t", "nt_table", "SpaceTimeSystem",
-    "SystemBatch", "ThermalConfig", "ThermalSolver",
-    "Problem", "SlabConfig", "SlabSolver", "set_cache", "invalidate", "profile", "profile_read",
+    "Csr", "kronspmv", "kronspgemv", "kronlusol", "kronpgmres", "gmres_log", "gmres_log_lines",
+    "chkelesta", "kokkos_host", "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m",
+    "getfextc_t", "nt_table", "SpaceTimeSystem", "SystemBatch", "ThermalConfig", "ThermalSolver",
+    "Problem", "SlabConfig", "SlabSolver", "slab_log_line", "set_cache", "invalidate", "profile",
+    "profile_read",
 ]
 
 
@@ -564,31 +566,58 @@ class ThermalSolver:
 
 STAT_KEYS = ["slab", "its", "cycles", "outer", "ierr", "relres", "maxD", "nfailed", "deleted",
              "plastic_steps", "screened_steps", "exact_steps"]
+_INT_STATS = {"slab", "its", "cycles", "outer", "ierr", "nfailed", "deleted", "plastic_steps",
+              "screened_steps", "exact_steps"}
+
+
+def slab_log_line(stats, seconds):
+    """One slab as one JSON line: the slab's statistics (iterations, the true
+    relative residual, max D, failed and newly deleted elements, damage
+    steps) and its host wall time in seconds."""
+    import json
+
+    rec = {k: (int(v) if k in _INT_STATS else float(v)) for k, v in stats.items()}
+    rec["seconds"] = round(float(seconds), 6)
+    return json.dumps(rec)
 
 
 class SlabSolver:
     """The mechanical slab loop with its state on the GPU."""
 
-    def __init__(self, problem: Problem, cfg: SlabConfig):
+    def __init__(self, problem: Problem, cfg: SlabConfig, log=None):
+        """log: a path or text file; each step() then appends one JSON line
+        (slab_log_line) to it."""
         self.problem, self.cfg = problem, cfg
         h = C.c_void_p()
         check(lib().xt_slab_create(problem._h, C.byref(cfg), C.byref(h)), "xt_slab_create")
         self._h = h
         nn, ne, _, _ = problem.sizes()
         self.p, self.ne, self.ngp = 3 * nn, ne, 8 * ne
+        self._own_log = isinstance(log, (str, bytes, os.PathLike))
+        self._log = open(log, "a") if self._own_log else log
 
     def close(self):
         # also called by __del__ of an object whose constructor raised
         if getattr(self, "_h", None):
             lib().xt_slab_destroy(self._h)
             self._h = None
+        if getattr(self, "_own_log", False) and self._log is not None:
+            self._log.close()
+            self._log = None
 
     __del__ = close
 
     def step(self):
+        import time
+
         st = np.zeros(12)
+        t0 = time.perf_counter()
         check(lib().xt_slab_step(self._h, dptr(st)), "xt_slab_step")
-        return dict(zip(STAT_KEYS, st.tolist()))
+        out = dict(zip(STAT_KEYS, st.tolist()))
+        if getattr(self, "_log", None) is not None:
+            self._log.write(slab_log_line(out, time.perf_counter() - t0) + "\n")
+            self._log.flush()
+        return out
 
     def step_host(self, fext, disp_out, D_out):
         st = np.zeros(12)
