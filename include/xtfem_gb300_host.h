@@ -64,6 +64,15 @@ int xth_problem_delete(xth_problem pr, int nef, const int *nefail, int *bc,
  * norm, with 1e-4 rounded to single precision as in the reference. */
 int xth_ilut(int n, const int *ia, const int *ja, const double *a, int lfil,
              double droptol, int iwk, double *alu, int *jlu, int *ju);
+/* The same factor when rows [0, first_row) of the matrix equal those of the
+ * matrix prev_alu/prev_jlu/prev_ju was computed from (same lfil, droptol):
+ * those rows are copied and the rest refactored (ILUT row i depends only on
+ * rows <= i).  After a deletion, first_row is 3 (m - 1) for the smallest
+ * node m of the failed elements.  No counterpart in the reference, which
+ * refactors every row. */
+int xth_ilut_update(int n, const int *ia, const int *ja, const double *a, int lfil,
+                    double droptol, int iwk, int first_row, const double *prev_alu,
+                    const int *prev_jlu, const int *prev_ju, double *alu, int *jlu, int *ju);
 
 /* src/stcoeff.f90:62-356 (mechanical, 6x6) and 1-60 (thermal, 3x3),
  * column-major. */

@@ -325,6 +325,42 @@ def test_ilut_of_the_thermal_matrix_matches_oracle(xt, orc):
     assert ierr == 0 and all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju)))
 
 
+def test_refactor_from_the_first_changed_row(xt):
+    """After a deletion only the DOF rows of the failed elements' nodes
+    change, so the factor's rows below 3 (m - 1), m the smallest such node,
+    are kept and the others refactored: the result equals a full refactor
+    bit for bit, on the rod (failures near the clamp, numbered last, and in
+    the middle) at 1 and 4 threads."""
+    import os
+
+    pr = rod_problem(xt, 30, 10, 10)
+    xyz, conn = pr.mesh()
+    bc = clamp_mask(xyz)
+    pr.apply_bc(bc)
+    old = xt.ilut(pr.K(), 20, 1e-4)
+    ne = len(conn)
+    near_clamp = np.flatnonzero(xyz[conn - 1][:, :, 0].min(1) == 0.0)[:3] + 1
+    middle = np.array([ne // 2, ne // 2 + 7]) + 1
+    try:
+        for nef in (near_clamp, middle):
+            nef = np.sort(nef).astype(np.int32)
+            pr.delete(nef, bc)
+            K = pr.K()
+            r0 = 3 * (int(conn[nef - 1].min()) - 1)
+            for t in ("1", "4"):
+                os.environ["XTFEM_ILUT_THREADS"] = t
+                full = xt.ilut(K, 20, 1e-4)
+                upd = xt.ilut(K, 20, 1e-4, reuse=(*old, r0))
+                assert all(np.array_equal(a, b) for a, b in zip(full, upd)), (nef, t)
+            # the rows below r0 were indeed unchanged by the surgery
+            assert np.array_equal(full[1][: r0 + 1], old[1][: r0 + 1])
+            old = full
+    finally:
+        os.environ.pop("XTFEM_ILUT_THREADS", None)
+    assert r0 > 0
+    pr.close()
+
+
 def test_qsplit_partial_order(orc):
     rng = np.random.default_rng(4)
     a = rng.standard_normal(50)

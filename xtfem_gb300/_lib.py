@@ -81,6 +81,8 @@ SIGNATURES = {
     "xth_stcoeff_t": (None, [C.c_double] + [_dp] * 6),
     "xth_getfextc_m": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "xth_getfextc_t": (None, [C.c_double, C.c_double, _dp]),
+    "xth_ilut_update": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
+                                  _dp, _ip, _ip, _dp, _ip, _ip]),
     "xt_gmres_log": (C.c_int, [_dp, C.c_int]),
     "xth_nt_table": (None, [C.c_int, _dp, C.c_double, _dp]),
     "xt_thermal_create": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),

@@ -218,18 +218,27 @@ def kokkos_host(rank, ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, nodes, Nx, Ny,
     _raise_if_error()
 
 
-def ilut(A: Csr, lfil=20, droptol=1e-4, iwk=None):
+def ilut(A: Csr, lfil=20, droptol=1e-4, iwk=None, reuse=None):
     """SPARSKIT ILUT on the host in FP64 (src/ilut.f:152-495).  Returns
     (alu, jlu, ju) in MSR form with 1-based indices, trimmed to size.  iwk
     is the capacity of alu/jlu (default: enough for any factor); an error
-    raises XtError carrying SPARSKIT's ierr (.ierr)."""
+    raises XtError carrying SPARSKIT's ierr (.ierr).  reuse = (alu, jlu, ju,
+    first_row): the factor of a matrix whose rows [0, first_row) equal A's
+    (same lfil, droptol); those rows are copied, the others refactored, and
+    the result is A's factor bit for bit."""
     n = A.n
     iwk = iwk or n * (2 * max(lfil, 0) + 2) + n + 2
     alu = np.zeros(iwk)
     jlu = np.zeros(iwk, np.int32)
     ju = np.zeros(n, np.int32)
-    ierr = lib().xth_ilut(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk, dptr(alu),
-                          iptr(jlu), iptr(ju))
+    if reuse is None:
+        ierr = lib().xth_ilut(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk,
+                              dptr(alu), iptr(jlu), iptr(ju))
+    else:
+        palu, pjlu, pju = _f64(reuse[0]), _i32(reuse[1]), _i32(reuse[2])
+        ierr = lib().xth_ilut_update(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk,
+                                     int(reuse[3]), dptr(palu), iptr(pjlu), iptr(pju),
+                                     dptr(alu), iptr(jlu), iptr(ju))
     if ierr != 0:
         err = XtError(f"ilut failed with ierr = {ierr}")
         err.ierr = ierr

@@ -240,8 +240,8 @@ int xth_problem_delete(xth_problem h, int nef, const int* nefail, int* bc, int* 
     return guarded([&] { return P(h)->delete_elements(nef, nefail, bc, ndf_out); });
 }
 
-int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, double droptol,
-             int iwk, double* alu, int* jlu, int* ju)
+static int ilut_into(int n, const int* ia, const int* ja, const double* a, int lfil, double droptol,
+                     int iwk, double* alu, int* jlu, int* ju, const Msr* prev, int first_row)
 {
     if (n <= 0 || !ia || !ja || !a || !alu || !jlu || !ju) {
         set_error("xth_ilut: bad arguments");
@@ -254,7 +254,7 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
         m.ja.assign(ja, ja + (ia[n] - 1));
         m.a.assign(a, a + (ia[n] - 1));
         Msr f;
-        const int ierr = ilut(m, lfil, droptol, f);
+        const int ierr = ilut(m, lfil, droptol, f, prev, first_row);
         // The storage test of src/ilut.f:152-495, row by row over the rows
         // the factorisation finished: -2 when an L entry would be stored
         // past iwk, -3 when the U part (counted with its diagonal, as the
@@ -277,6 +277,31 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
         std::memcpy(jlu, f.jlu.data(), f.jlu.size() * sizeof(int));
         std::memcpy(ju, f.ju.data(), f.ju.size() * sizeof(int));
         return 0;
+    });
+}
+
+int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, double droptol,
+             int iwk, double* alu, int* jlu, int* ju)
+{
+    return ilut_into(n, ia, ja, a, lfil, droptol, iwk, alu, jlu, ju, nullptr, 0);
+}
+
+int xth_ilut_update(int n, const int* ia, const int* ja, const double* a, int lfil,
+                    double droptol, int iwk, int first_row, const double* prev_alu,
+                    const int* prev_jlu, const int* prev_ju, double* alu, int* jlu, int* ju)
+{
+    if (n <= 0 || !prev_alu || !prev_jlu || !prev_ju || prev_jlu[0] != n + 2) {
+        set_error("xth_ilut_update: bad previous factor");
+        return XT_ERR_ARG;
+    }
+    return guarded([&] {
+        Msr prev;
+        prev.n = n;
+        const int end = prev_jlu[n] - 1;  // entries of the previous factor
+        prev.alu.assign(prev_alu, prev_alu + end);
+        prev.jlu.assign(prev_jlu, prev_jlu + end);
+        prev.ju.assign(prev_ju, prev_ju + n);
+        return ilut_into(n, ia, ja, a, lfil, droptol, iwk, alu, jlu, ju, &prev, first_row);
     });
 }
 

@@ -112,11 +112,30 @@ struct Shared {
     std::vector<int> code;  // error code of a failing row
     std::mutex error_m;     // an exception of a thread (allocation), for the caller
     std::exception_ptr error;
+    int first_row = 0;           // rows below it are taken from a previous factor
+    std::vector<int> prev_cols;  // that factor's columns, 0-based
     Shared(const Csr& a, int lf, double dt)
         : A(a), n(a.n), lfil(lf), droptol(dt), rows(a.n), done(new std::atomic<int>[a.n]),
           first_fail(a.n), code(a.n, 0)
     {
         for (int i = 0; i < n; ++i) done[i].store(0, std::memory_order_relaxed);
+    }
+    // Rows [0, r0) of the factor from prev (SPARSKIT MSR of the same order),
+    // marked done before any thread starts.
+    void reuse(const Msr& prev, int r0)
+    {
+        const size_t nz = prev.jlu.size();
+        prev_cols.assign(nz, 0);
+        for (size_t k = (size_t)n + 1; k < nz; ++k) prev_cols[k] = prev.jlu[k] - 1;
+        for (int i = 0; i < r0; ++i) {
+            RowOut& O = rows[i];
+            const int b = prev.jlu[i] - 1, m = prev.ju[i] - 1, e = prev.jlu[i + 1] - 1;
+            O.lv = prev.alu.data() + b; O.lc = prev_cols.data() + b; O.nl = m - b;
+            O.uv = prev.alu.data() + m; O.uc = prev_cols.data() + m; O.nu = e - m;
+            O.dinv = prev.alu[i];
+            done[i].store(1, std::memory_order_relaxed);
+        }
+        first_row = r0;
     }
     void fail(int i, int c)
     {
@@ -151,6 +170,7 @@ void factor_rows(Shared& S, RowStore& store, int first, int stride)
     std::vector<double> wl(n + 1);
     std::vector<int> cl(n + 1);
     for (int i = first; i < n; i += stride) {
+        if (i < S.first_row) continue;  // taken from the previous factor
         if (S.first_fail.load(std::memory_order_relaxed) < i) return;
         const int b = A.ia[i] - 1, e = A.ia[i + 1] - 1;
         double tnorm = 0.0;
@@ -309,10 +329,12 @@ void assemble(const Shared& S, Msr& F)
 // The factor on T threads, assembled into F with its code in ierr; false
 // when a thread could not be started (the threads already running are
 // stopped and joined first, and F is left alone).
-bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr)
+bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr,
+             const Msr* prev, int r0)
 {
     const int n = A.n;
     Shared S(A, lfil, droptol);
+    if (prev && r0 > 0) S.reuse(*prev, r0);
     // one row store per thread; blocks hold at least one row's L and U
     const size_t row_max = (size_t)(lfil < n ? lfil : n) * 2 + 2;
     std::vector<RowStore> stores;
@@ -345,12 +367,27 @@ bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr)
 
 }  // namespace
 
-int ilut(const Csr& A, int lfil, double droptol, Msr& F)
+int ilut(const Csr& A, int lfil, double droptol, Msr& F, const Msr* prev, int first_row)
 {
     if (lfil < 0) return -4;
-    const int T = A.n > 0 ? std::min(ilut_threads(A.n), A.n) : 1;
+    const int n = A.n;
+    // a previous factor is used only when it has this matrix's order and
+    // its row pointers are consistent; first_row is clamped to [0, n]
+    int r0 = 0;
+    if (prev && first_row > 0 && prev->n == n && (int)prev->ju.size() == n &&
+        (int)prev->jlu.size() > n && prev->jlu[0] == n + 2) {
+        r0 = first_row < n ? first_row : n;
+        for (int i = 0; i < r0; ++i)
+            if (prev->ju[i] < prev->jlu[i] || prev->jlu[i + 1] < prev->ju[i] ||
+                prev->jlu[i + 1] - 1 > (int)prev->jlu.size()) {
+                r0 = 0;
+                break;
+            }
+    }
+    const int T = n > 0 ? std::min(ilut_threads(n), n) : 1;
     int ierr = 0;
-    if (!ilut_on(A, lfil, droptol, T, F, ierr)) ilut_on(A, lfil, droptol, 1, F, ierr);
+    if (!ilut_on(A, lfil, droptol, T, F, ierr, prev, r0))
+        ilut_on(A, lfil, droptol, 1, F, ierr, prev, r0);
     return ierr;
 }
 

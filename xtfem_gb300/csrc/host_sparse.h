@@ -94,7 +94,11 @@ struct Msr {
     std::vector<double> alu;
     std::vector<int> jlu, ju;  // 1-based
 };
-int ilut(const Csr& A, int lfil, double droptol, Msr& out);
+// prev / first_row: rows [0, first_row) are taken from prev, the factor of a
+// matrix whose rows [0, first_row) equal A's (ILUT row i depends only on
+// rows <= i), so the result is the full factor of A bit for bit.
+int ilut(const Csr& A, int lfil, double droptol, Msr& out, const Msr* prev = nullptr,
+         int first_row = 0);
 
 // src/stcoeff.f90:62-356 closed forms (6x6 each, column-major).
 void stcoeff_m(double t1, double dt, double w, double* k, double* m,

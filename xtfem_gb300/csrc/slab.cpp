@@ -24,6 +24,7 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/xtfem_gb300_host.h"
@@ -68,6 +69,7 @@ struct xt_slab_s {
     DBuf<double> xyzd, ymc, nuc, ve, vv, work;
     int coupled_slabs = 0;
     bool force_refactor = false;
+    Msr fac;  // the host factor of the host K (n = 0: none), reused from the first changed row
     ~xt_slab_s()
     {
         if (ds) {
@@ -82,16 +84,22 @@ struct xt_slab_s {
 
 namespace {
 
-int refactor(xt_slab_s& s)
+// ILUT of the host K.  first_row > 0: K's rows below it are those the kept
+// factor was computed from, so its rows there are kept (the same factor).
+int refactor(xt_slab_s& s, int first_row = 0)
 {
     const Csr& K = s.pr->sys.K;
     Msr f;
-    const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f);
+    const Msr* prev = (first_row > 0 && s.fac.n == K.n) ? &s.fac : nullptr;
+    const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f, prev, first_row);
+    s.fac = Msr{};  // kept again only once the new factor is in place
     if (ierr != 0) {
         set_error("ILUT failed with ierr = " + std::to_string(ierr));
         return XT_ERR_HOST;
     }
-    return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group);
+    XT_TRY(system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group));
+    s.fac = std::move(f);
+    return XT_OK;
 }
 
 // ILUT of the device K (after a reassembly on the device)
@@ -110,6 +118,7 @@ int refactor_device(xt_slab_s& s)
     XT_CUDA(cudaStreamSynchronize(st));
     for (int& v : K.ia) ++v;
     for (int& v : K.ja) ++v;
+    s.fac = Msr{};  // the kept factor no longer matches the host K
     Msr f;
     const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f);
     if (ierr != 0) {
@@ -214,7 +223,16 @@ int deletion_check(xt_slab_s& s, int& deleted)
         XT_TRY(couple_maps(s));
         s.force_refactor = true;
     } else {
-        XT_TRY(refactor(s));
+        // the surgery changes only the DOF rows of the failed elements'
+        // nodes (element matrices removed, disconnected nodes fixed), so K's
+        // rows below 3 (m - 1), m the smallest of those nodes, are unchanged
+        int m = s.nn + 1;
+        for (int k = 0; k < nef; ++k)
+            for (int i = 0; i < 8; ++i) {
+                const int nd = s.pr->mesh.conn[(size_t)(list[k] - 1) * 8 + i];
+                if (nd < m) m = nd;
+            }
+        XT_TRY(refactor(s, nef > 0 ? 3 * (m - 1) : 0));
     }
     s.dt = s.cfg.dt0 * s.cfg.n2;
     s.nip = s.cfg.nipc * s.cfg.n2;
