@@ -300,6 +300,42 @@ def test_ilut_rows_without_off_diagonals(xt, orc, monkeypatch):
             assert all(np.array_equal(a, b) for a, b in zip(got, (alu, jlu, ju))), (A.n, t)
 
 
+def test_row_local_surgery_equals_whole_matrix_surgery(xt, monkeypatch):
+    """The deletion surgery rebuilds only the DOF rows of the failed
+    elements' nodes; the result (K, M, the boundary mask, the count of
+    disconnected nodes) equals the whole-matrix form of the same steps
+    (XTFEM_SURGERY=full: cs_add, adddiagonal, csrapplybc over everything)
+    array for array, over a sequence of deletions: elements on the clamped
+    face, a corner element that disconnects a node, and elements
+    mid-rod."""
+    pa, pb = rod_problem(xt, 24, 6, 6), rod_problem(xt, 24, 6, 6)
+    xyz, conn = pa.mesh()
+    bca = clamp_mask(xyz)
+    bcb = bca.copy()
+    pa.apply_bc(bca)
+    pb.apply_bc(bcb)
+    ne = len(conn)
+    clamp = np.flatnonzero(xyz[conn - 1][:, :, 0].min(1) == 0.0)[:3] + 1
+    far = np.flatnonzero(np.all(xyz == [3.0, 1.0, 1.0], axis=1))[0]
+    corner = [next(e for e in range(ne) if far + 1 in conn[e]) + 1]
+    middle = [ne // 2 + 1, ne // 2 + 2, ne // 3 + 1]
+    disconnected = []
+    for nef in (clamp, corner, middle):
+        nef = np.array(sorted(nef), np.int32)
+        monkeypatch.delenv("XTFEM_SURGERY", raising=False)
+        nda = pa.delete(nef, bca)
+        monkeypatch.setenv("XTFEM_SURGERY", "full")
+        ndb = pb.delete(nef, bcb)
+        assert nda == ndb and np.array_equal(bca, bcb)
+        disconnected.append(nda)
+        for A, B in ((pa.K(), pb.K()), (pa.M(), pb.M())):
+            assert np.array_equal(A.ia, B.ia) and np.array_equal(A.ja, B.ja)
+            assert np.array_equal(A.a, B.a)
+    assert disconnected[1] == 1  # the corner element's far node
+    pa.close()
+    pb.close()
+
+
 def test_ilut_of_the_thermal_matrix_matches_oracle(xt, orc):
     """The thermal slab's factor (one scalar DOF per node, both rod ends at
     a fixed temperature, so the first rows are identity rows): product and

@@ -1,6 +1,7 @@
 // host_abi.cpp -- C ABI of the host-side set-up (include/xtfem_gb300_host.h)
 // and the element-deletion surgery of src/main3d.f90:634-687.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -12,6 +13,101 @@
 using namespace xt;
 
 namespace xt {
+
+namespace {
+
+// The surgery on the rows it can change, each row taken through the same
+// steps and arithmetic as the whole-matrix form below:
+//   1. K - T (cs_add: 1.0 * k + (-1.0) * t over the union of the row's
+//      columns), exact zeros removed;
+//   2. + I on the DOFs of disconnected nodes (cs_add: 1.0 * k + 1.0 * 1.0,
+//      or a new diagonal 1.0), exact zeros removed;
+//   3. the boundary conditions (csrapplybc: entries of a fixed row or
+//      column become 1 on the diagonal and 0 elsewhere), zeros removed;
+// and M through step 3.  Only the DOF rows of the failed elements' nodes
+// can change: T and the new diagonal live there, and a newly fixed DOF
+// belongs to a node whose every neighbour is such a node.  The other rows
+// are copied unchanged (they hold no zeros and already satisfy the old
+// conditions), so both forms give the same arrays.
+void surgery_rows(Csr& K, Csr& M, const Csr& T, const std::vector<int>& diag_rows,
+                  const std::vector<char>& touched, const int* bc)
+{
+    const int n = K.n;
+    std::vector<char> add_diag(n, 0);
+    for (int r : diag_rows) add_diag[r] = 1;
+    std::vector<int> cols;
+    std::vector<double> vals;
+    auto rebuild = [&](Csr& A, bool stiffness) {
+        Csr C;
+        C.n = n;
+        C.ia.assign(n + 1, 0);
+        C.ia[0] = 1;
+        C.ja.reserve(A.ja.size() + (stiffness ? T.ja.size() : 0));
+        C.a.reserve(C.ja.capacity());
+        for (int r = 0; r < n; ++r) {
+            const int b = A.ia[r] - 1, e = A.ia[r + 1] - 1;
+            if (!touched[r]) {
+                C.ja.insert(C.ja.end(), A.ja.begin() + b, A.ja.begin() + e);
+                C.a.insert(C.a.end(), A.a.begin() + b, A.a.begin() + e);
+                C.ia[r + 1] = (int)C.ja.size() + 1;
+                continue;
+            }
+            cols.clear();
+            vals.clear();
+            if (stiffness) {
+                // step 1: merge the sorted rows of A and T
+                int p = b, q = T.ia[r] - 1;
+                const int qe = T.ia[r + 1] - 1;
+                while (p < e || q < qe) {
+                    int c;
+                    double v;
+                    if (q >= qe || (p < e && A.ja[p] < T.ja[q])) {
+                        c = A.ja[p]; v = 1.0 * A.a[p]; ++p;
+                    } else if (p >= e || T.ja[q] < A.ja[p]) {
+                        c = T.ja[q]; v = -1.0 * T.a[q]; ++q;
+                    } else {
+                        c = A.ja[p]; v = 1.0 * A.a[p] + -1.0 * T.a[q]; ++p; ++q;
+                    }
+                    if (v != 0.0) { cols.push_back(c); vals.push_back(v); }
+                }
+                // step 2
+                if (add_diag[r]) {
+                    const int dc = r + 1;
+                    size_t k = 0;
+                    while (k < cols.size() && cols[k] < dc) ++k;
+                    if (k < cols.size() && cols[k] == dc) {
+                        vals[k] = 1.0 * vals[k] + 1.0 * 1.0;
+                        if (vals[k] == 0.0) { cols.erase(cols.begin() + k); vals.erase(vals.begin() + k); }
+                    } else {
+                        cols.insert(cols.begin() + k, dc);
+                        vals.insert(vals.begin() + k, 1.0);
+                    }
+                }
+            } else {
+                cols.assign(A.ja.begin() + b, A.ja.begin() + e);
+                vals.assign(A.a.begin() + b, A.a.begin() + e);
+            }
+            // step 3
+            for (size_t k = 0; k < cols.size(); ++k) {
+                const int c = cols[k] - 1;
+                if (bc[r] != 0 || bc[c] != 0) vals[k] = (r == c) ? 1.0 : 0.0;
+                if (vals[k] != 0.0) { C.ja.push_back(cols[k]); C.a.push_back(vals[k]); }
+            }
+            C.ia[r + 1] = (int)C.ja.size() + 1;
+        }
+        A = std::move(C);
+    };
+    rebuild(K, true);
+    rebuild(M, false);
+}
+
+bool whole_matrix_surgery()
+{
+    const char* e = std::getenv("XTFEM_SURGERY");
+    return e && std::strcmp(e, "full") == 0;
+}
+
+}  // namespace
 
 int Problem::delete_elements(int nef, const int* nefail, int* bc, int* ndf_out)
 {
@@ -33,20 +129,23 @@ int Problem::delete_elements(int nef, const int* nefail, int* bc, int* ndf_out)
     t.j.reserve((size_t)nef * 576);
     t.v.reserve((size_t)nef * 576);
     double ke[576];
+    std::vector<char> touched(ndof, 0);
     for (int k = 0; k < nef; ++k) {
         const int e = nefail[k] - 1;
         element_stiffness(mesh, e, sys.stiff.data(), ke);
         int dofs[24];
         for (int i = 0; i < 8; ++i)
             for (int c = 0; c < 3; ++c) dofs[3 * i + c] = 3 * (mesh.conn[(size_t)e * 8 + i] - 1) + c + 1;
-        for (int r = 0; r < 24; ++r)
+        for (int r = 0; r < 24; ++r) {
+            touched[dofs[r] - 1] = 1;
             for (int c = 0; c < 24; ++c) {
                 t.i.push_back(dofs[r]);
                 t.j.push_back(dofs[c]);
                 t.v.push_back(ke[r * 24 + c]);
             }
+        }
     }
-    cs_add(sys.K, tricsr(t, ndof), 1.0, -1.0);
+    const Csr T = tricsr(t, ndof);
     // chkcnsta, then chkndsta (src/delelement.f90:139-201)
     for (int k = 0; k < nef; ++k) {
         const int e = nefail[k] - 1;
@@ -64,21 +163,30 @@ int Problem::delete_elements(int nef, const int* nefail, int* bc, int* ndf_out)
             }
         }
     }
-    // adddiagonal (src/delelement.f90:204-247)
-    if (!ndfail.empty()) {
-        Triplets d;
-        for (int nd : ndfail)
-            for (int c = 1; c <= 3; ++c) {
-                d.i.push_back((nd - 1) * 3 + c);
-                d.j.push_back((nd - 1) * 3 + c);
+    // adddiagonal (src/delelement.f90:204-247): a unit diagonal on the
+    // disconnected nodes' DOFs, which become fixed
+    std::vector<int> diag_rows;
+    for (int nd : ndfail)
+        for (int c = 0; c < 3; ++c) diag_rows.push_back((nd - 1) * 3 + c);
+    if (whole_matrix_surgery()) {
+        // the same steps on the whole matrices (the reference's form)
+        cs_add(sys.K, T, 1.0, -1.0);
+        if (!diag_rows.empty()) {
+            Triplets d;
+            for (int r : diag_rows) {
+                d.i.push_back(r + 1);
+                d.j.push_back(r + 1);
                 d.v.push_back(1.0);
             }
-        cs_add(sys.K, tricsr(d, ndof), 1.0, 1.0);
-        for (int nd : ndfail)
-            for (int c = 0; c < 3; ++c) bc[(nd - 1) * 3 + c] = 1;
+            cs_add(sys.K, tricsr(d, ndof), 1.0, 1.0);
+        }
+        for (int r : diag_rows) bc[r] = 1;
+        csrapplybc(sys.M, bc);
+        csrapplybc(sys.K, bc);
+    } else {
+        for (int r : diag_rows) bc[r] = 1;
+        surgery_rows(sys.K, sys.M, T, diag_rows, touched, bc);
     }
-    csrapplybc(sys.M, bc);
-    csrapplybc(sys.K, bc);
     if (ndf_out) *ndf_out = (int)ndfail.size();
     return XT_OK;
 }
