@@ -56,6 +56,12 @@ int xth_problem_apply_bc(xth_problem pr, const int *bc);
 int xth_problem_delete(xth_problem pr, int nef, const int *nefail, int *bc,
                        int *ndf_out);
 
+/* The first row (0-based) of K that the last xth_problem_delete changed:
+ * a DOF row of a failed element, or a row coupled to a newly fixed DOF.
+ * Rows above it are unchanged, so it is the first_row for xth_ilut_update.
+ * -1 for a null handle. */
+int xth_problem_first_changed_row(xth_problem pr);
+
 /* src/ilut.f:152-495 ILUT(lfil, droptol) in FP64; alu/jlu hold iwk entries,
  * ju n entries; returns SPARSKIT's ierr: 0 success, -1 a row's L or U
  * length exceeds n, -2 the L part overflows iwk, -3 the U part overflows
@@ -67,9 +73,8 @@ int xth_ilut(int n, const int *ia, const int *ja, const double *a, int lfil,
 /* The same factor when rows [0, first_row) of the matrix equal those of the
  * matrix prev_alu/prev_jlu/prev_ju was computed from (same lfil, droptol):
  * those rows are copied and the rest refactored (ILUT row i depends only on
- * rows <= i).  After a deletion, first_row is 3 (m - 1) for the smallest
- * node m of the failed elements.  No counterpart in the reference, which
- * refactors every row. */
+ * rows <= i).  After a deletion, first_row is xth_problem_first_changed_row.
+ * No counterpart in the reference, which refactors every row. */
 int xth_ilut_update(int n, const int *ia, const int *ja, const double *a, int lfil,
                     double droptol, int iwk, int first_row, const double *prev_alu,
                     const int *prev_jlu, const int *prev_ju, double *alu, int *jlu, int *ju);

@@ -334,6 +334,30 @@ def test_row_local_surgery_equals_whole_matrix_surgery(xt, monkeypatch):
     assert disconnected[1] == 1  # the corner element's far node
     pa.close()
     pb.close()
+    # the holed panel: nodes disconnected after some of their elements went
+    # in earlier steps (their other neighbours' rows change too)
+    from xtfem_gb300.meshes import holed_panel
+
+    xyz, conn = holed_panel(32, 6, 1)
+    probs = [xt.Problem.from_mesh(xyz, conn) for _ in range(2)]
+    bcs = [np.repeat((xyz[:, 1] == 0.0).astype(np.int32), 3) for _ in range(2)]
+    for p, b in zip(probs, bcs):
+        p.apply_bc(b)
+    rng = np.random.default_rng(1)
+    total = 0
+    for _ in range(6):
+        nef = np.sort(rng.choice(len(conn), 5, replace=False) + 1).astype(np.int32)
+        monkeypatch.delenv("XTFEM_SURGERY", raising=False)
+        n0 = probs[0].delete(nef, bcs[0])
+        monkeypatch.setenv("XTFEM_SURGERY", "full")
+        n1 = probs[1].delete(nef, bcs[1])
+        total += n0
+        assert n0 == n1 and np.array_equal(bcs[0], bcs[1])
+        for A, B in ((probs[0].K(), probs[1].K()), (probs[0].M(), probs[1].M())):
+            assert all(np.array_equal(getattr(A, f), getattr(B, f)) for f in ("ia", "ja", "a"))
+    assert total > 0
+    for p in probs:
+        p.close()
 
 
 def test_ilut_of_the_thermal_matrix_matches_oracle(xt, orc):
@@ -382,7 +406,8 @@ def test_refactor_from_the_first_changed_row(xt):
             nef = np.sort(nef).astype(np.int32)
             pr.delete(nef, bc)
             K = pr.K()
-            r0 = 3 * (int(conn[nef - 1].min()) - 1)
+            r0 = pr.first_changed_row()
+            assert r0 == 3 * (int(conn[nef - 1].min()) - 1)  # no node disconnected here
             for t in ("1", "4"):
                 os.environ["XTFEM_ILUT_THREADS"] = t
                 full = xt.ilut(K, 20, 1e-4)
@@ -395,6 +420,30 @@ def test_refactor_from_the_first_changed_row(xt):
         os.environ.pop("XTFEM_ILUT_THREADS", None)
     assert r0 > 0
     pr.close()
+    # deletions that disconnect nodes whose other elements went earlier: the
+    # first changed row can lie above the failed elements' own rows
+    from xtfem_gb300.meshes import holed_panel
+
+    xyz, conn = holed_panel(32, 6, 1)
+    above = 0
+    for seed in (7, 9, 10):
+        pr = xt.Problem.from_mesh(xyz, conn)
+        bc = np.repeat((xyz[:, 1] == 0.0).astype(np.int32), 3)
+        pr.apply_bc(bc)
+        old = xt.ilut(pr.K(), 20, 1e-4)
+        rng = np.random.default_rng(seed)
+        for _ in range(6):
+            nef = np.sort(rng.choice(len(conn), 5, replace=False) + 1).astype(np.int32)
+            pr.delete(nef, bc)
+            K = pr.K()
+            r0 = pr.first_changed_row()
+            above += r0 < 3 * (int(conn[nef - 1].min()) - 1)
+            full = xt.ilut(K, 20, 1e-4)
+            upd = xt.ilut(K, 20, 1e-4, reuse=(*old, r0))
+            assert all(np.array_equal(a, b) for a, b in zip(full, upd)), (seed, r0)
+            old = full
+        pr.close()
+    assert above >= 3
 
 
 def test_qsplit_partial_order(orc):

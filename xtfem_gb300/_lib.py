@@ -81,6 +81,7 @@ SIGNATURES = {
     "xth_stcoeff_t": (None, [C.c_double] + [_dp] * 6),
     "xth_getfextc_m": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),
     "xth_getfextc_t": (None, [C.c_double, C.c_double, _dp]),
+    "xth_problem_first_changed_row": (C.c_int, [_vp]),
     "xth_ilut_update": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
                                   _dp, _ip, _ip, _dp, _ip, _ip]),
     "xt_gmres_log": (C.c_int, [_dp, C.c_int]),

@@ -479,6 +479,11 @@ class Problem:
     def apply_bc(self, bc):
         check(lib().xth_problem_apply_bc(self._h, iptr(_i32(bc))), "apply_bc")
 
+    def first_changed_row(self):
+        """The first row of K the last delete() changed (rows above it are as
+        before): the first_row for ilut(..., reuse=)."""
+        return int(lib().xth_problem_first_changed_row(self._h))
+
     def delete(self, nefail, bc):
         """Element-deletion surgery; bc (int32, 3nn) is updated in place."""
         if bc.dtype != np.int32:

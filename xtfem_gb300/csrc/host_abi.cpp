@@ -24,16 +24,19 @@ namespace {
 //      or a new diagonal 1.0), exact zeros removed;
 //   3. the boundary conditions (csrapplybc: entries of a fixed row or
 //      column become 1 on the diagonal and 0 elsewhere), zeros removed;
-// and M through step 3.  Only the DOF rows of the failed elements' nodes
-// can change: T and the new diagonal live there, and a newly fixed DOF
-// belongs to a node whose every neighbour is such a node.  The other rows
-// are copied unchanged (they hold no zeros and already satisfy the old
-// conditions), so both forms give the same arrays.
+// and M through step 3.  Steps 1 and 2 change only the DOF rows of the
+// failed elements' nodes (T and the new diagonal live there).  Step 3
+// changes those rows and any row with a column among the newly fixed DOFs:
+// a disconnected node's neighbours through elements deleted earlier keep
+// their couplings to it (M keeps the mass of deleted elements, K may keep
+// rounding residues).  Every other row is copied unchanged (it holds no
+// zeros and already satisfies the old conditions), so both forms give the
+// same arrays.
 void surgery_rows(Csr& K, Csr& M, const Csr& T, const std::vector<int>& diag_rows,
                   const std::vector<char>& touched, const int* bc)
 {
     const int n = K.n;
-    std::vector<char> add_diag(n, 0);
+    std::vector<char> add_diag(n, 0);  // the newly fixed DOFs
     for (int r : diag_rows) add_diag[r] = 1;
     std::vector<int> cols;
     std::vector<double> vals;
@@ -46,7 +49,10 @@ void surgery_rows(Csr& K, Csr& M, const Csr& T, const std::vector<int>& diag_row
         C.a.reserve(C.ja.capacity());
         for (int r = 0; r < n; ++r) {
             const int b = A.ia[r] - 1, e = A.ia[r + 1] - 1;
-            if (!touched[r]) {
+            bool fixed_col = false;
+            if (!touched[r] && !diag_rows.empty())
+                for (int k = b; k < e && !fixed_col; ++k) fixed_col = add_diag[A.ja[k] - 1] != 0;
+            if (!touched[r] && !fixed_col) {
                 C.ja.insert(C.ja.end(), A.ja.begin() + b, A.ja.begin() + e);
                 C.a.insert(C.a.end(), A.a.begin() + b, A.a.begin() + e);
                 C.ia[r + 1] = (int)C.ja.size() + 1;
@@ -54,7 +60,7 @@ void surgery_rows(Csr& K, Csr& M, const Csr& T, const std::vector<int>& diag_row
             }
             cols.clear();
             vals.clear();
-            if (stiffness) {
+            if (stiffness && touched[r]) {
                 // step 1: merge the sorted rows of A and T
                 int p = b, q = T.ia[r] - 1;
                 const int qe = T.ia[r + 1] - 1;
@@ -168,6 +174,23 @@ int Problem::delete_elements(int nef, const int* nefail, int* bc, int* ndf_out)
     std::vector<int> diag_rows;
     for (int nd : ndfail)
         for (int c = 0; c < 3; ++c) diag_rows.push_back((nd - 1) * 3 + c);
+    // the first row of K this surgery changes: a failed element's DOF row,
+    // or a row with a column among the newly fixed DOFs (a neighbour through
+    // an element deleted earlier)
+    int first = ndof;
+    for (int r = 0; r < ndof; ++r)
+        if (touched[r]) { first = r; break; }
+    if (!diag_rows.empty()) {
+        std::vector<char> fixed_now(ndof, 0);
+        for (int r : diag_rows) fixed_now[r] = 1;
+        for (int r = 0; r < first; ++r) {
+            bool hit = false;
+            for (int k = sys.K.ia[r] - 1; k < sys.K.ia[r + 1] - 1 && !hit; ++k)
+                hit = fixed_now[sys.K.ja[k] - 1] != 0;
+            if (hit) { first = r; break; }
+        }
+    }
+    first_changed = first;
     if (whole_matrix_surgery()) {
         // the same steps on the whole matrices (the reference's form)
         cs_add(sys.K, T, 1.0, -1.0);
@@ -386,6 +409,11 @@ static int ilut_into(int n, const int* ia, const int* ja, const double* a, int l
         std::memcpy(ju, f.ju.data(), f.ju.size() * sizeof(int));
         return 0;
     });
+}
+
+int xth_problem_first_changed_row(xth_problem h)
+{
+    return h ? P(h)->first_changed : -1;
 }
 
 int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, double droptol,

@@ -223,16 +223,8 @@ int deletion_check(xt_slab_s& s, int& deleted)
         XT_TRY(couple_maps(s));
         s.force_refactor = true;
     } else {
-        // the surgery changes only the DOF rows of the failed elements'
-        // nodes (element matrices removed, disconnected nodes fixed), so K's
-        // rows below 3 (m - 1), m the smallest of those nodes, are unchanged
-        int m = s.nn + 1;
-        for (int k = 0; k < nef; ++k)
-            for (int i = 0; i < 8; ++i) {
-                const int nd = s.pr->mesh.conn[(size_t)(list[k] - 1) * 8 + i];
-                if (nd < m) m = nd;
-            }
-        XT_TRY(refactor(s, nef > 0 ? 3 * (m - 1) : 0));
+        // K's rows above the first one the surgery changed are as before
+        XT_TRY(refactor(s, nef > 0 ? s.pr->first_changed : 0));
     }
     s.dt = s.cfg.dt0 * s.cfg.n2;
     s.nip = s.cfg.nipc * s.cfg.n2;
