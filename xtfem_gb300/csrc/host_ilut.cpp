@@ -367,9 +367,17 @@ bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr,
 
 }  // namespace
 
+// factorisations running in this process: concurrent callers (specimens
+// set up side by side) each take one thread instead of all of them
+static std::atomic<int> g_running{0};
+
 int ilut(const Csr& A, int lfil, double droptol, Msr& F, const Msr* prev, int first_row)
 {
     if (lfil < 0) return -4;
+    const int others = g_running.fetch_add(1);
+    struct Leave {
+        ~Leave() { g_running.fetch_sub(1); }
+    } leave;
     const int n = A.n;
     // a previous factor is used only when it has this matrix's order and
     // its row pointers are consistent; first_row is clamped to [0, n]
@@ -384,7 +392,7 @@ int ilut(const Csr& A, int lfil, double droptol, Msr& F, const Msr* prev, int fi
                 break;
             }
     }
-    const int T = n > 0 ? std::min(ilut_threads(n), n) : 1;
+    const int T = (n > 0 && others == 0) ? std::min(ilut_threads(n), n) : 1;
     int ierr = 0;
     if (!ilut_on(A, lfil, droptol, T, F, ierr, prev, r0))
         ilut_on(A, lfil, droptol, 1, F, ierr, prev, r0);
