@@ -84,8 +84,9 @@ struct xt_slab_s {
 
 namespace {
 
-// ILUT of the host K.  first_row > 0: K's rows below it are those the kept
-// factor was computed from, so its rows there are kept (the same factor).
+// ILUT of the host K.  first_row > 0: K's rows [0, first_row) are those the
+// kept factor was computed from, so its rows there are kept (the same
+// factor).
 int refactor(xt_slab_s& s, int first_row = 0)
 {
     const Csr& K = s.pr->sys.K;
