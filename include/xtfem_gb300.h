@@ -155,7 +155,13 @@ int xt_damage(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
  *     stream capture.
  *   - One scratch per process and device, keeping the last call's
  *     contents: calls whose work overlaps on the GPU (two host threads)
- *     race on it.  Returns after the update has finished. */
+ *     race on it.
+ *   - Ordering: the call starts with cudaDeviceSynchronize, so every kernel
+ *     or copy the caller queued before it, on any stream of the device,
+ *     has finished writing the inputs and the state before the update
+ *     reads them.  It returns after the update has finished.
+ *   - The work runs on the library's device (xt_init); the calling
+ *     thread's current device is restored before the call returns. */
 int xt_damage_device(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe,
                      int ncmp, int nip, const int *nodes, const double *Nx,
                      const double *Ny, const double *Nz, const double *Nt,

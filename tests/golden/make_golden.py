@@ -8,7 +8,9 @@ the 325-node mesh.  The tests compare the product's rod generator with
 these, so the generated meshes are pinned to the reference's files without
 the reference being present at test time.
 
-Usage: python tests/golden/make_golden.py [reference_root]
+Usage: python tests/golden/make_golden.py REFERENCE_ROOT
+
+REFERENCE_ROOT is the directory of the reference checkout that holds inp/.
 """
 import hashlib
 import json
@@ -54,4 +56,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py REFERENCE_ROOT")
+    main(sys.argv[1])

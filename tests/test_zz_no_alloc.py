@@ -85,3 +85,44 @@ def test_device_entry_rejects_oversize_nip(xt):
     msg = xt.lib().xt_last_error().decode()
     assert "exceeds the static scratch" in msg and str(MAX_NIP) in msg
     xt.lib().xt_clear_error()
+
+
+@pytest.mark.gpu
+def test_device_entry_waits_for_writes_on_callers_stream(xt):
+    """The caller's kernels write the state on a stream of its own and the
+    call follows without a host synchronisation: the entry point waits for
+    that work (device-wide) before it reads, so the result equals
+    xt_damage's on the written values."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    xt.lib().xt_init(0)
+    d = damage_case(xt)
+    ref = {k: v.copy() for k, v in d["state"].items()}
+    src = {k: torch.from_numpy(v.copy()).cuda() for k, v in d["state"].items()}
+    dev = {k: torch.full_like(v, float("nan")) for k, v in src.items()}
+    inp = {k: torch.from_numpy(np.ascontiguousarray(d[k])).cuda()
+           for k in ["nodes", "Nx", "Ny", "Nz", "Nt", "sol", "ym", "nu"]}
+    xt.damage(d["ne"], d["nn"], d["nip"], d["nodes"], d["Nx"], d["Ny"], d["Nz"], d["Nt"],
+              d["sol"], d["ym"], d["nu"], ref)
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        # keep the stream busy for a while, then write the real state
+        if hasattr(torch.cuda, "_sleep"):
+            torch.cuda._sleep(200_000_000)
+        else:
+            m = torch.randn(2048, 2048, device="cuda")
+            for _ in range(50):
+                m = torch.tanh(m @ m)
+        for k in KEYS:
+            dev[k].copy_(src[k])
+    ptr = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    st = xt.lib().xt_damage_device(
+        d["ne"], d["nn"], 3, 8, 3, 8, 6, d["nip"],
+        *[ptr(inp[k]) for k in ["nodes", "Nx", "Ny", "Nz", "Nt", "sol", "ym", "nu"]],
+        *[ptr(dev[k]) for k in KEYS], None)
+    assert st == 0, xt.lib().xt_last_error()
+    torch.cuda.synchronize()
+    for k in KEYS:
+        assert np.array_equal(dev[k].cpu().numpy(), ref[k]), k

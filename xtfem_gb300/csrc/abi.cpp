@@ -40,6 +40,22 @@ std::map<IluKey, std::shared_ptr<DevIlu>> g_ilus;
 
 int to_status(int s) { return s; }
 
+// Makes the library's device current for the lifetime of the guard and
+// gives the calling thread its own current device back afterwards.
+struct DeviceGuard {
+    int saved = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceGuard(int device)
+    {
+        err = cudaGetDevice(&saved);
+        if (err == cudaSuccess && saved != device) err = cudaSetDevice(device);
+    }
+    ~DeviceGuard()
+    {
+        if (saved >= 0) cudaSetDevice(saved);
+    }
+};
+
 int upload_blocks(xt_system_s& h, const double* host, double* dev_itl)
 {
     System& S = h.sys;
@@ -144,6 +160,7 @@ int xt_finalize(void)
 {
     g_ops.clear();
     g_ilus.clear();
+    damage_static_forget();
     Context& c = ctx();
     if (c.ready) {
         cudaStreamSynchronize(c.stream);
@@ -484,6 +501,12 @@ int batch_run(xt_batch b, const double* const* rhs, double* const* sol, int im, 
     std::vector<std::string> msg(count);
     std::atomic<int> next{0};
     const int device = ctx().device;
+    // the caller's thread runs work() too: it gets its current device back
+    DeviceGuard guard(device);
+    if (guard.err != cudaSuccess) {
+        set_error("xt_batch_solve: could not select the library's device");
+        return XT_ERR_CUDA;
+    }
     auto work = [&] {
         if (cudaSetDevice(device) != cudaSuccess) return;
         for (int k; (k = next.fetch_add(1)) < count;) {
@@ -727,10 +750,21 @@ int xt_damage_device(int ne, int nn, int ndofn, int nnse, int nnte, int ngpe, in
         return XT_ERR_ARG;
     }
     XT_TRY(ensure_init());
+    // The launches go to the library's stream, which belongs to the
+    // library's device: make that device current for this call (the
+    // caller's thread may have another one current) and give the caller's
+    // back on return.
+    DeviceGuard guard(ctx().device);
+    XT_CUDA(guard.err);
+    // The inputs and the state were written by the caller's own kernels, on
+    // streams that nothing here orders after (the library's stream is
+    // non-blocking).  Wait for all work on the device first; this allocates
+    // nothing.
+    XT_CUDA(cudaDeviceSynchronize());
     cudaStream_t s = ctx().stream;
     float *nt32 = nullptr, *ntmax = nullptr;
     unsigned long long* counters = nullptr;
-    XT_TRY(damage_static_scratch(&nt32, &ntmax, &counters));
+    XT_TRY(damage_static_scratch(ctx().device, &nt32, &ntmax, &counters));
     // the step counters accumulate with atomics: they must start at zero
     XT_CUDA(cudaMemsetAsync(counters, 0, 3 * sizeof(unsigned long long), s));
     if (nip > 0) XT_TRY(to_f32(Nt, nt32, (size_t)2 * nnte * nip, s));

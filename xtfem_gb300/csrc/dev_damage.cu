@@ -26,6 +26,8 @@
 // before a plastic step, or before the slab ends, has to be evaluated).
 // Steps the screen cannot decide, and plastic steps, are evaluated exactly
 // in FP64 with the reference's operation order.
+#include <mutex>
+
 #include "xt_device.h"
 
 namespace xt {
@@ -519,28 +521,53 @@ static __device__ __align__(256) unsigned char g_damage_scratch[kStaticBytes];
 
 }  // namespace
 
-int damage_static_scratch(float** nt32, float** ntmax, unsigned long long** counters)
+namespace {
+// Per-device address of g_damage_scratch, looked up once per device and
+// context.  A mutex guards it: two host threads making their first call at
+// once must not race on the entry.  damage_static_forget() clears it when
+// the library context is torn down (a new context may place the symbol at
+// another address).
+std::mutex g_scratch_mu;
+constexpr int kMaxDevices = 64;
+void* g_scratch_addr[kMaxDevices] = {nullptr};
+}  // namespace
+
+int damage_static_scratch(int device, float** nt32, float** ntmax, unsigned long long** counters)
 {
-    // The address is looked up once per device (cudaGetSymbolAddress can load
-    // the module, so the first call must not sit inside a stream capture).
-    constexpr int kMaxDevices = 64;
-    static void* addr[kMaxDevices] = {nullptr};
-    int dev = -1;
-    XT_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
+    if (device < 0 || device >= kMaxDevices) {
         set_error("damage scratch: device index out of range");
         return XT_ERR_ARG;
     }
-    if (!addr[dev]) {
-        void* p = nullptr;
-        XT_CUDA(cudaGetSymbolAddress(&p, g_damage_scratch));
-        addr[dev] = p;
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        if (!g_scratch_addr[device]) {
+            // the caller has made `device` current; cudaGetSymbolAddress can
+            // load the module, so the first call must not sit inside a
+            // stream capture
+            int cur = -1;
+            XT_CUDA(cudaGetDevice(&cur));
+            if (cur != device) {
+                set_error("damage scratch: the library's device is not current");
+                return XT_ERR_CUDA;
+            }
+            void* p = nullptr;
+            XT_CUDA(cudaGetSymbolAddress(&p, g_damage_scratch));
+            g_scratch_addr[device] = p;
+        }
+        base = g_scratch_addr[device];
     }
-    unsigned char* b = static_cast<unsigned char*>(addr[dev]);
+    unsigned char* b = static_cast<unsigned char*>(base);
     *nt32 = reinterpret_cast<float*>(b);
     *ntmax = reinterpret_cast<float*>(b + kStaticNt * sizeof(float));
     *counters = reinterpret_cast<unsigned long long*>(b + kStaticNt * sizeof(float) + 64);
     return XT_OK;
+}
+
+void damage_static_forget()
+{
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    for (int d = 0; d < kMaxDevices; ++d) g_scratch_addr[d] = nullptr;
 }
 
 int nt_table_device(int nip, double t0, double t1, double t2, double w, double* Nt64,

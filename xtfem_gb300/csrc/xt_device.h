@@ -296,10 +296,12 @@ int damage_update(const DamageArgs& a, cudaStream_t s);
 
 // Static device scratch of the allocation-free damage entry point: FP32
 // shape table (6 * kDamageStaticMaxNip floats), 6 shape-value bounds and 3
-// step counters.  Address looked up once per device (the device must be
-// current).
+// step counters.  The address is looked up once per device, under a lock;
+// `device` must be the current device.  damage_static_forget() drops the
+// looked-up addresses (library teardown).
 constexpr int kDamageStaticMaxNip = 65536;
-int damage_static_scratch(float** nt32, float** ntmax, unsigned long long** counters);
+int damage_static_scratch(int device, float** nt32, float** ntmax, unsigned long long** counters);
+void damage_static_forget();
 
 // Temporal shape table on the device (FP64 and FP32 copies).
 int nt_table_device(int nip, double t0, double t1, double t2, double w, double* Nt64,
