@@ -5,10 +5,13 @@ routines of the space-time solve path (see xt_oracle.h for the file:line of
 each).  It is the checker for the GPU library and the timed CPU baseline;
 the product never imports it.
 
-Parity pinning: the reference ships no tests or golden vectors for this path
-and cannot be built here, so parity is unpinned by the reference's own
-tests; the oracle is validated by invariants and independent statements in
-tests/test_host.py.
+Parity pinning: the reference ships no tests or golden vectors for this path.
+Its damage kernel (src/kokkos_host.cpp with src/kokkos_kernel.h) is compiled
+unchanged against a host-only Kokkos stand-in (Makefile target `ref`), and
+the damage statement here equals it bit for bit (tests/test_ref_damage.py,
+fixture tests/golden/damage_ref.npz).  The Fortran routines cannot be built
+(no Fortran compiler); the rest of the oracle is validated by invariants
+and independent statements in tests/test_host.py.
 """
 from __future__ import annotations
 
@@ -28,8 +31,16 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
+# The reference's own damage kernel compiled unchanged (Makefile target
+# `ref`) where the reference checkout exists; absent elsewhere.
+REF_LIB = HERE / "_ref" / "libxtref.so"
+REF_ROOT = Path(os.environ.get("XTFEM_REFERENCE", "/root/reference"))
+
+
 def build() -> Path:
     subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    if (REF_ROOT / "src" / "kokkos_host.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_ROOT}"], check=True)
     return LIB
 
 
@@ -219,6 +230,41 @@ def damage(ne, nn, nip, nodes, Nx, Ny, Nz, Nt, sol, ym, nu, state, nthreads=1):
         assert state[k].dtype == np.float64 and state[k].flags.c_contiguous
     lib().orc_damage(ne, nn, 3, 8, 3, 8, 6, nip, *[x[1] for x in ins],
                      *[state[k].ctypes.data_as(_dp) for k in STATE_KEYS], nthreads)
+    return state
+
+
+_ref = None
+
+
+def ref_lib():
+    """The reference's kokkos_host_ (src/kokkos_host.cpp, src/kokkos_kernel.h)
+    built unchanged into oracle/_ref/libxtref.so, or None where it is not
+    built (no reference checkout: the GPU machine)."""
+    global _ref
+    if _ref is None and REF_LIB.exists():
+        L = C.CDLL(str(REF_LIB))
+        L.kokkos_host_.restype = None
+        L.kokkos_host_.argtypes = [C.c_int] * 9 + [_ip] + [_dp] * 16
+        L.xtref_set_threads.restype = None
+        L.xtref_set_threads.argtypes = [C.c_int]
+        L.kokkos_init_.restype = None
+        L.kokkos_init_()
+        _ref = L
+    return _ref
+
+
+def ref_damage(ne, nn, nip, nodes, Nx, Ny, Nz, Nt, sol, ym, nu, state, nthreads=1):
+    """The reference's own kokkos_host_ (rank 0) on the CPU, with the
+    arguments of damage(); state arrays updated in place."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("oracle/_ref/libxtref.so is not built (make -C oracle ref)")
+    ins = [_i(nodes), _d(Nx), _d(Ny), _d(Nz), _d(Nt), _d(sol), _d(ym), _d(nu)]
+    for k in STATE_KEYS:
+        assert state[k].dtype == np.float64 and state[k].flags.c_contiguous
+    L.xtref_set_threads(int(nthreads))
+    L.kokkos_host_(0, ne, nn, 3, 8, 3, 8, 6, nip, *[x[1] for x in ins],
+                   *[state[k].ctypes.data_as(_dp) for k in STATE_KEYS])
     return state
 
 
