@@ -243,14 +243,8 @@ def run_gpu(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": DTYPE_NAMES[WORKLOAD["precision"]],
         "data": "synthetic (generated rod mesh, seeded load amplitude)",
-        "config": {"workload": "C2 prismatic rod 20x20x60 C3D8, 80,703 DOF x 6 temporal blocks",
-                   "nip": WORKLOAD["nipc"] * WORKLOAD["n1"], "ilut": [WORKLOAD["droptol"],
-                                                                      WORKLOAD["lfil"]],
-                   "gmres_restart": WORKLOAD["im"], "tol": WORKLOAD["tol"],
-                   "precision": PRECISION_NAMES[WORKLOAD["precision"]],
-                   "amplitude_mpa": cfg.amplitude,
-                   "l2": "inputs larger than L2 (operator+factor+basis >> 129 MB)",
-                   "parallelism": f"replicas x{world}"},
+        "config": dict(workload_config(cfg.amplitude), parallelism=f"replicas x{world}"),
+        "precision": PRECISION_NAMES[WORKLOAD["precision"]],
         "iterations_per_slab": float(np.mean(its)), "relres_max": float(np.max(res)),
         "host_ms_per_step": round(t_host / args.steps, 3),
         "roofline": {"bound": "hbm", "kernel": CLASS_NAMES[dom], "achieved": round(achieved, 1),
@@ -271,8 +265,7 @@ def run_gpu(args, rank, world):
     if rank == 0 and not args.skip_e2e:
         out["e2e"] = run_e2e(xt, args, world)
     if rank == 0 and not args.skip_cpu:
-        out["cpu_baseline"] = cpu_baseline(its=float(np.mean(its)), sample_its=args.cpu_its,
-                                           threads=os.cpu_count() or 1, for_arm=False)
+        out["cpu_baseline"] = cpu_baseline(threads=os.cpu_count() or 1)
     if rank == 0 and not args.skip_variants:
         out["variants"] = run_variants(xt, args)
     if rank == 0:
@@ -570,111 +563,181 @@ def run_e2e(xt, args, world):
 
 
 # -------------------------------------------------------- CPU baseline
-def cpu_baseline(its, sample_its, threads, for_arm):
-    """The reference's CPU path (oracle restatement) on a bounded sample of
-    the same slab: sample_its GMRES iterations and the damage update of a
-    slice of the Gauss points (OpenMP over points, as src/cpu_damage.f90),
-    scaled to one full slab.  GMRES is timed twice: in the reference's serial
-    order (kronpgmres has no threading) and on all the host threads (OpenMP
-    over the rows of each amux pass and vector update and over the q
-    independent lusol calls); the threaded one gives the value."""
-    import xtfem_gb300 as xt
-    from oracle import oracle as orc
+def workload_config(amp):
+    """The workload definition both arms report as `config`."""
+    return {"workload": "C2 prismatic rod 20x20x60 C3D8, 80,703 DOF x 6 temporal blocks",
+            "nip": WORKLOAD["nipc"] * WORKLOAD["n1"],
+            "ilut": [WORKLOAD["droptol"], WORKLOAD["lfil"]],
+            "gmres_restart": WORKLOAD["im"], "tol": WORKLOAD["tol"], "amplitude_mpa": amp,
+            "l2": "inputs larger than L2 (operator+factor+basis >> 129 MB)",
+            "parallelism": "replicas x1"}
 
-    prob = make_problem(xt)
-    xyz, conn = prob.mesh()
-    nn, ne = len(xyz), len(conn)
-    p = 3 * nn
-    bc = np.zeros(p, np.int32)
-    bc[np.repeat(xyz[:, 0] == 0.0, 3)] = 1
-    prob.apply_bc(bc)
-    K, M = prob.K(), prob.M()
-    (alu, jlu, ju), ierr = orc.ilut(K, WORKLOAD["lfil"], WORKLOAD["droptol"])
-    w = 2 * np.pi * WORKLOAD["freq"]
-    dt = WORKLOAD["dt0"] * WORKLOAD["n1"]
-    k, m, kt, mt, k1, m1 = xt.stcoeff_m(0.0, dt, w)
-    share = np.bincount(conn.ravel() - 1, minlength=nn).astype(float)
-    face = xyz[:, 0] == WORKLOAD["lx"]
-    rext = np.zeros(p)
-    np.add.at(rext, 3 * (conn.ravel()[face[conn.ravel() - 1]] - 1),
-              amplitude(WORKLOAD["seed"]) / share[face].sum())
-    fextc, _ = xt.getfextc_m(0.0, w, dt)
-    rhs = np.concatenate([f * rext for f in fextc])
-    def gmres_sample(nt):
-        # one restart cycle of sample_its steps (maxits is only tested at the
-        # end of a cycle in kronpgmres); shorter cycles make the
-        # orthogonalisation cheaper than in GMRES(im), so the scaled baseline
-        # errs on the fast side
-        orc.set_threads(nt)
+
+class CpuSlab:
+    """The reference's CPU path for the C2 slab loop, on the oracle (the C
+    restatement of src/kronecker.f90, src/ilut.f and the damage kernel,
+    src/kokkos_kernel.h): its inputs come from oracle/fem.py (the mesh,
+    K, M, strain rows, boundary conditions and load restated in numpy) and
+    the oracle's quadrature of the temporal integrals, so the GPU library is
+    not loaded.
+
+    One step is one slab of src/main3d.f90:609-937 in full except for the
+    damage update, which runs on a stratified sample of the Gauss points
+    over the slab's full 25,600 steps: stratum A is every point of the
+    clamped layer (400 elements; it holds every plastic point of the slab,
+    the four clamped corners), stratum B a seeded 1/sample_every of the
+    other elements.  The update's full-slab time is tA + tB * (points of B
+    in the rod / points of B sampled).  GMRES runs to the reference's
+    convergence test (|rs| <= 1e-8 ||r0||, GMRES(200)) on the slab's real
+    right-hand side, OpenMP over the rows of every amux pass and vector
+    update and over the q independent lusol calls (bit-identical to the
+    serial order); the damage update is OpenMP over the points, as
+    src/cpu_damage.f90."""
+
+    def __init__(self, threads, seed=0, sample_every=64):
+        from oracle import fem
+        from oracle import oracle as orc
+
+        self.orc, self.threads = orc, threads
+        w = WORKLOAD
+        t0 = time.perf_counter()
+        xyz, conn = fem.rod_mesh(w["nx"], w["ny"], w["nz"], w["lx"], w["ly"], w["lz"])
+        K, M, (Nx, Ny, Nz) = fem.assemble(xyz, conn, w["E"], w["nu"], w["rho"])
+        self.bc = fem.face_mask(xyz, 0, 0.0)
+        self.K, self.M = fem.applybc(K, self.bc), fem.applybc(M, self.bc)
+        self.amp = amplitude(seed)
+        self.rext = fem.traction(xyz, conn, 0, w["lx"], 0, self.amp, w["ly"] * w["lz"])
+        self.t_setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        (self.alu, self.jlu, self.ju), ierr = orc.ilut(self.K, w["lfil"], w["droptol"])
+        self.t_ilut = time.perf_counter() - t0
+        if ierr != 0:
+            raise RuntimeError(f"oracle ILUT ierr {ierr}")
+        self.nn, self.ne, self.p = len(xyz), len(conn), 3 * len(xyz)
+        xmin = xyz[conn - 1, 0].max(1)
+        layer = np.flatnonzero(xmin <= w["lx"] / w["nx"] + 1e-9)
+        rest = np.setdiff1d(np.arange(self.ne), layer)
+        pick = np.sort(np.random.default_rng(seed).choice(rest, len(rest) // sample_every,
+                                                          replace=False))
+        self.strata = []
+        for elems, weight in ((layer, 1.0), (pick, len(rest) / len(pick))):
+            gps = (elems[:, None] * 8 + np.arange(8)).ravel()
+            rows = (gps[:, None] * 8 + np.arange(8)).ravel()
+            st = {k: np.zeros(len(gps) * 6) for k in orc.STATE_KEYS[:4]}
+            st.update({k: np.zeros(len(gps)) for k in orc.STATE_KEYS[4:]})
+            self.strata.append(dict(
+                ne=len(elems), weight=weight, state=st,
+                nodes=np.repeat(conn[elems], 8, axis=0).ravel().astype(np.int32),
+                Nx=Nx[rows], Ny=Ny[rows], Nz=Nz[rows], ym=np.full(len(gps), w["E"]),
+                nu=np.full(len(gps), w["nu"])))
+        self.npts = 8 * (len(layer) + len(pick))
+        self.disp = np.zeros(6 * self.p)
+        self.bc6 = np.tile(self.bc, 6) == 1
+        self.w = 2 * np.pi * w["freq"]
+        self.dt = w["dt0"] * w["n1"]
+        self.nip = w["nipc"] * w["n1"]
+        self.tc = np.zeros(3)
+
+    def step(self):
+        orc = self.orc
+        t_start = time.perf_counter()
+        self.tc = self.tc[2] + np.arange(3) * self.dt / 2.0
+        ck, cm, ckt, cmt, ck1, cm1 = orc.stcoeff_m_quad(self.tc[0], self.dt, self.w)
+        fextc = orc.getfextc_m_quad(self.tc[0], self.w, self.dt)
+        orc.set_threads(self.threads)
         try:
-            t0 = time.perf_counter()
-            _, _, done, _ = orc.kronpgmres(k + kt, m + mt, K, M, alu, jlu, ju, rhs,
-                                           im=sample_its, eps=1e-30, maxits=sample_its)
-            return (time.perf_counter() - t0) / max(done, 1), done
+            f = np.concatenate([c * self.rext for c in fextc])
+            f = orc.kronspgemv(ck1, cm1, 1.0, 1.0, self.K, self.M, self.disp, f)
+            f[self.bc6] = 0.0
+            disp, ierr, its, _ = orc.kronpgmres(ck + ckt, cm + cmt, self.K, self.M, self.alu,
+                                                self.jlu, self.ju, f, im=WORKLOAD["im"],
+                                                eps=WORKLOAD["tol"], maxits=4000)
         finally:
             orc.set_threads(1)
+        if ierr != 0:
+            raise RuntimeError(f"oracle GMRES ierr {ierr}")
+        disp[self.bc6] = 0.0
+        self.disp = disp
+        t_solve = time.perf_counter() - t_start
+        Nt = orc.nt_table(self.nip, self.tc, self.w)
+        t_dmg = 0.0
+        plastic = 0
+        maxD = 0.0
+        for s in self.strata:
+            t0 = time.perf_counter()
+            orc.damage(s["ne"], self.nn, self.nip, s["nodes"], s["Nx"], s["Ny"], s["Nz"], Nt,
+                       disp, s["ym"], s["nu"], s["state"], nthreads=self.threads)
+            t_dmg += (time.perf_counter() - t0) * s["weight"]
+            plastic += int(np.count_nonzero(s["state"]["p"]))
+            maxD = max(maxD, float(s["state"]["D"].max()))
+        deletion = maxD >= WORKLOAD["Dc"]  # the deletion test over the sampled points
+        return {"wall_s": time.perf_counter() - t_start, "slab_s": t_solve + t_dmg,
+                "solve_s": t_solve, "damage_s": t_dmg, "its": its, "plastic_points": plastic,
+                "deletion": bool(deletion)}
 
-    t_serial, done = gmres_sample(1)
-    t_iter, _ = gmres_sample(threads) if threads > 1 else (t_serial, done)
-    # damage: a slice of the points over the full slab resolution
-    nip = WORKLOAD["nipc"] * WORKLOAD["n1"]
-    ne_s = max(1, min(ne, 8 * threads))
-    Nx, Ny, Nz = prob.strain_rows()
-    sol = np.random.default_rng(0).standard_normal(p * 6) * 1e-4
-    nodes = np.repeat(conn[:ne_s], 8, axis=0).ravel().astype(np.int32)
-    Nt = xt.nt_table(nip, np.array([0.0, dt / 2, dt]), w)
-    ngs = 8 * ne_s
-    st = {kk: np.zeros(ngs * 6) for kk in ["eps_old", "eps_pl", "sig_eff", "sig_back"]}
-    st.update({kk: np.zeros(ngs) for kk in ["p", "D", "ws", "del_po", "sig_d"]})
-    t0 = time.perf_counter()
-    orc.damage(ne_s, nn, nip, nodes, Nx[: ngs * 8], Ny[: ngs * 8], Nz[: ngs * 8], Nt, sol,
-               np.full(ngs, WORKLOAD["E"]), np.full(ngs, WORKLOAD["nu"]), st, nthreads=threads)
-    t_dmg = (time.perf_counter() - t0) * (ne / ne_s)
-    t_slab = t_iter * its + t_dmg
-    prob.close()
-    return {"value": round(1.0 / t_slab, 6), "unit": UNIT, "cores": threads,
-            "kind": "port",
-            "sample": (f"{done} GMRES iterations (one cycle) on {threads} threads "
-                       f"({t_iter * 1e3:.1f} ms each; {t_serial * 1e3:.1f} ms in the reference's "
-                       f"serial order), scaled to {its:.0f} per slab + damage of "
-                       f"{ngs} of {8 * ne} Gauss points x {nip} steps on {threads} threads "
-                       f"(scaled to all points)"),
-            "seconds_per_slab": round(t_slab, 3), "gmres_s_per_iter": round(t_iter, 5),
-            "gmres_s_per_iter_serial": round(t_serial, 5),
-            "value_serial_gmres": round(1.0 / (t_serial * its + t_dmg), 6),
-            "damage_s_per_slab": round(t_dmg, 3)}
+    def sample_text(self):
+        a, b = self.strata
+        return (f"each step one full C2 slab on {self.threads} host threads: oracle jump "
+                f"term, GMRES(200) to the reference's test |rs| <= 1e-8 ||r0|| on the slab's "
+                f"right-hand side, damage update over the full {self.nip} steps on a "
+                f"stratified sample of {self.npts} of {8 * self.ne} Gauss points (all "
+                f"{8 * a['ne']} points of the clamped layer, which hold every plastic point, "
+                f"+ a seeded 1/{round(b['weight'])} of the other elements, time scaled by "
+                f"stratum to all points); inputs from oracle/fem.py and the oracle's quadrature "
+                f"(the GPU library not loaded)")
+
+
+def cpu_baseline(threads, steps=1):
+    """cpu_baseline of the GPU arm: `steps` slabs of CpuSlab on the host's
+    cores, median projected slab time."""
+    slab = CpuSlab(threads)
+    recs = [slab.step() for _ in range(steps)]
+    t = float(np.median([r["slab_s"] for r in recs]))
+    return {"value": round(1.0 / t, 6), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": slab.sample_text(), "seconds_per_slab": round(t, 3),
+            "solve_s": round(float(np.median([r["solve_s"] for r in recs])), 3),
+            "damage_s_per_slab": round(float(np.median([r["damage_s"] for r in recs])), 3),
+            "iterations_per_slab": float(np.mean([r["its"] for r in recs])),
+            "plastic_points": recs[-1]["plastic_points"], "slabs": steps}
 
 
 def run_reference(args, rank, world):
+    """The reference arm: CpuSlab steps timed on rank 0 (other ranks exit
+    without work).  ms_per_step is the measured wall time of a step (the
+    work actually run); value is the projected full-slab rate of those
+    steps (the damage update scaled from its sample by stratum)."""
     if rank != 0:
         return None
     threads = os.cpu_count() or 1
-    vals = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        pass
+    t_run = time.perf_counter()
+    slab = CpuSlab(threads)
+    for _ in range(args.warmup):
+        slab.step()
+    recs = []
     t0 = time.perf_counter()
-    its_guess = float(args.ref_its)
     for _ in range(args.steps):
-        b = cpu_baseline(its=its_guess, sample_its=args.cpu_its, threads=threads, for_arm=True)
-        vals.append(b)
+        recs.append(slab.step())
     sec = time.perf_counter() - t0
-    v = float(np.median([b["value"] for b in vals]))
-    cfg = {"workload": "C2 prismatic rod 20x20x60 C3D8, 80,703 DOF x 6 temporal blocks",
-           "nip": WORKLOAD["nipc"] * WORKLOAD["n1"], "ilut": [WORKLOAD["droptol"],
-                                                              WORKLOAD["lfil"]],
-           "gmres_restart": WORKLOAD["im"], "tol": WORKLOAD["tol"],
-           "iterations_per_slab_assumed": its_guess}
+    t_slab = float(np.median([r["slab_s"] for r in recs]))
+    v = 1.0 / t_slab
     return {"impl": "reference", "metric": METRIC, "value": round(v, 6), "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(1e3 / v, 1), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "fp64", "data": "synthetic", "config": cfg,
+            "ms_per_step": round(sec * 1e3 / args.steps, 1), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+            "config": workload_config(slab.amp),
+            "precision": "fp64 gmres (the reference's kronpgmres), fp64 damage",
             "cpu_baseline": {"value": round(v, 6), "unit": UNIT, "cores": threads,
-                             "kind": "port", "sample": vals[0]["sample"],
-                             "value_serial_gmres": float(np.median(
-                                 [b["value_serial_gmres"] for b in vals]))},
+                             "kind": "port", "sample": slab.sample_text()},
             "e2e": {"value": round(v, 6), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "wall_s": round(sec, 1)}
+            "value_measured_steps": round(args.steps / sec, 6),
+            "projected_slab_s": round(t_slab, 3),
+            "solve_s": round(float(np.median([r["solve_s"] for r in recs])), 3),
+            "damage_s_per_slab": round(float(np.median([r["damage_s"] for r in recs])), 3),
+            "iterations_per_slab": float(np.mean([r["its"] for r in recs])),
+            "plastic_points": recs[-1]["plastic_points"],
+            "setup_s": {"mesh_assembly": round(slab.t_setup, 2), "ilut": round(slab.t_ilut, 2)},
+            "wall_s": round(time.perf_counter() - t_run, 1)}
 
 
 # ------------------------------------------------------------ harness
@@ -713,8 +776,6 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-its", type=int, default=40)
-    ap.add_argument("--ref-its", type=float, default=182.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
