@@ -684,7 +684,7 @@ class CpuSlab:
                 f"{8 * a['ne']} points of the clamped layer, which hold every plastic point, "
                 f"+ a seeded 1/{round(b['weight'])} of the other elements, time scaled by "
                 f"stratum to all points); inputs from oracle/fem.py and the oracle's quadrature "
-                f"(the GPU library not loaded)")
+                f"(built without the GPU library)")
 
 
 def cpu_baseline(threads, steps=1):

@@ -81,14 +81,21 @@ def rod8_system(xt):
 
 
 ILU_VARIANTS = [
-    {},                                  # defaults: column records, one temporal block per
-                                         # thread block, H=2 (FP32); rows S=2 (FP64)
-    {"XTFEM_ILU_SHARES": "1"},
+    {},                                  # defaults: rows with register-prefetched records,
+                                         # one temporal block per thread block, H=2 (FP32);
+                                         # rows through the ring, S=2 (FP64)
+    {"XTFEM_ILU_SHARES": "1"},           # register rows, one lane per row
+    {"XTFEM_ILU_SHARES": "4"},
+    {"XTFEM_ILU_WARPS": "1"},            # one compute warp: every level overflows
+    {"XTFEM_ILU_WARPS": "2"},
+    {"XTFEM_ILU_WARPS": "16"},           # more warps than chunks on most levels
+    {"XTFEM_ILU_FMT": "3"},              # column records through the TMA ring
+    {"XTFEM_ILU_FMT": "3", "XTFEM_ILU_SHARES": "1"},
+    {"XTFEM_ILU_FMT": "3", "XTFEM_ILU_WARPS": "1"},  # many passes per level
+    {"XTFEM_ILU_FMT": "3", "XTFEM_ILU_WARPS": "3"},
     {"XTFEM_ILU_FMT": "2"},              # column records, one pair per thread block
     {"XTFEM_ILU_FMT": "2", "XTFEM_ILU_SHARES": "2"},
     {"XTFEM_ILU_FMT": "2", "XTFEM_ILU_RING_KB": "10"},
-    {"XTFEM_ILU_WARPS": "1"},            # one compute warp: many passes per level
-    {"XTFEM_ILU_WARPS": "3"},
     {"XTFEM_ILU_FMT": "1"},              # node blocks, 3 thread blocks per sweep
     {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SHARES": "1"},
     {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SHARES": "4"},
@@ -96,15 +103,15 @@ ILU_VARIANTS = [
     {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1"},  # all temporal-block pairs in one thread block
     {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_SHARES": "4"},
     {"XTFEM_ILU_FMT": "1", "XTFEM_ILU_SPLIT": "1", "XTFEM_ILU_WARPS": "1"},
-    {"XTFEM_ILU_FMT": "0"},              # row format for FP32 too
+    {"XTFEM_ILU_FMT": "0"},              # row format through the ring for FP32 too
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "1"},
     {"XTFEM_ILU_FMT": "0", "XTFEM_ILU_LANES": "4"},
     {"XTFEM_ILU_SIMPLE": "1"},           # one-warp-per-group fallback
     # tight rings: a level's copy often needs the region of the level just
     # before it, so that level must be released before the next can start
-    {"XTFEM_ILU_RING_KB": "10"},
-    {"XTFEM_ILU_RING_KB": "14"},
-    {"XTFEM_ILU_RING_KB": "20"},
+    {"XTFEM_ILU_RING_KB": "10", "XTFEM_ILU_FMT": "3"},
+    {"XTFEM_ILU_RING_KB": "14", "XTFEM_ILU_FMT": "3"},
+    {"XTFEM_ILU_RING_KB": "20", "XTFEM_ILU_FMT": "3"},
     {"XTFEM_ILU_RING_KB": "6", "XTFEM_ILU_FMT": "1"},
     {"XTFEM_ILU_RING_KB": "10", "XTFEM_ILU_FMT": "1"},
     {"XTFEM_ILU_RING_KB": "6", "XTFEM_ILU_FMT": "0"},

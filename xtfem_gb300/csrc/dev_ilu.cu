@@ -657,11 +657,18 @@ int build_col_tri(const TriHost& h, int Q, int H, const std::vector<int>& gdst, 
 
 }  // namespace
 
+struct RegTri;
 struct IluStage {
     int q = 0;
     unsigned rs = 0;  // right-hand-side record stride in bytes
     StageTri L, U;
     DBuf<unsigned char> rhsL, rhsU;  // ngroups records each, level order
+    // register-prefetched row sweep (fmt 4): both triangles, the pre-pass
+    // map and the per-temporal-block right-hand-side arrays
+    std::shared_ptr<RegTri> regL, regU;
+    DBuf<int> srcL;
+    DBuf<float> rrhsL, rrhsU;
+    bool reg_ok = false;
 };
 
 namespace {
@@ -1417,6 +1424,459 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_tri_col(StageArgs<float> a
     stage_main<float>(a, body, smem);
 }
 
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Register-prefetched row sweep (FP32, g = 3; the default for FP32).
+//
+// One thread block per temporal block (Q blocks per sweep, each on its own
+// SM), each the whole level chain, as the column format; but the factor
+// data never passes through shared memory.  Shared memory holds only the
+// solution window (3 rows x 1 value per slot); every record of a level is
+// loaded from global memory (L2) straight into registers two levels ahead
+// of its use, so a level's critical path is: window reads at offsets
+// already in registers, one multiply-add per factor entry, the share and
+// diagonal-block shuffles, the window store and one block barrier.
+//
+// Layout.  Lane = (group of the warp's chunk, row r of the group, share h
+// of the row's entries, H shares): lanes g*3H + r*H + h; a lane takes the
+// row's off-diagonal entries h, h+H, h+2H, ... (one per step).  The groups
+// of a level are sorted by their longest row and dealt to chunks of
+// 32/(3H) groups; chunk w < ncw of level l sits at the fixed slot
+// l*ncw + w (a level's chunks beyond ncw go to an overflow area, processed
+// by the same warps in extra passes).  A slot holds, per lane:
+//   float4 {minv[r][0..2] (row r of the inverted 3 x 3 diagonal block),
+//           window offset of the row (-1: lane stores nothing)}   512 B
+//   int    destination (forward: the backward sweep's right-hand-side
+//          slot of the row; backward: row * Q of z)               128 B
+//   u16 x 2 window offsets of steps (2k, 2k+1)                   SMAX/2 x 128 B
+//   float  factor value of each step                             SMAX x 128 B
+// Missing entries point at an all-zero window slot with value 0.  A byte
+// table per warp gives the steps of each level's chunk (0xFF: none; bit
+// 0x40: the level has overflow chunks); a warp keeps 32 levels of it in a
+// register and reads it by shuffle.  The right-hand sides are
+// per-temporal-block arrays in the same lane-slot order (the forward
+// sweep's from a pre-pass that also applies the q x q mixing with A^-1; the
+// backward sweep's written by the forward sweep), so every load of a level
+// has an address known in advance.
+constexpr int kRegMaxWarps = 16;
+constexpr unsigned kRegLaneTab = 640;
+
+struct RegTri {
+    int nl = 0, nlp = 0, ncw = 0, H = 0, smax = 0, novf = 0, slot_bytes = 0;
+    int win_elems = 0, zero_off = 0;
+    long long lanes = 0;  // (nl * ncw + novf) * 32
+    DBuf<unsigned char> slots, steps, ovf_steps;
+    DBuf<int> ovf;                 // per level {chunks, first overflow chunk}
+    std::vector<int> row_slot;     // host: lane slot of each row's h = 0 lane
+    std::vector<std::vector<int>> chunks;  // host (build only): level-order groups per chunk
+    std::vector<int> chunk_level, chunk_slot, chunk_steps;
+};
+
+namespace {
+
+int reg_warps(const TriHost& h, int GPW)
+{
+    std::vector<int> nch;
+    for (int l = 0; l < h.nlevels; ++l)
+        nch.push_back((h.level_ptr[l + 1] - h.level_ptr[l] + GPW - 1) / GPW);
+    std::sort(nch.begin(), nch.end());
+    const int p97 = nch[(size_t)(0.97 * (nch.size() - 1))];
+    const int w = env_int("XTFEM_ILU_WARPS", p97);
+    return std::max(1, std::min(kRegMaxWarps, w));
+}
+
+// Chunks, slots and steps of one triangle (no device data yet).
+bool reg_plan(const TriHost& h, int H, RegTri& t)
+{
+    const int g = 3, GS = 3 * H, GPW = 32 / GS, nl = h.nlevels;
+    t.nl = nl;
+    t.H = H;
+    t.ncw = reg_warps(h, GPW);
+    t.row_slot.assign((size_t)h.ngroups * g, -1);
+    t.chunks.clear();
+    t.chunk_level.clear();
+    t.chunk_slot.clear();
+    t.chunk_steps.clear();
+    int novf = 0, smax = 0;
+    std::vector<int> ord;
+    for (int l = 0; l < nl; ++l) {
+        const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
+        ord.resize(ng);
+        auto rowlen = [&](int i, int r) {
+            return h.ext_ptr[(size_t)i * g + r + 1] - h.ext_ptr[(size_t)i * g + r];
+        };
+        auto longest = [&](int i) {
+            return std::max(rowlen(i, 0), std::max(rowlen(i, 1), rowlen(i, 2)));
+        };
+        for (int j = 0; j < ng; ++j) ord[j] = gb + j;
+        std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return longest(a) > longest(b); });
+        const int nch = (ng + GPW - 1) / GPW;
+        for (int c = 0; c < nch; ++c) {
+            std::vector<int> grp(ord.begin() + c * GPW, ord.begin() + std::min(ng, (c + 1) * GPW));
+            const long long slot = c < t.ncw ? (long long)l * t.ncw + c
+                                             : (long long)nl * t.ncw + novf++;
+            int steps = 0;
+            for (int gw = 0; gw < (int)grp.size(); ++gw) {
+                const int i = grp[gw], G = h.order[i];
+                for (int r = 0; r < g; ++r) {
+                    steps = std::max(steps, (rowlen(i, r) + H - 1) / H);
+                    t.row_slot[(size_t)G * g + r] = (int)(slot * 32 + gw * GS + r * H);
+                }
+            }
+            if (slot * 32 + 31 >= INT32_MAX) return false;
+            smax = std::max(smax, steps);
+            t.chunks.push_back(std::move(grp));
+            t.chunk_level.push_back(l);
+            t.chunk_slot.push_back((int)slot);
+            t.chunk_steps.push_back(steps);
+        }
+    }
+    t.novf = novf;
+    t.smax = smax;
+    t.lanes = ((long long)nl * t.ncw + novf) * 32;
+    t.nlp = ((nl + 31) / 32 + 1) * 32;
+    t.zero_off = h.nslots * g;
+    t.win_elems = (h.nslots + 1) * g;
+    return smax < 0x40 && t.win_elems <= 65536 &&
+           (long long)t.win_elems * 4 <= (long long)max_dyn_smem();
+}
+
+// Slots and tables of a planned triangle.  dst: forward, the other
+// triangle's row_slot; backward (dst empty): row * Q.
+int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int>* dst,
+             cudaStream_t s)
+{
+    const int g = 3, H = t.H, GS = 3 * H, GPW = 32 / GS;
+    t.smax = smax;
+    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 2) * 128u + (unsigned)smax * 128u);
+    const size_t nslot = (size_t)t.nl * t.ncw + t.novf;
+    std::vector<unsigned char> blob(nslot * t.slot_bytes, 0);
+    std::vector<unsigned char> steps((size_t)t.ncw * t.nlp, 0xFF);
+    std::vector<unsigned char> osteps(std::max(1, t.novf), 0);
+    std::vector<int> ovf((size_t)2 * t.nl, 0);
+    bool valid = true;
+    for (size_t c = 0; c < t.chunks.size(); ++c) {
+        const int l = t.chunk_level[c], slot = t.chunk_slot[c], stp = t.chunk_steps[c];
+        unsigned char* b = blob.data() + (size_t)slot * t.slot_bytes;
+        float* gm = reinterpret_cast<float*>(b);
+        int* go = reinterpret_cast<int*>(b + 512);
+        unsigned short* off = reinterpret_cast<unsigned short*>(b + kRegLaneTab);
+        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 2) * 128);
+        const auto& grp = t.chunks[c];
+        for (int lane = 0; lane < 32; ++lane) {
+            const int gw = lane / GS, r = (lane % GS) / H, hh = lane % H;
+            const bool live = gw < GPW && gw < (int)grp.size();
+            int wo = -1;
+            for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = 0.0f;
+            int kb = 0, ke = 0;
+            if (live) {
+                const int i = grp[gw], G = h.order[i];
+                for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = (float)h.minv[(size_t)i * 9 + r * 3 + k];
+                if (hh == 0) {
+                    wo = h.slot[G] * g + r;
+                    const long long d = dst ? (long long)(*dst)[(size_t)G * g + r]
+                                            : ((long long)G * g + r) * Q;
+                    valid = valid && d >= 0 && d < INT32_MAX;
+                    go[lane] = (int)d;
+                }
+                kb = h.ext_ptr[(size_t)i * g + r];
+                ke = h.ext_ptr[(size_t)i * g + r + 1];
+            }
+            std::memcpy(&gm[lane * 4 + 3], &wo, 4);
+            for (int st = 0; st < smax; ++st) {
+                const int k = kb + hh + st * H;
+                int o = t.zero_off;
+                float v = 0.0f;
+                if (live && k < ke) {
+                    const int col = h.ext_col[k], Gc = col / g;
+                    o = h.slot[Gc] * g + (col - Gc * g);
+                    v = (float)h.ext_v[k];
+                }
+                valid = valid && o >= 0 && o + 1 <= t.win_elems && o < 65536;
+                off[(size_t)(st >> 1) * 64 + lane * 2 + (st & 1)] = (unsigned short)o;
+                val[(size_t)st * 32 + lane] = v;
+            }
+        }
+        if (slot < t.nl * t.ncw) {
+            steps[(size_t)(slot % t.ncw) * t.nlp + l] = (unsigned char)stp;
+        } else {
+            osteps[slot - t.nl * t.ncw] = (unsigned char)stp;
+        }
+    }
+    // levels with overflow chunks: flag every warp's entry, record the list
+    {
+        int oi = 0;
+        std::vector<int> nch(t.nl, 0);
+        for (size_t c = 0; c < t.chunks.size(); ++c) nch[t.chunk_level[c]]++;
+        for (int l = 0; l < t.nl; ++l) {
+            ovf[2 * l] = nch[l];
+            ovf[2 * l + 1] = oi;
+            if (nch[l] > t.ncw) {
+                oi += nch[l] - t.ncw;
+                for (int w = 0; w < t.ncw; ++w) steps[(size_t)w * t.nlp + l] |= 0x40;
+            }
+        }
+        valid = valid && oi == t.novf;
+    }
+    if (!valid) return XT_OK;
+    XT_TRY(t.slots.upload(blob.data(), blob.size(), s));
+    XT_TRY(t.steps.upload(steps.data(), steps.size(), s));
+    XT_TRY(t.ovf_steps.upload(osteps.data(), osteps.size(), s));
+    XT_TRY(t.ovf.upload(ovf.data(), ovf.size(), s));
+    XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    t.chunks.clear();
+    t.chunks.shrink_to_fit();
+    return XT_OK;
+}
+
+// Register capacities (steps per lane) compiled for each share count.
+int reg_smax(int H, int need)
+{
+    static const int caps2[] = {8, 12, 16}, caps1[] = {12, 24, 32}, caps4[] = {8};
+    const int* c = H == 2 ? caps2 : (H == 1 ? caps1 : caps4);
+    const int n = H == 2 ? 3 : (H == 1 ? 3 : 1);
+    for (int i = 0; i < n; ++i)
+        if (need <= c[i]) return c[i];
+    return 0;
+}
+
+int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
+{
+    st.reg_ok = false;
+    if (S.L.g != 3 || (H != 1 && H != 2 && H != 4)) return XT_OK;
+    auto L = std::make_shared<RegTri>(), U = std::make_shared<RegTri>();
+    if (!reg_plan(S.L, H, *L) || !reg_plan(S.U, H, *U)) return XT_OK;
+    const int smax = reg_smax(H, std::max(L->smax, U->smax));
+    if (smax == 0) return XT_OK;
+    XT_TRY(reg_fill(S.U, *U, smax, Q, nullptr, s));
+    XT_TRY(reg_fill(S.L, *L, smax, Q, &U->row_slot, s));
+    if (!L->slots.p || !U->slots.p) return XT_OK;
+    std::vector<int> src((size_t)L->lanes, -1);
+    for (size_t r = 0; r < L->row_slot.size(); ++r) src[(size_t)L->row_slot[r]] = (int)r;
+    XT_TRY(st.srcL.upload(src.data(), src.size(), s));
+    XT_TRY(st.rrhsL.alloc((size_t)Q * L->lanes));
+    XT_TRY(st.rrhsU.alloc((size_t)Q * U->lanes));
+    // slots the forward sweep never writes are read (not used) by the
+    // backward sweep's padding lanes: keep them finite
+    XT_CUDA(cudaMemsetAsync(st.rrhsU.p, 0, sizeof(float) * Q * U->lanes, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    L->row_slot.clear();
+    U->row_slot.clear();
+    if (trace_on())
+        std::fprintf(stderr, "[xtfem] register sweep: H %d, steps %d, warps %d/%d, overflow chunks %d/%d\n",
+                     H, smax, L->ncw, U->ncw, L->novf, U->novf);
+    st.regL = L;
+    st.regU = U;
+    st.reg_ok = true;
+    return XT_OK;
+}
+
+struct RegArgs {
+    const unsigned char* slots;
+    const unsigned char* steps;
+    const int2* ovf;
+    const unsigned char* ovf_steps;
+    const float* rhs;      // [Q][rstride] right-hand sides in lane-slot order
+    float* out;            // forward: the backward sweep's rhs; backward: z
+    long long rstride, ostride;
+    int nl, nlp, ncw, slot_bytes, zero_off;
+};
+
+template <int SMAX>
+struct RegSet {
+    int code;
+    unsigned off2[SMAX / 2];
+    float val[SMAX];
+    float4 gm;
+    int go;
+    float b;
+};
+
+template <int SMAX>
+__device__ __forceinline__ void reg_load(RegSet<SMAX>& S, const unsigned char* base, int code,
+                                         const float* bsrc, int lane)
+{
+    S.code = code;
+    if (code == 0xFF) return;
+    const int stp = code & 0x3F;
+    S.gm = __ldg(reinterpret_cast<const float4*>(base) + lane);
+    S.go = __ldg(reinterpret_cast<const int*>(base + 512) + lane);
+    const unsigned* o = reinterpret_cast<const unsigned*>(base + kRegLaneTab);
+    const float* v = reinterpret_cast<const float*>(base + kRegLaneTab + (SMAX / 2) * 128);
+#pragma unroll
+    for (int k = 0; k < SMAX / 2; ++k)
+        if (2 * k < stp) S.off2[k] = __ldg(o + k * 32 + lane);
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st)
+        if (st < stp) S.val[st] = __ldg(v + st * 32 + lane);
+    S.b = __ldg(bsrc);
+}
+
+template <int H, int SMAX, bool UPPER>
+__device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, float* win, const RegArgs& a,
+                                          int lane0, int tb)
+{
+    const int stp = S.code & 0x3F;
+    float acc0 = 0.0f, acc1 = 0.0f;
+#pragma unroll
+    for (int st = 0; st < SMAX; ++st) {
+        if (st < stp) {
+            const unsigned w2 = S.off2[st >> 1];
+            const unsigned o = (st & 1) ? (w2 >> 16) : (w2 & 0xFFFFu);
+            const float x = win[o];
+            if (st & 1) acc1 = fmaf(S.val[st], x, acc1);
+            else acc0 = fmaf(S.val[st], x, acc0);
+        }
+    }
+    float acc = acc0 + acc1;
+#pragma unroll
+    for (int m = 1; m < H; m <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    const float d = S.b - acc;
+    const float d0 = __shfl_sync(0xffffffffu, d, lane0);
+    const float d1 = __shfl_sync(0xffffffffu, d, lane0 + H);
+    const float d2 = __shfl_sync(0xffffffffu, d, lane0 + 2 * H);
+    const float sol = fmaf(S.gm.z, d2, fmaf(S.gm.y, d1, S.gm.x * d0));
+    const int wo = __float_as_int(S.gm.w);
+    if (wo >= 0) {
+        win[wo] = sol;
+        if (UPPER) a.out[(size_t)S.go + tb] = sol;
+        else a.out[(size_t)tb * a.ostride + S.go] = sol;
+    }
+}
+
+// The chunks of level L beyond the ncw primary ones (wide levels).
+template <int H, int SMAX, bool UPPER>
+__device__ __noinline__ void reg_overflow(const RegArgs& a, int L, float* win, const float* rhs,
+                                          int warp, int lane, int lane0, int tb)
+{
+    const int2 ov = a.ovf[L];
+    for (int c = a.ncw + warp; c < ov.x; c += a.ncw) {
+        const int oi = ov.y + (c - a.ncw);
+        const size_t sl = (size_t)a.nl * a.ncw + oi;
+        RegSet<SMAX> T;
+        reg_load<SMAX>(T, a.slots + sl * a.slot_bytes, a.ovf_steps[oi], rhs + sl * 32 + lane, lane);
+        reg_level<H, SMAX, UPPER>(T, win, a, lane0, tb);
+    }
+}
+
+template <int H, int SMAX, bool UPPER>
+__global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
+{
+    extern __shared__ __align__(16) float rwin[];
+    const int tb = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int GS = 3 * H;
+    const int lane0 = (lane / GS) * GS;
+    const float* rhs = a.rhs + (size_t)tb * a.rstride;
+    if (threadIdx.x < 3) rwin[a.zero_off + threadIdx.x] = 0.0f;
+    // the warp's step codes, 32 levels per register
+    const unsigned char* stw = a.steps + (size_t)warp * a.nlp;
+    int st_cur = stw[lane], st_next = stw[32 + lane], blk = 0;
+    RegSet<SMAX> s0, s1;
+    auto load = [&](RegSet<SMAX>& S, int L) {
+        int code = 0xFF;
+        if (L < a.nl) {
+            if ((L >> 5) != blk) {  // L advances one level per call
+                st_cur = st_next;
+                ++blk;
+                st_next = stw[(size_t)(blk + 1) * 32 + lane];
+            }
+            code = __shfl_sync(0xffffffffu, st_cur, L & 31);
+        }
+        const size_t sl = (size_t)L * a.ncw + warp;
+        reg_load<SMAX>(S, a.slots + sl * a.slot_bytes, code, rhs + sl * 32 + lane, lane);
+    };
+    load(s0, 0);
+    load(s1, 1);
+    __syncthreads();  // the zero slot is set
+    for (int l = 0; l < a.nl; l += 2) {
+        if (s0.code != 0xFF) {
+            reg_level<H, SMAX, UPPER>(s0, rwin, a, lane0, tb);
+            if (s0.code & 0x40) reg_overflow<H, SMAX, UPPER>(a, l, rwin, rhs, warp, lane, lane0, tb);
+        }
+        load(s0, l + 2);
+        __syncthreads();
+        if (l + 1 < a.nl) {
+            if (s1.code != 0xFF) {
+                reg_level<H, SMAX, UPPER>(s1, rwin, a, lane0, tb);
+                if (s1.code & 0x40)
+                    reg_overflow<H, SMAX, UPPER>(a, l + 1, rwin, rhs, warp, lane, lane0, tb);
+            }
+            load(s1, l + 3);
+            __syncthreads();
+        }
+    }
+}
+
+// Forward-sweep right-hand sides in lane-slot order, one array per temporal
+// block: rhs[q][s] = sum_j Ainv(q, j) v(row(s), j) (0 for unused slots).
+template <int Q>
+__global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
+                            const double* __restrict__ dAinv, const float* __restrict__ v,
+                            float* __restrict__ rhs)
+{
+    __shared__ float sA[Q * Q];
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sA[i] = (float)dAinv[i];
+    __syncthreads();
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < lanes;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int row = src[t];
+        float vr[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) vr[j] = row >= 0 ? v[(size_t)row * Q + j] : 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            float b = 0.0f;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) b = fmaf(sA[j * Q + q], vr[j], b);
+            rhs[(size_t)q * lanes + t] = b;
+        }
+    }
+}
+
+template <int Q, int H, int SMAX>
+int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s)
+{
+    static std::atomic<bool> attr{false};
+    if (!attr.load(std::memory_order_acquire)) {
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+        attr.store(true, std::memory_order_release);
+    }
+    const RegTri& L = *st.regL;
+    const RegTri& U = *st.regU;
+    const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
+    k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p);
+    RegArgs aL{L.slots.p, L.steps.p, reinterpret_cast<const int2*>(L.ovf.p), L.ovf_steps.p,
+               st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.nlp, L.ncw, L.slot_bytes,
+               L.zero_off};
+    RegArgs aU{U.slots.p, U.steps.p, reinterpret_cast<const int2*>(U.ovf.p), U.ovf_steps.p,
+               st.rrhsU.p, z, U.lanes, 0, U.nl, U.nlp, U.ncw, U.slot_bytes, U.zero_off};
+    k_tri_reg<H, SMAX, false><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
+    k_tri_reg<H, SMAX, true><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
+    note_launches(3);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+template <int Q>
+int launch_reg_any(const IluStage& st, const double* dAinv, const float* v, float* z,
+                   cudaStream_t s)
+{
+    const int H = st.regL->H, smax = st.regL->smax;
+    if (H == 2 && smax == 8) return launch_reg<Q, 2, 8>(st, dAinv, v, z, s);
+    if (H == 2 && smax == 12) return launch_reg<Q, 2, 12>(st, dAinv, v, z, s);
+    if (H == 2 && smax == 16) return launch_reg<Q, 2, 16>(st, dAinv, v, z, s);
+    if (H == 1 && smax == 12) return launch_reg<Q, 1, 12>(st, dAinv, v, z, s);
+    if (H == 1 && smax == 24) return launch_reg<Q, 1, 24>(st, dAinv, v, z, s);
+    if (H == 1 && smax == 32) return launch_reg<Q, 1, 32>(st, dAinv, v, z, s);
+    if (H == 4 && smax == 8) return launch_reg<Q, 4, 8>(st, dAinv, v, z, s);
+    set_error("register sweep: no kernel for these shares and steps");
+    return XT_ERR_ARG;
+}
+
 // ---------------------------------------------------------------------------
 // Launchers.
 template <class T, int Q>
@@ -1442,8 +1902,11 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
     const bool col = fmt == 2 || fmt == 3;
     const int wenv = col ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
     const int rkb = std::max(0, std::min(255, env_int("XTFEM_ILU_RING_KB", 0)));
+    const bool hkey = col || fmt == 4;
+    const int wkey = (col || fmt == 4) ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
     const int key =
-        ((((q * 4 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 4 + (col ? H : 0)) * 64 + wenv) * 256 + rkb;
+        ((((q * 8 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 8 + (hkey ? H : 0)) * 64 + wkey) * 256 + rkb;
+    (void)wenv;
     auto it = F.stages.find(key);
     if (it == F.stages.end()) {
         auto st = std::make_shared<IluStage>();
@@ -1455,6 +1918,12 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
         for (int G = 0; G < ng; ++G) {
             gdL[G] = U.pos[G];
             gdU[G] = G * g;
+        }
+        if (fmt == 4) {
+            if (sizeof(T) == 4) XT_TRY(build_reg(*F.sched, q, H, *st, s));
+            it = F.stages.emplace(key, st).first;
+            out = st->reg_ok ? st.get() : nullptr;
+            return XT_OK;
         }
         if (fmt == 2 || fmt == 3) {
             if (sizeof(T) == 4) {
@@ -1477,6 +1946,10 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
             XT_TRY(st->rhsU.alloc((size_t)ng * st->rs));
         }
         it = F.stages.emplace(key, st).first;
+    }
+    if (fmt == 4) {
+        out = it->second->reg_ok ? it->second.get() : nullptr;
+        return XT_OK;
     }
     if (it->second->L.ok && it->second->U.ok) out = it->second.get();
     return XT_OK;
@@ -1565,11 +2038,21 @@ template <class T, int Q>
 int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
 {
     IluStage* st = nullptr;
+    // 4 (default): rows with register-prefetched records, one temporal
+    // block per thread block; 3: column records through a TMA ring, one
+    // temporal block per thread block; 2: column records, one pair per
+    // thread block; 1: node blocks; 0: rows through the ring.  A format
+    // that cannot be laid out for the factor falls back to the next.
+    int fmt = env_int("XTFEM_ILU_FMT", 4);
+    if constexpr (sizeof(T) == 4) {
+        if (F.L.g == 3 && fmt == 4) {
+            const int H = env_int("XTFEM_ILU_SHARES", 2);
+            XT_TRY(get_stage<T>(F, Q, 4, s, st, H));
+            if (st) return launch_reg_any<Q>(*st, dAinv, v, z, s);
+            fmt = 3;
+        }
+    }
     if constexpr (sizeof(T) == 4 && Q % 2 == 0) {
-        // 3 (default): column records, one temporal block per thread block;
-        // 2: column records, one pair per thread block; 1: node blocks;
-        // 0: rows
-        const int fmt = env_int("XTFEM_ILU_FMT", 3);
         if (F.L.g == 3 && fmt == 3) {
             const int H = env_int("XTFEM_ILU_SHARES", 2) == 1 ? 1 : 2;
             XT_TRY(get_stage<T>(F, Q, 3, s, st, H));
