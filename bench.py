@@ -218,6 +218,7 @@ def run_gpu(args, rank, world):
         t_host = (time.perf_counter() - t_host0) * 1e3
     launches = xt.lib().xt_launch_count() - launches0
     prof = {c: xt.profile_read(c) for c in CLASS_NAMES}
+    orth_bytes = {c: xt.profile_bytes(c) for c in (5, 6)}
     xt.profile(False)
     ms_max = dist_max(ms, world)
     value = args.steps * world / (ms_max / 1e3)
@@ -225,6 +226,9 @@ def run_gpu(args, rank, world):
     # roofline of the dominant kernel class
     hbm, peak_kind = peaks()
     nbytes = algorithmic_bytes(prob, ilu_nnz, p, merged=merged)
+    for c in (5, 6):  # Gram-Schmidt steps: mean of the recorded per-step bytes
+        if prof[c][0]:
+            nbytes[c] = int(orth_bytes[c] / prof[c][0])
     dom = max((c for c in prof if nbytes[c]), key=lambda c: prof[c][1])
     cnt, tot = prof[dom]
     avg_ms = tot / max(cnt, 1)

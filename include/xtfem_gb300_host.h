@@ -245,6 +245,10 @@ int xt_slab_couple(xt_slab s, xt_thermal t, const xt_coupling_config *cc);
  * basis, 7 Kronecker double-float on an FP32 vector). */
 int xt_profile(int enable);
 int xt_profile_read(int cls, long long *count, double *ms);
+/* Algorithmic bytes summed over the timed launches of a class, for the
+ * classes that record them (5, 6: (4i + 6) n values per Arnoldi step i,
+ * two dot passes and two update passes over the i basis vectors). */
+int xt_profile_bytes(int cls, double *bytes);
 /* Kernel launches issued by the library since load. */
 long long xt_launch_count(void);
 /* CUDA events on the library stream: record slot 0..7, elapsed ms a -> b

@@ -101,6 +101,7 @@ SIGNATURES = {
     "xt_slab_get": (C.c_int, [_vp, _dp, _dp, _dp, _ip]),
     "xt_profile": (C.c_int, [C.c_int]),
     "xt_profile_read": (C.c_int, [C.c_int, C.POINTER(C.c_longlong), _dp]),
+    "xt_profile_bytes": (C.c_int, [C.c_int, _dp]),
     "xt_launch_count": (C.c_longlong, []),
     "xt_mark": (C.c_int, [C.c_int]),
     "xt_elapsed_ms": (C.c_double, [C.c_int, C.c_int]),

@@ -29,7 +29,7 @@ __all__ = [
     "chkelesta", "kokkos_host", "damage", "ilut", "stcoeff_m", "stcoeff_t", "getfextc_m",
     "getfextc_t", "nt_table", "SpaceTimeSystem", "SystemBatch", "ThermalConfig", "ThermalSolver",
     "Problem", "SlabConfig", "SlabSolver", "slab_log_line", "set_cache", "invalidate", "profile",
-    "profile_read",
+    "profile_read", "profile_bytes",
 ]
 
 
@@ -683,3 +683,11 @@ def profile_read(cls: int):
     n, ms = C.c_longlong(0), C.c_double(0)
     check(lib().xt_profile_read(cls, C.byref(n), C.byref(ms)), "xt_profile_read")
     return n.value, ms.value
+
+
+def profile_bytes(cls: int) -> float:
+    """Algorithmic bytes recorded for the timed launches of a class (0.0
+    for the classes whose bytes bench.py counts from the sizes)."""
+    b = C.c_double(0)
+    check(lib().xt_profile_bytes(cls, C.byref(b)), "xt_profile_bytes")
+    return b.value

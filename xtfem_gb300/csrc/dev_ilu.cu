@@ -801,9 +801,10 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
     return ok != 0;
 }
 // Bounded wait for the phase of the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity)
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity,
+                                          long long limit = kSpinLimit)
 {
-    for (long long i = 0; i < kSpinLimit; ++i)
+    for (long long i = 0; i < limit; ++i)
         if (mbar_try_wait(b, parity)) return true;
     return false;
 }
@@ -897,6 +898,8 @@ struct StageArgs {
     int nl, g, ncw, window_bytes;
     unsigned rs;               // record stride in bytes
     int aux;                   // column format: offset of the all-zero window slot
+    long long spin;            // polls before a wait for a level gives up (the
+                               // drain of copies in flight always polls kSpinLimit)
 };
 
 // Producer: one thread copies every level's blob and right-hand-side chunk
@@ -910,7 +913,7 @@ __device__ void stage_producer(const StageArgs<T>& a, unsigned long long* full,
         const int iss = t0.w;
         if (iss > 0) {
             const int c = iss - 1;
-            if (!mbar_wait(cons + c % kNB, (unsigned)(c / kNB) & 1u)) {
+            if (!mbar_wait(cons + c % kNB, (unsigned)(c / kNB) & 1u, a.spin)) {
                 atomicExch(&g_ilu_error, 2);
                 // let the copies already issued land before the block exits
                 for (int L2 = max(0, L - kNB); L2 < L; ++L2)
@@ -969,7 +972,7 @@ __device__ __forceinline__ void stage_main(const StageArgs<T>& a, Body& body, un
     if (warp == a.ncw + 1) {
         for (int l = 0; l < a.nl; ++l) {
             int ok = 1;
-            if (lane == 0) ok = mbar_wait(full + l % kNB, (unsigned)(l / kNB) & 1u) ? 1 : 0;
+            if (lane == 0) ok = mbar_wait(full + l % kNB, (unsigned)(l / kNB) & 1u, a.spin) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok && lane == 0) {
                 *s_abort = 1;
@@ -1449,8 +1452,11 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_tri_col(StageArgs<float> a
 //           window offset of the row (-1: lane stores nothing)}   512 B
 //   int    destination (forward: the backward sweep's right-hand-side
 //          slot of the row; backward: row * Q of z)               128 B
-//   u16 x 2 window offsets of steps (2k, 2k+1)                   SMAX/2 x 128 B
-//   float  factor value of each step                             SMAX x 128 B
+//   u16 x 4 window offsets of steps 4k..4k+3                     SMAX/4 x 256 B
+//   float4 factor values of steps 4k..4k+3                       SMAX/4 x 512 B
+// The loads are inline-PTX non-coherent loads (volatile, so they are
+// issued where they stand: two levels before their use, not sunk to it),
+// and the level barrier is a volatile bar.sync that they do not cross.
 // Missing entries point at an all-zero window slot with value 0.  A byte
 // table per warp gives the steps of each level's chunk (0xFF: none; bit
 // 0x40: the level has overflow chunks); a warp keeps 32 levels of it in a
@@ -1549,7 +1555,7 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
 {
     const int g = 3, H = t.H, GS = 3 * H, GPW = 32 / GS;
     t.smax = smax;
-    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 2) * 128u + (unsigned)smax * 128u);
+    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 4) * 768u);
     const size_t nslot = (size_t)t.nl * t.ncw + t.novf;
     std::vector<unsigned char> blob(nslot * t.slot_bytes, 0);
     std::vector<unsigned char> steps((size_t)t.ncw * t.nlp, 0xFF);
@@ -1562,7 +1568,7 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
         float* gm = reinterpret_cast<float*>(b);
         int* go = reinterpret_cast<int*>(b + 512);
         unsigned short* off = reinterpret_cast<unsigned short*>(b + kRegLaneTab);
-        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 2) * 128);
+        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * 256);
         const auto& grp = t.chunks[c];
         for (int lane = 0; lane < 32; ++lane) {
             const int gw = lane / GS, r = (lane % GS) / H, hh = lane % H;
@@ -1594,8 +1600,8 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
                     v = (float)h.ext_v[k];
                 }
                 valid = valid && o >= 0 && o + 1 <= t.win_elems && o < 65536;
-                off[(size_t)(st >> 1) * 64 + lane * 2 + (st & 1)] = (unsigned short)o;
-                val[(size_t)st * 32 + lane] = v;
+                off[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = (unsigned short)o;
+                val[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = v;
             }
         }
         if (slot < t.nl * t.ncw) {
@@ -1633,9 +1639,9 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
 // Register capacities (steps per lane) compiled for each share count.
 int reg_smax(int H, int need)
 {
-    static const int caps2[] = {8, 12, 16}, caps1[] = {12, 24, 32}, caps4[] = {8};
+    static const int caps2[] = {8, 12, 16}, caps1[] = {12, 24}, caps4[] = {8};
     const int* c = H == 2 ? caps2 : (H == 1 ? caps1 : caps4);
-    const int n = H == 2 ? 3 : (H == 1 ? 3 : 1);
+    const int n = H == 2 ? 3 : (H == 1 ? 2 : 1);
     for (int i = 0; i < n; ++i)
         if (need <= c[i]) return c[i];
     return 0;
@@ -1683,11 +1689,42 @@ struct RegArgs {
     int nl, nlp, ncw, slot_bytes, zero_off;
 };
 
+__device__ __forceinline__ float4 nc_v4f(const void* p)
+{
+    float4 r;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(r.x), "=f"(r.y), "=f"(r.z), "=f"(r.w)
+                 : "l"(p));
+    return r;
+}
+__device__ __forceinline__ uint2 nc_v2u(const void* p)
+{
+    uint2 r;
+    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ float nc_f(const void* p)
+{
+    float r;
+    asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(r) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ int nc_i(const void* p)
+{
+    int r;
+    asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(r) : "l"(p));
+    return r;
+}
+__device__ __forceinline__ void level_barrier()
+{
+    asm volatile("bar.sync 0;" ::: "memory");
+}
+
 template <int SMAX>
 struct RegSet {
     int code;
-    unsigned off2[SMAX / 2];
-    float val[SMAX];
+    uint2 off[SMAX / 4];
+    float4 val[SMAX / 4];
     float4 gm;
     int go;
     float b;
@@ -1700,17 +1737,18 @@ __device__ __forceinline__ void reg_load(RegSet<SMAX>& S, const unsigned char* b
     S.code = code;
     if (code == 0xFF) return;
     const int stp = code & 0x3F;
-    S.gm = __ldg(reinterpret_cast<const float4*>(base) + lane);
-    S.go = __ldg(reinterpret_cast<const int*>(base + 512) + lane);
-    const unsigned* o = reinterpret_cast<const unsigned*>(base + kRegLaneTab);
-    const float* v = reinterpret_cast<const float*>(base + kRegLaneTab + (SMAX / 2) * 128);
+    S.gm = nc_v4f(base + (size_t)lane * 16);
+    S.go = nc_i(base + 512 + (size_t)lane * 4);
+    S.b = nc_f(bsrc);
+    const unsigned char* o = base + kRegLaneTab + (size_t)lane * 8;
+    const unsigned char* v = base + kRegLaneTab + (SMAX / 4) * 256 + (size_t)lane * 16;
 #pragma unroll
-    for (int k = 0; k < SMAX / 2; ++k)
-        if (2 * k < stp) S.off2[k] = __ldg(o + k * 32 + lane);
-#pragma unroll
-    for (int st = 0; st < SMAX; ++st)
-        if (st < stp) S.val[st] = __ldg(v + st * 32 + lane);
-    S.b = __ldg(bsrc);
+    for (int k = 0; k < SMAX / 4; ++k) {
+        if (4 * k < stp) {
+            S.off[k] = nc_v2u(o + (size_t)k * 256);
+            S.val[k] = nc_v4f(v + (size_t)k * 512);
+        }
+    }
 }
 
 template <int H, int SMAX, bool UPPER>
@@ -1720,13 +1758,15 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, float* win, con
     const int stp = S.code & 0x3F;
     float acc0 = 0.0f, acc1 = 0.0f;
 #pragma unroll
-    for (int st = 0; st < SMAX; ++st) {
-        if (st < stp) {
-            const unsigned w2 = S.off2[st >> 1];
-            const unsigned o = (st & 1) ? (w2 >> 16) : (w2 & 0xFFFFu);
-            const float x = win[o];
-            if (st & 1) acc1 = fmaf(S.val[st], x, acc1);
-            else acc0 = fmaf(S.val[st], x, acc0);
+    for (int k = 0; k < SMAX / 4; ++k) {
+        if (4 * k < stp) {
+            // steps past the chunk's count within this quad read the zero slot
+            const float x0 = win[S.off[k].x & 0xFFFFu], x1 = win[S.off[k].x >> 16];
+            const float x2 = win[S.off[k].y & 0xFFFFu], x3 = win[S.off[k].y >> 16];
+            acc0 = fmaf(S.val[k].x, x0, acc0);
+            acc1 = fmaf(S.val[k].y, x1, acc1);
+            acc0 = fmaf(S.val[k].z, x2, acc0);
+            acc1 = fmaf(S.val[k].w, x3, acc1);
         }
     }
     float acc = acc0 + acc1;
@@ -1788,14 +1828,14 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
     };
     load(s0, 0);
     load(s1, 1);
-    __syncthreads();  // the zero slot is set
+    level_barrier();  // the zero slot is set
     for (int l = 0; l < a.nl; l += 2) {
         if (s0.code != 0xFF) {
             reg_level<H, SMAX, UPPER>(s0, rwin, a, lane0, tb);
             if (s0.code & 0x40) reg_overflow<H, SMAX, UPPER>(a, l, rwin, rhs, warp, lane, lane0, tb);
         }
         load(s0, l + 2);
-        __syncthreads();
+        level_barrier();
         if (l + 1 < a.nl) {
             if (s1.code != 0xFF) {
                 reg_level<H, SMAX, UPPER>(s1, rwin, a, lane0, tb);
@@ -1803,7 +1843,7 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
                     reg_overflow<H, SMAX, UPPER>(a, l + 1, rwin, rhs, warp, lane, lane0, tb);
             }
             load(s1, l + 3);
-            __syncthreads();
+            level_barrier();
         }
     }
 }
@@ -1871,7 +1911,6 @@ int launch_reg_any(const IluStage& st, const double* dAinv, const float* v, floa
     if (H == 2 && smax == 16) return launch_reg<Q, 2, 16>(st, dAinv, v, z, s);
     if (H == 1 && smax == 12) return launch_reg<Q, 1, 12>(st, dAinv, v, z, s);
     if (H == 1 && smax == 24) return launch_reg<Q, 1, 24>(st, dAinv, v, z, s);
-    if (H == 1 && smax == 32) return launch_reg<Q, 1, 32>(st, dAinv, v, z, s);
     if (H == 4 && smax == 8) return launch_reg<Q, 4, 8>(st, dAinv, v, z, s);
     set_error("register sweep: no kernel for these shares and steps");
     return XT_ERR_ARG;
@@ -1958,8 +1997,12 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
 template <class T>
 StageArgs<T> stage_args(const StageTri& t, const unsigned char* rhs, T* out, int ncw, unsigned rs)
 {
+    // XTFEM_ILU_SPIN_LIMIT shortens the waits for a level's data (tests use
+    // it to make a wait run out with the GPU still answering)
+    const long long spin = env_int("XTFEM_ILU_SPIN_LIMIT", 0) > 0
+                               ? (long long)env_int("XTFEM_ILU_SPIN_LIMIT", 0) : kSpinLimit;
     return {t.blob.p, reinterpret_cast<const int4*>(t.table.p), rhs, out, t.nlevels, t.g, ncw,
-            t.window_bytes, rs, t.aux};
+            t.window_bytes, rs, t.aux, spin};
 }
 
 // Pre-pass, forward sweep kl and backward sweep ku of a staged solve; GPW

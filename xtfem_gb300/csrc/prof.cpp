@@ -26,6 +26,7 @@ struct Rec {
     int cls;
     cudaEvent_t a, b;
     bool ended;
+    double bytes;
 };
 std::mutex g_mu;
 bool g_on = false;
@@ -34,6 +35,7 @@ std::map<int, Rec> g_open;
 std::vector<cudaEvent_t> g_pool;
 long long g_count[PROF_NCLASS] = {0};
 double g_ms[PROF_NCLASS] = {0};
+double g_bytes[PROF_NCLASS] = {0};
 
 cudaEvent_t take()
 {
@@ -58,6 +60,7 @@ void settle_locked()
         if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
             g_count[r.cls] += 1;
             g_ms[r.cls] += ms;
+            g_bytes[r.cls] += r.bytes;
         }
         g_pool.push_back(r.a);
         g_pool.push_back(r.b);
@@ -78,7 +81,7 @@ int prof_begin(int cls, cudaStream_t s)
     if (!g_on) return -1;
     if (g_open.size() > 4096) settle_locked();
     const int id = g_next++ & 0x3fffffff;
-    Rec r{cls, take(), take(), false};
+    Rec r{cls, take(), take(), false, 0.0};
     cudaEventRecord(r.a, s);
     g_open[id] = r;
     return id;
@@ -94,6 +97,14 @@ void prof_end(int token, cudaStream_t s)
     it->second.ended = true;
 }
 
+void prof_bytes(int token, double bytes)
+{
+    if (token < 0) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_open.find(token);
+    if (it != g_open.end()) it->second.bytes += bytes;
+}
+
 }  // namespace xt
 
 extern "C" {
@@ -106,6 +117,7 @@ int xt_profile(int enable)
     for (int c = 0; c < xt::PROF_NCLASS; ++c) {
         xt::g_count[c] = 0;
         xt::g_ms[c] = 0.0;
+        xt::g_bytes[c] = 0.0;
     }
     return XT_OK;
 }
@@ -117,6 +129,15 @@ int xt_profile_read(int cls, long long* count, double* ms)
     std::lock_guard<std::mutex> lk(xt::g_mu);
     if (count) *count = xt::g_count[cls];
     if (ms) *ms = xt::g_ms[cls];
+    return XT_OK;
+}
+
+int xt_profile_bytes(int cls, double* bytes)
+{
+    if (cls < 0 || cls >= xt::PROF_NCLASS || !bytes) return XT_ERR_ARG;
+    xt::settle();
+    std::lock_guard<std::mutex> lk(xt::g_mu);
+    *bytes = xt::g_bytes[cls];
     return XT_OK;
 }
 

@@ -11,5 +11,8 @@ enum ProfClass { PROF_KRON64 = 0, PROF_KRON32 = 1, PROF_ILU64 = 2, PROF_ILU32 = 
 // Returns a token for prof_end, or -1 when profiling is off.
 int prof_begin(int cls, cudaStream_t s);
 void prof_end(int token, cudaStream_t s);
+// Algorithmic bytes of the timed launch (summed per class; bench.py divides
+// them by the summed time).  No-op for token -1.
+void prof_bytes(int token, double bytes);
 
 }  // namespace xt

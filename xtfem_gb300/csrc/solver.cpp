@@ -340,6 +340,9 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
             XT_TRY(apply_op<T>(S, z, col(i1 - 1)));
             // CGS2 projection against the i previous vectors
             const int otok = prof_begin(sizeof(T) == 8 ? PROF_ORTH64 : PROF_ORTH32, s);
+            // two dot passes ((i + 1) n reads each) and two updates (i + 1 reads
+            // and one write of n each)
+            prof_bytes(otok, (4.0 * i + 6.0) * (double)n * sizeof(T));
             XT_TRY(multi_dot<T>(V, n, i, col(i1 - 1), n, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
@@ -480,6 +483,8 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
                 prof_end(tok, s);
             }
             const int otok = prof_begin(PROF_ORTH64, s);
+            // as above, double-float values of 8 bytes
+            prof_bytes(otok, (4.0 * i + 6.0) * (double)nl * 8.0);
             XT_TRY(df_multi_dot(V, nl, i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
