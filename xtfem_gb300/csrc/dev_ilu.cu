@@ -1561,6 +1561,8 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
     std::vector<unsigned char> steps((size_t)t.ncw * t.nlp, 0xFF);
     std::vector<unsigned char> osteps(std::max(1, t.novf), 0);
     std::vector<int> ovf((size_t)2 * t.nl, 0);
+    std::vector<int> seen(t.win_elems, 0);
+    int epoch = 0;
     bool valid = true;
     for (size_t c = 0; c < t.chunks.size(); ++c) {
         const int l = t.chunk_level[c], slot = t.chunk_slot[c], stp = t.chunk_steps[c];
@@ -1570,12 +1572,13 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
         unsigned short* off = reinterpret_cast<unsigned short*>(b + kRegLaneTab);
         float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * 256);
         const auto& grp = t.chunks[c];
+        // each lane's entries: window offset and value
+        std::vector<std::vector<std::pair<int, float>>> ent(32);
         for (int lane = 0; lane < 32; ++lane) {
             const int gw = lane / GS, r = (lane % GS) / H, hh = lane % H;
             const bool live = gw < GPW && gw < (int)grp.size();
             int wo = -1;
             for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = 0.0f;
-            int kb = 0, ke = 0;
             if (live) {
                 const int i = grp[gw], G = h.order[i];
                 for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = (float)h.minv[(size_t)i * 9 + r * 3 + k];
@@ -1586,24 +1589,53 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
                     valid = valid && d >= 0 && d < INT32_MAX;
                     go[lane] = (int)d;
                 }
-                kb = h.ext_ptr[(size_t)i * g + r];
-                ke = h.ext_ptr[(size_t)i * g + r + 1];
+                const int kb = h.ext_ptr[(size_t)i * g + r], ke = h.ext_ptr[(size_t)i * g + r + 1];
+                for (int k = kb + hh; k < ke; k += H) {
+                    const int col = h.ext_col[k], Gc = col / g;
+                    ent[lane].push_back({h.slot[Gc] * g + (col - Gc * g), (float)h.ext_v[k]});
+                }
             }
             std::memcpy(&gm[lane * 4 + 3], &wo, 4);
-            for (int st = 0; st < smax; ++st) {
-                const int k = kb + hh + st * H;
+        }
+        // Step assignment: a row's entries may be summed in any order, so at
+        // every step each lane takes, of its remaining entries, one whose
+        // shared-memory bank the warp's reads of that step use least (an
+        // address another lane already reads is a broadcast and costs
+        // nothing); lanes with more entries left choose first.  Lanes with
+        // none left read the zero slot.
+        std::vector<int> lanes(32);
+        const bool banks = env_int("XTFEM_ILU_BANKS", 1) != 0;  // 0: entries in row order
+        for (int st = 0; st < smax; ++st) {
+            int load[32] = {0};
+            ++epoch;  // seen[a] == epoch: address a is read at this step already
+            for (int l2 = 0; l2 < 32; ++l2) lanes[l2] = l2;
+            std::stable_sort(lanes.begin(), lanes.end(),
+                             [&](int a, int b) { return ent[a].size() > ent[b].size(); });
+            for (int lane : lanes) {
                 int o = t.zero_off;
                 float v = 0.0f;
-                if (live && k < ke) {
-                    const int col = h.ext_col[k], Gc = col / g;
-                    o = h.slot[Gc] * g + (col - Gc * g);
-                    v = (float)h.ext_v[k];
+                if (!ent[lane].empty()) {
+                    size_t best = 0;
+                    int bcost = 1 << 30;
+                    for (size_t e = 0; banks && e < ent[lane].size(); ++e) {
+                        const int a = ent[lane][e].first;
+                        const int cost = seen[a] == epoch ? 0 : load[a & 31] + 1;
+                        if (cost < bcost) { bcost = cost; best = e; }
+                    }
+                    o = ent[lane][best].first;
+                    v = ent[lane][best].second;
+                    ent[lane].erase(ent[lane].begin() + best);
                 }
                 valid = valid && o >= 0 && o + 1 <= t.win_elems && o < 65536;
+                if (valid && seen[o] != epoch) {
+                    seen[o] = epoch;
+                    load[o & 31]++;
+                }
                 off[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = (unsigned short)o;
                 val[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = v;
             }
         }
+        for (int lane = 0; lane < 32; ++lane) valid = valid && ent[lane].empty();
         if (slot < t.nl * t.ncw) {
             steps[(size_t)(slot % t.ncw) * t.nlp + l] = (unsigned char)stp;
         } else {
@@ -1942,7 +1974,9 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
     const int wenv = col ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
     const int rkb = std::max(0, std::min(255, env_int("XTFEM_ILU_RING_KB", 0)));
     const bool hkey = col || fmt == 4;
-    const int wkey = (col || fmt == 4) ? std::max(0, std::min(63, env_int("XTFEM_ILU_WARPS", 0))) : 0;
+    const int wkey = (col || fmt == 4) ? std::max(0, std::min(31, env_int("XTFEM_ILU_WARPS", 0))) +
+                                             (fmt == 4 && env_int("XTFEM_ILU_BANKS", 1) == 0 ? 32 : 0)
+                                       : 0;
     const int key =
         ((((q * 8 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 8 + (hkey ? H : 0)) * 64 + wkey) * 256 + rkb;
     (void)wenv;
