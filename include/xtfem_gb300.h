@@ -210,7 +210,9 @@ int xt_system_gmres(xt_system s, const double *rhs, double *sol, int im,
  * factor and Krylov basis (FP64 dot products and Hessenberg) inside FP64
  * iterative refinement, 2 runs flexible GMRES with the FP32 factor and a
  * double-float (FP32 pair) basis and operator on the preconditioned
- * vectors.  out_stats (may be NULL) gets 6 values: iterations, cycles,
+ * vectors, 3 runs mode 1 with K and M of the inner operator stored in BF16
+ * (rounded to nearest, widened to FP32 and accumulated in FP32; the
+ * BF16-stored experiment).  out_stats (may be NULL) gets 6 values: iterations, cycles,
  * refinement passes, ierr, true relative residual, last estimate. */
 int xt_system_solve(xt_system s, const double *rhs, double *sol, int im,
                     double tol, int maxits, int precision, double inner_tol,

@@ -1,8 +1,9 @@
 """The holed panel (the generated stand-in for the reference's missing
-thin-panel mesh) in a coupled thermo-mechanical run: the plain FP64 loop and
-the mixed-precision loop give the same temperatures (1e-6) and displacements
-(1e-5, the thin panel being badly conditioned), slab by slab, and the
-heating acts."""
+thin-panel mesh) in a coupled thermo-mechanical run: the plain FP64 loop,
+the mixed-precision loop and the FP32 loop with BF16-stored K and M (all
+three under FP64 refinement) give the same temperatures (1e-6) and
+displacements (1e-5, the thin panel being badly conditioned), slab by
+slab, and the heating acts."""
 import numpy as np
 import pytest
 
@@ -35,9 +36,10 @@ def run(xt, precision):
     return out
 
 
-def test_coupled_panel_fp64_and_mixed_agree(xt):
+@pytest.mark.parametrize("precision", [2, 1, 3])
+def test_coupled_panel_modes_agree_with_fp64(xt, precision):
     ref = run(xt, 0)
-    mix = run(xt, 2)
+    mix = run(xt, precision)
     for k in range(NSLAB):
         assert ref[k][0]["relres"] <= 1e-9 and mix[k][0]["relres"] <= 1e-9
         assert np.linalg.norm(mix[k][1] - ref[k][1]) <= 1e-6 * np.linalg.norm(ref[k][1]), k

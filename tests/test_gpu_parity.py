@@ -200,7 +200,7 @@ def test_gmres_iteration_history_tracks_oracle(xt, orc, rod_system):
     sysm.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1, 2])
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
 def test_refined_solve_reaches_true_residual(xt, orc, rod_system, precision):
     s = rod_system
     rhs = c1_rhs(xt, s)

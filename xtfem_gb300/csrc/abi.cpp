@@ -332,7 +332,7 @@ static int system_solve_host(xt_system h, const double* rhs, double* sol, int im
                              int maxits, int precision, double inner_tol, double* out_stats)
 {
     if (!h || !rhs || !sol) { set_error("xt_system_solve: null argument"); return XT_ERR_ARG; }
-    if (precision < 0 || precision > 2) { set_error("xt_system_solve: precision is 0, 1 or 2"); return XT_ERR_ARG; }
+    if (precision < 0 || precision > 3) { set_error("xt_system_solve: precision is 0, 1, 2 or 3"); return XT_ERR_ARG; }
     System& S = h->sys;
     XT_TRY(system_stream(S));
     const size_t n = (size_t)S.p * S.q;

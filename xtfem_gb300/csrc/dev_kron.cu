@@ -22,6 +22,8 @@
 #include <vector>
 
 #include "df.cuh"
+#include <cuda_bf16.h>
+
 #include "xt_device.h"
 
 namespace xt {
@@ -73,11 +75,16 @@ const double* vals<double>(const double* v64, const float*) { return v64; }
 template <>
 const float* vals<float>(const double*, const float* v32) { return v32; }
 
-template <class T, int Q, int LANES, bool MERGED>
+// stored value -> arithmetic type (BF16 values widen exactly to FP32)
+template <class T>
+__device__ __forceinline__ T widen(T v) { return v; }
+__device__ __forceinline__ float widen(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <class T, int Q, int LANES, bool MERGED, class V = T>
 __global__ void __launch_bounds__(256)
 k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
-            const T* __restrict__ kval, const int* __restrict__ mptr,
-            const int* __restrict__ mcol, const T* __restrict__ mval,
+            const V* __restrict__ kval, const int* __restrict__ mptr,
+            const int* __restrict__ mcol, const V* __restrict__ mval,
             const double* __restrict__ dA, const double* __restrict__ dB, T alpha, T beta,
             const T* __restrict__ x, T* __restrict__ y)
 {
@@ -104,7 +111,7 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
         if constexpr (MERGED) {  // one pattern: one index and one X row for both
 #pragma unroll 4
             for (int k = k0 + lane; k < k1; k += LANES) {
-                const T vk = kval[k], vm = mval[k];
+                const T vk = widen(kval[k]), vm = widen(mval[k]);
                 T xr[Q];
                 load_row<T, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
@@ -116,7 +123,7 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
         } else {
 #pragma unroll 4
             for (int k = k0 + lane; k < k1; k += LANES) {
-                const T v = kval[k];
+                const T v = widen(kval[k]);
                 T xr[Q];
                 load_row<T, Q>(x + (size_t)kcol[k] * Q, xr);
 #pragma unroll
@@ -125,7 +132,7 @@ k_kron_spmm(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
             const int m0 = act ? mptr[r] : 0, m1 = act ? mptr[r + 1] : 0;
 #pragma unroll 4
             for (int k = m0 + lane; k < m1; k += LANES) {
-                const T v = mval[k];
+                const T v = widen(mval[k]);
                 T xr[Q];
                 load_row<T, Q>(x + (size_t)mcol[k] * Q, xr);
 #pragma unroll
@@ -403,6 +410,47 @@ int launch_df(const DevCsr& K, const DevCsr& M, const double* dA, const double* 
     return XT_OK;
 }
 
+__global__ void k_to_bf16(const double* __restrict__ a, __nv_bfloat16* __restrict__ b, size_t n)
+{
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (; i < n; i += stride) b[i] = __double2bfloat16(a[i]);  // round to nearest even
+}
+
+int ensure_bf16(DevCsr& A, cudaStream_t s)
+{
+    if (A.v16.p && A.v16.n == (size_t)A.nnz) return XT_OK;
+    XT_TRY(A.v16.alloc((size_t)A.nnz));
+    if (A.nnz) {
+        k_to_bf16<<<1024, 256, 0, s>>>(A.v64.p, A.v16.p, (size_t)A.nnz);
+        note_launches(1);
+        XT_CUDA(cudaGetLastError());
+    }
+    return XT_OK;
+}
+
+template <int Q>
+int launch_bf16(const DevCsr& K, const DevCsr& M, const double* dA, const double* dB,
+                double alpha, double beta, const float* x, float* y, cudaStream_t s)
+{
+    constexpr int LANES = 8;
+    const int threads = 256;
+    const int rows_per_block = threads / LANES;
+    int blocks = (K.n + rows_per_block - 1) / rows_per_block;
+    if (blocks < 1) blocks = 1;
+    if (M.same_pattern && M.nnz == K.nnz)
+        k_kron_spmm<float, Q, LANES, true, __nv_bfloat16><<<blocks, threads, 0, s>>>(
+            K.n, K.rowptr.p, K.col.p, K.v16.p, M.rowptr.p, M.col.p, M.v16.p, dA, dB,
+            (float)alpha, (float)beta, x, y);
+    else
+        k_kron_spmm<float, Q, LANES, false, __nv_bfloat16><<<blocks, threads, 0, s>>>(
+            K.n, K.rowptr.p, K.col.p, K.v16.p, M.rowptr.p, M.col.p, M.v16.p, dA, dB,
+            (float)alpha, (float)beta, x, y);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
 int ensure_df(DevCsr& A, cudaStream_t s)
 {
     if (A.vdf.p && A.vdf.n == (size_t)A.nnz) return XT_OK;
@@ -634,6 +682,28 @@ int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB
     case 6: return launch_df<6>(K, M, dA, dB, x, y, s);
     case 7: return launch_df<7>(K, M, dA, dB, x, y, s);
     default: return launch_df<8>(K, M, dA, dB, x, y, s);
+    }
+}
+
+int kron_spmm_bf16(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB,
+                   double alpha, double beta, const float* x, float* y, cudaStream_t s)
+{
+    if (K.n != M.n || q < 1 || q > 8) {
+        set_error("kron_spmm_bf16: K and M must have the same order and 1 <= q <= 8");
+        return XT_ERR_ARG;
+    }
+    if (K.n == 0) return XT_OK;
+    XT_TRY(ensure_bf16(K, s));
+    XT_TRY(ensure_bf16(M, s));
+    switch (q) {
+    case 1: return launch_bf16<1>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 2: return launch_bf16<2>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 3: return launch_bf16<3>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 4: return launch_bf16<4>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 5: return launch_bf16<5>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 6: return launch_bf16<6>(K, M, dA, dB, alpha, beta, x, y, s);
+    case 7: return launch_bf16<7>(K, M, dA, dB, alpha, beta, x, y, s);
+    default: return launch_bf16<8>(K, M, dA, dB, alpha, beta, x, y, s);
     }
 }
 

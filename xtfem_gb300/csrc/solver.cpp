@@ -260,11 +260,23 @@ struct Ws<float> {
     static float* u(System& S) { return S.u32.p; }
 };
 
+// The FP32 inner operator reads K and M as FP32, or as BF16 when S.op16
+// (precision mode 3); both accumulate in FP32.
+template <class T>
+int kron_inner(System& S, double alpha, double beta, const T* x, T* y)
+{
+    if constexpr (sizeof(T) == 4) {
+        if (S.op16)
+            return kron_spmm_bf16(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, S.stream);
+    }
+    return kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, S.stream);
+}
+
 template <class T>
 int apply_op(System& S, const T* x, T* y)
 {
     const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, S.stream);
-    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, 1.0, 0.0, x, y, S.stream);
+    const int st = kron_inner<T>(S, 1.0, 0.0, x, y);
     prof_end(tok, S.stream);
     return st;
 }
@@ -273,7 +285,7 @@ template <class T>
 int apply_op_ab(System& S, double alpha, double beta, const T* x, T* y)
 {
     const int tok = prof_begin(sizeof(T) == 8 ? PROF_KRON64 : PROF_KRON32, S.stream);
-    const int st = kron_spmm<T>(S.K, S.M, S.q, S.A.p, S.B.p, alpha, beta, x, y, S.stream);
+    const int st = kron_inner<T>(S, alpha, beta, x, y);
     prof_end(tok, S.stream);
     return st;
 }
@@ -572,6 +584,14 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
     XT_TRY(system_stream(S));
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
+    // mode 3 is mode 1 with the inner operator's K and M stored in BF16
+    const bool bf16 = inner == 3;
+    if (bf16) inner = 1;
+    struct Op16 {
+        System& S;
+        ~Op16() { S.op16 = false; }
+    } op16_reset{S};
+    S.op16 = bf16;
     XT_TRY(ensure_workspace(S, im, inner == 1, inner == 2));
     double hb[2];
     XT_TRY(norm2<double>(b, n, S.red, s));

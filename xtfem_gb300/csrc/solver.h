@@ -40,6 +40,7 @@ struct System {
     DBuf<int> bcmask;                 // p entries (0/1), optional
     // GMRES workspace
     int im_cap = 0;
+    bool op16 = false;  // FP32 inner operator reads BF16-stored K and M (mode 3)
     DBuf<double> V64, z64, w64, u64;
     DBuf<float> V32, z32, w32, u32, d32, r32;
     DBuf<float> Z32;  // flexible GMRES: preconditioned basis, im columns

@@ -210,7 +210,7 @@ int xt_thermal_create(xth_problem pr, const xt_thermal_config* cfg, xt_thermal* 
     if (!pr || !cfg || !out) { set_error("xt_thermal_create: null argument"); return XT_ERR_ARG; }
     *out = nullptr;
     if (cfg->fixed_axis < 0 || cfg->fixed_axis > 2 || cfg->flux_axis < 0 || cfg->flux_axis > 2 ||
-        cfg->n1 <= 0 || cfg->dt0 <= 0 || cfg->im <= 0 || cfg->precision < 0 || cfg->precision > 2) {
+        cfg->n1 <= 0 || cfg->dt0 <= 0 || cfg->im <= 0 || cfg->precision < 0 || cfg->precision > 3) {
         set_error("xt_thermal_create: bad configuration");
         return XT_ERR_ARG;
     }

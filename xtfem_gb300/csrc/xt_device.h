@@ -8,6 +8,7 @@
 // k at k*p + r, src/kronecker.f90:64) is converted at the C-ABI boundary.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "../../include/xtfem_gb300.h"
@@ -116,6 +117,7 @@ struct DevCsr {
     DBuf<double> v64;
     DBuf<float> v32;
     DBuf<float2> vdf;  // double-float (hi, lo) copy, made on first use
+    DBuf<__nv_bfloat16> v16;  // BF16 copy (round to nearest), made on first use
     // set on M when its pattern equals K's (same mesh): the Kronecker
     // kernels then read one column index and one X row per nonzero for both
     bool same_pattern = false;
@@ -158,6 +160,11 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 // values on first use.
 int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,
                  float2* y, cudaStream_t s);
+
+// The same operator with K and M stored in BF16, FP32 vectors and FP32
+// accumulation (the BF16-stored experiment of precision mode 3).
+int kron_spmm_bf16(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB,
+                   double alpha, double beta, const float* x, float* y, cudaStream_t s);
 
 // -------------------------------------------------- ILU triangular solves
 // Level-scheduled form of a SPARSKIT MSR factor.  Rows are handled in groups
