@@ -1437,46 +1437,47 @@ __global__ void __launch_bounds__(kStageThreads, 1) k_tri_col(StageArgs<float> a
 // data never passes through shared memory.  Shared memory holds only the
 // solution window (3 rows x 1 value per slot); every record of a level is
 // loaded from global memory (L2) straight into registers two levels ahead
-// of its use, so a level's critical path is: window reads at offsets
+// of its use, so a level's critical path is: window reads at byte offsets
 // already in registers, one multiply-add per factor entry, the share and
-// diagonal-block shuffles, the window store and one block barrier.
+// diagonal-block shuffles, the window store and one block barrier.  A level
+// has no branch: every warp has a fixed-size slot at every level.
 //
 // Layout.  Lane = (group of the warp's chunk, row r of the group, share h
-// of the row's entries, H shares): lanes g*3H + r*H + h; a lane takes the
-// row's off-diagonal entries h, h+H, h+2H, ... (one per step).  The groups
-// of a level are sorted by their longest row and dealt to chunks of
-// 32/(3H) groups; chunk w < ncw of level l sits at the fixed slot
-// l*ncw + w (a level's chunks beyond ncw go to an overflow area, processed
-// by the same warps in extra passes).  A slot holds, per lane:
+// of the row's entries, H shares): lanes g*3H + r*H + h; a lane owns a
+// share of the row's off-diagonal entries, one per step, SMAX steps (a
+// multiple of 4; entries past the lane's own read an all-zero window slot
+// with value 0).  The groups of a level are sorted by their longest row
+// and dealt to chunks of 32/(3H) groups; a level with more chunks than the
+// ncw warps is split into consecutive sub-levels (its groups are
+// independent).  Chunk w of (sub-)level l sits in the fixed slot l*ncw + w;
+// warps without a chunk at a level get an empty slot.  A slot holds, per
+// lane (loads of 16 bytes, consecutive lanes adjacent):
 //   float4 {minv[r][0..2] (row r of the inverted 3 x 3 diagonal block),
 //           window offset of the row (-1: lane stores nothing)}   512 B
 //   int    destination (forward: the backward sweep's right-hand-side
 //          slot of the row; backward: row * Q of z)               128 B
-//   u16 x 4 window offsets of steps 4k..4k+3                     SMAX/4 x 256 B
+//   uint4  byte offsets in the window of steps 4k..4k+3          SMAX/4 x 512 B
 //   float4 factor values of steps 4k..4k+3                       SMAX/4 x 512 B
-// The loads are inline-PTX non-coherent loads (volatile, so they are
-// issued where they stand: two levels before their use, not sunk to it),
-// and the level barrier is a volatile bar.sync that they do not cross.
-// Missing entries point at an all-zero window slot with value 0.  A byte
-// table per warp gives the steps of each level's chunk (0xFF: none; bit
-// 0x40: the level has overflow chunks); a warp keeps 32 levels of it in a
-// register and reads it by shuffle.  The right-hand sides are
-// per-temporal-block arrays in the same lane-slot order (the forward
-// sweep's from a pre-pass that also applies the q x q mixing with A^-1; the
-// backward sweep's written by the forward sweep), so every load of a level
-// has an address known in advance.
+// The right-hand sides are per-temporal-block arrays in the same lane-slot
+// order (the forward sweep's from a pre-pass that also applies the q x q
+// mixing with A^-1; the backward sweep's written by the forward sweep), so
+// every load of a level has an address known in advance.  The loads are
+// inline-PTX non-coherent loads (volatile, so they are issued where they
+// stand, two levels before their use), and the level barrier is a
+// volatile bar.sync that they do not cross.  A row's entries are summed in
+// a step order chosen on the host so that a warp's window reads of one
+// step fall into distinct shared-memory banks where possible.
 constexpr int kRegMaxWarps = 16;
 constexpr unsigned kRegLaneTab = 640;
 
 struct RegTri {
-    int nl = 0, nlp = 0, ncw = 0, H = 0, smax = 0, novf = 0, slot_bytes = 0;
+    int nl = 0, ncw = 0, H = 0, smax = 0, slot_bytes = 0;
     int win_elems = 0, zero_off = 0;
-    long long lanes = 0;  // (nl * ncw + novf) * 32
-    DBuf<unsigned char> slots, steps, ovf_steps;
-    DBuf<int> ovf;                 // per level {chunks, first overflow chunk}
-    std::vector<int> row_slot;     // host: lane slot of each row's h = 0 lane
+    long long lanes = 0;  // nl * ncw * 32
+    DBuf<unsigned char> slots;
+    std::vector<int> row_slot;             // host: lane slot of each row's h = 0 lane
     std::vector<std::vector<int>> chunks;  // host (build only): level-order groups per chunk
-    std::vector<int> chunk_level, chunk_slot, chunk_steps;
+    std::vector<int> chunk_slot, chunk_steps;
 };
 
 namespace {
@@ -1487,41 +1488,37 @@ int reg_warps(const TriHost& h, int GPW)
     for (int l = 0; l < h.nlevels; ++l)
         nch.push_back((h.level_ptr[l + 1] - h.level_ptr[l] + GPW - 1) / GPW);
     std::sort(nch.begin(), nch.end());
-    const int p97 = nch[(size_t)(0.97 * (nch.size() - 1))];
-    const int w = env_int("XTFEM_ILU_WARPS", p97);
+    const int p90 = nch[(size_t)(0.90 * (nch.size() - 1))];
+    const int w = env_int("XTFEM_ILU_WARPS", p90);
     return std::max(1, std::min(kRegMaxWarps, w));
 }
 
-// Chunks, slots and steps of one triangle (no device data yet).
+// Chunks, sub-levels, slots and steps of one triangle (no device data yet).
 bool reg_plan(const TriHost& h, int H, RegTri& t)
 {
-    const int g = 3, GS = 3 * H, GPW = 32 / GS, nl = h.nlevels;
-    t.nl = nl;
+    const int g = 3, GS = 3 * H, GPW = 32 / GS;
     t.H = H;
     t.ncw = reg_warps(h, GPW);
     t.row_slot.assign((size_t)h.ngroups * g, -1);
     t.chunks.clear();
-    t.chunk_level.clear();
     t.chunk_slot.clear();
     t.chunk_steps.clear();
-    int novf = 0, smax = 0;
+    int nl = 0, smax = 0;
     std::vector<int> ord;
-    for (int l = 0; l < nl; ++l) {
+    auto rowlen = [&](int i, int r) {
+        return h.ext_ptr[(size_t)i * g + r + 1] - h.ext_ptr[(size_t)i * g + r];
+    };
+    auto longest = [&](int i) { return std::max(rowlen(i, 0), std::max(rowlen(i, 1), rowlen(i, 2))); };
+    for (int l = 0; l < h.nlevels; ++l) {
         const int gb = h.level_ptr[l], ng = h.level_ptr[l + 1] - gb;
         ord.resize(ng);
-        auto rowlen = [&](int i, int r) {
-            return h.ext_ptr[(size_t)i * g + r + 1] - h.ext_ptr[(size_t)i * g + r];
-        };
-        auto longest = [&](int i) {
-            return std::max(rowlen(i, 0), std::max(rowlen(i, 1), rowlen(i, 2)));
-        };
         for (int j = 0; j < ng; ++j) ord[j] = gb + j;
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return longest(a) > longest(b); });
         const int nch = (ng + GPW - 1) / GPW;
         for (int c = 0; c < nch; ++c) {
+            if (c % t.ncw == 0) ++nl;  // a new (sub-)level every ncw chunks
             std::vector<int> grp(ord.begin() + c * GPW, ord.begin() + std::min(ng, (c + 1) * GPW));
-            const long long slot = c < t.ncw ? (long long)l * t.ncw + c
-                                             : (long long)nl * t.ncw + novf++;
+            const long long slot = (long long)(nl - 1) * t.ncw + c % t.ncw;
             int steps = 0;
             for (int gw = 0; gw < (int)grp.size(); ++gw) {
                 const int i = grp[gw], G = h.order[i];
@@ -1533,84 +1530,80 @@ bool reg_plan(const TriHost& h, int H, RegTri& t)
             if (slot * 32 + 31 >= INT32_MAX) return false;
             smax = std::max(smax, steps);
             t.chunks.push_back(std::move(grp));
-            t.chunk_level.push_back(l);
             t.chunk_slot.push_back((int)slot);
             t.chunk_steps.push_back(steps);
         }
     }
-    t.novf = novf;
-    t.smax = smax;
-    t.lanes = ((long long)nl * t.ncw + novf) * 32;
-    t.nlp = ((nl + 31) / 32 + 1) * 32;
+    t.nl = nl;
+    t.smax = (smax + 3) / 4 * 4;
+    t.lanes = (long long)nl * t.ncw * 32;
     t.zero_off = h.nslots * g;
     t.win_elems = (h.nslots + 1) * g;
-    return smax < 0x40 && t.win_elems <= 65536 &&
-           (long long)t.win_elems * 4 <= (long long)max_dyn_smem();
+    return t.smax <= 32 && (long long)t.win_elems * 4 <= (long long)max_dyn_smem();
 }
 
-// Slots and tables of a planned triangle.  dst: forward, the other
-// triangle's row_slot; backward (dst empty): row * Q.
+// Slots of a planned triangle.  dst: forward, the other triangle's
+// row_slot; backward (dst empty): row * Q.
 int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int>* dst,
              cudaStream_t s)
 {
     const int g = 3, H = t.H, GS = 3 * H, GPW = 32 / GS;
     t.smax = smax;
-    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 4) * 768u);
-    const size_t nslot = (size_t)t.nl * t.ncw + t.novf;
+    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 4) * 1024u);
+    const size_t nslot = (size_t)t.nl * t.ncw;
     std::vector<unsigned char> blob(nslot * t.slot_bytes, 0);
-    std::vector<unsigned char> steps((size_t)t.ncw * t.nlp, 0xFF);
-    std::vector<unsigned char> osteps(std::max(1, t.novf), 0);
-    std::vector<int> ovf((size_t)2 * t.nl, 0);
+    // every lane of every slot starts empty: no store, all steps on the zero slot
+    for (size_t sl = 0; sl < nslot; ++sl) {
+        unsigned char* b = blob.data() + sl * t.slot_bytes;
+        const int none = -1;
+        unsigned* off = reinterpret_cast<unsigned*>(b + kRegLaneTab);
+        for (int lane = 0; lane < 32; ++lane) std::memcpy(b + lane * 16 + 12, &none, 4);
+        for (int e = 0; e < (smax / 4) * 128; ++e) off[e] = (unsigned)t.zero_off * 4u;
+    }
     std::vector<int> seen(t.win_elems, 0);
     int epoch = 0;
     bool valid = true;
+    const bool banks = env_int("XTFEM_ILU_BANKS", 1) != 0;  // 0: entries in row order
+    std::vector<std::vector<std::pair<int, float>>> ent(32);
+    std::vector<int> lanes(32);
     for (size_t c = 0; c < t.chunks.size(); ++c) {
-        const int l = t.chunk_level[c], slot = t.chunk_slot[c], stp = t.chunk_steps[c];
+        const int slot = t.chunk_slot[c];
         unsigned char* b = blob.data() + (size_t)slot * t.slot_bytes;
         float* gm = reinterpret_cast<float*>(b);
         int* go = reinterpret_cast<int*>(b + 512);
-        unsigned short* off = reinterpret_cast<unsigned short*>(b + kRegLaneTab);
-        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * 256);
+        unsigned* off = reinterpret_cast<unsigned*>(b + kRegLaneTab);
+        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * 512);
         const auto& grp = t.chunks[c];
-        // each lane's entries: window offset and value
-        std::vector<std::vector<std::pair<int, float>>> ent(32);
         for (int lane = 0; lane < 32; ++lane) {
+            ent[lane].clear();
             const int gw = lane / GS, r = (lane % GS) / H, hh = lane % H;
-            const bool live = gw < GPW && gw < (int)grp.size();
-            int wo = -1;
-            for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = 0.0f;
-            if (live) {
-                const int i = grp[gw], G = h.order[i];
-                for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = (float)h.minv[(size_t)i * 9 + r * 3 + k];
-                if (hh == 0) {
-                    wo = h.slot[G] * g + r;
-                    const long long d = dst ? (long long)(*dst)[(size_t)G * g + r]
-                                            : ((long long)G * g + r) * Q;
-                    valid = valid && d >= 0 && d < INT32_MAX;
-                    go[lane] = (int)d;
-                }
-                const int kb = h.ext_ptr[(size_t)i * g + r], ke = h.ext_ptr[(size_t)i * g + r + 1];
-                for (int k = kb + hh; k < ke; k += H) {
-                    const int col = h.ext_col[k], Gc = col / g;
-                    ent[lane].push_back({h.slot[Gc] * g + (col - Gc * g), (float)h.ext_v[k]});
-                }
+            if (gw >= GPW || gw >= (int)grp.size()) continue;
+            const int i = grp[gw], G = h.order[i];
+            for (int k = 0; k < 3; ++k) gm[lane * 4 + k] = (float)h.minv[(size_t)i * 9 + r * 3 + k];
+            if (hh == 0) {
+                const int wo = h.slot[G] * g + r;
+                std::memcpy(&gm[lane * 4 + 3], &wo, 4);
+                const long long d = dst ? (long long)(*dst)[(size_t)G * g + r]
+                                        : ((long long)G * g + r) * Q;
+                valid = valid && wo >= 0 && wo < t.zero_off && d >= 0 && d < INT32_MAX;
+                go[lane] = (int)d;
             }
-            std::memcpy(&gm[lane * 4 + 3], &wo, 4);
+            const int kb = h.ext_ptr[(size_t)i * g + r], ke = h.ext_ptr[(size_t)i * g + r + 1];
+            for (int k = kb + hh; k < ke; k += H) {
+                const int col = h.ext_col[k], Gc = col / g;
+                ent[lane].push_back({h.slot[Gc] * g + (col - Gc * g), (float)h.ext_v[k]});
+            }
         }
-        // Step assignment: a row's entries may be summed in any order, so at
-        // every step each lane takes, of its remaining entries, one whose
-        // shared-memory bank the warp's reads of that step use least (an
-        // address another lane already reads is a broadcast and costs
-        // nothing); lanes with more entries left choose first.  Lanes with
-        // none left read the zero slot.
-        std::vector<int> lanes(32);
-        const bool banks = env_int("XTFEM_ILU_BANKS", 1) != 0;  // 0: entries in row order
+        // Step order: at every step each lane takes, of its remaining
+        // entries, one whose shared-memory bank the warp's reads of that step
+        // use least (an address another lane already reads is a broadcast
+        // and costs nothing); lanes with more entries left choose first.
         for (int st = 0; st < smax; ++st) {
             int load[32] = {0};
-            ++epoch;  // seen[a] == epoch: address a is read at this step already
+            ++epoch;
             for (int l2 = 0; l2 < 32; ++l2) lanes[l2] = l2;
             std::stable_sort(lanes.begin(), lanes.end(),
-                             [&](int a, int b) { return ent[a].size() > ent[b].size(); });
+                             [&](int a, int b2) { return ent[a].size() > ent[b2].size(); });
             for (int lane : lanes) {
                 int o = t.zero_off;
                 float v = 0.0f;
@@ -1626,42 +1619,19 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
                     v = ent[lane][best].second;
                     ent[lane].erase(ent[lane].begin() + best);
                 }
-                valid = valid && o >= 0 && o + 1 <= t.win_elems && o < 65536;
+                valid = valid && o >= 0 && o < t.win_elems;
                 if (valid && seen[o] != epoch) {
                     seen[o] = epoch;
                     load[o & 31]++;
                 }
-                off[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = (unsigned short)o;
+                off[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = (unsigned)o * 4u;
                 val[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = v;
             }
         }
         for (int lane = 0; lane < 32; ++lane) valid = valid && ent[lane].empty();
-        if (slot < t.nl * t.ncw) {
-            steps[(size_t)(slot % t.ncw) * t.nlp + l] = (unsigned char)stp;
-        } else {
-            osteps[slot - t.nl * t.ncw] = (unsigned char)stp;
-        }
-    }
-    // levels with overflow chunks: flag every warp's entry, record the list
-    {
-        int oi = 0;
-        std::vector<int> nch(t.nl, 0);
-        for (size_t c = 0; c < t.chunks.size(); ++c) nch[t.chunk_level[c]]++;
-        for (int l = 0; l < t.nl; ++l) {
-            ovf[2 * l] = nch[l];
-            ovf[2 * l + 1] = oi;
-            if (nch[l] > t.ncw) {
-                oi += nch[l] - t.ncw;
-                for (int w = 0; w < t.ncw; ++w) steps[(size_t)w * t.nlp + l] |= 0x40;
-            }
-        }
-        valid = valid && oi == t.novf;
     }
     if (!valid) return XT_OK;
     XT_TRY(t.slots.upload(blob.data(), blob.size(), s));
-    XT_TRY(t.steps.upload(steps.data(), steps.size(), s));
-    XT_TRY(t.ovf_steps.upload(osteps.data(), osteps.size(), s));
-    XT_TRY(t.ovf.upload(ovf.data(), ovf.size(), s));
     XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     t.chunks.clear();
     t.chunks.shrink_to_fit();
@@ -1671,7 +1641,7 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
 // Register capacities (steps per lane) compiled for each share count.
 int reg_smax(int H, int need)
 {
-    static const int caps2[] = {8, 12, 16}, caps1[] = {12, 24}, caps4[] = {8};
+    static const int caps2[] = {8, 12, 16}, caps1[] = {12, 20}, caps4[] = {8};
     const int* c = H == 2 ? caps2 : (H == 1 ? caps1 : caps4);
     const int n = H == 2 ? 3 : (H == 1 ? 2 : 1);
     for (int i = 0; i < n; ++i)
@@ -1696,14 +1666,14 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
     XT_TRY(st.rrhsL.alloc((size_t)Q * L->lanes));
     XT_TRY(st.rrhsU.alloc((size_t)Q * U->lanes));
     // slots the forward sweep never writes are read (not used) by the
-    // backward sweep's padding lanes: keep them finite
+    // backward sweep's other lanes: keep them finite
     XT_CUDA(cudaMemsetAsync(st.rrhsU.p, 0, sizeof(float) * Q * U->lanes, s));
     XT_CUDA(cudaStreamSynchronize(s));
     L->row_slot.clear();
     U->row_slot.clear();
     if (trace_on())
-        std::fprintf(stderr, "[xtfem] register sweep: H %d, steps %d, warps %d/%d, overflow chunks %d/%d\n",
-                     H, smax, L->ncw, U->ncw, L->novf, U->novf);
+        std::fprintf(stderr, "[xtfem] register sweep: H %d, steps %d, warps %d/%d, levels %d/%d\n",
+                     H, smax, L->ncw, U->ncw, L->nl, U->nl);
     st.regL = L;
     st.regU = U;
     st.reg_ok = true;
@@ -1712,13 +1682,10 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
 
 struct RegArgs {
     const unsigned char* slots;
-    const unsigned char* steps;
-    const int2* ovf;
-    const unsigned char* ovf_steps;
     const float* rhs;      // [Q][rstride] right-hand sides in lane-slot order
     float* out;            // forward: the backward sweep's rhs; backward: z
     long long rstride, ostride;
-    int nl, nlp, ncw, slot_bytes, zero_off;
+    int nl, ncw, slot_bytes, zero_off;
 };
 
 __device__ __forceinline__ float4 nc_v4f(const void* p)
@@ -1729,10 +1696,12 @@ __device__ __forceinline__ float4 nc_v4f(const void* p)
                  : "l"(p));
     return r;
 }
-__device__ __forceinline__ uint2 nc_v2u(const void* p)
+__device__ __forceinline__ uint4 nc_v4u(const void* p)
 {
-    uint2 r;
-    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+    uint4 r;
+    asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r.x), "=r"(r.y), "=r"(r.z), "=r"(r.w)
+                 : "l"(p));
     return r;
 }
 __device__ __forceinline__ float nc_f(const void* p)
@@ -1747,6 +1716,12 @@ __device__ __forceinline__ int nc_i(const void* p)
     asm volatile("ld.global.nc.s32 %0, [%1];" : "=r"(r) : "l"(p));
     return r;
 }
+__device__ __forceinline__ float lds_f(unsigned addr)
+{
+    float r;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(addr));
+    return r;
+}
 __device__ __forceinline__ void level_barrier()
 {
     asm volatile("bar.sync 0;" ::: "memory");
@@ -1754,52 +1729,42 @@ __device__ __forceinline__ void level_barrier()
 
 template <int SMAX>
 struct RegSet {
-    int code;
-    uint2 off[SMAX / 4];
+    uint4 off[SMAX / 4];
     float4 val[SMAX / 4];
     float4 gm;
     int go;
     float b;
 };
 
+// The slot at p (already offset to this warp's slot of the level) and the
+// right-hand side at bsrc.
 template <int SMAX>
-__device__ __forceinline__ void reg_load(RegSet<SMAX>& S, const unsigned char* base, int code,
+__device__ __forceinline__ void reg_load(RegSet<SMAX>& S, const unsigned char* p,
                                          const float* bsrc, int lane)
 {
-    S.code = code;
-    if (code == 0xFF) return;
-    const int stp = code & 0x3F;
-    S.gm = nc_v4f(base + (size_t)lane * 16);
-    S.go = nc_i(base + 512 + (size_t)lane * 4);
+    S.gm = nc_v4f(p + lane * 16);
+    S.go = nc_i(p + 512 + lane * 4);
     S.b = nc_f(bsrc);
-    const unsigned char* o = base + kRegLaneTab + (size_t)lane * 8;
-    const unsigned char* v = base + kRegLaneTab + (SMAX / 4) * 256 + (size_t)lane * 16;
 #pragma unroll
     for (int k = 0; k < SMAX / 4; ++k) {
-        if (4 * k < stp) {
-            S.off[k] = nc_v2u(o + (size_t)k * 256);
-            S.val[k] = nc_v4f(v + (size_t)k * 512);
-        }
+        S.off[k] = nc_v4u(p + kRegLaneTab + k * 512 + lane * 16);
+        S.val[k] = nc_v4f(p + kRegLaneTab + (SMAX / 4) * 512 + k * 512 + lane * 16);
     }
 }
 
-template <int H, int SMAX, bool UPPER>
-__device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, float* win, const RegArgs& a,
-                                          int lane0, int tb)
+template <int H, int SMAX>
+__device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, unsigned wbase, float* win,
+                                          float* out, int lane0)
 {
-    const int stp = S.code & 0x3F;
     float acc0 = 0.0f, acc1 = 0.0f;
 #pragma unroll
     for (int k = 0; k < SMAX / 4; ++k) {
-        if (4 * k < stp) {
-            // steps past the chunk's count within this quad read the zero slot
-            const float x0 = win[S.off[k].x & 0xFFFFu], x1 = win[S.off[k].x >> 16];
-            const float x2 = win[S.off[k].y & 0xFFFFu], x3 = win[S.off[k].y >> 16];
-            acc0 = fmaf(S.val[k].x, x0, acc0);
-            acc1 = fmaf(S.val[k].y, x1, acc1);
-            acc0 = fmaf(S.val[k].z, x2, acc0);
-            acc1 = fmaf(S.val[k].w, x3, acc1);
-        }
+        const float x0 = lds_f(wbase + S.off[k].x), x1 = lds_f(wbase + S.off[k].y);
+        const float x2 = lds_f(wbase + S.off[k].z), x3 = lds_f(wbase + S.off[k].w);
+        acc0 = fmaf(S.val[k].x, x0, acc0);
+        acc1 = fmaf(S.val[k].y, x1, acc1);
+        acc0 = fmaf(S.val[k].z, x2, acc0);
+        acc1 = fmaf(S.val[k].w, x3, acc1);
     }
     float acc = acc0 + acc1;
 #pragma unroll
@@ -1812,23 +1777,7 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, float* win, con
     const int wo = __float_as_int(S.gm.w);
     if (wo >= 0) {
         win[wo] = sol;
-        if (UPPER) a.out[(size_t)S.go + tb] = sol;
-        else a.out[(size_t)tb * a.ostride + S.go] = sol;
-    }
-}
-
-// The chunks of level L beyond the ncw primary ones (wide levels).
-template <int H, int SMAX, bool UPPER>
-__device__ __noinline__ void reg_overflow(const RegArgs& a, int L, float* win, const float* rhs,
-                                          int warp, int lane, int lane0, int tb)
-{
-    const int2 ov = a.ovf[L];
-    for (int c = a.ncw + warp; c < ov.x; c += a.ncw) {
-        const int oi = ov.y + (c - a.ncw);
-        const size_t sl = (size_t)a.nl * a.ncw + oi;
-        RegSet<SMAX> T;
-        reg_load<SMAX>(T, a.slots + sl * a.slot_bytes, a.ovf_steps[oi], rhs + sl * 32 + lane, lane);
-        reg_level<H, SMAX, UPPER>(T, win, a, lane0, tb);
+        out[S.go] = sol;
     }
 }
 
@@ -1839,42 +1788,30 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
     const int tb = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int GS = 3 * H;
     const int lane0 = (lane / GS) * GS;
-    const float* rhs = a.rhs + (size_t)tb * a.rstride;
+    const unsigned wbase = (unsigned)__cvta_generic_to_shared(rwin);
+    float* out = UPPER ? a.out + tb : a.out + (size_t)tb * a.ostride;
     if (threadIdx.x < 3) rwin[a.zero_off + threadIdx.x] = 0.0f;
-    // the warp's step codes, 32 levels per register
-    const unsigned char* stw = a.steps + (size_t)warp * a.nlp;
-    int st_cur = stw[lane], st_next = stw[32 + lane], blk = 0;
+    // this warp's slot and right-hand side advance by one level's worth
+    const size_t sstep = (size_t)a.ncw * a.slot_bytes;
+    const unsigned char* sp = a.slots + (size_t)warp * a.slot_bytes;
+    const float* bp = a.rhs + (size_t)tb * a.rstride + (size_t)warp * 32 + lane;
     RegSet<SMAX> s0, s1;
-    auto load = [&](RegSet<SMAX>& S, int L) {
-        int code = 0xFF;
-        if (L < a.nl) {
-            if ((L >> 5) != blk) {  // L advances one level per call
-                st_cur = st_next;
-                ++blk;
-                st_next = stw[(size_t)(blk + 1) * 32 + lane];
-            }
-            code = __shfl_sync(0xffffffffu, st_cur, L & 31);
-        }
-        const size_t sl = (size_t)L * a.ncw + warp;
-        reg_load<SMAX>(S, a.slots + sl * a.slot_bytes, code, rhs + sl * 32 + lane, lane);
-    };
-    load(s0, 0);
-    load(s1, 1);
+    reg_load<SMAX>(s0, sp, bp, lane);
+    if (a.nl > 1) reg_load<SMAX>(s1, sp + sstep, bp + a.ncw * 32, lane);
+    sp += 2 * sstep;
+    bp += 2 * a.ncw * 32;
     level_barrier();  // the zero slot is set
     for (int l = 0; l < a.nl; l += 2) {
-        if (s0.code != 0xFF) {
-            reg_level<H, SMAX, UPPER>(s0, rwin, a, lane0, tb);
-            if (s0.code & 0x40) reg_overflow<H, SMAX, UPPER>(a, l, rwin, rhs, warp, lane, lane0, tb);
-        }
-        load(s0, l + 2);
+        reg_level<H, SMAX>(s0, wbase, rwin, out, lane0);
+        if (l + 2 < a.nl) reg_load<SMAX>(s0, sp, bp, lane);
+        sp += sstep;
+        bp += a.ncw * 32;
         level_barrier();
         if (l + 1 < a.nl) {
-            if (s1.code != 0xFF) {
-                reg_level<H, SMAX, UPPER>(s1, rwin, a, lane0, tb);
-                if (s1.code & 0x40)
-                    reg_overflow<H, SMAX, UPPER>(a, l + 1, rwin, rhs, warp, lane, lane0, tb);
-            }
-            load(s1, l + 3);
+            reg_level<H, SMAX>(s1, wbase, rwin, out, lane0);
+            if (l + 3 < a.nl) reg_load<SMAX>(s1, sp, bp, lane);
+            sp += sstep;
+            bp += a.ncw * 32;
             level_barrier();
         }
     }
@@ -1921,11 +1858,9 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
     const RegTri& U = *st.regU;
     const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
     k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p);
-    RegArgs aL{L.slots.p, L.steps.p, reinterpret_cast<const int2*>(L.ovf.p), L.ovf_steps.p,
-               st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.nlp, L.ncw, L.slot_bytes,
+    RegArgs aL{L.slots.p, st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw, L.slot_bytes,
                L.zero_off};
-    RegArgs aU{U.slots.p, U.steps.p, reinterpret_cast<const int2*>(U.ovf.p), U.ovf_steps.p,
-               st.rrhsU.p, z, U.lanes, 0, U.nl, U.nlp, U.ncw, U.slot_bytes, U.zero_off};
+    RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off};
     k_tri_reg<H, SMAX, false><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
     k_tri_reg<H, SMAX, true><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
@@ -1942,7 +1877,7 @@ int launch_reg_any(const IluStage& st, const double* dAinv, const float* v, floa
     if (H == 2 && smax == 12) return launch_reg<Q, 2, 12>(st, dAinv, v, z, s);
     if (H == 2 && smax == 16) return launch_reg<Q, 2, 16>(st, dAinv, v, z, s);
     if (H == 1 && smax == 12) return launch_reg<Q, 1, 12>(st, dAinv, v, z, s);
-    if (H == 1 && smax == 24) return launch_reg<Q, 1, 24>(st, dAinv, v, z, s);
+    if (H == 1 && smax == 20) return launch_reg<Q, 1, 20>(st, dAinv, v, z, s);
     if (H == 4 && smax == 8) return launch_reg<Q, 4, 8>(st, dAinv, v, z, s);
     set_error("register sweep: no kernel for these shares and steps");
     return XT_ERR_ARG;
