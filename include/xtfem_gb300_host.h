@@ -125,6 +125,13 @@ typedef struct xt_slab_config {
     int overlap;         /* 1 = run each slab's damage update on a second,
                             lower-priority stream while the next slab is
                             solved (see xt_slab_step) */
+    double load_ratio;   /* R = F_min / F_max of the cyclic traction
+                            F(t) = amplitude (m + sin(w t)), m = (1 + R) / (1 - R);
+                            -1 (the reference's fully reversed sine) gives
+                            m = 0.  The mean part m enters the load blocks
+                            with the weights of a load constant in time,
+                            N_j(t1 + dt) - N_j(t1) = (-1, 0, 1, 0, 0, 0),
+                            beside the sine weights of src/getfextc.f90. */
 } xt_slab_config;
 
 typedef struct xt_slab_s *xt_slab;

@@ -10,7 +10,8 @@ Per slab, in the reference's order:
      checked against an assembly of the surviving elements in
      tests/test_host.py), a new ILUT factor (oracle), and the slab length
      and damage resolution switch from n1 to n2 load cycles;
-  3. load blocks fextc(j) * rext, then the jump term
+  3. load blocks fextc(j) * rext (plus, for a load ratio R > -1, the mean
+     load's weights (-1, 0, 1, 0, 0, 0) times (1 + R) / (1 - R)), then the jump term
      (ktn1 (x) K + mtn1 (x) M) u_prev (oracle kronspgemv), fixed rows zeroed
      (:804-823);
   4. GMRES from a zero start (oracle kronpgmres), fixed DOFs of the
@@ -89,6 +90,12 @@ class OracleSlabLoop:
             self.nip = cfg.nipc * cfg.n2
         ck, cm, ckt, cmt, ck1, cm1 = xt.stcoeff_m(self.tc[0], self.dt, self.w)
         fextc, _ = xt.getfextc_m(self.tc[0], self.w, self.dt)
+        fextc = np.array(fextc, dtype=float)
+        R = getattr(cfg, "load_ratio", -1.0)
+        if R > -1.0:  # mean load: weights of a load constant over the slab
+            m = (1.0 + R) / (1.0 - R)
+            fextc[0] -= m
+            fextc[2] += m
         f = np.concatenate([fextc[j] * self.rext for j in range(6)])
         f = orc.kronspgemv(ck1, cm1, 1.0, 1.0, self.K, self.M, self.disp, f)
         bc6 = np.tile(self.bc, 6) == 1

@@ -266,6 +266,15 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check 
     } else {
         double fextc[6], fint[6];
         getfextc_m(s.tc[0], s.w, s.dt, fextc, fint);
+        // a mean load m * amplitude (load ratio R > -1): weights of a load
+        // constant over the slab, the integrals of the temporal shape
+        // functions' time derivatives, (-1, 0, 1, 0, 0, 0)
+        const double R = s.cfg.load_ratio;
+        if (R > -1.0) {
+            const double m = (1.0 + R) / (1.0 - R);
+            fextc[0] -= m;
+            fextc[2] += m;
+        }
         XT_TRY(fill_load(s.drext.p, fextc, s.fext.p, s.p, s.q, st));
         if (s.therm) {  // + fint(j) vv, the thermal stress load (src/main3d.f90:813)
             XT_TRY(fill_load(s.vv.p, fint, s.work.p, s.p, s.q, st));
@@ -593,7 +602,8 @@ int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
         const Mesh& m = pr.mesh;
         if (cfg->clamp_axis < 0 || cfg->clamp_axis > 2 || cfg->load_axis < 0 || cfg->load_axis > 2 ||
             cfg->load_comp < 0 || cfg->load_comp > 2 || cfg->im < 1 || cfg->dt0 <= 0 || cfg->n1 < 1 ||
-            cfg->n2 < 1 || cfg->nipc < 0 || cfg->lfil < 0) {
+            cfg->n2 < 1 || cfg->nipc < 0 || cfg->lfil < 0 || !(cfg->load_ratio >= -1.0) ||
+            !(cfg->load_ratio < 1.0)) {
             set_error("xt_slab_create: invalid configuration");
             return XT_ERR_ARG;
         }
