@@ -40,13 +40,14 @@ WORKLOAD = dict(nx=60, ny=20, nz=20, lx=3.0, ly=1.0, lz=1.0, E=2.0e5, nu=0.3, rh
 METRIC = "time-slab solves/s to rel.res 1e-8, mixed-prec batched vs FP64 GMRES, 1 GB300"
 UNIT = "slab-solves/s"
 DTYPE_NAMES = {0: "fp64", 1: "fp32 operator/factor/basis, fp64 residual+refinement+damage",
-               3: "bf16-stored K and M with fp32 accumulation, fp32 factor and basis; fp64 "
-                  "residual, refinement and damage",
+               3: "bf16-stored K and M with fp32 accumulation in the preconditioner, fp32 "
+                  "factor; double-float operator and basis; fp64 residual, refinement and damage",
                2: "fp32 ilu factor and apply; double-float (fp32 pair) operator and Krylov basis; "
                   "fp64 true residual, refinement and damage"}
 PRECISION_NAMES = {0: "fp64 gmres", 1: "fp32 gmres inside fp64 refinement",
                    2: "flexible gmres: double-float operator+basis, fp32 ilu, fp64 refinement",
-                   3: "fp32 gmres with bf16-stored K and M inside fp64 refinement"}
+                   3: "flexible gmres preconditioned by fp32 gmres on bf16-stored K and M, "
+                      "fp64 refinement"}
 
 
 def amplitude(seed):

@@ -210,9 +210,12 @@ int xt_system_gmres(xt_system s, const double *rhs, double *sol, int im,
  * factor and Krylov basis (FP64 dot products and Hessenberg) inside FP64
  * iterative refinement, 2 runs flexible GMRES with the FP32 factor and a
  * double-float (FP32 pair) basis and operator on the preconditioned
- * vectors, 3 runs mode 1 with K and M of the inner operator stored in BF16
+ * vectors, 3 runs mode 2 with a preconditioner that is itself a short
+ * FP32 GMRES (10 steps, ILU-preconditioned) on K and M stored in BF16
  * (rounded to nearest, widened to FP32 and accumulated in FP32; the
- * BF16-stored experiment).  out_stats (may be NULL) gets 6 values: iterations, cycles,
+ * BF16-stored experiment: with BF16 K and M as the operator of plain
+ * refinement the error of a stiff system's K makes it diverge).
+ * out_stats (may be NULL) gets 6 values: iterations, cycles,
  * refinement passes, ierr, true relative residual, last estimate. */
 int xt_system_solve(xt_system s, const double *rhs, double *sol, int im,
                     double tol, int maxits, int precision, double inner_tol,

@@ -117,7 +117,8 @@ typedef struct xt_slab_config {
     int maxits;          /* Arnoldi steps per slab at most */
     int precision;       /* as in xt_system_solve: 0 FP64 GMRES, 1 FP32 inner
                             + FP64 refinement, 2 flexible (default of the
-                            bench), 3 as 1 with BF16-stored K and M */
+                            bench), 3 as 2 with a nested FP32 GMRES on
+                            BF16-stored K and M as preconditioner */
     double inner_tol;    /* relative tolerance of an FP32 inner solve */
     double Dc;           /* critical damage */
     int damage;          /* 1 = run the damage update */

@@ -200,7 +200,7 @@ def test_gmres_iteration_history_tracks_oracle(xt, orc, rod_system):
     sysm.close()
 
 
-@pytest.mark.parametrize("precision", [0, 1, 2])
+@pytest.mark.parametrize("precision", [0, 1, 2, 3])
 def test_refined_solve_reaches_true_residual(xt, orc, rod_system, precision):
     s = rod_system
     rhs = c1_rhs(xt, s)
@@ -328,26 +328,22 @@ def test_node_block_operator_matches_csr_operator(xt, orc, rod_system, monkeypat
 
 
 def test_bf16_stored_operator_under_refinement(xt, orc, rod_system):
-    """Mode 3 (FP32 GMRES on BF16-stored K and M inside FP64 refinement):
-    each refinement pass contracts the error by about the relative error of
-    the BF16 operator times the conditioning, so it reaches the FP64 true
-    residual when that product is below one.  The measured passes,
-    iterations and final residual are printed; converged, the solution
-    agrees with the oracle's."""
+    """Mode 3: flexible GMRES whose preconditioner is a short FP32 GMRES on
+    K and M stored in BF16 (with the FP32 ILU), under the FP64 true residual
+    of the refinement loop.  Used directly as the operator of the inner
+    solve, the BF16 rounding of this stiff system's K (relative error 2^-9
+    per entry, times its conditioning) makes plain refinement diverge;
+    inside the preconditioner it only slows convergence.  The solution
+    reaches the FP64 residual and the oracle's answer."""
     s = rod_system
     rhs = c1_rhs(xt, s)
     sysm = xt.SpaceTimeSystem(s["K"], s["M"])
     sysm.set_ilu(s["alu"], s["jlu"], s["ju"])
     sysm.set_temporal(s["A"], s["B"])
-    rows = []
-    for inner_tol in (1e-2, 1e-3, 1e-5):
-        sol, info = sysm.solve(rhs, im=30, tol=1e-8, maxits=20000, precision=3,
-                               inner_tol=inner_tol)
-        rows.append((inner_tol, info))
-        print(f"bf16 inner_tol {inner_tol}: {info}")
+    sol, info = sysm.solve(rhs, im=30, tol=1e-8, maxits=3000, precision=3)
+    print(f"bf16 mode: {info}")
     sysm.close()
-    done = [(t, i) for t, i in rows if i["ierr"] == 0]
-    assert done, rows
+    assert info["ierr"] == 0 and info["relres"] <= 1e-8
     sol_ref, _, _, _ = orc.kronpgmres(s["A"], s["B"], s["K"], s["M"], s["alu"], s["jlu"],
                                       s["ju"], rhs, im=30, eps=1e-10, maxits=3000)
-    assert done[0][1]["relres"] <= 1e-8
+    assert rel(sol, sol_ref) <= 1e-6

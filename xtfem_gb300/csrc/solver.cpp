@@ -443,6 +443,24 @@ int gmres_core(System& S, const T* rhs, T* sol, int im, double eps, int maxits, 
 // double-float accuracy however the FP32 preconditioner rounds; the
 // operator is applied to z_j in double-float too (FP64-class result at FP32
 // throughput).  A restart rebuilds the residual explicitly (FP64).
+// Preconditioner of the BF16 experiment (mode 3): a few steps of FP32
+// GMRES on the BF16-stored operator, right-preconditioned with the FP32
+// ILU, from z = 0 (a variable preconditioner, which the flexible outer
+// GMRES allows; the outer Arnoldi relation keeps the double-float
+// operator, so the BF16 rounding of K and M only slows convergence).
+constexpr int kNestSteps = 10;
+constexpr double kNestTol = 1e-3;
+
+int nested_prec(System& S, const float* v, float* z)
+{
+    const size_t n = (size_t)S.p * S.q;
+    XT_CUDA(cudaMemsetAsync(z, 0, n * sizeof(float), S.stream));
+    GmresStats in;
+    XT_TRY(gmres_core<float>(S, v, z, kNestSteps, kNestTol, kNestSteps, in, nullptr));
+    S.nest_its += in.its;
+    return XT_OK;
+}
+
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
@@ -488,7 +506,8 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             ++its;
             const int i1 = i + 1;
             XT_TRY(df_hi(col(i - 1), S.d32.p, n, s));
-            XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
+            if (S.op16) XT_TRY(nested_prec(S, S.d32.p, zc(i - 1)));
+            else XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
             {  // w = A z in double-float, straight into the basis column
                 const int tok = prof_begin(PROF_KRONDF, s);
                 XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, zc(i - 1), col(i1 - 1), s));
@@ -584,15 +603,18 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
     XT_TRY(system_stream(S));
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
-    // mode 3 is mode 1 with the inner operator's K and M stored in BF16
+    // mode 3: the flexible GMRES of mode 2 whose preconditioner is a short
+    // FP32 GMRES on K and M stored in BF16 (nested_prec)
     const bool bf16 = inner == 3;
-    if (bf16) inner = 1;
+    if (bf16) inner = 2;
     struct Op16 {
         System& S;
         ~Op16() { S.op16 = false; }
     } op16_reset{S};
     S.op16 = bf16;
+    S.nest_its = 0;
     XT_TRY(ensure_workspace(S, im, inner == 1, inner == 2));
+    if (bf16) XT_TRY(ensure_workspace(S, kNestSteps, true));
     double hb[2];
     XT_TRY(norm2<double>(b, n, S.red, s));
     XT_TRY(fetch(s, hb, S.red.out.p, 1));

@@ -41,6 +41,7 @@ struct System {
     // GMRES workspace
     int im_cap = 0;
     bool op16 = false;  // FP32 inner operator reads BF16-stored K and M (mode 3)
+    long long nest_its = 0;  // inner iterations of the last mode-3 solve
     DBuf<double> V64, z64, w64, u64;
     DBuf<float> V32, z32, w32, u32, d32, r32;
     DBuf<float> Z32;  // flexible GMRES: preconditioned basis, im columns
