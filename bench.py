@@ -748,6 +748,61 @@ def run_reference(args, rank, world):
             "wall_s": round(time.perf_counter() - t_run, 1)}
 
 
+# ------------------------------------------------- other workloads (side runs)
+def run_workload(args):
+    """--workload c3|c5 (or any workload file): args.steps slabs of that
+    workload's device slab loop at its full size, sequential (each slab's
+    damage update before the next solve), host wall clock per slab with the
+    device synchronised.  --predamage D seeds every Gauss point's damage at
+    D and its stored energy just below the damage threshold (a specimen
+    near the end of its fatigue life), so that elements reach Dc = 0.99
+    within a few slabs.  Prints one JSON line with a record per slab.  Not
+    the headline: bench.py without --workload measures C2."""
+    import xtfem_gb300 as xt
+    from xtfem_gb300 import workloads
+
+    xt.lib().xt_init(int(os.environ.get("LOCAL_RANK", "0")))
+    t0 = time.perf_counter()
+    w = workloads.load(args.workload)
+    cfg = w.slab
+    if args.precision is not None:
+        cfg.precision = args.precision
+    cfg.overlap = 0
+    nn, ne, nnz_k, _ = w.problem.sizes()
+    s = xt.SlabSolver(w.problem, cfg)
+    th = None
+    if w.thermal is not None:
+        w.thermal.precision = cfg.precision
+        th = xt.ThermalSolver(w.problem, w.thermal)
+        s.couple(th, **w.coupling)
+    if args.predamage is not None:
+        s.set_state(D=np.full(s.ngp, args.predamage), ws=np.full(s.ngp, 31.7))
+    setup = time.perf_counter() - t0
+    rows = []
+    for _ in range(args.steps):
+        xt.lib().xt_sync()
+        t1 = time.perf_counter()
+        st = s.step()
+        xt.lib().xt_sync()
+        rows.append({"slab": int(st["slab"]), "seconds": round(time.perf_counter() - t1, 3),
+                     "its": int(st["its"]), "outer": int(st["outer"]),
+                     "relres": float(st["relres"]), "ierr": int(st["ierr"]),
+                     "deleted": int(st["deleted"]), "failed": int(st["nfailed"]),
+                     "maxD": float(st["maxD"])})
+    state = s.state()
+    s.close()
+    if th is not None:
+        th.close()
+    name = w.name
+    w.close()
+    return {"workload": name, "description": w.description, "nodes": nn, "elements": ne,
+            "spatial_dofs": 3 * nn, "nnz_k": nnz_k, "precision": PRECISION_NAMES[cfg.precision],
+            "predamage": args.predamage, "setup_s": round(setup, 2), "slabs": rows,
+            "slab_s_mean": round(float(np.mean([r["seconds"] for r in rows])), 3),
+            "deleted_elements": [int(e) for e in np.flatnonzero(state["elesta"] == 0) + 1],
+            "timer": "host wall clock per slab, device synchronised"}
+
+
 # ------------------------------------------------------------ harness
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -789,6 +844,12 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-variants", action="store_true",
                     help="skip the no-damage and reduced-nip slab lines")
+    ap.add_argument("--workload", default=None,
+                    help="side run of another workload file (c3, c5, ...): --steps slabs at "
+                         "full size, one JSON line with a record per slab")
+    ap.add_argument("--predamage", type=float, default=None,
+                    help="with --workload: seed D at this value and the stored energy just "
+                         "below the damage threshold")
     ap.add_argument("--inner-tol", type=float, default=None)
     ap.add_argument("--im", type=int, default=None)
     ap.add_argument("--specimens", type=int, default=8,
@@ -813,7 +874,9 @@ def main():
     if args.overlap is not None:
         WORKLOAD["overlap"] = args.overlap
     rank, world = dist_setup()
-    if args.impl == "reference":
+    if args.workload:
+        out = run_workload(args) if rank == 0 else None
+    elif args.impl == "reference":
         out = run_reference(args, rank, world)
     else:
         out = run_gpu(args, rank, world)
