@@ -245,6 +245,16 @@ def run_gpu(args, rank, world):
                for c in prof}
     its = [s["its"] for s in steps]
     res = [s["relres"] for s in steps]
+    # damage update: FP64 work of its exact steps against the FP64 pipe.
+    # An exact step restates src/kokkos_kernel.h:56-180 in FP64: the
+    # displacement interpolation (144 multiply-adds), the strain (144
+    # flops), the elastic matrix, the predictor and the equivalent stress
+    # (about 180 flops): 610 flops counted from the kernel source, more when
+    # the plastic corrector runs.  Screened steps are FP32.
+    exact = float(np.mean([s["exact_steps"] for s in steps]))
+    screened = float(np.mean([s["screened_steps"] for s in steps]))
+    dcnt, dms = prof[4]
+    fp64_gflops = exact * 610.0 / (dms / max(dcnt, 1) / 1e3) / 1e9 if dcnt else 0.0
     out = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3),
@@ -261,6 +271,15 @@ def run_gpu(args, rank, world):
                      "note": ROOFLINE_NOTES.get(dom)},
         "roofline_streaming": streaming_roofline(prof, nbytes, hbm),
         "kernels": kernels,
+        "damage_pipes": {"exact_steps_per_slab": exact, "screened_steps_per_slab": screened,
+                         "fp64_flops_per_exact_step": 610,
+                         "fp64_achieved_gflops": round(fp64_gflops, 3),
+                         "fp64_peak_gflops": 1250.0, "fp64_peak_kind": "nominal (no measured "
+                         "FP64 peak on this pool)",
+                         "fp64_frac": round(fp64_gflops / 1250.0, 7),
+                         "note": "the update's time is set by the few points whose steps are "
+                                 "plastic (C2: the four clamped corners), each a serial FP64 "
+                                 "chain; every other step is proven elastic by the FP32 screen"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
@@ -369,6 +388,7 @@ def run_rod_batch(xt, count, seed):
     kw = dict(im=0, tol=WORKLOAD["tol"], precision=2)  # tuned restart length
     batch.solve(rhs, **kw)  # tunes, then solves (untimed)
     kw["im"] = batch.restart
+    shares = batch.ilu_shares
     xt.lib().xt_sync()
     t0 = time.perf_counter()
     _, stats, _ = batch.solve(rhs, **kw)
@@ -385,7 +405,7 @@ def run_rod_batch(xt, count, seed):
         s.close()
     return {"rods": count, "value": round(count / t_batch, 2), "unit": "rod-slab-solves/s",
             "ms_all": round(t_batch * 1e3, 2), "one_after_another_ms": round(t_seq * 1e3, 2),
-            "restart": kw["im"],
+            "restart": kw["im"], "ilu_lanes_per_row": shares,
             "iterations_mean": round(float(np.mean([st["its"] for st in stats])), 1),
             "relres_max": float(max(st["relres"] for st in stats)),
             "space_time_dofs": dofs, "n_values": ns.tolist(),

@@ -266,10 +266,12 @@ int xt_batch_create(int count, const xt_system *systems, int workers, xt_batch *
 int xt_batch_destroy(xt_batch b);
 /* xt_system_solve on every system of the batch: rhs[i] and sol[i] are
  * system i's host vectors (block layout; sol[i] is the initial guess and
- * receives the solution).  im <= 0 uses the batch's tuned restart length;
- * the first such call tunes it (each of 30, 60, 120 and 200, capped at the
- * largest system's unknowns, solves the whole batch once from the given
- * initial guesses; the fastest is kept for the batch's later calls).
+ * receives the solution).  im <= 0 uses the batch's tuned restart length
+ * and ILU lanes per row; the first such call tunes them (each restart of
+ * 30, 60, 120 and 200, capped at the largest system's unknowns, with 2 and
+ * with 1 lanes per row of the FP32 register sweep, i.e. 5 or 10 node rows
+ * per warp, solves the whole batch once from the given initial guesses;
+ * the fastest pair is kept for the batch's later calls).
  * stats (may be NULL) gets 6 values per system as in xt_system_solve;
  * status (may be NULL) gets each system's return code.  Returns XT_OK when
  * every system succeeded, else the first failing system's code (its
@@ -279,6 +281,9 @@ int xt_batch_solve(xt_batch b, const double *const *rhs, double *const *sol, int
                    double *stats, int *status);
 /* The restart length the tuner picked (0 before the first tuned call). */
 int xt_batch_restart(xt_batch b);
+/* The ILU lanes per row the tuner picked (1 or 2; 0 before the first tuned
+ * call).  No counterpart in the reference. */
+int xt_batch_ilu_shares(xt_batch b);
 
 #ifdef __cplusplus
 }

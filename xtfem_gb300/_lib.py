@@ -59,6 +59,7 @@ SIGNATURES = {
     "xt_batch_create": (C.c_int, [C.c_int, C.POINTER(_vp), C.c_int, C.POINTER(_vp)]),
     "xt_batch_destroy": (C.c_int, [_vp]),
     "xt_batch_restart": (C.c_int, [_vp]),
+    "xt_batch_ilu_shares": (C.c_int, [_vp]),
     "xt_batch_solve": (C.c_int, [_vp, C.POINTER(_dp), C.POINTER(_dp), C.c_int, C.c_double, C.c_int,
                                  C.c_int, C.c_double, _dp, _ip]),
     "xth_problem_from_inp": (C.c_int, [C.c_char_p, C.c_double, C.c_double, C.c_double,

@@ -391,6 +391,11 @@ class SystemBatch:
         """The restart length picked by the tuner (0 before a solve with im=0)."""
         return lib().xt_batch_restart(self._h)
 
+    @property
+    def ilu_shares(self) -> int:
+        """The ILU lanes per row picked by the tuner (0 before a solve with im=0)."""
+        return lib().xt_batch_ilu_shares(self._h)
+
     def solve(self, rhs, sols=None, im=30, tol=1e-8, maxits=2000, precision=0, inner_tol=1e-5):
         """rhs: list of host vectors; returns (solutions, stats list, status
         array).  im=0 uses the tuned restart length (tuned on first use).

@@ -403,6 +403,7 @@ struct xt_batch_s {
     std::vector<int> order;  // largest system first
     int workers = 1;
     int tuned_im = 0;        // restart length picked by the tuner, 0 before
+    int tuned_shares = 0;    // ILU lanes per row picked by the tuner
 };
 
 int xt_batch_create(int count, const xt_system* systems, int workers, xt_batch* out)
@@ -442,9 +443,16 @@ namespace {
 int batch_run(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
               int maxits, int precision, double inner_tol, double* stats, int* status);
 
-// Restart-length tuner: each candidate length solves the whole batch from
-// the caller's initial guesses; the fastest (host wall clock, device work
-// included: every solve ends with its download) is kept.
+// Tuner of the restart length and of the ILU sweep's lanes per row (the
+// register sweep's rows per warp): each candidate pair solves the whole
+// batch from the caller's initial guesses; the fastest (host wall clock,
+// device work included: every solve ends with its download) is kept.
+void set_shares(xt_batch b, int shares)
+{
+    for (xt_system h : b->sys)
+        if (h->sys.ilu) h->sys.ilu->shares = shares;
+}
+
 int batch_tune(xt_batch b, const double* const* rhs, double* const* sol, double tol, int maxits,
                int precision, double inner_tol)
 {
@@ -457,26 +465,36 @@ int batch_tune(xt_batch b, const double* const* rhs, double* const* sol, double 
         x0[i].assign(sol[i], sol[i] + n);
     }
     double best = 0.0;
-    int best_im = 0;
-    for (int cand : {30, 60, 120, 200}) {
-        const int im = (int)std::min<long long>(cand, nmax);
-        if (im == best_im) continue;
-        for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
-        const auto t0 = std::chrono::steady_clock::now();
-        XT_TRY(batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, nullptr, nullptr));
-        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (best_im == 0 || t < best) {
-            best = t;
-            best_im = im;
+    int best_im = 0, best_sh = 0;
+    for (int sh : {2, 1}) {
+        set_shares(b, sh);
+        int last_im = 0;
+        for (int cand : {30, 60, 120, 200}) {
+            const int im = (int)std::min<long long>(cand, nmax);
+            if (im == last_im) continue;
+            last_im = im;
+            for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
+            const auto t0 = std::chrono::steady_clock::now();
+            XT_TRY(batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, nullptr, nullptr));
+            const double t =
+                std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (best_im == 0 || t < best) {
+                best = t;
+                best_im = im;
+                best_sh = sh;
+            }
         }
     }
     for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
     b->tuned_im = best_im;
+    b->tuned_shares = best_sh;
+    set_shares(b, best_sh);
     return XT_OK;
 }
 }  // namespace
 
 int xt_batch_restart(xt_batch b) { return b ? b->tuned_im : 0; }
+int xt_batch_ilu_shares(xt_batch b) { return b ? b->tuned_shares : 0; }
 
 int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
                    int maxits, int precision, double inner_tol, double* stats, int* status)
@@ -488,6 +506,7 @@ int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int
     if (im <= 0) {
         if (b->tuned_im == 0) XT_TRY(batch_tune(b, rhs, sol, tol, maxits, precision, inner_tol));
         im = b->tuned_im;
+        set_shares(b, b->tuned_shares);
     }
     return batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, stats, status);
 }

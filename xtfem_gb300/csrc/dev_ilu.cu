@@ -2058,7 +2058,7 @@ int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, 
     int fmt = env_int("XTFEM_ILU_FMT", 4);
     if constexpr (sizeof(T) == 4) {
         if (F.L.g == 3 && fmt == 4) {
-            const int H = env_int("XTFEM_ILU_SHARES", 2);
+            const int H = F.shares > 0 ? F.shares : env_int("XTFEM_ILU_SHARES", 2);
             XT_TRY(get_stage<T>(F, Q, 4, s, st, H));
             if (st) return launch_reg_any<Q>(*st, dAinv, v, z, s);
             fmt = 3;

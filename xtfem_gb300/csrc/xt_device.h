@@ -194,6 +194,10 @@ struct DevIlu {
     std::shared_ptr<IluSched> sched;
     // built on first use for a (q, precision) pair; key 2*q + (FP32 ? 1 : 0)
     mutable std::map<int, std::shared_ptr<IluStage>> stages;
+    // lanes per row of the FP32 register sweep (its rows per warp: 10 node
+    // rows at 1, 5 at 2, 2 at 4); 0 = XTFEM_ILU_SHARES or 2.  Set by the
+    // batch tuner.
+    mutable int shares = 0;
 };
 
 // Build the level schedule from the 1-based MSR arrays and upload it.
