@@ -16,8 +16,9 @@ basis, FP64 true residual); the oracle solves with the reference's GMRES to
 an estimated relative residual of 1e-10.
 
 Checked every slab: the set of elements deleted is the oracle's; the
-displacement agrees to 1e-6 of its scale and the damage to 1e-6 absolute
-until the first deletion.  After it (measured on a GB300, with margin):
+displacement agrees to 1e-6 (relative L2) and the damage to 1e-6 absolute
+until the first deletion, and the points at or past the critical damage
+are the oracle's after every slab.  After it (measured on a GB300, with margin):
 the rod stays within 1e-8 of the oracle's damage; on the notched plate the
 deleted tip elements leave a badly conditioned system, on which a 1e-8
 residual pins the displacement only to about 1e-2 and the damage to about
@@ -94,6 +95,11 @@ def run_pair(xt, orc, case, precision, tol=None):
 POST_DELETION = {"rod": 1e-6, "sent": 1e-2, "sent_r01": 1e-2}
 
 
+def r_dc(case, xt):
+    """Critical damage of a case."""
+    return CASES[case](xt)[1]["Dc"]
+
+
 @pytest.mark.parametrize("precision", [0, 2])
 @pytest.mark.parametrize("case", ["rod", "sent", "sent_r01"])
 def test_slab_loop_matches_oracle_loop(xt, orc, case, precision):
@@ -108,15 +114,19 @@ def test_slab_loop_matches_oracle_loop(xt, orc, case, precision):
         assert np.array_equal(got["elesta"], r["elesta"]), k
         total += len(r["deleted_orc"])
         seen_deletion = seen_deletion or len(r["deleted_orc"]) > 0
-        scale = np.max(np.abs(r["disp"]))
-        dD = np.max(np.abs(got["D"] - r["D"]))
+        du = np.linalg.norm(got["disp"] - r["disp"]) / np.linalg.norm(r["disp"])
+        # damage compared where it is physical (D < 1 in both loops; past
+        # D = 1 the law runs away, and those points fail at the next check)
+        live = (r["D"] < 1.0) & (got["D"] < 1.0)
+        dD = np.max(np.abs(got["D"] - r["D"])[live], initial=0.0)
         print(f"{case} p{precision} slab {k + 1}: deleted {len(r['deleted_orc'])}, "
-              f"|du|/|u| {np.max(np.abs(got['disp'] - r['disp'])) / scale:.2e}, |dD| {dD:.2e}")
+              f"|du|/|u| {du:.2e}, |dD| {dD:.2e}, points past D = 1: {int((~live).sum())}")
+        # the next slab's deletion check sees the same failed points
+        assert np.array_equal(got["D"] >= r_dc(case, xt), r["D"] >= r_dc(case, xt)), k
         if not seen_deletion:
-            assert np.max(np.abs(got["disp"] - r["disp"])) <= 1e-6 * scale, k
+            assert du <= 1e-6, (k, du)
             assert dD <= 1e-6, (k, dD)
             assert np.max(np.abs(got["ws"] - r["ws"])) <= 1e-6 * max(1.0, r["ws"].max()), k
-        else:  # relative to the damage where it has run past 1
-            rD = np.max(np.abs(got["D"] - r["D"]) / np.maximum(1.0, np.abs(r["D"])))
-            assert rD <= POST_DELETION[case], (k, rD)
+        else:
+            assert dD <= POST_DELETION[case], (k, dD)
     assert total > 0

@@ -1687,6 +1687,7 @@ struct RegArgs {
     long long rstride, ostride;
     int nl, ncw, slot_bytes, zero_off;
     int pf;  // levels ahead of use at which a warp's slot is prefetched into L2 (0: off)
+    const int* skip;  // optional: nothing to do when skip[0] != 0
 };
 
 __device__ __forceinline__ float4 nc_v4f(const void* p)
@@ -1790,6 +1791,7 @@ template <int H, int SMAX, bool UPPER>
 __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
 {
     extern __shared__ __align__(16) float rwin[];
+    if (a.skip && a.skip[0] != 0) return;  // uniform: before any barrier
     const int tb = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int GS = 3 * H;
     const int lane0 = (lane / GS) * GS;
@@ -1843,9 +1845,10 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
 template <int Q>
 __global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
                             const double* __restrict__ dAinv, const float* __restrict__ v,
-                            float* __restrict__ rhs)
+                            float* __restrict__ rhs, const int* __restrict__ skip)
 {
     __shared__ float sA[Q * Q];
+    if (skip && skip[0] != 0) return;
     for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sA[i] = (float)dAinv[i];
     __syncthreads();
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < lanes;
@@ -1865,7 +1868,8 @@ __global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
 }
 
 template <int Q, int H, int SMAX>
-int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s)
+int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
+               const int* skip)
 {
     static std::atomic<bool> attr{false};
     if (!attr.load(std::memory_order_acquire)) {
@@ -1878,11 +1882,12 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
     const RegTri& L = *st.regL;
     const RegTri& U = *st.regU;
     const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
-    k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p);
+    k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p, skip);
     const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
     RegArgs aL{L.slots.p, st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw, L.slot_bytes,
-               L.zero_off, pf};
-    RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf};
+               L.zero_off, pf, skip};
+    RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
+               skip};
     k_tri_reg<H, SMAX, false><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
     k_tri_reg<H, SMAX, true><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
@@ -1892,15 +1897,15 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
 
 template <int Q>
 int launch_reg_any(const IluStage& st, const double* dAinv, const float* v, float* z,
-                   cudaStream_t s)
+                   cudaStream_t s, const int* skip)
 {
     const int H = st.regL->H, smax = st.regL->smax;
-    if (H == 2 && smax == 8) return launch_reg<Q, 2, 8>(st, dAinv, v, z, s);
-    if (H == 2 && smax == 12) return launch_reg<Q, 2, 12>(st, dAinv, v, z, s);
-    if (H == 2 && smax == 16) return launch_reg<Q, 2, 16>(st, dAinv, v, z, s);
-    if (H == 1 && smax == 12) return launch_reg<Q, 1, 12>(st, dAinv, v, z, s);
-    if (H == 1 && smax == 20) return launch_reg<Q, 1, 20>(st, dAinv, v, z, s);
-    if (H == 4 && smax == 8) return launch_reg<Q, 4, 8>(st, dAinv, v, z, s);
+    if (H == 2 && smax == 8) return launch_reg<Q, 2, 8>(st, dAinv, v, z, s, skip);
+    if (H == 2 && smax == 12) return launch_reg<Q, 2, 12>(st, dAinv, v, z, s, skip);
+    if (H == 2 && smax == 16) return launch_reg<Q, 2, 16>(st, dAinv, v, z, s, skip);
+    if (H == 1 && smax == 12) return launch_reg<Q, 1, 12>(st, dAinv, v, z, s, skip);
+    if (H == 1 && smax == 20) return launch_reg<Q, 1, 20>(st, dAinv, v, z, s, skip);
+    if (H == 4 && smax == 8) return launch_reg<Q, 4, 8>(st, dAinv, v, z, s, skip);
     set_error("register sweep: no kernel for these shares and steps");
     return XT_ERR_ARG;
 }
@@ -2069,7 +2074,8 @@ int launch_cols1(const DevIlu& F, const IluStage& st, const double* dAinv, const
 }
 
 template <class T, int Q>
-int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s)
+int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, cudaStream_t s,
+               const int* skip)
 {
     IluStage* st = nullptr;
     // 4 (default): rows with register-prefetched records, one temporal
@@ -2082,7 +2088,7 @@ int launch_tri(const DevIlu& F, const double* dAinv, const T* v, T* z, T* work, 
         if (F.L.g == 3 && fmt == 4) {
             const int H = F.shares > 0 ? F.shares : env_int("XTFEM_ILU_SHARES", 2);
             XT_TRY(get_stage<T>(F, Q, 4, s, st, H));
-            if (st) return launch_reg_any<Q>(*st, dAinv, v, z, s);
+            if (st) return launch_reg_any<Q>(*st, dAinv, v, z, s, skip);
             fmt = 3;
         }
     }
@@ -2198,17 +2204,17 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
 
 template <class T>
 int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* work,
-              cudaStream_t s)
+              cudaStream_t s, const int* skip)
 {
     switch (q) {
-    case 1: return launch_tri<T, 1>(F, dAinv, v, z, work, s);
-    case 2: return launch_tri<T, 2>(F, dAinv, v, z, work, s);
-    case 3: return launch_tri<T, 3>(F, dAinv, v, z, work, s);
-    case 4: return launch_tri<T, 4>(F, dAinv, v, z, work, s);
-    case 5: return launch_tri<T, 5>(F, dAinv, v, z, work, s);
-    case 6: return launch_tri<T, 6>(F, dAinv, v, z, work, s);
-    case 7: return launch_tri<T, 7>(F, dAinv, v, z, work, s);
-    case 8: return launch_tri<T, 8>(F, dAinv, v, z, work, s);
+    case 1: return launch_tri<T, 1>(F, dAinv, v, z, work, s, skip);
+    case 2: return launch_tri<T, 2>(F, dAinv, v, z, work, s, skip);
+    case 3: return launch_tri<T, 3>(F, dAinv, v, z, work, s, skip);
+    case 4: return launch_tri<T, 4>(F, dAinv, v, z, work, s, skip);
+    case 5: return launch_tri<T, 5>(F, dAinv, v, z, work, s, skip);
+    case 6: return launch_tri<T, 6>(F, dAinv, v, z, work, s, skip);
+    case 7: return launch_tri<T, 7>(F, dAinv, v, z, work, s, skip);
+    case 8: return launch_tri<T, 8>(F, dAinv, v, z, work, s, skip);
     default:
         set_error("ilu_apply: 1 <= q <= 8");
         return XT_ERR_ARG;
@@ -2216,9 +2222,9 @@ int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* 
 }
 
 template int ilu_apply<double>(const DevIlu&, int, const double*, const double*, double*,
-                               double*, cudaStream_t);
+                               double*, cudaStream_t, const int*);
 template int ilu_apply<float>(const DevIlu&, int, const double*, const float*, float*, float*,
-                              cudaStream_t);
+                              cudaStream_t, const int*);
 
 int ilu_check(cudaStream_t s)
 {

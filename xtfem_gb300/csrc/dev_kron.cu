@@ -302,9 +302,10 @@ __global__ void __launch_bounds__(256)
 k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
           const float2* __restrict__ kv, const float2* __restrict__ mv,
           const double* __restrict__ dA, const double* __restrict__ dB,
-          const float* __restrict__ x, float2* __restrict__ y)
+          const float* __restrict__ x, float2* __restrict__ y, const int* __restrict__ skip)
 {
     static_assert(Q % 2 == 0 && Q <= 8, "pairs of temporal blocks");
+    if (skip && skip[0] != 0) return;
     constexpr int NP = Q / 2, LPR = 3 * NP, RPW = 32 / LPR;
     __shared__ float2 sA[Q * Q], sB[Q * Q];
     for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) {
@@ -376,13 +377,13 @@ k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
 
 template <int Q>
 int launch_nb(const DevNodeBlocks& nb, const double* dA, const double* dB, const float* x,
-              float2* y, cudaStream_t s)
+              float2* y, cudaStream_t s, const int* skip)
 {
     constexpr int RPW = 32 / (3 * (Q / 2));
     const int threads = 256, rows_per_block = (threads / 32) * RPW;
     const int blocks = std::max(1, (nb.nodes + rows_per_block - 1) / rows_per_block);
     k_kron_nb<Q><<<blocks, threads, 0, s>>>(nb.nodes, nb.ptr.p, nb.col.p, nb.kdf.p, nb.mdf.p, dA,
-                                            dB, x, y);
+                                            dB, x, y, skip);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -654,7 +655,7 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 }
 
 int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,
-                 float2* y, cudaStream_t s)
+                 float2* y, cudaStream_t s, const int* skip)
 {
     if (K.n != M.n || q < 1 || q > 8) {
         set_error("kron_spmm_df: K and M must have the same order and 1 <= q <= 8");
@@ -665,10 +666,10 @@ int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB
     if (K.nb.ok && q % 2 == 0 && reinterpret_cast<uintptr_t>(y) % 16 == 0 &&
         reinterpret_cast<uintptr_t>(x) % 8 == 0 && nb_enabled()) {
         switch (q) {
-        case 2: return launch_nb<2>(K.nb, dA, dB, x, y, s);
-        case 4: return launch_nb<4>(K.nb, dA, dB, x, y, s);
-        case 6: return launch_nb<6>(K.nb, dA, dB, x, y, s);
-        default: return launch_nb<8>(K.nb, dA, dB, x, y, s);
+        case 2: return launch_nb<2>(K.nb, dA, dB, x, y, s, skip);
+        case 4: return launch_nb<4>(K.nb, dA, dB, x, y, s, skip);
+        case 6: return launch_nb<6>(K.nb, dA, dB, x, y, s, skip);
+        default: return launch_nb<8>(K.nb, dA, dB, x, y, s, skip);
         }
     }
     XT_TRY(ensure_df(K, s));

@@ -114,16 +114,26 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
 // its FP64-accurate Krylov basis in this form: the same bytes as FP64, but
 // every operation runs on the FP32 pipe.
 
-// partial[(j0+c) nb + b] = (hi, lo) of sum over block b's rows of V_j w
-__global__ void __launch_bounds__(256, 6) k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,
-                               const float4* __restrict__ w, size_t n2,
-                               double* __restrict__ partial)
+// Row blocks per chunk of kChunk basis vectors in a double-float dot pass:
+// about eight resident blocks per SM over all chunks (row blocks shrink as
+// k grows, so each block's rows outweigh its block reduction).
+__host__ __device__ __forceinline__ int df_dot_blocks(int k, int nblocks)
+{
+    const int nchunk = (k + kChunk - 1) / kChunk;
+    const int b = (8 * 152 + nchunk - 1) / nchunk;
+    return b < nblocks ? (b > 38 ? b : 38) : (nblocks > 38 ? nblocks : 38);
+}
+
+// partial[(j0+c) nb + b] = (hi, lo) of sum over row block rb's rows of V_j w
+__device__ __forceinline__ void multi_dot_df_body(const float4* __restrict__ V, size_t ld2, int k,
+                                                  const float4* __restrict__ w, size_t n2,
+                                                  double* __restrict__ partial, int rb, int nb,
+                                                  int chunk)
 {
     __shared__ float2 sh[kChunk][32];
-    const int j0 = blockIdx.y * kChunk;
-    const int nb = gridDim.x;
+    const int j0 = chunk * kChunk;
     const size_t per = (n2 + nb - 1) / nb;
-    const size_t r0 = per * blockIdx.x, r1 = min(n2, r0 + per);
+    const size_t r0 = per * rb, r1 = min(n2, r0 + per);
     float hi[kChunk], lo[kChunk];
 #pragma unroll
     for (int c = 0; c < kChunk; ++c) hi[c] = lo[c] = 0.0f;
@@ -155,8 +165,32 @@ __global__ void __launch_bounds__(256, 6) k_multi_dot_df(const float4* __restric
         const int c = threadIdx.x;
         float h = 0.0f, l = 0.0f;
         for (int wi = 0; wi < nw; ++wi) df_add_df(h, l, sh[c][wi].x, sh[c][wi].y);
-        reinterpret_cast<float2*>(partial)[(size_t)(j0 + c) * nb + blockIdx.x] = make_float2(h, l);
+        reinterpret_cast<float2*>(partial)[(size_t)(j0 + c) * nb + rb] = make_float2(h, l);
     }
+}
+
+__global__ void __launch_bounds__(256, 6) k_multi_dot_df(const float4* __restrict__ V, size_t ld2, int k,
+                               const float4* __restrict__ w, size_t n2,
+                               double* __restrict__ partial)
+{
+    multi_dot_df_body(V, ld2, k, w, n2, partial, blockIdx.x, gridDim.x, blockIdx.y);
+}
+
+// The same pass with k = ctl[0] + 1 read on the device (a step of the
+// device-driven GMRES; nothing to do once ctl[1] is set): block b takes row
+// block b mod nb of chunk b / nb, nb as the host launch would choose it,
+// so the partial sums are those of k_multi_dot_df bit for bit.
+__global__ void __launch_bounds__(256, 6) k_multi_dot_df_ctl(const float4* __restrict__ V, size_t ld2,
+                               const float4* __restrict__ w, size_t n2,
+                               double* __restrict__ partial, int nblocks,
+                               const int* __restrict__ ctl)
+{
+    if (ctl[1] != 0) return;
+    const int k = ctl[0] + 1;
+    const int nb = df_dot_blocks(k, nblocks), nchunk = (k + kChunk - 1) / kChunk;
+    const int chunk = blockIdx.x / nb;
+    if (chunk >= nchunk) return;
+    multi_dot_df_body(V, ld2, k, w, n2, partial, blockIdx.x - chunk * nb, nb, chunk);
 }
 
 // (wh, wl) -= (hh + hl)(vh + vl)
@@ -174,10 +208,14 @@ __device__ __forceinline__ void df_sub_mul(float& wh, float& wl, float hh, float
 template <bool NORM>
 __global__ void k_update_df(const float4* __restrict__ V, size_t ld2, int k,
                             const double* __restrict__ h, float4* __restrict__ w, size_t n2,
-                            double* __restrict__ partial)
+                            double* __restrict__ partial, const int* __restrict__ ctl)
 {
     __shared__ float2 hs[512];
     __shared__ float2 sh[32];
+    if (ctl) {  // device-driven step: k = ctl[0] + 1, nothing once ctl[1] is set
+        if (ctl[1] != 0) return;
+        k = ctl[0] + 1;
+    }
     for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) {
         const float a = (float)h[j];
         hs[j] = make_float2(a, (float)(h[j] - (double)a));
@@ -275,6 +313,145 @@ __global__ void k_finish_df(const double* __restrict__ partial, int nb, double* 
     for (int b = threadIdx.x; b < nb; b += blockDim.x) v += (double)p[b].x + (double)p[b].y;
     const double s = block_sum(v, sh);
     if (threadIdx.x == 0) out[j] = s;
+}
+
+// k_finish_df for a device-driven step: dot mode (norm == 0) sums the
+// k = ctl[0] + 1 dots of the last k_multi_dot_df_ctl pass (block j < k),
+// norm mode sums the nblocks partials of k_update_df<true> (block 0).
+__global__ void k_finish_df_ctl(const double* __restrict__ partial, int nblocks,
+                                double* __restrict__ out, const int* __restrict__ ctl, int norm)
+{
+    __shared__ double sh[32];
+    if (ctl[1] != 0) return;
+    const int k = ctl[0] + 1;
+    const int j = blockIdx.x;
+    if (norm ? j > 0 : j >= k) return;
+    const int nb = norm ? nblocks : df_dot_blocks(k, nblocks);
+    const float2* p = reinterpret_cast<const float2*>(partial) + (size_t)j * nb;
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) v += (double)p[b].x + (double)p[b].y;
+    const double sum = block_sum(v, sh);
+    if (threadIdx.x == 0) out[j] = sum;
+}
+
+// ---------------------------------------------------------------------------
+// Device-driven flexible GMRES (solver.cpp, gmres_flex_dev): the Arnoldi
+// step's bookkeeping on the device.  ctl = {j, status, its, maxits}: j is
+// the step's input basis column, status 0 while the cycle runs (1 once it
+// has ended: converged, restart length or maxits reached; 4 on a
+// non-finite vector).  Every kernel that indexes by j does nothing once the
+// status is set, so steps issued past the end of a cycle cost only their
+// launches.  st holds the Hessenberg matrix, the rotations, rs, the two
+// projections, the squared norm and the scalars (FlexLayout).
+
+__global__ void k_flexd_hi(const int* __restrict__ ctl, const float2* __restrict__ V, size_t nl,
+                           float* __restrict__ d, size_t n)
+{
+    if (ctl[1] != 0) return;
+    const float2* col = V + (size_t)ctl[0] * nl;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) d[i] = col[i].x;
+}
+
+__global__ void k_flexd_zcopy(const int* __restrict__ ctl, const float* __restrict__ z,
+                              float* __restrict__ Z, size_t n)
+{
+    if (ctl[1] != 0) return;
+    float* col = Z + (size_t)ctl[0] * n;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) col[i] = z[i];
+}
+
+// One thread: the Hessenberg column of step i = j + 1 from the two
+// projections and the norm, the previous rotations, the new rotation, rs,
+// the convergence test -- the arithmetic of the host loop of gmres_flex
+// (src/kronecker.f90:286-312 in the reference), in the same order and
+// without contraction, so that both drivers give the same bits.
+__global__ void k_flexd_givens(int* __restrict__ ctl, double* __restrict__ st, int im)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl[1] != 0) return;
+    const FlexLayout Lo(im);
+    const int i = ctl[0] + 1;
+    double* hh = st + Lo.hh;
+    double* c = st + Lo.cs;
+    double* sn = st + Lo.sn;
+    double* rs = st + Lo.rs;
+    const double* h1 = st + Lo.h1;
+    const double* h2 = st + Lo.h2;
+    auto HH = [&](int r, int k) -> double& { return hh[(size_t)k * (im + 1) + r]; };
+    for (int jj = 0; jj < i; ++jj) HH(jj, i - 1) = __dadd_rn(h1[jj], h2[jj]);
+    double t = sqrt(st[Lo.nrm]);
+    if (!isfinite(t)) {
+        ctl[1] = 4;
+        return;
+    }
+    HH(i, i - 1) = t;
+    st[Lo.tinv] = (t != 0.0) ? 1.0 / t : 0.0;
+    for (int k = 2; k <= i; ++k) {
+        const int k1 = k - 1;
+        t = HH(k1 - 1, i - 1);
+        HH(k1 - 1, i - 1) = __dadd_rn(__dmul_rn(c[k1 - 1], t), __dmul_rn(sn[k1 - 1], HH(k - 1, i - 1)));
+        HH(k - 1, i - 1) = __dadd_rn(__dmul_rn(-sn[k1 - 1], t), __dmul_rn(c[k1 - 1], HH(k - 1, i - 1)));
+    }
+    double gam = sqrt(__dadd_rn(__dmul_rn(HH(i - 1, i - 1), HH(i - 1, i - 1)),
+                                __dmul_rn(HH(i, i - 1), HH(i, i - 1))));
+    if (gam == 0.0) gam = 1.0e-16;
+    c[i - 1] = HH(i - 1, i - 1) / gam;
+    sn[i - 1] = HH(i, i - 1) / gam;
+    rs[i] = __dmul_rn(-sn[i - 1], rs[i - 1]);
+    rs[i - 1] = __dmul_rn(c[i - 1], rs[i - 1]);
+    HH(i - 1, i - 1) = __dadd_rn(__dmul_rn(c[i - 1], HH(i - 1, i - 1)), __dmul_rn(sn[i - 1], HH(i, i - 1)));
+    const double ro = fabs(rs[i]);
+    st[Lo.ro] = ro;
+    const int its = ctl[2] + 1;
+    ctl[2] = its;
+    ctl[0] = i;
+    if (!(i < im && ro > st[Lo.eps1] && its < ctl[3])) ctl[1] = 1;
+}
+
+// V column j (the new one) = w / t, as df_scale: the FP64 factor split into
+// (hi, lo) FP32 values; unscaled when t = 0.
+__global__ void k_flexd_scale_copy(const int* __restrict__ ctl, const double* __restrict__ st,
+                                   size_t tinv_at, const float2* __restrict__ w,
+                                   float2* __restrict__ V, size_t nl, size_t n)
+{
+    if (ctl[1] != 0) return;
+    const double a = st[tinv_at];
+    const float ah = (float)a, al = (float)(a - (double)ah);
+    float2* col = V + (size_t)ctl[0] * nl;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 v = w[i];
+        if (a == 0.0) {
+            col[i] = v;
+        } else {
+            float h = 0.0f, l = 0.0f;
+            df_mul_acc(h, l, v.x, v.y, ah, al);
+            col[i] = df_norm(h, l);
+        }
+    }
+}
+
+// One thread: y = H^-1 rs over the cycle's i = ctl[0] steps by back
+// substitution, as the host loop does.
+__global__ void k_flexd_solve(const int* __restrict__ ctl, double* __restrict__ st, int im)
+{
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const FlexLayout Lo(im);
+    const int i = ctl[0];
+    if (i < 1) return;
+    const double* hh = st + Lo.hh;
+    const double* rs = st + Lo.rs;
+    double* y = st + Lo.y;
+    auto HH = [&](int r, int k) { return hh[(size_t)k * (im + 1) + r]; };
+    for (int k = 0; k < i; ++k) y[k] = rs[k];
+    y[i - 1] = y[i - 1] / HH(i - 1, i - 1);
+    for (int ii = 2; ii <= i; ++ii) {
+        const int k = i - ii + 1;
+        double t = y[k - 1];
+        for (int j = k + 1; j <= i; ++j) t = __dsub_rn(t, __dmul_rn(HH(k - 1, j - 1), y[j - 1]));
+        y[k - 1] = t / HH(k - 1, k - 1);
+    }
 }
 
 // acc := acc - (a + b) v for acc = hi + lo held as two FP32 values: the
@@ -657,7 +834,7 @@ int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, R
     // about eight resident blocks per SM over all chunks: row blocks shrink
     // as k grows, so each block's rows outweigh its block reduction
     const int nchunk = (k + kChunk - 1) / kChunk;
-    const int nb = std::max(38, std::min(r.nblocks, (8 * 152 + nchunk - 1) / nchunk));
+    const int nb = df_dot_blocks(k, r.nblocks);
     dim3 grid(nb, nchunk);
     k_multi_dot_df<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                              reinterpret_cast<const float4*>(w), n / 2,
@@ -675,7 +852,7 @@ int df_update_and_dot(const float2* V, size_t ld, int k, const double* h, float2
     if (n % 2 || ld % 2) { set_error("df_update: n and ld must be even"); return XT_ERR_ARG; }
     k_update_df<false><<<grid_for(n / 2), kThreads, 0, s>>>(
         reinterpret_cast<const float4*>(V), ld / 2, k, h, reinterpret_cast<float4*>(w), n / 2,
-        nullptr);
+        nullptr, nullptr);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return df_multi_dot(V, ld, k, w, n, r, s);
@@ -688,7 +865,7 @@ int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float
     const int nb = r.nblocks;
     k_update_df<true><<<nb, 2 * kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                                   h, reinterpret_cast<float4*>(w), n / 2,
-                                                  r.partial.p);
+                                                  r.partial.p, nullptr);
     k_finish_df<<<1, kThreads, 0, s>>>(r.partial.p, nb, r.out.p);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
@@ -723,6 +900,73 @@ int df_scale(float2* y, double a, size_t n, cudaStream_t s)
 {
     const float ah = (float)a;
     k_df_scale<<<grid_for(n), kThreads, 0, s>>>(y, ah, (float)(a - (double)ah), n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_hi(const int* ctl, const float2* V, size_t nl, float* d, size_t n, cudaStream_t s)
+{
+    k_flexd_hi<<<grid_for(n), kThreads, 0, s>>>(ctl, V, nl, d, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_zcopy(const int* ctl, const float* z, float* Z, size_t n, cudaStream_t s)
+{
+    k_flexd_zcopy<<<grid_for(n), kThreads, 0, s>>>(ctl, z, Z, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st, int im,
+               Reduce& r, cudaStream_t s)
+{
+    if (im > r.kmax) { set_error("flexd_orth: restart length exceeds reduction capacity"); return XT_ERR_ARG; }
+    if (nl % 2) { set_error("flexd_orth: the basis stride must be even"); return XT_ERR_ARG; }
+    const FlexLayout Lo(im);
+    // the most blocks any k <= im asks for (blocks past it return at once)
+    int grid = 1;
+    for (int k = 1; k <= im; ++k)
+        grid = std::max(grid, df_dot_blocks(k, r.nblocks) * ((k + kChunk - 1) / kChunk));
+    const float4* V4 = reinterpret_cast<const float4*>(V);
+    float4* w4 = reinterpret_cast<float4*>(w);
+    const size_t n2 = nl / 2;
+    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
+    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h1, ctl, 0);
+    k_update_df<false><<<grid_for(n2), kThreads, 0, s>>>(V4, n2, 0, st + Lo.h1, w4, n2, nullptr, ctl);
+    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
+    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h2, ctl, 0);
+    k_update_df<true><<<r.nblocks, 2 * kThreads, 0, s>>>(V4, n2, 0, st + Lo.h2, w4, n2,
+                                                         r.partial.p, ctl);
+    k_finish_df_ctl<<<1, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.nrm, ctl, 1);
+    note_launches(7);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_givens(int* ctl, double* st, int im, cudaStream_t s)
+{
+    k_flexd_givens<<<1, 32, 0, s>>>(ctl, st, im);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, float2* V,
+                     size_t nl, size_t n, cudaStream_t s)
+{
+    k_flexd_scale_copy<<<grid_for(n), kThreads, 0, s>>>(ctl, st, FlexLayout(im).tinv, w, V, nl, n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s)
+{
+    k_flexd_solve<<<1, 32, 0, s>>>(ctl, st, im);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

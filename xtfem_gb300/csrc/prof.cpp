@@ -97,6 +97,19 @@ void prof_end(int token, cudaStream_t s)
     it->second.ended = true;
 }
 
+void prof_cancel(int token)
+{
+    if (token < 0) return;
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_open.find(token);
+    if (it == g_open.end()) return;
+    // the events may still be pending on the stream: wait before reusing them
+    if (it->second.ended) cudaEventSynchronize(it->second.b);
+    g_pool.push_back(it->second.a);
+    g_pool.push_back(it->second.b);
+    g_open.erase(it);
+}
+
 void prof_bytes(int token, double bytes)
 {
     if (token < 0) return;

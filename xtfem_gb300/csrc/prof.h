@@ -14,5 +14,8 @@ void prof_end(int token, cudaStream_t s);
 // Algorithmic bytes of the timed launch (summed per class; bench.py divides
 // them by the summed time).  No-op for token -1.
 void prof_bytes(int token, double bytes);
+// Drops a record (a launch that turned out to have nothing to do: a step
+// issued past the end of a device-driven GMRES cycle).  No-op for -1.
+void prof_cancel(int token);
 
 }  // namespace xt

@@ -15,6 +15,8 @@
 #include "prof.h"
 
 #include <cmath>
+#include <cstdlib>
+#include <algorithm>
 #include <string>
 #include <cstring>
 #include <mutex>
@@ -574,6 +576,131 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     return XT_OK;
 }
 
+// The flexible GMRES above with its Arnoldi bookkeeping on the device: the
+// host issues the steps of a cycle in chunks and reads the step control
+// once per chunk instead of the Hessenberg column once per step.  A step is
+// the same kernels on fixed buffers: the hi part of basis column j, the
+// FP32 ILU into zfix (copied to Z column j), the double-float operator into
+// wfix, the CGS2 passes on wfix against columns 0..j (k read on the
+// device, the row blocks and reduction order of the host-driven passes),
+// the rotations and the convergence test (k_flexd_givens, the host loop's
+// arithmetic), and wfix scaled into column j + 1.  Steps issued past the
+// end of a cycle do nothing but launch, and their profile records are
+// dropped.  The result equals gmres_flex's bit for bit.
+int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
+                   GmresStats& st)
+{
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    const size_t nl = n + (n & 1);
+    float2* V = reinterpret_cast<float2*>(S.V64.p);
+    float* Z = S.Z32.p;
+    if (nl != n) XT_CUDA(cudaMemsetAsync(V, 0, (size_t)(im + 1) * nl * sizeof(float2), s));
+    const FlexLayout Lo(im);
+    XT_TRY(S.fst.alloc(Lo.total));
+    XT_TRY(S.fctl.alloc(4));
+    XT_TRY(S.zfix.alloc(n));
+    XT_TRY(S.wfix.alloc(nl));
+    XT_CUDA(cudaMemsetAsync(S.wfix.p, 0, nl * sizeof(float2), s));  // the pad entry stays 0
+    int* ctl = S.fctl.p;
+    double* dst = S.fst.p;
+    const int chunk = [] {  // steps issued between two reads of the control
+        const char* e = std::getenv("XTFEM_GMRES_CHUNK");
+        const int v = e ? std::atoi(e) : 16;
+        return v > 0 ? v : 16;
+    }();
+    std::vector<double> hbuf(2), rs(im + 1, 0.0);
+    int its = 0, i = 0, ierr = 0;
+    double ro = 0.0, eps1 = 0.0;
+    XT_TRY(norm2<double>(rhs, n, S.red, s));
+    XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
+    const double ro0 = std::sqrt(hbuf[0]);
+    for (;;) {
+        XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
+        XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
+        XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
+        ro = std::sqrt(hbuf[0]);
+        if (!std::isfinite(ro)) {
+            set_error("gmres: non-finite residual");
+            return XT_ERR_NONFINITE;
+        }
+        if (ro == 0.0) { ierr = -1; break; }
+        XT_TRY(df_from_f64(S.w64.p, V, n, s));
+        XT_TRY(df_scale(V, 1.0 / ro, n, s));
+        if (its == 0) eps1 = eps * ro;
+        // cycle state: rs = (ro, 0, ...), eps1, control {j = 0, running, its, maxits}
+        std::fill(rs.begin(), rs.end(), 0.0);
+        rs[0] = ro;
+        const int hctl[4] = {0, 0, its, maxits};
+        XT_CUDA(cudaMemcpyAsync(dst + Lo.rs, rs.data(), (im + 1) * sizeof(double),
+                                cudaMemcpyHostToDevice, s));
+        XT_CUDA(cudaMemcpyAsync(dst + Lo.eps1, &eps1, sizeof(double), cudaMemcpyHostToDevice, s));
+        XT_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(hctl), cudaMemcpyHostToDevice, s));
+        ++st.cycles;
+        int issued = 0, status = 0, j = 0;
+        int rctl[4] = {0, 0, 0, 0};
+        while (status == 0 && issued < im) {
+            const int nstep = std::min(chunk, im - issued);
+            std::vector<int> tok((size_t)3 * nstep, -1);
+            for (int k = 0; k < nstep; ++k) {
+                XT_TRY(flexd_hi(ctl, V, nl, S.d32.p, n, s));
+                tok[3 * k] = prof_begin(PROF_ILU32, s);
+                XT_TRY(ilu_apply<float>(*S.ilu, S.q, S.Ainv.p, S.d32.p, S.zfix.p, S.w32.p, s,
+                                        ctl + 1));
+                prof_end(tok[3 * k], s);
+                XT_TRY(flexd_zcopy(ctl, S.zfix.p, Z, n, s));
+                tok[3 * k + 1] = prof_begin(PROF_KRONDF, s);
+                XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, S.zfix.p, S.wfix.p, s, ctl + 1));
+                prof_end(tok[3 * k + 1], s);
+                tok[3 * k + 2] = prof_begin(PROF_ORTH64, s);
+                XT_TRY(flexd_orth(ctl, V, nl, S.wfix.p, dst, im, S.red, s));
+                XT_TRY(flexd_givens(ctl, dst, im, s));
+                XT_TRY(flexd_scale_copy(ctl, dst, im, S.wfix.p, V, nl, n, s));
+                prof_end(tok[3 * k + 2], s);
+            }
+            issued += nstep;
+            XT_CUDA(cudaMemcpyAsync(rctl, ctl, sizeof(rctl), cudaMemcpyDeviceToHost, s));
+            XT_CUDA(cudaStreamSynchronize(s));
+            // steps of this chunk that ran: each advanced j by one
+            const int ran = rctl[0] - j;
+            for (int k = 0; k < nstep; ++k) {
+                if (k < ran) {
+                    prof_bytes(tok[3 * k + 2], (4.0 * (j + k + 1) + 6.0) * (double)nl * 8.0);
+                } else {
+                    for (int c = 0; c < 3; ++c) prof_cancel(tok[3 * k + c]);
+                }
+            }
+            j = rctl[0];
+            status = rctl[1];
+        }
+        if (status == 4) {
+            set_error("gmres: non-finite Krylov vector");
+            return XT_ERR_NONFINITE;
+        }
+        i = j;
+        its = rctl[2];
+        XT_CUDA(cudaMemcpyAsync(&ro, dst + Lo.ro, sizeof(double), cudaMemcpyDeviceToHost, s));
+        XT_TRY(flexd_solve(ctl, dst, im, s));
+        XT_TRY((lincomb<float, double>(Z, n, i, dst + Lo.y, S.u64.p, n, s)));
+        XT_TRY((axpby<double, double>(n, 1.0, S.u64.p, 1.0, sol, s)));
+        XT_CUDA(cudaStreamSynchronize(s));
+        if (ro <= eps1) { ierr = 0; break; }
+        if (its >= maxits) { ierr = 1; break; }
+    }
+    st.its += its;
+    st.ierr = ierr;
+    st.est = ro0 > 0 ? ro / ro0 : 0.0;
+    return XT_OK;
+}
+
+// XTFEM_DEVICE_GMRES=0 selects the host-driven flexible GMRES
+bool device_gmres_on()
+{
+    const char* e = std::getenv("XTFEM_DEVICE_GMRES");
+    return !e || std::atoi(e) != 0;
+}
+
 }  // namespace
 
 int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int maxits,
@@ -652,7 +779,10 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
             XT_TRY((axpby<float, double>(n, rn, S.d32.p, 1.0, x, s)));
         } else if (inner == 2) {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
-            XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
+            if (!S.op16 && device_gmres_on())
+                XT_TRY(gmres_flex_dev(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
+            else
+                XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
             XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
         } else {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));

@@ -42,6 +42,12 @@ struct System {
     int im_cap = 0;
     bool op16 = false;  // FP32 inner operator reads BF16-stored K and M (mode 3)
     long long nest_its = 0;  // inner iterations of the last mode-3 solve
+    // device-driven flexible GMRES: step control, cycle state, the fixed
+    // preconditioned and operator vectors of a step, host copy of the control
+    DBuf<int> fctl;
+    DBuf<double> fst;
+    DBuf<float> zfix;
+    DBuf<float2> wfix;
     DBuf<double> V64, z64, w64, u64;
     DBuf<float> V32, z32, w32, u32, d32, r32;
     DBuf<float> Z32;  // flexible GMRES: preconditioned basis, im columns

@@ -159,7 +159,7 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
 // accuracy at FP32 throughput.  Makes the double-float copies of the CSR
 // values on first use.
 int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,
-                 float2* y, cudaStream_t s);
+                 float2* y, cudaStream_t s, const int* skip = nullptr);
 
 // The same operator with K and M stored in BF16, FP32 vectors and FP32
 // accumulation (the BF16-stored experiment of precision mode 3).
@@ -208,9 +208,11 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
 // inverse temporal matrix is applied to v first (it commutes with the
 // spatial solve), then the forward and backward sweeps.  dAinv is q x q
 // column-major FP64 on the device.  work has n*q entries.
+// skip (optional, device): when skip[0] is non-zero the FP32 register
+// sweep does nothing (a step past the end of a device-driven GMRES cycle).
 template <class T>
 int ilu_apply(const DevIlu& F, int q, const double* dAinv, const T* v, T* z, T* work,
-              cudaStream_t s);
+              cudaStream_t s, const int* skip = nullptr);
 
 // Reads and clears the device-side error word of the staged sweeps (a
 // bounded wait that gave up); XT_OK when clear.
@@ -224,6 +226,41 @@ struct Reduce {
     int nblocks = 0, kmax = 0;
 };
 int reduce_init(Reduce& r, int kmax);
+
+// ----------------------------------- device-driven flexible GMRES steps
+// Layout of the device state of one cycle (doubles): the (im+1) x im
+// Hessenberg matrix (column-major), the rotations, rs, the two projections
+// of the new vector, its squared norm, eps1, 1/t, the residual estimate and
+// the solution y of the small triangular system.
+struct FlexLayout {
+    size_t hh, cs, sn, rs, h1, h2, nrm, eps1, tinv, ro, y, total;
+    __host__ __device__ explicit FlexLayout(int im)
+    {
+        const size_t m = (size_t)im;
+        hh = 0;
+        cs = (m + 1) * m;
+        sn = cs + m;
+        rs = sn + m;
+        h1 = rs + m + 1;
+        h2 = h1 + m;
+        nrm = h2 + m;
+        eps1 = nrm + 1;
+        tinv = eps1 + 1;
+        ro = tinv + 1;
+        y = ro + 1;
+        total = y + m;
+    }
+};
+// ctl = {j, status, its, maxits} on the device (see dev_krylov.cu)
+int flexd_hi(const int* ctl, const float2* V, size_t nl, float* d, size_t n, cudaStream_t s);
+int flexd_zcopy(const int* ctl, const float* z, float* Z, size_t n, cudaStream_t s);
+int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st, int im,
+               Reduce& r, cudaStream_t s);
+int flexd_givens(int* ctl, double* st, int im, cudaStream_t s);
+int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, float2* V,
+                     size_t nl, size_t n, cudaStream_t s);
+int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s);
+
 
 // h[j] = <V_j, w> for j < k (V column-major, column stride ld), FP64
 // accumulation; result in r.out (device).
