@@ -18,12 +18,14 @@ an estimated relative residual of 1e-10.
 Checked every slab: the set of elements deleted is the oracle's; the
 displacement agrees to 1e-6 (relative L2) and the damage to 1e-6 absolute
 until the first deletion, and the points at or past the critical damage
-are the oracle's after every slab.  After it (measured on a GB300, with margin):
-the rod stays within 1e-8 of the oracle's damage; on the notched plate the
-deleted tip elements leave a badly conditioned system, on which a 1e-8
-residual pins the displacement only to about 1e-2 and the damage to about
-3e-3 -- the reference's own GMRES at 1e-8 moves that far from itself at
-1e-12 (tests/test_oracle_loop_tolerance.py) -- so the bound there is 1e-2.
+are the oracle's.  After it (measured on a GB300, with margin): the rod
+stays within 1e-8 of the oracle's damage; on the notched plate the deleted
+tip elements leave a badly conditioned system, on which a 1e-8 residual
+pins the displacement only to about 1e-2 and the damage to about 3e-3 --
+the reference's own GMRES at 1e-8 moves that far from itself at 1e-12
+(tests/test_oracle_loop_tolerance.py) -- so the bound there is 1e-2, and a
+point may sit on the other side of the critical damage only within that
+distance of it.
 """
 import numpy as np
 import pytest
@@ -51,11 +53,15 @@ def sent_case(xt):
 def sent_r01_case(xt):
     """The notched plate under tension-tension cycling, load ratio 0.1
     (a mean load of 1.22 times the sine amplitude): two tip elements fail
-    after the third slab.  The loop stops after the fourth: with the tip
-    gone its neighbours' damage runs away (the law is unstable past D = 1,
-    which only a deletion threshold above 1 would let a point keep), and at
-    a higher load the next slab's system is too badly conditioned for a
-    converged solve -- the oracle's GMRES stops at maxits too."""
+    after the third slab and are deleted at the start of the fourth.  Under
+    a mean load the slab ends at a large static displacement; the deletion
+    constrains the nodes it frees to zero from there, and the jump drives
+    the damage of almost every point past D = 1 during the fourth slab, in
+    the oracle's loop as in the device loop (the reference's load is a
+    fully reversed sine, which ends each slab near zero displacement).  So
+    the fourth slab is compared by its deletions and displacement only, and
+    the loop stops there: the next slab's system is too badly conditioned
+    for a converged solve -- the oracle's GMRES stops at maxits too."""
     make, cfg, n = sent_case(xt)
     return make, dict(cfg, amplitude=100.0, load_ratio=0.1), n
 
@@ -93,6 +99,11 @@ def run_pair(xt, orc, case, precision, tol=None):
 # (mixed), where the oracle alone at 1e-8 differs from itself at 1e-12 by
 # 3.2e-3.
 POST_DELETION = {"rod": 1e-6, "sent": 1e-2, "sent_r01": 1e-2}
+# relative L2 displacement bound after the first deletion (measured: notched
+# plate 4.5e-3 in FP64 at the deletion slab, 9e-6 at R = 0.1)
+POST_DELETION_DISP = {"rod": 1e-4, "sent": 1e-2, "sent_r01": 1e-2}
+# the slab whose damage runs away in both loops (sent_r01_case)
+RUNAWAY = {"sent_r01": 4}
 
 
 def r_dc(case, xt):
@@ -121,12 +132,25 @@ def test_slab_loop_matches_oracle_loop(xt, orc, case, precision):
         dD = np.max(np.abs(got["D"] - r["D"])[live], initial=0.0)
         print(f"{case} p{precision} slab {k + 1}: deleted {len(r['deleted_orc'])}, "
               f"|du|/|u| {du:.2e}, |dD| {dD:.2e}, points past D = 1: {int((~live).sum())}")
-        # the next slab's deletion check sees the same failed points
-        assert np.array_equal(got["D"] >= r_dc(case, xt), r["D"] >= r_dc(case, xt)), k
+        dc = r_dc(case, xt)
+        failed_got, failed_orc = got["D"] >= dc, r["D"] >= dc
         if not seen_deletion:
+            # the next slab's deletion check sees the same failed points
+            assert np.array_equal(failed_got, failed_orc), k
             assert du <= 1e-6, (k, du)
             assert dD <= 1e-6, (k, dD)
             assert np.max(np.abs(got["ws"] - r["ws"])) <= 1e-6 * max(1.0, r["ws"].max()), k
-        else:
-            assert dD <= POST_DELETION[case], (k, dD)
+            continue
+        assert du <= POST_DELETION_DISP[case], (k, du)
+        if RUNAWAY.get(case) == k + 1:
+            # both loops' damage has left [0, 1) at almost every point
+            for d in (r["D"], got["D"]):
+                assert np.mean((d < 0.0) | (d >= 1.0)) > 0.5, k
+            continue
+        assert dD <= POST_DELETION[case], (k, dD)
+        # after a deletion the damage agrees to POST_DELETION: a point may
+        # fall on the other side of Dc only within that distance of it (the
+        # next slab's deletions are compared exactly above)
+        differ = failed_got != failed_orc
+        assert np.all(np.abs(r["D"][differ] - dc) <= POST_DELETION[case]), (k, int(differ.sum()))
     assert total > 0

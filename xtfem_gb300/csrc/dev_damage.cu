@@ -39,6 +39,7 @@ constexpr double CY = 1740.0, HH = 0.2, SD = 0.5, SEXP = 0.5, SIGF = 180.0, SIGU
                  EPSD = 0.08;
 constexpr double WD = (SIGU - SIGF) * EPSD;
 constexpr int kNtChunk = 1024;  // temporal points per shared-memory chunk
+constexpr int kRun = 32;        // steps proven elastic by one bound
 
 struct Mat {
     double nu, E, ca, cb, G, Kb, coef;
@@ -174,7 +175,7 @@ __device__ void corrector(const Mat& m, const double eps[6], State& st)
 // teq^2.
 __device__ void screen_setup(const Mat& m, const State& st, const double E[6][6],
                              const float* __restrict__ ntmax, float G[6][6], float C0[6],
-                             float& err2)
+                             float& err2, float ecomp[6])
 {
     const double d = st.d;
     const double c1 = 1.0 / (1.0 - m.cb * d);
@@ -206,6 +207,7 @@ __device__ void screen_setup(const Mat& m, const State& st, const double E[6][6]
     for (int i = 0; i < 6; ++i) {
         const double w = i < 3 ? 1.5 : 3.0;
         const double ei = u * S[i];
+        ecomp[i] = (float)(ei * 1.0001);
         e2 += w * (2.0 * S[i] * ei + ei * ei);
         tot += w * S[i] * S[i];
     }
@@ -223,12 +225,13 @@ struct Slow {
 struct Screen {
     float G[6][6];
     float C0[6];
+    float e[6];  // bound on each screened component's error
     float err2;
 };
 
 __device__ __noinline__ void slow_screen(const Slow* s, const float* __restrict__ ntmax, Screen* sc)
 {
-    screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+    screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2, sc->e);
 }
 
 __device__ __forceinline__ void strain_at(const Slow* s, const double* __restrict__ Nt, int jj,
@@ -269,7 +272,7 @@ __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, in
         for (int i = 0; i < 6; ++i) { s->st.sef[i] = tse[i]; s->st.epo[i] = eps[i]; }
         s->st.sigd = teq;
         if (isinf(sc->err2)) {
-            screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2);
+            screen_setup(s->m, s->st, s->E, ntmax, sc->G, sc->C0, sc->err2, sc->e);
             return 2;
         }
         return 0;
@@ -337,13 +340,16 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
 
     Screen sc;
     slow_screen(&s, ntmax, &sc);
-    float G[6][6], C0[6], err2;
+    float G[6][6], C0[6], ecomp[6], err2;
 #pragma unroll
     for (int k = 0; k < 6; ++k)
 #pragma unroll
         for (int i = 0; i < 6; ++i) G[k][i] = sc.G[k][i];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) C0[i] = sc.C0[i];
+    for (int i = 0; i < 6; ++i) {
+        C0[i] = sc.C0[i];
+        ecomp[i] = sc.e[i];
+    }
     err2 = sc.err2;
     // proven elastic when q + err2 < sig_f^2 (margin covers the float add)
     const float thr = (float)(SIGF * SIGF) * 0.99999976f;
@@ -353,13 +359,63 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     // through shared memory in chunks, so each step's six values are a
     // broadcast shared-memory read instead of an L2 round trip.
     __shared__ float2 sNt[3 * kNtChunk];
+    __shared__ float sDel[kNtChunk / kRun][6];
     const float2* nt2 = reinterpret_cast<const float2*>(a.Nt32);
     for (int j0 = 0; j0 < a.nip; j0 += kNtChunk) {
     const int jn = min(kNtChunk, a.nip - j0);
     __syncthreads();
     for (int i = threadIdx.x; i < 3 * jn; i += blockDim.x) sNt[i] = __ldg(nt2 + 3 * (size_t)j0 + i);
     __syncthreads();
-    for (int jq = 0; jq < jn; ++jq) {
+    // Run bounds: delta_k >= |Nt_k(t) - Nt_k(t0)| of the FP64 table over each
+    // run of kRun steps from its first step t0.  The FP32 table differs from
+    // the FP64 one by at most u |Nt_k| <= u ntmax_k per entry (u = 2^-24),
+    // and the FP32 difference by one more rounding: inflated accordingly.
+    for (int t = threadIdx.x; t < (kNtChunk / kRun) * 8; t += blockDim.x) {
+        const int run = t >> 3, k = t & 7;
+        const int r0 = run * kRun;
+        if (k < 6 && r0 < jn) {
+            const float* f = reinterpret_cast<const float*>(sNt);
+            const float base = f[r0 * 6 + k];
+            float mx = 0.0f;
+            for (int j = r0 + 1; j < min(r0 + kRun, jn); ++j) mx = fmaxf(mx, fabsf(f[j * 6 + k] - base));
+            sDel[run][k] = mx * 1.000001f + __ldg(ntmax + k) * 2.4e-7f;
+        }
+    }
+    __syncthreads();
+    for (int jr = 0; jr < jn; jr += kRun) {
+    const int jre = min(jn, jr + kRun);
+    // One bound for the whole run (fresh screens only: a stale one has an
+    // infinite err2): with acc_i(t0) the screened component at the run's
+    // first step, every step of the run has |tsig_i| <= |acc_i(t0)| + e_i +
+    // sum_k delta_k |g_ki| =: B_i (g the FP64 coefficient, |g| <= |G|(1 +
+    // 1.01u); the FP32 sum of the six non-negative products is inflated by
+    // 16u for that and its own rounding), so teq^2 <= sum w_i B_i^2; that
+    // sum of non-negative FP32 terms is inflated by 2^-18 (64u) for its own
+    // rounding.  Below the threshold, every step of the run is elastic.
+    if (err2 < thr) {
+        const float2 t0 = sNt[3 * jr], t1 = sNt[3 * jr + 1], t2 = sNt[3 * jr + 2];
+        const float w[6] = {t0.x, t0.y, t1.x, t1.y, t2.x, t2.y};
+        float dl[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dl[k] = sDel[jr / kRun][k];
+        float qb = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            float acc = C0[i], dev = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                acc = fmaf(w[k], G[k][i], acc);
+                dev = fmaf(dl[k], fabsf(G[k][i]), dev);
+            }
+            const float b = fabsf(acc) + ecomp[i] + dev * 1.000001f;
+            qb = fmaf(i < 3 ? 1.5f : 3.0f, b * b, qb);
+        }
+        if (qb * 1.0000039f < thr) {
+            last_el = j0 + jre - 1;
+            continue;
+        }
+    }
+    for (int jq = jr; jq < jre; ++jq) {
         const int jj = j0 + jq;
         const float2 t0 = sNt[3 * jq], t1 = sNt[3 * jq + 1], t2 = sNt[3 * jq + 2];
         const float w[6] = {t0.x, t0.y, t1.x, t1.y, t2.x, t2.y};
@@ -387,10 +443,14 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
 #pragma unroll
                 for (int i = 0; i < 6; ++i) G[k][i] = sc.G[k][i];
 #pragma unroll
-            for (int i = 0; i < 6; ++i) C0[i] = sc.C0[i];
+            for (int i = 0; i < 6; ++i) {
+                C0[i] = sc.C0[i];
+                ecomp[i] = sc.e[i];
+            }
             err2 = sc.err2;
         }
         last_el = -1;
+    }
     }
     }
     if (last_el >= 0) slow_materialize(&s, a.Nt, last_el);

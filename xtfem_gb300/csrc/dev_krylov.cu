@@ -362,51 +362,72 @@ __global__ void k_flexd_zcopy(const int* __restrict__ ctl, const float* __restri
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) col[i] = z[i];
 }
 
-// One thread: the Hessenberg column of step i = j + 1 from the two
-// projections and the norm, the previous rotations, the new rotation, rs,
-// the convergence test -- the arithmetic of the host loop of gmres_flex
-// (src/kronecker.f90:286-312 in the reference), in the same order and
-// without contraction, so that both drivers give the same bits.
-__global__ void k_flexd_givens(int* __restrict__ ctl, double* __restrict__ st, int im)
+// The Hessenberg column of step i = j + 1 from the two projections and the
+// norm, the previous rotations, the new rotation, rs, the convergence test
+// -- the arithmetic of the host loop of gmres_flex (src/kronecker.f90:286-312
+// in the reference), in the same order and without contraction, so that both
+// drivers give the same bits.  The rotations are one dependent chain: the
+// block stages the column and the rotations in shared memory (kFlexdMaxIm + 1
+// entries each), one thread runs the chain from there, and the block writes
+// the column back.
+constexpr int kGivensMax = kFlexdMaxIm;
+
+__global__ void __launch_bounds__(128) k_flexd_givens(int* __restrict__ ctl,
+                                                      double* __restrict__ st, int im)
 {
-    if (threadIdx.x != 0 || blockIdx.x != 0 || ctl[1] != 0) return;
+    __shared__ double col[kGivensMax + 1], out[kGivensMax + 1], cs[kGivensMax], sn[kGivensMax];
+    __shared__ int bad;
+    if (ctl[1] != 0) return;  // the same for every thread of the block
     const FlexLayout Lo(im);
     const int i = ctl[0] + 1;
-    double* hh = st + Lo.hh;
-    double* c = st + Lo.cs;
-    double* sn = st + Lo.sn;
-    double* rs = st + Lo.rs;
-    const double* h1 = st + Lo.h1;
-    const double* h2 = st + Lo.h2;
-    auto HH = [&](int r, int k) -> double& { return hh[(size_t)k * (im + 1) + r]; };
-    for (int jj = 0; jj < i; ++jj) HH(jj, i - 1) = __dadd_rn(h1[jj], h2[jj]);
-    double t = sqrt(st[Lo.nrm]);
-    if (!isfinite(t)) {
-        ctl[1] = 4;
-        return;
+    for (int jj = threadIdx.x; jj < i; jj += blockDim.x) {
+        col[jj] = __dadd_rn(st[Lo.h1 + jj], st[Lo.h2 + jj]);
+        if (jj < i - 1) {
+            cs[jj] = st[Lo.cs + jj];
+            sn[jj] = st[Lo.sn + jj];
+        }
     }
-    HH(i, i - 1) = t;
-    st[Lo.tinv] = (t != 0.0) ? 1.0 / t : 0.0;
-    for (int k = 2; k <= i; ++k) {
-        const int k1 = k - 1;
-        t = HH(k1 - 1, i - 1);
-        HH(k1 - 1, i - 1) = __dadd_rn(__dmul_rn(c[k1 - 1], t), __dmul_rn(sn[k1 - 1], HH(k - 1, i - 1)));
-        HH(k - 1, i - 1) = __dadd_rn(__dmul_rn(-sn[k1 - 1], t), __dmul_rn(c[k1 - 1], HH(k - 1, i - 1)));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = sqrt(st[Lo.nrm]);
+        bad = !isfinite(t);
+        if (!bad) {
+            col[i] = t;
+            st[Lo.tinv] = (t != 0.0) ? 1.0 / t : 0.0;
+            // rotation k1 = k - 1 maps entries (k1 - 1, k - 1); the carry is
+            // the rotated entry k - 1, which the next rotation takes as t
+            double carry = col[0];
+            for (int k = 2; k <= i; ++k) {
+                const double c = cs[k - 2], s = sn[k - 2], h = col[k - 1];
+                out[k - 2] = __dadd_rn(__dmul_rn(c, carry), __dmul_rn(s, h));
+                carry = __dadd_rn(__dmul_rn(-s, carry), __dmul_rn(c, h));
+            }
+            const double hd = carry, hs = t;
+            double gam = sqrt(__dadd_rn(__dmul_rn(hd, hd), __dmul_rn(hs, hs)));
+            if (gam == 0.0) gam = 1.0e-16;
+            const double cn = hd / gam, snn = hs / gam;
+            st[Lo.cs + i - 1] = cn;
+            st[Lo.sn + i - 1] = snn;
+            double* rs = st + Lo.rs;
+            const double r = rs[i - 1];
+            rs[i] = __dmul_rn(-snn, r);
+            rs[i - 1] = __dmul_rn(cn, r);
+            out[i - 1] = __dadd_rn(__dmul_rn(cn, hd), __dmul_rn(snn, hs));
+            out[i] = hs;
+            const double ro = fabs(rs[i]);
+            st[Lo.ro] = ro;
+            const int its = ctl[2] + 1;
+            ctl[2] = its;
+            ctl[0] = i;
+            if (!(i < im && ro > st[Lo.eps1] && its < ctl[3])) ctl[1] = 1;
+        } else {
+            ctl[1] = 4;
+        }
     }
-    double gam = sqrt(__dadd_rn(__dmul_rn(HH(i - 1, i - 1), HH(i - 1, i - 1)),
-                                __dmul_rn(HH(i, i - 1), HH(i, i - 1))));
-    if (gam == 0.0) gam = 1.0e-16;
-    c[i - 1] = HH(i - 1, i - 1) / gam;
-    sn[i - 1] = HH(i, i - 1) / gam;
-    rs[i] = __dmul_rn(-sn[i - 1], rs[i - 1]);
-    rs[i - 1] = __dmul_rn(c[i - 1], rs[i - 1]);
-    HH(i - 1, i - 1) = __dadd_rn(__dmul_rn(c[i - 1], HH(i - 1, i - 1)), __dmul_rn(sn[i - 1], HH(i, i - 1)));
-    const double ro = fabs(rs[i]);
-    st[Lo.ro] = ro;
-    const int its = ctl[2] + 1;
-    ctl[2] = its;
-    ctl[0] = i;
-    if (!(i < im && ro > st[Lo.eps1] && its < ctl[3])) ctl[1] = 1;
+    __syncthreads();
+    if (bad) return;
+    double* hh = st + Lo.hh + (size_t)(i - 1) * (im + 1);
+    for (int jj = threadIdx.x; jj <= i; jj += blockDim.x) hh[jj] = out[jj];
 }
 
 // V column j (the new one) = w / t, as df_scale: the FP64 factor split into
@@ -949,7 +970,8 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
 
 int flexd_givens(int* ctl, double* st, int im, cudaStream_t s)
 {
-    k_flexd_givens<<<1, 32, 0, s>>>(ctl, st, im);
+    if (im > kGivensMax) { set_error("flexd_givens: restart length exceeds the device rotation buffer"); return XT_ERR_ARG; }
+    k_flexd_givens<<<1, 128, 0, s>>>(ctl, st, im);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

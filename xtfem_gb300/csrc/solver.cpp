@@ -466,6 +466,13 @@ int nested_prec(System& S, const float* v, float* z)
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
+    // XTFEM_CGS_PASSES=1: one classical Gram-Schmidt pass per Arnoldi step
+    // (two reads of the basis instead of four; the Hessenberg column is the
+    // one pass's projections)
+    const bool two_pass = [] {
+        const char* e = std::getenv("XTFEM_CGS_PASSES");
+        return !e || std::atoi(e) != 1;
+    }();
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     const size_t nl = n + (n & 1);  // basis column stride: even, zero pad when n is odd
@@ -517,13 +524,19 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             }
             const int otok = prof_begin(PROF_ORTH64, s);
             // as above, double-float values of 8 bytes
-            prof_bytes(otok, (4.0 * i + 6.0) * (double)nl * 8.0);
+            prof_bytes(otok, (two_pass ? 4.0 * i + 6.0 : 2.0 * i + 3.0) * (double)nl * 8.0);
             XT_TRY(df_multi_dot(V, nl, i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
-            XT_TRY(df_update_and_dot(V, nl, i, S.hsave.p, col(i1 - 1), nl, S.red, s));
-            XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, s));
+            if (two_pass) {
+                XT_TRY(df_update_and_dot(V, nl, i, S.hsave.p, col(i1 - 1), nl, S.red, s));
+                XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, s));
+            } else {
+                XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.hsave.p, i * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, s));
+                XT_CUDA(cudaMemsetAsync(S.hsave.p, 0, i * sizeof(double), s));
+            }
             XT_TRY(df_update_and_norm(V, nl, i, S.hsave.p + i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
@@ -694,11 +707,14 @@ int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps
     return XT_OK;
 }
 
-// XTFEM_DEVICE_GMRES=0 selects the host-driven flexible GMRES
+// XTFEM_DEVICE_GMRES=1 selects the device-driven flexible GMRES (measured
+// on the C2 rod and the rod batch: slower than the host-driven loop, whose
+// one host read per Arnoldi step costs less than the device path's extra
+// rotation, copy and control kernels)
 bool device_gmres_on()
 {
     const char* e = std::getenv("XTFEM_DEVICE_GMRES");
-    return !e || std::atoi(e) != 0;
+    return e && std::atoi(e) != 0;
 }
 
 }  // namespace
@@ -779,7 +795,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
             XT_TRY((axpby<float, double>(n, rn, S.d32.p, 1.0, x, s)));
         } else if (inner == 2) {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
-            if (!S.op16 && device_gmres_on())
+            if (!S.op16 && im <= kFlexdMaxIm && device_gmres_on())
                 XT_TRY(gmres_flex_dev(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
             else
                 XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));

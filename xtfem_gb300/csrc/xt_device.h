@@ -232,6 +232,10 @@ int reduce_init(Reduce& r, int kmax);
 // Hessenberg matrix (column-major), the rotations, rs, the two projections
 // of the new vector, its squared norm, eps1, 1/t, the residual estimate and
 // the solution y of the small triangular system.
+// the longest restart the device-driven flexible GMRES takes (its rotation
+// kernel stages a Hessenberg column in shared memory); longer ones run
+// host-driven
+constexpr int kFlexdMaxIm = 1024;
 struct FlexLayout {
     size_t hh, cs, sn, rs, h1, h2, nrm, eps1, tinv, ro, y, total;
     __host__ __device__ explicit FlexLayout(int im)
