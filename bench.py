@@ -36,7 +36,7 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = dict(nx=60, ny=20, nz=20, lx=3.0, ly=1.0, lz=1.0, E=2.0e5, nu=0.3, rho=7.8e-9,
                 freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256, lfil=20, droptol=1e-4, im=200,
-                tol=1e-8, inner_tol=1e-5, Dc=0.99, seed=0, precision=2, overlap=1)
+                tol=1e-8, inner_tol=1e-5, Dc=0.99, seed=0, precision=2, overlap=1, gs_passes=1)
 METRIC = "time-slab solves/s to rel.res 1e-8, mixed-prec batched vs FP64 GMRES, 1 GB300"
 UNIT = "slab-solves/s"
 DTYPE_NAMES = {0: "fp64", 1: "fp32 operator/factor/basis, fp64 residual+refinement+damage",
@@ -62,7 +62,7 @@ def make_config(xt, precision, seed):
                               nipc=w["nipc"], lfil=w["lfil"], droptol=w["droptol"], im=w["im"],
                               tol=w["tol"], maxits=4000, precision=precision,
                               inner_tol=w["inner_tol"], Dc=w["Dc"], damage=1, group=3,
-                              overlap=w["overlap"])
+                              overlap=w["overlap"], gs_passes=w["gs_passes"])
 
 
 def make_problem(xt):
@@ -596,7 +596,8 @@ def workload_config(amp):
     return {"workload": "C2 prismatic rod 20x20x60 C3D8, 80,703 DOF x 6 temporal blocks",
             "nip": WORKLOAD["nipc"] * WORKLOAD["n1"],
             "ilut": [WORKLOAD["droptol"], WORKLOAD["lfil"]],
-            "gmres_restart": WORKLOAD["im"], "tol": WORKLOAD["tol"], "amplitude_mpa": amp,
+            "gmres_restart": WORKLOAD["im"], "gram_schmidt_passes": WORKLOAD["gs_passes"],
+            "tol": WORKLOAD["tol"], "amplitude_mpa": amp,
             "l2": "inputs larger than L2 (operator+factor+basis >> 129 MB)",
             "parallelism": "replicas x1"}
 

@@ -133,6 +133,14 @@ typedef struct xt_slab_config {
                             with the weights of a load constant in time,
                             N_j(t1 + dt) - N_j(t1) = (-1, 0, 1, 0, 0, 0),
                             beside the sine weights of src/getfextc.f90. */
+    int gs_passes;       /* classical Gram-Schmidt passes per Arnoldi step of
+                            the flexible GMRES (precision 2 and 3): 2 (also
+                            for 0) or 1.  One pass reads the Krylov basis
+                            twice per step instead of four times; a solve
+                            with one pass switches to two for the rest of the
+                            solve when the true residual at a restart
+                            exceeds the estimate it followed tenfold (the
+                            basis has lost orthogonality). */
 } xt_slab_config;
 
 typedef struct xt_slab_s *xt_slab;

@@ -349,17 +349,20 @@ def test_bf16_stored_operator_under_refinement(xt, orc, rod_system):
     assert rel(sol, sol_ref) <= 1e-6
 
 
-@pytest.mark.parametrize("chunk", ["16", "1", "7"])
-def test_device_driven_gmres_equals_host_driven(xt, rod_system, monkeypatch, chunk):
+@pytest.mark.parametrize("chunk,passes", [("16", "2"), ("1", "2"), ("7", "2"), ("16", "1"),
+                                          ("5", "1")])
+def test_device_driven_gmres_equals_host_driven(xt, rod_system, monkeypatch, chunk, passes):
     """The flexible GMRES with its Arnoldi bookkeeping on the device (steps
     issued in chunks, the control read once per chunk) gives the host-driven
     loop's solution and statistics bit for bit, whatever the chunk size
-    (steps issued past the end of a cycle do nothing)."""
+    (steps issued past the end of a cycle do nothing), with one or two
+    Gram-Schmidt passes per step."""
     s = rod_system
     rhs = c1_rhs(xt, s)
     sysm = xt.SpaceTimeSystem(s["K"], s["M"])
     sysm.set_ilu(s["alu"], s["jlu"], s["ju"])
     sysm.set_temporal(s["A"], s["B"])
+    monkeypatch.setenv("XTFEM_CGS_PASSES", passes)
     monkeypatch.setenv("XTFEM_DEVICE_GMRES", "0")
     ref, info_ref = sysm.solve(rhs, im=30, tol=1e-10, maxits=3000, precision=2)
     monkeypatch.setenv("XTFEM_DEVICE_GMRES", "1")

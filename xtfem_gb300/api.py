@@ -510,14 +510,15 @@ class SlabConfig(C.Structure):
                 ("im", C.c_int), ("tol", C.c_double), ("maxits", C.c_int),
                 ("precision", C.c_int), ("inner_tol", C.c_double), ("Dc", C.c_double),
                 ("damage", C.c_int), ("group", C.c_int), ("overlap", C.c_int),
-                ("load_ratio", C.c_double)]
+                ("load_ratio", C.c_double), ("gs_passes", C.c_int)]
 
     @classmethod
     def make(cls, **kw):
         d = dict(clamp_axis=0, clamp_value=0.0, load_axis=0, load_value=3.0, load_comp=0,
                  amplitude=100.0, area=1.0, freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256,
                  lfil=20, droptol=1e-4, im=30, tol=1e-8, maxits=3000, precision=0,
-                 inner_tol=1e-5, Dc=0.99, damage=1, group=3, overlap=0, load_ratio=-1.0)
+                 inner_tol=1e-5, Dc=0.99, damage=1, group=3, overlap=0, load_ratio=-1.0,
+                 gs_passes=0)
         d.update(kw)
         return cls(**d)
 

@@ -26,6 +26,7 @@
 // before a plastic step, or before the slab ends, has to be evaluated).
 // Steps the screen cannot decide, and plastic steps, are evaluated exactly
 // in FP64 with the reference's operation order.
+#include <cstdlib>
 #include <mutex>
 
 #include "xt_device.h"
@@ -284,7 +285,7 @@ __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, in
 }
 
 __global__ void __launch_bounds__(256)
-k_damage(DamageArgs a, const float* __restrict__ ntmax)
+k_damage(DamageArgs a, const float* __restrict__ ntmax, int run_bound)
 {
     // Points are dealt to blocks round-robin (thread t of block b takes point
     // t * gridDim + b): plastic points cluster in space, i.e. in consecutive
@@ -392,7 +393,7 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax)
     // 16u for that and its own rounding), so teq^2 <= sum w_i B_i^2; that
     // sum of non-negative FP32 terms is inflated by 2^-18 (64u) for its own
     // rounding.  Below the threshold, every step of the run is elastic.
-    if (err2 < thr) {
+    if (run_bound && err2 < thr) {
         const float2 t0 = sNt[3 * jr], t1 = sNt[3 * jr + 1], t2 = sNt[3 * jr + 2];
         const float w[6] = {t0.x, t0.y, t1.x, t1.y, t2.x, t2.y};
         float dl[6];
@@ -652,7 +653,10 @@ int damage_update(const DamageArgs& a, cudaStream_t s)
         return XT_ERR_ARG;
     }
     k_ntmax<<<1, 1024, 0, s>>>(a.Nt32, a.nip, a.ntmax);
-    k_damage<<<(a.ngp + 255) / 256, 256, 0, s>>>(a, a.ntmax);
+    // XTFEM_DAMAGE_RUN=0: screen every step (no per-run bound)
+    const char* e = std::getenv("XTFEM_DAMAGE_RUN");
+    const int run_bound = (!e || std::atoi(e) != 0) ? 1 : 0;
+    k_damage<<<(a.ngp + 255) / 256, 256, 0, s>>>(a, a.ntmax, run_bound);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

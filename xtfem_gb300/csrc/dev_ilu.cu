@@ -1473,6 +1473,7 @@ constexpr unsigned kRegLaneTab = 640;
 struct RegTri {
     int nl = 0, ncw = 0, H = 0, smax = 0, slot_bytes = 0;
     int win_elems = 0, zero_off = 0;
+    bool w16 = false;  // 16-bit window byte offsets (window <= 64 KB)
     long long lanes = 0;  // nl * ncw * 32
     DBuf<unsigned char> slots;
     std::vector<int> row_slot;             // host: lane slot of each row's h = 0 lane
@@ -1549,16 +1550,19 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
 {
     const int g = 3, H = t.H, GS = 3 * H, GPW = 32 / GS;
     t.smax = smax;
-    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 4) * 1024u);
+    const unsigned ob = t.w16 ? 256u : 512u;  // bytes of one offset quad per warp
+    t.slot_bytes = (int)(kRegLaneTab + (unsigned)(smax / 4) * (ob + 512u));
     const size_t nslot = (size_t)t.nl * t.ncw;
     std::vector<unsigned char> blob(nslot * t.slot_bytes, 0);
     // every lane of every slot starts empty: no store, all steps on the zero slot
     for (size_t sl = 0; sl < nslot; ++sl) {
         unsigned char* b = blob.data() + sl * t.slot_bytes;
         const int none = -1;
-        unsigned* off = reinterpret_cast<unsigned*>(b + kRegLaneTab);
         for (int lane = 0; lane < 32; ++lane) std::memcpy(b + lane * 16 + 12, &none, 4);
-        for (int e = 0; e < (smax / 4) * 128; ++e) off[e] = (unsigned)t.zero_off * 4u;
+        for (int e = 0; e < (smax / 4) * 128; ++e) {
+            if (t.w16) reinterpret_cast<unsigned short*>(b + kRegLaneTab)[e] = (unsigned short)(t.zero_off * 4);
+            else reinterpret_cast<unsigned*>(b + kRegLaneTab)[e] = (unsigned)t.zero_off * 4u;
+        }
     }
     std::vector<int> seen(t.win_elems, 0);
     int epoch = 0;
@@ -1572,7 +1576,8 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
         float* gm = reinterpret_cast<float*>(b);
         int* go = reinterpret_cast<int*>(b + 512);
         unsigned* off = reinterpret_cast<unsigned*>(b + kRegLaneTab);
-        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * 512);
+        unsigned short* off16 = reinterpret_cast<unsigned short*>(b + kRegLaneTab);
+        float* val = reinterpret_cast<float*>(b + kRegLaneTab + (smax / 4) * ob);
         const auto& grp = t.chunks[c];
         for (int lane = 0; lane < 32; ++lane) {
             ent[lane].clear();
@@ -1624,7 +1629,9 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
                     seen[o] = epoch;
                     load[o & 31]++;
                 }
-                off[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = (unsigned)o * 4u;
+                const size_t oi = ((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3);
+                if (t.w16) off16[oi] = (unsigned short)(o * 4);
+                else off[oi] = (unsigned)o * 4u;
                 val[((size_t)(st >> 2) * 32 + lane) * 4 + (st & 3)] = v;
             }
         }
@@ -1657,6 +1664,11 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
     if (!reg_plan(S.L, H, *L) || !reg_plan(S.U, H, *U)) return XT_OK;
     const int smax = reg_smax(H, std::max(L->smax, U->smax));
     if (smax == 0) return XT_OK;
+    // 16-bit window offsets when every byte offset of both windows fits
+    // (XTFEM_ILU_W16=0: 32-bit)
+    const bool w16 = (long long)std::max(L->win_elems, U->win_elems) * 4 <= 65536 &&
+                     env_int("XTFEM_ILU_W16", 1) != 0;
+    L->w16 = U->w16 = w16;
     XT_TRY(reg_fill(S.U, *U, smax, Q, nullptr, s));
     XT_TRY(reg_fill(S.L, *L, smax, Q, &U->row_slot, s));
     if (!L->slots.p || !U->slots.p) return XT_OK;
@@ -1733,9 +1745,28 @@ __device__ __forceinline__ void level_barrier()
     asm volatile("bar.sync 0;" ::: "memory");
 }
 
-template <int SMAX>
+// Offsets of four steps: four 32-bit window byte offsets, or (W16) four
+// 16-bit ones packed in two words.
+template <bool W16> struct RegOff;
+template <> struct RegOff<false> {
+    uint4 o;
+    __device__ __forceinline__ unsigned at(int i) const
+    {
+        return i == 0 ? o.x : (i == 1 ? o.y : (i == 2 ? o.z : o.w));
+    }
+};
+template <> struct RegOff<true> {
+    uint2 o;
+    __device__ __forceinline__ unsigned at(int i) const
+    {
+        const unsigned w = i < 2 ? o.x : o.y;
+        return (i & 1) ? (w >> 16) : (w & 0xffffu);
+    }
+};
+
+template <int SMAX, bool W16>
 struct RegSet {
-    uint4 off[SMAX / 4];
+    RegOff<W16> off[SMAX / 4];
     float4 val[SMAX / 4];
     float4 gm;
     int go;
@@ -1744,29 +1775,38 @@ struct RegSet {
 
 // The slot at p (already offset to this warp's slot of the level) and the
 // right-hand side at bsrc.
-template <int SMAX>
-__device__ __forceinline__ void reg_load(RegSet<SMAX>& S, const unsigned char* p,
+__device__ __forceinline__ uint2 nc_v2u(const void* p)
+{
+    uint2 r;
+    asm volatile("ld.global.nc.v2.u32 {%0, %1}, [%2];" : "=r"(r.x), "=r"(r.y) : "l"(p));
+    return r;
+}
+
+template <int SMAX, bool W16>
+__device__ __forceinline__ void reg_load(RegSet<SMAX, W16>& S, const unsigned char* p,
                                          const float* bsrc, int lane)
 {
+    constexpr int ob = W16 ? 256 : 512;
     S.gm = nc_v4f(p + lane * 16);
     S.go = nc_i(p + 512 + lane * 4);
     S.b = nc_f(bsrc);
 #pragma unroll
     for (int k = 0; k < SMAX / 4; ++k) {
-        S.off[k] = nc_v4u(p + kRegLaneTab + k * 512 + lane * 16);
-        S.val[k] = nc_v4f(p + kRegLaneTab + (SMAX / 4) * 512 + k * 512 + lane * 16);
+        if constexpr (W16) S.off[k].o = nc_v2u(p + kRegLaneTab + k * 256 + lane * 8);
+        else S.off[k].o = nc_v4u(p + kRegLaneTab + k * 512 + lane * 16);
+        S.val[k] = nc_v4f(p + kRegLaneTab + (SMAX / 4) * ob + k * 512 + lane * 16);
     }
 }
 
-template <int H, int SMAX>
-__device__ __forceinline__ void reg_level(const RegSet<SMAX>& S, unsigned wbase, float* win,
+template <int H, int SMAX, bool W16>
+__device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned wbase, float* win,
                                           float* out, int lane0)
 {
     float acc0 = 0.0f, acc1 = 0.0f;
 #pragma unroll
     for (int k = 0; k < SMAX / 4; ++k) {
-        const float x0 = lds_f(wbase + S.off[k].x), x1 = lds_f(wbase + S.off[k].y);
-        const float x2 = lds_f(wbase + S.off[k].z), x3 = lds_f(wbase + S.off[k].w);
+        const float x0 = lds_f(wbase + S.off[k].at(0)), x1 = lds_f(wbase + S.off[k].at(1));
+        const float x2 = lds_f(wbase + S.off[k].at(2)), x3 = lds_f(wbase + S.off[k].at(3));
         acc0 = fmaf(S.val[k].x, x0, acc0);
         acc1 = fmaf(S.val[k].y, x1, acc1);
         acc0 = fmaf(S.val[k].z, x2, acc0);
@@ -1794,7 +1834,7 @@ constexpr int kRegMaxWarps3 = 12;
 // DEPTH register sets rotate through the levels: the set a level used is
 // reloaded, right after it, with the level DEPTH ahead, so a load has
 // DEPTH - 1 levels of work to land in.
-template <int H, int SMAX, bool UPPER, int DEPTH>
+template <int H, int SMAX, bool UPPER, int DEPTH, bool W16>
 __global__ void __launch_bounds__((DEPTH > 2 ? kRegMaxWarps3 : kRegMaxWarps) * 32, 1)
     k_tri_reg(RegArgs a)
 {
@@ -1824,10 +1864,10 @@ __global__ void __launch_bounds__((DEPTH > 2 ? kRegMaxWarps3 : kRegMaxWarps) * 3
         }
     };
     for (int L = DEPTH; L < DEPTH + a.pf; ++L) prefetch(L);
-    RegSet<SMAX> rs[DEPTH];
+    RegSet<SMAX, W16> rs[DEPTH];
 #pragma unroll
     for (int d = 0; d < DEPTH; ++d) {
-        if (d < a.nl) reg_load<SMAX>(rs[d], sp, bp, lane);
+        if (d < a.nl) reg_load<SMAX, W16>(rs[d], sp, bp, lane);
         sp += sstep;
         bp += a.ncw * 32;
     }
@@ -1836,8 +1876,8 @@ __global__ void __launch_bounds__((DEPTH > 2 ? kRegMaxWarps3 : kRegMaxWarps) * 3
 #pragma unroll
         for (int d = 0; d < DEPTH; ++d) {
             if (l + d < a.nl) {  // uniform over the block
-                reg_level<H, SMAX>(rs[d], wbase, rwin, out, lane0);
-                if (l + d + DEPTH < a.nl) reg_load<SMAX>(rs[d], sp, bp, lane);
+                reg_level<H, SMAX, W16>(rs[d], wbase, rwin, out, lane0);
+                if (l + d + DEPTH < a.nl) reg_load<SMAX, W16>(rs[d], sp, bp, lane);
                 prefetch(l + d + DEPTH + a.pf);
                 sp += sstep;
                 bp += a.ncw * 32;
@@ -1874,15 +1914,15 @@ __global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
     }
 }
 
-template <int Q, int H, int SMAX, int DEPTH>
+template <int Q, int H, int SMAX, int DEPTH, bool W16>
 int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
                const int* skip)
 {
     static std::atomic<bool> attr{false};
     if (!attr.load(std::memory_order_acquire)) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, DEPTH>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, DEPTH, W16>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, DEPTH>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, DEPTH, W16>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         attr.store(true, std::memory_order_release);
     }
@@ -1895,25 +1935,30 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
                L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
                skip};
-    k_tri_reg<H, SMAX, false, DEPTH><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
-    k_tri_reg<H, SMAX, true, DEPTH><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
+    k_tri_reg<H, SMAX, false, DEPTH, W16><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
+    k_tri_reg<H, SMAX, true, DEPTH, W16><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
 }
 
-// Three register sets where the registers allow (at most 12 warps and 12
-// steps per lane; XTFEM_ILU_DEPTH=2 keeps two).
+// Three register sets where the registers allow (16-bit offsets, at most 12
+// warps and 12 steps per lane; XTFEM_ILU_DEPTH=2 keeps two).
 template <int Q, int H, int SMAX>
 int launch_reg_depth(const IluStage& st, const double* dAinv, const float* v, float* z,
                      cudaStream_t s, const int* skip)
 {
+    if (st.regL->w16 != st.regU->w16) {
+        set_error("register sweep: triangles with different offset widths");
+        return XT_ERR_STATE;
+    }
+    if (!st.regL->w16) return launch_reg<Q, H, SMAX, 2, false>(st, dAinv, v, z, s, skip);
     if constexpr (SMAX <= 12) {
         if (std::max(st.regL->ncw, st.regU->ncw) <= kRegMaxWarps3 &&
             env_int("XTFEM_ILU_DEPTH", 3) >= 3)
-            return launch_reg<Q, H, SMAX, 3>(st, dAinv, v, z, s, skip);
+            return launch_reg<Q, H, SMAX, 3, true>(st, dAinv, v, z, s, skip);
     }
-    return launch_reg<Q, H, SMAX, 2>(st, dAinv, v, z, s, skip);
+    return launch_reg<Q, H, SMAX, 2, true>(st, dAinv, v, z, s, skip);
 }
 
 template <int Q>

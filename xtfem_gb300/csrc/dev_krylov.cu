@@ -943,7 +943,7 @@ int flexd_zcopy(const int* ctl, const float* z, float* Z, size_t n, cudaStream_t
 }
 
 int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st, int im,
-               Reduce& r, cudaStream_t s)
+               Reduce& r, cudaStream_t s, bool two_pass)
 {
     if (im > r.kmax) { set_error("flexd_orth: restart length exceeds reduction capacity"); return XT_ERR_ARG; }
     if (nl % 2) { set_error("flexd_orth: the basis stride must be even"); return XT_ERR_ARG; }
@@ -955,15 +955,22 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
     const float4* V4 = reinterpret_cast<const float4*>(V);
     float4* w4 = reinterpret_cast<float4*>(w);
     const size_t n2 = nl / 2;
-    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
-    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h1, ctl, 0);
-    k_update_df<false><<<grid_for(n2), kThreads, 0, s>>>(V4, n2, 0, st + Lo.h1, w4, n2, nullptr, ctl);
+    if (two_pass) {
+        k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
+        k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h1, ctl, 0);
+        k_update_df<false><<<grid_for(n2), kThreads, 0, s>>>(V4, n2, 0, st + Lo.h1, w4, n2, nullptr, ctl);
+        note_launches(3);
+    } else {
+        // one pass: the projections go to h2 and h1 stays zero, as the host
+        // loop's Hessenberg column 0 + h
+        XT_CUDA(cudaMemsetAsync(st + Lo.h1, 0, (size_t)im * sizeof(double), s));
+    }
     k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
     k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h2, ctl, 0);
     k_update_df<true><<<r.nblocks, 2 * kThreads, 0, s>>>(V4, n2, 0, st + Lo.h2, w4, n2,
                                                          r.partial.p, ctl);
     k_finish_df_ctl<<<1, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.nrm, ctl, 1);
-    note_launches(7);
+    note_launches(4);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
 }

@@ -286,6 +286,7 @@ int solve_slab(xt_slab_s& s, const double* fext_host, double* stats, bool check 
     // solve from zero
     XT_CUDA(cudaMemsetAsync(s.disp.p, 0, n * sizeof(double), st));
     GmresStats gs;
+    s.S.gs_passes = s.cfg.gs_passes == 1 ? 1 : 2;
     XT_TRY(solve_refined(s.S, s.fext.p, s.disp.p, s.cfg.im, s.cfg.tol, s.cfg.maxits, s.cfg.precision,
                          s.cfg.inner_tol, gs));
     XT_TRY(mask_rows<double>(s.disp.p, s.S.bcmask.p, s.p, s.q, st));
@@ -603,7 +604,7 @@ int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
         if (cfg->clamp_axis < 0 || cfg->clamp_axis > 2 || cfg->load_axis < 0 || cfg->load_axis > 2 ||
             cfg->load_comp < 0 || cfg->load_comp > 2 || cfg->im < 1 || cfg->dt0 <= 0 || cfg->n1 < 1 ||
             cfg->n2 < 1 || cfg->nipc < 0 || cfg->lfil < 0 || !(cfg->load_ratio >= -1.0) ||
-            !(cfg->load_ratio < 1.0)) {
+            !(cfg->load_ratio < 1.0) || cfg->gs_passes < 0 || cfg->gs_passes > 2) {
             set_error("xt_slab_create: invalid configuration");
             return XT_ERR_ARG;
         }

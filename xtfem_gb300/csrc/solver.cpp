@@ -463,16 +463,28 @@ int nested_prec(System& S, const float* v, float* z)
     return XT_OK;
 }
 
+// Classical Gram-Schmidt passes per Arnoldi step of the flexible GMRES: the
+// system's setting (XTFEM_CGS_PASSES=1 or 2 overrides it), two once the
+// solve has switched after a loss of orthogonality.  One pass reads the
+// basis twice per step instead of four times; the Hessenberg column is then
+// that pass's projections.
+bool cgs_two_pass(const System& S)
+{
+    if (S.gs_latched) return true;
+    const char* e = std::getenv("XTFEM_CGS_PASSES");
+    const int passes = e ? std::atoi(e) : S.gs_passes;
+    return passes != 1;
+}
+
+// A restart whose true residual exceeds the estimate of the cycle before it
+// tenfold: the one-pass basis has lost orthogonality, so the rest of the
+// solve takes two passes.
+constexpr double kOrthLoss = 10.0;
+
 int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                GmresStats& st)
 {
-    // XTFEM_CGS_PASSES=1: one classical Gram-Schmidt pass per Arnoldi step
-    // (two reads of the basis instead of four; the Hessenberg column is the
-    // one pass's projections)
-    const bool two_pass = [] {
-        const char* e = std::getenv("XTFEM_CGS_PASSES");
-        return !e || std::atoi(e) != 1;
-    }();
+    bool two_pass = cgs_two_pass(S);
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     const size_t nl = n + (n & 1);  // basis column stride: even, zero pad when n is odd
@@ -493,6 +505,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     const double ro0 = std::sqrt(hbuf[0]);
     for (;;) {
         // v1 = (rhs - A sol) / ||rhs - A sol||, the residual formed in FP64
+        const double ro_est = ro;  // the previous cycle's estimate
         XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
         XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
@@ -503,6 +516,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             return XT_ERR_NONFINITE;
         }
         if (ro == 0.0) { ierr = -1; break; }
+        if (its > 0 && !two_pass && ro > kOrthLoss * ro_est) two_pass = S.gs_latched = true;
         XT_TRY(df_from_f64(S.w64.p, col(0), n, s));
         XT_TRY(df_scale(col(0), 1.0 / ro, n, s));
         if (its == 0) eps1 = eps * ro;
@@ -603,6 +617,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
 int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
                    GmresStats& st)
 {
+    bool two_pass = cgs_two_pass(S);
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
     const size_t nl = n + (n & 1);
@@ -629,6 +644,7 @@ int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps
     XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
     const double ro0 = std::sqrt(hbuf[0]);
     for (;;) {
+        const double ro_est = ro;  // the previous cycle's estimate
         XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
         XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
@@ -639,6 +655,7 @@ int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps
             return XT_ERR_NONFINITE;
         }
         if (ro == 0.0) { ierr = -1; break; }
+        if (its > 0 && !two_pass && ro > kOrthLoss * ro_est) two_pass = S.gs_latched = true;
         XT_TRY(df_from_f64(S.w64.p, V, n, s));
         XT_TRY(df_scale(V, 1.0 / ro, n, s));
         if (its == 0) eps1 = eps * ro;
@@ -667,7 +684,7 @@ int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps
                 XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, S.zfix.p, S.wfix.p, s, ctl + 1));
                 prof_end(tok[3 * k + 1], s);
                 tok[3 * k + 2] = prof_begin(PROF_ORTH64, s);
-                XT_TRY(flexd_orth(ctl, V, nl, S.wfix.p, dst, im, S.red, s));
+                XT_TRY(flexd_orth(ctl, V, nl, S.wfix.p, dst, im, S.red, s, two_pass));
                 XT_TRY(flexd_givens(ctl, dst, im, s));
                 XT_TRY(flexd_scale_copy(ctl, dst, im, S.wfix.p, V, nl, n, s));
                 prof_end(tok[3 * k + 2], s);
@@ -679,7 +696,8 @@ int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps
             const int ran = rctl[0] - j;
             for (int k = 0; k < nstep; ++k) {
                 if (k < ran) {
-                    prof_bytes(tok[3 * k + 2], (4.0 * (j + k + 1) + 6.0) * (double)nl * 8.0);
+                    const double jk = j + k + 1;
+                    prof_bytes(tok[3 * k + 2], (two_pass ? 4.0 * jk + 6.0 : 2.0 * jk + 3.0) * (double)nl * 8.0);
                 } else {
                     for (int c = 0; c < 3; ++c) prof_cancel(tok[3 * k + c]);
                 }
@@ -756,6 +774,8 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
     } op16_reset{S};
     S.op16 = bf16;
     S.nest_its = 0;
+    S.gs_latched = false;
+    double predicted = -1.0;  // the last inner solve's estimate of the residual it left
     XT_TRY(ensure_workspace(S, im, inner == 1, inner == 2));
     if (bf16) XT_TRY(ensure_workspace(S, kNestSteps, true));
     double hb[2];
@@ -783,6 +803,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
         }
         if (st.relres <= tol) { st.ierr = 0; break; }
         if (st.its >= maxits) { st.ierr = 1; break; }
+        if (inner == 2 && predicted > 0.0 && rn > kOrthLoss * predicted) S.gs_latched = true;
         ++st.outer;
         const int left = maxits - st.its;
         const double want = std::max(tol * bn / rn, inner == 1 ? inner_tol : 0.0);
@@ -799,6 +820,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
                 XT_TRY(gmres_flex_dev(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
             else
                 XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
+            predicted = rn * in.est;
             XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
         } else {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));

@@ -41,6 +41,10 @@ struct System {
     // GMRES workspace
     int im_cap = 0;
     bool op16 = false;  // FP32 inner operator reads BF16-stored K and M (mode 3)
+    // Gram-Schmidt passes per step of the flexible GMRES (1 or 2), and the
+    // switch to two for the rest of a solve after a loss of orthogonality
+    int gs_passes = 2;
+    bool gs_latched = false;
     long long nest_its = 0;  // inner iterations of the last mode-3 solve
     // device-driven flexible GMRES: step control, cycle state, the fixed
     // preconditioned and operator vectors of a step, host copy of the control

@@ -259,7 +259,7 @@ struct FlexLayout {
 int flexd_hi(const int* ctl, const float2* V, size_t nl, float* d, size_t n, cudaStream_t s);
 int flexd_zcopy(const int* ctl, const float* z, float* Z, size_t n, cudaStream_t s);
 int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st, int im,
-               Reduce& r, cudaStream_t s);
+               Reduce& r, cudaStream_t s, bool two_pass = true);
 int flexd_givens(int* ctl, double* st, int im, cudaStream_t s);
 int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, float2* V,
                      size_t nl, size_t n, cudaStream_t s);
