@@ -164,13 +164,14 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6, merged=True):
 # read its blob, DRAM serves it once).  kron_spmm_df = the node-block
 # kernel, which reads K as 3 x 3 blocks and M as one scalar per block (its
 # algorithmic bytes are counted for the CSR operands, as for the others).
-NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 23_080_960 + 22_542_336,
+NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 26_068_736 + 26_402_560,
                4: 99_808_256 + 41_192_960, 7: 57_748_992 + 28_160}
 
 ROOFLINE_NOTES = {
     3: "level-scheduled triangular sweeps: 764 + 743 dependent levels, each sweep on six SMs, one "
-       "per temporal block; bound by per-level shared-memory latency and barriers, not by HBM "
-       "(DRAM at 0.5 % of peak under ncu); roofline_streaming gives the HBM-bound kernel",
+       "per temporal block; bound by per-level latency (shared-memory window reads, shuffles, the "
+       "level barrier), not by HBM (DRAM at about 1 % of peak under ncu); roofline_streaming gives "
+       "the HBM-bound kernel",
 }
 
 

@@ -1827,16 +1827,8 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned w
     }
 }
 
-// Warps of a three-deep register sweep: 12 warps leave each thread the 170
-// registers that three register sets need.
-constexpr int kRegMaxWarps3 = 12;
-
-// DEPTH register sets rotate through the levels: the set a level used is
-// reloaded, right after it, with the level DEPTH ahead, so a load has
-// DEPTH - 1 levels of work to land in.
-template <int H, int SMAX, bool UPPER, int DEPTH, bool W16>
-__global__ void __launch_bounds__((DEPTH > 2 ? kRegMaxWarps3 : kRegMaxWarps) * 32, 1)
-    k_tri_reg(RegArgs a)
+template <int H, int SMAX, bool UPPER, bool W16>
+__global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
 {
     extern __shared__ __align__(16) float rwin[];
     if (a.skip && a.skip[0] != 0) return;  // uniform: before any barrier
@@ -1863,26 +1855,29 @@ __global__ void __launch_bounds__((DEPTH > 2 ? kRegMaxWarps3 : kRegMaxWarps) * 3
                 prefetch_l2(a.rhs + (size_t)tb * a.rstride + ((size_t)L * a.ncw + warp) * 32);
         }
     };
-    for (int L = DEPTH; L < DEPTH + a.pf; ++L) prefetch(L);
-    RegSet<SMAX, W16> rs[DEPTH];
-#pragma unroll
-    for (int d = 0; d < DEPTH; ++d) {
-        if (d < a.nl) reg_load<SMAX, W16>(rs[d], sp, bp, lane);
+    for (int L = 2; L < 2 + a.pf; ++L) prefetch(L);
+    // two register sets, a pair of levels per trip: the set a level used is
+    // reloaded, right after it, with the level two ahead
+    RegSet<SMAX, W16> s0, s1;
+    reg_load<SMAX, W16>(s0, sp, bp, lane);
+    if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
+    sp += 2 * sstep;
+    bp += 2 * a.ncw * 32;
+    level_barrier();  // the zero slot is set
+    for (int l = 0; l < a.nl; l += 2) {
+        reg_level<H, SMAX, W16>(s0, wbase, rwin, out, lane0);
+        if (l + 2 < a.nl) reg_load<SMAX, W16>(s0, sp, bp, lane);
+        prefetch(l + 2 + a.pf);
         sp += sstep;
         bp += a.ncw * 32;
-    }
-    level_barrier();  // the zero slot is set
-    for (int l = 0; l < a.nl; l += DEPTH) {
-#pragma unroll
-        for (int d = 0; d < DEPTH; ++d) {
-            if (l + d < a.nl) {  // uniform over the block
-                reg_level<H, SMAX, W16>(rs[d], wbase, rwin, out, lane0);
-                if (l + d + DEPTH < a.nl) reg_load<SMAX, W16>(rs[d], sp, bp, lane);
-                prefetch(l + d + DEPTH + a.pf);
-                sp += sstep;
-                bp += a.ncw * 32;
-                level_barrier();
-            }
+        level_barrier();
+        if (l + 1 < a.nl) {
+            reg_level<H, SMAX, W16>(s1, wbase, rwin, out, lane0);
+            if (l + 3 < a.nl) reg_load<SMAX, W16>(s1, sp, bp, lane);
+            prefetch(l + 3 + a.pf);
+            sp += sstep;
+            bp += a.ncw * 32;
+            level_barrier();
         }
     }
 }
@@ -1914,15 +1909,15 @@ __global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
     }
 }
 
-template <int Q, int H, int SMAX, int DEPTH, bool W16>
+template <int Q, int H, int SMAX, bool W16>
 int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
                const int* skip)
 {
     static std::atomic<bool> attr{false};
     if (!attr.load(std::memory_order_acquire)) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, DEPTH, W16>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, W16>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, DEPTH, W16>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, W16>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         attr.store(true, std::memory_order_release);
     }
@@ -1935,30 +1930,24 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
                L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
                skip};
-    k_tri_reg<H, SMAX, false, DEPTH, W16><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
-    k_tri_reg<H, SMAX, true, DEPTH, W16><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
+    k_tri_reg<H, SMAX, false, W16><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
+    k_tri_reg<H, SMAX, true, W16><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
 }
 
-// Three register sets where the registers allow (16-bit offsets, at most 12
-// warps and 12 steps per lane; XTFEM_ILU_DEPTH=2 keeps two).
+// The kernel for the layout's offset width.
 template <int Q, int H, int SMAX>
-int launch_reg_depth(const IluStage& st, const double* dAinv, const float* v, float* z,
+int launch_reg_width(const IluStage& st, const double* dAinv, const float* v, float* z,
                      cudaStream_t s, const int* skip)
 {
     if (st.regL->w16 != st.regU->w16) {
         set_error("register sweep: triangles with different offset widths");
         return XT_ERR_STATE;
     }
-    if (!st.regL->w16) return launch_reg<Q, H, SMAX, 2, false>(st, dAinv, v, z, s, skip);
-    if constexpr (SMAX <= 12) {
-        if (std::max(st.regL->ncw, st.regU->ncw) <= kRegMaxWarps3 &&
-            env_int("XTFEM_ILU_DEPTH", 3) >= 3)
-            return launch_reg<Q, H, SMAX, 3, true>(st, dAinv, v, z, s, skip);
-    }
-    return launch_reg<Q, H, SMAX, 2, true>(st, dAinv, v, z, s, skip);
+    if (st.regL->w16) return launch_reg<Q, H, SMAX, true>(st, dAinv, v, z, s, skip);
+    return launch_reg<Q, H, SMAX, false>(st, dAinv, v, z, s, skip);
 }
 
 template <int Q>
@@ -1966,12 +1955,12 @@ int launch_reg_any(const IluStage& st, const double* dAinv, const float* v, floa
                    cudaStream_t s, const int* skip)
 {
     const int H = st.regL->H, smax = st.regL->smax;
-    if (H == 2 && smax == 8) return launch_reg_depth<Q, 2, 8>(st, dAinv, v, z, s, skip);
-    if (H == 2 && smax == 12) return launch_reg_depth<Q, 2, 12>(st, dAinv, v, z, s, skip);
-    if (H == 2 && smax == 16) return launch_reg_depth<Q, 2, 16>(st, dAinv, v, z, s, skip);
-    if (H == 1 && smax == 12) return launch_reg_depth<Q, 1, 12>(st, dAinv, v, z, s, skip);
-    if (H == 1 && smax == 20) return launch_reg_depth<Q, 1, 20>(st, dAinv, v, z, s, skip);
-    if (H == 4 && smax == 8) return launch_reg_depth<Q, 4, 8>(st, dAinv, v, z, s, skip);
+    if (H == 2 && smax == 8) return launch_reg_width<Q, 2, 8>(st, dAinv, v, z, s, skip);
+    if (H == 2 && smax == 12) return launch_reg_width<Q, 2, 12>(st, dAinv, v, z, s, skip);
+    if (H == 2 && smax == 16) return launch_reg_width<Q, 2, 16>(st, dAinv, v, z, s, skip);
+    if (H == 1 && smax == 12) return launch_reg_width<Q, 1, 12>(st, dAinv, v, z, s, skip);
+    if (H == 1 && smax == 20) return launch_reg_width<Q, 1, 20>(st, dAinv, v, z, s, skip);
+    if (H == 4 && smax == 8) return launch_reg_width<Q, 4, 8>(st, dAinv, v, z, s, skip);
     set_error("register sweep: no kernel for these shares and steps");
     return XT_ERR_ARG;
 }

@@ -115,13 +115,14 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
 // every operation runs on the FP32 pipe.
 
 // Row blocks per chunk of kChunk basis vectors in a double-float dot pass:
-// about eight resident blocks per SM over all chunks (row blocks shrink as
-// k grows, so each block's rows outweigh its block reduction).
+// one wave of the six blocks per SM that the pass's registers allow, over
+// all chunks (row blocks shrink as k grows, so each block's rows outweigh
+// its block reduction).  Eight per SM made 1.34 waves (ncu).
 __host__ __device__ __forceinline__ int df_dot_blocks(int k, int nblocks)
 {
     const int nchunk = (k + kChunk - 1) / kChunk;
-    const int b = (8 * 152 + nchunk - 1) / nchunk;
-    return b < nblocks ? (b > 38 ? b : 38) : (nblocks > 38 ? nblocks : 38);
+    const int b = (6 * 152) / nchunk;
+    return b < nblocks ? (b > 24 ? b : 24) : (nblocks > 24 ? nblocks : 24);
 }
 
 // partial[(j0+c) nb + b] = (hi, lo) of sum over row block rb's rows of V_j w
