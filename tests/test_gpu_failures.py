@@ -11,6 +11,9 @@
   * Non-finite input: a NaN in the right-hand side is reported as
     XT_ERR_NONFINITE by the solve entry points (status-returning and
     Fortran-style), and the system stays usable.
+  * A factor that broke down (an infinite entry, as a near-zero pivot
+    leaves) is refused when it is set, with XT_ERR_NONFINITE, and the
+    system keeps its previous factor.
 """
 import numpy as np
 import pytest
@@ -81,5 +84,22 @@ def test_nonfinite_right_hand_side_is_reported(xt, rod8):
                       eps=1e-8, maxits=100)
     assert "non-finite" in str(e.value)
     # the system is still usable: the same solve gives the same bits again
+    sol, info = s["sys"].solve(rhs, im=60, tol=1e-8, precision=2)
+    assert info == info0 and np.array_equal(sol, sol0)
+
+
+def test_nonfinite_factor_is_refused(xt, rod8):
+    s = rod8
+    rng = np.random.default_rng(5)
+    x_true = rng.standard_normal(s["K"].n * 6)
+    x_true[np.tile(s["bc"], 6) == 1] = 0.0
+    rhs = s["sys"].apply(s["A"], s["B"], x_true)
+    sol0, info0 = s["sys"].solve(rhs, im=60, tol=1e-8, precision=2)
+    bad = np.array(s["alu"], dtype=float).copy()
+    p = s["K"].n
+    bad[p + 1 + len(bad[p + 1:]) // 2] = np.inf  # an off-diagonal entry
+    with pytest.raises(xt.XtError) as e:
+        s["sys"].set_ilu(bad, s["jlu"], s["ju"], group=3)
+    assert f"status {XT_ERR_NONFINITE}" in str(e.value) and "broke down" in str(e.value)
     sol, info = s["sys"].solve(rhs, im=60, tol=1e-8, precision=2)
     assert info == info0 and np.array_equal(sol, sol0)

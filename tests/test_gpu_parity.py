@@ -200,6 +200,34 @@ def test_gmres_iteration_history_tracks_oracle(xt, orc, rod_system):
     sysm.close()
 
 
+def test_kronpgmres_residual_log(xt, orc, rod_system):
+    """The Fortran-style kronpgmres_ with iout > 0 keeps the residual
+    history the reference writes to unit iout (src/kronecker.f90:257-259,
+    311): entry 0 is ||r0||/||rhs|| (1 from a zero start), entry k the
+    estimate after iteration k.  It is the handle API's history of the same
+    solve, bit for bit, one entry per iteration, and it tracks the oracle's
+    (MGS) estimates."""
+    s = rod_system
+    rhs = c1_rhs(xt, s)
+    sol, ierr = xt.kronpgmres(s["A"], s["B"], s["K"], s["M"], s["alu"], s["jlu"], s["ju"],
+                              rhs.copy(), im=30, eps=1e-8, maxits=1000, iout=40)
+    log = xt.gmres_log()
+    assert ierr == 0 and log[0] == 1.0 and log[-1] <= 1e-8 and np.all(log[1:] < 1.0)
+    sysm = xt.SpaceTimeSystem(s["K"], s["M"])
+    sysm.set_ilu(s["alu"], s["jlu"], s["ju"])
+    sysm.set_temporal(s["A"], s["B"])
+    _, info = sysm.gmres(rhs, im=30, eps=1e-8, maxits=1000, hist_len=1000)
+    sysm.close()
+    assert len(log) == info["its"] + 1
+    assert np.array_equal(log[1:], info["hist"][:info["its"]])
+    _, _, its, hist = orc.kronpgmres(s["A"], s["B"], s["K"], s["M"], s["alu"], s["jlu"],
+                                     s["ju"], rhs, im=30, eps=1e-8, maxits=1000, hist_len=1000)
+    m = min(len(hist), len(log) - 1, 20)
+    assert np.allclose(np.log10(log[1:m + 1]), np.log10(hist[:m]), atol=0.05)
+    lines = xt.gmres_log_lines(log, iout=40)
+    assert len(lines) == len(log)
+
+
 @pytest.mark.parametrize("precision", [0, 1, 2, 3])
 def test_refined_solve_reaches_true_residual(xt, orc, rod_system, precision):
     s = rod_system

@@ -307,9 +307,10 @@ class SpaceTimeSystem:
     __del__ = close
 
     def set_ilu(self, alu, jlu, ju, group=3):
-        self._f = (_f64(alu), _i32(jlu), _i32(ju))
-        check(lib().xt_system_set_ilu(self._h, dptr(self._f[0]), iptr(self._f[1]),
-                                      iptr(self._f[2]), group), "set_ilu")
+        f = (_f64(alu), _i32(jlu), _i32(ju))
+        check(lib().xt_system_set_ilu(self._h, dptr(f[0]), iptr(f[1]), iptr(f[2]), group),
+              "set_ilu")
+        self._f = f
 
     def set_temporal(self, a, b):
         check(lib().xt_system_set_temporal(self._h, dptr(_colmajor(a)), dptr(_colmajor(b))),

@@ -656,7 +656,14 @@ int damage_update(const DamageArgs& a, cudaStream_t s)
     // XTFEM_DAMAGE_RUN=0: screen every step (no per-run bound)
     const char* e = std::getenv("XTFEM_DAMAGE_RUN");
     const int run_bound = (!e || std::atoi(e) != 0) ? 1 : 0;
-    k_damage<<<(a.ngp + 255) / 256, 256, 0, s>>>(a, a.ntmax, run_bound);
+    // 128 threads per block (XTFEM_DAMAGE_THREADS=256: 256).  A block that
+    // holds a plastic point runs for the whole update; at 170 registers a
+    // thread, a 128-thread block leaves its SM room for the solve's blocks
+    // beside it, where a 256-thread block (43.5 K registers) left room for
+    // two dot-pass blocks of six.
+    const char* et = std::getenv("XTFEM_DAMAGE_THREADS");
+    const int nt = (et && std::atoi(et) == 256) ? 256 : 128;
+    k_damage<<<(a.ngp + nt - 1) / nt, nt, 0, s>>>(a, a.ntmax, run_bound);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

@@ -117,11 +117,14 @@ __global__ void k_multi_dot_f32(const float2* __restrict__ V, size_t ld2, int k,
 // Row blocks per chunk of kChunk basis vectors in a double-float dot pass:
 // one wave of the six blocks per SM that the pass's registers allow, over
 // all chunks (row blocks shrink as k grows, so each block's rows outweigh
-// its block reduction).  Eight per SM made 1.34 waves (ncu).
+// its block reduction).  Eight per SM made 1.34 waves (ncu).  The wave is
+// sized for 148 of the 152 SMs: a few SMs may hold a long-running block of
+// the damage update on the side stream, and a pass sized for every SM
+// would leave its last blocks a second wave.
 __host__ __device__ __forceinline__ int df_dot_blocks(int k, int nblocks)
 {
     const int nchunk = (k + kChunk - 1) / kChunk;
-    const int b = (6 * 152) / nchunk;
+    const int b = (6 * 148) / nchunk;
     return b < nblocks ? (b > 24 ? b : 24) : (nblocks > 24 ? nblocks : 24);
 }
 

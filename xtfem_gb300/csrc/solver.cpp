@@ -168,6 +168,14 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
 
 int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group)
 {
+    // a factorisation that broke down (a pivot at or near zero) leaves
+    // infinities or NaNs in the factor; every apply would then return them
+    const long long len = (long long)jlu[S.p] - 1;  // MSR, 1-based pointers
+    for (long long k = 0; k < len; ++k)
+        if (k != S.p && !std::isfinite(alu[k])) {
+            set_error("set_ilu: the factor has a non-finite entry (the factorisation broke down)");
+            return XT_ERR_NONFINITE;
+        }
     auto f = std::make_shared<DevIlu>();
     XT_TRY(system_stream(S));
     XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, S.stream));
