@@ -272,6 +272,14 @@ int xt_batch_destroy(xt_batch b);
  * with 1 lanes per row of the FP32 register sweep, i.e. 5 or 10 node rows
  * per warp, solves the whole batch once from the given initial guesses;
  * the fastest pair is kept for the batch's later calls).
+ * Precision 2 runs the batch in lockstep on the calling thread: every
+ * system's refined solve with its Arnoldi bookkeeping on the device, and
+ * per round the next 16 Arnoldi steps of every system as one CUDA graph
+ * (one branch per system, captured once per call and replayed; a system
+ * whose cycle or solve has ended does nothing in it), one host
+ * synchronisation per round for all control words.  Other precisions run
+ * each system's solve on a pool of `workers` host threads.  Either way
+ * each solution equals the system's own xt_system_solve bit for bit.
  * stats (may be NULL) gets 6 values per system as in xt_system_solve;
  * status (may be NULL) gets each system's return code.  Returns XT_OK when
  * every system succeeded, else the first failing system's code (its

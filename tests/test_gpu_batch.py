@@ -2,7 +2,9 @@
 elements with uneven n and their own load amplitudes, as in the many-rod
 workload, solved together; each result equals the same system solved
 alone, and the smallest rod (the 4 x 4 x 12 mesh) matches the oracle's
-FP64 GMRES."""
+FP64 GMRES.  Mode 2 runs the batch in lockstep rounds of Arnoldi steps
+(one CUDA graph per round over every rod); the rounds issued directly and
+the thread pool give the same bits."""
 import numpy as np
 import pytest
 
@@ -99,3 +101,29 @@ def test_batch_restart_tuner(xt, cases):
     batch.close()
     for a, b, c in zip(sols, again, fixed):
         assert np.array_equal(a, b) and np.array_equal(a, c)
+
+
+def test_batch_lockstep_graph_direct_and_pool_agree(xt, cases, monkeypatch):
+    """The lockstep batch with its rounds replayed from one captured graph,
+    the same rounds issued directly (XTFEM_BATCH_GRAPH=0) and the thread
+    pool of separate solves (XTFEM_BATCH_LOCKSTEP=0) give the same solutions
+    and statistics bit for bit, with one and with two Gram-Schmidt passes."""
+    rhs = [c["rhs"] for c in cases]
+    for passes in ("2", "1"):
+        monkeypatch.setenv("XTFEM_CGS_PASSES", passes)
+        out = {}
+        for mode, env in (("graph", {}), ("direct", {"XTFEM_BATCH_GRAPH": "0"}),
+                          ("pool", {"XTFEM_BATCH_LOCKSTEP": "0"})):
+            for k in ("XTFEM_BATCH_GRAPH", "XTFEM_BATCH_LOCKSTEP"):
+                monkeypatch.delenv(k, raising=False)
+            for k, v in env.items():
+                monkeypatch.setenv(k, v)
+            batch = xt.SystemBatch([c["sys"] for c in cases], workers=4)
+            out[mode] = batch.solve(rhs, im=30, tol=1e-8, precision=2)
+            batch.close()
+        for mode in ("direct", "pool"):
+            sols, stats, status = out[mode]
+            assert (status == 0).all()
+            for a, b in zip(out["graph"][0], sols):
+                assert np.array_equal(a, b), (passes, mode)
+            assert out["graph"][1] == stats, (passes, mode)

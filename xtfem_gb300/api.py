@@ -369,8 +369,10 @@ class SpaceTimeSystem:
 
 
 class SystemBatch:
-    """Independent systems solved together (xt_batch_*): one host worker
-    thread per system at a time, each system on its own stream."""
+    """Independent systems solved together (xt_batch_*).  Mode 2 runs in
+    lockstep rounds of Arnoldi steps, one CUDA graph per round over every
+    system; other modes run one host worker thread per system at a time,
+    each system on its own stream."""
 
     def __init__(self, systems, workers=0):
         self.systems = list(systems)

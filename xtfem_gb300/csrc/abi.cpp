@@ -8,6 +8,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -19,6 +20,8 @@
 
 #include "../../include/xtfem_gb300.h"
 #include "solver.h"
+
+extern "C" long long xt_launch_count(void);  // prof.cpp
 
 using namespace xt;
 
@@ -512,10 +515,264 @@ int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int
 }
 
 namespace {
+// The batch in lockstep (mode 2, the default): every system runs the
+// refined solve with the device-driven flexible GMRES (FlexRun), and a round
+// issues the next kRound Arnoldi steps of every system (16,
+// XTFEM_BATCH_ROUND) as kRound launches of one CUDA graph that holds one
+// step of every system, one branch per system, each branch ending with the
+// copy of its control word into pinned host memory.  The graph is captured
+// in the second round, after every run has issued a
+// round directly (so the device data built on first use exists); it is
+// replayed every round after that, and runs whose cycle or solve has ended
+// do nothing in it (their kernels read the ended status).  One host
+// synchronisation per round reads every control word; the host work between
+// cycles (residuals, the least-squares update, refinement) is each run's
+// own, on its stream.  XTFEM_BATCH_GRAPH=0: the same rounds issued directly.
+// The results equal each system's own solve bit for bit.
+// Arnoldi steps per round (XTFEM_BATCH_ROUND, 16)
+int batch_round()
+{
+    const char* e = std::getenv("XTFEM_BATCH_ROUND");
+    const int v = e ? std::atoi(e) : 16;
+    return v > 0 && v <= 256 ? v : 16;
+}
+
+struct PinnedInts {
+    int* p = nullptr;
+    ~PinnedInts() { if (p) cudaFreeHost(p); }
+};
+struct GraphParts {
+    cudaStream_t master = nullptr;
+    std::vector<cudaEvent_t> ev;
+    cudaGraphExec_t exec = nullptr;
+    ~GraphParts()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+        if (master) cudaStreamDestroy(master);
+    }
+};
+
+bool batch_graph_on()
+{
+    const char* e = std::getenv("XTFEM_BATCH_GRAPH");
+    return !e || std::atoi(e) != 0;
+}
+
+int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
+                    int maxits, double* stats, int* status)
+{
+    const int count = (int)b->sys.size();
+    const int kRound = batch_round();
+    DeviceGuard guard(ctx().device);
+    if (guard.err != cudaSuccess) {
+        set_error("xt_batch_solve: could not select the library's device");
+        return XT_ERR_CUDA;
+    }
+    std::vector<int> code(count, XT_OK);
+    std::vector<std::string> msg(count);
+    std::vector<FlexRun> run(count);
+    auto fail = [&](int i, int rc) {
+        code[i] = rc;
+        msg[i] = last_error();
+    };
+    PinnedInts hctl;
+    XT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&hctl.p), sizeof(int) * 4 * (size_t)count,
+                          cudaHostAllocDefault));
+    // the host work of the runs (set-up, cycle ends and starts, refinement
+    // steps: each with its own host reads) spread over the batch's workers,
+    // largest system first; each run is touched by one thread at a time
+    const int device = ctx().device;
+    bool lost_device = false;
+    auto parallel = [&](auto fn) {
+        std::atomic<int> next{0};
+        std::atomic<bool> lost{false};
+        auto work = [&] {
+            if (cudaSetDevice(device) != cudaSuccess) {
+                lost = true;
+                return;
+            }
+            for (int k; (k = next.fetch_add(1)) < count;) fn(b->order[k]);
+        };
+        std::vector<std::thread> pool;
+        for (int w = 1; w < b->workers; ++w) pool.emplace_back(work);
+        work();
+        for (auto& t : pool) t.join();
+        lost_device = lost_device || lost.load();
+    };
+    // XTFEM_TRACE: the time of each phase, printed at the end
+    const bool tracing = std::getenv("XTFEM_TRACE") != nullptr;
+    using clk = std::chrono::steady_clock;
+    double t_start = 0, t_capture = 0, t_steps = 0, t_host = 0, t_down = 0;
+    int rounds = 0;
+    auto since = [](clk::time_point t0) {
+        return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+    };
+    auto tp = clk::now();
+    parallel([&](int i) {
+        xt_system_s& h = *b->sys[i];
+        System& S = h.sys;
+        const size_t n = (size_t)S.p * S.q;
+        int rc = system_stream(S);
+        if (rc == XT_OK) rc = ensure_vec(S.b64, n);
+        if (rc == XT_OK) rc = ensure_vec(S.x64, n);
+        if (rc == XT_OK) rc = upload_blocks(h, rhs[i], S.b64.p);
+        if (rc == XT_OK) rc = upload_blocks(h, sol[i], S.x64.p);
+        if (rc == XT_OK) rc = run[i].start(S, S.b64.p, S.x64.p, im, tol, maxits);
+        if (rc != XT_OK) fail(i, rc);
+    });
+    t_start = since(tp);
+    auto live = [&](int i) { return code[i] == XT_OK && !run[i].done; };
+    GraphParts gp;
+    std::vector<char> in_graph(count, 0), cap_two(count, 0);
+    long long graph_kernels = 0;
+    bool tried = false;
+    for (int round = 0;; ++round) {
+        bool any = false;
+        for (int i = 0; i < count; ++i) any = any || live(i);
+        if (!any) break;
+        // a run that switched to two Gram-Schmidt passes after the capture
+        // needs its steps captured again
+        if (gp.exec) {
+            bool stale = false;
+            for (int i = 0; i < count; ++i)
+                stale = stale || (live(i) && run[i].two_pass != (bool)cap_two[i]);
+            if (stale) {
+                cudaGraphExecDestroy(gp.exec);
+                gp.exec = nullptr;
+                tried = false;
+                std::fill(in_graph.begin(), in_graph.end(), 0);
+            }
+        }
+        ++rounds;
+        tp = clk::now();
+        if (round >= 1 && !tried && batch_graph_on()) {
+            tried = true;
+            if (!gp.master) {
+                XT_CUDA(cudaStreamCreateWithFlags(&gp.master, cudaStreamNonBlocking));
+                gp.ev.assign(count + 1, nullptr);
+                for (auto& e : gp.ev) XT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            }
+            const long long before = xt_launch_count();
+            cudaGraph_t g = nullptr;
+            bool ok = cudaStreamBeginCapture(gp.master, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+            if (ok) {
+                ok = cudaEventRecord(gp.ev[count], gp.master) == cudaSuccess;
+                for (int i = 0; ok && i < count; ++i) {
+                    if (!live(i)) continue;
+                    System& S = b->sys[i]->sys;
+                    ok = cudaStreamWaitEvent(S.stream, gp.ev[count], 0) == cudaSuccess &&
+                         run[i].issue(1, nullptr) == XT_OK &&
+                         cudaMemcpyAsync(hctl.p + 4 * i, S.fctl.p, 4 * sizeof(int),
+                                         cudaMemcpyDeviceToHost, S.stream) == cudaSuccess &&
+                         cudaEventRecord(gp.ev[i], S.stream) == cudaSuccess &&
+                         cudaStreamWaitEvent(gp.master, gp.ev[i], 0) == cudaSuccess;
+                    in_graph[i] = 1;
+                    cap_two[i] = run[i].two_pass;
+                }
+                const cudaError_t e = cudaStreamEndCapture(gp.master, &g);
+                ok = ok && e == cudaSuccess && g != nullptr &&
+                     cudaGraphInstantiate(&gp.exec, g, 0) == cudaSuccess;
+            }
+            if (g) cudaGraphDestroy(g);
+            graph_kernels = xt_launch_count() - before;
+            if (!ok) {  // issue the rounds directly instead
+                if (gp.exec) cudaGraphExecDestroy(gp.exec);
+                gp.exec = nullptr;
+                cudaGetLastError();
+                std::fill(in_graph.begin(), in_graph.end(), 0);
+            }
+            note_launches((int)-graph_kernels);  // captured, not run: counted per replay
+            t_capture += since(tp);
+            tp = clk::now();
+        }
+        if (gp.exec) {
+            for (int k = 0; k < kRound; ++k) XT_CUDA(cudaGraphLaunch(gp.exec, gp.master));
+            XT_CUDA(cudaStreamSynchronize(gp.master));
+            note_launches((int)(graph_kernels * kRound));
+            for (int i = 0; i < count; ++i)
+                if (live(i) && !in_graph[i]) {
+                    set_error("xt_batch_solve: a running system is missing from the round graph");
+                    fail(i, XT_ERR_STATE);
+                }
+        } else {
+            for (int i = 0; i < count; ++i) {
+                if (!live(i)) continue;
+                System& S = b->sys[i]->sys;
+                int rc = run[i].issue(kRound, nullptr);
+                if (rc == XT_OK &&
+                    cudaMemcpyAsync(hctl.p + 4 * i, S.fctl.p, 4 * sizeof(int),
+                                    cudaMemcpyDeviceToHost, S.stream) != cudaSuccess) {
+                    set_error("xt_batch_solve: control read failed");
+                    rc = XT_ERR_CUDA;
+                }
+                if (rc != XT_OK) fail(i, rc);
+            }
+            for (int i = 0; i < count; ++i)
+                if (live(i) && cudaStreamSynchronize(b->sys[i]->sys.stream) != cudaSuccess) {
+                    set_error("xt_batch_solve: stream synchronisation failed");
+                    fail(i, XT_ERR_CUDA);
+                }
+        }
+        t_steps += since(tp);
+        tp = clk::now();
+        parallel([&](int i) {
+            if (!live(i)) return;
+            const int rc = run[i].advance(hctl.p + 4 * i);
+            if (rc != XT_OK) fail(i, rc);
+        });
+        t_host += since(tp);
+        if (lost_device) break;
+    }
+    tp = clk::now();
+    parallel([&](int i) {
+        if (code[i] != XT_OK) return;
+        xt_system_s& h = *b->sys[i];
+        const int d = download_blocks(h, h.sys.x64.p, sol[i]);
+        if (d != XT_OK) fail(i, d);
+    });
+    t_down = since(tp);
+    if (tracing)
+        std::fprintf(stderr,
+                     "[xtfem] batch lockstep: %d systems, %d rounds of %d steps, graph %s "
+                     "(%lld kernels); ms: start %.1f, capture %.1f, steps %.1f, host between "
+                     "rounds %.1f, download %.1f\n",
+                     count, rounds, kRound, gp.exec ? "yes" : "no", graph_kernels, t_start,
+                     t_capture, t_steps, t_host, t_down);
+    if (lost_device) {
+        set_error("xt_batch_solve: worker thread could not select the device");
+        return XT_ERR_CUDA;
+    }
+    int rc = XT_OK;
+    for (int i = 0; i < count; ++i) {
+        if (stats && code[i] == XT_OK) {
+            const GmresStats& st = run[i].st;
+            double* o = stats + (size_t)6 * i;
+            o[0] = st.its;
+            o[1] = st.cycles;
+            o[2] = st.outer;
+            o[3] = st.ierr;
+            o[4] = st.relres;
+            o[5] = st.est;
+        }
+        if (status) status[i] = code[i];
+        if (code[i] != XT_OK && rc == XT_OK) {
+            rc = code[i];
+            set_error("xt_batch_solve: system " + std::to_string(i) + ": " + msg[i]);
+        }
+    }
+    return rc;
+}
+
 int batch_run(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
               int maxits, int precision, double inner_tol, double* stats, int* status)
 {
     const int count = (int)b->sys.size();
+    // XTFEM_BATCH_LOCKSTEP=0: mode 2 on the thread pool below as well
+    const char* ls = std::getenv("XTFEM_BATCH_LOCKSTEP");
+    if (precision == 2 && im >= 1 && im <= kFlexdMaxIm && (!ls || std::atoi(ls) != 0))
+        return batch_run_graph(b, rhs, sol, im, tol, maxits, stats, status);
     std::vector<int> code(count, XT_OK);
     std::vector<std::string> msg(count);
     std::atomic<int> next{0};

@@ -611,126 +611,13 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     return XT_OK;
 }
 
-// The flexible GMRES above with its Arnoldi bookkeeping on the device: the
-// host issues the steps of a cycle in chunks and reads the step control
-// once per chunk instead of the Hessenberg column once per step.  A step is
-// the same kernels on fixed buffers: the hi part of basis column j, the
-// FP32 ILU into zfix (copied to Z column j), the double-float operator into
-// wfix, the CGS2 passes on wfix against columns 0..j (k read on the
-// device, the row blocks and reduction order of the host-driven passes),
-// the rotations and the convergence test (k_flexd_givens, the host loop's
-// arithmetic), and wfix scaled into column j + 1.  Steps issued past the
-// end of a cycle do nothing but launch, and their profile records are
-// dropped.  The result equals gmres_flex's bit for bit.
-int gmres_flex_dev(System& S, const double* rhs, double* sol, int im, double eps, int maxits,
-                   GmresStats& st)
+// XTFEM_GMRES_CHUNK: Arnoldi steps the device-driven GMRES issues between
+// two reads of its control word (16).
+int gmres_chunk()
 {
-    bool two_pass = cgs_two_pass(S);
-    cudaStream_t s = S.stream;
-    const size_t n = (size_t)S.p * S.q;
-    const size_t nl = n + (n & 1);
-    float2* V = reinterpret_cast<float2*>(S.V64.p);
-    float* Z = S.Z32.p;
-    if (nl != n) XT_CUDA(cudaMemsetAsync(V, 0, (size_t)(im + 1) * nl * sizeof(float2), s));
-    const FlexLayout Lo(im);
-    XT_TRY(S.fst.alloc(Lo.total));
-    XT_TRY(S.fctl.alloc(4));
-    XT_TRY(S.zfix.alloc(n));
-    XT_TRY(S.wfix.alloc(nl));
-    XT_CUDA(cudaMemsetAsync(S.wfix.p, 0, nl * sizeof(float2), s));  // the pad entry stays 0
-    int* ctl = S.fctl.p;
-    double* dst = S.fst.p;
-    const int chunk = [] {  // steps issued between two reads of the control
-        const char* e = std::getenv("XTFEM_GMRES_CHUNK");
-        const int v = e ? std::atoi(e) : 16;
-        return v > 0 ? v : 16;
-    }();
-    std::vector<double> hbuf(2), rs(im + 1, 0.0);
-    int its = 0, i = 0, ierr = 0;
-    double ro = 0.0, eps1 = 0.0;
-    XT_TRY(norm2<double>(rhs, n, S.red, s));
-    XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
-    const double ro0 = std::sqrt(hbuf[0]);
-    for (;;) {
-        const double ro_est = ro;  // the previous cycle's estimate
-        XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, sol, S.w64.p));
-        XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
-        XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
-        ro = std::sqrt(hbuf[0]);
-        if (!std::isfinite(ro)) {
-            set_error("gmres: non-finite residual");
-            return XT_ERR_NONFINITE;
-        }
-        if (ro == 0.0) { ierr = -1; break; }
-        if (its > 0 && !two_pass && ro > kOrthLoss * ro_est) two_pass = S.gs_latched = true;
-        XT_TRY(df_from_f64(S.w64.p, V, n, s));
-        XT_TRY(df_scale(V, 1.0 / ro, n, s));
-        if (its == 0) eps1 = eps * ro;
-        // cycle state: rs = (ro, 0, ...), eps1, control {j = 0, running, its, maxits}
-        std::fill(rs.begin(), rs.end(), 0.0);
-        rs[0] = ro;
-        const int hctl[4] = {0, 0, its, maxits};
-        XT_CUDA(cudaMemcpyAsync(dst + Lo.rs, rs.data(), (im + 1) * sizeof(double),
-                                cudaMemcpyHostToDevice, s));
-        XT_CUDA(cudaMemcpyAsync(dst + Lo.eps1, &eps1, sizeof(double), cudaMemcpyHostToDevice, s));
-        XT_CUDA(cudaMemcpyAsync(ctl, hctl, sizeof(hctl), cudaMemcpyHostToDevice, s));
-        ++st.cycles;
-        int issued = 0, status = 0, j = 0;
-        int rctl[4] = {0, 0, 0, 0};
-        while (status == 0 && issued < im) {
-            const int nstep = std::min(chunk, im - issued);
-            std::vector<int> tok((size_t)3 * nstep, -1);
-            for (int k = 0; k < nstep; ++k) {
-                XT_TRY(flexd_hi(ctl, V, nl, S.d32.p, n, s));
-                tok[3 * k] = prof_begin(PROF_ILU32, s);
-                XT_TRY(ilu_apply<float>(*S.ilu, S.q, S.Ainv.p, S.d32.p, S.zfix.p, S.w32.p, s,
-                                        ctl + 1));
-                prof_end(tok[3 * k], s);
-                XT_TRY(flexd_zcopy(ctl, S.zfix.p, Z, n, s));
-                tok[3 * k + 1] = prof_begin(PROF_KRONDF, s);
-                XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, S.zfix.p, S.wfix.p, s, ctl + 1));
-                prof_end(tok[3 * k + 1], s);
-                tok[3 * k + 2] = prof_begin(PROF_ORTH64, s);
-                XT_TRY(flexd_orth(ctl, V, nl, S.wfix.p, dst, im, S.red, s, two_pass));
-                XT_TRY(flexd_givens(ctl, dst, im, s));
-                XT_TRY(flexd_scale_copy(ctl, dst, im, S.wfix.p, V, nl, n, s));
-                prof_end(tok[3 * k + 2], s);
-            }
-            issued += nstep;
-            XT_CUDA(cudaMemcpyAsync(rctl, ctl, sizeof(rctl), cudaMemcpyDeviceToHost, s));
-            XT_CUDA(cudaStreamSynchronize(s));
-            // steps of this chunk that ran: each advanced j by one
-            const int ran = rctl[0] - j;
-            for (int k = 0; k < nstep; ++k) {
-                if (k < ran) {
-                    const double jk = j + k + 1;
-                    prof_bytes(tok[3 * k + 2], (two_pass ? 4.0 * jk + 6.0 : 2.0 * jk + 3.0) * (double)nl * 8.0);
-                } else {
-                    for (int c = 0; c < 3; ++c) prof_cancel(tok[3 * k + c]);
-                }
-            }
-            j = rctl[0];
-            status = rctl[1];
-        }
-        if (status == 4) {
-            set_error("gmres: non-finite Krylov vector");
-            return XT_ERR_NONFINITE;
-        }
-        i = j;
-        its = rctl[2];
-        XT_CUDA(cudaMemcpyAsync(&ro, dst + Lo.ro, sizeof(double), cudaMemcpyDeviceToHost, s));
-        XT_TRY(flexd_solve(ctl, dst, im, s));
-        XT_TRY((lincomb<float, double>(Z, n, i, dst + Lo.y, S.u64.p, n, s)));
-        XT_TRY((axpby<double, double>(n, 1.0, S.u64.p, 1.0, sol, s)));
-        XT_CUDA(cudaStreamSynchronize(s));
-        if (ro <= eps1) { ierr = 0; break; }
-        if (its >= maxits) { ierr = 1; break; }
-    }
-    st.its += its;
-    st.ierr = ierr;
-    st.est = ro0 > 0 ? ro / ro0 : 0.0;
-    return XT_OK;
+    const char* e = std::getenv("XTFEM_GMRES_CHUNK");
+    const int v = e ? std::atoi(e) : 16;
+    return v > 0 ? v : 16;
 }
 
 // XTFEM_DEVICE_GMRES=1 selects the device-driven flexible GMRES (measured
@@ -744,6 +631,245 @@ bool device_gmres_on()
 }
 
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// FlexRun: the device-driven flexible GMRES inside the FP64 refinement loop.
+// A step is the same kernels on fixed buffers whatever its index: the hi
+// part of basis column j into the ILU input, the FP32 ILU apply into a fixed
+// vector and its copy into Z column j, the double-float operator into a
+// fixed vector, the control-driven Gram-Schmidt passes, the rotations and
+// convergence test (k_flexd_givens), and the scaled copy into V column j+1.
+// Every kernel reads j (and whether the cycle still runs) from the control
+// word {j, status, its, maxits} on the device.  The host work between
+// cycles follows gmres_flex and solve_refined step for step.
+
+int FlexRun::start(System& S, const double* b, double* x, int im, double tol, int maxits)
+{
+    S_ = &S;
+    b_ = b;
+    x_ = x;
+    im_ = im;
+    tol_ = tol;
+    maxits_ = maxits;
+    st = GmresStats();
+    done = false;
+    cycle = 0;
+    j = 0;
+    predicted_ = -1.0;
+    if (!S.ilu) {
+        set_error("solve: no preconditioner set");
+        return XT_ERR_STATE;
+    }
+    if (im < 1 || im > kFlexdMaxIm) {
+        set_error("solve: the device-driven GMRES takes a restart length of 1 to " +
+                  std::to_string(kFlexdMaxIm));
+        return XT_ERR_ARG;
+    }
+    XT_TRY(system_stream(S));
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    S.op16 = false;
+    S.nest_its = 0;
+    S.gs_latched = false;
+    XT_TRY(ensure_workspace(S, im, false, true));
+    double hb[2];
+    XT_TRY(norm2<double>(b, n, S.red, s));
+    XT_TRY(fetch(s, hb, S.red.out.p, 1));
+    bn_ = std::sqrt(hb[0]);
+    if (bn_ == 0.0) {
+        XT_CUDA(cudaMemsetAsync(x, 0, n * sizeof(double), s));
+        XT_CUDA(cudaStreamSynchronize(s));
+        st.ierr = -1;
+        done = true;
+        return XT_OK;
+    }
+    return outer_step();
+}
+
+// A refinement step: the FP64 true residual, the tests, the inner solve's start.
+int FlexRun::outer_step()
+{
+    System& S = *S_;
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    double hb[2];
+    XT_CUDA(cudaMemcpyAsync(S.r64.p, b_, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    XT_TRY(system_apply(S, -1.0, 1.0, x_, S.r64.p));
+    XT_TRY(norm2<double>(S.r64.p, n, S.red, s));
+    XT_TRY(fetch(s, hb, S.red.out.p, 1));
+    rn_ = std::sqrt(hb[0]);
+    st.relres = rn_ / bn_;
+    if (!std::isfinite(rn_)) {
+        set_error("solve: non-finite residual");
+        return XT_ERR_NONFINITE;
+    }
+    if (st.relres <= tol_) {
+        st.ierr = 0;
+        done = true;
+        return XT_OK;
+    }
+    if (st.its >= maxits_) {
+        st.ierr = 1;
+        done = true;
+        return XT_OK;
+    }
+    if (predicted_ > 0.0 && rn_ > kOrthLoss * predicted_) S.gs_latched = true;
+    ++st.outer;
+    left_ = maxits_ - st.its;
+    XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
+    eps_in_ = tol_ * bn_ / rn_;
+    return inner_begin();
+}
+
+// The inner solve of r64 into t64 (gmres_flex's set-up).
+int FlexRun::inner_begin()
+{
+    System& S = *S_;
+    two_pass = cgs_two_pass(S);
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    const size_t nl = n + (n & 1);
+    float2* V = reinterpret_cast<float2*>(S.V64.p);
+    if (nl != n) XT_CUDA(cudaMemsetAsync(V, 0, (size_t)(im_ + 1) * nl * sizeof(float2), s));
+    const FlexLayout Lo(im_);
+    XT_TRY(S.fst.alloc(Lo.total));
+    XT_TRY(S.fctl.alloc(4));
+    XT_TRY(S.zfix.alloc(n));
+    XT_TRY(S.wfix.alloc(nl));
+    XT_CUDA(cudaMemsetAsync(S.wfix.p, 0, nl * sizeof(float2), s));  // the pad entry stays 0
+    rs_.assign(im_ + 1, 0.0);
+    in_ = GmresStats();
+    its_in_ = 0;
+    ro_ = 0.0;
+    eps1_ = 0.0;
+    double hb[2];
+    XT_TRY(norm2<double>(S.r64.p, n, S.red, s));
+    XT_TRY(fetch(s, hb, S.red.out.p, 1));
+    ro0_ = std::sqrt(hb[0]);
+    return cycle_begin();
+}
+
+// A cycle's start: v1 from the residual formed in FP64, then the cycle state
+// {rs = (ro, 0, ...), eps1, control {0, running, its, maxits}} on the device.
+int FlexRun::cycle_begin()
+{
+    System& S = *S_;
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    float2* V = reinterpret_cast<float2*>(S.V64.p);
+    const FlexLayout Lo(im_);
+    double hb[2];
+    const double ro_est = ro_;  // the previous cycle's estimate
+    XT_CUDA(cudaMemcpyAsync(S.w64.p, S.r64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    XT_TRY(apply_op_ab<double>(S, -1.0, 1.0, S.t64.p, S.w64.p));
+    XT_TRY(norm2<double>(S.w64.p, n, S.red, s));
+    XT_TRY(fetch(s, hb, S.red.out.p, 1));
+    ro_ = std::sqrt(hb[0]);
+    if (!std::isfinite(ro_)) {
+        set_error("gmres: non-finite residual");
+        return XT_ERR_NONFINITE;
+    }
+    if (ro_ == 0.0) return inner_end(-1);
+    if (its_in_ > 0 && !two_pass && ro_ > kOrthLoss * ro_est) two_pass = S.gs_latched = true;
+    XT_TRY(df_from_f64(S.w64.p, V, n, s));
+    XT_TRY(df_scale(V, 1.0 / ro_, n, s));
+    if (its_in_ == 0) eps1_ = eps_in_ * ro_;
+    std::fill(rs_.begin(), rs_.end(), 0.0);
+    rs_[0] = ro_;
+    hctl_[0] = 0;
+    hctl_[1] = 0;
+    hctl_[2] = its_in_;
+    hctl_[3] = left_;
+    XT_CUDA(cudaMemcpyAsync(S.fst.p + Lo.rs, rs_.data(), (im_ + 1) * sizeof(double),
+                            cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaMemcpyAsync(S.fst.p + Lo.eps1, &eps1_, sizeof(double), cudaMemcpyHostToDevice, s));
+    XT_CUDA(cudaMemcpyAsync(S.fctl.p, hctl_, sizeof(hctl_), cudaMemcpyHostToDevice, s));
+    ++in_.cycles;
+    ++cycle;
+    j = 0;
+    // complete before any step reads it: steps may run from a graph
+    // launched on another stream
+    XT_CUDA(cudaStreamSynchronize(s));
+    return XT_OK;
+}
+
+int FlexRun::issue(int nstep, std::vector<int>* tok)
+{
+    System& S = *S_;
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    const size_t nl = n + (n & 1);
+    float2* V = reinterpret_cast<float2*>(S.V64.p);
+    int* ctl = S.fctl.p;
+    double* dst = S.fst.p;
+    if (tok) tok->assign((size_t)3 * nstep, -1);
+    for (int k = 0; k < nstep; ++k) {
+        XT_TRY(flexd_hi(ctl, V, nl, S.d32.p, n, s));
+        if (tok) (*tok)[3 * k] = prof_begin(PROF_ILU32, s);
+        XT_TRY(ilu_apply<float>(*S.ilu, S.q, S.Ainv.p, S.d32.p, S.zfix.p, S.w32.p, s, ctl + 1));
+        if (tok) prof_end((*tok)[3 * k], s);
+        XT_TRY(flexd_zcopy(ctl, S.zfix.p, S.Z32.p, n, s));
+        if (tok) (*tok)[3 * k + 1] = prof_begin(PROF_KRONDF, s);
+        XT_TRY(kron_spmm_df(S.K, S.M, S.q, S.A.p, S.B.p, S.zfix.p, S.wfix.p, s, ctl + 1));
+        if (tok) prof_end((*tok)[3 * k + 1], s);
+        if (tok) (*tok)[3 * k + 2] = prof_begin(PROF_ORTH64, s);
+        XT_TRY(flexd_orth(ctl, V, nl, S.wfix.p, dst, im_, S.red, s, two_pass));
+        XT_TRY(flexd_givens(ctl, dst, im_, s));
+        XT_TRY(flexd_scale_copy(ctl, dst, im_, S.wfix.p, V, nl, n, s));
+        if (tok) prof_end((*tok)[3 * k + 2], s);
+    }
+    return XT_OK;
+}
+
+// After a chunk: a cycle that has ended (status set) is finished on the
+// host side, then the next cycle, refinement step or the end follows.
+int FlexRun::advance(const int* c)
+{
+    j = c[0];
+    if (c[1] == 0) return XT_OK;  // the cycle goes on
+    if (c[1] == 4) {
+        set_error("gmres: non-finite Krylov vector");
+        return XT_ERR_NONFINITE;
+    }
+    System& S = *S_;
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    const FlexLayout Lo(im_);
+    const int i = c[0];
+    its_in_ = c[2];
+    XT_CUDA(cudaMemcpyAsync(&ro_, S.fst.p + Lo.ro, sizeof(double), cudaMemcpyDeviceToHost, s));
+    XT_TRY(flexd_solve(S.fctl.p, S.fst.p, im_, s));
+    XT_TRY((lincomb<float, double>(S.Z32.p, n, i, S.fst.p + Lo.y, S.u64.p, n, s)));
+    XT_TRY((axpby<double, double>(n, 1.0, S.u64.p, 1.0, S.t64.p, s)));
+    XT_CUDA(cudaStreamSynchronize(s));
+    if (ro_ <= eps1_) return inner_end(0);
+    if (its_in_ >= left_) return inner_end(1);
+    return cycle_begin();
+}
+
+// The inner solve's end and the rest of the refinement step.
+int FlexRun::inner_end(int ierr_in)
+{
+    System& S = *S_;
+    cudaStream_t s = S.stream;
+    const size_t n = (size_t)S.p * S.q;
+    in_.its += its_in_;
+    in_.ierr = ierr_in;
+    in_.est = ro0_ > 0 ? ro_ / ro0_ : 0.0;
+    predicted_ = rn_ * in_.est;
+    XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x_, s)));
+    XT_CUDA(cudaStreamSynchronize(s));
+    XT_TRY(ilu_check(s));
+    st.its += in_.its;
+    st.cycles += in_.cycles;
+    st.est = in_.est;
+    if (in_.its == 0) {
+        st.ierr = 1;
+        done = true;
+        return XT_OK;
+    }
+    return outer_step();
+}
 
 int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int maxits,
                GmresStats& st, std::vector<double>* hist)
@@ -762,6 +888,54 @@ int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int ma
     return ilu_check(S.stream);
 }
 
+namespace {
+// Mode 2 with the device-driven flexible GMRES on one system: the run's
+// steps issued in chunks, the control read once per chunk.  The profile
+// tokens of steps past a cycle's end (they do nothing) are cancelled.
+int solve_flex_run(System& S, const double* b, double* x, int im, double tol, int maxits,
+                   GmresStats& st)
+{
+    FlexRun R;
+    XT_TRY(R.start(S, b, x, im, tol, maxits));
+    const int chunk = gmres_chunk();
+    const size_t n = (size_t)S.p * S.q;
+    const size_t nl = n + (n & 1);
+    int issued = 0, cyc = R.cycle;
+    std::vector<int> tok;
+    int rctl[4] = {0, 0, 0, 0};
+    while (!R.done) {
+        if (R.cycle != cyc) {
+            cyc = R.cycle;
+            issued = 0;
+        }
+        const int nstep = std::min(chunk, im - issued);
+        if (nstep <= 0) {
+            set_error("gmres: a cycle ran past its restart length");
+            return XT_ERR_STATE;
+        }
+        const int j0 = R.j;
+        XT_TRY(R.issue(nstep, &tok));
+        issued += nstep;
+        XT_CUDA(cudaMemcpyAsync(rctl, S.fctl.p, sizeof(rctl), cudaMemcpyDeviceToHost, S.stream));
+        XT_CUDA(cudaStreamSynchronize(S.stream));
+        // steps of this chunk that ran: each advanced j by one
+        const int ran = rctl[0] - j0;
+        for (int k = 0; k < nstep; ++k) {
+            if (k < ran) {
+                const double jk = j0 + k + 1;
+                prof_bytes(tok[3 * k + 2],
+                           (R.two_pass ? 4.0 * jk + 6.0 : 2.0 * jk + 3.0) * (double)nl * 8.0);
+            } else {
+                for (int c = 0; c < 3; ++c) prof_cancel(tok[3 * k + c]);
+            }
+        }
+        XT_TRY(R.advance(rctl));
+    }
+    st = R.st;
+    return XT_OK;
+}
+}  // namespace
+
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
                   int inner, double inner_tol, GmresStats& st)
 {
@@ -769,6 +943,8 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
         set_error("solve: no preconditioner set");
         return XT_ERR_STATE;
     }
+    if (inner == 2 && im <= kFlexdMaxIm && device_gmres_on())
+        return solve_flex_run(S, b, x, im, tol, maxits, st);
     XT_TRY(system_stream(S));
     cudaStream_t s = S.stream;
     const size_t n = (size_t)S.p * S.q;
@@ -824,10 +1000,7 @@ int solve_refined(System& S, const double* b, double* x, int im, double tol, int
             XT_TRY((axpby<float, double>(n, rn, S.d32.p, 1.0, x, s)));
         } else if (inner == 2) {
             XT_CUDA(cudaMemsetAsync(S.t64.p, 0, n * sizeof(double), s));
-            if (!S.op16 && im <= kFlexdMaxIm && device_gmres_on())
-                XT_TRY(gmres_flex_dev(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
-            else
-                XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
+            XT_TRY(gmres_flex(S, S.r64.p, S.t64.p, im, tol * bn / rn, left, in));
             predicted = rn * in.est;
             XT_TRY((axpby<double, double>(n, 1.0, S.t64.p, 1.0, x, s)));
         } else {

@@ -115,6 +115,47 @@ int gmres_fp64(System& S, const double* b, double* x, int im, double eps, int ma
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
                   int inner, double inner_tol, GmresStats& st);
 
+// The refined solve of mode 2 (flexible GMRES, FP64 refinement) with the
+// Arnoldi bookkeeping on the device, as a resumable run:
+//   start()   sets the solve up (host work and host reads); afterwards the
+//             run is either done or in a cycle whose steps can be issued;
+//   issue()   enqueues nstep Arnoldi steps on the system's stream and
+//             nothing else (no host synchronisation, no allocation): the
+//             steps can be captured into a CUDA graph and replayed, since
+//             every kernel reads the step index from the control word and
+//             does nothing once the cycle has ended;
+//   advance() takes the control word read after a chunk of steps and does
+//             the host work of a cycle's end, of the next cycle's start and
+//             of the refinement steps between inner solves.
+// solve_refined drives one run chunk by chunk; the batch drives many in
+// lockstep, one graph per round.  Results equal the host-driven loop's bit
+// for bit.
+struct FlexRun {
+    GmresStats st;       // the refined solve's statistics (final once done)
+    bool done = false;   // the solve has ended
+    int cycle = 0;       // cycles started so far
+    int j = 0;           // steps of the current cycle at the last control read
+    bool two_pass = true;
+
+    int start(System& S, const double* b, double* x, int im, double tol, int maxits);
+    int issue(int nstep, std::vector<int>* prof_tokens);
+    int advance(const int* ctl);
+
+  private:
+    System* S_ = nullptr;
+    const double* b_ = nullptr;
+    double* x_ = nullptr;
+    int im_ = 0, maxits_ = 0, its_in_ = 0, left_ = 0;
+    double tol_ = 0.0, bn_ = 0.0, rn_ = 0.0, predicted_ = -1.0;
+    double ro_ = 0.0, ro0_ = 0.0, eps1_ = 0.0, eps_in_ = 0.0;
+    GmresStats in_;
+    std::vector<double> rs_;
+    int hctl_[4] = {0, 0, 0, 0};
+    int outer_step();
+    int inner_begin();
+    int cycle_begin();
+    int inner_end(int ierr_in);
+};
 // y := alpha (A (x) K + B (x) M) x + beta y with the system's current A, B
 // (FP64, interleaved).
 int system_apply(System& S, double alpha, double beta, const double* x, double* y);
