@@ -512,14 +512,19 @@ def run_fp64_reference_point(xt, args):
 
 
 def run_variants(xt, args):
-    """The C2 slab two more ways, timed like fp64_gpu (CUDA events around
-    n slabs after one untimed slab): without the damage update (the solve,
-    load and jump terms only; sequential loop), and with the damage update
-    at a reduced temporal resolution (16 points per load cycle, 1,600 per
-    slab instead of 25,600; overlapped loop as the headline)."""
+    """The C2 slab more ways, timed like fp64_gpu (CUDA events around n
+    slabs after one untimed slab): without the damage update (the solve,
+    load and jump terms only; sequential loop); with the damage update at a
+    reduced temporal resolution (16 points per load cycle, 1,600 per slab
+    instead of 25,600; overlapped loop as the headline); and with the
+    block-Jacobi ILUT of 4 and 8 row blocks in place of the ILUT of K (a
+    different preconditioner from the reference's: more iterations, each
+    block's triangular solves on SMs of their own)."""
     out = {}
     variants = (("no_damage", {"damage": 0, "overlap": 0}),
-                ("reduced_nip", {"nipc": 16}))
+                ("reduced_nip", {"nipc": 16}),
+                ("ilu_blocks_4", {"ilu_blocks": 4}),
+                ("ilu_blocks_8", {"ilu_blocks": 8}))
     for name, change in variants:
         try:
             prob = make_problem(xt)
@@ -539,6 +544,7 @@ def run_variants(xt, args):
             prob.close()
             out[name] = {"value": round(n / (ms / 1e3), 4), "unit": UNIT, "steps": n,
                          "nip": cfg.nipc * cfg.n1, "damage": int(cfg.damage),
+                         "ilu_blocks": max(1, int(cfg.ilu_blocks)),
                          "iterations_per_slab": float(np.mean([s["its"] for s in st])),
                          "relres_max": float(max(s["relres"] for s in st))}
         except Exception as e:  # a failure here must not cost the headline line

@@ -186,6 +186,18 @@ int xt_system_destroy(xt_system s);
  * for the level schedule (3 for three DOFs per node; 1 = row levels). */
 int xt_system_set_ilu(xt_system s, const double *alu, const int *jlu,
                       const int *ju, int group);
+/* The same for a block-Jacobi factor of `blocks` row blocks
+ * (xth_ilut_blocks of include/xtfem_gb300_host.h): when the factor has no
+ * entry between the blocks, the FP32 register sweep runs each block's
+ * triangular solves in a thread block of its own (blocks x q thread
+ * blocks per sweep instead of q); other sweeps use the one schedule of the
+ * whole factor.  A factor with entries between blocks falls back to that
+ * schedule too.  blocks <= 1: xt_system_set_ilu. */
+int xt_system_set_ilu_blocks(xt_system s, const double *alu, const int *jlu,
+                             const int *ju, int group, int blocks);
+/* The row blocks the FP32 register sweep runs as independent solves (1 for
+ * the whole factor). */
+int xt_system_ilu_blocks(xt_system s);
 /* Temporal matrices A (with the slab-start jump) and B, q x q column-major. */
 int xt_system_set_temporal(xt_system s, const double *a, const double *b);
 /* kronspgemv semantics with explicit temporal matrices (host vectors,

@@ -70,6 +70,18 @@ int xth_problem_first_changed_row(xth_problem pr);
  * norm, with 1e-4 rounded to single precision as in the reference. */
 int xth_ilut(int n, const int *ia, const int *ja, const double *a, int lfil,
              double droptol, int iwk, double *alu, int *jlu, int *ju);
+/* Block-Jacobi ILUT: the ILUT above of A with its entries between `blocks`
+ * contiguous row blocks dropped first.  Block b holds whole node groups of
+ * `group` rows: rows from floor(ng b / blocks) group on, ng = n / group
+ * (group 1 when n is not a multiple of it).  The factor has no entry
+ * between blocks, so its triangular solves split into independent ones
+ * (xt_system_set_ilu_blocks runs them on separate SMs).  A weaker
+ * preconditioner than the ILUT of A (more GMRES iterations) with shorter
+ * dependency chains.  blocks <= 1: xth_ilut.  No counterpart in the
+ * reference, whose ILUT factors the whole K. */
+int xth_ilut_blocks(int n, const int *ia, const int *ja, const double *a, int lfil,
+                    double droptol, int iwk, int group, int blocks, double *alu, int *jlu,
+                    int *ju);
 /* The same factor when rows [0, first_row) of the matrix equal those of the
  * matrix prev_alu/prev_jlu/prev_ju was computed from (same lfil, droptol):
  * those rows are copied and the rest refactored (ILUT row i depends only on
@@ -141,6 +153,11 @@ typedef struct xt_slab_config {
                             solve when the true residual at a restart
                             exceeds the estimate it followed tenfold (the
                             basis has lost orthogonality). */
+    int ilu_blocks;      /* > 1: the block-Jacobi ILUT of that many row
+                            blocks (xth_ilut_blocks) in place of the ILUT of
+                            K, its blocks' triangular solves on separate SMs
+                            (xt_system_set_ilu_blocks); 0 or 1: the ILUT of
+                            K, as the reference. */
 } xt_slab_config;
 
 typedef struct xt_slab_s *xt_slab;

@@ -399,3 +399,63 @@ def test_device_driven_gmres_equals_host_driven(xt, rod_system, monkeypatch, chu
     sysm.close()
     assert info == info_ref
     assert np.array_equal(got, ref)
+
+
+# --- block-Jacobi ILUT: each row block's triangular solves in thread blocks
+# of their own
+
+@pytest.mark.parametrize("blocks", [2, 3, 5])
+def test_block_jacobi_ilu_sweep_matches_oracle(xt, orc, rod8_system, blocks):
+    """The factor of the block-Jacobi part of K (no entry between the row
+    blocks): the FP32 register sweep over blocks x 6 thread blocks gives the
+    oracle's FP64 lusol of the same factor to FP32 accuracy, and the sweep
+    of the factor's one schedule (XTFEM_ILU_BLOCKS=0) agrees with it."""
+    s = rod8_system
+    alu, jlu, ju = xt.ilut(s["K"], 20, 1e-4, blocks=blocks)
+    sysm = xt.SpaceTimeSystem(s["K"], s["M"])
+    sysm.set_ilu(alu, jlu, ju, group=3, blocks=blocks)
+    assert sysm.ilu_blocks == blocks
+    x = np.random.default_rng(7).standard_normal(s["K"].n * 6)
+    y_ref = orc.kronlusol(s["A"], alu, jlu, ju, x)
+    y = sysm.lusol(s["A"], x, fp32=True)
+    assert rel(y, y_ref) <= 1e-4
+    assert rel(sysm.lusol(s["A"], x), y_ref) <= 1e-10  # FP64 sweeps: one schedule
+    sysm.close()
+    import os
+    os.environ["XTFEM_ILU_BLOCKS"] = "0"
+    try:
+        one = xt.SpaceTimeSystem(s["K"], s["M"])
+        one.set_ilu(alu, jlu, ju, group=3, blocks=blocks)
+        y1 = one.lusol(s["A"], x, fp32=True)
+        one.close()
+    finally:
+        del os.environ["XTFEM_ILU_BLOCKS"]
+    assert rel(y1, y) <= 1e-5
+
+
+def test_block_jacobi_refined_solve_matches_oracle(xt, orc, rod_system):
+    """GMRES preconditioned by the block-Jacobi factor reaches the FP64 true
+    residual and the oracle's solution of the same system."""
+    s = rod_system
+    rhs = c1_rhs(xt, s)
+    alu, jlu, ju = xt.ilut(s["K"], 20, 1e-4, blocks=4)
+    sysm = xt.SpaceTimeSystem(s["K"], s["M"])
+    sysm.set_ilu(alu, jlu, ju, group=3, blocks=4)
+    sysm.set_temporal(s["A"], s["B"])
+    assert sysm.ilu_blocks == 4
+    sol, info = sysm.solve(rhs, im=30, tol=1e-8, maxits=3000, precision=2)
+    sysm.close()
+    assert info["ierr"] == 0 and info["relres"] <= 1e-8
+    sol_ref, ierr, _, _ = orc.kronpgmres(s["A"], s["B"], s["K"], s["M"], s["alu"], s["jlu"],
+                                         s["ju"], rhs, im=30, eps=1e-10, maxits=3000)
+    assert ierr == 0 and rel(sol, sol_ref) <= 1e-6
+
+
+def test_block_jacobi_factor_with_coupling_entries_falls_back(xt, rod_system):
+    """A factor with entries between the blocks (the ILUT of the whole K)
+    set with blocks > 1 keeps the one schedule."""
+    s = rod_system
+    sysm = xt.SpaceTimeSystem(s["K"], s["M"])
+    sysm.set_ilu(s["alu"], s["jlu"], s["ju"], group=3, blocks=4)
+    assert sysm.ilu_blocks == 1
+    sysm.close()

@@ -745,3 +745,34 @@ def test_holed_panel_generator(xt):
     # O-grid (3 % of them here)
     spread = lambda c: np.percentile(np.ptp(c, axis=1), 95)
     assert spread(cr) < spread(conn) / 3
+
+
+def test_block_jacobi_ilut_equals_oracle_ilut_of_block_part(xt, orc):
+    """xth_ilut_blocks = the oracle's ILUT of K with its entries between the
+    row blocks dropped (blocks of whole node groups: rows from
+    floor(ng b / blocks) * 3), bit for bit, and the factor has no entry
+    between blocks."""
+    pr = xt.Problem.rod(12, 4, 4, 3.0, 1.0, 1.0, 2.0e5, 0.3, 7.8e-9)
+    xyz, _ = pr.mesh()
+    bc = np.zeros(3 * len(xyz), np.int32)
+    bc[(3 * np.flatnonzero(xyz[:, 0] == 0.0)[:, None] + np.arange(3)).ravel()] = 1
+    pr.apply_bc(bc)
+    K = pr.K()
+    pr.close()
+    n, g = K.n, 3
+    for blocks in (2, 4, 5):
+        ng = n // g
+        bd = [(ng * b // blocks) * g for b in range(blocks + 1)]
+        part = np.searchsorted(np.array(bd), np.arange(n), side="right") - 1
+        rows = np.repeat(np.arange(n), np.diff(K.ia))
+        cols = K.ja - 1
+        keep = part[rows] == part[cols]
+        ia = np.concatenate([[1], 1 + np.cumsum(np.bincount(rows[keep], minlength=n))]).astype(np.int32)
+        Kb = xt.Csr(ia, K.ja[keep].astype(np.int32), K.a[keep].copy())
+        alu, jlu, ju = xt.ilut(K, 20, 1e-4, blocks=blocks, group=g)
+        (oalu, ojlu, oju), oerr = orc.ilut(Kb, 20, 1e-4)
+        assert oerr == 0
+        assert np.array_equal(alu, oalu) and np.array_equal(jlu, ojlu) and np.array_equal(ju, oju)
+        for r in range(n):
+            c = jlu[jlu[r] - 1:jlu[r + 1] - 1] - 1
+            assert np.all(part[c] == part[r])

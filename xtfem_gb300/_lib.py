@@ -44,6 +44,8 @@ SIGNATURES = {
     "xt_system_create": (C.c_int, [C.c_int, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp, C.POINTER(_vp)]),
     "xt_system_destroy": (C.c_int, [_vp]),
     "xt_system_set_ilu": (C.c_int, [_vp, _dp, _ip, _ip, C.c_int]),
+    "xt_system_set_ilu_blocks": (C.c_int, [_vp, _dp, _ip, _ip, C.c_int, C.c_int]),
+    "xt_system_ilu_blocks": (C.c_int, [_vp]),
     "xt_system_set_temporal": (C.c_int, [_vp, _dp, _dp]),
     "xt_system_apply": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_double, _dp, _dp]),
     "xt_system_lusol": (C.c_int, [_vp, _dp, _dp, _dp]),
@@ -78,6 +80,8 @@ SIGNATURES = {
     "xth_problem_apply_bc": (C.c_int, [_vp, _ip]),
     "xth_problem_delete": (C.c_int, [_vp, C.c_int, _ip, _ip, _ip]),
     "xth_ilut": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, _dp, _ip, _ip]),
+    "xth_ilut_blocks": (C.c_int, [C.c_int, _ip, _ip, _dp, C.c_int, C.c_double, C.c_int, C.c_int,
+                                  C.c_int, _dp, _ip, _ip]),
     "xth_stcoeff_m": (None, [C.c_double, C.c_double, C.c_double] + [_dp] * 6),
     "xth_stcoeff_t": (None, [C.c_double] + [_dp] * 6),
     "xth_getfextc_m": (None, [C.c_double, C.c_double, C.c_double, _dp, _dp]),

@@ -218,20 +218,27 @@ def kokkos_host(rank, ne, nn, ndofn, nnse, nnte, ngpe, ncmp, nip, nodes, Nx, Ny,
     _raise_if_error()
 
 
-def ilut(A: Csr, lfil=20, droptol=1e-4, iwk=None, reuse=None):
+def ilut(A: Csr, lfil=20, droptol=1e-4, iwk=None, reuse=None, blocks=1, group=3):
     """SPARSKIT ILUT on the host in FP64 (src/ilut.f:152-495).  Returns
     (alu, jlu, ju) in MSR form with 1-based indices, trimmed to size.  iwk
     is the capacity of alu/jlu (default: enough for any factor); an error
     raises XtError carrying SPARSKIT's ierr (.ierr).  reuse = (alu, jlu, ju,
     first_row): the factor of a matrix whose rows [0, first_row) equal A's
     (same lfil, droptol); those rows are copied, the others refactored, and
-    the result is A's factor bit for bit."""
+    the result is A's factor bit for bit.  blocks > 1: the block-Jacobi ILUT
+    of `blocks` contiguous row blocks of whole node groups of `group` rows
+    (xth_ilut_blocks; not with reuse)."""
     n = A.n
     iwk = iwk or n * (2 * max(lfil, 0) + 2) + n + 2
     alu = np.zeros(iwk)
     jlu = np.zeros(iwk, np.int32)
     ju = np.zeros(n, np.int32)
-    if reuse is None:
+    if blocks > 1:
+        if reuse is not None:
+            raise ValueError("ilut: blocks > 1 does not take reuse")
+        ierr = lib().xth_ilut_blocks(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk,
+                                     group, blocks, dptr(alu), iptr(jlu), iptr(ju))
+    elif reuse is None:
         ierr = lib().xth_ilut(n, iptr(A.ia), iptr(A.ja), dptr(A.a), lfil, droptol, iwk,
                               dptr(alu), iptr(jlu), iptr(ju))
     else:
@@ -306,11 +313,18 @@ class SpaceTimeSystem:
 
     __del__ = close
 
-    def set_ilu(self, alu, jlu, ju, group=3):
+    def set_ilu(self, alu, jlu, ju, group=3, blocks=1):
+        """blocks > 1: a block-Jacobi factor (ilut(..., blocks=)) whose row
+        blocks the FP32 register sweep runs as independent solves."""
         f = (_f64(alu), _i32(jlu), _i32(ju))
-        check(lib().xt_system_set_ilu(self._h, dptr(f[0]), iptr(f[1]), iptr(f[2]), group),
-              "set_ilu")
+        check(lib().xt_system_set_ilu_blocks(self._h, dptr(f[0]), iptr(f[1]), iptr(f[2]), group,
+                                             blocks), "set_ilu")
         self._f = f
+
+    @property
+    def ilu_blocks(self) -> int:
+        """Row blocks the FP32 register sweep runs as independent solves."""
+        return lib().xt_system_ilu_blocks(self._h)
 
     def set_temporal(self, a, b):
         check(lib().xt_system_set_temporal(self._h, dptr(_colmajor(a)), dptr(_colmajor(b))),
@@ -513,7 +527,7 @@ class SlabConfig(C.Structure):
                 ("im", C.c_int), ("tol", C.c_double), ("maxits", C.c_int),
                 ("precision", C.c_int), ("inner_tol", C.c_double), ("Dc", C.c_double),
                 ("damage", C.c_int), ("group", C.c_int), ("overlap", C.c_int),
-                ("load_ratio", C.c_double), ("gs_passes", C.c_int)]
+                ("load_ratio", C.c_double), ("gs_passes", C.c_int), ("ilu_blocks", C.c_int)]
 
     @classmethod
     def make(cls, **kw):
@@ -521,7 +535,7 @@ class SlabConfig(C.Structure):
                  amplitude=100.0, area=1.0, freq=20.0, dt0=0.005, n1=100, n2=10, nipc=256,
                  lfil=20, droptol=1e-4, im=30, tol=1e-8, maxits=3000, precision=0,
                  inner_tol=1e-5, Dc=0.99, damage=1, group=3, overlap=0, load_ratio=-1.0,
-                 gs_passes=0)
+                 gs_passes=0, ilu_blocks=0)
         d.update(kw)
         return cls(**d)
 

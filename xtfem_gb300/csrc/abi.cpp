@@ -214,6 +214,18 @@ int xt_system_destroy(xt_system s)
     return XT_OK;
 }
 
+int xt_system_set_ilu_blocks(xt_system s, const double* alu, const int* jlu, const int* ju,
+                             int group, int blocks)
+{
+    if (!s || !alu || !jlu || !ju) { set_error("xt_system_set_ilu: null argument"); return XT_ERR_ARG; }
+    return system_set_ilu(s->sys, alu, jlu, ju, group, blocks);
+}
+
+int xt_system_ilu_blocks(xt_system s)
+{
+    return (s && s->sys.ilu) ? std::max(1, s->sys.ilu->blocks) : 0;
+}
+
 int xt_system_set_ilu(xt_system s, const double* alu, const int* jlu, const int* ju, int group)
 {
     if (!s || !alu || !jlu || !ju) { set_error("xt_system_set_ilu: null argument"); return XT_ERR_ARG; }

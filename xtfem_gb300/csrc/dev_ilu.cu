@@ -669,6 +669,12 @@ struct IluStage {
     DBuf<int> srcL;
     DBuf<float> rrhsL, rrhsU;
     bool reg_ok = false;
+    // the same per row block of a block-Jacobi factor: one thread block per
+    // (block, temporal block), each block's sweep arguments in a device table
+    int parts = 0, ncw = 0, win_elems = 0;
+    long long lanesL = 0, lanesU = 0;
+    std::vector<std::shared_ptr<RegTri>> regLp, regUp;
+    DBuf<unsigned char> argsL, argsU;  // RegArgs per block
 };
 
 namespace {
@@ -1495,11 +1501,11 @@ int reg_warps(const TriHost& h, int GPW)
 }
 
 // Chunks, sub-levels, slots and steps of one triangle (no device data yet).
-bool reg_plan(const TriHost& h, int H, RegTri& t)
+bool reg_plan(const TriHost& h, int H, RegTri& t, int force_ncw = 0)
 {
     const int g = 3, GS = 3 * H, GPW = 32 / GS;
     t.H = H;
-    t.ncw = reg_warps(h, GPW);
+    t.ncw = force_ncw > 0 ? force_ncw : reg_warps(h, GPW);
     t.row_slot.assign((size_t)h.ngroups * g, -1);
     t.chunks.clear();
     t.chunk_slot.clear();
@@ -1546,7 +1552,7 @@ bool reg_plan(const TriHost& h, int H, RegTri& t)
 // Slots of a planned triangle.  dst: forward, the other triangle's
 // row_slot; backward (dst empty): row * Q.
 int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int>* dst,
-             cudaStream_t s)
+             cudaStream_t s, int row0 = 0)
 {
     const int g = 3, H = t.H, GS = 3 * H, GPW = 32 / GS;
     t.smax = smax;
@@ -1589,7 +1595,7 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
                 const int wo = h.slot[G] * g + r;
                 std::memcpy(&gm[lane * 4 + 3], &wo, 4);
                 const long long d = dst ? (long long)(*dst)[(size_t)G * g + r]
-                                        : ((long long)G * g + r) * Q;
+                                        : ((long long)row0 + (long long)G * g + r) * Q;
                 valid = valid && wo >= 0 && wo < t.zero_off && d >= 0 && d < INT32_MAX;
                 go[lane] = (int)d;
             }
@@ -1827,12 +1833,13 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned w
     }
 }
 
+// One temporal block tb of one sweep (one thread block).
 template <int H, int SMAX, bool UPPER, bool W16>
-__global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
+__device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
 {
     extern __shared__ __align__(16) float rwin[];
     if (a.skip && a.skip[0] != 0) return;  // uniform: before any barrier
-    const int tb = blockIdx.x, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     constexpr int GS = 3 * H;
     const int lane0 = (lane / GS) * GS;
     const unsigned wbase = (unsigned)__cvta_generic_to_shared(rwin);
@@ -1882,6 +1889,27 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
     }
 }
 
+template <int H, int SMAX, bool UPPER, bool W16>
+__global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
+{
+    tri_reg_body<H, SMAX, UPPER, W16>(a, blockIdx.x);
+}
+
+// One thread block per (row block, temporal block) of a block-Jacobi
+// factor: row block blockIdx.x / q with its sweep arguments from the table,
+// temporal block blockIdx.x % q; the output, the prefetch distance and the
+// skip flag are the launch's.
+template <int H, int SMAX, bool UPPER, bool W16>
+__global__ void __launch_bounds__(kRegMaxWarps * 32, 1)
+    k_tri_reg_parts(const RegArgs* __restrict__ args, int q, int pf, const int* skip, float* out)
+{
+    RegArgs a = args[blockIdx.x / q];
+    a.pf = pf;
+    a.skip = skip;
+    a.out = out;
+    tri_reg_body<H, SMAX, UPPER, W16>(a, blockIdx.x % q);
+}
+
 // Forward-sweep right-hand sides in lane-slot order, one array per temporal
 // block: rhs[q][s] = sum_j Ainv(q, j) v(row(s), j) (0 for unused slots).
 template <int Q>
@@ -1909,6 +1937,92 @@ __global__ void k_rhs_slots(const int* __restrict__ src, long long lanes,
     }
 }
 
+// Register layouts of every row block of a block-Jacobi factor, with the
+// warps, steps per lane and offset width of the whole set (the largest
+// block's warps, the longest row's steps); the blocks' lanes are laid end
+// to end, so the pre-pass and the right-hand-side arrays are those of one
+// factor.  Leaves st.reg_ok false when a block does not fit.
+int build_reg_parts(const DevIlu& F, int Q, int H, IluStage& st, cudaStream_t s)
+{
+    st.reg_ok = false;
+    const int P = F.blocks;
+    if (P < 2 || (int)F.part_sched.size() != P || (H != 1 && H != 2 && H != 4)) return XT_OK;
+    const int GPW = 32 / (3 * H);
+    int ncw = 1;
+    for (const auto& ps : F.part_sched) {
+        if (ps->L.g != 3) return XT_OK;
+        ncw = std::max(ncw, std::max(reg_warps(ps->L, GPW), reg_warps(ps->U, GPW)));
+    }
+    std::vector<std::shared_ptr<RegTri>> Ls(P), Us(P);
+    int need = 0, win = 0;
+    for (int b = 0; b < P; ++b) {
+        Ls[b] = std::make_shared<RegTri>();
+        Us[b] = std::make_shared<RegTri>();
+        if (!reg_plan(F.part_sched[b]->L, H, *Ls[b], ncw) ||
+            !reg_plan(F.part_sched[b]->U, H, *Us[b], ncw))
+            return XT_OK;
+        need = std::max(need, std::max(Ls[b]->smax, Us[b]->smax));
+        win = std::max(win, std::max(Ls[b]->win_elems, Us[b]->win_elems));
+    }
+    const int smax = reg_smax(H, need);
+    if (smax == 0) return XT_OK;
+    const bool w16 = (long long)win * 4 <= 65536 && env_int("XTFEM_ILU_W16", 1) != 0;
+    std::vector<long long> offL(P + 1, 0), offU(P + 1, 0);
+    for (int b = 0; b < P; ++b) {
+        offL[b + 1] = offL[b] + Ls[b]->lanes;
+        offU[b + 1] = offU[b] + Us[b]->lanes;
+    }
+    if (offL[P] >= INT32_MAX || offU[P] >= INT32_MAX) return XT_OK;
+    std::vector<int> src((size_t)offL[P], -1);
+    for (int b = 0; b < P; ++b) {
+        Ls[b]->w16 = Us[b]->w16 = w16;
+        XT_TRY(reg_fill(F.part_sched[b]->U, *Us[b], smax, Q, nullptr, s, F.bounds[b]));
+        for (int& v : Us[b]->row_slot)
+            if (v >= 0) v += (int)offU[b];
+        XT_TRY(reg_fill(F.part_sched[b]->L, *Ls[b], smax, Q, &Us[b]->row_slot, s));
+        if (!Ls[b]->slots.p || !Us[b]->slots.p) return XT_OK;
+        for (size_t r = 0; r < Ls[b]->row_slot.size(); ++r)
+            src[(size_t)(offL[b] + Ls[b]->row_slot[r])] = F.bounds[b] + (int)r;
+        Ls[b]->row_slot.clear();
+        Us[b]->row_slot.clear();
+    }
+    XT_TRY(st.srcL.upload(src.data(), src.size(), s));
+    XT_TRY(st.rrhsL.alloc((size_t)Q * offL[P]));
+    XT_TRY(st.rrhsU.alloc((size_t)Q * offU[P]));
+    XT_CUDA(cudaMemsetAsync(st.rrhsU.p, 0, sizeof(float) * Q * offU[P], s));
+    std::vector<RegArgs> aL(P), aU(P);
+    for (int b = 0; b < P; ++b) {
+        aL[b] = RegArgs{Ls[b]->slots.p, st.rrhsL.p + offL[b], nullptr, offL[P], offU[P],
+                        Ls[b]->nl, ncw, Ls[b]->slot_bytes, Ls[b]->zero_off, 0, nullptr};
+        aU[b] = RegArgs{Us[b]->slots.p, st.rrhsU.p + offU[b], nullptr, offU[P], 0,
+                        Us[b]->nl, ncw, Us[b]->slot_bytes, Us[b]->zero_off, 0, nullptr};
+    }
+    XT_TRY(st.argsL.upload(reinterpret_cast<const unsigned char*>(aL.data()), sizeof(RegArgs) * P, s));
+    XT_TRY(st.argsU.upload(reinterpret_cast<const unsigned char*>(aU.data()), sizeof(RegArgs) * P, s));
+    XT_CUDA(cudaStreamSynchronize(s));
+    if (trace_on()) {
+        int nlL = 0, nlU = 0;
+        for (int b = 0; b < P; ++b) {
+            nlL = std::max(nlL, Ls[b]->nl);
+            nlU = std::max(nlU, Us[b]->nl);
+        }
+        std::fprintf(stderr,
+                     "[xtfem] register sweep over %d row blocks: H %d, steps %d, warps %d, "
+                     "levels at most %d/%d\n", P, H, smax, ncw, nlL, nlU);
+    }
+    st.parts = P;
+    st.ncw = ncw;
+    st.win_elems = win;
+    st.lanesL = offL[P];
+    st.lanesU = offU[P];
+    st.regLp = Ls;
+    st.regUp = Us;
+    st.regL = Ls[0];  // H, steps and offset width of the set
+    st.regU = Us[0];
+    st.reg_ok = true;
+    return XT_OK;
+}
+
 template <int Q, int H, int SMAX, bool W16>
 int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
                const int* skip)
@@ -1921,11 +2035,32 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         attr.store(true, std::memory_order_release);
     }
+    const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
+    if (st.parts > 1) {
+        static std::atomic<bool> pattr{false};
+        if (!pattr.load(std::memory_order_acquire)) {
+            XT_CUDA(cudaFuncSetAttribute(k_tri_reg_parts<H, SMAX, false, W16>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+            XT_CUDA(cudaFuncSetAttribute(k_tri_reg_parts<H, SMAX, true, W16>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+            pattr.store(true, std::memory_order_release);
+        }
+        const int nb = (int)std::max(1LL, std::min<long long>((st.lanesL + 255) / 256, 152LL * 8));
+        k_rhs_slots<Q><<<nb, 256, 0, s>>>(st.srcL.p, st.lanesL, dAinv, v, st.rrhsL.p, skip);
+        const RegArgs* aL = reinterpret_cast<const RegArgs*>(st.argsL.p);
+        const RegArgs* aU = reinterpret_cast<const RegArgs*>(st.argsU.p);
+        const size_t smem = (size_t)st.win_elems * 4;
+        k_tri_reg_parts<H, SMAX, false, W16><<<Q * st.parts, st.ncw * 32, smem, s>>>(aL, Q, pf, skip,
+                                                                                  st.rrhsU.p);
+        k_tri_reg_parts<H, SMAX, true, W16><<<Q * st.parts, st.ncw * 32, smem, s>>>(aU, Q, pf, skip, z);
+        note_launches(3);
+        XT_CUDA(cudaGetLastError());
+        return XT_OK;
+    }
     const RegTri& L = *st.regL;
     const RegTri& U = *st.regU;
     const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
     k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p, skip);
-    const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
     RegArgs aL{L.slots.p, st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw, L.slot_bytes,
                L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
@@ -1994,8 +2129,10 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
     const int wkey = (col || fmt == 4) ? std::max(0, std::min(31, env_int("XTFEM_ILU_WARPS", 0))) +
                                              (fmt == 4 && env_int("XTFEM_ILU_BANKS", 1) == 0 ? 32 : 0)
                                        : 0;
+    const int bkey = (fmt == 4 && F.blocks > 1 && env_int("XTFEM_ILU_BLOCKS", 1) != 0) ? 1 : 0;
     const int key =
-        ((((q * 8 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 8 + (hkey ? H : 0)) * 64 + wkey) * 256 + rkb;
+        (((((q * 8 + fmt) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 8 + (hkey ? H : 0)) * 64 + wkey) * 2 +
+         bkey) * 256 + rkb;
     (void)wenv;
     auto it = F.stages.find(key);
     if (it == F.stages.end()) {
@@ -2010,7 +2147,10 @@ int get_stage(const DevIlu& F, int q, int fmt, cudaStream_t s, IluStage*& out, i
             gdU[G] = G * g;
         }
         if (fmt == 4) {
-            if (sizeof(T) == 4) XT_TRY(build_reg(*F.sched, q, H, *st, s));
+            // XTFEM_ILU_BLOCKS=0: the one schedule of a block-Jacobi factor
+            if (sizeof(T) == 4 && F.blocks > 1 && env_int("XTFEM_ILU_BLOCKS", 1) != 0)
+                XT_TRY(build_reg_parts(F, q, H, *st, s));
+            if (sizeof(T) == 4 && !st->reg_ok) XT_TRY(build_reg(*F.sched, q, H, *st, s));
             it = F.stages.emplace(key, st).first;
             out = st->reg_ok ? st.get() : nullptr;
             return XT_OK;
@@ -2222,8 +2362,33 @@ int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
 
 }  // namespace
 
+namespace {
+// The rows [r0, r1) of a 1-based MSR factor with no entry outside them, as
+// a factor of their own (local 1-based indices).
+void sub_factor(const double* alu, const int* jlu, const int* ju, int r0, int r1,
+                std::vector<double>& a, std::vector<int>& jl, std::vector<int>& jd)
+{
+    const int m = r1 - r0;
+    a.assign((size_t)m + 1, 0.0);
+    jl.assign((size_t)m + 1, 0);
+    jd.assign((size_t)m, 0);
+    for (int r = 0; r < m; ++r) a[r] = alu[r0 + r];
+    jl[0] = m + 2;
+    for (int r = 0; r < m; ++r) {
+        const int gr = r0 + r;
+        for (int k = jlu[gr] - 1; k < jlu[gr + 1] - 1; ++k) {
+            if (k == ju[gr] - 1) jd[r] = (int)jl.size() + 1;
+            a.push_back(alu[k]);
+            jl.push_back(jlu[k] - r0);
+        }
+        if (ju[gr] == jlu[gr + 1]) jd[r] = (int)jl.size() + 1;  // no U part
+        jl[r + 1] = (int)jl.size() + 1;
+    }
+}
+}  // namespace
+
 int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju, int group,
-              cudaStream_t s)
+              cudaStream_t s, int blocks)
 {
     if (n <= 0 || !alu || !jlu || !ju) {
         set_error("build_ilu: bad arguments");
@@ -2254,6 +2419,37 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
     XT_TRY(upload_tri(d.U, sc->U, s));
     d.sched = sc;
     d.stages.clear();
+    d.blocks = 1;
+    d.bounds.clear();
+    d.part_sched.clear();
+    if (blocks > 1) {
+        const std::vector<int> bd = ilu_block_bounds(n, g, blocks);
+        const int nb = (int)bd.size() - 1;
+        bool diag = nb > 1;
+        for (int b = 0; diag && b < nb; ++b)
+            for (int r = bd[b]; diag && r < bd[b + 1]; ++r)
+                for (int k = jlu[r] - 1; k < jlu[r + 1] - 1; ++k) {
+                    const int c = jlu[k] - 1;
+                    if (c < bd[b] || c >= bd[b + 1]) {
+                        diag = false;
+                        break;
+                    }
+                }
+        if (diag) {
+            std::vector<double> a;
+            std::vector<int> jl, jd;
+            for (int b = 0; b < nb; ++b) {
+                sub_factor(alu, jlu, ju, bd[b], bd[b + 1], a, jl, jd);
+                auto ps = std::make_shared<IluSched>();
+                const int m = bd[b + 1] - bd[b];
+                ps->L = schedule(m, a.data(), jl.data(), jd.data(), g, false);
+                ps->U = schedule(m, a.data(), jl.data(), jd.data(), g, true);
+                d.part_sched.push_back(ps);
+            }
+            d.blocks = nb;
+            d.bounds = bd;
+        }
+    }
     return XT_OK;
 }
 

@@ -422,6 +422,28 @@ int xth_ilut(int n, const int* ia, const int* ja, const double* a, int lfil, dou
     return ilut_into(n, ia, ja, a, lfil, droptol, iwk, alu, jlu, ju, nullptr, 0);
 }
 
+int xth_ilut_blocks(int n, const int* ia, const int* ja, const double* a, int lfil,
+                    double droptol, int iwk, int group, int blocks, double* alu, int* jlu, int* ju)
+{
+    if (n <= 0 || !ia || !ja || !a) {
+        set_error("xth_ilut_blocks: bad arguments");
+        return XT_ERR_ARG;
+    }
+    if (blocks <= 1) return ilut_into(n, ia, ja, a, lfil, droptol, iwk, alu, jlu, ju, nullptr, 0);
+    Csr m, b;
+    const int rc = guarded([&] {
+        m.n = n;
+        m.ia.assign(ia, ia + n + 1);
+        m.ja.assign(ja, ja + (ia[n] - 1));
+        m.a.assign(a, a + (ia[n] - 1));
+        b = block_diagonal(m, group, blocks);
+        return 0;
+    });
+    if (rc != 0) return rc;
+    return ilut_into(n, b.ia.data(), b.ja.data(), b.a.data(), lfil, droptol, iwk, alu, jlu, ju,
+                     nullptr, 0);
+}
+
 int xth_ilut_update(int n, const int* ia, const int* ja, const double* a, int lfil,
                     double droptol, int iwk, int first_row, const double* prev_alu,
                     const int* prev_jlu, const int* prev_ju, double* alu, int* jlu, int* ju)

@@ -371,6 +371,40 @@ bool ilut_on(const Csr& A, int lfil, double droptol, int T, Msr& F, int& ierr,
 // set up side by side) each take one thread instead of all of them
 static std::atomic<int> g_running{0};
 
+std::vector<int> ilu_block_bounds(int n, int g, int blocks)
+{
+    if (g < 1 || n % g) g = 1;
+    const long long ng = n / g;
+    blocks = std::max(1, std::min<int>(blocks, (int)std::max<long long>(ng, 1)));
+    std::vector<int> b(blocks + 1);
+    for (int k = 0; k <= blocks; ++k) b[k] = (int)(ng * k / blocks) * g;
+    return b;
+}
+
+Csr block_diagonal(const Csr& A, int g, int blocks)
+{
+    if (blocks <= 1) return A;
+    const std::vector<int> bd = ilu_block_bounds(A.n, g, blocks);
+    Csr B;
+    B.n = A.n;
+    B.ia.assign(A.n + 1, 1);
+    B.ja.reserve(A.ja.size());
+    B.a.reserve(A.a.size());
+    int blk = 0;
+    for (int r = 0; r < A.n; ++r) {
+        while (r >= bd[blk + 1]) ++blk;
+        for (int k = A.ia[r] - 1; k < A.ia[r + 1] - 1; ++k) {
+            const int c = A.ja[k] - 1;
+            if (c >= bd[blk] && c < bd[blk + 1]) {
+                B.ja.push_back(A.ja[k]);
+                B.a.push_back(A.a[k]);
+            }
+        }
+        B.ia[r + 1] = (int)B.ja.size() + 1;
+    }
+    return B;
+}
+
 int ilut(const Csr& A, int lfil, double droptol, Msr& F, const Msr* prev, int first_row)
 {
     if (lfil < 0) return -4;

@@ -100,6 +100,16 @@ struct Msr {
 int ilut(const Csr& A, int lfil, double droptol, Msr& out, const Msr* prev = nullptr,
          int first_row = 0);
 
+// Row bounds of the block-Jacobi ILU's `blocks` contiguous row blocks of
+// whole node groups of g rows (blocks + 1 entries, 0-based rows):
+// floor(ng b / blocks) g with ng = n / g (g = 1 when n is not a multiple of g).
+std::vector<int> ilu_block_bounds(int n, int g, int blocks);
+// The block-Jacobi part of A: its entries whose row and column lie in the
+// same block of ilu_block_bounds(n, g, blocks); blocks <= 1 gives A.  Its
+// ILUT has no entry between blocks, so the triangular solves of the blocks
+// are independent.
+Csr block_diagonal(const Csr& A, int g, int blocks);
+
 // src/stcoeff.f90:62-356 closed forms (6x6 each, column-major).
 void stcoeff_m(double t1, double dt, double w, double* k, double* m,
                double* ktn, double* mtn, double* ktn1, double* mtn1);

@@ -89,7 +89,11 @@ namespace {
 // factor).
 int refactor(xt_slab_s& s, int first_row = 0)
 {
-    const Csr& K = s.pr->sys.K;
+    // cfg.ilu_blocks > 1: the block-Jacobi part of K (its rows are as
+    // row-local as K's, so the kept rows stay valid)
+    Csr Kb;
+    if (s.cfg.ilu_blocks > 1) Kb = block_diagonal(s.pr->sys.K, s.cfg.group, s.cfg.ilu_blocks);
+    const Csr& K = s.cfg.ilu_blocks > 1 ? Kb : s.pr->sys.K;
     Msr f;
     const Msr* prev = (first_row > 0 && s.fac.n == K.n) ? &s.fac : nullptr;
     const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f, prev, first_row);
@@ -98,7 +102,8 @@ int refactor(xt_slab_s& s, int first_row = 0)
         set_error("ILUT failed with ierr = " + std::to_string(ierr));
         return XT_ERR_HOST;
     }
-    XT_TRY(system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group));
+    XT_TRY(system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group,
+                          s.cfg.ilu_blocks));
     s.fac = std::move(f);
     return XT_OK;
 }
@@ -121,12 +126,16 @@ int refactor_device(xt_slab_s& s)
     for (int& v : K.ja) ++v;
     s.fac = Msr{};  // the kept factor no longer matches the host K
     Msr f;
-    const int ierr = ilut(K, s.cfg.lfil, s.cfg.droptol, f);
+    const int ierr = s.cfg.ilu_blocks > 1
+                         ? ilut(block_diagonal(K, s.cfg.group, s.cfg.ilu_blocks), s.cfg.lfil,
+                                s.cfg.droptol, f)
+                         : ilut(K, s.cfg.lfil, s.cfg.droptol, f);
     if (ierr != 0) {
         set_error("ILUT of the reassembled K failed with ierr = " + std::to_string(ierr));
         return XT_ERR_HOST;
     }
-    return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group);
+    return system_set_ilu(s.S, f.alu.data(), f.jlu.data(), f.ju.data(), s.cfg.group,
+                          s.cfg.ilu_blocks);
 }
 
 // Maps of the coupled loop for the live elements: K's element pattern and
@@ -604,7 +613,8 @@ int xt_slab_create(xth_problem h, const xt_slab_config* cfg, xt_slab* out)
         if (cfg->clamp_axis < 0 || cfg->clamp_axis > 2 || cfg->load_axis < 0 || cfg->load_axis > 2 ||
             cfg->load_comp < 0 || cfg->load_comp > 2 || cfg->im < 1 || cfg->dt0 <= 0 || cfg->n1 < 1 ||
             cfg->n2 < 1 || cfg->nipc < 0 || cfg->lfil < 0 || !(cfg->load_ratio >= -1.0) ||
-            !(cfg->load_ratio < 1.0) || cfg->gs_passes < 0 || cfg->gs_passes > 2) {
+            !(cfg->load_ratio < 1.0) || cfg->gs_passes < 0 || cfg->gs_passes > 2 ||
+            cfg->ilu_blocks < 0) {
             set_error("xt_slab_create: invalid configuration");
             return XT_ERR_ARG;
         }

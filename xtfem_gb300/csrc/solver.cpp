@@ -166,7 +166,8 @@ int system_create(System& S, int p, int q, const int* ki, const int* kj, const d
     return XT_OK;
 }
 
-int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group)
+int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group,
+                   int blocks)
 {
     // a factorisation that broke down (a pivot at or near zero) leaves
     // infinities or NaNs in the factor; every apply would then return them
@@ -178,7 +179,7 @@ int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, 
         }
     auto f = std::make_shared<DevIlu>();
     XT_TRY(system_stream(S));
-    XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, S.stream));
+    XT_TRY(build_ilu(*f, S.p, alu, jlu, ju, group, S.stream, blocks));
     S.ilu = f;
     return XT_OK;
 }

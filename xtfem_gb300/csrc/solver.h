@@ -67,7 +67,8 @@ int system_stream(System& S);
 // Status-returning building blocks
 int system_create(System& S, int p, int q, const int* ki, const int* kj, const double* kv,
                   const int* mi, const int* mj, const double* mv);
-int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group);
+int system_set_ilu(System& S, const double* alu, const int* jlu, const int* ju, int group,
+                   int blocks = 1);
 int system_set_temporal(System& S, const double* A, const double* B);
 // Device reassembly of K from per-Gauss-point moduli (dev_assembly.cu):
 // the mesh and constrained DOFs once, then any number of reassemblies.

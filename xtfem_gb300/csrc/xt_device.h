@@ -198,11 +198,21 @@ struct DevIlu {
     // rows at 1, 5 at 2, 2 at 4); 0 = XTFEM_ILU_SHARES or 2.  Set by the
     // batch tuner.
     mutable int shares = 0;
+    // block-Jacobi factor: independent row blocks (1 = the whole factor),
+    // their row bounds and one schedule per block
+    int blocks = 1;
+    std::vector<int> bounds;
+    std::vector<std::shared_ptr<IluSched>> part_sched;
 };
 
 // Build the level schedule from the 1-based MSR arrays and upload it.
+// blocks > 1: a block-Jacobi factor of that many row blocks (the bounds of
+// ilu_block_bounds); when it has no entry between blocks, each block also
+// gets a schedule of its own for the FP32 register sweep.
 int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju,
-              int group, cudaStream_t s);
+              int group, cudaStream_t s, int blocks = 1);
+// Row bounds of the block-Jacobi ILU's blocks (host_ilut.cpp).
+std::vector<int> ilu_block_bounds(int n, int g, int blocks);
 
 // z := (Ainv (x) (LU)^-1) v on interleaved blocks: the q x q mixing with the
 // inverse temporal matrix is applied to v first (it commutes with the
