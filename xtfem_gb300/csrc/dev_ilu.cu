@@ -1808,17 +1808,18 @@ template <int H, int SMAX, bool W16>
 __device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned wbase, float* win,
                                           float* out, int lane0)
 {
-    float acc0 = 0.0f, acc1 = 0.0f;
+    // four accumulators: dependent chains of SMAX / 4 multiply-adds
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
 #pragma unroll
     for (int k = 0; k < SMAX / 4; ++k) {
         const float x0 = lds_f(wbase + S.off[k].at(0)), x1 = lds_f(wbase + S.off[k].at(1));
         const float x2 = lds_f(wbase + S.off[k].at(2)), x3 = lds_f(wbase + S.off[k].at(3));
         acc0 = fmaf(S.val[k].x, x0, acc0);
         acc1 = fmaf(S.val[k].y, x1, acc1);
-        acc0 = fmaf(S.val[k].z, x2, acc0);
-        acc1 = fmaf(S.val[k].w, x3, acc1);
+        acc2 = fmaf(S.val[k].z, x2, acc2);
+        acc3 = fmaf(S.val[k].w, x3, acc3);
     }
-    float acc = acc0 + acc1;
+    float acc = (acc0 + acc1) + (acc2 + acc3);
 #pragma unroll
     for (int m = 1; m < H; m <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
     const float d = S.b - acc;
@@ -1833,8 +1834,9 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned w
     }
 }
 
-// One temporal block tb of one sweep (one thread block).
-template <int H, int SMAX, bool UPPER, bool W16>
+// One temporal block tb of one sweep (one thread block).  D3: three
+// register sets, so a set's loads have two levels of work to land in.
+template <int H, int SMAX, bool UPPER, bool W16, bool D3>
 __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
 {
     extern __shared__ __align__(16) float rwin[];
@@ -1862,7 +1864,59 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
                 prefetch_l2(a.rhs + (size_t)tb * a.rstride + ((size_t)L * a.ncw + warp) * 32);
         }
     };
-    for (int L = 2; L < 2 + a.pf; ++L) prefetch(L);
+    constexpr int DEP = D3 ? 3 : 2;  // register sets: loads DEP levels ahead
+    for (int L = DEP; L < DEP + a.pf; ++L) prefetch(L);
+    // In the level loop the prefetch is a running pointer: the line this
+    // thread touches at level DEP + pf, advanced by one level's worth (no
+    // address arithmetic per level).  pfl: the loop's last level index l
+    // whose level l + DEP + pf exists.
+    const bool pf_slot = a.pf > 0 && lane * 128 < a.slot_bytes;
+    const bool pf_rhs = a.pf > 0 && !pf_slot && lane == 31;
+    const unsigned char* pp =
+        pf_slot ? a.slots + ((size_t)(DEP + a.pf) * a.ncw + warp) * a.slot_bytes + (size_t)lane * 128
+                : reinterpret_cast<const unsigned char*>(
+                      a.rhs + (size_t)tb * a.rstride + ((size_t)(DEP + a.pf) * a.ncw + warp) * 32);
+    const size_t pstep = pf_slot ? sstep : (size_t)a.ncw * 32 * sizeof(float);
+    const bool pf_on = pf_slot || pf_rhs;
+    const int pfl = a.nl - DEP - a.pf;
+    if constexpr (D3) {
+        // three register sets, three levels per trip
+        RegSet<SMAX, W16> s0, s1, s2;
+        reg_load<SMAX, W16>(s0, sp, bp, lane);
+        if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
+        if (a.nl > 2) reg_load<SMAX, W16>(s2, sp + 2 * sstep, bp + 2 * a.ncw * 32, lane);
+        sp += 3 * sstep;
+        bp += 3 * a.ncw * 32;
+        level_barrier();  // the zero slot is set
+        for (int l = 0; l < a.nl; l += 3) {
+            reg_level<H, SMAX, W16>(s0, wbase, rwin, out, lane0);
+            if (l + 3 < a.nl) reg_load<SMAX, W16>(s0, sp, bp, lane);
+            if (pf_on && l < pfl) prefetch_l2(pp);
+            pp += pstep;
+            sp += sstep;
+            bp += a.ncw * 32;
+            level_barrier();
+            if (l + 1 < a.nl) {
+                reg_level<H, SMAX, W16>(s1, wbase, rwin, out, lane0);
+                if (l + 4 < a.nl) reg_load<SMAX, W16>(s1, sp, bp, lane);
+                if (pf_on && l + 1 < pfl) prefetch_l2(pp);
+                pp += pstep;
+                sp += sstep;
+                bp += a.ncw * 32;
+                level_barrier();
+            }
+            if (l + 2 < a.nl) {
+                reg_level<H, SMAX, W16>(s2, wbase, rwin, out, lane0);
+                if (l + 5 < a.nl) reg_load<SMAX, W16>(s2, sp, bp, lane);
+                if (pf_on && l + 2 < pfl) prefetch_l2(pp);
+                pp += pstep;
+                sp += sstep;
+                bp += a.ncw * 32;
+                level_barrier();
+            }
+        }
+        return;
+    }
     // two register sets, a pair of levels per trip: the set a level used is
     // reloaded, right after it, with the level two ahead
     RegSet<SMAX, W16> s0, s1;
@@ -1874,14 +1928,16 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     for (int l = 0; l < a.nl; l += 2) {
         reg_level<H, SMAX, W16>(s0, wbase, rwin, out, lane0);
         if (l + 2 < a.nl) reg_load<SMAX, W16>(s0, sp, bp, lane);
-        prefetch(l + 2 + a.pf);
+        if (pf_on && l < pfl) prefetch_l2(pp);
+        pp += pstep;
         sp += sstep;
         bp += a.ncw * 32;
         level_barrier();
         if (l + 1 < a.nl) {
             reg_level<H, SMAX, W16>(s1, wbase, rwin, out, lane0);
             if (l + 3 < a.nl) reg_load<SMAX, W16>(s1, sp, bp, lane);
-            prefetch(l + 3 + a.pf);
+            if (pf_on && l + 1 < pfl) prefetch_l2(pp);
+            pp += pstep;
             sp += sstep;
             bp += a.ncw * 32;
             level_barrier();
@@ -1889,10 +1945,10 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     }
 }
 
-template <int H, int SMAX, bool UPPER, bool W16>
+template <int H, int SMAX, bool UPPER, bool W16, bool D3>
 __global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
 {
-    tri_reg_body<H, SMAX, UPPER, W16>(a, blockIdx.x);
+    tri_reg_body<H, SMAX, UPPER, W16, D3>(a, blockIdx.x);
 }
 
 // One thread block per (row block, temporal block) of a block-Jacobi
@@ -1907,7 +1963,7 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1)
     a.pf = pf;
     a.skip = skip;
     a.out = out;
-    tri_reg_body<H, SMAX, UPPER, W16>(a, blockIdx.x % q);
+    tri_reg_body<H, SMAX, UPPER, W16, false>(a, blockIdx.x % q);
 }
 
 // Forward-sweep right-hand sides in lane-slot order, one array per temporal
@@ -2023,15 +2079,15 @@ int build_reg_parts(const DevIlu& F, int Q, int H, IluStage& st, cudaStream_t s)
     return XT_OK;
 }
 
-template <int Q, int H, int SMAX, bool W16>
+template <int Q, int H, int SMAX, bool W16, bool D3 = false>
 int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
                const int* skip)
 {
     static std::atomic<bool> attr{false};
     if (!attr.load(std::memory_order_acquire)) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, W16>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, W16, D3>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, W16>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, W16, D3>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         attr.store(true, std::memory_order_release);
     }
@@ -2065,8 +2121,8 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
                L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
                skip};
-    k_tri_reg<H, SMAX, false, W16><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
-    k_tri_reg<H, SMAX, true, W16><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
+    k_tri_reg<H, SMAX, false, W16, D3><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
+    k_tri_reg<H, SMAX, true, W16, D3><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -2080,6 +2136,12 @@ int launch_reg_width(const IluStage& st, const double* dAinv, const float* v, fl
     if (st.regL->w16 != st.regU->w16) {
         set_error("register sweep: triangles with different offset widths");
         return XT_ERR_STATE;
+    }
+    // three register sets (16-bit offsets, at most 12 steps per lane;
+    // XTFEM_ILU_DEPTH=2: two)
+    if constexpr (SMAX <= 12) {
+        if (st.regL->w16 && st.parts <= 1 && env_int("XTFEM_ILU_DEPTH", 3) == 3)
+            return launch_reg<Q, H, SMAX, true, true>(st, dAinv, v, z, s, skip);
     }
     if (st.regL->w16) return launch_reg<Q, H, SMAX, true>(st, dAinv, v, z, s, skip);
     return launch_reg<Q, H, SMAX, false>(st, dAinv, v, z, s, skip);
