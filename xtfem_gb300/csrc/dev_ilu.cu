@@ -1834,9 +1834,9 @@ __device__ __forceinline__ void reg_level(const RegSet<SMAX, W16>& S, unsigned w
     }
 }
 
-// One temporal block tb of one sweep (one thread block).  D3: three
-// register sets, so a set's loads have two levels of work to land in.
-template <int H, int SMAX, bool UPPER, bool W16, bool D3>
+// One temporal block tb of one sweep (one thread block).  DEP register
+// sets (2, 3 or 4): a set's loads have DEP - 1 levels of work to land in.
+template <int H, int SMAX, bool UPPER, bool W16, int DEP>
 __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
 {
     extern __shared__ __align__(16) float rwin[];
@@ -1864,7 +1864,6 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
                 prefetch_l2(a.rhs + (size_t)tb * a.rstride + ((size_t)L * a.ncw + warp) * 32);
         }
     };
-    constexpr int DEP = D3 ? 3 : 2;  // register sets: loads DEP levels ahead
     for (int L = DEP; L < DEP + a.pf; ++L) prefetch(L);
     // In the level loop the prefetch is a running pointer: the line this
     // thread touches at level DEP + pf, advanced by one level's worth (no
@@ -1879,7 +1878,36 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     const size_t pstep = pf_slot ? sstep : (size_t)a.ncw * 32 * sizeof(float);
     const bool pf_on = pf_slot || pf_rhs;
     const int pfl = a.nl - DEP - a.pf;
-    if constexpr (D3) {
+    // one level: compute it with set S, reload S with the level DEP ahead,
+    // prefetch, advance, barrier
+    auto level = [&](RegSet<SMAX, W16>& S, int lk) {
+        reg_level<H, SMAX, W16>(S, wbase, rwin, out, lane0);
+        if (lk + DEP < a.nl) reg_load<SMAX, W16>(S, sp, bp, lane);
+        if (pf_on && lk < pfl) prefetch_l2(pp);
+        pp += pstep;
+        sp += sstep;
+        bp += a.ncw * 32;
+        level_barrier();
+    };
+    if constexpr (DEP == 4) {
+        // four register sets, four levels per trip
+        RegSet<SMAX, W16> s0, s1, s2, s3;
+        reg_load<SMAX, W16>(s0, sp, bp, lane);
+        if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
+        if (a.nl > 2) reg_load<SMAX, W16>(s2, sp + 2 * sstep, bp + 2 * a.ncw * 32, lane);
+        if (a.nl > 3) reg_load<SMAX, W16>(s3, sp + 3 * sstep, bp + 3 * a.ncw * 32, lane);
+        sp += 4 * sstep;
+        bp += 4 * a.ncw * 32;
+        level_barrier();  // the zero slot is set
+        for (int l = 0; l < a.nl; l += 4) {
+            level(s0, l);
+            if (l + 1 < a.nl) level(s1, l + 1);
+            if (l + 2 < a.nl) level(s2, l + 2);
+            if (l + 3 < a.nl) level(s3, l + 3);
+        }
+        return;
+    }
+    if constexpr (DEP == 3) {
         // three register sets, three levels per trip
         RegSet<SMAX, W16> s0, s1, s2;
         reg_load<SMAX, W16>(s0, sp, bp, lane);
@@ -1945,10 +1973,18 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     }
 }
 
-template <int H, int SMAX, bool UPPER, bool W16, bool D3>
-__global__ void __launch_bounds__(kRegMaxWarps * 32, 1) k_tri_reg(RegArgs a)
+// Warps of a sweep with DEP register sets: at most 12 for four sets leave
+// each thread the registers (131) the sets need.
+__host__ __device__ constexpr int reg_max_warps(int dep)
 {
-    tri_reg_body<H, SMAX, UPPER, W16, D3>(a, blockIdx.x);
+    return dep <= 3 ? kRegMaxWarps : 12;
+}
+
+template <int H, int SMAX, bool UPPER, bool W16, int DEP>
+__global__ void __launch_bounds__(reg_max_warps(DEP) * 32, 1)
+    k_tri_reg(RegArgs a)
+{
+    tri_reg_body<H, SMAX, UPPER, W16, DEP>(a, blockIdx.x);
 }
 
 // One thread block per (row block, temporal block) of a block-Jacobi
@@ -1963,7 +1999,7 @@ __global__ void __launch_bounds__(kRegMaxWarps * 32, 1)
     a.pf = pf;
     a.skip = skip;
     a.out = out;
-    tri_reg_body<H, SMAX, UPPER, W16, false>(a, blockIdx.x % q);
+    tri_reg_body<H, SMAX, UPPER, W16, 2>(a, blockIdx.x % q);
 }
 
 // Forward-sweep right-hand sides in lane-slot order, one array per temporal
@@ -2079,15 +2115,15 @@ int build_reg_parts(const DevIlu& F, int Q, int H, IluStage& st, cudaStream_t s)
     return XT_OK;
 }
 
-template <int Q, int H, int SMAX, bool W16, bool D3 = false>
+template <int Q, int H, int SMAX, bool W16, int DEP = 2>
 int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z, cudaStream_t s,
                const int* skip)
 {
     static std::atomic<bool> attr{false};
     if (!attr.load(std::memory_order_acquire)) {
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, W16, D3>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, false, W16, DEP>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
-        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, W16, D3>,
+        XT_CUDA(cudaFuncSetAttribute(k_tri_reg<H, SMAX, true, W16, DEP>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
         attr.store(true, std::memory_order_release);
     }
@@ -2121,8 +2157,8 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
                L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
                skip};
-    k_tri_reg<H, SMAX, false, W16, D3><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
-    k_tri_reg<H, SMAX, true, W16, D3><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
+    k_tri_reg<H, SMAX, false, W16, DEP><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
+    k_tri_reg<H, SMAX, true, W16, DEP><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -2137,11 +2173,16 @@ int launch_reg_width(const IluStage& st, const double* dAinv, const float* v, fl
         set_error("register sweep: triangles with different offset widths");
         return XT_ERR_STATE;
     }
-    // three register sets (16-bit offsets, at most 12 steps per lane;
-    // XTFEM_ILU_DEPTH=2: two)
+    // four register sets (16-bit offsets, at most 12 steps per lane and 12
+    // warps), else three; XTFEM_ILU_DEPTH=2 or 3 caps them
     if constexpr (SMAX <= 12) {
-        if (st.regL->w16 && st.parts <= 1 && env_int("XTFEM_ILU_DEPTH", 3) == 3)
-            return launch_reg<Q, H, SMAX, true, true>(st, dAinv, v, z, s, skip);
+        const int dep = env_int("XTFEM_ILU_DEPTH", 4);
+        const int w = std::max(st.regL->ncw, st.regU->ncw);
+        if (st.regL->w16 && st.parts <= 1) {
+            if (dep >= 4 && w <= reg_max_warps(4))
+                return launch_reg<Q, H, SMAX, true, 4>(st, dAinv, v, z, s, skip);
+            if (dep >= 3) return launch_reg<Q, H, SMAX, true, 3>(st, dAinv, v, z, s, skip);
+        }
     }
     if (st.regL->w16) return launch_reg<Q, H, SMAX, true>(st, dAinv, v, z, s, skip);
     return launch_reg<Q, H, SMAX, false>(st, dAinv, v, z, s, skip);
