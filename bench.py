@@ -164,7 +164,7 @@ def algorithmic_bytes(problem, ilu_nnz, p, q=6, merged=True):
 # read its blob, DRAM serves it once).  kron_spmm_df = the node-block
 # kernel, which reads K as 3 x 3 blocks and M as one scalar per block (its
 # algorithmic bytes are counted for the CSR operands, as for the others).
-NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 26_068_992 + 512 + 26_406_400 + 256,
+NCU_TRAFFIC = {1: 65_922_560 + 519_168, 3: 26_072_064 + 26_405_888,
                4: 99_808_256 + 41_192_960, 7: 57_748_992 + 28_160}
 
 ROOFLINE_NOTES = {
