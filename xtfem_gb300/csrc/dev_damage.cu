@@ -284,16 +284,12 @@ __device__ __noinline__ int slow_step(Slow* s, const double* __restrict__ Nt, in
     return 1;
 }
 
-__global__ void __launch_bounds__(256)
-k_damage(DamageArgs a, const float* __restrict__ ntmax, int run_bound)
+// The slab's update of point gidx (a copy of the last point, storing
+// nothing, when gidx is past it: every thread of the block must reach the
+// barriers of the chunk loop).
+__device__ __forceinline__ void damage_point(const DamageArgs& a, const float* __restrict__ ntmax,
+                                             int run_bound, long long gidx)
 {
-    // Points are dealt to blocks round-robin (thread t of block b takes point
-    // t * gridDim + b): plastic points cluster in space, i.e. in consecutive
-    // point numbers, and their FP64 steps would otherwise pile up in a few
-    // blocks on a few SMs while the rest of the GPU idles.  Threads past the
-    // last point run a copy of it (they must reach the block barriers of the
-    // chunk loop) and store nothing.
-    const long long gidx = (long long)threadIdx.x * gridDim.x + blockIdx.x;
     const bool live = gidx < a.ngp;
     const int gp = live ? (int)gidx : a.ngp - 1;
     Slow s;
@@ -477,6 +473,20 @@ k_damage(DamageArgs a, const float* __restrict__ ntmax, int run_bound)
         atomicAdd(&a.counters[1], (unsigned long long)a.nip - n_exact);
         atomicAdd(&a.counters[2], (unsigned long long)n_exact);
     }
+}
+
+// Points are dealt to blocks round-robin (pass it, thread t of block b
+// takes point (it blockDim + t) gridDim + b): plastic points cluster in
+// space, i.e. in consecutive point numbers, and their FP64 steps would
+// otherwise pile up in a few blocks on a few SMs while the rest of the GPU
+// idles.  One pass per thread is one thread per point; a small grid with
+// several passes keeps the update on a few SMs.
+__global__ void __launch_bounds__(256)
+k_damage(DamageArgs a, const float* __restrict__ ntmax, int run_bound, int passes)
+{
+    for (int it = 0; it < passes; ++it)
+        damage_point(a, ntmax, run_bound,
+                     ((long long)it * blockDim.x + threadIdx.x) * gridDim.x + blockIdx.x);
 }
 
 // max_t |Nt_k(t)| per k over the slab (single block)
@@ -663,7 +673,14 @@ int damage_update(const DamageArgs& a, cudaStream_t s)
     // two dot-pass blocks of six.
     const char* et = std::getenv("XTFEM_DAMAGE_THREADS");
     const int nt = (et && std::atoi(et) == 256) ? 256 : 128;
-    k_damage<<<(a.ngp + nt - 1) / nt, nt, 0, s>>>(a, a.ntmax, run_bound);
+    // XTFEM_DAMAGE_BLOCKS=B: a grid of B blocks, each thread taking several
+    // points in turn (0: one thread per point)
+    const char* eb = std::getenv("XTFEM_DAMAGE_BLOCKS");
+    const long long want = eb ? std::atoll(eb) : 0;
+    const long long full = ((long long)a.ngp + nt - 1) / nt;
+    const int grid = (int)((want > 0 && want < full) ? want : full);
+    const int passes = (int)(((long long)a.ngp + (long long)grid * nt - 1) / ((long long)grid * nt));
+    k_damage<<<grid, nt, 0, s>>>(a, a.ntmax, run_bound, passes);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

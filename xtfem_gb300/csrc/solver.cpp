@@ -549,22 +549,25 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             // as above, double-float values of 8 bytes
             prof_bytes(otok, (two_pass ? 4.0 * i + 6.0 : 2.0 * i + 3.0) * (double)nl * 8.0);
             XT_TRY(df_multi_dot(V, nl, i, col(i1 - 1), nl, S.red, s));
-            XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, s));
+            // two passes: hsave = (h1, h2, ||w||^2); one pass: (-, h, ||w||^2)
+            // with h1 = 0 taken on the host
             if (two_pass) {
+                XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
+                                        cudaMemcpyDeviceToDevice, s));
                 XT_TRY(df_update_and_dot(V, nl, i, S.hsave.p, col(i1 - 1), nl, S.red, s));
-                XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
-                                        cudaMemcpyDeviceToDevice, s));
-            } else {
-                XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.hsave.p, i * sizeof(double),
-                                        cudaMemcpyDeviceToDevice, s));
-                XT_CUDA(cudaMemsetAsync(S.hsave.p, 0, i * sizeof(double), s));
             }
+            XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
             XT_TRY(df_update_and_norm(V, nl, i, S.hsave.p + i, col(i1 - 1), nl, S.red, s));
             XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
             prof_end(otok, s);
-            XT_TRY(fetch(s, hbuf.data(), S.hsave.p, 2 * i + 1));
+            if (two_pass) {
+                XT_TRY(fetch(s, hbuf.data(), S.hsave.p, 2 * i + 1));
+            } else {
+                XT_TRY(fetch(s, hbuf.data() + i, S.hsave.p + i, i + 1));
+                std::fill(hbuf.begin(), hbuf.begin() + i, 0.0);
+            }
             for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
             t = std::sqrt(hbuf[2 * i]);
             if (!std::isfinite(t)) {
