@@ -391,7 +391,8 @@ def run_rod_batch(xt, count, seed):
     """The many-rod workload: `count` rods of n x n x 3n elements, n drawn
     uniformly from 4..10 and the load amplitude from U(50, 150) MPa with
     numpy's default_rng(seed); one slab solve each (flexible GMRES with the
-    batch's tuned restart length, FP32 ILU, true residual <= 1e-8) through
+    batch's tuned restart length, ILU lanes per row and Gram-Schmidt
+    passes, FP32 ILU, true residual <= 1e-8) through
     xt_batch_solve, against the same systems solved one after another.
     Host wall clock with the device synchronised at both ends; the tuning
     call (one batch solve per candidate restart length) is untimed."""
@@ -406,6 +407,7 @@ def run_rod_batch(xt, count, seed):
     batch.solve(rhs, **kw)  # tunes, then solves (untimed)
     kw["im"] = batch.restart
     shares = batch.ilu_shares
+    passes = batch.gs_passes
     xt.lib().xt_sync()
     t0 = time.perf_counter()
     _, stats, _ = batch.solve(rhs, **kw)
@@ -422,7 +424,7 @@ def run_rod_batch(xt, count, seed):
         s.close()
     return {"rods": count, "value": round(count / t_batch, 2), "unit": "rod-slab-solves/s",
             "ms_all": round(t_batch * 1e3, 2), "one_after_another_ms": round(t_seq * 1e3, 2),
-            "restart": kw["im"], "ilu_lanes_per_row": shares,
+            "restart": kw["im"], "ilu_lanes_per_row": shares, "gram_schmidt_passes": passes,
             "iterations_mean": round(float(np.mean([st["its"] for st in stats])), 1),
             "relres_max": float(max(st["relres"] for st in stats)),
             "space_time_dofs": dofs, "n_values": ns.tolist(),

@@ -198,6 +198,10 @@ int xt_system_set_ilu_blocks(xt_system s, const double *alu, const int *jlu,
 /* The row blocks the FP32 register sweep runs as independent solves (1 for
  * the whole factor). */
 int xt_system_ilu_blocks(xt_system s);
+/* Classical Gram-Schmidt passes per Arnoldi step of the flexible GMRES
+ * (precision 2): 2 (the default) or 1, with the switch to two for the rest
+ * of a solve after a loss of orthogonality (as xt_slab_config.gs_passes). */
+int xt_system_set_gs_passes(xt_system s, int passes);
 /* Temporal matrices A (with the slab-start jump) and B, q x q column-major. */
 int xt_system_set_temporal(xt_system s, const double *a, const double *b);
 /* kronspgemv semantics with explicit temporal matrices (host vectors,
@@ -304,6 +308,10 @@ int xt_batch_restart(xt_batch b);
 /* The ILU lanes per row the tuner picked (1 or 2; 0 before the first tuned
  * call).  No counterpart in the reference. */
 int xt_batch_ilu_shares(xt_batch b);
+/* The Gram-Schmidt passes the tuner picked (precision 2: it tries one pass
+ * at the best restart length and lanes per row; 0 before the first tuned
+ * call). */
+int xt_batch_gs_passes(xt_batch b);
 
 #ifdef __cplusplus
 }

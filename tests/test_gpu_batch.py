@@ -94,6 +94,7 @@ def test_batch_restart_tuner(xt, cases):
     sols, stats, _ = batch.solve([c["rhs"] for c in cases], im=0, tol=1e-8, precision=2)
     im = batch.restart
     assert im in (30, 60, 120, 200)
+    assert batch.gs_passes in (1, 2)
     assert all(st["relres"] <= 1e-8 for st in stats)
     again, _, _ = batch.solve([c["rhs"] for c in cases], im=0, tol=1e-8, precision=2)
     assert batch.restart == im

@@ -46,6 +46,8 @@ SIGNATURES = {
     "xt_system_set_ilu": (C.c_int, [_vp, _dp, _ip, _ip, C.c_int]),
     "xt_system_set_ilu_blocks": (C.c_int, [_vp, _dp, _ip, _ip, C.c_int, C.c_int]),
     "xt_system_ilu_blocks": (C.c_int, [_vp]),
+    "xt_system_set_gs_passes": (C.c_int, [_vp, C.c_int]),
+    "xt_batch_gs_passes": (C.c_int, [_vp]),
     "xt_system_set_temporal": (C.c_int, [_vp, _dp, _dp]),
     "xt_system_apply": (C.c_int, [_vp, _dp, _dp, C.c_double, C.c_double, _dp, _dp]),
     "xt_system_lusol": (C.c_int, [_vp, _dp, _dp, _dp]),

@@ -326,6 +326,10 @@ class SpaceTimeSystem:
         """Row blocks the FP32 register sweep runs as independent solves."""
         return lib().xt_system_ilu_blocks(self._h)
 
+    def set_gs_passes(self, passes):
+        """Gram-Schmidt passes per step of the flexible GMRES (1 or 2)."""
+        check(lib().xt_system_set_gs_passes(self._h, int(passes)), "set_gs_passes")
+
     def set_temporal(self, a, b):
         check(lib().xt_system_set_temporal(self._h, dptr(_colmajor(a)), dptr(_colmajor(b))),
               "set_temporal")
@@ -412,6 +416,11 @@ class SystemBatch:
     def ilu_shares(self) -> int:
         """The ILU lanes per row picked by the tuner (0 before a solve with im=0)."""
         return lib().xt_batch_ilu_shares(self._h)
+
+    @property
+    def gs_passes(self) -> int:
+        """Gram-Schmidt passes the tuner picked (0 before a solve with im=0)."""
+        return lib().xt_batch_gs_passes(self._h)
 
     def solve(self, rhs, sols=None, im=30, tol=1e-8, maxits=2000, precision=0, inner_tol=1e-5):
         """rhs: list of host vectors; returns (solutions, stats list, status

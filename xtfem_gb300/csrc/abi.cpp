@@ -221,6 +221,16 @@ int xt_system_set_ilu_blocks(xt_system s, const double* alu, const int* jlu, con
     return system_set_ilu(s->sys, alu, jlu, ju, group, blocks);
 }
 
+int xt_system_set_gs_passes(xt_system s, int passes)
+{
+    if (!s || (passes != 1 && passes != 2)) {
+        set_error("xt_system_set_gs_passes: passes is 1 or 2");
+        return XT_ERR_ARG;
+    }
+    s->sys.gs_passes = passes;
+    return XT_OK;
+}
+
 int xt_system_ilu_blocks(xt_system s)
 {
     return (s && s->sys.ilu) ? std::max(1, s->sys.ilu->blocks) : 0;
@@ -419,6 +429,7 @@ struct xt_batch_s {
     int workers = 1;
     int tuned_im = 0;        // restart length picked by the tuner, 0 before
     int tuned_shares = 0;    // ILU lanes per row picked by the tuner
+    int tuned_passes = 0;    // Gram-Schmidt passes picked by the tuner
 };
 
 int xt_batch_create(int count, const xt_system* systems, int workers, xt_batch* out)
@@ -468,6 +479,11 @@ void set_shares(xt_batch b, int shares)
         if (h->sys.ilu) h->sys.ilu->shares = shares;
 }
 
+void set_passes(xt_batch b, int passes)
+{
+    for (xt_system h : b->sys) h->sys.gs_passes = passes;
+}
+
 int batch_tune(xt_batch b, const double* const* rhs, double* const* sol, double tol, int maxits,
                int precision, double inner_tol)
 {
@@ -500,16 +516,31 @@ int batch_tune(xt_batch b, const double* const* rhs, double* const* sol, double 
             }
         }
     }
+    // one Gram-Schmidt pass at the best pair (mode 2 only; two are the default)
+    int best_passes = 2;
+    if (precision == 2) {
+        set_shares(b, best_sh);
+        set_passes(b, 1);
+        for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
+        const auto t0 = std::chrono::steady_clock::now();
+        XT_TRY(batch_run(b, rhs, sol, best_im, tol, maxits, precision, inner_tol, nullptr, nullptr));
+        const double t = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (t < best) best_passes = 1;
+        set_passes(b, 2);
+    }
     for (int i = 0; i < count; ++i) std::copy(x0[i].begin(), x0[i].end(), sol[i]);
     b->tuned_im = best_im;
     b->tuned_shares = best_sh;
+    b->tuned_passes = best_passes;
     set_shares(b, best_sh);
+    set_passes(b, best_passes);
     return XT_OK;
 }
 }  // namespace
 
 int xt_batch_restart(xt_batch b) { return b ? b->tuned_im : 0; }
 int xt_batch_ilu_shares(xt_batch b) { return b ? b->tuned_shares : 0; }
+int xt_batch_gs_passes(xt_batch b) { return b ? b->tuned_passes : 0; }
 
 int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
                    int maxits, int precision, double inner_tol, double* stats, int* status)
@@ -522,6 +553,7 @@ int xt_batch_solve(xt_batch b, const double* const* rhs, double* const* sol, int
         if (b->tuned_im == 0) XT_TRY(batch_tune(b, rhs, sol, tol, maxits, precision, inner_tol));
         im = b->tuned_im;
         set_shares(b, b->tuned_shares);
+        set_passes(b, b->tuned_passes);
     }
     return batch_run(b, rhs, sol, im, tol, maxits, precision, inner_tol, stats, status);
 }
