@@ -105,24 +105,27 @@ def test_batch_restart_tuner(xt, cases):
 
 
 def test_batch_lockstep_graph_direct_and_pool_agree(xt, cases, monkeypatch):
-    """The lockstep batch with its rounds replayed from one captured graph,
-    the same rounds issued directly (XTFEM_BATCH_GRAPH=0) and the thread
-    pool of separate solves (XTFEM_BATCH_LOCKSTEP=0) give the same solutions
-    and statistics bit for bit, with one and with two Gram-Schmidt passes."""
+    """The lockstep batch with its rounds replayed from one captured graph
+    of batched kernels (every rod's step in one launch per kernel), the same
+    graph with one branch of step kernels per rod (XTFEM_BATCH_FUSED=0), the
+    rounds issued directly (XTFEM_BATCH_GRAPH=0) and the thread pool of
+    separate solves (XTFEM_BATCH_LOCKSTEP=0) give the same solutions and
+    statistics bit for bit, with one and with two Gram-Schmidt passes."""
     rhs = [c["rhs"] for c in cases]
     for passes in ("2", "1"):
         monkeypatch.setenv("XTFEM_CGS_PASSES", passes)
         out = {}
-        for mode, env in (("graph", {}), ("direct", {"XTFEM_BATCH_GRAPH": "0"}),
+        for mode, env in (("graph", {}), ("branches", {"XTFEM_BATCH_FUSED": "0"}),
+                          ("direct", {"XTFEM_BATCH_GRAPH": "0"}),
                           ("pool", {"XTFEM_BATCH_LOCKSTEP": "0"})):
-            for k in ("XTFEM_BATCH_GRAPH", "XTFEM_BATCH_LOCKSTEP"):
+            for k in ("XTFEM_BATCH_GRAPH", "XTFEM_BATCH_LOCKSTEP", "XTFEM_BATCH_FUSED"):
                 monkeypatch.delenv(k, raising=False)
             for k, v in env.items():
                 monkeypatch.setenv(k, v)
             batch = xt.SystemBatch([c["sys"] for c in cases], workers=4)
             out[mode] = batch.solve(rhs, im=30, tol=1e-8, precision=2)
             batch.close()
-        for mode in ("direct", "pool"):
+        for mode in ("branches", "direct", "pool"):
             sols, stats, status = out[mode]
             assert (status == 0).all()
             for a, b in zip(out["graph"][0], sols):

@@ -604,6 +604,122 @@ bool batch_graph_on()
     return !e || std::atoi(e) != 0;
 }
 
+// The round graph's step of the systems whose operator has the node-block
+// form (XTFEM_BATCH_FUSED=0: none): batched kernels that serve all of them
+// in one launch each (flexb_*, kron_nb_batch), driven by a device table of
+// their buffers, with each system's two ILU sweeps as its own branch; the
+// step is about 20 graph nodes however many systems there are, instead of
+// 15 per system.  One gathered copy brings their control words back.
+bool batch_fused_on()
+{
+    const char* e = std::getenv("XTFEM_BATCH_FUSED");
+    return !e || std::atoi(e) != 0;
+}
+
+struct FusedStep {
+    DBuf<unsigned char> table;  // entries of all, then of two, then of one
+    DBuf<int> dctl;             // gathered control words, four per entry of all
+    int* hgat = nullptr;        // their pinned host copy
+    std::vector<int> sys;       // batch index of each entry of all
+    int nall = 0, ntwo = 0, none = 0, q = 0;
+    FlexStepDims dims;
+    ~FusedStep()
+    {
+        if (hgat) cudaFreeHost(hgat);
+    }
+};
+
+FlexStepItem fused_item(System& S, int im)
+{
+    const long long n = (long long)S.p * S.q, nl = n + (n & 1);
+    FlexStepItem e{};
+    e.ctl = S.fctl.p;
+    e.st = S.fst.p;
+    e.partial = S.red.partial.p;
+    e.V = reinterpret_cast<float2*>(S.V64.p);
+    e.d32 = S.d32.p;
+    e.zfix = S.zfix.p;
+    e.Z = S.Z32.p;
+    e.wfix = S.wfix.p;
+    e.n = n;
+    e.nl = nl;
+    e.im = im;
+    e.rowblocks = df_row_blocks_for(nl, S.red);
+    e.nodes = S.K.nb.nodes;
+    e.bptr = S.K.nb.ptr.p;
+    e.bcol = S.K.nb.col.p;
+    e.kv = S.K.nb.kdf.p;
+    e.mv = S.K.nb.mdf.p;
+    e.A = S.A.p;
+    e.B = S.B.p;
+    return e;
+}
+
+// The table of the live systems in `idx` (each with its run's Gram-Schmidt
+// passes), uploaded before the capture: nothing is allocated inside it.
+int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
+                const std::vector<FlexRun>& run, int im, int count)
+{
+    std::vector<FlexStepItem> all, two, one;
+    f.sys = idx;
+    f.dims = FlexStepDims{};
+    f.dims.im = im;
+    for (int i : idx) {
+        System& S = b->sys[i]->sys;
+        const FlexStepItem e = fused_item(S, im);
+        if (!e.ctl || !e.st || !e.partial || !e.V || !e.d32 || !e.zfix || !e.Z || !e.wfix) {
+            set_error("xt_batch_solve: a system's step buffers are missing");
+            return XT_ERR_STATE;
+        }
+        all.push_back(e);
+        (run[i].two_pass ? two : one).push_back(e);
+        f.dims.nmax = std::max(f.dims.nmax, e.n);
+        f.dims.nodes_max = std::max(f.dims.nodes_max, e.nodes);
+        f.dims.rb_max = std::max(f.dims.rb_max, e.rowblocks);
+    }
+    f.nall = (int)all.size();
+    f.ntwo = (int)two.size();
+    f.none = (int)one.size();
+    std::vector<FlexStepItem> tab(all);
+    tab.insert(tab.end(), two.begin(), two.end());
+    tab.insert(tab.end(), one.begin(), one.end());
+    XT_TRY(f.table.alloc(tab.size() * sizeof(FlexStepItem)));
+    XT_CUDA(cudaMemcpy(f.table.p, tab.data(), tab.size() * sizeof(FlexStepItem),
+                       cudaMemcpyHostToDevice));
+    XT_TRY(f.dctl.alloc((size_t)4 * count));
+    if (!f.hgat)
+        XT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&f.hgat), sizeof(int) * 4 * (size_t)count,
+                              cudaHostAllocDefault));
+    return XT_OK;
+}
+
+// The fused step into the capture on `master`, after the fork event.
+bool fused_capture(FusedStep& f, xt_batch b, cudaStream_t master, cudaEvent_t after_hi,
+                   std::vector<cudaEvent_t>& ev)
+{
+    const FlexStepItem* all = reinterpret_cast<const FlexStepItem*>(f.table.p);
+    const FlexStepItem* two = all + f.nall;
+    const FlexStepItem* one = two + f.ntwo;
+    bool ok = flexb_hi(all, f.nall, f.dims, master) == XT_OK &&
+              cudaEventRecord(after_hi, master) == cudaSuccess;
+    for (int k = 0; ok && k < f.nall; ++k) {
+        const int i = f.sys[k];
+        System& S = b->sys[i]->sys;
+        ok = cudaStreamWaitEvent(S.stream, after_hi, 0) == cudaSuccess &&
+             ilu_apply<float>(*S.ilu, S.q, S.Ainv.p, S.d32.p, S.zfix.p, S.w32.p, S.stream,
+                              S.fctl.p + 1) == XT_OK &&
+             cudaEventRecord(ev[i], S.stream) == cudaSuccess &&
+             cudaStreamWaitEvent(master, ev[i], 0) == cudaSuccess;
+    }
+    return ok && flexb_zcopy(all, f.nall, f.dims, master) == XT_OK &&
+           kron_nb_batch(all, f.nall, f.q, f.dims, master) == XT_OK &&
+           flexb_orth(all, f.nall, two, f.ntwo, one, f.none, f.dims, master) == XT_OK &&
+           flexb_givens_scale(all, f.nall, f.dims, master) == XT_OK &&
+           flexb_ctl_gather(all, f.nall, f.dctl.p, master) == XT_OK &&
+           cudaMemcpyAsync(f.hgat, f.dctl.p, sizeof(int) * 4 * (size_t)f.nall,
+                           cudaMemcpyDeviceToHost, master) == cudaSuccess;
+}
+
 int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
                     int maxits, double* stats, int* status)
 {
@@ -669,6 +785,7 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
     t_start = since(tp);
     auto live = [&](int i) { return code[i] == XT_OK && !run[i].done; };
     GraphParts gp;
+    FusedStep fs;
     std::vector<char> in_graph(count, 0), cap_two(count, 0);
     long long graph_kernels = 0;
     bool tried = false;
@@ -695,16 +812,45 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
             tried = true;
             if (!gp.master) {
                 XT_CUDA(cudaStreamCreateWithFlags(&gp.master, cudaStreamNonBlocking));
-                gp.ev.assign(count + 1, nullptr);
+                gp.ev.assign(count + 2, nullptr);
                 for (auto& e : gp.ev) XT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
             }
+            // the live systems of the fused step: node-block operator, the
+            // first such system's q
+            std::vector<int> fused;
+            fs.q = 0;
+            for (int i = 0; batch_fused_on() && i < count; ++i) {
+                if (!live(i)) continue;
+                System& S = b->sys[i]->sys;
+                if (!S.ilu || !kron_nb_batchable(S.K, S.q) || (fs.q && S.q != fs.q) ||
+                    fused.size() >= 65535)  // the table entry is blockIdx.y
+                    continue;
+                fs.q = S.q;
+                fused.push_back(i);
+            }
+            if (!fused.empty() && fused_build(fs, b, fused, run, im, count) != XT_OK) {
+                fused.clear();  // their own branches instead
+                fs.sys.clear();
+                fs.nall = 0;
+                cudaGetLastError();
+            }
+            std::vector<char> is_fused(count, 0);
+            for (int i : fused) is_fused[i] = 1;
             const long long before = xt_launch_count();
             cudaGraph_t g = nullptr;
             bool ok = cudaStreamBeginCapture(gp.master, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
             if (ok) {
                 ok = cudaEventRecord(gp.ev[count], gp.master) == cudaSuccess;
+                if (ok && !fused.empty()) {
+                    ok = fused_capture(fs, b, gp.master, gp.ev[count + 1], gp.ev);
+                    for (int i : fused) {
+                        in_graph[i] = 1;
+                        cap_two[i] = run[i].two_pass;
+                    }
+                }
+                // every other live system: its own step kernels, one branch
                 for (int i = 0; ok && i < count; ++i) {
-                    if (!live(i)) continue;
+                    if (!live(i) || is_fused[i]) continue;
                     System& S = b->sys[i]->sys;
                     ok = cudaStreamWaitEvent(S.stream, gp.ev[count], 0) == cudaSuccess &&
                          run[i].issue(1, nullptr) == XT_OK &&
@@ -726,6 +872,8 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
                 gp.exec = nullptr;
                 cudaGetLastError();
                 std::fill(in_graph.begin(), in_graph.end(), 0);
+                fs.sys.clear();
+                fs.nall = 0;
             }
             note_launches((int)-graph_kernels);  // captured, not run: counted per replay
             t_capture += since(tp);
@@ -735,6 +883,8 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
             for (int k = 0; k < kRound; ++k) XT_CUDA(cudaGraphLaunch(gp.exec, gp.master));
             XT_CUDA(cudaStreamSynchronize(gp.master));
             note_launches((int)(graph_kernels * kRound));
+            for (int k = 0; k < fs.nall; ++k)
+                std::memcpy(hctl.p + 4 * fs.sys[k], fs.hgat + 4 * k, 4 * sizeof(int));
             for (int i = 0; i < count; ++i)
                 if (live(i) && !in_graph[i]) {
                     set_error("xt_batch_solve: a running system is missing from the round graph");
@@ -780,10 +930,10 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
     if (tracing)
         std::fprintf(stderr,
                      "[xtfem] batch lockstep: %d systems, %d rounds of %d steps, graph %s "
-                     "(%lld kernels); ms: start %.1f, capture %.1f, steps %.1f, host between "
-                     "rounds %.1f, download %.1f\n",
-                     count, rounds, kRound, gp.exec ? "yes" : "no", graph_kernels, t_start,
-                     t_capture, t_steps, t_host, t_down);
+                     "(%lld kernels, %d systems in batched kernels); ms: start %.1f, capture "
+                     "%.1f, steps %.1f, host between rounds %.1f, download %.1f\n",
+                     count, rounds, kRound, gp.exec ? "yes" : "no", graph_kernels, fs.nall,
+                     t_start, t_capture, t_steps, t_host, t_down);
     if (lost_device) {
         set_error("xt_batch_solve: worker thread could not select the device");
         return XT_ERR_CUDA;

@@ -297,15 +297,19 @@ k_kron_df(int p, const int* __restrict__ kptr, const int* __restrict__ kcol,
 // The Q/2 lanes of (a, c) then exchange their sums and each finishes its
 // two outputs with the q x q temporal mixing.  3 Q/2 lanes per node row,
 // 32 / (3 Q/2) node rows per warp.
+// This thread block is block bx of a gx-block pass (a batched launch runs
+// one such pass per system).
 template <int Q>
-__global__ void __launch_bounds__(256)
-k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
-          const float2* __restrict__ kv, const float2* __restrict__ mv,
-          const double* __restrict__ dA, const double* __restrict__ dB,
-          const float* __restrict__ x, float2* __restrict__ y, const int* __restrict__ skip)
+__device__ __forceinline__ void kron_nb_body(int nodes, const int* __restrict__ bptr,
+                                             const int* __restrict__ bcol,
+                                             const float2* __restrict__ kv,
+                                             const float2* __restrict__ mv,
+                                             const double* __restrict__ dA,
+                                             const double* __restrict__ dB,
+                                             const float* __restrict__ x, float2* __restrict__ y,
+                                             int bx, int gx)
 {
     static_assert(Q % 2 == 0 && Q <= 8, "pairs of temporal blocks");
-    if (skip && skip[0] != 0) return;
     constexpr int NP = Q / 2, LPR = 3 * NP, RPW = 32 / LPR;
     __shared__ float2 sA[Q * Q], sB[Q * Q];
     for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) {
@@ -317,8 +321,8 @@ k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
     const int lane = threadIdx.x & 31, slot = lane / LPR, inl = lane - slot * LPR;
     const int c = inl / NP, qp = inl - c * NP;
     const bool lane_ok = slot < RPW;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    const int nwarp = (gridDim.x * blockDim.x) / 32;
+    const int gwarp = (bx * blockDim.x + threadIdx.x) / 32;
+    const int nwarp = (gx * blockDim.x) / 32;
     for (int a0 = gwarp * RPW; a0 < nodes; a0 += nwarp * RPW) {
         const int a = a0 + slot;
         const bool act = lane_ok && a < nodes;
@@ -373,6 +377,28 @@ k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
                 make_float4(out[0].x, out[0].y, out[1].x, out[1].y);
         }
     }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(256)
+k_kron_nb(int nodes, const int* __restrict__ bptr, const int* __restrict__ bcol,
+          const float2* __restrict__ kv, const float2* __restrict__ mv,
+          const double* __restrict__ dA, const double* __restrict__ dB,
+          const float* __restrict__ x, float2* __restrict__ y, const int* __restrict__ skip)
+{
+    if (skip && skip[0] != 0) return;
+    kron_nb_body<Q>(nodes, bptr, bcol, kv, mv, dA, dB, x, y, blockIdx.x, gridDim.x);
+}
+
+// The node-block operator of table entry blockIdx.y: wfix = op(zfix), nothing
+// once the entry's cycle has ended.
+template <int Q>
+__global__ void __launch_bounds__(256) kb_kron_nb(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    if (e.ctl[1] != 0) return;
+    kron_nb_body<Q>(e.nodes, e.bptr, e.bcol, e.kv, e.mv, e.A, e.B, e.zfix, e.wfix, blockIdx.x,
+                    gridDim.x);
 }
 
 template <int Q>
@@ -652,6 +678,32 @@ int kron_spmm(const DevCsr& K, const DevCsr& M, int q, const double* dA,
     case 7: return launch_q<T, 7>(K, M, dA, dB, alpha, beta, x, y, s);
     default: return launch_q<T, 8>(K, M, dA, dB, alpha, beta, x, y, s);
     }
+}
+
+bool kron_nb_batchable(const DevCsr& K, int q)
+{
+    return K.nb.ok && q % 2 == 0 && q >= 2 && q <= 8 && nb_enabled();
+}
+
+int kron_nb_batch(const FlexStepItem* t, int count, int q, const FlexStepDims& d, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    // a quarter of the largest system's node rows per block pass: each warp
+    // loops over about four row groups (any split gives the same rows)
+    const int RPW = q == 2 ? 10 : (q == 4 ? 5 : (q == 6 ? 3 : 2));
+    const int rows_per_block = 8 * RPW;
+    const int gx = std::max(1, (d.nodes_max + 4 * rows_per_block - 1) / (4 * rows_per_block));
+    const dim3 grid(gx, count);
+    switch (q) {
+    case 2: kb_kron_nb<2><<<grid, 256, 0, s>>>(t); break;
+    case 4: kb_kron_nb<4><<<grid, 256, 0, s>>>(t); break;
+    case 6: kb_kron_nb<6><<<grid, 256, 0, s>>>(t); break;
+    case 8: kb_kron_nb<8><<<grid, 256, 0, s>>>(t); break;
+    default: set_error("kron_nb_batch: q must be 2, 4, 6 or 8"); return XT_ERR_ARG;
+    }
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
 }
 
 int kron_spmm_df(DevCsr& K, DevCsr& M, int q, const double* dA, const double* dB, const float* x,

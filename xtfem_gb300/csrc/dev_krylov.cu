@@ -125,7 +125,30 @@ __host__ __device__ __forceinline__ int df_dot_blocks(int k, int nblocks)
 {
     const int nchunk = (k + kChunk - 1) / kChunk;
     const int b = (6 * 148) / nchunk;
-    return b < nblocks ? (b > 24 ? b : 24) : (nblocks > 24 ? nblocks : 24);
+    const int lo = nblocks < 24 ? nblocks : 24;
+    return b < lo ? lo : (b < nblocks ? b : nblocks);
+}
+
+// Row blocks of the double-float dot and norm passes of a vector of n2
+// entry pairs: one 512-row slice per block up to kRowBlocks (a system of
+// fewer than kRowBlocks * 512 pairs gets no empty blocks, so a batch of
+// small systems is not a batch of mostly idle grids).  The norm pass's
+// partial sums are those of the kRowBlocks grid bit for bit: the blocks
+// dropped held no rows, and their zero partials added nothing.
+__host__ __device__ __forceinline__ int df_row_blocks(long long n2, int nblocks)
+{
+    const long long b = (n2 + 511) / 512;
+    return b < 1 ? 1 : (b < nblocks ? (int)b : nblocks);
+}
+
+// Blocks of a device-driven dot pass: the most any k <= im asks for with
+// nb row blocks (blocks past the step's own count return at once).
+inline int df_dot_grid(int im, int nb)
+{
+    int grid = 1;
+    for (int k = 1; k <= im; ++k)
+        grid = std::max(grid, df_dot_blocks(k, nb) * ((k + kChunk - 1) / kChunk));
+    return grid;
 }
 
 // partial[(j0+c) nb + b] = (hi, lo) of sum over row block rb's rows of V_j w
@@ -208,26 +231,24 @@ __device__ __forceinline__ void df_sub_mul(float& wh, float& wl, float hh, float
 }
 
 // w -= V h on double-float vectors (two entries per float4); optional
-// ||w||^2 as a (hi, lo) partial per block.
+// ||w||^2 as a (hi, lo) partial per block.  This thread block is block bx
+// of a gx-block pass (a batched launch runs one such pass per system).
 template <bool NORM>
-__global__ void k_update_df(const float4* __restrict__ V, size_t ld2, int k,
-                            const double* __restrict__ h, float4* __restrict__ w, size_t n2,
-                            double* __restrict__ partial, const int* __restrict__ ctl)
+__device__ __forceinline__ void update_df_body(const float4* __restrict__ V, size_t ld2, int k,
+                                               const double* __restrict__ h,
+                                               float4* __restrict__ w, size_t n2,
+                                               double* __restrict__ partial, int bx, int gx)
 {
     __shared__ float2 hs[512];
     __shared__ float2 sh[32];
-    if (ctl) {  // device-driven step: k = ctl[0] + 1, nothing once ctl[1] is set
-        if (ctl[1] != 0) return;
-        k = ctl[0] + 1;
-    }
     for (int j = threadIdx.x; j < k && j < 512; j += blockDim.x) {
         const float a = (float)h[j];
         hs[j] = make_float2(a, (float)(h[j] - (double)a));
     }
     __syncthreads();
     float nh = 0.0f, nl = 0.0f;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t r = (size_t)blockIdx.x * blockDim.x + threadIdx.x; r < n2; r += stride) {
+    const size_t stride = (size_t)gx * blockDim.x;
+    for (size_t r = (size_t)bx * blockDim.x + threadIdx.x; r < n2; r += stride) {
         const float4 wv = w[r];
         float ah = wv.x, al = wv.y, bh = wv.z, bl = wv.w;
         for (int jb = 0; jb < k; jb += 8) {
@@ -269,9 +290,21 @@ __global__ void k_update_df(const float4* __restrict__ V, size_t ld2, int k,
         if (threadIdx.x == 0) {
             float hh = 0.0f, ll = 0.0f;
             for (int wi = 0; wi < nw; ++wi) df_add_df(hh, ll, sh[wi].x, sh[wi].y);
-            reinterpret_cast<float2*>(partial)[blockIdx.x] = make_float2(hh, ll);
+            reinterpret_cast<float2*>(partial)[bx] = make_float2(hh, ll);
         }
     }
+}
+
+template <bool NORM>
+__global__ void k_update_df(const float4* __restrict__ V, size_t ld2, int k,
+                            const double* __restrict__ h, float4* __restrict__ w, size_t n2,
+                            double* __restrict__ partial, const int* __restrict__ ctl)
+{
+    if (ctl) {  // device-driven step: k = ctl[0] + 1, nothing once ctl[1] is set
+        if (ctl[1] != 0) return;
+        k = ctl[0] + 1;
+    }
+    update_df_body<NORM>(V, ld2, k, h, w, n2, partial, blockIdx.x, gridDim.x);
 }
 
 // y = (hi, lo) split of x; y = hi part only; y = a * y (a FP64, split)
@@ -322,13 +355,13 @@ __global__ void k_finish_df(const double* __restrict__ partial, int nb, double* 
 // k_finish_df for a device-driven step: dot mode (norm == 0) sums the
 // k = ctl[0] + 1 dots of the last k_multi_dot_df_ctl pass (block j < k),
 // norm mode sums the nblocks partials of k_update_df<true> (block 0).
-__global__ void k_finish_df_ctl(const double* __restrict__ partial, int nblocks,
-                                double* __restrict__ out, const int* __restrict__ ctl, int norm)
+__device__ __forceinline__ void finish_df_ctl_body(const double* __restrict__ partial, int nblocks,
+                                                   double* __restrict__ out,
+                                                   const int* __restrict__ ctl, int norm, int j)
 {
     __shared__ double sh[32];
     if (ctl[1] != 0) return;
     const int k = ctl[0] + 1;
-    const int j = blockIdx.x;
     if (norm ? j > 0 : j >= k) return;
     const int nb = norm ? nblocks : df_dot_blocks(k, nblocks);
     const float2* p = reinterpret_cast<const float2*>(partial) + (size_t)j * nb;
@@ -336,6 +369,12 @@ __global__ void k_finish_df_ctl(const double* __restrict__ partial, int nblocks,
     for (int b = threadIdx.x; b < nb; b += blockDim.x) v += (double)p[b].x + (double)p[b].y;
     const double sum = block_sum(v, sh);
     if (threadIdx.x == 0) out[j] = sum;
+}
+
+__global__ void k_finish_df_ctl(const double* __restrict__ partial, int nblocks,
+                                double* __restrict__ out, const int* __restrict__ ctl, int norm)
+{
+    finish_df_ctl_body(partial, nblocks, out, ctl, norm, blockIdx.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -376,8 +415,8 @@ __global__ void k_flexd_zcopy(const int* __restrict__ ctl, const float* __restri
 // the column back.
 constexpr int kGivensMax = kFlexdMaxIm;
 
-__global__ void __launch_bounds__(128) k_flexd_givens(int* __restrict__ ctl,
-                                                      double* __restrict__ st, int im)
+__device__ __forceinline__ void flexd_givens_body(int* __restrict__ ctl, double* __restrict__ st,
+                                                  int im)
 {
     __shared__ double col[kGivensMax + 1], out[kGivensMax + 1], cs[kGivensMax], sn[kGivensMax];
     __shared__ int bad;
@@ -434,18 +473,26 @@ __global__ void __launch_bounds__(128) k_flexd_givens(int* __restrict__ ctl,
     for (int jj = threadIdx.x; jj <= i; jj += blockDim.x) hh[jj] = out[jj];
 }
 
+__global__ void __launch_bounds__(128) k_flexd_givens(int* __restrict__ ctl,
+                                                      double* __restrict__ st, int im)
+{
+    flexd_givens_body(ctl, st, im);
+}
+
 // V column j (the new one) = w / t, as df_scale: the FP64 factor split into
 // (hi, lo) FP32 values; unscaled when t = 0.
-__global__ void k_flexd_scale_copy(const int* __restrict__ ctl, const double* __restrict__ st,
-                                   size_t tinv_at, const float2* __restrict__ w,
-                                   float2* __restrict__ V, size_t nl, size_t n)
+__device__ __forceinline__ void flexd_scale_copy_body(const int* __restrict__ ctl,
+                                                      const double* __restrict__ st,
+                                                      size_t tinv_at, const float2* __restrict__ w,
+                                                      float2* __restrict__ V, size_t nl, size_t n,
+                                                      int bx, int gx)
 {
     if (ctl[1] != 0) return;
     const double a = st[tinv_at];
     const float ah = (float)a, al = (float)(a - (double)ah);
     float2* col = V + (size_t)ctl[0] * nl;
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const size_t stride = (size_t)gx * blockDim.x;
+    for (size_t i = (size_t)bx * blockDim.x + threadIdx.x; i < n; i += stride) {
         const float2 v = w[i];
         if (a == 0.0) {
             col[i] = v;
@@ -455,6 +502,13 @@ __global__ void k_flexd_scale_copy(const int* __restrict__ ctl, const double* __
             col[i] = df_norm(h, l);
         }
     }
+}
+
+__global__ void k_flexd_scale_copy(const int* __restrict__ ctl, const double* __restrict__ st,
+                                   size_t tinv_at, const float2* __restrict__ w,
+                                   float2* __restrict__ V, size_t nl, size_t n)
+{
+    flexd_scale_copy_body(ctl, st, tinv_at, w, V, nl, n, blockIdx.x, gridDim.x);
 }
 
 // One thread: y = H^-1 rs over the cycle's i = ctl[0] steps by back
@@ -859,7 +913,7 @@ int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, R
     // about eight resident blocks per SM over all chunks: row blocks shrink
     // as k grows, so each block's rows outweigh its block reduction
     const int nchunk = (k + kChunk - 1) / kChunk;
-    const int nb = df_dot_blocks(k, r.nblocks);
+    const int nb = df_dot_blocks(k, df_row_blocks((long long)n / 2, r.nblocks));
     dim3 grid(nb, nchunk);
     k_multi_dot_df<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                              reinterpret_cast<const float4*>(w), n / 2,
@@ -887,7 +941,7 @@ int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float
                        Reduce& r, cudaStream_t s)
 {
     if (n % 2 || ld % 2) { set_error("df_update: n and ld must be even"); return XT_ERR_ARG; }
-    const int nb = r.nblocks;
+    const int nb = df_row_blocks((long long)n / 2, r.nblocks);
     k_update_df<true><<<nb, 2 * kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                                   h, reinterpret_cast<float4*>(w), n / 2,
                                                   r.partial.p, nullptr);
@@ -952,16 +1006,14 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
     if (im > r.kmax) { set_error("flexd_orth: restart length exceeds reduction capacity"); return XT_ERR_ARG; }
     if (nl % 2) { set_error("flexd_orth: the basis stride must be even"); return XT_ERR_ARG; }
     const FlexLayout Lo(im);
-    // the most blocks any k <= im asks for (blocks past it return at once)
-    int grid = 1;
-    for (int k = 1; k <= im; ++k)
-        grid = std::max(grid, df_dot_blocks(k, r.nblocks) * ((k + kChunk - 1) / kChunk));
     const float4* V4 = reinterpret_cast<const float4*>(V);
     float4* w4 = reinterpret_cast<float4*>(w);
     const size_t n2 = nl / 2;
+    const int rb = df_row_blocks((long long)n2, r.nblocks);
+    const int grid = df_dot_grid(im, rb);
     if (two_pass) {
-        k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
-        k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h1, ctl, 0);
+        k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rb, ctl);
+        k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.h1, ctl, 0);
         k_update_df<false><<<grid_for(n2), kThreads, 0, s>>>(V4, n2, 0, st + Lo.h1, w4, n2, nullptr, ctl);
         note_launches(3);
     } else {
@@ -969,11 +1021,10 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
         // loop's Hessenberg column 0 + h
         XT_CUDA(cudaMemsetAsync(st + Lo.h1, 0, (size_t)im * sizeof(double), s));
     }
-    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, r.nblocks, ctl);
-    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.h2, ctl, 0);
-    k_update_df<true><<<r.nblocks, 2 * kThreads, 0, s>>>(V4, n2, 0, st + Lo.h2, w4, n2,
-                                                         r.partial.p, ctl);
-    k_finish_df_ctl<<<1, kThreads, 0, s>>>(r.partial.p, r.nblocks, st + Lo.nrm, ctl, 1);
+    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rb, ctl);
+    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.h2, ctl, 0);
+    k_update_df<true><<<rb, 2 * kThreads, 0, s>>>(V4, n2, 0, st + Lo.h2, w4, n2, r.partial.p, ctl);
+    k_finish_df_ctl<<<1, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.nrm, ctl, 1);
     note_launches(4);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -1000,6 +1051,190 @@ int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, 
 int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s)
 {
     k_flexd_solve<<<1, 32, 0, s>>>(ctl, st, im);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Batched device-driven steps: blockIdx.y selects the system's table entry,
+// blockIdx.x is the block of that system's pass.  Each body is the
+// per-system kernel's, with the system's own row partition where a
+// reduction depends on it, so a batched step gives each system the bits of
+// its own step.
+
+namespace {
+
+// Blocks in x of an elementwise batched pass: about eight entries per
+// thread of the largest system (smaller systems leave blocks idle).
+int ew_grid(long long nmax)
+{
+    const long long b = (nmax + 8LL * kThreads - 1) / (8LL * kThreads);
+    return (int)std::max(1LL, std::min(b, 4096LL));
+}
+
+__global__ void kb_flex_hi(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const int* ctl = e.ctl;
+    if (ctl[1] != 0) return;
+    const float2* col = e.V + (size_t)ctl[0] * (size_t)e.nl;
+    float* d = e.d32;
+    const size_t n = (size_t)e.n, stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) d[i] = col[i].x;
+}
+
+__global__ void kb_flex_zcopy(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const int* ctl = e.ctl;
+    if (ctl[1] != 0) return;
+    const size_t n = (size_t)e.n, stride = (size_t)gridDim.x * blockDim.x;
+    float* col = e.Z + (size_t)ctl[0] * n;
+    const float* z = e.zfix;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) col[i] = z[i];
+}
+
+// k_multi_dot_df_ctl of entry blockIdx.y
+__global__ void __launch_bounds__(256, 6) kb_dot(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const int* ctl = e.ctl;
+    if (ctl[1] != 0) return;
+    const int k = ctl[0] + 1;
+    const int nb = df_dot_blocks(k, e.rowblocks), nchunk = (k + kChunk - 1) / kChunk;
+    const int chunk = blockIdx.x / nb;
+    if (chunk >= nchunk) return;
+    const size_t n2 = (size_t)e.nl / 2;
+    multi_dot_df_body(reinterpret_cast<const float4*>(e.V), n2,  k,
+                      reinterpret_cast<const float4*>(e.wfix), n2, e.partial,
+                      blockIdx.x - chunk * nb, nb, chunk);
+}
+
+// k_finish_df_ctl of entry blockIdx.y into h1 (which 0), h2 (1) or the norm (2)
+__global__ void kb_finish(const FlexStepItem* __restrict__ t, int which)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const FlexLayout Lo(e.im);
+    double* out = e.st + (which == 0 ? Lo.h1 : (which == 1 ? Lo.h2 : Lo.nrm));
+    finish_df_ctl_body(e.partial, e.rowblocks, out, e.ctl, which == 2 ? 1 : 0, blockIdx.x);
+}
+
+// k_update_df of entry blockIdx.y with h = h1 (NORM false) or h2 and the norm
+// partials over the system's own row blocks (NORM true)
+template <bool NORM>
+__global__ void kb_update(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const int* ctl = e.ctl;
+    if (ctl[1] != 0) return;
+    const int gx = NORM ? e.rowblocks : (int)gridDim.x;
+    if ((int)blockIdx.x >= gx) return;
+    const FlexLayout Lo(e.im);
+    const size_t n2 = (size_t)e.nl / 2;
+    update_df_body<NORM>(reinterpret_cast<const float4*>(e.V), n2, ctl[0] + 1,
+                         e.st + (NORM ? Lo.h2 : Lo.h1), reinterpret_cast<float4*>(e.wfix), n2,
+                         e.partial, blockIdx.x, gx);
+}
+
+// h1 = 0 for a one-pass step (the host-driven loop's Hessenberg column is 0 + h)
+__global__ void kb_zero_h1(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    const FlexLayout Lo(e.im);
+    for (int j = threadIdx.x; j < e.im; j += blockDim.x) e.st[Lo.h1 + j] = 0.0;
+}
+
+__global__ void __launch_bounds__(128) kb_givens(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.x];
+    flexd_givens_body(e.ctl, e.st, e.im);
+}
+
+__global__ void kb_scale_copy(const FlexStepItem* __restrict__ t)
+{
+    const FlexStepItem& e = t[blockIdx.y];
+    flexd_scale_copy_body(e.ctl, e.st, FlexLayout(e.im).tinv, e.wfix, e.V, (size_t)e.nl,
+                          (size_t)e.n, blockIdx.x, gridDim.x);
+}
+
+__global__ void kb_ctl_gather(const FlexStepItem* __restrict__ t, int count, int* __restrict__ out)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * count; i += gridDim.x * blockDim.x)
+        out[i] = t[i / 4].ctl[i % 4];
+}
+
+}  // namespace
+
+int df_row_blocks_for(long long nl, const Reduce& r) { return df_row_blocks(nl / 2, r.nblocks); }
+
+int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    kb_flex_hi<<<dim3(ew_grid(d.nmax), count), kThreads, 0, s>>>(t);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexb_zcopy(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    kb_flex_zcopy<<<dim3(ew_grid(d.nmax), count), kThreads, 0, s>>>(t);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexb_orth(const FlexStepItem* all, int nall, const FlexStepItem* two, int ntwo,
+               const FlexStepItem* one, int none, const FlexStepDims& d, cudaStream_t s)
+{
+    if (nall <= 0) return XT_OK;
+    if (d.im < 1 || d.im > kFlexdMaxIm || d.rb_max < 1 || d.rb_max > kRowBlocks) {
+        set_error("flexb_orth: bad batch dimensions");
+        return XT_ERR_ARG;
+    }
+    const int grid = df_dot_grid(d.im, d.rb_max);
+    const int ew = ew_grid((d.nmax + 1) / 2);
+    int launches = 0;
+    if (ntwo > 0) {
+        kb_dot<<<dim3(grid, ntwo), kThreads, 0, s>>>(two);
+        kb_finish<<<dim3(d.im, ntwo), kThreads, 0, s>>>(two, 0);
+        kb_update<false><<<dim3(ew, ntwo), kThreads, 0, s>>>(two);
+        launches += 3;
+    }
+    if (none > 0) {
+        kb_zero_h1<<<dim3(1, none), kThreads, 0, s>>>(one);
+        ++launches;
+    }
+    kb_dot<<<dim3(grid, nall), kThreads, 0, s>>>(all);
+    kb_finish<<<dim3(d.im, nall), kThreads, 0, s>>>(all, 1);
+    kb_update<true><<<dim3(d.rb_max, nall), 2 * kThreads, 0, s>>>(all);
+    kb_finish<<<dim3(1, nall), kThreads, 0, s>>>(all, 2);
+    note_launches(launches + 4);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexb_givens_scale(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    if (d.im > kGivensMax) {
+        set_error("flexb_givens_scale: restart length exceeds the device rotation buffer");
+        return XT_ERR_ARG;
+    }
+    kb_givens<<<count, 128, 0, s>>>(t);
+    kb_scale_copy<<<dim3(ew_grid(d.nmax), count), kThreads, 0, s>>>(t);
+    note_launches(2);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int flexb_ctl_gather(const FlexStepItem* t, int count, int* out, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    const int th = 256, b = std::max(1, std::min(64, (4 * count + th - 1) / th));
+    kb_ctl_gather<<<b, th, 0, s>>>(t, count, out);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

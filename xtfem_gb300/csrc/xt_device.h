@@ -275,6 +275,54 @@ int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, 
                      size_t nl, size_t n, cudaStream_t s);
 int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s);
 
+// ------------------------------------- batched device-driven Arnoldi steps
+// One system of a batch in a table that drives kernels serving every system
+// of the batch in one launch (blockIdx.y = the system's entry): the buffers
+// the system's FlexRun step uses and its node-block operator.  The kernels
+// do per system what the per-system step kernels do, with the same row
+// partitions, so the results are the same bits.
+struct FlexStepItem {
+    int* ctl;          // {j, status, its, maxits}
+    double* st;        // FlexLayout(im) state of the cycle
+    double* partial;   // reduction scratch
+    float2* V;         // double-float basis, column stride nl
+    float* d32;        // ILU input: hi part of basis column j
+    float* zfix;       // ILU output
+    float* Z;          // preconditioned vectors, column stride n
+    float2* wfix;      // operator output, orthogonalised in place
+    long long n, nl;
+    int im, rowblocks;  // restart length; row blocks of the dot and norm passes
+    int nodes;          // node-block operator: K's 3 x 3 blocks, M's scalars
+    const int* bptr;
+    const int* bcol;
+    const float2* kv;
+    const float2* mv;
+    const double* A;    // temporal matrices (q x q)
+    const double* B;
+};
+// The largest sizes over a table's entries (launch grids are sized by them).
+struct FlexStepDims {
+    long long nmax = 0;
+    int nodes_max = 0, rb_max = 0, im = 0;
+};
+// Row blocks of a system's double-float dot and norm passes.
+int df_row_blocks_for(long long nl, const Reduce& r);
+// Basis column j's hi part into the ILU input; the ILU output into Z column j.
+int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
+int flexb_zcopy(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
+// Gram-Schmidt of every system's operator output: the first pass of the
+// systems in `two` (two passes), h1 = 0 for those in `one`, then the
+// projection and norm pass of all.
+int flexb_orth(const FlexStepItem* all, int nall, const FlexStepItem* two, int ntwo,
+               const FlexStepItem* one, int none, const FlexStepDims& d, cudaStream_t s);
+// The rotations and convergence test, then the scaled new basis column.
+int flexb_givens_scale(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
+// out[4 e .. 4 e + 3] = the control word of entry e.
+int flexb_ctl_gather(const FlexStepItem* t, int count, int* out, cudaStream_t s);
+// The node-block double-float operator of every system: wfix = op(zfix).
+bool kron_nb_batchable(const DevCsr& K, int q);
+int kron_nb_batch(const FlexStepItem* t, int count, int q, const FlexStepDims& d, cudaStream_t s);
+
 
 // h[j] = <V_j, w> for j < k (V column-major, column stride ld), FP64
 // accumulation; result in r.out (device).
