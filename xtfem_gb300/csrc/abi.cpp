@@ -645,6 +645,8 @@ FlexStepItem fused_item(System& S, int im)
     e.nl = nl;
     e.im = im;
     e.rowblocks = df_row_blocks_for(nl, S.red);
+    e.dotrows = df_dot_rows_for(nl, S.red);
+    e.dotblocks = 1;  // set from the batch's sizes
     e.nodes = S.K.nb.nodes;
     e.bptr = S.K.nb.ptr.p;
     e.bcol = S.K.nb.col.p;
@@ -677,6 +679,17 @@ int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
         f.dims.nodes_max = std::max(f.dims.nodes_max, e.nodes);
         f.dims.rb_max = std::max(f.dims.rb_max, e.rowblocks);
     }
+    // the dot pass's wave dealt to the systems by size, each at most the
+    // items its longest pass has
+    double ntot = 0.0;
+    for (const FlexStepItem& e : all) ntot += (double)e.n;
+    for (std::vector<FlexStepItem>* v : {&all, &two, &one})
+        for (FlexStepItem& e : *v) {
+            const int most = df_dot_blocks_max(im, e.dotrows);
+            const int share = (int)std::lround(df_dot_wave() * (double)e.n / ntot);
+            e.dotblocks = std::max(1, std::min(most, share));
+            f.dims.dot_blocks_max = std::max(f.dims.dot_blocks_max, e.dotblocks);
+        }
     f.nall = (int)all.size();
     f.ntwo = (int)two.size();
     f.none = (int)one.size();
@@ -817,9 +830,11 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
             }
             // the live systems of the fused step: node-block operator, the
             // first such system's q
+            // largest first: their ILU branches, the longest chains, start first
             std::vector<int> fused;
             fs.q = 0;
-            for (int i = 0; batch_fused_on() && i < count; ++i) {
+            for (int o = 0; batch_fused_on() && o < count; ++o) {
+                const int i = b->order[o];
                 if (!live(i)) continue;
                 System& S = b->sys[i]->sys;
                 if (!S.ilu || !kron_nb_batchable(S.K, S.q) || (fs.q && S.q != fs.q) ||

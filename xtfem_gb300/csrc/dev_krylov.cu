@@ -141,6 +141,18 @@ __host__ __device__ __forceinline__ int df_row_blocks(long long n2, int nblocks)
     return b < 1 ? 1 : (b < nblocks ? (int)b : nblocks);
 }
 
+// Row blocks of the dot pass: those of the norm pass for a system of at
+// least kRowBlocks 512-row slices; a smaller system's row blocks hold 2048
+// rows or more (the pass per basis chunk would otherwise be a few hundred
+// rows per block, all block reduction and partial sums).
+__host__ __device__ __forceinline__ int df_dot_rows(long long n2, int nblocks)
+{
+    const int b = df_row_blocks(n2, nblocks);
+    if (b >= nblocks) return nblocks;
+    const long long d = (n2 + 2047) / 2048;
+    return d < 1 ? 1 : (int)d;
+}
+
 // Blocks of a device-driven dot pass: the most any k <= im asks for with
 // nb row blocks (blocks past the step's own count return at once).
 inline int df_dot_grid(int im, int nb)
@@ -913,7 +925,7 @@ int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, R
     // about eight resident blocks per SM over all chunks: row blocks shrink
     // as k grows, so each block's rows outweigh its block reduction
     const int nchunk = (k + kChunk - 1) / kChunk;
-    const int nb = df_dot_blocks(k, df_row_blocks((long long)n / 2, r.nblocks));
+    const int nb = df_dot_blocks(k, df_dot_rows((long long)n / 2, r.nblocks));
     dim3 grid(nb, nchunk);
     k_multi_dot_df<<<grid, kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                              reinterpret_cast<const float4*>(w), n / 2,
@@ -1010,10 +1022,11 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
     float4* w4 = reinterpret_cast<float4*>(w);
     const size_t n2 = nl / 2;
     const int rb = df_row_blocks((long long)n2, r.nblocks);
-    const int grid = df_dot_grid(im, rb);
+    const int rd = df_dot_rows((long long)n2, r.nblocks);
+    const int grid = df_dot_grid(im, rd);
     if (two_pass) {
-        k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rb, ctl);
-        k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.h1, ctl, 0);
+        k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rd, ctl);
+        k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rd, st + Lo.h1, ctl, 0);
         k_update_df<false><<<grid_for(n2), kThreads, 0, s>>>(V4, n2, 0, st + Lo.h1, w4, n2, nullptr, ctl);
         note_launches(3);
     } else {
@@ -1021,8 +1034,8 @@ int flexd_orth(const int* ctl, const float2* V, size_t nl, float2* w, double* st
         // loop's Hessenberg column 0 + h
         XT_CUDA(cudaMemsetAsync(st + Lo.h1, 0, (size_t)im * sizeof(double), s));
     }
-    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rb, ctl);
-    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.h2, ctl, 0);
+    k_multi_dot_df_ctl<<<grid, kThreads, 0, s>>>(V4, n2, w4, n2, r.partial.p, rd, ctl);
+    k_finish_df_ctl<<<im, kThreads, 0, s>>>(r.partial.p, rd, st + Lo.h2, ctl, 0);
     k_update_df<true><<<rb, 2 * kThreads, 0, s>>>(V4, n2, 0, st + Lo.h2, w4, n2, r.partial.p, ctl);
     k_finish_df_ctl<<<1, kThreads, 0, s>>>(r.partial.p, rb, st + Lo.nrm, ctl, 1);
     note_launches(4);
@@ -1095,20 +1108,25 @@ __global__ void kb_flex_zcopy(const FlexStepItem* __restrict__ t)
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) col[i] = z[i];
 }
 
-// k_multi_dot_df_ctl of entry blockIdx.y
+// The partial sums of k_multi_dot_df_ctl for entry blockIdx.y: the entry's
+// (row block, chunk) items dealt to its e.dotblocks blocks in turn (a
+// system's share of one wave, by its size), so small and large systems
+// finish together and no block of the grid is there for the largest alone.
 __global__ void __launch_bounds__(256, 6) kb_dot(const FlexStepItem* __restrict__ t)
 {
     const FlexStepItem& e = t[blockIdx.y];
     const int* ctl = e.ctl;
-    if (ctl[1] != 0) return;
+    if (ctl[1] != 0 || (int)blockIdx.x >= e.dotblocks) return;
     const int k = ctl[0] + 1;
-    const int nb = df_dot_blocks(k, e.rowblocks), nchunk = (k + kChunk - 1) / kChunk;
-    const int chunk = blockIdx.x / nb;
-    if (chunk >= nchunk) return;
+    const int nb = df_dot_blocks(k, e.dotrows), nchunk = (k + kChunk - 1) / kChunk;
     const size_t n2 = (size_t)e.nl / 2;
-    multi_dot_df_body(reinterpret_cast<const float4*>(e.V), n2,  k,
-                      reinterpret_cast<const float4*>(e.wfix), n2, e.partial,
-                      blockIdx.x - chunk * nb, nb, chunk);
+    for (int w = blockIdx.x; w < nb * nchunk; w += e.dotblocks) {
+        const int chunk = w / nb;
+        multi_dot_df_body(reinterpret_cast<const float4*>(e.V), n2, k,
+                          reinterpret_cast<const float4*>(e.wfix), n2, e.partial, w - chunk * nb,
+                          nb, chunk);
+        __syncthreads();  // the body's shared sums are read before the next item writes them
+    }
 }
 
 // k_finish_df_ctl of entry blockIdx.y into h1 (which 0), h2 (1) or the norm (2)
@@ -1117,7 +1135,8 @@ __global__ void kb_finish(const FlexStepItem* __restrict__ t, int which)
     const FlexStepItem& e = t[blockIdx.y];
     const FlexLayout Lo(e.im);
     double* out = e.st + (which == 0 ? Lo.h1 : (which == 1 ? Lo.h2 : Lo.nrm));
-    finish_df_ctl_body(e.partial, e.rowblocks, out, e.ctl, which == 2 ? 1 : 0, blockIdx.x);
+    finish_df_ctl_body(e.partial, which == 2 ? e.rowblocks : e.dotrows, out, e.ctl,
+                       which == 2 ? 1 : 0, blockIdx.x);
 }
 
 // k_update_df of entry blockIdx.y with h = h1 (NORM false) or h2 and the norm
@@ -1167,6 +1186,9 @@ __global__ void kb_ctl_gather(const FlexStepItem* __restrict__ t, int count, int
 }  // namespace
 
 int df_row_blocks_for(long long nl, const Reduce& r) { return df_row_blocks(nl / 2, r.nblocks); }
+int df_dot_rows_for(long long nl, const Reduce& r) { return df_dot_rows(nl / 2, r.nblocks); }
+int df_dot_blocks_max(int im, int dotrows) { return df_dot_grid(im, dotrows); }
+int df_dot_wave() { return 6 * 148; }
 
 int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
 {
@@ -1190,11 +1212,12 @@ int flexb_orth(const FlexStepItem* all, int nall, const FlexStepItem* two, int n
                const FlexStepItem* one, int none, const FlexStepDims& d, cudaStream_t s)
 {
     if (nall <= 0) return XT_OK;
-    if (d.im < 1 || d.im > kFlexdMaxIm || d.rb_max < 1 || d.rb_max > kRowBlocks) {
+    if (d.im < 1 || d.im > kFlexdMaxIm || d.rb_max < 1 || d.rb_max > kRowBlocks ||
+        d.dot_blocks_max < 1 || d.dot_blocks_max > 65535) {
         set_error("flexb_orth: bad batch dimensions");
         return XT_ERR_ARG;
     }
-    const int grid = df_dot_grid(d.im, d.rb_max);
+    const int grid = std::max(1, d.dot_blocks_max);
     const int ew = ew_grid((d.nmax + 1) / 2);
     int launches = 0;
     if (ntwo > 0) {

@@ -291,7 +291,10 @@ struct FlexStepItem {
     float* Z;          // preconditioned vectors, column stride n
     float2* wfix;      // operator output, orthogonalised in place
     long long n, nl;
-    int im, rowblocks;  // restart length; row blocks of the dot and norm passes
+    int im;
+    int rowblocks;      // row blocks of the norm pass
+    int dotrows;        // row blocks per basis chunk of the dot pass (at most)
+    int dotblocks;      // thread blocks of the system's dot pass
     int nodes;          // node-block operator: K's 3 x 3 blocks, M's scalars
     const int* bptr;
     const int* bcol;
@@ -303,10 +306,16 @@ struct FlexStepItem {
 // The largest sizes over a table's entries (launch grids are sized by them).
 struct FlexStepDims {
     long long nmax = 0;
-    int nodes_max = 0, rb_max = 0, im = 0;
+    int nodes_max = 0, rb_max = 0, dot_blocks_max = 0, im = 0;
 };
-// Row blocks of a system's double-float dot and norm passes.
+// Row blocks of a system's double-float norm and dot passes; the most
+// blocks a dot pass over im basis vectors has items for.
 int df_row_blocks_for(long long nl, const Reduce& r);
+int df_dot_rows_for(long long nl, const Reduce& r);
+int df_dot_blocks_max(int im, int dotrows);
+// The thread blocks of one wave of a dot pass (a batch deals them to its
+// systems by size).
+int df_dot_wave();
 // Basis column j's hi part into the ILU input; the ILU output into Z column j.
 int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
 int flexb_zcopy(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
