@@ -622,22 +622,36 @@ struct FusedStep {
     int* hgat = nullptr;        // their pinned host copy
     std::vector<int> sys;       // batch index of each entry of all
     int nall = 0, ntwo = 0, none = 0, q = 0;
+    long long lanes_max = 0;
     FlexStepDims dims;
+    // the ILU sweeps: one launch per group of equal kernel shape, forward
+    // groups, then backward groups, each group on a branch of its own
+    std::vector<std::unique_ptr<RegGroup>> gl, gu;
+    std::vector<cudaEvent_t> gev;
     ~FusedStep()
     {
         if (hgat) cudaFreeHost(hgat);
+        for (cudaEvent_t e : gev)
+            if (e) cudaEventDestroy(e);
     }
 };
 
-FlexStepItem fused_item(System& S, int im)
+// A live system's entry of the fused step; false when its ILU apply or its
+// operator has no batched launch (it then runs its own step kernels).
+bool fused_item(System& S, int im, FlexStepItem& e, IluRegEntry& r)
 {
+    if (!S.ilu || !kron_nb_batchable(S.K, S.q)) return false;
+    if (ilu_reg_entry(*S.ilu, S.q, S.zfix.p, S.fctl.p + 1, S.stream, r) != XT_OK) {
+        cudaGetLastError();
+        return false;
+    }
+    if (!r.ok) return false;
     const long long n = (long long)S.p * S.q, nl = n + (n & 1);
-    FlexStepItem e{};
+    e = FlexStepItem{};
     e.ctl = S.fctl.p;
     e.st = S.fst.p;
     e.partial = S.red.partial.p;
     e.V = reinterpret_cast<float2*>(S.V64.p);
-    e.d32 = S.d32.p;
     e.zfix = S.zfix.p;
     e.Z = S.Z32.p;
     e.wfix = S.wfix.p;
@@ -647,6 +661,10 @@ FlexStepItem fused_item(System& S, int im)
     e.rowblocks = df_row_blocks_for(nl, S.red);
     e.dotrows = df_dot_rows_for(nl, S.red);
     e.dotblocks = 1;  // set from the batch's sizes
+    e.src = r.src;
+    e.lanes = r.lanes;
+    e.rrhs = r.rrhs;
+    e.Ainv = S.Ainv.p;
     e.nodes = S.K.nb.nodes;
     e.bptr = S.K.nb.ptr.p;
     e.bcol = S.K.nb.col.p;
@@ -654,42 +672,69 @@ FlexStepItem fused_item(System& S, int im)
     e.mv = S.K.nb.mdf.p;
     e.A = S.A.p;
     e.B = S.B.p;
-    return e;
+    return e.ctl && e.st && e.partial && e.V && e.zfix && e.Z && e.wfix && e.src && e.rrhs &&
+           e.Ainv && e.A && e.B;
+}
+
+// Sweep groups of one direction: entries with equal shares, steps, offset
+// width and warps, their argument tables uploaded.
+int fused_groups(std::vector<std::unique_ptr<RegGroup>>& out, const std::vector<IluRegEntry>& ent,
+                 bool upper)
+{
+    out.clear();
+    std::map<std::tuple<int, int, int, int>, std::vector<RegArgs>> by;
+    std::map<std::tuple<int, int, int, int>, size_t> smem;
+    for (const IluRegEntry& r : ent) {
+        const RegArgs& a = upper ? r.U : r.L;
+        const auto key = std::make_tuple(r.H, r.smax, r.w16, a.ncw);
+        by[key].push_back(a);
+        smem[key] = std::max(smem[key], upper ? r.smemU : r.smemL);
+    }
+    for (auto& kv : by) {
+        auto g = std::make_unique<RegGroup>();
+        g->H = std::get<0>(kv.first);
+        g->smax = std::get<1>(kv.first);
+        g->w16 = std::get<2>(kv.first);
+        g->ncw = std::get<3>(kv.first);
+        g->upper = upper ? 1 : 0;
+        g->count = (int)kv.second.size();
+        g->smem = smem[kv.first];
+        XT_TRY(g->args.alloc(kv.second.size() * sizeof(RegArgs)));
+        XT_CUDA(cudaMemcpy(g->args.p, kv.second.data(), kv.second.size() * sizeof(RegArgs),
+                           cudaMemcpyHostToDevice));
+        XT_TRY(reg_group_prepare(*g));
+        out.push_back(std::move(g));
+    }
+    return XT_OK;
 }
 
 // The table of the live systems in `idx` (each with its run's Gram-Schmidt
-// passes), uploaded before the capture: nothing is allocated inside it.
+// passes) and their sweep groups, uploaded before the capture: nothing is
+// allocated inside it.
 int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
+                const std::vector<FlexStepItem>& items, const std::vector<IluRegEntry>& ilu,
                 const std::vector<FlexRun>& run, int im, int count)
 {
-    std::vector<FlexStepItem> all, two, one;
+    std::vector<FlexStepItem> all(items), two, one;
     f.sys = idx;
     f.dims = FlexStepDims{};
     f.dims.im = im;
-    for (int i : idx) {
-        System& S = b->sys[i]->sys;
-        const FlexStepItem e = fused_item(S, im);
-        if (!e.ctl || !e.st || !e.partial || !e.V || !e.d32 || !e.zfix || !e.Z || !e.wfix) {
-            set_error("xt_batch_solve: a system's step buffers are missing");
-            return XT_ERR_STATE;
-        }
-        all.push_back(e);
-        (run[i].two_pass ? two : one).push_back(e);
+    f.lanes_max = 0;
+    double ntot = 0.0;
+    for (const FlexStepItem& e : all) ntot += (double)e.n;
+    // the dot pass's wave dealt to the systems by size, each at most the
+    // items its longest pass has
+    for (FlexStepItem& e : all) {
+        const int most = df_dot_blocks_max(im, e.dotrows);
+        const int share = (int)std::lround(df_dot_wave() * (double)e.n / ntot);
+        e.dotblocks = std::max(1, std::min(most, share));
+        f.dims.dot_blocks_max = std::max(f.dims.dot_blocks_max, e.dotblocks);
         f.dims.nmax = std::max(f.dims.nmax, e.n);
         f.dims.nodes_max = std::max(f.dims.nodes_max, e.nodes);
         f.dims.rb_max = std::max(f.dims.rb_max, e.rowblocks);
+        f.lanes_max = std::max(f.lanes_max, e.lanes);
     }
-    // the dot pass's wave dealt to the systems by size, each at most the
-    // items its longest pass has
-    double ntot = 0.0;
-    for (const FlexStepItem& e : all) ntot += (double)e.n;
-    for (std::vector<FlexStepItem>* v : {&all, &two, &one})
-        for (FlexStepItem& e : *v) {
-            const int most = df_dot_blocks_max(im, e.dotrows);
-            const int share = (int)std::lround(df_dot_wave() * (double)e.n / ntot);
-            e.dotblocks = std::max(1, std::min(most, share));
-            f.dims.dot_blocks_max = std::max(f.dims.dot_blocks_max, e.dotblocks);
-        }
+    for (size_t k = 0; k < idx.size(); ++k) (run[idx[k]].two_pass ? two : one).push_back(all[k]);
     f.nall = (int)all.size();
     f.ntwo = (int)two.size();
     f.none = (int)one.size();
@@ -703,26 +748,40 @@ int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
     if (!f.hgat)
         XT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&f.hgat), sizeof(int) * 4 * (size_t)count,
                               cudaHostAllocDefault));
+    XT_TRY(fused_groups(f.gl, ilu, false));
+    XT_TRY(fused_groups(f.gu, ilu, true));
+    const size_t nev = 2 + f.gl.size() + f.gu.size();
+    while (f.gev.size() < nev) {
+        cudaEvent_t e = nullptr;
+        XT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        f.gev.push_back(e);
+    }
     return XT_OK;
 }
 
-// The fused step into the capture on `master`, after the fork event.
-bool fused_capture(FusedStep& f, xt_batch b, cudaStream_t master, cudaEvent_t after_hi,
-                   std::vector<cudaEvent_t>& ev)
+// The fused step into the capture on `master`: the ILU pre-pass of all, the
+// forward sweep groups side by side, then the backward ones, then the
+// operator, Gram-Schmidt, rotations and the new basis column of all, and
+// the gathered control words.  Group g runs on the stream of the batch's
+// g-th entry (distinct streams: there are no more groups than entries).
+bool fused_capture(FusedStep& f, xt_batch b, cudaStream_t master)
 {
     const FlexStepItem* all = reinterpret_cast<const FlexStepItem*>(f.table.p);
     const FlexStepItem* two = all + f.nall;
     const FlexStepItem* one = two + f.ntwo;
-    bool ok = flexb_hi(all, f.nall, f.dims, master) == XT_OK &&
-              cudaEventRecord(after_hi, master) == cudaSuccess;
-    for (int k = 0; ok && k < f.nall; ++k) {
-        const int i = f.sys[k];
-        System& S = b->sys[i]->sys;
-        ok = cudaStreamWaitEvent(S.stream, after_hi, 0) == cudaSuccess &&
-             ilu_apply<float>(*S.ilu, S.q, S.Ainv.p, S.d32.p, S.zfix.p, S.w32.p, S.stream,
-                              S.fctl.p + 1) == XT_OK &&
-             cudaEventRecord(ev[i], S.stream) == cudaSuccess &&
-             cudaStreamWaitEvent(master, ev[i], 0) == cudaSuccess;
+    bool ok = flexb_rhs(all, f.nall, f.q, f.lanes_max, master) == XT_OK;
+    size_t ev = 0;
+    for (auto* groups : {&f.gl, &f.gu}) {
+        const cudaEvent_t fork = f.gev[ev++];
+        ok = ok && cudaEventRecord(fork, master) == cudaSuccess;
+        for (size_t g = 0; ok && g < groups->size(); ++g) {
+            cudaStream_t st = b->sys[f.sys[g]]->sys.stream;
+            const cudaEvent_t join = f.gev[ev++];
+            ok = cudaStreamWaitEvent(st, fork, 0) == cudaSuccess &&
+                 reg_group_launch(*(*groups)[g], f.q, st) == XT_OK &&
+                 cudaEventRecord(join, st) == cudaSuccess &&
+                 cudaStreamWaitEvent(master, join, 0) == cudaSuccess;
+        }
     }
     return ok && flexb_zcopy(all, f.nall, f.dims, master) == XT_OK &&
            kron_nb_batch(all, f.nall, f.q, f.dims, master) == XT_OK &&
@@ -830,20 +889,26 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
             }
             // the live systems of the fused step: node-block operator, the
             // first such system's q
-            // largest first: their ILU branches, the longest chains, start first
+            // largest first (their sweeps, the longest chains, lead the tables)
             std::vector<int> fused;
+            std::vector<FlexStepItem> items;
+            std::vector<IluRegEntry> ilu;
             fs.q = 0;
             for (int o = 0; batch_fused_on() && o < count; ++o) {
                 const int i = b->order[o];
                 if (!live(i)) continue;
                 System& S = b->sys[i]->sys;
-                if (!S.ilu || !kron_nb_batchable(S.K, S.q) || (fs.q && S.q != fs.q) ||
-                    fused.size() >= 65535)  // the table entry is blockIdx.y
+                if ((fs.q && S.q != fs.q) || fused.size() >= 65535)  // entry = blockIdx.y
                     continue;
+                FlexStepItem e;
+                IluRegEntry r;
+                if (!fused_item(S, im, e, r)) continue;
                 fs.q = S.q;
                 fused.push_back(i);
+                items.push_back(e);
+                ilu.push_back(r);
             }
-            if (!fused.empty() && fused_build(fs, b, fused, run, im, count) != XT_OK) {
+            if (!fused.empty() && fused_build(fs, b, fused, items, ilu, run, im, count) != XT_OK) {
                 fused.clear();  // their own branches instead
                 fs.sys.clear();
                 fs.nall = 0;
@@ -857,7 +922,7 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
             if (ok) {
                 ok = cudaEventRecord(gp.ev[count], gp.master) == cudaSuccess;
                 if (ok && !fused.empty()) {
-                    ok = fused_capture(fs, b, gp.master, gp.ev[count + 1], gp.ev);
+                    ok = fused_capture(fs, b, gp.master);
                     for (int i : fused) {
                         in_graph[i] = 1;
                         cap_two[i] = run[i].two_pass;

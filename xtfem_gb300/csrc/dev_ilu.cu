@@ -1698,16 +1698,6 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
     return XT_OK;
 }
 
-struct RegArgs {
-    const unsigned char* slots;
-    const float* rhs;      // [Q][rstride] right-hand sides in lane-slot order
-    float* out;            // forward: the backward sweep's rhs; backward: z
-    long long rstride, ostride;
-    int nl, ncw, slot_bytes, zero_off;
-    int pf;  // levels ahead of use at which a warp's slot is prefetched into L2 (0: off)
-    const int* skip;  // optional: nothing to do when skip[0] != 0
-};
-
 __device__ __forceinline__ float4 nc_v4f(const void* p)
 {
     float4 r;
@@ -1987,18 +1977,19 @@ __global__ void __launch_bounds__(reg_max_warps(DEP) * 32, 1)
     tri_reg_body<H, SMAX, UPPER, W16, DEP>(a, blockIdx.x);
 }
 
-// One thread block per (row block, temporal block) of a block-Jacobi
-// factor: row block blockIdx.x / q with its sweep arguments from the table,
-// temporal block blockIdx.x % q; the output, the prefetch distance and the
-// skip flag are the launch's.
+// One thread block per (entry, temporal block): entry blockIdx.x / q of the
+// table, temporal block blockIdx.x % q.  The entries are the row blocks of
+// a block-Jacobi factor (the output and the skip flag are the launch's) or
+// the sweeps of a batch of systems (each entry's own); the prefetch
+// distance is the launch's.
 template <int H, int SMAX, bool UPPER, bool W16>
 __global__ void __launch_bounds__(kRegMaxWarps * 32, 1)
     k_tri_reg_parts(const RegArgs* __restrict__ args, int q, int pf, const int* skip, float* out)
 {
     RegArgs a = args[blockIdx.x / q];
     a.pf = pf;
-    a.skip = skip;
-    a.out = out;
+    if (skip) a.skip = skip;
+    if (out) a.out = out;
     tri_reg_body<H, SMAX, UPPER, W16, 2>(a, blockIdx.x % q);
 }
 
@@ -2463,7 +2454,145 @@ int upload_tri(DevTri& d, const TriHost& h, cudaStream_t s)
     return XT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batches of systems (the lockstep batch's step graph): the register
+// sweeps of many systems in one launch per group of equal kernel shape.
+
+// The pre-pass of k_rhs_slots for table entry blockIdx.y, its input the hi
+// part of the entry's basis column j (what the per-system step copies into
+// the ILU input first): the same products in the same order.
+template <int Q>
+__global__ void kb_rhs_slots(const FlexStepItem* __restrict__ t)
+{
+    __shared__ float sA[Q * Q];
+    const FlexStepItem& e = t[blockIdx.y];
+    const int* ctl = e.ctl;
+    if (ctl[1] != 0) return;
+    for (int i = threadIdx.x; i < Q * Q; i += blockDim.x) sA[i] = (float)e.Ainv[i];
+    __syncthreads();
+    const float2* col = e.V + (size_t)ctl[0] * (size_t)e.nl;
+    const long long lanes = e.lanes;
+    const int* src = e.src;
+    float* rhs = e.rrhs;
+    for (long long tt = blockIdx.x * (long long)blockDim.x + threadIdx.x; tt < lanes;
+         tt += (long long)gridDim.x * blockDim.x) {
+        const int row = src[tt];
+        float vr[Q];
+#pragma unroll
+        for (int j = 0; j < Q; ++j) vr[j] = row >= 0 ? col[(size_t)row * Q + j].x : 0.0f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            float b = 0.0f;
+#pragma unroll
+            for (int j = 0; j < Q; ++j) b = fmaf(sA[j * Q + q], vr[j], b);
+            rhs[(size_t)q * lanes + tt] = b;
+        }
+    }
+}
+
 }  // namespace
+
+int flexb_rhs(const FlexStepItem* t, int count, int q, long long lanes_max, cudaStream_t s)
+{
+    if (count <= 0) return XT_OK;
+    const long long bx = std::max(1LL, std::min(4096LL, (lanes_max + 1023) / 1024));
+    const dim3 grid((unsigned)bx, (unsigned)count);
+    switch (q) {
+    case 1: kb_rhs_slots<1><<<grid, 256, 0, s>>>(t); break;
+    case 2: kb_rhs_slots<2><<<grid, 256, 0, s>>>(t); break;
+    case 3: kb_rhs_slots<3><<<grid, 256, 0, s>>>(t); break;
+    case 4: kb_rhs_slots<4><<<grid, 256, 0, s>>>(t); break;
+    case 5: kb_rhs_slots<5><<<grid, 256, 0, s>>>(t); break;
+    case 6: kb_rhs_slots<6><<<grid, 256, 0, s>>>(t); break;
+    case 7: kb_rhs_slots<7><<<grid, 256, 0, s>>>(t); break;
+    case 8: kb_rhs_slots<8><<<grid, 256, 0, s>>>(t); break;
+    default: set_error("flexb_rhs: 1 <= q <= 8"); return XT_ERR_ARG;
+    }
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+namespace {
+// The (shares, steps) pairs the register sweep has kernels for (as
+// launch_reg_any dispatches them).
+bool reg_pair_ok(int H, int smax)
+{
+    return (H == 2 && (smax == 8 || smax == 12 || smax == 16)) || (H == 1 && (smax == 12 || smax == 20)) ||
+           (H == 4 && smax == 8);
+}
+
+template <int H, int SMAX>
+int reg_group_hs(const RegGroup& g, int q, cudaStream_t s, bool prepare)
+{
+    const RegArgs* a = reinterpret_cast<const RegArgs*>(g.args.p);
+    auto kernel = g.upper ? (g.w16 ? k_tri_reg_parts<H, SMAX, true, true> : k_tri_reg_parts<H, SMAX, true, false>)
+                          : (g.w16 ? k_tri_reg_parts<H, SMAX, false, true> : k_tri_reg_parts<H, SMAX, false, false>);
+    if (prepare) {
+        XT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem()));
+        return XT_OK;
+    }
+    const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
+    kernel<<<q * g.count, g.ncw * 32, g.smem, s>>>(a, q, pf, nullptr, nullptr);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int reg_group_any(const RegGroup& g, int q, cudaStream_t s, bool prepare)
+{
+    if (g.count < 1 || g.ncw < 1 || g.ncw > kRegMaxWarps || (long long)q * g.count > INT32_MAX ||
+        g.smem > (size_t)max_dyn_smem() || !g.args.p) {
+        set_error("register sweep group: bad shape");
+        return XT_ERR_ARG;
+    }
+    if (g.H == 2 && g.smax == 8) return reg_group_hs<2, 8>(g, q, s, prepare);
+    if (g.H == 2 && g.smax == 12) return reg_group_hs<2, 12>(g, q, s, prepare);
+    if (g.H == 2 && g.smax == 16) return reg_group_hs<2, 16>(g, q, s, prepare);
+    if (g.H == 1 && g.smax == 12) return reg_group_hs<1, 12>(g, q, s, prepare);
+    if (g.H == 1 && g.smax == 20) return reg_group_hs<1, 20>(g, q, s, prepare);
+    if (g.H == 4 && g.smax == 8) return reg_group_hs<4, 8>(g, q, s, prepare);
+    set_error("register sweep group: no kernel for these shares and steps");
+    return XT_ERR_ARG;
+}
+}  // namespace
+
+int ilu_reg_entry(const DevIlu& F, int q, float* z, const int* skip, cudaStream_t s,
+                  IluRegEntry& e)
+{
+    e = IluRegEntry{};
+    // the apply launch_tri would run: FP32, register sweep, one row block
+    if (F.L.g != 3 || env_int("XTFEM_ILU_FMT", 4) != 4 || q < 1 || q > 8) return XT_OK;
+    const int H = F.shares > 0 ? F.shares : env_int("XTFEM_ILU_SHARES", 2);
+    IluStage* st = nullptr;
+    XT_TRY(get_stage<float>(F, q, 4, s, st, H));
+    if (!st || !st->reg_ok || st->parts > 1 || !st->regL || !st->regU) return XT_OK;
+    const RegTri& L = *st->regL;
+    const RegTri& U = *st->regU;
+    if (L.w16 != U.w16 || L.H != U.H || L.smax != U.smax || !reg_pair_ok(L.H, L.smax)) return XT_OK;
+    const int pf = std::max(0, std::min(64, env_int("XTFEM_ILU_PF", 8)));
+    e.src = st->srcL.p;
+    e.lanes = L.lanes;
+    e.rrhs = st->rrhsL.p;
+    e.H = L.H;
+    e.smax = L.smax;
+    e.w16 = L.w16 ? 1 : 0;
+    e.L = RegArgs{L.slots.p, st->rrhsL.p, st->rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw,
+                  L.slot_bytes, L.zero_off, pf, skip};
+    e.U = RegArgs{U.slots.p, st->rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off,
+                  pf, skip};
+    e.smemL = (size_t)L.win_elems * 4;
+    e.smemU = (size_t)U.win_elems * 4;
+    e.ok = true;
+    return XT_OK;
+}
+
+int reg_group_prepare(const RegGroup& g) { return reg_group_any(g, 1, nullptr, true); }
+
+int reg_group_launch(const RegGroup& g, int q, cudaStream_t s)
+{
+    return reg_group_any(g, q, s, false);
+}
 
 namespace {
 // The rows [r0, r1) of a 1-based MSR factor with no entry outside them, as

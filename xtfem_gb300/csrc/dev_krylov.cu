@@ -1086,17 +1086,6 @@ int ew_grid(long long nmax)
     return (int)std::max(1LL, std::min(b, 4096LL));
 }
 
-__global__ void kb_flex_hi(const FlexStepItem* __restrict__ t)
-{
-    const FlexStepItem& e = t[blockIdx.y];
-    const int* ctl = e.ctl;
-    if (ctl[1] != 0) return;
-    const float2* col = e.V + (size_t)ctl[0] * (size_t)e.nl;
-    float* d = e.d32;
-    const size_t n = (size_t)e.n, stride = (size_t)gridDim.x * blockDim.x;
-    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) d[i] = col[i].x;
-}
-
 __global__ void kb_flex_zcopy(const FlexStepItem* __restrict__ t)
 {
     const FlexStepItem& e = t[blockIdx.y];
@@ -1189,15 +1178,6 @@ int df_row_blocks_for(long long nl, const Reduce& r) { return df_row_blocks(nl /
 int df_dot_rows_for(long long nl, const Reduce& r) { return df_dot_rows(nl / 2, r.nblocks); }
 int df_dot_blocks_max(int im, int dotrows) { return df_dot_grid(im, dotrows); }
 int df_dot_wave() { return 6 * 148; }
-
-int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
-{
-    if (count <= 0) return XT_OK;
-    kb_flex_hi<<<dim3(ew_grid(d.nmax), count), kThreads, 0, s>>>(t);
-    note_launches(1);
-    XT_CUDA(cudaGetLastError());
-    return XT_OK;
-}
 
 int flexb_zcopy(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s)
 {

@@ -275,6 +275,46 @@ int flexd_scale_copy(const int* ctl, const double* st, int im, const float2* w, 
                      size_t nl, size_t n, cudaStream_t s);
 int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s);
 
+// Arguments of one register sweep (one triangle of one factor or row block;
+// dev_ilu.cu): the slots, the right-hand sides in lane-slot order ([q]
+// arrays of rstride), the output (forward: the backward sweep's right-hand
+// sides, ostride apart; backward: z, interleaved), levels, warps, slot
+// bytes, the window's zero slot, the L2 prefetch distance in levels (0 off)
+// and an optional skip flag (nothing to do when skip[0] != 0).
+struct RegArgs {
+    const unsigned char* slots;
+    const float* rhs;
+    float* out;
+    long long rstride, ostride;
+    int nl, ncw, slot_bytes, zero_off;
+    int pf;
+    const int* skip;
+};
+// A system's default FP32 ILU apply as a batch entry: the pre-pass's lane
+// map and right-hand-side arrays and the two sweeps' arguments (output z,
+// skip flag skip).  ok is false when the apply is another format (a
+// block-Jacobi factor, a fall-back sweep) or has no batched launch.
+struct IluRegEntry {
+    bool ok = false;
+    const int* src = nullptr;  // row of each forward lane slot (-1: none)
+    long long lanes = 0;
+    float* rrhs = nullptr;     // forward right-hand sides, [q][lanes]
+    int H = 0, smax = 0, w16 = 0;
+    RegArgs L{}, U{};
+    size_t smemL = 0, smemU = 0;  // window bytes
+};
+int ilu_reg_entry(const DevIlu& F, int q, float* z, const int* skip, cudaStream_t s,
+                  IluRegEntry& e);
+// One launch of a batch's sweeps: entries with the same shares, steps,
+// offset width, warps and direction (args: a device table of count entries).
+struct RegGroup {
+    int H = 0, smax = 0, w16 = 0, ncw = 0, upper = 0, count = 0;
+    size_t smem = 0;
+    DBuf<unsigned char> args;
+};
+int reg_group_prepare(const RegGroup& g);  // outside a capture: kernel attributes
+int reg_group_launch(const RegGroup& g, int q, cudaStream_t s);
+
 // ------------------------------------- batched device-driven Arnoldi steps
 // One system of a batch in a table that drives kernels serving every system
 // of the batch in one launch (blockIdx.y = the system's entry): the buffers
@@ -286,7 +326,6 @@ struct FlexStepItem {
     double* st;        // FlexLayout(im) state of the cycle
     double* partial;   // reduction scratch
     float2* V;         // double-float basis, column stride nl
-    float* d32;        // ILU input: hi part of basis column j
     float* zfix;       // ILU output
     float* Z;          // preconditioned vectors, column stride n
     float2* wfix;      // operator output, orthogonalised in place
@@ -295,6 +334,10 @@ struct FlexStepItem {
     int rowblocks;      // row blocks of the norm pass
     int dotrows;        // row blocks per basis chunk of the dot pass (at most)
     int dotblocks;      // thread blocks of the system's dot pass
+    const int* src;     // ILU pre-pass (IluRegEntry): lane map, lanes, right-hand
+    long long lanes;    // sides, A^-1 (q x q)
+    float* rrhs;
+    const double* Ainv;
     int nodes;          // node-block operator: K's 3 x 3 blocks, M's scalars
     const int* bptr;
     const int* bcol;
@@ -316,8 +359,9 @@ int df_dot_blocks_max(int im, int dotrows);
 // The thread blocks of one wave of a dot pass (a batch deals them to its
 // systems by size).
 int df_dot_wave();
-// Basis column j's hi part into the ILU input; the ILU output into Z column j.
-int flexb_hi(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
+// The ILU pre-pass of every entry from the hi part of its basis column j;
+// the ILU output into Z column j.
+int flexb_rhs(const FlexStepItem* t, int count, int q, long long lanes_max, cudaStream_t s);
 int flexb_zcopy(const FlexStepItem* t, int count, const FlexStepDims& d, cudaStream_t s);
 // Gram-Schmidt of every system's operator output: the first pass of the
 // systems in `two` (two passes), h1 = 0 for those in `one`, then the
