@@ -1482,23 +1482,12 @@ struct RegTri {
     bool w16 = false;  // 16-bit window byte offsets (window <= 64 KB)
     long long lanes = 0;  // nl * ncw * 32
     DBuf<unsigned char> slots;
-    // warps with a chunk at each (sub-)level: chunks are dealt to warps
-    // 0, 1, ... in order, so the warps from act[l] on have empty slots there
-    std::vector<int> act_h;
-    DBuf<int> act;
     std::vector<int> row_slot;             // host: lane slot of each row's h = 0 lane
     std::vector<std::vector<int>> chunks;  // host (build only): level-order groups per chunk
     std::vector<int> chunk_slot, chunk_steps;
 };
 
 namespace {
-
-// The active-warp counts of a planned triangle for its sweep, or null (every
-// warp runs every level's slot, empty or not): XTFEM_ILU_SKIP=0.
-const int* reg_act(const RegTri& t)
-{
-    return env_int("XTFEM_ILU_SKIP", 1) != 0 ? t.act.p : nullptr;
-}
 
 int reg_warps(const TriHost& h, int GPW)
 {
@@ -1521,7 +1510,6 @@ bool reg_plan(const TriHost& h, int H, RegTri& t, int force_ncw = 0)
     t.chunks.clear();
     t.chunk_slot.clear();
     t.chunk_steps.clear();
-    t.act_h.clear();
     int nl = 0, smax = 0;
     std::vector<int> ord;
     auto rowlen = [&](int i, int r) {
@@ -1535,11 +1523,7 @@ bool reg_plan(const TriHost& h, int H, RegTri& t, int force_ncw = 0)
         std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return longest(a) > longest(b); });
         const int nch = (ng + GPW - 1) / GPW;
         for (int c = 0; c < nch; ++c) {
-            if (c % t.ncw == 0) {  // a new (sub-)level every ncw chunks
-                ++nl;
-                t.act_h.push_back(0);
-            }
-            ++t.act_h.back();
+            if (c % t.ncw == 0) ++nl;  // a new (sub-)level every ncw chunks
             std::vector<int> grp(ord.begin() + c * GPW, ord.begin() + std::min(ng, (c + 1) * GPW));
             const long long slot = (long long)(nl - 1) * t.ncw + c % t.ncw;
             int steps = 0;
@@ -1659,9 +1643,8 @@ int reg_fill(const TriHost& h, RegTri& t, int smax, int Q, const std::vector<int
         }
         for (int lane = 0; lane < 32; ++lane) valid = valid && ent[lane].empty();
     }
-    if (!valid || (int)t.act_h.size() != t.nl) return XT_OK;
+    if (!valid) return XT_OK;
     XT_TRY(t.slots.upload(blob.data(), blob.size(), s));
-    XT_TRY(t.act.upload(t.act_h.data(), t.act_h.size(), s));
     XT_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
     t.chunks.clear();
     t.chunks.shrink_to_fit();
@@ -1784,7 +1767,6 @@ struct RegSet {
     float4 gm;
     int go;
     float b;
-    bool on;  // the warp has a chunk at the set's level (else the slot is empty)
 };
 
 // The slot at p (already offset to this warp's slot of the level) and the
@@ -1886,41 +1868,24 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     const size_t pstep = pf_slot ? sstep : (size_t)a.ncw * 32 * sizeof(float);
     const bool pf_on = pf_slot || pf_rhs;
     const int pfl = a.nl - DEP - a.pf;
-    // Empty slots: chunks are dealt to warps 0, 1, ... at every (sub-)level,
-    // so this warp has one at level L when warp < act[L]; an empty slot (no
-    // store, every step on the zero slot) is neither loaded nor computed.
-    // act of the level a reload is for is read one level ahead.
-    const int* actp = a.act;
-    auto active = [&](int L) { return !actp || warp < nc_i(actp + L); };
-    int act_next = a.ncw;  // act[lk + DEP] at level lk
     // one level: compute it with set S, reload S with the level DEP ahead,
     // prefetch, advance, barrier
     auto level = [&](RegSet<SMAX, W16>& S, int lk) {
-        if (S.on) reg_level<H, SMAX, W16>(S, wbase, rwin, out, lane0);
-        if (lk + DEP < a.nl) {
-            S.on = warp < act_next;
-            if (S.on) reg_load<SMAX, W16>(S, sp, bp, lane);
-        }
-        if (actp && lk + DEP + 1 < a.nl) act_next = nc_i(actp + lk + DEP + 1);
+        reg_level<H, SMAX, W16>(S, wbase, rwin, out, lane0);
+        if (lk + DEP < a.nl) reg_load<SMAX, W16>(S, sp, bp, lane);
         if (pf_on && lk < pfl) prefetch_l2(pp);
         pp += pstep;
         sp += sstep;
         bp += a.ncw * 32;
         level_barrier();
     };
-    // the first DEP levels' sets, and act of level DEP
-    auto first = [&](RegSet<SMAX, W16>& S, int L) {
-        S.on = L < a.nl && active(L);
-        if (S.on) reg_load<SMAX, W16>(S, sp + L * sstep, bp + L * a.ncw * 32, lane);
-    };
-    if (actp && DEP < a.nl) act_next = nc_i(actp + DEP);
     if constexpr (DEP == 4) {
         // four register sets, four levels per trip
         RegSet<SMAX, W16> s0, s1, s2, s3;
-        first(s0, 0);
-        first(s1, 1);
-        first(s2, 2);
-        first(s3, 3);
+        reg_load<SMAX, W16>(s0, sp, bp, lane);
+        if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
+        if (a.nl > 2) reg_load<SMAX, W16>(s2, sp + 2 * sstep, bp + 2 * a.ncw * 32, lane);
+        if (a.nl > 3) reg_load<SMAX, W16>(s3, sp + 3 * sstep, bp + 3 * a.ncw * 32, lane);
         sp += 4 * sstep;
         bp += 4 * a.ncw * 32;
         level_barrier();  // the zero slot is set
@@ -1935,30 +1900,66 @@ __device__ __forceinline__ void tri_reg_body(const RegArgs& a, int tb)
     if constexpr (DEP == 3) {
         // three register sets, three levels per trip
         RegSet<SMAX, W16> s0, s1, s2;
-        first(s0, 0);
-        first(s1, 1);
-        first(s2, 2);
+        reg_load<SMAX, W16>(s0, sp, bp, lane);
+        if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
+        if (a.nl > 2) reg_load<SMAX, W16>(s2, sp + 2 * sstep, bp + 2 * a.ncw * 32, lane);
         sp += 3 * sstep;
         bp += 3 * a.ncw * 32;
         level_barrier();  // the zero slot is set
         for (int l = 0; l < a.nl; l += 3) {
-            level(s0, l);
-            if (l + 1 < a.nl) level(s1, l + 1);
-            if (l + 2 < a.nl) level(s2, l + 2);
+            reg_level<H, SMAX, W16>(s0, wbase, rwin, out, lane0);
+            if (l + 3 < a.nl) reg_load<SMAX, W16>(s0, sp, bp, lane);
+            if (pf_on && l < pfl) prefetch_l2(pp);
+            pp += pstep;
+            sp += sstep;
+            bp += a.ncw * 32;
+            level_barrier();
+            if (l + 1 < a.nl) {
+                reg_level<H, SMAX, W16>(s1, wbase, rwin, out, lane0);
+                if (l + 4 < a.nl) reg_load<SMAX, W16>(s1, sp, bp, lane);
+                if (pf_on && l + 1 < pfl) prefetch_l2(pp);
+                pp += pstep;
+                sp += sstep;
+                bp += a.ncw * 32;
+                level_barrier();
+            }
+            if (l + 2 < a.nl) {
+                reg_level<H, SMAX, W16>(s2, wbase, rwin, out, lane0);
+                if (l + 5 < a.nl) reg_load<SMAX, W16>(s2, sp, bp, lane);
+                if (pf_on && l + 2 < pfl) prefetch_l2(pp);
+                pp += pstep;
+                sp += sstep;
+                bp += a.ncw * 32;
+                level_barrier();
+            }
         }
         return;
     }
     // two register sets, a pair of levels per trip: the set a level used is
     // reloaded, right after it, with the level two ahead
     RegSet<SMAX, W16> s0, s1;
-    first(s0, 0);
-    first(s1, 1);
+    reg_load<SMAX, W16>(s0, sp, bp, lane);
+    if (a.nl > 1) reg_load<SMAX, W16>(s1, sp + sstep, bp + a.ncw * 32, lane);
     sp += 2 * sstep;
     bp += 2 * a.ncw * 32;
     level_barrier();  // the zero slot is set
     for (int l = 0; l < a.nl; l += 2) {
-        level(s0, l);
-        if (l + 1 < a.nl) level(s1, l + 1);
+        reg_level<H, SMAX, W16>(s0, wbase, rwin, out, lane0);
+        if (l + 2 < a.nl) reg_load<SMAX, W16>(s0, sp, bp, lane);
+        if (pf_on && l < pfl) prefetch_l2(pp);
+        pp += pstep;
+        sp += sstep;
+        bp += a.ncw * 32;
+        level_barrier();
+        if (l + 1 < a.nl) {
+            reg_level<H, SMAX, W16>(s1, wbase, rwin, out, lane0);
+            if (l + 3 < a.nl) reg_load<SMAX, W16>(s1, sp, bp, lane);
+            if (pf_on && l + 1 < pfl) prefetch_l2(pp);
+            pp += pstep;
+            sp += sstep;
+            bp += a.ncw * 32;
+            level_barrier();
+        }
     }
 }
 
@@ -2075,11 +2076,9 @@ int build_reg_parts(const DevIlu& F, int Q, int H, IluStage& st, cudaStream_t s)
     std::vector<RegArgs> aL(P), aU(P);
     for (int b = 0; b < P; ++b) {
         aL[b] = RegArgs{Ls[b]->slots.p, st.rrhsL.p + offL[b], nullptr, offL[P], offU[P],
-                        Ls[b]->nl, ncw, Ls[b]->slot_bytes, Ls[b]->zero_off, 0, nullptr,
-                        reg_act(*Ls[b])};
+                        Ls[b]->nl, ncw, Ls[b]->slot_bytes, Ls[b]->zero_off, 0, nullptr};
         aU[b] = RegArgs{Us[b]->slots.p, st.rrhsU.p + offU[b], nullptr, offU[P], 0,
-                        Us[b]->nl, ncw, Us[b]->slot_bytes, Us[b]->zero_off, 0, nullptr,
-                        reg_act(*Us[b])};
+                        Us[b]->nl, ncw, Us[b]->slot_bytes, Us[b]->zero_off, 0, nullptr};
     }
     XT_TRY(st.argsL.upload(reinterpret_cast<const unsigned char*>(aL.data()), sizeof(RegArgs) * P, s));
     XT_TRY(st.argsU.upload(reinterpret_cast<const unsigned char*>(aU.data()), sizeof(RegArgs) * P, s));
@@ -2146,9 +2145,9 @@ int launch_reg(const IluStage& st, const double* dAinv, const float* v, float* z
     const int nblk = (int)std::max(1LL, std::min<long long>((L.lanes + 255) / 256, 152LL * 8));
     k_rhs_slots<Q><<<nblk, 256, 0, s>>>(st.srcL.p, L.lanes, dAinv, v, st.rrhsL.p, skip);
     RegArgs aL{L.slots.p, st.rrhsL.p, st.rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw, L.slot_bytes,
-               L.zero_off, pf, skip, reg_act(L)};
+               L.zero_off, pf, skip};
     RegArgs aU{U.slots.p, st.rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off, pf,
-               skip, reg_act(U)};
+               skip};
     k_tri_reg<H, SMAX, false, W16, DEP><<<Q, L.ncw * 32, (size_t)L.win_elems * 4, s>>>(aL);
     k_tri_reg<H, SMAX, true, W16, DEP><<<Q, U.ncw * 32, (size_t)U.win_elems * 4, s>>>(aU);
     note_launches(3);
@@ -2579,9 +2578,9 @@ int ilu_reg_entry(const DevIlu& F, int q, float* z, const int* skip, cudaStream_
     e.smax = L.smax;
     e.w16 = L.w16 ? 1 : 0;
     e.L = RegArgs{L.slots.p, st->rrhsL.p, st->rrhsU.p, L.lanes, U.lanes, L.nl, L.ncw,
-                  L.slot_bytes, L.zero_off, pf, skip, reg_act(L)};
+                  L.slot_bytes, L.zero_off, pf, skip};
     e.U = RegArgs{U.slots.p, st->rrhsU.p, z, U.lanes, 0, U.nl, U.ncw, U.slot_bytes, U.zero_off,
-                  pf, skip, reg_act(U)};
+                  pf, skip};
     e.smemL = (size_t)L.win_elems * 4;
     e.smemU = (size_t)U.win_elems * 4;
     e.ok = true;

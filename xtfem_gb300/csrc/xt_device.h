@@ -279,9 +279,8 @@ int flexd_solve(const int* ctl, double* st, int im, cudaStream_t s);
 // dev_ilu.cu): the slots, the right-hand sides in lane-slot order ([q]
 // arrays of rstride), the output (forward: the backward sweep's right-hand
 // sides, ostride apart; backward: z, interleaved), levels, warps, slot
-// bytes, the window's zero slot, the L2 prefetch distance in levels (0 off),
-// an optional skip flag (nothing to do when skip[0] != 0) and the active
-// warps per level.
+// bytes, the window's zero slot, the L2 prefetch distance in levels (0 off)
+// and an optional skip flag (nothing to do when skip[0] != 0).
 struct RegArgs {
     const unsigned char* slots;
     const float* rhs;
@@ -290,7 +289,6 @@ struct RegArgs {
     int nl, ncw, slot_bytes, zero_off;
     int pf;
     const int* skip;
-    const int* act;  // warps with a chunk at each level (the rest: empty slots), or null
 };
 // A system's default FP32 ILU apply as a batch entry: the pre-pass's lane
 // map and right-hand-side arrays and the two sweeps' arguments (output z,
