@@ -291,9 +291,10 @@ int xt_batch_destroy(xt_batch b);
  * Precision 2 runs the batch in lockstep on the calling thread: every
  * system's refined solve with its Arnoldi bookkeeping on the device, and
  * per round the next 16 Arnoldi steps of every system as one CUDA graph
- * (one branch per system, captured once per call and replayed; a system
- * whose cycle or solve has ended does nothing in it), one host
- * synchronisation per round for all control words.  Other precisions run
+ * (captured once per call and replayed; each kernel of a step serves every
+ * system in one launch, the ILU sweeps one launch per group of equal
+ * kernel shape, and a system whose cycle or solve has ended does nothing
+ * in it), one host synchronisation per round for all control words.  Other precisions run
  * each system's solve on a pool of `workers` host threads.  Either way
  * each solution equals the system's own xt_system_solve bit for bit.
  * stats (may be NULL) gets 6 values per system as in xt_system_solve;

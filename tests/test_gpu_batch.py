@@ -3,8 +3,9 @@ elements with uneven n and their own load amplitudes, as in the many-rod
 workload, solved together; each result equals the same system solved
 alone, and the smallest rod (the 4 x 4 x 12 mesh) matches the oracle's
 FP64 GMRES.  Mode 2 runs the batch in lockstep rounds of Arnoldi steps
-(one CUDA graph per round over every rod); the rounds issued directly and
-the thread pool give the same bits."""
+(one CUDA graph per round over every rod, each step kernel one launch for
+all rods); the graph with one branch per rod, the rounds issued directly
+and the thread pool give the same bits."""
 import numpy as np
 import pytest
 

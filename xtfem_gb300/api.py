@@ -389,8 +389,9 @@ class SpaceTimeSystem:
 class SystemBatch:
     """Independent systems solved together (xt_batch_*).  Mode 2 runs in
     lockstep rounds of Arnoldi steps, one CUDA graph per round over every
-    system; other modes run one host worker thread per system at a time,
-    each system on its own stream."""
+    system, each step kernel one launch for all systems; other modes run
+    one host worker thread per system at a time, each system on its own
+    stream."""
 
     def __init__(self, systems, workers=0):
         self.systems = list(systems)
