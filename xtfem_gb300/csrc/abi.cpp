@@ -616,64 +616,23 @@ bool batch_fused_on()
     return !e || std::atoi(e) != 0;
 }
 
-// XTFEM_BATCH_HALVES=1: the fused step's systems as one set; by default
-// two halves run half a step apart (below).
-bool batch_halves_on()
-{
-    const char* e = std::getenv("XTFEM_BATCH_HALVES");
-    return !e || std::atoi(e) != 1;
-}
-
-// One half of the fused step's systems: their table (every entry, then the
-// two-pass and the one-pass ones), sizes, ILU sweep groups (one launch per
-// group of equal kernel shape, forward groups then backward groups, each
-// group on a branch of its own) and the events of those branches.
-struct FusedHalf {
-    DBuf<unsigned char> table;
-    std::vector<int> sys;  // batch index of each entry
-    int nall = 0, ntwo = 0, none = 0;
-    int off = 0;           // first entry of this half among the gathered control words
+struct FusedStep {
+    DBuf<unsigned char> table;  // entries of all, then of two, then of one
+    DBuf<int> dctl;             // gathered control words, four per entry of all
+    int* hgat = nullptr;        // their pinned host copy
+    std::vector<int> sys;       // batch index of each entry of all
+    int nall = 0, ntwo = 0, none = 0, q = 0;
     long long lanes_max = 0;
     FlexStepDims dims;
+    // the ILU sweeps: one launch per group of equal kernel shape, forward
+    // groups, then backward groups, each group on a branch of its own
     std::vector<std::unique_ptr<RegGroup>> gl, gu;
     std::vector<cudaEvent_t> gev;
-    FusedHalf() = default;
-    FusedHalf(const FusedHalf&) = delete;
-    FusedHalf& operator=(const FusedHalf&) = delete;
-    ~FusedHalf()
-    {
-        for (cudaEvent_t e : gev)
-            if (e) cudaEventDestroy(e);
-    }
-};
-
-// The fused step.  With two halves the second runs half a step behind the
-// first: in one graph launch the first half does its ILU apply and then the
-// rest of its step (operator, Gram-Schmidt, rotations, new basis column),
-// while the second half does the rest of its step and then the ILU apply of
-// its next one, so each half's latency-bound sweeps run under the other
-// half's bandwidth-bound passes.  The second half's first ILU apply of a
-// round is issued directly before the round's launches.
-struct FusedStep {
-    FusedHalf h[2];
-    int nh = 0, nall = 0, q = 0;
-    std::vector<int> sys;  // batch index of each gathered entry (first half, then second)
-    DBuf<int> dctl;        // gathered control words, four per entry
-    int* hgat = nullptr;   // their pinned host copy
-    cudaStream_t second = nullptr;
-    cudaEvent_t fork2 = nullptr, join2 = nullptr, pre = nullptr;
     ~FusedStep()
     {
         if (hgat) cudaFreeHost(hgat);
-        for (cudaEvent_t e : {fork2, join2, pre})
+        for (cudaEvent_t e : gev)
             if (e) cudaEventDestroy(e);
-        if (second) cudaStreamDestroy(second);
-    }
-    void clear()
-    {
-        nh = 0;
-        nall = 0;
-        sys.clear();
     }
 };
 
@@ -749,10 +708,12 @@ int fused_groups(std::vector<std::unique_ptr<RegGroup>>& out, const std::vector<
     return XT_OK;
 }
 
-// One half's table and sweep groups, uploaded before the capture: nothing
-// is allocated inside it.
-int half_build(FusedHalf& f, const std::vector<int>& idx, const std::vector<FlexStepItem>& items,
-               const std::vector<IluRegEntry>& ilu, const std::vector<FlexRun>& run, int im)
+// The table of the live systems in `idx` (each with its run's Gram-Schmidt
+// passes) and their sweep groups, uploaded before the capture: nothing is
+// allocated inside it.
+int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
+                const std::vector<FlexStepItem>& items, const std::vector<IluRegEntry>& ilu,
+                const std::vector<FlexRun>& run, int im, int count)
 {
     std::vector<FlexStepItem> all(items), two, one;
     f.sys = idx;
@@ -783,6 +744,10 @@ int half_build(FusedHalf& f, const std::vector<int>& idx, const std::vector<Flex
     XT_TRY(f.table.alloc(tab.size() * sizeof(FlexStepItem)));
     XT_CUDA(cudaMemcpy(f.table.p, tab.data(), tab.size() * sizeof(FlexStepItem),
                        cudaMemcpyHostToDevice));
+    XT_TRY(f.dctl.alloc((size_t)4 * count));
+    if (!f.hgat)
+        XT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&f.hgat), sizeof(int) * 4 * (size_t)count,
+                              cudaHostAllocDefault));
     XT_TRY(fused_groups(f.gl, ilu, false));
     XT_TRY(fused_groups(f.gu, ilu, true));
     const size_t nev = 2 + f.gl.size() + f.gu.size();
@@ -794,109 +759,37 @@ int half_build(FusedHalf& f, const std::vector<int>& idx, const std::vector<Flex
     return XT_OK;
 }
 
-// The fused step of the live systems in `idx` (largest first), split into
-// halves of alternate entries so that both hold large and small systems.
-int fused_build(FusedStep& f, const std::vector<int>& idx, const std::vector<FlexStepItem>& items,
-                const std::vector<IluRegEntry>& ilu, const std::vector<FlexRun>& run, int im,
-                int count)
-{
-    f.clear();
-    const int nh = (idx.size() >= 2 && batch_halves_on()) ? 2 : 1;
-    int off = 0;
-    for (int k = 0; k < nh; ++k) {
-        std::vector<int> si;
-        std::vector<FlexStepItem> it;
-        std::vector<IluRegEntry> ie;
-        for (size_t e = k; e < idx.size(); e += nh) {
-            si.push_back(idx[e]);
-            it.push_back(items[e]);
-            ie.push_back(ilu[e]);
-        }
-        XT_TRY(half_build(f.h[k], si, it, ie, run, im));
-        f.h[k].off = off;
-        off += f.h[k].nall;
-        f.sys.insert(f.sys.end(), si.begin(), si.end());
-    }
-    XT_TRY(f.dctl.alloc((size_t)4 * count));
-    if (!f.hgat)
-        XT_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&f.hgat), sizeof(int) * 4 * (size_t)count,
-                              cudaHostAllocDefault));
-    if (nh == 2 && !f.second) {
-        XT_CUDA(cudaStreamCreateWithFlags(&f.second, cudaStreamNonBlocking));
-        for (cudaEvent_t* e : {&f.fork2, &f.join2, &f.pre})
-            XT_CUDA(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    }
-    f.nh = nh;
-    f.nall = off;
-    return XT_OK;
-}
-
-// A half's ILU apply on stream s: the pre-pass of all its systems, then the
-// forward sweep groups side by side, then the backward ones.  Group g runs
-// on the stream of the half's g-th system (distinct streams: a half has no
-// more groups than systems).
-bool half_ilu(FusedHalf& f, xt_batch b, int q, cudaStream_t s)
-{
-    const FlexStepItem* all = reinterpret_cast<const FlexStepItem*>(f.table.p);
-    bool ok = flexb_rhs(all, f.nall, q, f.lanes_max, s) == XT_OK;
-    size_t ev = 0;
-    for (auto* groups : {&f.gl, &f.gu}) {
-        const cudaEvent_t fork = f.gev[ev++];
-        ok = ok && cudaEventRecord(fork, s) == cudaSuccess;
-        for (size_t g = 0; ok && g < groups->size(); ++g) {
-            cudaStream_t st = b->sys[f.sys[g]]->sys.stream;
-            const cudaEvent_t join = f.gev[ev++];
-            ok = cudaStreamWaitEvent(st, fork, 0) == cudaSuccess &&
-                 reg_group_launch(*(*groups)[g], q, st) == XT_OK &&
-                 cudaEventRecord(join, st) == cudaSuccess &&
-                 cudaStreamWaitEvent(s, join, 0) == cudaSuccess;
-        }
-    }
-    return ok;
-}
-
-// The rest of a half's step on stream s: the copy into Z, the operator,
-// Gram-Schmidt, the rotations and the new basis column, then the gather of
-// its control words.
-bool half_rest(FusedHalf& f, int q, int* dctl, cudaStream_t s)
+// The fused step into the capture on `master`: the ILU pre-pass of all, the
+// forward sweep groups side by side, then the backward ones, then the
+// operator, Gram-Schmidt, rotations and the new basis column of all, and
+// the gathered control words.  Group g runs on the stream of the batch's
+// g-th entry (distinct streams: there are no more groups than entries).
+bool fused_capture(FusedStep& f, xt_batch b, cudaStream_t master)
 {
     const FlexStepItem* all = reinterpret_cast<const FlexStepItem*>(f.table.p);
     const FlexStepItem* two = all + f.nall;
     const FlexStepItem* one = two + f.ntwo;
-    return flexb_zcopy(all, f.nall, f.dims, s) == XT_OK &&
-           kron_nb_batch(all, f.nall, q, f.dims, s) == XT_OK &&
-           flexb_orth(all, f.nall, two, f.ntwo, one, f.none, f.dims, s) == XT_OK &&
-           flexb_givens_scale(all, f.nall, f.dims, s) == XT_OK &&
-           flexb_ctl_gather(all, f.nall, dctl + 4 * (size_t)f.off, s) == XT_OK;
-}
-
-// The fused step into the capture on `master`, then the gathered control
-// words copied to the host in one transfer.
-bool fused_capture(FusedStep& f, xt_batch b, cudaStream_t master)
-{
-    bool ok = true;
-    if (f.nh == 2)
-        ok = cudaEventRecord(f.fork2, master) == cudaSuccess &&
-             cudaStreamWaitEvent(f.second, f.fork2, 0) == cudaSuccess &&
-             half_rest(f.h[1], f.q, f.dctl.p, f.second) && half_ilu(f.h[1], b, f.q, f.second) &&
-             cudaEventRecord(f.join2, f.second) == cudaSuccess;
-    ok = ok && half_ilu(f.h[0], b, f.q, master) && half_rest(f.h[0], f.q, f.dctl.p, master);
-    if (f.nh == 2) ok = ok && cudaStreamWaitEvent(master, f.join2, 0) == cudaSuccess;
-    return ok && cudaMemcpyAsync(f.hgat, f.dctl.p, sizeof(int) * 4 * (size_t)f.nall,
-                                 cudaMemcpyDeviceToHost, master) == cudaSuccess;
-}
-
-// Before a round's launches: the second half's ILU apply of its current
-// step (the launches then start that half at the rest of its step).
-int fused_prestep(FusedStep& f, xt_batch b, cudaStream_t master)
-{
-    if (f.nh != 2) return XT_OK;
-    if (!half_ilu(f.h[1], b, f.q, f.second) || cudaEventRecord(f.pre, f.second) != cudaSuccess ||
-        cudaStreamWaitEvent(master, f.pre, 0) != cudaSuccess) {
-        set_error("xt_batch_solve: the second half's ILU apply could not be issued");
-        return XT_ERR_CUDA;
+    bool ok = flexb_rhs(all, f.nall, f.q, f.lanes_max, master) == XT_OK;
+    size_t ev = 0;
+    for (auto* groups : {&f.gl, &f.gu}) {
+        const cudaEvent_t fork = f.gev[ev++];
+        ok = ok && cudaEventRecord(fork, master) == cudaSuccess;
+        for (size_t g = 0; ok && g < groups->size(); ++g) {
+            cudaStream_t st = b->sys[f.sys[g]]->sys.stream;
+            const cudaEvent_t join = f.gev[ev++];
+            ok = cudaStreamWaitEvent(st, fork, 0) == cudaSuccess &&
+                 reg_group_launch(*(*groups)[g], f.q, st) == XT_OK &&
+                 cudaEventRecord(join, st) == cudaSuccess &&
+                 cudaStreamWaitEvent(master, join, 0) == cudaSuccess;
+        }
     }
-    return XT_OK;
+    return ok && flexb_zcopy(all, f.nall, f.dims, master) == XT_OK &&
+           kron_nb_batch(all, f.nall, f.q, f.dims, master) == XT_OK &&
+           flexb_orth(all, f.nall, two, f.ntwo, one, f.none, f.dims, master) == XT_OK &&
+           flexb_givens_scale(all, f.nall, f.dims, master) == XT_OK &&
+           flexb_ctl_gather(all, f.nall, f.dctl.p, master) == XT_OK &&
+           cudaMemcpyAsync(f.hgat, f.dctl.p, sizeof(int) * 4 * (size_t)f.nall,
+                           cudaMemcpyDeviceToHost, master) == cudaSuccess;
 }
 
 int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, int im, double tol,
@@ -1015,9 +908,10 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
                 items.push_back(e);
                 ilu.push_back(r);
             }
-            if (!fused.empty() && fused_build(fs, fused, items, ilu, run, im, count) != XT_OK) {
+            if (!fused.empty() && fused_build(fs, b, fused, items, ilu, run, im, count) != XT_OK) {
                 fused.clear();  // their own branches instead
-                fs.clear();
+                fs.sys.clear();
+                fs.nall = 0;
                 cudaGetLastError();
             }
             std::vector<char> is_fused(count, 0);
@@ -1058,15 +952,14 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
                 gp.exec = nullptr;
                 cudaGetLastError();
                 std::fill(in_graph.begin(), in_graph.end(), 0);
-                fs.clear();
+                fs.sys.clear();
+                fs.nall = 0;
             }
             note_launches((int)-graph_kernels);  // captured, not run: counted per replay
             t_capture += since(tp);
             tp = clk::now();
         }
         if (gp.exec) {
-            const int pr = fused_prestep(fs, b, gp.master);
-            if (pr != XT_OK) return pr;
             for (int k = 0; k < kRound; ++k) XT_CUDA(cudaGraphLaunch(gp.exec, gp.master));
             XT_CUDA(cudaStreamSynchronize(gp.master));
             note_launches((int)(graph_kernels * kRound));
@@ -1117,9 +1010,9 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
     if (tracing)
         std::fprintf(stderr,
                      "[xtfem] batch lockstep: %d systems, %d rounds of %d steps, graph %s "
-                     "(%lld kernels, %d systems in batched kernels, %d halves); ms: start %.1f, "
-                     "capture %.1f, steps %.1f, host between rounds %.1f, download %.1f\n",
-                     count, rounds, kRound, gp.exec ? "yes" : "no", graph_kernels, fs.nall, fs.nh,
+                     "(%lld kernels, %d systems in batched kernels); ms: start %.1f, capture "
+                     "%.1f, steps %.1f, host between rounds %.1f, download %.1f\n",
+                     count, rounds, kRound, gp.exec ? "yes" : "no", graph_kernels, fs.nall,
                      t_start, t_capture, t_steps, t_host, t_down);
     if (lost_device) {
         set_error("xt_batch_solve: worker thread could not select the device");
