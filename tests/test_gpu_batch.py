@@ -132,3 +132,37 @@ def test_batch_lockstep_graph_direct_and_pool_agree(xt, cases, monkeypatch):
             for a, b in zip(out["graph"][0], sols):
                 assert np.array_equal(a, b), (passes, mode)
             assert out["graph"][1] == stats, (passes, mode)
+
+
+def test_batch_mixed_batched_and_branch_systems(xt, cases, monkeypatch):
+    """A round graph with both kinds of step: the rods served by the batched
+    step kernels and one rod with a block-Jacobi factor (four row blocks,
+    which has no batched sweep) on its own branch of step kernels.  Every
+    system gets the bits of its own solve, as with one branch per system and
+    as in the thread pool."""
+    c = cases[1]
+    alu, jlu, ju = xt.ilut(c["K"], 20, 1e-4, blocks=4)
+    bj = xt.SpaceTimeSystem(c["K"], c["M"])
+    bj.set_ilu(alu, jlu, ju, group=3, blocks=4)
+    bj.set_temporal(c["A"], c["B"])
+    assert bj.ilu_blocks == 4
+    systems = [cases[0]["sys"], bj, cases[2]["sys"], cases[3]["sys"]]
+    rhs = [cases[0]["rhs"], c["rhs"], cases[2]["rhs"], cases[3]["rhs"]]
+    out = {}
+    for mode, env in (("mixed", {}), ("branches", {"XTFEM_BATCH_FUSED": "0"}),
+                      ("pool", {"XTFEM_BATCH_LOCKSTEP": "0"})):
+        for k in ("XTFEM_BATCH_LOCKSTEP", "XTFEM_BATCH_FUSED"):
+            monkeypatch.delenv(k, raising=False)
+        for k, v in env.items():
+            monkeypatch.setenv(k, v)
+        batch = xt.SystemBatch(systems, workers=2)
+        out[mode] = batch.solve(rhs, im=30, tol=1e-8, precision=2)
+        batch.close()
+    bj.close()
+    sols, stats, status = out["mixed"]
+    assert (status == 0).all()
+    assert all(st["relres"] <= 1e-8 for st in stats)
+    for mode in ("branches", "pool"):
+        for a, b in zip(sols, out[mode][0]):
+            assert np.array_equal(a, b), mode
+        assert stats == out[mode][1], mode
