@@ -47,6 +47,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "xt_device.h"
@@ -248,6 +251,46 @@ int max_dyn_smem()
 }
 
 bool trace_on() { return std::getenv("XTFEM_TRACE") != nullptr; }
+
+// Runs a() on a second host thread (on the caller's device) while b() runs
+// on this one; returns the first failure, its message set on this thread
+// (an exception in a() becomes XT_ERR_HOST; one in b() is rethrown after
+// the join).
+template <class A, class B>
+int side_by_side(A&& a, B&& b)
+{
+    int dev = 0;
+    XT_CUDA(cudaGetDevice(&dev));
+    int ra = XT_OK;
+    std::string ea;
+    std::thread t([&] {
+        try {
+            if (cudaSetDevice(dev) != cudaSuccess) {
+                ra = XT_ERR_CUDA;
+                ea = "could not select the device on a helper thread";
+                return;
+            }
+            ra = a();
+            if (ra != XT_OK) ea = last_error();
+        } catch (const std::exception& e) {
+            ra = XT_ERR_HOST;
+            ea = e.what();
+        }
+    });
+    int rb = XT_OK;
+    try {
+        rb = b();
+    } catch (...) {
+        t.join();
+        throw;
+    }
+    t.join();
+    if (ra != XT_OK) {
+        set_error(ea);
+        return ra;
+    }
+    return rb;
+}
 
 int env_int(const char* name, int dflt)
 {
@@ -1667,7 +1710,12 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
     st.reg_ok = false;
     if (S.L.g != 3 || (H != 1 && H != 2 && H != 4)) return XT_OK;
     auto L = std::make_shared<RegTri>(), U = std::make_shared<RegTri>();
-    if (!reg_plan(S.L, H, *L) || !reg_plan(S.U, H, *U)) return XT_OK;
+    // the triangles are planned side by side, then filled side by side (the
+    // forward fill reads the backward triangle's row slots, set by its plan)
+    bool okL = false, okU = false;
+    XT_TRY(side_by_side([&] { okU = reg_plan(S.U, H, *U); return XT_OK; },
+                        [&] { okL = reg_plan(S.L, H, *L); return XT_OK; }));
+    if (!okL || !okU) return XT_OK;
     const int smax = reg_smax(H, std::max(L->smax, U->smax));
     if (smax == 0) return XT_OK;
     // 16-bit window offsets when every byte offset of both windows fits
@@ -1675,8 +1723,8 @@ int build_reg(const IluSched& S, int Q, int H, IluStage& st, cudaStream_t s)
     const bool w16 = (long long)std::max(L->win_elems, U->win_elems) * 4 <= 65536 &&
                      env_int("XTFEM_ILU_W16", 1) != 0;
     L->w16 = U->w16 = w16;
-    XT_TRY(reg_fill(S.U, *U, smax, Q, nullptr, s));
-    XT_TRY(reg_fill(S.L, *L, smax, Q, &U->row_slot, s));
+    XT_TRY(side_by_side([&] { return reg_fill(S.U, *U, smax, Q, nullptr, s); },
+                        [&] { return reg_fill(S.L, *L, smax, Q, &U->row_slot, s); }));
     if (!L->slots.p || !U->slots.p) return XT_OK;
     std::vector<int> src((size_t)L->lanes, -1);
     for (size_t r = 0; r < L->row_slot.size(); ++r) src[(size_t)L->row_slot[r]] = (int)r;
@@ -2645,8 +2693,8 @@ int build_ilu(DevIlu& d, int n, const double* alu, const int* jlu, const int* ju
     const int g = (group > 1 && n % group == 0 && group <= kMaxG) ? group : 1;
     d.n = n;
     auto sc = std::make_shared<IluSched>();
-    sc->L = schedule(n, alu, jlu, ju, g, false);
-    sc->U = schedule(n, alu, jlu, ju, g, true);
+    XT_TRY(side_by_side([&] { sc->U = schedule(n, alu, jlu, ju, g, true); return XT_OK; },
+                        [&] { sc->L = schedule(n, alu, jlu, ju, g, false); return XT_OK; }));
     XT_TRY(upload_tri(d.L, sc->L, s));
     XT_TRY(upload_tri(d.U, sc->U, s));
     d.sched = sc;
