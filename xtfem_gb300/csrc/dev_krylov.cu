@@ -351,6 +351,20 @@ __global__ void k_df_scale(float2* __restrict__ y, float ah, float al, size_t n)
         y[i] = df_norm(h, l);
     }
 }
+// k_df_scale, and the hi part of the result into hi (the next ILU input)
+__global__ void k_df_scale_hi(float2* __restrict__ y, float ah, float al, float* __restrict__ hi,
+                              size_t n)
+{
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const float2 v = y[i];
+        float h = 0.0f, l = 0.0f;
+        df_mul_acc(h, l, v.x, v.y, ah, al);
+        const float2 r = df_norm(h, l);
+        y[i] = r;
+        hi[i] = r.x;
+    }
+}
 
 // out[j] = sum_b (hi_b + lo_b) in FP64, one block per j, fixed order
 __global__ void k_finish_df(const double* __restrict__ partial, int nb, double* __restrict__ out)
@@ -950,14 +964,14 @@ int df_update_and_dot(const float2* V, size_t ld, int k, const double* h, float2
 }
 
 int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
-                       Reduce& r, cudaStream_t s)
+                       Reduce& r, cudaStream_t s, double* out)
 {
     if (n % 2 || ld % 2) { set_error("df_update: n and ld must be even"); return XT_ERR_ARG; }
     const int nb = df_row_blocks((long long)n / 2, r.nblocks);
     k_update_df<true><<<nb, 2 * kThreads, 0, s>>>(reinterpret_cast<const float4*>(V), ld / 2, k,
                                                   h, reinterpret_cast<float4*>(w), n / 2,
                                                   r.partial.p, nullptr);
-    k_finish_df<<<1, kThreads, 0, s>>>(r.partial.p, nb, r.out.p);
+    k_finish_df<<<1, kThreads, 0, s>>>(r.partial.p, nb, out ? out : r.out.p);
     note_launches(2);
     XT_CUDA(cudaGetLastError());
     return XT_OK;
@@ -991,6 +1005,15 @@ int df_scale(float2* y, double a, size_t n, cudaStream_t s)
 {
     const float ah = (float)a;
     k_df_scale<<<grid_for(n), kThreads, 0, s>>>(y, ah, (float)(a - (double)ah), n);
+    note_launches(1);
+    XT_CUDA(cudaGetLastError());
+    return XT_OK;
+}
+
+int df_scale_hi(float2* y, double a, float* hi, size_t n, cudaStream_t s)
+{
+    const float ah = (float)a;
+    k_df_scale_hi<<<grid_for(n), kThreads, 0, s>>>(y, ah, (float)(a - (double)ah), hi, n);
     note_launches(1);
     XT_CUDA(cudaGetLastError());
     return XT_OK;

@@ -526,8 +526,10 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
         }
         if (ro == 0.0) { ierr = -1; break; }
         if (its > 0 && !two_pass && ro > kOrthLoss * ro_est) two_pass = S.gs_latched = true;
+        // v1 and its hi part, the first step's ILU input; each step leaves
+        // the next one's the same way when it scales its new column
         XT_TRY(df_from_f64(S.w64.p, col(0), n, s));
-        XT_TRY(df_scale(col(0), 1.0 / ro, n, s));
+        XT_TRY(df_scale_hi(col(0), 1.0 / ro, S.d32.p, n, s));
         if (its == 0) eps1 = eps * ro;
         rs.assign(im + 1, 0.0);
         rs[0] = ro;
@@ -537,7 +539,6 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             ++i;
             ++its;
             const int i1 = i + 1;
-            XT_TRY(df_hi(col(i - 1), S.d32.p, n, s));
             if (S.op16) XT_TRY(nested_prec(S, S.d32.p, zc(i - 1)));
             else XT_TRY(apply_prec<float>(S, S.d32.p, zc(i - 1)));
             {  // w = A z in double-float, straight into the basis column
@@ -549,25 +550,24 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
             // as above, double-float values of 8 bytes
             prof_bytes(otok, (two_pass ? 4.0 * i + 6.0 : 2.0 * i + 3.0) * (double)nl * 8.0);
             XT_TRY(df_multi_dot(V, nl, i, col(i1 - 1), nl, S.red, s));
-            // two passes: hsave = (h1, h2, ||w||^2); one pass: (-, h, ||w||^2)
-            // with h1 = 0 taken on the host
+            // the last pass's projections h stay in red.out with the squared
+            // norm after them, red.out = (h, ||w||^2); two passes keep the
+            // first pass's in hsave.  The host's column: h1 + h (h1 = 0 for
+            // one pass).
             if (two_pass) {
                 XT_CUDA(cudaMemcpyAsync(S.hsave.p, S.red.out.p, i * sizeof(double),
                                         cudaMemcpyDeviceToDevice, s));
                 XT_TRY(df_update_and_dot(V, nl, i, S.hsave.p, col(i1 - 1), nl, S.red, s));
             }
-            XT_CUDA(cudaMemcpyAsync(S.hsave.p + i, S.red.out.p, i * sizeof(double),
-                                    cudaMemcpyDeviceToDevice, s));
-            XT_TRY(df_update_and_norm(V, nl, i, S.hsave.p + i, col(i1 - 1), nl, S.red, s));
-            XT_CUDA(cudaMemcpyAsync(S.hsave.p + 2 * i, S.red.out.p, sizeof(double),
-                                    cudaMemcpyDeviceToDevice, s));
+            XT_TRY(df_update_and_norm(V, nl, i, S.red.out.p, col(i1 - 1), nl, S.red, s,
+                                      S.red.out.p + i));
             prof_end(otok, s);
-            if (two_pass) {
-                XT_TRY(fetch(s, hbuf.data(), S.hsave.p, 2 * i + 1));
-            } else {
-                XT_TRY(fetch(s, hbuf.data() + i, S.hsave.p + i, i + 1));
+            if (two_pass)
+                XT_CUDA(cudaMemcpyAsync(hbuf.data(), S.hsave.p, i * sizeof(double),
+                                        cudaMemcpyDeviceToHost, s));
+            else
                 std::fill(hbuf.begin(), hbuf.begin() + i, 0.0);
-            }
+            XT_TRY(fetch(s, hbuf.data() + i, S.red.out.p, i + 1));
             for (int j = 0; j < i; ++j) HH(j, i - 1) = hbuf[j] + hbuf[i + j];
             t = std::sqrt(hbuf[2 * i]);
             if (!std::isfinite(t)) {
@@ -575,7 +575,8 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
                 return XT_ERR_NONFINITE;
             }
             HH(i1 - 1, i - 1) = t;
-            if (t != 0.0) XT_TRY(df_scale(col(i1 - 1), 1.0 / t, n, s));
+            if (t != 0.0) XT_TRY(df_scale_hi(col(i1 - 1), 1.0 / t, S.d32.p, n, s));
+            else XT_TRY(df_hi(col(i1 - 1), S.d32.p, n, s));
             for (int k = 2; k <= i; ++k) {
                 const int k1 = k - 1;
                 t = HH(k1 - 1, i - 1);

@@ -405,12 +405,16 @@ int df_multi_dot(const float2* V, size_t ld, int k, const float2* w, size_t n, R
                  cudaStream_t s);
 int df_update_and_dot(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
                       Reduce& r, cudaStream_t s);
+// update_and_norm: the squared norm into out (default r.out[0]); h may be
+// r.out itself (the update has read it before the norm is written)
 int df_update_and_norm(const float2* V, size_t ld, int k, const double* h, float2* w, size_t n,
-                       Reduce& r, cudaStream_t s);
+                       Reduce& r, cudaStream_t s, double* out = nullptr);
 int df_from_f64(const double* x, float2* y, size_t n, cudaStream_t s);
 int df_hi(const float2* x, float* y, size_t n, cudaStream_t s);
 int df_to_f64(const float2* x, double* y, size_t n, cudaStream_t s);
 int df_scale(float2* y, double a, size_t n, cudaStream_t s);
+// df_scale, and the hi part of the scaled y into hi
+int df_scale_hi(float2* y, double a, float* hi, size_t n, cudaStream_t s);
 // ||x||^2 (FP64) into r.out[0].
 template <class T>
 int norm2(const T* x, size_t n, Reduce& r, cudaStream_t s);
