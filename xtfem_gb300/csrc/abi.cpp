@@ -862,6 +862,7 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
     long long graph_kernels = 0;
     bool tried = false;
     for (int round = 0;; ++round) {
+        TraceRange tr("xtfem batch round");
         bool any = false;
         for (int i = 0; i < count; ++i) any = any || live(i);
         if (!any) break;

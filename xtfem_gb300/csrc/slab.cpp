@@ -711,6 +711,7 @@ int xt_slab_step(xt_slab s, double* stats)
     double local[12] = {0};
     double* st = stats ? stats : local;
     return guarded([&]() -> int {
+        TraceRange tr("xtfem slab step");
         if (s->cfg.overlap) {
             XT_TRY(step_overlap(*s, nullptr, st, nullptr));
             XT_CUDA(cudaStreamSynchronize(s->S.stream));
@@ -733,6 +734,7 @@ int xt_slab_step_host(xt_slab s, const double* fext, double* disp, double* D, do
     double local[12] = {0};
     double* st = stats ? stats : local;
     return guarded([&]() -> int {
+        TraceRange tr("xtfem slab step");
         cudaStream_t cs = s->S.stream;
         const size_t n = (size_t)s->p * s->q;
         if (s->cfg.overlap) {

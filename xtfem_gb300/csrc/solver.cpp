@@ -513,6 +513,7 @@ int gmres_flex(System& S, const double* rhs, double* sol, int im, double eps, in
     XT_TRY(fetch(s, hbuf.data(), S.red.out.p, 1));
     const double ro0 = std::sqrt(hbuf[0]);
     for (;;) {
+        TraceRange cycle("xtfem gmres cycle");
         // v1 = (rhs - A sol) / ||rhs - A sol||, the residual formed in FP64
         const double ro_est = ro;  // the previous cycle's estimate
         XT_CUDA(cudaMemcpyAsync(S.w64.p, rhs, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
@@ -944,6 +945,7 @@ int solve_flex_run(System& S, const double* b, double* x, int im, double tol, in
 int solve_refined(System& S, const double* b, double* x, int im, double tol, int maxits,
                   int inner, double inner_tol, GmresStats& st)
 {
+    TraceRange tr("xtfem solve");
     if (!S.ilu) {
         set_error("solve: no preconditioner set");
         return XT_ERR_STATE;

@@ -10,6 +10,7 @@
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "../../include/xtfem_gb300.h"
 
@@ -28,6 +29,16 @@ void set_error(const std::string& msg);
 const char* last_error();
 // Running count of kernel launches issued by the library.
 void note_launches(int n);
+
+// A named NVTX range over this scope on a profiler's timeline (a slab step,
+// a refined solve, a GMRES cycle, a round of the lockstep batch); without a
+// profiler attached the calls do nothing.
+struct TraceRange {
+    explicit TraceRange(const char* name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange&) = delete;
+    TraceRange& operator=(const TraceRange&) = delete;
+};
 // Diagnostics: when the environment variable XTFEM_TRACE is set, trace()
 // prints the step and synchronizes the device to surface errors early.
 void trace(const char* what);
