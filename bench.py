@@ -532,12 +532,14 @@ def run_batched(xt, args, specimens):
 
 
 def run_fp64_reference_point(xt, args):
-    """The plain FP64 GPU GMRES on the same workload (the 3x denominator)."""
+    """The plain FP64 GPU GMRES on the same workload (the 3x denominator),
+    CUDA events around up to 6 slabs after one untimed slab (about 2 s
+    each)."""
     prob = make_problem(xt)
     slab = xt.SlabSolver(prob, make_config(xt, precision=0, seed=WORKLOAD["seed"]))
     slab.step()
     xt.lib().xt_sync()
-    n = max(1, min(args.steps, 3))
+    n = max(1, min(args.steps, 6))
     xt.lib().xt_mark(2)
     st = [slab.step() for _ in range(n)]
     slab.drain()
