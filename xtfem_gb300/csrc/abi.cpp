@@ -711,7 +711,7 @@ int fused_groups(std::vector<std::unique_ptr<RegGroup>>& out, const std::vector<
 // The table of the live systems in `idx` (each with its run's Gram-Schmidt
 // passes) and their sweep groups, uploaded before the capture: nothing is
 // allocated inside it.
-int fused_build(FusedStep& f, xt_batch b, const std::vector<int>& idx,
+int fused_build(FusedStep& f, const std::vector<int>& idx,
                 const std::vector<FlexStepItem>& items, const std::vector<IluRegEntry>& ilu,
                 const std::vector<FlexRun>& run, int im, int count)
 {
@@ -909,7 +909,7 @@ int batch_run_graph(xt_batch b, const double* const* rhs, double* const* sol, in
                 items.push_back(e);
                 ilu.push_back(r);
             }
-            if (!fused.empty() && fused_build(fs, b, fused, items, ilu, run, im, count) != XT_OK) {
+            if (!fused.empty() && fused_build(fs, fused, items, ilu, run, im, count) != XT_OK) {
                 fused.clear();  // their own branches instead
                 fs.sys.clear();
                 fs.nall = 0;
